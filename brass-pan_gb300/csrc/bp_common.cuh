@@ -1,0 +1,209 @@
+// bp_common.cuh -- device-side building blocks shared by the solver kernels.
+//
+// Layout of the particle state in HBM (structure of arrays, cell-sorted):
+//   X[i] = float4(x, y, z, mass)            committed position
+//   P[i] = float4(px, py, pz, phase bits)   predicted position (the iterate)
+//   V[i] = float4(vx, vy, vz, phase bits)   velocity
+// plus int32 original ids, a compact float mass array, and per-pass scratch.
+// All loads of a particle record are one 16-byte vector load.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/brasspan.h"
+
+namespace bp {
+
+constexpr int kMaxPlanes = 16;
+
+// Constants of one substep, passed by value to every kernel (graph friendly).
+struct SimConsts {
+    int n;
+    int D;            // grid dimension (power of two)
+    unsigned mask;    // D - 1
+    float cell;       // hash cell edge
+    // SPH (K/fluid.cuh:11-27), computed on the host with the reference's formulas
+    float h, h2, half_h, c_poly6, c_spiky, c_akinci, c_akinci_off;
+    // PBF
+    float rho0, inv_rho0, solid_scale, lambda_den, relaxation;
+    float scorr_k, scorr_n, scorr_wq;  // wq = poly6((dq*h)^2)
+    int scorr_on;                      // reference: s_corr only when Akinci is off
+    int clamp_c;                       // reference: C = max(C, 0) when Akinci is on
+    float delta_clamp;                 // <= 0: no clamp
+    int textbook;
+    // post passes
+    float vort_eps, tension, xsph_c;
+    int use_vort, use_akinci, use_xsph;
+    // contacts
+    float radius, fs, fd, mass_k;
+    float3 gravity;
+    float3 wind;
+    float wind_drag, wind_lift;
+    int rot_iters;
+    float dt, inv_dt;
+    int nplanes;
+    float4 plane_o[kMaxPlanes];
+    float4 plane_n[kMaxPlanes];
+};
+
+// ---- small vector helpers (own code; component-wise, left-to-right dot) ----
+
+__device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator-(float3 a) { return make_float3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float3 operator/(float3 a, float s) { return make_float3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ void operator+=(float3 &a, float3 b) { a = a + b; }
+__device__ __forceinline__ void operator-=(float3 &a, float3 b) { a = a - b; }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b)
+{
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float len2(float3 a) { return dot3(a, a); }
+__device__ __forceinline__ float len3(float3 a) { return sqrtf(dot3(a, a)); }
+__device__ __forceinline__ int phase_of(float4 a) { return __float_as_int(a.w); }
+
+// ---- SPH kernels (same formulas as K/fluid.cuh:31-74) ----
+
+__device__ __forceinline__ float poly6(const SimConsts &C, float r2)
+{
+    const float t = C.h2 - r2;
+    return C.c_poly6 * t * t * t;
+}
+__device__ __forceinline__ float3 spiky_grad(const SimConsts &C, float3 v, float r2)
+{
+    const float r = sqrtf(r2);
+    const float t = C.h - r;
+    return (C.c_spiky * t * t * v) / r;
+}
+__device__ __forceinline__ float akinci_spline(const SimConsts &C, float r)
+{
+    const float t = (C.h - r) * r;
+    const float t3 = t * t * t;
+    return (r >= C.half_h) ? C.c_akinci * t3 : 2.0f * C.c_akinci * t3 - C.c_akinci_off;
+}
+
+// ---- hash grid (same cell function as K/grid.cuh:9-28) ----
+// cell = trunc((p + 50000) / cell) with IEEE add and divide.
+
+__device__ __forceinline__ int cell_coord(float p, float cell)
+{
+    return (int)__fdiv_rn(__fadd_rn(p, 50000.0f), cell);
+}
+__device__ __forceinline__ int3 cell_of(float3 p, const SimConsts &C)
+{
+    return make_int3(cell_coord(p.x, C.cell), cell_coord(p.y, C.cell), cell_coord(p.z, C.cell));
+}
+__device__ __forceinline__ int cell_addr(int x, int y, int z, int D, unsigned mask)
+{
+    return (int)(((unsigned)x & mask) * ((unsigned)D * (unsigned)D) + ((unsigned)y & mask) * (unsigned)D +
+                 ((unsigned)z & mask));
+}
+
+// Walk the 27 cells around the cell of `pi`.  Cells are addressed x-major
+// (x*D*D + y*D + z), so for a fixed (x, y) column the three z cells are
+// consecutive addresses and their particles are one contiguous run of the
+// sorted arrays: [off[base+z-1], off[base+z+2]).  The walk therefore visits
+// 9 column runs (split in two where z wraps around the table), using the
+// dense prefix table `off` of D^3+1 entries.
+template <class F>
+__device__ __forceinline__ void for_each_candidate(float3 pi, const int *__restrict__ off, const SimConsts &C,
+                                                   F &&f)
+{
+    const int3 c = cell_of(pi, C);
+    const unsigned m = C.mask;
+    const unsigned D = (unsigned)C.D;
+    const unsigned z0 = (unsigned)(c.z - 1) & m;
+    const unsigned z2 = (unsigned)(c.z + 1) & m;
+#pragma unroll 1
+    for (int dx = -1; dx <= 1; ++dx) {
+        const unsigned bx = ((unsigned)(c.x + dx) & m) * D * D;
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy) {
+            const unsigned base = bx + ((unsigned)(c.y + dy) & m) * D;
+            if (z0 < z2) {
+                const int b = __ldg(off + base + z0), e = __ldg(off + base + z2 + 1);
+#pragma unroll 1
+                for (int j = b; j < e; ++j) f(j);
+            } else {
+                const int b1 = __ldg(off + base + z0), e1 = __ldg(off + base + D);
+#pragma unroll 1
+                for (int j = b1; j < e1; ++j) f(j);
+                const int b2 = __ldg(off + base), e2 = __ldg(off + base + z2 + 1);
+#pragma unroll 1
+                for (int j = b2; j < e2; ++j) f(j);
+            }
+        }
+    }
+}
+
+// Same walk restricted to sorted indices j >= lo (used by the reference-mode
+// density, which only sums j >= i).
+template <class F>
+__device__ __forceinline__ void for_each_candidate_from(float3 pi, int lo, const int *__restrict__ off,
+                                                        const SimConsts &C, F &&f)
+{
+    const int3 c = cell_of(pi, C);
+    const unsigned m = C.mask;
+    const unsigned D = (unsigned)C.D;
+    const unsigned z0 = (unsigned)(c.z - 1) & m;
+    const unsigned z2 = (unsigned)(c.z + 1) & m;
+#pragma unroll 1
+    for (int dx = -1; dx <= 1; ++dx) {
+        const unsigned bx = ((unsigned)(c.x + dx) & m) * D * D;
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy) {
+            const unsigned base = bx + ((unsigned)(c.y + dy) & m) * D;
+            if (z0 < z2) {
+                const int b = max(__ldg(off + base + z0), lo), e = __ldg(off + base + z2 + 1);
+#pragma unroll 1
+                for (int j = b; j < e; ++j) f(j);
+            } else {
+                const int b1 = max(__ldg(off + base + z0), lo), e1 = __ldg(off + base + D);
+#pragma unroll 1
+                for (int j = b1; j < e1; ++j) f(j);
+                const int b2 = max(__ldg(off + base), lo), e2 = __ldg(off + base + z2 + 1);
+#pragma unroll 1
+                for (int j = b2; j < e2; ++j) f(j);
+            }
+        }
+    }
+}
+
+// Plane walls: planeStabilize / particlePlaneCollisionConstraint
+// (K/particleplane.cuh:3-58) for one particle, planes in scene order.
+__device__ __forceinline__ void plane_stabilize(const SimConsts &C, float3 &x, float3 &p)
+{
+    for (int k = 0; k < C.nplanes; ++k) {
+        const float3 o = f3(C.plane_o[k]), nn = f3(C.plane_n[k]);
+        const float d = dot3(o - x, nn) + C.radius;
+        if (d <= 0.f) continue;
+        x += d * nn;
+        p += d * nn;
+    }
+}
+__device__ __forceinline__ void plane_collide(const SimConsts &C, float3 x, float3 &p)
+{
+    for (int k = 0; k < C.nplanes; ++k) {
+        const float3 o = f3(C.plane_o[k]), nn = f3(C.plane_n[k]);
+        const float d = dot3(o - p, nn) + C.radius;
+        if (d <= 0.f) continue;
+        const float3 diff = p - x;
+        const float dn = dot3(diff, nn);
+        const float3 dt = diff - dn * nn;
+        const float dtl = len3(dt);
+        const float3 resolved = d * nn + p;
+        const float3 dx = resolved - x;
+        const float3 tdx = dx - dot3(dx, nn) * nn;
+        if (dtl < C.fs * dn)
+            p = resolved - tdx;
+        else
+            p = resolved - tdx * fminf(C.fd * -dn / dtl, 1.0f);
+    }
+}
+
+}  // namespace bp

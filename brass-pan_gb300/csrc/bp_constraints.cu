@@ -1,0 +1,431 @@
+// bp_constraints.cu -- per-particle passes and the non-fluid constraints.
+//
+// Reference kernels (paths inside brass-pan, K/ = brasstower/kernel/):
+//   particlePlaneCollisionConstraint (K/particleplane.cuh:21-58) -> k_planes
+//   updateVelocity + updatePositions (particlesolver.cuh:71-81,121-137) -> k_commit
+//   particleParticleCollisionConstraint (K/particleparticle.cuh:5-101) -> k_particle_collision
+//   distanceConstraints (K/distance.cuh:3-40) -> k_distance_edges + k_distance_apply
+//   applyWindForce (K/wind.cuh:3-50) -> k_wind_faces + k_wind_apply
+//   shapeMatchingAlphaOne (K/shapematching.cuh:8-99) -> k_shape_matching (any body size)
+//   immovableConstraints (K/immovable.cuh:3-14) -> k_immovable
+//   mapParticleInfos (main.cu:273-282) -> k_pack_infos
+// Scatter-with-atomics constraints become two deterministic passes: one
+// thread per constraint computes its correction once, then one thread per
+// affected particle sums its incident corrections in a fixed (CSR) order.
+#include "bp_internal.h"
+
+namespace bp {
+
+__global__ void k_planes(SimConsts C, const float4 *__restrict__ Xs, float4 *__restrict__ P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    const float4 p4 = P[i];
+    float3 p = f3(p4);
+    plane_collide(C, f3(Xs[i]), p);
+    P[i] = make_float4(p.x, p.y, p.z, p4.w);
+}
+
+void launch_planes(cudaStream_t st, const SimConsts &C, const float4 *Xs, float4 *P, int64_t *launches)
+{
+    if (C.n <= 0 || C.nplanes <= 0) return;
+    k_planes<<<(C.n + 255) / 256, 256, 0, st>>>(C, Xs, P);
+    ++*launches;
+}
+
+__global__ void k_commit(SimConsts C, const float4 *__restrict__ P, const float4 *__restrict__ Xs,
+                         const float4 *__restrict__ Vs, const int *__restrict__ orig_s, float4 *__restrict__ Xc,
+                         float4 *__restrict__ Vc, int *__restrict__ orig_c)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    const float4 p4 = P[i];
+    const float4 xs = Xs[i];
+    const float3 p = f3(p4);
+    const float3 v = (p - f3(xs)) * C.inv_dt;
+    Xc[i] = make_float4(p.x, p.y, p.z, xs.w);
+    Vc[i] = make_float4(v.x, v.y, v.z, Vs[i].w);
+    orig_c[i] = orig_s[i];
+}
+
+void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs, const float4 *Vs,
+                   const int *orig_s, float4 *Xc, float4 *Vc, int *orig_c, int64_t *launches)
+{
+    if (C.n <= 0) return;
+    k_commit<<<(C.n + 255) / 256, 256, 0, st>>>(C, P, Xs, Vs, orig_s, Xc, Vc, orig_c);
+    ++*launches;
+}
+
+// Solid contacts: pairs of different phase with at least one solid, closer
+// than two radii; mass-weighted projection plus friction averaged over the
+// counted contacts; only particle i moves (the reference's j update is
+// commented out).  Reads P, writes Pout = P + delta.
+__global__ void __launch_bounds__(128) k_particle_collision(SimConsts C, const float4 *__restrict__ P,
+                                                            const float4 *__restrict__ Xs,
+                                                            const float *__restrict__ w,
+                                                            const int *__restrict__ off, float4 *__restrict__ Pout)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    const float4 pi4 = P[i];
+    const float3 xip = f3(pi4);
+    const float3 xi = f3(Xs[i]);
+    const int phi = phase_of(pi4);
+    const float wi = w[i];
+    const float r = C.radius;
+    float3 sd = make_float3(0.f, 0.f, 0.f), sf = make_float3(0.f, 0.f, 0.f);
+    int count = 0;
+    for_each_candidate(xip, off, C, [&](int j) {
+        const float4 pj4 = P[j];
+        const int phj = phase_of(pj4);
+        if (!(j != i && phi != phj && (phi > 0 || phj > 0))) return;
+        const float3 xjp = f3(pj4);
+        const float3 diff = xip - xjp;
+        const float d2 = len2(diff);
+        if (!(d2 < r * r * 4.0f && d2 > 1e-5f)) return;
+        const float dist = sqrtf(d2);
+        const float wj = w[j];
+        const float w1 = wi / (wi + wj);
+        const float w2 = wj / (wi + wj);
+        const float3 proj = diff * (2.0f * r / dist - 1.0f);
+        const float3 dxi = w1 * proj;
+        const float3 xistar = dxi + xip;
+        sd += dxi;
+        const float3 dxj = -w2 * proj;
+        const float dxi2 = len2(dxi);
+        if (dxi2 > r * r * 0.001f * 0.001f) {
+            count += 1;
+            const float3 xj = f3(Xs[j]);
+            const float3 xjstar = dxj + xjp;
+            const float3 t1 = (xistar - xi) - (xjstar - xj);
+            const float3 nn = diff / dist;
+            const float3 tdx = t1 - dot3(t1, nn) * nn;
+            const float tl2 = len2(tdx);
+            if (tl2 <= (C.fs * C.fs) * dxi2)
+                sf -= w1 * tdx;
+            else
+                sf -= (w1 * tdx) * fminf(C.fd * sqrtf(dxi2 / tl2), 1.0f);
+        }
+    });
+    const float3 d = (count == 0) ? sd : sd + sf / (float)count;
+    const float3 p = xip + d;
+    Pout[i] = make_float4(p.x, p.y, p.z, pi4.w);
+}
+
+void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
+                               const float *w, const int *off, float4 *Pout, int64_t *launches)
+{
+    if (C.n <= 0) return;
+    k_particle_collision<<<(C.n + 127) / 128, 128, 0, st>>>(C, P, Xs, w, off, Pout);
+    ++*launches;
+}
+
+// ---- distance constraints ----
+
+__global__ void k_distance_edges(int m, const int2 *__restrict__ pairs, const float2 *__restrict__ params,
+                                 const float4 *__restrict__ P, const float *__restrict__ w,
+                                 const int *__restrict__ to_new, float4 *__restrict__ edge_k)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    const int2 pr = pairs[e];
+    const float2 prm = params[e];
+    const int id1 = to_new[pr.x], id2 = to_new[pr.y];
+    const float3 x12 = f3(P[id1]) - f3(P[id2]);
+    const float d12 = len3(x12);
+    float3 k = make_float3(0.f, 0.f, 0.f);
+    if (!(d12 <= 1e-5f)) {
+        const float3 nn = x12 / d12;
+        const float sw = w[id1] + w[id2];
+        k = (nn * ((d12 - prm.x) / sw)) * prm.y;
+    }
+    edge_k[e] = make_float4(k.x, k.y, k.z, 0.f);
+}
+
+__global__ void k_distance_apply(int nn_, const int *__restrict__ node_ids, const int *__restrict__ ptr,
+                                 const int *__restrict__ inc, const float4 *__restrict__ edge_k,
+                                 const float *__restrict__ w, const int *__restrict__ to_new, float4 *__restrict__ P)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nn_) return;
+    const int i = to_new[node_ids[t]];
+    const float wi = w[i];
+    float3 d = make_float3(0.f, 0.f, 0.f);
+    for (int q = ptr[t]; q < ptr[t + 1]; ++q) {
+        const int code = inc[q];
+        const float3 k = f3(edge_k[code >> 1]);
+        d += (code & 1) ? wi * k : -wi * k;
+    }
+    const float4 p4 = P[i];
+    P[i] = make_float4(p4.x + d.x, p4.y + d.y, p4.z + d.z, p4.w);
+}
+
+void launch_distance(cudaStream_t st, const SimConsts &C, const DistanceArgs &a, float4 *P, const float *w,
+                     const int *to_new, unsigned *err, int64_t *launches)
+{
+    (void)C;
+    (void)err;
+    if (a.num_edges <= 0) return;
+    k_distance_edges<<<(a.num_edges + 255) / 256, 256, 0, st>>>(a.num_edges, a.pairs, a.params, P, w, to_new,
+                                                                a.edge_k);
+    k_distance_apply<<<(a.num_nodes + 255) / 256, 256, 0, st>>>(a.num_nodes, a.node_ids, a.node_ptr, a.node_inc,
+                                                                a.edge_k, w, to_new, P);
+    *launches += 2;
+}
+
+// ---- wind ----
+
+__global__ void k_wind_faces(SimConsts C, int nf, const int *__restrict__ faces, const float4 *__restrict__ P,
+                             const float4 *__restrict__ V, const int *__restrict__ to_new,
+                             float4 *__restrict__ move)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const int id1 = to_new[faces[3 * f]], id2 = to_new[faces[3 * f + 1]], id3 = to_new[faces[3 * f + 2]];
+    const float3 p1 = f3(P[id1]), p2 = f3(P[id2]), p3 = f3(P[id3]);
+    const float3 a = p2 - p1, b = p3 - p1;
+    float3 v = ((f3(V[id1]) + f3(V[id2])) + f3(V[id3])) / 3.f;
+    if (C.textbook) v = v - C.wind;
+    float3 mv = make_float3(0.f, 0.f, 0.f);
+    const float lv = len3(v);
+    if (!(lv <= 1e-5f)) {
+        const float3 vh = v / lv;
+        float3 fn = cross3(a, b);
+        const float lf = len3(fn);
+        if (!(lf <= 1e-5f)) {
+            fn = fn / lf;
+            fn = (dot3(fn, v) > 0.f) ? fn : -fn;
+            const float area = 0.5f * lf;
+            const float3 drag = (C.wind_drag * (lv * lv) * area * dot3(fn, vh)) * (-vh);
+            const float3 uh = cross3(cross3(fn, vh), vh);
+            const float3 lift = (C.wind_lift * (lv * lv) * area * dot3(fn, vh)) * uh;
+            mv = ((drag + lift) * C.dt) * C.dt;
+        }
+    }
+    move[f] = make_float4(mv.x, mv.y, mv.z, 0.f);
+}
+
+__global__ void k_wind_apply(int nn_, const int *__restrict__ node_ids, const int *__restrict__ ptr,
+                             const int *__restrict__ inc, const float4 *__restrict__ move,
+                             const float *__restrict__ mass, const int *__restrict__ to_new, float4 *__restrict__ P)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nn_) return;
+    const int i = to_new[node_ids[t]];
+    const float m = mass[i];
+    float3 d = make_float3(0.f, 0.f, 0.f);
+    for (int q = ptr[t]; q < ptr[t + 1]; ++q) d += f3(move[inc[q]]) / m;
+    const float4 p4 = P[i];
+    P[i] = make_float4(p4.x + d.x, p4.y + d.y, p4.z + d.z, p4.w);
+}
+
+void launch_wind(cudaStream_t st, const SimConsts &C, const WindArgs &a, float4 *P, const float4 *Vs,
+                 const float *mass, const int *to_new, int64_t *launches)
+{
+    if (a.num_faces <= 0) return;
+    k_wind_faces<<<(a.num_faces + 255) / 256, 256, 0, st>>>(C, a.num_faces, a.faces, P, Vs, to_new, a.face_move);
+    k_wind_apply<<<(a.num_nodes + 255) / 256, 256, 0, st>>>(a.num_nodes, a.node_ids, a.node_ptr, a.node_inc,
+                                                            a.face_move, mass, to_new, P);
+    *launches += 2;
+}
+
+// ---- shape matching ----
+
+struct Quat { float x, y, z, w; };
+
+__device__ __forceinline__ Quat qmul(Quat a, Quat b)
+{
+    Quat r;
+    r.x = a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y;
+    r.y = a.w * b.y - a.x * b.z + a.y * b.w + a.z * b.x;
+    r.z = a.w * b.z + a.x * b.y - a.y * b.x + a.z * b.w;
+    r.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
+    return r;
+}
+
+struct Mat3 { float3 c0, c1, c2; };
+
+__device__ __forceinline__ Mat3 qmatrix(Quat q)
+{
+    const float x2 = q.x * q.x, y2 = q.y * q.y, z2 = q.z * q.z;
+    Mat3 m;
+    m.c0 = make_float3(1 - 2 * y2 - 2 * z2, 2 * q.x * q.y + 2 * q.w * q.z, 2 * q.x * q.z - 2 * q.w * q.y);
+    m.c1 = make_float3(2 * q.x * q.y - 2 * q.w * q.z, 1 - 2 * x2 - 2 * z2, 2 * q.y * q.z + 2 * q.w * q.x);
+    m.c2 = make_float3(2 * q.x * q.z + 2 * q.w * q.y, 2 * q.y * q.z - 2 * q.w * q.x, 1 - 2 * x2 - 2 * y2);
+    return m;
+}
+
+constexpr int kSmThreads = 256;
+
+// Block-wide sum of `nv` floats per thread (warp shuffles, then smem).
+template <int NV>
+__device__ __forceinline__ void block_sum(float (&v)[NV], float (*red)[32])
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        float s = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) red[k][warp] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        float s = 0.f;
+        for (int q = 0; q < kSmThreads / 32; ++q) s += red[k][q];
+        v[k] = s;
+    }
+    __syncthreads();
+}
+
+// One CTA per body, any number of particles (looped in chunks of 256).
+// Centre of mass (unweighted), A_pq columns, warm-started robust rotation
+// extraction (Mueller et al. 2016, the reference's iteration with its
+// 1/|sum| + 1e-9 denominator), goal positions with alpha = 1.
+__global__ void __launch_bounds__(kSmThreads) k_shape_matching(SimConsts C, RigidArgs a, float4 *__restrict__ P,
+                                                               const int *__restrict__ to_new)
+{
+    __shared__ float red[9][32];
+    __shared__ float3 s_cm;
+    __shared__ Mat3 s_R;
+    const int b = blockIdx.x;
+    const int2 rg = a.ranges[b];
+    const int np = rg.y - rg.x;
+    float c[3] = {0.f, 0.f, 0.f};
+    for (int t = threadIdx.x; t < np; t += kSmThreads) {
+        const float4 p = P[to_new[rg.x + t]];
+        c[0] += p.x;
+        c[1] += p.y;
+        c[2] += p.z;
+    }
+    block_sum<3>(c, red);
+    const float3 cm = make_float3(c[0], c[1], c[2]) / (float)np;
+    float A[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int t = threadIdx.x; t < np; t += kSmThreads) {
+        const float3 q = f3(a.rest[rg.x + t]);
+        const float3 pc = f3(P[to_new[rg.x + t]]) - cm;
+        A[0] += pc.x * q.x; A[1] += pc.y * q.x; A[2] += pc.z * q.x;
+        A[3] += pc.x * q.y; A[4] += pc.y * q.y; A[5] += pc.z * q.y;
+        A[6] += pc.x * q.z; A[7] += pc.y * q.z; A[8] += pc.z * q.z;
+    }
+    block_sum<9>(A, red);
+    if (threadIdx.x == 0) {
+        const float3 a0 = make_float3(A[0], A[1], A[2]), a1 = make_float3(A[3], A[4], A[5]),
+                     a2 = make_float3(A[6], A[7], A[8]);
+        const float4 q4 = a.rot[b];
+        Quat q = {q4.x, q4.y, q4.z, q4.w};
+        for (int it = 0; it < C.rot_iters; ++it) {
+            const Mat3 R = qmatrix(q);
+            const float3 num = (cross3(R.c0, a0) + cross3(R.c1, a1)) + cross3(R.c2, a2);
+            const float den = 1.0f / fabsf(dot3(R.c0, a0) + dot3(R.c1, a1) + dot3(R.c2, a2)) + 1e-9f;
+            const float3 om = num * den;
+            const float w2 = len2(om);
+            if (w2 <= 1e-9f) break;
+            const float wl = sqrtf(w2);
+            const float3 ax = om / wl;
+            float sh, ch;
+            sincosf(wl * 0.5f, &sh, &ch);
+            const Quat dq = {ax.x * sh, ax.y * sh, ax.z * sh, ch};
+            q = qmul(dq, q);
+            const float inv = 1.0f / sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+            q.x *= inv; q.y *= inv; q.z *= inv; q.w *= inv;
+        }
+        s_R = qmatrix(q);
+        s_cm = cm;
+        a.rot[b] = make_float4(q.x, q.y, q.z, q.w);
+        a.cm[b] = make_float4(cm.x, cm.y, cm.z, 0.f);
+    }
+    __syncthreads();
+    const Mat3 R = s_R;
+    const float3 cmv = s_cm;
+    for (int t = threadIdx.x; t < np; t += kSmThreads) {
+        const float3 q = f3(a.rest[rg.x + t]);
+        const int id = to_new[rg.x + t];
+        const float3 g = ((R.c0 * q.x + R.c1 * q.y) + R.c2 * q.z) + cmv;
+        const float4 p4 = P[id];
+        P[id] = make_float4(g.x, g.y, g.z, p4.w);
+    }
+}
+
+void launch_shape_matching(cudaStream_t st, const SimConsts &C, const RigidArgs &a, float4 *P,
+                           const int *to_new, int64_t *launches)
+{
+    if (a.num_bodies <= 0) return;
+    k_shape_matching<<<a.num_bodies, kSmThreads, 0, st>>>(C, a, P, to_new);
+    ++*launches;
+}
+
+__global__ void k_immovable(int k, const int *__restrict__ ids, const int *__restrict__ to_new,
+                            const float4 *__restrict__ Xs, float4 *__restrict__ P)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= k) return;
+    const int i = to_new[ids[t]];
+    const float4 x = Xs[i];
+    P[i] = make_float4(x.x, x.y, x.z, P[i].w);
+}
+
+void launch_immovable(cudaStream_t st, int k, const int *ids, const int *to_new, const float4 *Xs, float4 *P,
+                      int64_t *launches)
+{
+    if (k <= 0) return;
+    k_immovable<<<(k + 255) / 256, 256, 0, st>>>(k, ids, to_new, Xs, P);
+    ++*launches;
+}
+
+// setParticle (particlesolver.cuh:388-393) on the picked particle.
+__global__ void k_pick(int id_orig, const int *__restrict__ to_new, float4 *pos, float3 p, int set_pos, float4 *vel,
+                       float3 v)
+{
+    const int i = to_new[id_orig];
+    if (set_pos) {
+        const float4 o = pos[i];
+        pos[i] = make_float4(p.x, p.y, p.z, o.w);
+    }
+    if (vel) {
+        const float4 o = vel[i];
+        vel[i] = make_float4(v.x, v.y, v.z, o.w);
+    }
+}
+
+void launch_pick(cudaStream_t st, int id_orig, const int *to_new, float4 *pos, float3 p, int set_pos, float4 *vel,
+                 float3 v, int64_t *launches)
+{
+    k_pick<<<1, 1, 0, st>>>(id_orig, to_new, pos, p, set_pos, vel, v);
+    ++*launches;
+}
+
+// {x, y, z, phase} records for a renderer.
+__global__ void k_pack_infos(int n, const float4 *__restrict__ X, const float4 *__restrict__ V, float4 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 x = X[i];
+    out[i] = make_float4(x.x, x.y, x.z, V[i].w);
+}
+
+void launch_pack_infos(cudaStream_t st, int n, const float4 *X, const float4 *V, void *out)
+{
+    if (n <= 0) return;
+    k_pack_infos<<<(n + 255) / 256, 256, 0, st>>>(n, X, V, (float4 *)out);
+}
+
+// Device error word: NaN / Inf positions.
+__global__ void k_check_finite(int n, const float4 *__restrict__ X, unsigned *err)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 x = X[i];
+    const bool bad = !(isfinite(x.x) && isfinite(x.y) && isfinite(x.z));
+    if (__any_sync(__activemask(), bad) && bad) atomicOr(err, BP_DEVERR_NONFINITE);
+}
+
+void launch_check_finite(cudaStream_t st, int n, const float4 *X, unsigned *err, int64_t *launches)
+{
+    if (n <= 0) return;
+    k_check_finite<<<(n + 255) / 256, 256, 0, st>>>(n, X, err);
+    ++*launches;
+}
+
+}  // namespace bp

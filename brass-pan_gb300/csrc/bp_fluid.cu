@@ -1,0 +1,326 @@
+// bp_fluid.cu -- position-based fluid passes (gather form, fixed neighbour order).
+//
+// Reference kernels (brasstower/kernel/fluid.cuh):
+//   fluidLambda (:78-159)              -> k_lambda
+//   fluidPosition (:161-228) + accDevArr_float3 (kernel/util.cuh:261-269)
+//                                      -> k_deltap (gather, no atomics, epilogue fused)
+//   fluidOmega (:231-279) + fluidNormal (:387-434)            -> k_post_a (one walk)
+//   fluidVorticity (:281-336) + fluidAkinciTension (:436-488) -> k_post_b (one walk)
+//   fluidXSph (:338-385)                                      -> k_post_c
+//
+// The reference scatters each pair's position correction to both particles
+// with float atomics; here every particle gathers its own sum over the same
+// pairs in a fixed order, so results are deterministic run to run.  The pair
+// term for (k, j) is bit-identical to the reference's term for (j, k) up to
+// sign, because the spiky gradient is odd in the difference vector.
+#include "bp_internal.h"
+
+namespace bp {
+
+constexpr int kScanThreads = 128;
+
+// Reference mode (Q1): density sums only sorted indices j >= i; solid
+// neighbours count x solid_scale; C = rho/rho0 - 1, clamped at 0 when Akinci
+// is on; lambda = -C / lambda_den.  Textbook mode: all j, exact denominator.
+__global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const float4 *__restrict__ P,
+                                                         const float *__restrict__ mass,
+                                                         const int *__restrict__ off, float *__restrict__ lam,
+                                                         float *__restrict__ rho)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    const float4 pi4 = P[i];
+    if (phase_of(pi4) > 0) {  // solids carry lambda 0 (read by the position pass)
+        lam[i] = 0.f;
+        return;
+    }
+    const float3 pi = f3(pi4);
+    float density = 0.f;
+    if (!C.textbook) {
+        for_each_candidate_from(pi, i, off, C, [&](int j) {
+            const float4 pj = P[j];
+            const float d2 = len2(pi - f3(pj));
+            if (d2 <= C.h2) {
+                const float ld = __ldg(mass + j) * poly6(C, d2);
+                density += (phase_of(pj) < 0) ? ld : C.solid_scale * ld;
+            }
+        });
+        float c = density / C.rho0 - 1.0f;
+        if (C.clamp_c) c = fmaxf(c, 0.0f);
+        lam[i] = -c / C.lambda_den;
+    } else {
+        float sum_g2 = 0.f;
+        float3 gi = make_float3(0.f, 0.f, 0.f);
+        for_each_candidate(pi, off, C, [&](int j) {
+            const float4 pj = P[j];
+            const float3 diff = pi - f3(pj);
+            const float d2 = len2(diff);
+            if (d2 <= C.h2) {
+                const float mj = __ldg(mass + j);
+                const float ld = mj * poly6(C, d2);
+                density += (phase_of(pj) < 0) ? ld : C.solid_scale * ld;
+                if (d2 > 0.f) {
+                    const float3 g = (-mj * spiky_grad(C, diff, d2)) / C.rho0;
+                    sum_g2 += dot3(g, g);
+                    gi -= g;
+                }
+            }
+        });
+        float c = density / C.rho0 - 1.0f;
+        if (C.clamp_c) c = fmaxf(c, 0.0f);
+        sum_g2 += dot3(gi, gi);
+        lam[i] = -c / (sum_g2 + C.relaxation);
+    }
+    rho[i] = density;
+}
+
+void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const float *mass, const int *off,
+                   float *lam, float *rho, int64_t *launches)
+{
+    if (C.n <= 0) return;
+    k_lambda<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, mass, off, lam, rho);
+    ++*launches;
+}
+
+// Position correction.  Reference mode: the pair (a, b), a < b, contributes
+// when a is a fluid particle (only fluid threads run fluidPosition and they
+// only visit b > a), to both ends.  In gather form particle k includes j when
+// the lower-indexed of (k, j) is fluid.  Textbook mode: fluid k gathers over
+// every neighbour; solids do not move.
+__global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs a)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= C.n) return;
+    const float4 pk4 = a.P[k];
+    const int phk = phase_of(pk4);
+    const float3 pk = f3(pk4);
+    float3 sum = make_float3(0.f, 0.f, 0.f);
+    if (!(C.textbook && phk > 0)) {
+        const float lk = a.lam[k];
+        for_each_candidate(pk, a.off, C, [&](int j) {
+            if (j == k) return;
+            const float4 pj4 = a.P[j];
+            const float3 diff = pk - f3(pj4);
+            const float d2 = len2(diff);
+            if (d2 <= C.h2 && d2 > 0.f) {
+                const bool inc = C.textbook ? true : ((j > k) ? (phk < 0) : (phase_of(pj4) < 0));
+                if (!inc) return;
+                float sl = lk + __ldg(a.lam + j);
+                if (C.scorr_on) sl += -C.scorr_k * powf(poly6(C, d2) / C.scorr_wq, C.scorr_n);
+                float3 delta = sl * spiky_grad(C, diff, d2);
+                if (C.delta_clamp > 0.f) {
+                    const float len = len3(delta);
+                    delta = (len < C.delta_clamp) ? delta : (delta * fminf(len, C.delta_clamp)) / len;
+                }
+                sum += __ldg(a.mass + j) * delta;
+            }
+        });
+    }
+    float3 p = pk + sum * C.inv_rho0;
+    if (a.epilogue == 1) {
+        plane_collide(C, f3(a.Xs[k]), p);
+    } else if (a.epilogue == 2) {  // updateVelocity + updatePositions (PS:71-81, 121-137)
+        const float4 xs = a.Xs[k];
+        const float3 v = (p - f3(xs)) * C.inv_dt;
+        a.Xc[k] = make_float4(p.x, p.y, p.z, xs.w);
+        a.Vc[k] = make_float4(v.x, v.y, v.z, pk4.w);
+        a.orig_c[k] = a.orig_s[k];
+    }
+    a.Pout[k] = make_float4(p.x, p.y, p.z, pk4.w);
+}
+
+void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, int64_t *launches)
+{
+    if (C.n <= 0) return;
+    k_deltap<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, a);
+    ++*launches;
+}
+
+// Pass A: vorticity omega_i (fluidOmega) and Akinci normal n_i (fluidNormal)
+// in one walk over same-phase neighbours with 0 < r^2 <= h^2.
+// Om[i] = (omega, |omega|); Nm[i] = (h * n, rho_i).
+__global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const float4 *__restrict__ P,
+                                                         const float4 *__restrict__ V,
+                                                         const float *__restrict__ rho, const int *__restrict__ off,
+                                                         float4 *__restrict__ Om, float4 *__restrict__ Nm)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    const float4 pi4 = P[i];
+    const int phi = phase_of(pi4);
+    if (phi >= 0) return;
+    const float3 pi = f3(pi4);
+    const float3 vi = f3(V[i]);
+    float3 om = make_float3(0.f, 0.f, 0.f), nn = make_float3(0.f, 0.f, 0.f);
+    const bool want_om = C.use_vort, want_n = C.use_akinci;
+    for_each_candidate(pi, off, C, [&](int j) {
+        const float4 pj4 = P[j];
+        if (j == i || phase_of(pj4) != phi) return;
+        const float3 diff = pi - f3(pj4);
+        const float d2 = len2(diff);
+        if (d2 <= C.h2 && d2 > 0.f) {
+            const float3 g = spiky_grad(C, diff, d2);
+            if (want_om) om += cross3(f3(V[j]) - vi, g);
+            if (want_n) nn += (1.0f / __ldg(rho + j)) * g;
+        }
+    });
+    Om[i] = make_float4(om.x, om.y, om.z, len3(om));
+    const float3 n = C.h * nn;
+    Nm[i] = make_float4(n.x, n.y, n.z, rho[i]);
+}
+
+// Pass B: vorticity confinement (fluidVorticity) then Akinci tension
+// (fluidAkinciTension), both on the same neighbours.  v' = v + eps (N x w) dt,
+// v'' = v' + F dt, exactly the reference's sequence (in-place update followed
+// by newVelocities = velocities + F dt).  Solids pass through.
+__global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const float4 *__restrict__ P,
+                                                         const float4 *__restrict__ V,
+                                                         const float4 *__restrict__ Om,
+                                                         const float4 *__restrict__ Nm,
+                                                         const int *__restrict__ off, float4 *__restrict__ Vout)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    const float4 pi4 = P[i];
+    const float4 vi4 = V[i];
+    const int phi = phase_of(pi4);
+    if (phi >= 0) {
+        Vout[i] = vi4;
+        return;
+    }
+    const float3 pi = f3(pi4);
+    const float4 ni4 = Nm[i];
+    const float3 ni = f3(ni4);
+    const float rhoi = ni4.w;
+    float3 eta = make_float3(0.f, 0.f, 0.f), ft = make_float3(0.f, 0.f, 0.f);
+    const bool want_v = C.use_vort, want_t = C.use_akinci;
+    for_each_candidate(pi, off, C, [&](int j) {
+        const float4 pj4 = P[j];
+        if (j == i || phase_of(pj4) != phi) return;
+        const float3 pj = f3(pj4);
+        const float3 diff = pi - pj;
+        const float d2 = len2(diff);
+        if (d2 <= C.h2 && d2 > 0.f) {
+            if (want_v) eta += Om[j].w * spiky_grad(C, diff, d2);
+            if (want_t) {
+                const float4 nj4 = Nm[j];
+                const float dist = sqrtf(d2);
+                const float3 fco = (-C.tension * akinci_spline(C, dist) * (pi - pj)) / dist;
+                const float3 fcu = -C.tension * (ni - f3(nj4));
+                const float kij = 2.0f * C.rho0 / (rhoi + nj4.w);
+                ft += kij * (fco + fcu);
+            }
+        }
+    });
+    float3 v = f3(vi4);
+    if (want_v && len2(eta) > 1e-3f) {
+        const float inv = 1.0f / sqrtf(dot3(eta, eta));
+        const float3 nrm = eta * inv;
+        v += (C.vort_eps * cross3(nrm, f3(Om[i]))) * C.dt;
+    }
+    if (want_t) v = v + ft * C.dt;
+    Vout[i] = make_float4(v.x, v.y, v.z, vi4.w);
+}
+
+// Pass C: XSPH viscosity (fluidXSph): same phase, j != i, r^2 <= h^2 (r = 0 included).
+__global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const float4 *__restrict__ P,
+                                                         const float4 *__restrict__ V,
+                                                         const int *__restrict__ off, float4 *__restrict__ Vout)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    const float4 pi4 = P[i];
+    const float4 vi4 = V[i];
+    const int phi = phase_of(pi4);
+    if (phi >= 0) {
+        Vout[i] = vi4;
+        return;
+    }
+    const float3 pi = f3(pi4), vi = f3(vi4);
+    float3 vn = make_float3(0.f, 0.f, 0.f);
+    for_each_candidate(pi, off, C, [&](int j) {
+        const float4 pj4 = P[j];
+        if (j == i || phase_of(pj4) != phi) return;
+        const float d2 = len2(pi - f3(pj4));
+        if (d2 <= C.h2) vn += (f3(V[j]) - vi) * poly6(C, d2);
+    });
+    const float3 v = vi + C.xsph_c * vn;
+    Vout[i] = make_float4(v.x, v.y, v.z, vi4.w);
+}
+
+void launch_post_a(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float *rho,
+                   const int *off, float4 *Om, float4 *Nm, int64_t *launches)
+{
+    if (C.n <= 0) return;
+    k_post_a<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, V, rho, off, Om, Nm);
+    ++*launches;
+}
+void launch_post_b(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float4 *Om,
+                   const float4 *Nm, const int *off, float4 *Vout, int64_t *launches)
+{
+    if (C.n <= 0) return;
+    k_post_b<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, V, Om, Nm, off, Vout);
+    ++*launches;
+}
+void launch_post_c(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
+                   float4 *Vout, int64_t *launches)
+{
+    if (C.n <= 0) return;
+    k_post_c<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, V, off, Vout);
+    ++*launches;
+}
+
+// Neighbour counts on the solver's grid: j in the 27 cells with r^2 <= h^2 (self included).
+__global__ void k_neighbor_counts(SimConsts C, const float4 *__restrict__ P, const int *__restrict__ off,
+                                  int *__restrict__ counts)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    const float3 pi = f3(P[i]);
+    int cnt = 0;
+    for_each_candidate(pi, off, C, [&](int j) {
+        if (len2(pi - f3(P[j])) <= C.h2) ++cnt;
+    });
+    counts[i] = cnt;
+}
+
+void launch_neighbor_counts(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, int *counts,
+                            int64_t *launches)
+{
+    if (C.n <= 0) return;
+    k_neighbor_counts<<<(C.n + 127) / 128, 128, 0, st>>>(C, P, off, counts);
+    ++*launches;
+}
+
+// Same count on caller buffers in the reference's start/end format.
+__global__ void k_neighbor_counts_f3(int n, const float *__restrict__ pos3, float cell, int D, float h2,
+                                     const int *__restrict__ start, const int *__restrict__ end,
+                                     int *__restrict__ counts)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float3 pi = make_float3(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2]);
+    const unsigned m = (unsigned)D - 1u;
+    const int cx = cell_coord(pi.x, cell), cy = cell_coord(pi.y, cell), cz = cell_coord(pi.z, cell);
+    int cnt = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int a = cell_addr(cx + dx, cy + dy, cz + dz, D, m);
+                const int b = start[a], e = end[a];
+                for (int j = b; j < e; ++j) {
+                    const float3 pj = make_float3(pos3[3 * j], pos3[3 * j + 1], pos3[3 * j + 2]);
+                    if (len2(pi - pj) <= h2) ++cnt;
+                }
+            }
+    counts[i] = cnt;
+}
+
+void launch_neighbor_counts_f3(cudaStream_t st, int n, const float *pos3, float cell, int D, float h,
+                               const int *start, const int *end, int *counts)
+{
+    if (n <= 0) return;
+    k_neighbor_counts_f3<<<(n + 127) / 128, 128, 0, st>>>(n, pos3, cell, D, h * h, start, end, counts);
+}
+
+}  // namespace bp

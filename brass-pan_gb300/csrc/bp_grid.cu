@@ -1,0 +1,391 @@
+// bp_grid.cu -- hash grid: cell keys, stable radix sort, cell ranges, reorder.
+//
+// Replaces updateGrid() of the reference (brasstower/particlesolver.cuh:712-765):
+//   updateGridId        (kernel/grid.cuh:30-47)   -> k_hash_*  (+ fused pass-0 histogram)
+//   cub::DeviceRadixSort::SortPairs (PS:721-738) -> own LSD radix sort, 9-bit digits
+//   findStartEndId      (kernel/grid.cuh:70-99)   -> k_find_start_end (stand-alone API)
+//                                                    k_cell_offsets (dense prefix, solver)
+//   reorderParticlesData (kernel/grid.cuh:134-163)
+//   + inverseMapping    (kernel/util.cuh:348-358) -> k_reorder (float4 records, fused predict,
+//                                                    mass scaling and plane stabilisation)
+#include "bp_internal.h"
+
+namespace bp {
+
+// ------------------------------------------------------------------------
+// radix sort
+// ------------------------------------------------------------------------
+
+size_t sort_scratch_bytes(int n, int D)
+{
+    const size_t tiles = (size_t)sort_tiles(n);
+    const int passes = sort_passes(D);
+    const size_t alts = passes > 2 ? 2 : 1;
+    size_t b = alts * 2 * ((size_t)n * 4 + 256);
+    b += (size_t)kRadixBins * tiles * 4 + 256;
+    b += (size_t)kRadixBins * 4 + 256;
+    return b;
+}
+
+void sort_scratch_carve(void *base, int n, int D, SortScratch *s)
+{
+    char *p = (char *)base;
+    auto take = [&](size_t bytes) {
+        char *r = p;
+        p += (bytes + 255) & ~(size_t)255;
+        return r;
+    };
+    const int passes = sort_passes(D);
+    const size_t tiles = (size_t)sort_tiles(n);
+    s->keys_alt[0] = (int *)take((size_t)n * 4);
+    s->vals_alt[0] = (int *)take((size_t)n * 4);
+    if (passes > 2) {
+        s->keys_alt[1] = (int *)take((size_t)n * 4);
+        s->vals_alt[1] = (int *)take((size_t)n * 4);
+    } else {
+        s->keys_alt[1] = s->keys_alt[0];
+        s->vals_alt[1] = s->vals_alt[0];
+    }
+    s->hist = (int *)take((size_t)kRadixBins * tiles * 4);
+    s->digit_total = (int *)take((size_t)kRadixBins * 4);
+}
+
+// Per-tile digit histogram, digit-major: hist[d * tiles + tile].
+__global__ void __launch_bounds__(kSortThreads) k_radix_upsweep(const int *__restrict__ keys, int n, int shift,
+                                                               int *__restrict__ hist, int tiles)
+{
+    __shared__ int h[kRadixBins];
+    for (int d = threadIdx.x; d < kRadixBins; d += kSortThreads) h[d] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile;
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        const int idx = base + k * kSortThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & (kRadixBins - 1)], 1);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadixBins; d += kSortThreads) hist[(size_t)d * tiles + blockIdx.x] = h[d];
+}
+
+// One CTA per digit: exclusive scan over the tiles, digit total on the side.
+__global__ void __launch_bounds__(256) k_radix_scan(int *__restrict__ hist, int tiles, int *__restrict__ digit_total)
+{
+    __shared__ int warp_sums[8];
+    int *row = hist + (size_t)blockIdx.x * tiles;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int carry = 0;
+    for (int base = 0; base < tiles; base += 256) {
+        const int idx = base + threadIdx.x;
+        const int v = idx < tiles ? row[idx] : 0;
+        int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) warp_sums[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            int ws = lane < 8 ? warp_sums[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 8; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, ws, o);
+                if (lane >= o) ws += t;
+            }
+            if (lane < 8) warp_sums[lane] = ws;  // inclusive over warps
+        }
+        __syncthreads();
+        const int warp_prefix = warp ? warp_sums[warp - 1] : 0;
+        if (idx < tiles) row[idx] = carry + warp_prefix + incl - v;
+        const int chunk_total = warp_sums[7];
+        __syncthreads();
+        carry += chunk_total;
+    }
+    if (threadIdx.x == 0) digit_total[blockIdx.x] = carry;
+}
+
+// Stable scatter of one tile.  Each warp owns a contiguous 256-key segment
+// (8 rounds of 32); within a round lanes holding the same digit are ranked
+// with __match_any_sync, so the order inside the tile is preserved: warp
+// segment first, then round, then lane.
+__global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(
+    const int *__restrict__ keys_in, const int *__restrict__ vals_in, int n, int shift,
+    const int *__restrict__ hist, const int *__restrict__ digit_total, int tiles, int *__restrict__ keys_out,
+    int *__restrict__ vals_out)
+{
+    constexpr int W = kSortThreads / 32;
+    constexpr int SEG = kSortTile / W;        // keys per warp
+    constexpr int ROUNDS = SEG / 32;
+    __shared__ int cnt[W][kRadixBins];
+    __shared__ int dbase[kRadixBins];
+    __shared__ int wsum[W];
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int e = threadIdx.x; e < W * kRadixBins; e += kSortThreads) (&cnt[0][0])[e] = 0;
+
+    // exclusive prefix of the digit totals (one digit per thread)
+    {
+        const int d = threadIdx.x;  // kSortThreads == kRadixBins
+        const int v = digit_total[d];
+        int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        int wp = 0;
+        for (int k = 0; k < warp; ++k) wp += wsum[k];
+        dbase[d] = wp + incl - v + hist[(size_t)d * tiles + blockIdx.x];
+    }
+    __syncthreads();
+
+    int key[ROUNDS], val[ROUNDS], dig[ROUNDS], loc[ROUNDS];
+    const int seg0 = blockIdx.x * kSortTile + warp * SEG;
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int r = 0; r < ROUNDS; ++r) {
+        const int idx = seg0 + r * 32 + lane;
+        const bool valid = idx < n;
+        key[r] = valid ? keys_in[idx] : 0;
+        val[r] = valid ? (vals_in ? vals_in[idx] : idx) : 0;
+        const int d = valid ? ((key[r] >> shift) & (kRadixBins - 1)) : kRadixBins;
+        dig[r] = d;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int before = __popc(peers & lt);
+        int base = 0;
+        if (valid) base = cnt[warp][d];
+        __syncwarp();
+        if (valid && before == 0) cnt[warp][d] = base + __popc(peers);
+        __syncwarp();
+        loc[r] = base + before;
+    }
+    __syncthreads();
+    {
+        const int d = threadIdx.x;
+        int run = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const int c = cnt[w][d];
+            cnt[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < ROUNDS; ++r) {
+        const int idx = seg0 + r * 32 + lane;
+        if (idx < n) {
+            const int pos = dbase[dig[r]] + cnt[warp][dig[r]] + loc[r];
+            keys_out[pos] = key[r];
+            vals_out[pos] = val[r];
+        }
+    }
+}
+
+void radix_sort_pairs(cudaStream_t st, int n, int D, const int *keys_in, const int *vals_in, int *keys_out,
+                      int *vals_out, const SortScratch &s, bool hist_ready, int64_t *launches)
+{
+    if (n <= 0) return;
+    const int tiles = sort_tiles(n);
+    const int passes = sort_passes(D);
+    const int *ksrc = keys_in, *vsrc = vals_in;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = p * kRadixBits;
+        int *kdst = (p == passes - 1) ? keys_out : s.keys_alt[p & 1];
+        int *vdst = (p == passes - 1) ? vals_out : s.vals_alt[p & 1];
+        if (!(p == 0 && hist_ready)) {
+            k_radix_upsweep<<<tiles, kSortThreads, 0, st>>>(ksrc, n, shift, s.hist, tiles);
+            ++*launches;
+        }
+        k_radix_scan<<<kRadixBins, 256, 0, st>>>(s.hist, tiles, s.digit_total);
+        k_radix_downsweep<<<tiles, kSortThreads, 0, st>>>(ksrc, vsrc, n, shift, s.hist, s.digit_total, tiles,
+                                                          kdst, vdst);
+        *launches += 2;
+        ksrc = kdst;
+        vsrc = vdst;
+    }
+}
+
+// ------------------------------------------------------------------------
+// cell keys
+// ------------------------------------------------------------------------
+
+// Tile layout identical to the sort (4096 keys per CTA) so the pass-0
+// histogram is produced here and the first upsweep is skipped.
+template <class Pos>
+__device__ __forceinline__ void hash_tile(int n, float cell, int D, Pos pos, int *__restrict__ keys,
+                                          int *__restrict__ hist, int tiles)
+{
+    __shared__ int h[kRadixBins];
+    for (int d = threadIdx.x; d < kRadixBins; d += kSortThreads) h[d] = 0;
+    __syncthreads();
+    const unsigned m = (unsigned)D - 1u;
+    const int base = blockIdx.x * kSortTile;
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        const int idx = base + k * kSortThreads + threadIdx.x;
+        if (idx < n) {
+            const float3 p = pos(idx);
+            const int key = cell_addr(cell_coord(p.x, cell), cell_coord(p.y, cell), cell_coord(p.z, cell), D, m);
+            keys[idx] = key;
+            atomicAdd(&h[key & (kRadixBins - 1)], 1);
+        }
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < kRadixBins; d += kSortThreads) hist[(size_t)d * tiles + blockIdx.x] = h[d];
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_hash_f3(int n, const float *__restrict__ pos3, float cell, int D,
+                                                          int *__restrict__ keys, int *__restrict__ hist, int tiles)
+{
+    hash_tile(n, cell, D,
+              [&](int i) { return make_float3(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2]); }, keys, hist,
+              tiles);
+}
+
+// predictPositions + applyGravity (PS:59-69, 49-57) feeding the hash; the
+// rounding is pinned (no fused multiply-add) so that the prediction, and with
+// it every cell key, is bit-identical to a host evaluation of x + v*dt + (g*dt)*dt.
+__device__ __forceinline__ float3 predict(float3 x, float3 v, const SimConsts &C)
+{
+    float3 p;
+    p.x = __fadd_rn(x.x, __fmul_rn(v.x, C.dt));
+    p.y = __fadd_rn(x.y, __fmul_rn(v.y, C.dt));
+    p.z = __fadd_rn(x.z, __fmul_rn(v.z, C.dt));
+    p.x = __fadd_rn(p.x, __fmul_rn(__fmul_rn(C.gravity.x, C.dt), C.dt));
+    p.y = __fadd_rn(p.y, __fmul_rn(__fmul_rn(C.gravity.y, C.dt), C.dt));
+    p.z = __fadd_rn(p.z, __fmul_rn(__fmul_rn(C.gravity.z, C.dt), C.dt));
+    return p;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_hash_state(SimConsts C, const float4 *__restrict__ X,
+                                                             const float4 *__restrict__ V, int *__restrict__ keys,
+                                                             int *__restrict__ hist, int tiles)
+{
+    hash_tile(C.n, C.cell, C.D, [&](int i) { return predict(f3(X[i]), f3(V[i]), C); }, keys, hist, tiles);
+}
+
+void launch_hash_f3(cudaStream_t st, int n, const float *pos3, float cell, int D, int *keys, int *hist,
+                    int64_t *launches)
+{
+    if (n <= 0) return;
+    const int tiles = sort_tiles(n);
+    k_hash_f3<<<tiles, kSortThreads, 0, st>>>(n, pos3, cell, D, keys, hist, tiles);
+    ++*launches;
+}
+
+void launch_hash_state(cudaStream_t st, const SimConsts &C, const float4 *X, const float4 *V, int *keys,
+                       int *hist, int64_t *launches)
+{
+    if (C.n <= 0) return;
+    const int tiles = sort_tiles(C.n);
+    k_hash_state<<<tiles, kSortThreads, 0, st>>>(C, X, V, keys, hist, tiles);
+    ++*launches;
+}
+
+// ------------------------------------------------------------------------
+// cell ranges
+// ------------------------------------------------------------------------
+
+// findStartEndId semantics (kernel/grid.cuh:70-99): only occupied cells are written.
+__global__ void k_find_start_end(int n, const int *__restrict__ sorted, int *__restrict__ start,
+                                 int *__restrict__ end)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int u = sorted[i];
+    if (i == 0 || sorted[i - 1] != u) start[u] = i;
+    if (i == n - 1 || sorted[i + 1] != u) end[u] = i + 1;
+}
+
+// resetStartEndId semantics (kernel/grid.cuh:101-132).
+__global__ void k_reset_start_end(int n, const int *__restrict__ sorted, int *__restrict__ start,
+                                  int *__restrict__ end)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int u = sorted[i];
+    if (i == 0 || sorted[i - 1] != u) start[u] = -1;
+    if (i == n - 1 || sorted[i + 1] != u) end[u] = -1;
+}
+
+// Dense prefix: off[c] = number of particles whose key is below c, for
+// c in [0, ncells]; lower bound by binary search in the sorted keys.
+__global__ void k_cell_offsets(int n, int ncells, const int *__restrict__ sorted, int *__restrict__ off)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > ncells) return;
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(sorted + mid) < c) lo = mid + 1;
+        else hi = mid;
+    }
+    off[c] = lo;
+}
+
+void launch_find_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end, int64_t *launches)
+{
+    if (n <= 0) return;
+    k_find_start_end<<<(n + 255) / 256, 256, 0, st>>>(n, sorted, start, end);
+    ++*launches;
+}
+
+void launch_reset_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end, int64_t *launches)
+{
+    if (n <= 0) return;
+    k_reset_start_end<<<(n + 255) / 256, 256, 0, st>>>(n, sorted, start, end);
+    ++*launches;
+}
+
+void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, int64_t *launches)
+{
+    k_cell_offsets<<<(ncells + 1 + 255) / 256, 256, 0, st>>>(n, ncells, sorted, off);
+    ++*launches;
+}
+
+// ------------------------------------------------------------------------
+// reorder
+// ------------------------------------------------------------------------
+
+// Gathers the float4 records into cell order, recomputes the prediction
+// (bit-identical to the hashed one), then computeInvScaledMasses (PS:84-98,
+// on x before stabilisation), two rounds of planeStabilize (PS:822-833) and,
+// when nothing else runs between, iteration 0's plane collision.
+__global__ void __launch_bounds__(256) k_reorder(SimConsts C, ReorderArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    const int o = a.order[i];
+    const float4 X = a.Xc[o];
+    const float4 V = a.Vc[o];
+    const int id = a.orig_c[o];
+    float3 x = f3(X), v = f3(V);
+    float3 p = predict(x, v, C);
+    if (a.inv_scaled) {
+        const float scale = powf(2.7182818284f, -C.mass_k * x.y);
+        a.inv_scaled[i] = 1.0f / (scale * X.w);
+    }
+    if (a.stabilize) {
+        plane_stabilize(C, x, p);
+        plane_stabilize(C, x, p);
+    }
+    if (a.collide) plane_collide(C, x, p);
+    a.Xs[i] = make_float4(x.x, x.y, x.z, X.w);
+    a.Vs[i] = V;
+    a.P[i] = make_float4(p.x, p.y, p.z, V.w);
+    a.mass[i] = X.w;
+    a.orig_s[i] = id;
+    a.to_new[id] = i;
+}
+
+void launch_reorder(cudaStream_t st, const SimConsts &C, const ReorderArgs &a, int64_t *launches)
+{
+    if (C.n <= 0) return;
+    k_reorder<<<(C.n + 255) / 256, 256, 0, st>>>(C, a);
+    ++*launches;
+}
+
+}  // namespace bp

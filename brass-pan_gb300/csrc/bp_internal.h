@@ -1,0 +1,138 @@
+// bp_internal.h -- host-side declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "bp_common.cuh"
+
+namespace bp {
+
+// ---- stable LSD radix sort of (cell key, particle index) pairs -------------
+// 9-bit digits; a tile of 4096 keys per CTA (512 threads x 8 keys).
+constexpr int kRadixBits = 9;
+constexpr int kRadixBins = 1 << kRadixBits;
+constexpr int kSortThreads = 512;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+
+inline int sort_tiles(int n) { return (n + kSortTile - 1) / kSortTile; }
+inline int key_bits(int D)
+{
+    int b = 0;
+    while ((1 << b) < D) ++b;
+    return 3 * b;
+}
+inline int sort_passes(int D) { return (key_bits(D) + kRadixBits - 1) / kRadixBits; }
+
+// Scratch the sort needs beyond its input and output arrays.
+struct SortScratch {
+    int *keys_alt[2];   // n each (only [0] is needed for <= 2 passes)
+    int *vals_alt[2];
+    int *hist;          // kRadixBins * tiles
+    int *digit_total;   // kRadixBins
+};
+size_t sort_scratch_bytes(int n, int D);
+void sort_scratch_carve(void *base, int n, int D, SortScratch *s);
+
+// keys_in: cell keys (pass 0 histogram already in s.hist when hist_ready);
+// vals_in == nullptr means the identity permutation.
+void radix_sort_pairs(cudaStream_t st, int n, int D, const int *keys_in, const int *vals_in, int *keys_out,
+                      int *vals_out, const SortScratch &s, bool hist_ready, int64_t *launches);
+
+// ---- grid kernels launched by the solver and the stand-alone API ----
+void launch_hash_f3(cudaStream_t st, int n, const float *pos3, float cell, int D, int *keys, int *hist,
+                    int64_t *launches);
+void launch_hash_state(cudaStream_t st, const SimConsts &C, const float4 *X, const float4 *V, int *keys,
+                       int *hist, int64_t *launches);
+void launch_find_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end, int64_t *launches);
+void launch_reset_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end,
+                            int64_t *launches);
+void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, int64_t *launches);
+
+struct ReorderArgs {
+    const int *order;      // sorted position -> old index
+    const float4 *Xc, *Vc; // state in the old order
+    const int *orig_c;
+    float4 *Xs, *Vs, *P;   // new order
+    float *mass;
+    int *orig_s, *to_new;
+    float *inv_scaled;     // nullptr: not needed
+    int stabilize;         // run planeStabilize twice
+    int collide;           // also run iteration 0's plane collision
+};
+void launch_reorder(cudaStream_t st, const SimConsts &C, const ReorderArgs &a, int64_t *launches);
+
+// ---- fluid kernels ----
+void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const float *mass, const int *off,
+                   float *lam, float *rho, int64_t *launches);
+struct DeltaArgs {
+    const float4 *P;
+    const float *mass, *lam;
+    const int *off;
+    float4 *Pout;
+    int epilogue;          // 0 none, 1 plane collision (next iteration), 2 commit (+ plane none)
+    const float4 *Xs;      // x for planes / commit
+    float4 *Xc, *Vc;       // commit targets
+    const float4 *Vs;      // for phase bits on commit
+    const int *orig_s;
+    int *orig_c;
+};
+void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, int64_t *launches);
+void launch_post_a(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float *rho,
+                   const int *off, float4 *Om, float4 *Nm, int64_t *launches);
+void launch_post_b(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float4 *Om,
+                   const float4 *Nm, const int *off, float4 *Vout, int64_t *launches);
+void launch_post_c(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
+                   float4 *Vout, int64_t *launches);
+void launch_neighbor_counts(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, int *counts,
+                            int64_t *launches);
+void launch_neighbor_counts_f3(cudaStream_t st, int n, const float *pos3, float cell, int D, float h,
+                               const int *start, const int *end, int *counts);
+
+// ---- per-particle and constraint kernels ----
+void launch_planes(cudaStream_t st, const SimConsts &C, const float4 *Xs, float4 *P, int64_t *launches);
+void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs, const float4 *Vs,
+                   const int *orig_s, float4 *Xc, float4 *Vc, int *orig_c, int64_t *launches);
+void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
+                               const float *w, const int *off, float4 *Pout, int64_t *launches);
+struct DistanceArgs {
+    int num_edges;
+    const int2 *pairs;       // original ids
+    const float2 *params;    // rest length, stiffness
+    int num_nodes;           // particles with incident edges
+    const int *node_ids;     // original ids of those particles
+    const int *node_ptr;     // CSR row pointers (num_nodes + 1)
+    const int *node_inc;     // edge*2 + side
+    float4 *edge_k;          // per-edge correction vector
+};
+void launch_distance(cudaStream_t st, const SimConsts &C, const DistanceArgs &a, float4 *P, const float *w,
+                     const int *to_new, unsigned *err, int64_t *launches);
+struct WindArgs {
+    int num_faces;
+    const int *faces;        // [F][3] original ids
+    int num_nodes;
+    const int *node_ids;
+    const int *node_ptr;
+    const int *node_inc;     // face index
+    float4 *face_move;
+};
+void launch_wind(cudaStream_t st, const SimConsts &C, const WindArgs &a, float4 *P, const float4 *Vs,
+                 const float *mass, const int *to_new, int64_t *launches);
+struct RigidArgs {
+    int num_bodies;
+    const int2 *ranges;      // original ids
+    const float4 *rest;      // by original id
+    float4 *rot, *cm;
+};
+void launch_shape_matching(cudaStream_t st, const SimConsts &C, const RigidArgs &a, float4 *P,
+                           const int *to_new, int64_t *launches);
+void launch_immovable(cudaStream_t st, int k, const int *ids, const int *to_new, const float4 *Xs, float4 *P,
+                      int64_t *launches);
+void launch_pick(cudaStream_t st, int id_orig, const int *to_new, float4 *pos, float3 p, int set_pos, float4 *vel,
+                 float3 v, int64_t *launches);
+void launch_pack_infos(cudaStream_t st, int n, const float4 *X, const float4 *V, void *out);
+void launch_check_finite(cudaStream_t st, int n, const float4 *X, unsigned *err, int64_t *launches);
+
+}  // namespace bp

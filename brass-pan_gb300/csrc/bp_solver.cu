@@ -1,0 +1,815 @@
+// bp_solver.cu -- the solver handle, step orchestration and the C ABI.
+//
+// bp_solver_update replays the stage order of ParticleSolver::update
+// (brasstower/particlesolver.cuh:787-1063) with the commented constraint
+// block (:881-993) and wind block (:838-858) enabled and the iteration count
+// as a parameter.  The whole call is captured once into a CUDA graph per
+// (substeps, iterations, dt, parameters) and replayed afterwards.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bp_internal.h"
+
+using namespace bp;
+
+namespace {
+
+thread_local std::string g_err;
+
+bp_status fail(bp_status st, const std::string &msg)
+{
+    g_err = msg;
+    return st;
+}
+
+#define BP_CUDA(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(e_ == cudaErrorMemoryAllocation ? BP_ERR_OUT_OF_MEMORY : BP_ERR_CUDA,  \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+    } while (0)
+
+bool is_pow2(int d) { return d > 0 && (d & (d - 1)) == 0; }
+
+}  // namespace
+
+struct bp_solver {
+    int n = 0;
+    bp_params prm{};
+    int nplanes = 0;
+    float planes[kMaxPlanes][6];
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0;
+
+    std::vector<void *> allocs;
+
+    float4 *Xc = nullptr, *Vc = nullptr, *Xs = nullptr, *Vs = nullptr, *Pa = nullptr, *Pb = nullptr;
+    float4 *Om = nullptr, *Nm = nullptr;
+    float4 *Pcur = nullptr;  // predicted positions after the last substep
+    int *orig_c = nullptr, *orig_s = nullptr, *to_new = nullptr, *group = nullptr;
+    int *keys = nullptr, *sorted_keys = nullptr, *order = nullptr, *off = nullptr;
+    float *mass = nullptr, *lam = nullptr, *rho = nullptr, *w = nullptr;
+    unsigned *err = nullptr;
+    SortScratch sort{};
+
+    bool has_solid = false;
+    DistanceArgs dist{};
+    WindArgs wind{};
+    RigidArgs rigid{};
+    int nimm = 0;
+    int *imm = nullptr;
+
+    // graph cache
+    cudaGraphExec_t exec = nullptr;
+    int g_sub = -1, g_iter = -1;
+    float g_dt = 0.f;
+    uint64_t g_params_version = ~0ull;
+    uint64_t params_version = 0;
+    int64_t graph_launches = 0;
+    int64_t last_launches = 0;
+
+    ~bp_solver()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (void *p : allocs) cudaFree(p);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+
+    template <class T>
+    bp_status alloc(T **ptr, size_t count)
+    {
+        void *p = nullptr;
+        const size_t bytes = count * sizeof(T) > 0 ? count * sizeof(T) : 16;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess)
+            return fail(BP_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs.push_back(p);
+        *ptr = (T *)p;
+        return BP_OK;
+    }
+    template <class T>
+    bp_status upload(T **ptr, const void *host, size_t count)
+    {
+        bp_status st = alloc(ptr, count);
+        if (st != BP_OK) return st;
+        if (count) BP_CUDA(cudaMemcpy(*ptr, host, count * sizeof(T), cudaMemcpyHostToDevice));
+        return BP_OK;
+    }
+};
+
+extern "C" void bp_params_init(bp_params *p, float r)
+{
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->mode = BP_MODE_REFERENCE;
+    p->stage_mask = BP_STAGE_ALL;
+    p->gravity[0] = 0.f;
+    p->gravity[1] = -9.8f;
+    p->gravity[2] = 0.f;
+    p->particle_radius = r;
+    p->kernel_radius = 2.3f * r;
+    p->cell_size = r * 2.3f;
+    p->grid_dim = 512;
+    p->rest_density = 1200.f;
+    p->solid_density_scale = 2.0f;
+    p->lambda_denominator = 15000.0f;
+    p->relaxation = 300.0f;
+    p->scorr_k = 0.0001f;
+    p->scorr_n = 4;
+    p->scorr_dq = 0.03f;
+    p->delta_clamp = 5.0f;
+    p->vorticity_eps = 0.001f;
+    p->surface_tension = 0.5f;
+    p->xsph_c = 0.0002f;
+    p->friction_static = 0.5f;
+    p->friction_dynamic = 0.0f;
+    p->mass_scaling_k = 2.0f;
+    p->wind_drag = 10.0f;
+    p->wind_lift = 100.0f;
+    p->rotation_iterations = 20;
+}
+
+static bp_status check_params(const bp_params *p)
+{
+    if (!p) return fail(BP_ERR_INVALID_ARGUMENT, "params is NULL");
+    if (p->mode != BP_MODE_REFERENCE && p->mode != BP_MODE_TEXTBOOK) return fail(BP_ERR_INVALID_ARGUMENT, "unknown mode");
+    if (!is_pow2(p->grid_dim) || p->grid_dim < 4 || p->grid_dim > 512)
+        return fail(BP_ERR_INVALID_ARGUMENT, "grid_dim must be a power of two in [4, 512]");
+    if (!(p->cell_size > 0.f) || !(p->kernel_radius > 0.f) || !(p->rest_density > 0.f))
+        return fail(BP_ERR_INVALID_ARGUMENT, "cell_size, kernel_radius and rest_density must be positive");
+    if (p->kernel_radius > p->cell_size * 1.0001f)
+        return fail(BP_ERR_INVALID_ARGUMENT, "kernel_radius must not exceed cell_size (27-cell search)");
+    if (p->rotation_iterations < 0) return fail(BP_ERR_INVALID_ARGUMENT, "rotation_iterations < 0");
+    return BP_OK;
+}
+
+// Substep constants: SetKernelRadius (K/fluid.cuh:11-27) evaluated on the host.
+static SimConsts make_consts(const bp_solver *s, float sdt)
+{
+    const bp_params &p = s->prm;
+    SimConsts C;
+    memset(&C, 0, sizeof(C));
+    C.n = s->n;
+    C.D = p.grid_dim;
+    C.mask = (unsigned)p.grid_dim - 1u;
+    C.cell = p.cell_size;
+    const float h = p.kernel_radius;
+    C.h = h;
+    C.h2 = h * h;
+    C.half_h = h * 0.5f;
+    C.c_poly6 = 315.f / 64.f / 3.141592f / powf(h, 9.0f);
+    C.c_spiky = -45.f / 3.141592f / powf(h, 6.f);
+    C.c_akinci = 32.0f / 3.141592f / powf(h, 9.f);
+    C.c_akinci_off = powf(h, 6.0f) / 64.0f;
+    C.rho0 = p.rest_density;
+    C.inv_rho0 = 1.0f / p.rest_density;
+    C.solid_scale = p.solid_density_scale;
+    C.lambda_den = p.lambda_denominator;
+    C.relaxation = p.relaxation;
+    C.textbook = p.mode == BP_MODE_TEXTBOOK;
+    const bool akinci = (p.stage_mask & BP_STAGE_AKINCI) != 0;
+    C.scorr_on = C.textbook || !akinci;
+    C.clamp_c = akinci;
+    C.scorr_k = p.scorr_k;
+    C.scorr_n = (float)p.scorr_n;
+    {
+        const float dq = powf(p.scorr_dq * h, 2.f);
+        const float t = C.h2 - dq;
+        C.scorr_wq = C.c_poly6 * t * t * t;
+    }
+    C.delta_clamp = C.textbook ? -1.f : p.delta_clamp;  // textbook PBF has no per-pair clamp
+    C.vort_eps = p.vorticity_eps;
+    C.tension = p.surface_tension;
+    C.xsph_c = p.xsph_c;
+    C.use_vort = (p.stage_mask & BP_STAGE_VORTICITY) != 0;
+    C.use_akinci = akinci;
+    C.use_xsph = (p.stage_mask & BP_STAGE_XSPH) != 0;
+    C.radius = p.particle_radius;
+    C.fs = p.friction_static;
+    C.fd = p.friction_dynamic;
+    C.mass_k = p.mass_scaling_k;
+    C.gravity = make_float3(p.gravity[0], p.gravity[1], p.gravity[2]);
+    C.wind = make_float3(p.wind_velocity[0], p.wind_velocity[1], p.wind_velocity[2]);
+    C.wind_drag = p.wind_drag;
+    C.wind_lift = p.wind_lift;
+    C.rot_iters = p.rotation_iterations;
+    C.dt = sdt;
+    C.inv_dt = 1.0f / sdt;
+    C.nplanes = (p.stage_mask & BP_STAGE_PLANES) ? s->nplanes : 0;
+    for (int k = 0; k < s->nplanes; ++k) {
+        C.plane_o[k] = make_float4(s->planes[k][0], s->planes[k][1], s->planes[k][2], 0.f);
+        C.plane_n[k] = make_float4(s->planes[k][3], s->planes[k][4], s->planes[k][5], 0.f);
+    }
+    return C;
+}
+
+// Builds CSR incidence lists (node = original particle id) for a set of
+// constraints that each touch `arity` particles.
+static void build_incidence(int n, int count, int arity, const int32_t *ids, bool encode_side,
+                            std::vector<int> &nodes, std::vector<int> &ptr, std::vector<int> &inc)
+{
+    std::vector<int> deg(n, 0);
+    for (int c = 0; c < count; ++c)
+        for (int a = 0; a < arity; ++a) deg[ids[arity * c + a]]++;
+    std::vector<int> node_of(n, -1);
+    nodes.clear();
+    for (int i = 0; i < n; ++i)
+        if (deg[i]) {
+            node_of[i] = (int)nodes.size();
+            nodes.push_back(i);
+        }
+    ptr.assign(nodes.size() + 1, 0);
+    for (size_t k = 0; k < nodes.size(); ++k) ptr[k + 1] = ptr[k] + deg[nodes[k]];
+    inc.assign(ptr.back(), 0);
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (int c = 0; c < count; ++c)
+        for (int a = 0; a < arity; ++a) {
+            const int nd = node_of[ids[arity * c + a]];
+            inc[fill[nd]++] = encode_side ? (c * 2 + a) : c;
+        }
+}
+
+static bp_status validate_scene(const bp_scene_desc *sc)
+{
+    if (!sc) return fail(BP_ERR_INVALID_ARGUMENT, "scene is NULL");
+    const int n = sc->num_particles;
+    if (n < 0) return fail(BP_ERR_INVALID_ARGUMENT, "num_particles < 0");
+    if (n > (1 << 28)) return fail(BP_ERR_CAPACITY, "num_particles above 2^28");
+    if (n > 0 && (!sc->positions || !sc->masses || !sc->phases))
+        return fail(BP_ERR_INVALID_ARGUMENT, "positions, masses and phases are required");
+    for (int i = 0; i < n; ++i) {
+        if (sc->phases[i] == 0) return fail(BP_ERR_INVALID_ARGUMENT, "phase 0 is reserved (fluid < 0, solid > 0)");
+        if (!(sc->masses[i] > 0.f)) return fail(BP_ERR_INVALID_ARGUMENT, "masses must be positive");
+    }
+    if (sc->num_planes < 0 || sc->num_planes > kMaxPlanes)
+        return fail(BP_ERR_CAPACITY, "at most 16 planes");
+    if (sc->num_planes > 0 && !sc->planes) return fail(BP_ERR_INVALID_ARGUMENT, "planes is NULL");
+    auto check_ids = [&](int count, int arity, const int32_t *ids, const char *what) -> bp_status {
+        if (count < 0) return fail(BP_ERR_INVALID_ARGUMENT, std::string(what) + ": negative count");
+        if (count > 0 && !ids) return fail(BP_ERR_INVALID_ARGUMENT, std::string(what) + ": NULL");
+        for (long k = 0; k < (long)count * arity; ++k)
+            if (ids[k] < 0 || ids[k] >= n) return fail(BP_ERR_INVALID_ARGUMENT, std::string(what) + ": id out of range");
+        return BP_OK;
+    };
+    bp_status st;
+    if ((st = check_ids(sc->num_distance_constraints, 2, sc->distance_pairs, "distance_pairs")) != BP_OK) return st;
+    if (sc->num_distance_constraints > 0 && !sc->distance_params)
+        return fail(BP_ERR_INVALID_ARGUMENT, "distance_params is NULL");
+    if ((st = check_ids(sc->num_wind_faces, 3, sc->wind_faces, "wind_faces")) != BP_OK) return st;
+    if ((st = check_ids(sc->num_immovables, 1, sc->immovables, "immovables")) != BP_OK) return st;
+    if (sc->num_rigid_bodies < 0) return fail(BP_ERR_INVALID_ARGUMENT, "num_rigid_bodies < 0");
+    if (sc->num_rigid_bodies > 0 && (!sc->rigid_ranges || !sc->rigid_rest_positions))
+        return fail(BP_ERR_INVALID_ARGUMENT, "rigid_ranges / rigid_rest_positions is NULL");
+    for (int b = 0; b < sc->num_rigid_bodies; ++b) {
+        const int r0 = sc->rigid_ranges[2 * b], r1 = sc->rigid_ranges[2 * b + 1];
+        if (r0 < 0 || r1 > n || r1 <= r0) return fail(BP_ERR_INVALID_ARGUMENT, "rigid range out of bounds");
+    }
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_create(const bp_scene_desc *sc, const bp_params *prm, void *stream, bp_solver **out)
+{
+    if (!out) return fail(BP_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    bp_status st;
+    if ((st = validate_scene(sc)) != BP_OK) return st;
+    if ((st = check_params(prm)) != BP_OK) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(BP_ERR_NO_DEVICE, "no CUDA device visible");
+    }
+    bp_solver *s = new (std::nothrow) bp_solver();
+    if (!s) return fail(BP_ERR_OUT_OF_MEMORY, "host allocation failed");
+    auto bail = [&](bp_status e) {
+        delete s;
+        return e;
+    };
+    const int n = sc->num_particles;
+    s->n = n;
+    s->prm = *prm;
+    s->nplanes = sc->num_planes;
+    for (int k = 0; k < s->nplanes; ++k)
+        for (int c = 0; c < 6; ++c) s->planes[k][c] = sc->planes[6 * k + c];
+    cudaGetDevice(&s->device);
+    if (stream) {
+        s->stream = (cudaStream_t)stream;
+    } else {
+        // graphs cannot be captured on the legacy stream; a blocking stream
+        // still orders itself with it, like the reference's default-stream use
+        if (cudaStreamCreate(&s->stream) != cudaSuccess) return bail(fail(BP_ERR_CUDA, "cudaStreamCreate failed"));
+        s->own_stream = true;
+    }
+
+    const size_t N = (size_t)(n > 0 ? n : 1);
+    const int D = prm->grid_dim;
+    const size_t ncells = (size_t)D * D * D;
+    if ((st = s->alloc(&s->Xc, N)) || (st = s->alloc(&s->Vc, N)) || (st = s->alloc(&s->Xs, N)) ||
+        (st = s->alloc(&s->Vs, N)) || (st = s->alloc(&s->Pa, N)) || (st = s->alloc(&s->Pb, N)) ||
+        (st = s->alloc(&s->Om, N)) || (st = s->alloc(&s->Nm, N)) || (st = s->alloc(&s->orig_c, N)) ||
+        (st = s->alloc(&s->orig_s, N)) || (st = s->alloc(&s->to_new, N)) || (st = s->alloc(&s->group, N)) ||
+        (st = s->alloc(&s->keys, N)) || (st = s->alloc(&s->sorted_keys, N)) || (st = s->alloc(&s->order, N)) ||
+        (st = s->alloc(&s->off, ncells + 1)) || (st = s->alloc(&s->mass, N)) || (st = s->alloc(&s->lam, N)) ||
+        (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)))
+        return bail(st);
+    {
+        char *scratch = nullptr;
+        if ((st = s->alloc(&scratch, sort_scratch_bytes((int)N, D)))) return bail(st);
+        sort_scratch_carve(scratch, (int)N, D, &s->sort);
+    }
+
+    // initial state in original order (sorted order == identity)
+    std::vector<float4> X(N), V(N), P(N);
+    std::vector<int> ids(N), grp(N, 0);
+    bool has_solid = false;
+    for (int i = 0; i < n; ++i) {
+        const float *x = sc->positions + 3 * i;
+        const float *v = sc->velocities ? sc->velocities + 3 * i : nullptr;
+        int ph = sc->phases[i];
+        has_solid |= ph > 0;
+        float phf;
+        memcpy(&phf, &ph, 4);
+        X[i] = make_float4(x[0], x[1], x[2], sc->masses[i]);
+        V[i] = make_float4(v ? v[0] : 0.f, v ? v[1] : 0.f, v ? v[2] : 0.f, phf);
+        P[i] = make_float4(x[0], x[1], x[2], phf);
+        ids[i] = i;
+        if (sc->group_ids) grp[i] = sc->group_ids[i];
+    }
+    s->has_solid = has_solid;
+    if (n > 0) {
+        BP_CUDA(cudaMemcpy(s->Xc, X.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        BP_CUDA(cudaMemcpy(s->Vc, V.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        BP_CUDA(cudaMemcpy(s->Pa, P.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        BP_CUDA(cudaMemcpy(s->orig_c, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+        BP_CUDA(cudaMemcpy(s->to_new, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+        BP_CUDA(cudaMemcpy(s->group, grp.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+        std::vector<float> m(sc->masses, sc->masses + n);
+        BP_CUDA(cudaMemcpy(s->mass, m.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    s->Pcur = s->Pa;
+    BP_CUDA(cudaMemset(s->lam, 0, N * sizeof(float)));
+    BP_CUDA(cudaMemset(s->rho, 0, N * sizeof(float)));
+    BP_CUDA(cudaMemset(s->Om, 0, N * sizeof(float4)));
+    BP_CUDA(cudaMemset(s->Nm, 0, N * sizeof(float4)));
+    BP_CUDA(cudaMemset(s->off, 0, (ncells + 1) * sizeof(int)));
+    BP_CUDA(cudaMemset(s->sorted_keys, 0, N * sizeof(int)));
+    BP_CUDA(cudaMemset(s->err, 0, sizeof(unsigned)));
+
+    // distance constraints
+    if (sc->num_distance_constraints > 0) {
+        const int m = sc->num_distance_constraints;
+        std::vector<int> nodes, ptr, inc;
+        build_incidence(n, m, 2, sc->distance_pairs, true, nodes, ptr, inc);
+        s->dist.num_edges = m;
+        s->dist.num_nodes = (int)nodes.size();
+        int2 *pairs;
+        float2 *params;
+        int *nid, *nptr, *ninc;
+        float4 *ek;
+        if ((st = s->upload(&pairs, sc->distance_pairs, m)) || (st = s->upload(&params, sc->distance_params, m)) ||
+            (st = s->upload(&nid, nodes.data(), nodes.size())) || (st = s->upload(&nptr, ptr.data(), ptr.size())) ||
+            (st = s->upload(&ninc, inc.data(), inc.size())) || (st = s->alloc(&ek, m)))
+            return bail(st);
+        s->dist.pairs = pairs;
+        s->dist.params = params;
+        s->dist.node_ids = nid;
+        s->dist.node_ptr = nptr;
+        s->dist.node_inc = ninc;
+        s->dist.edge_k = ek;
+    }
+    if (sc->num_wind_faces > 0) {
+        const int f = sc->num_wind_faces;
+        std::vector<int> nodes, ptr, inc;
+        build_incidence(n, f, 3, sc->wind_faces, false, nodes, ptr, inc);
+        s->wind.num_faces = f;
+        s->wind.num_nodes = (int)nodes.size();
+        int *faces, *nid, *nptr, *ninc;
+        float4 *mv;
+        if ((st = s->upload(&faces, sc->wind_faces, 3 * (size_t)f)) || (st = s->upload(&nid, nodes.data(), nodes.size())) ||
+            (st = s->upload(&nptr, ptr.data(), ptr.size())) || (st = s->upload(&ninc, inc.data(), inc.size())) ||
+            (st = s->alloc(&mv, f)))
+            return bail(st);
+        s->wind.faces = faces;
+        s->wind.node_ids = nid;
+        s->wind.node_ptr = nptr;
+        s->wind.node_inc = ninc;
+        s->wind.face_move = mv;
+    }
+    if (sc->num_rigid_bodies > 0) {
+        const int b = sc->num_rigid_bodies;
+        std::vector<float4> rest(N, make_float4(0.f, 0.f, 0.f, 0.f));
+        for (int i = 0; i < n; ++i)
+            rest[i] = make_float4(sc->rigid_rest_positions[3 * i], sc->rigid_rest_positions[3 * i + 1],
+                                  sc->rigid_rest_positions[3 * i + 2], 0.f);
+        std::vector<float4> rot(b, make_float4(0.f, 0.f, 0.f, 1.f)), cm(b, make_float4(0.f, 0.f, 0.f, 0.f));
+        int2 *ranges;
+        float4 *drest, *drot, *dcm;
+        if ((st = s->upload(&ranges, sc->rigid_ranges, b)) || (st = s->upload(&drest, rest.data(), N)) ||
+            (st = s->upload(&drot, rot.data(), b)) || (st = s->upload(&dcm, cm.data(), b)))
+            return bail(st);
+        s->rigid.num_bodies = b;
+        s->rigid.ranges = ranges;
+        s->rigid.rest = drest;
+        s->rigid.rot = drot;
+        s->rigid.cm = dcm;
+    }
+    if (sc->num_immovables > 0) {
+        s->nimm = sc->num_immovables;
+        if ((st = s->upload(&s->imm, sc->immovables, s->nimm))) return bail(st);
+    }
+    BP_CUDA(cudaDeviceSynchronize());
+    *out = s;
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_destroy(bp_solver *s)
+{
+    if (!s) return BP_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    delete s;
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_set_params(bp_solver *s, const bp_params *prm)
+{
+    if (!s) return fail(BP_ERR_INVALID_ARGUMENT, "solver is NULL");
+    bp_status st = check_params(prm);
+    if (st != BP_OK) return st;
+    if (prm->grid_dim != s->prm.grid_dim) return fail(BP_ERR_INVALID_ARGUMENT, "grid_dim cannot change after creation");
+    s->prm = *prm;
+    s->params_version++;
+    return BP_OK;
+}
+
+// Enqueues one substep; returns the number of kernels launched.
+static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int picked, float3 ppos,
+                            int64_t *L)
+{
+    const cudaStream_t st = s->stream;
+    const int mask = s->prm.stage_mask;
+    const bool planes = (mask & BP_STAGE_PLANES) && s->nplanes > 0;
+    const bool wind = (mask & BP_STAGE_WIND) && s->wind.num_faces > 0;
+    const bool pcoll = (mask & BP_STAGE_PARTICLE_COLLISION) && s->has_solid;
+    const bool fluid = (mask & BP_STAGE_FLUID) != 0;
+    const bool distance = (mask & BP_STAGE_DISTANCE) && s->dist.num_edges > 0;
+    const bool rigid = (mask & BP_STAGE_SHAPE_MATCHING) && s->rigid.num_bodies > 0;
+    const bool immov = (mask & BP_STAGE_IMMOVABLE) && s->nimm > 0;
+    const bool picking = picked >= 0;
+    const bool tail = distance || rigid || immov;  // stages after the fluid position pass
+    const int D = s->prm.grid_dim;
+
+    if (picking) launch_pick(st, picked, s->to_new, s->Xc, ppos, 1, s->Vc, make_float3(0.f, 0.f, 0.f), L);
+
+    launch_hash_state(st, C, s->Xc, s->Vc, s->keys, s->sort.hist, L);
+    radix_sort_pairs(st, s->n, D, s->keys, nullptr, s->sorted_keys, s->order, s->sort, true, L);
+    launch_cell_offsets(st, s->n, D * D * D, s->sorted_keys, s->off, L);
+
+    const bool fuse_first_planes = planes && !wind && !picking && iterations > 0;
+    ReorderArgs ra;
+    ra.order = s->order;
+    ra.Xc = s->Xc;
+    ra.Vc = s->Vc;
+    ra.orig_c = s->orig_c;
+    ra.Xs = s->Xs;
+    ra.Vs = s->Vs;
+    ra.P = s->Pa;
+    ra.mass = s->mass;
+    ra.orig_s = s->orig_s;
+    ra.to_new = s->to_new;
+    ra.inv_scaled = (distance || pcoll) ? s->w : nullptr;
+    ra.stabilize = planes;
+    ra.collide = fuse_first_planes;
+    launch_reorder(st, C, ra, L);
+
+    float4 *cur = s->Pa, *other = s->Pb;
+    if (wind) launch_wind(st, C, s->wind, cur, s->Vs, s->mass, s->to_new, L);
+
+    bool planes_done = fuse_first_planes;
+    bool committed = false;
+    for (int it = 0; it < iterations; ++it) {
+        if (picking) launch_pick(st, picked, s->to_new, cur, ppos, 1, nullptr, make_float3(0.f, 0.f, 0.f), L);
+        if (planes && !planes_done) launch_planes(st, C, s->Xs, cur, L);
+        planes_done = false;
+        if (pcoll) {
+            launch_particle_collision(st, C, cur, s->Xs, s->w, s->off, other, L);
+            std::swap(cur, other);
+        }
+        if (fluid) {
+            launch_lambda(st, C, cur, s->mass, s->off, s->lam, s->rho, L);
+            DeltaArgs da;
+            da.P = cur;
+            da.mass = s->mass;
+            da.lam = s->lam;
+            da.off = s->off;
+            da.Pout = other;
+            da.epilogue = 0;
+            da.Xs = s->Xs;
+            da.Xc = s->Xc;
+            da.Vc = s->Vc;
+            da.Vs = s->Vs;
+            da.orig_s = s->orig_s;
+            da.orig_c = s->orig_c;
+            if (!tail) {
+                if (it == iterations - 1) {
+                    da.epilogue = 2;
+                    committed = true;
+                } else if (planes && !picking) {
+                    da.epilogue = 1;
+                    planes_done = true;
+                }
+            }
+            launch_deltap(st, C, da, L);
+            std::swap(cur, other);
+        }
+        if (distance) launch_distance(st, C, s->dist, cur, s->w, s->to_new, s->err, L);
+        if (rigid) launch_shape_matching(st, C, s->rigid, cur, s->to_new, L);
+        if (immov) launch_immovable(st, s->nimm, s->imm, s->to_new, s->Xs, cur, L);
+    }
+    if (!committed) launch_commit(st, C, cur, s->Xs, s->Vs, s->orig_s, s->Xc, s->Vc, s->orig_c, L);
+    s->Pcur = cur;
+
+    const bool post_ab = C.use_vort || C.use_akinci;
+    if (post_ab) {
+        launch_post_a(st, C, cur, s->Vc, s->rho, s->off, s->Om, s->Nm, L);
+        launch_post_b(st, C, cur, s->Vc, s->Om, s->Nm, s->off, C.use_xsph ? s->Vs : s->Vc, L);
+        if (C.use_xsph) launch_post_c(st, C, cur, s->Vs, s->off, s->Vc, L);
+    } else if (C.use_xsph) {
+        launch_post_c(st, C, cur, s->Vc, s->off, s->Vs, L);
+        cudaMemcpyAsync(s->Vc, s->Vs, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+    }
+}
+
+static bp_status enqueue_update(bp_solver *s, int nsub, float dt, int iterations, int picked, float3 ppos,
+                                float3 pvel, int64_t *L)
+{
+    const float sdt = dt / (float)nsub;
+    const SimConsts C = make_consts(s, sdt);
+    for (int k = 0; k < nsub; ++k) enqueue_substep(s, C, iterations, picked, ppos, L);
+    if (picked >= 0) launch_pick(s->stream, picked, s->to_new, s->Xc, ppos, 0, s->Vc, pvel, L);
+    launch_check_finite(s->stream, s->n, s->Xc, s->err, L);
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_update(bp_solver *s, int32_t nsub, float dt, int32_t iterations, int32_t picked,
+                                      const float *ppos, const float *pvel)
+{
+    if (!s) return fail(BP_ERR_INVALID_ARGUMENT, "solver is NULL");
+    if (nsub <= 0 || !(dt > 0.f) || iterations < 0)
+        return fail(BP_ERR_INVALID_ARGUMENT, "num_substeps > 0, dt > 0 and iterations >= 0 required");
+    if (s->n <= 0) return BP_OK;  // particlesolver.cuh:778
+    if (picked >= s->n) picked = -1;  // the reference ignores out-of-range picks (:790)
+    if (picked >= 0 && !ppos) return fail(BP_ERR_INVALID_ARGUMENT, "picked_position is NULL");
+    const float3 pp = ppos ? make_float3(ppos[0], ppos[1], ppos[2]) : make_float3(0.f, 0.f, 0.f);
+    const float3 pv = pvel ? make_float3(pvel[0], pvel[1], pvel[2]) : make_float3(0.f, 0.f, 0.f);
+    int64_t L = 0;
+    if (picked >= 0) {
+        enqueue_update(s, nsub, dt, iterations, picked, pp, pv, &L);
+        BP_CUDA(cudaGetLastError());
+        s->last_launches = L;
+        return BP_OK;
+    }
+    const bool hit = s->exec && s->g_sub == nsub && s->g_iter == iterations && s->g_dt == dt &&
+                     s->g_params_version == s->params_version;
+    if (!hit) {
+        if (s->exec) {
+            cudaGraphExecDestroy(s->exec);
+            s->exec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        BP_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_update(s, nsub, dt, iterations, -1, pp, pv, &L);
+        cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+        if (e != cudaSuccess) return fail(BP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&s->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(BP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        s->g_sub = nsub;
+        s->g_iter = iterations;
+        s->g_dt = dt;
+        s->g_params_version = s->params_version;
+        s->graph_launches = L;
+    }
+    BP_CUDA(cudaGraphLaunch(s->exec, s->stream));
+    s->last_launches = s->graph_launches;
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_step(bp_solver *s, float dt, int32_t nsub, int32_t iterations)
+{
+    return bp_solver_update(s, nsub, dt, iterations, -1, nullptr, nullptr);
+}
+
+extern "C" bp_status bp_solver_query_original_particle_id(bp_solver *s, int32_t sorted_index, int32_t *out)
+{
+    if (!s || !out) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (sorted_index < 0 || sorted_index >= s->n) return fail(BP_ERR_INVALID_ARGUMENT, "index out of range");
+    BP_CUDA(cudaMemcpyAsync(out, s->orig_c + sorted_index, 4, cudaMemcpyDeviceToHost, s->stream));
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_query_new_particle_id(bp_solver *s, int32_t original, int32_t *out)
+{
+    if (!s || !out) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (original < 0 || original >= s->n) return fail(BP_ERR_INVALID_ARGUMENT, "id out of range");
+    BP_CUDA(cudaMemcpyAsync(out, s->to_new + original, 4, cudaMemcpyDeviceToHost, s->stream));
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_get_particle_position(bp_solver *s, int32_t idx, float out[3])
+{
+    if (!s || !out) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (idx < 0 || idx >= s->n) {  // the reference returns (0,0,0) (particlesolver.cuh:380)
+        out[0] = out[1] = out[2] = 0.f;
+        return BP_OK;
+    }
+    float4 v;
+    BP_CUDA(cudaMemcpyAsync(&v, s->Xc + idx, sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    out[0] = v.x;
+    out[1] = v.y;
+    out[2] = v.z;
+    return BP_OK;
+}
+
+static bp_status copy_xyz(bp_solver *s, const float4 *src, float *dst, int order)
+{
+    if (!s || !dst) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (order != BP_ORDER_SORTED && order != BP_ORDER_ORIGINAL) return fail(BP_ERR_INVALID_ARGUMENT, "bad order");
+    const int n = s->n;
+    if (n == 0) return BP_OK;
+    std::vector<float4> tmp(n);
+    std::vector<int> ids;
+    BP_CUDA(cudaMemcpyAsync(tmp.data(), src, n * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
+    if (order == BP_ORDER_ORIGINAL) {
+        ids.resize(n);
+        BP_CUDA(cudaMemcpyAsync(ids.data(), s->orig_c, n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    }
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < n; ++i) {
+        const int o = order == BP_ORDER_ORIGINAL ? ids[i] : i;
+        dst[3 * o] = tmp[i].x;
+        dst[3 * o + 1] = tmp[i].y;
+        dst[3 * o + 2] = tmp[i].z;
+    }
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_copy_positions(bp_solver *s, float *host_xyz, int32_t order)
+{
+    return copy_xyz(s, s ? s->Xc : nullptr, host_xyz, order);
+}
+
+extern "C" bp_status bp_solver_copy_velocities(bp_solver *s, float *host_xyz, int32_t order)
+{
+    return copy_xyz(s, s ? s->Vc : nullptr, host_xyz, order);
+}
+
+extern "C" bp_status bp_solver_set_state(bp_solver *s, const float *hx, const float *hv, int32_t order)
+{
+    if (!s) return fail(BP_ERR_INVALID_ARGUMENT, "solver is NULL");
+    if (order != BP_ORDER_SORTED && order != BP_ORDER_ORIGINAL) return fail(BP_ERR_INVALID_ARGUMENT, "bad order");
+    const int n = s->n;
+    if (n == 0) return BP_OK;
+    std::vector<float4> X(n), V(n);
+    std::vector<int> ids(n);
+    BP_CUDA(cudaMemcpyAsync(X.data(), s->Xc, n * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
+    BP_CUDA(cudaMemcpyAsync(V.data(), s->Vc, n * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
+    BP_CUDA(cudaMemcpyAsync(ids.data(), s->orig_c, n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < n; ++i) {
+        const int o = order == BP_ORDER_ORIGINAL ? ids[i] : i;
+        if (hx) X[i] = make_float4(hx[3 * o], hx[3 * o + 1], hx[3 * o + 2], X[i].w);
+        if (hv) V[i] = make_float4(hv[3 * o], hv[3 * o + 1], hv[3 * o + 2], V[i].w);
+    }
+    BP_CUDA(cudaMemcpyAsync(s->Xc, X.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
+    BP_CUDA(cudaMemcpyAsync(s->Vc, V.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_field(bp_solver *s, int32_t field, void **ptr, size_t *bytes)
+{
+    if (!s || !ptr || !bytes) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    const size_t n = (size_t)s->n;
+    const int D = s->prm.grid_dim;
+    switch (field) {
+    case BP_FIELD_POSITIONS: *ptr = s->Xc; *bytes = n * 16; break;
+    case BP_FIELD_NEW_POSITIONS: *ptr = s->Pcur; *bytes = n * 16; break;
+    case BP_FIELD_VELOCITIES: *ptr = s->Vc; *bytes = n * 16; break;
+    case BP_FIELD_MAP_TO_ORIGINAL: *ptr = s->orig_c; *bytes = n * 4; break;
+    case BP_FIELD_MAP_TO_NEW: *ptr = s->to_new; *bytes = n * 4; break;
+    case BP_FIELD_LAMBDAS: *ptr = s->lam; *bytes = n * 4; break;
+    case BP_FIELD_DENSITIES: *ptr = s->rho; *bytes = n * 4; break;
+    case BP_FIELD_SORTED_CELL_IDS: *ptr = s->sorted_keys; *bytes = n * 4; break;
+    case BP_FIELD_CELL_OFFSETS: *ptr = s->off; *bytes = ((size_t)D * D * D + 1) * 4; break;
+    case BP_FIELD_RIGID_ROTATIONS: *ptr = s->rigid.rot; *bytes = (size_t)s->rigid.num_bodies * 16; break;
+    case BP_FIELD_RIGID_CMS: *ptr = s->rigid.cm; *bytes = (size_t)s->rigid.num_bodies * 16; break;
+    case BP_FIELD_INV_SCALED_MASSES: *ptr = s->w; *bytes = n * 4; break;
+    default: return fail(BP_ERR_INVALID_ARGUMENT, "unknown field");
+    }
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_copy_field(bp_solver *s, int32_t field, void *dst, size_t bytes)
+{
+    void *p;
+    size_t b;
+    bp_status st = bp_solver_field(s, field, &p, &b);
+    if (st != BP_OK) return st;
+    if (!dst || bytes < b) return fail(BP_ERR_INVALID_ARGUMENT, "destination too small");
+    if (b == 0) return BP_OK;
+    BP_CUDA(cudaMemcpyAsync(dst, p, b, cudaMemcpyDeviceToHost, s->stream));
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_pack_particle_infos(bp_solver *s, void *device_out)
+{
+    if (!s || (!device_out && s->n > 0)) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    launch_pack_infos(s->stream, s->n, s->Xc, s->Vc, device_out);
+    BP_CUDA(cudaGetLastError());
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_device_errors(bp_solver *s, uint32_t *out)
+{
+    if (!s || !out) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    unsigned v = 0;
+    BP_CUDA(cudaMemcpyAsync(&v, s->err, 4, cudaMemcpyDeviceToHost, s->stream));
+    BP_CUDA(cudaMemsetAsync(s->err, 0, 4, s->stream));
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    *out = v;
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_last_launch_count(bp_solver *s, int64_t *out)
+{
+    if (!s || !out) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = s->last_launches;
+    return BP_OK;
+}
+
+// ---- stand-alone grid -------------------------------------------------------
+
+extern "C" bp_status bp_grid_workspace_size(int32_t n, int32_t D, size_t *bytes)
+{
+    if (!bytes || n < 0 || !is_pow2(D) || D < 4 || D > 1024) return fail(BP_ERR_INVALID_ARGUMENT, "bad argument");
+    *bytes = sort_scratch_bytes(n > 0 ? n : 1, D);
+    return BP_OK;
+}
+
+extern "C" bp_status bp_grid_build(void *stream, int32_t n, const float *pos, float cell, int32_t D, int32_t *cell_ids,
+                                   int32_t *sorted_cell_ids, int32_t *sorted_ids, int32_t *start, int32_t *end,
+                                   void *ws, size_t ws_bytes)
+{
+    if (n < 0 || !is_pow2(D) || D < 4 || D > 1024 || !(cell > 0.f))
+        return fail(BP_ERR_INVALID_ARGUMENT, "bad argument");
+    if (n == 0) return BP_OK;
+    if (!pos || !cell_ids || !sorted_cell_ids || !sorted_ids || !start || !end || !ws)
+        return fail(BP_ERR_INVALID_ARGUMENT, "NULL buffer");
+    if (ws_bytes < sort_scratch_bytes(n, D)) return fail(BP_ERR_INVALID_ARGUMENT, "workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    SortScratch sc;
+    sort_scratch_carve(ws, n, D, &sc);
+    int64_t L = 0;
+    launch_hash_f3(st, n, pos, cell, D, cell_ids, sc.hist, &L);
+    radix_sort_pairs(st, n, D, cell_ids, nullptr, sorted_cell_ids, sorted_ids, sc, true, &L);
+    launch_find_start_end(st, n, sorted_cell_ids, start, end, &L);
+    BP_CUDA(cudaGetLastError());
+    return BP_OK;
+}
+
+extern "C" bp_status bp_grid_reset(void *stream, int32_t n, const int32_t *sorted, int32_t *start, int32_t *end)
+{
+    if (n < 0) return fail(BP_ERR_INVALID_ARGUMENT, "n < 0");
+    if (n == 0) return BP_OK;
+    if (!sorted || !start || !end) return fail(BP_ERR_INVALID_ARGUMENT, "NULL buffer");
+    int64_t L = 0;
+    launch_reset_start_end((cudaStream_t)stream, n, sorted, start, end, &L);
+    BP_CUDA(cudaGetLastError());
+    return BP_OK;
+}
+
+extern "C" bp_status bp_grid_neighbor_counts(void *stream, int32_t n, const float *sorted_pos, float cell, int32_t D,
+                                             float h, const int32_t *start, const int32_t *end, int32_t *counts)
+{
+    if (n < 0 || !is_pow2(D) || D < 4 || D > 1024 || !(cell > 0.f) || !(h > 0.f))
+        return fail(BP_ERR_INVALID_ARGUMENT, "bad argument");
+    if (n == 0) return BP_OK;
+    if (!sorted_pos || !start || !end || !counts) return fail(BP_ERR_INVALID_ARGUMENT, "NULL buffer");
+    launch_neighbor_counts_f3((cudaStream_t)stream, n, sorted_pos, cell, D, h, start, end, counts);
+    BP_CUDA(cudaGetLastError());
+    return BP_OK;
+}
+
+extern "C" const char *bp_last_error_string(void) { return g_err.c_str(); }
+
+extern "C" int32_t bp_abi_version(void) { return BP_ABI_VERSION; }

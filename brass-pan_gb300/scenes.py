@@ -1,0 +1,260 @@
+"""Scene description and builders (host side of the reference's Scene API).
+
+`Scene` holds flat arrays in original particle order, the content of the
+reference's `Scene` vectors (brasstower/scene.h:455-535).  The builders follow
+the reference's object factories and the way ParticleSolver's add* methods
+assign phases and ids (brasstower/particlesolver.cuh:395-710):
+
+* fluids share one negative phase per block (fluidPhaseCounter, -1, -2, ...);
+* granulars and self-colliding ropes/cloths get one solid phase per particle
+  (setDevArr_counterIncrement), rigid bodies one solid phase per body;
+* constraint ids are offset by the particle count before the object.
+
+The BASELINE benchmark scenes (`config0_dam_break`, `config1_mixed`) are
+built from the same factories with seeded jitter.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Scene:
+    positions: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.float32))
+    velocities: np.ndarray | None = None
+    masses: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    phases: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    group_ids: np.ndarray | None = field(default_factory=lambda: np.zeros(0, np.int32))
+    planes: np.ndarray = field(default_factory=lambda: np.zeros((0, 6), np.float32))
+    distance_pairs: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int32))
+    distance_params: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.float32))
+    faces: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.int32))
+    rigid_ranges: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int32))
+    rigid_rest: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.float32))
+    immovables: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    # counters as in the reference
+    solid_phase_counter: int = 1
+    fluid_phase_counter: int = -1
+    group_counter: int = 0
+    # solver parameters that belong to the scene
+    particle_radius: float = 0.05
+    kernel_radius: float = 0.115
+    cell_size: float = 0.115
+    grid_dim: int = 512
+    rest_density: float = 1200.0
+    name: str = "scene"
+
+    @property
+    def num_particles(self) -> int:
+        return int(len(self.positions))
+
+    # -- internal append -------------------------------------------------------
+    def _append(self, pos, mass, phases, rest=None):
+        pos = np.asarray(pos, np.float32).reshape(-1, 3)
+        n0 = self.num_particles
+        k = len(pos)
+        self.positions = np.concatenate([self.positions, pos]).astype(np.float32)
+        self.masses = np.concatenate([self.masses, np.full(k, mass, np.float32)])
+        self.phases = np.concatenate([self.phases, np.asarray(phases, np.int32)])
+        self.group_ids = np.concatenate([self.group_ids, np.full(k, self.group_counter, np.int32)])
+        self.group_counter += 1
+        r = np.zeros((k, 3), np.float32) if rest is None else np.asarray(rest, np.float32)
+        self.rigid_rest = np.concatenate([self.rigid_rest, r]).astype(np.float32)
+        if self.velocities is not None:
+            self.velocities = np.concatenate([self.velocities, np.zeros((k, 3), np.float32)])
+        return n0
+
+    def _solid_phases(self, k, self_collide=True):
+        if self_collide:
+            ph = np.arange(self.solid_phase_counter, self.solid_phase_counter + k, dtype=np.int32)
+            self.solid_phase_counter += k
+        else:
+            ph = np.full(k, self.solid_phase_counter, np.int32)
+            self.solid_phase_counter += 1
+        return ph
+
+    # -- builders ----------------------------------------------------------------
+    def add_plane(self, origin, normal):
+        """Plane(origin, normal) (scene.h:13-37); the normal is used as given."""
+        row = np.array([*origin, *normal], np.float32).reshape(1, 6)
+        self.planes = np.concatenate([self.planes, row])
+
+    @staticmethod
+    def _block(dim, start, step):
+        """CreateFluidBlock / CreateGranularsBlock / CreateRigidBox lattice order:
+        i (x) outer, k (z) inner (scene.h:62-67, 104-110, 131-137)."""
+        dim = np.asarray(dim, int)
+        i, j, k = np.meshgrid(np.arange(dim[0]), np.arange(dim[1]), np.arange(dim[2]), indexing="ij")
+        ijk = np.stack([i.ravel(), j.ravel(), k.ravel()], axis=1).astype(np.float32)
+        return np.asarray(start, np.float32) + np.asarray(step, np.float32) * ijk
+
+    def add_fluid_block(self, dim, start, step, mass, jitter=0.0, rng=None):
+        pos = self._block(dim, start, step)
+        if jitter:
+            pos = pos + rng.uniform(-jitter, jitter, pos.shape).astype(np.float32)
+        n0 = self._append(pos, mass, np.full(len(pos), self.fluid_phase_counter, np.int32))
+        self.fluid_phase_counter -= 1  # particlesolver.cuh:505
+        return n0, self.num_particles
+
+    def add_granulars_block(self, dim, start, step, mass):
+        pos = self._block(dim, start, step)
+        n0 = self._append(pos, mass, self._solid_phases(len(pos), True))
+        return n0, self.num_particles
+
+    def add_rigid_body(self, pos, mass):
+        """RigidBody + addRigidBody (scene.h:39-89, particlesolver.cuh:424-478):
+        rest shape = positions minus their (unweighted) centre of mass."""
+        pos = np.asarray(pos, np.float32).reshape(-1, 3)
+        cm = pos.mean(axis=0, dtype=np.float64).astype(np.float32)
+        rest = pos - cm
+        n0 = self._append(pos, mass, self._solid_phases(len(pos), False), rest=rest)
+        self.rigid_ranges = np.concatenate([self.rigid_ranges, np.array([[n0, self.num_particles]], np.int32)])
+        return n0, self.num_particles
+
+    def add_rigid_box(self, dim, start, step, mass):
+        return self.add_rigid_body(self._block(dim, start, step), mass)
+
+    def add_rope(self, start, end, num_joint, mass, self_collide=True):
+        """Rope::CreateRope + addNoodles (scene.h:141-179, particlesolver.cuh:510-573)."""
+        start = np.asarray(start, np.float32)
+        diff = np.asarray(end, np.float32) - start
+        d = float(np.linalg.norm(diff)) / float(num_joint - 1)
+        t = (np.arange(num_joint, dtype=np.float32) / np.float32(num_joint - 1))[:, None]
+        pos = start + t * diff
+        n0 = self._append(pos, mass, self._solid_phases(num_joint, self_collide))
+        pairs = [(i, i + 1) for i in range(num_joint - 1)] + [(i - 1, i + 1) for i in range(1, num_joint - 1)]
+        params = [(d, 1.0)] * (num_joint - 1) + [(2.0 * d, 0.1)] * (num_joint - 2)
+        self._add_pairs(np.array(pairs, np.int32) + n0, np.array(params, np.float32))
+        return n0, self.num_particles
+
+    def _add_pairs(self, pairs, params):
+        self.distance_pairs = np.concatenate([self.distance_pairs, pairs.reshape(-1, 2).astype(np.int32)])
+        self.distance_params = np.concatenate([self.distance_params, params.reshape(-1, 2).astype(np.float32)])
+
+    def add_cloth(self, start, offset_x, offset_y, nx, ny, mass, corners=(False, False, False, False),
+                  stretch=0.2, shear=None, bend=0.1, self_collide=True):
+        """Cloth::CreateCloth + addCloth (scene.h:226-330, particlesolver.cuh:576-710).
+
+        Positions are pushed x-outer / y-inner as start + y*offset_x + x*offset_y
+        while constraint ids use y*nx + x; for square cloths that only
+        transposes the lattice, exactly as the reference does.  Pairs:
+        horizontal and vertical (stretch), both diagonals (shear), and the
+        skip-one "hack bending" pairs of the 3x3 stencil (bend), with the
+        reference's repetitions."""
+        shear = stretch if shear is None else shear
+        ox = np.asarray(offset_x, np.float32)
+        oy = np.asarray(offset_y, np.float32)
+        lx = float(np.linalg.norm(ox))
+        ly = float(np.linalg.norm(oy))
+        ld = float(np.linalg.norm(ox + oy))
+        pos, faces, pairs, params, imm = [], [], [], [], []
+        if corners[0]:
+            imm.append(0)
+        if corners[1]:
+            imm.append(nx - 1)
+        if corners[2]:
+            imm.append(nx * (ny - 1))
+        if corners[3]:
+            imm.append(nx * ny - 1)
+        for x in range(nx):
+            for y in range(ny):
+                pos.append(np.asarray(start, np.float32) + np.float32(y) * ox + np.float32(x) * oy)
+                p1 = y * nx + x
+                p2 = y * nx + x + 1
+                p3 = (y + 1) * nx + x
+                p4 = (y + 1) * nx + x + 1
+                if x < nx - 1 and y < ny - 1:
+                    faces.append((p1, p2, p3))
+                    faces.append((p2, p3, p4))
+                if x < nx - 1:
+                    pairs.append((p1, p2)); params.append((lx, stretch))
+                if y < ny - 1:
+                    pairs.append((p1, p3)); params.append((ly, stretch))
+                if x < nx - 1 and y < ny - 1:
+                    pairs.append((p1, p4)); params.append((ld, shear))
+                    pairs.append((p2, p3)); params.append((ld, shear))
+                if 0 < x < nx - 1 and 0 < y < ny - 1:
+                    q = [[(y + i) * nx + x + j for j in (-1, 0, 1)] for i in (-1, 0, 1)]
+                    for i in range(3):
+                        pairs.append((q[i][0], q[i][2])); params.append((lx * 2, bend))
+                    for i in range(3):
+                        pairs.append((q[0][i], q[2][i])); params.append((ly * 2, bend))
+        pos = np.array(pos, np.float32)
+        n0 = self._append(pos, mass, self._solid_phases(len(pos), self_collide))
+        self._add_pairs(np.array(pairs, np.int32) + n0, np.array(params, np.float32))
+        if faces:
+            self.faces = np.concatenate([self.faces, np.array(faces, np.int32) + n0])
+        if imm:
+            self.immovables = np.concatenate([self.immovables, np.array(imm, np.int32) + n0])
+        return n0, self.num_particles
+
+    def make_immovable(self, ids):
+        self.immovables = np.concatenate([self.immovables, np.asarray(ids, np.int32).ravel()])
+
+
+def box_planes(scene: Scene, lo, hi, ceiling=False):
+    """Floor and four walls of the axis-aligned box [lo, hi] (normals inward)."""
+    lo = np.asarray(lo, np.float32)
+    hi = np.asarray(hi, np.float32)
+    scene.add_plane((0, lo[1], 0), (0, 1, 0))
+    scene.add_plane((lo[0], 0, 0), (1, 0, 0))
+    scene.add_plane((hi[0], 0, 0), (-1, 0, 0))
+    scene.add_plane((0, 0, lo[2]), (0, 0, 1))
+    scene.add_plane((0, 0, hi[2]), (0, 0, -1))
+    if ceiling:
+        scene.add_plane((0, hi[1], 0), (0, -1, 0))
+
+
+def pbf_scene(nx, ny, nz, spacing=0.1, seed=0, box=None, jitter_frac=0.01, grid_dim=64, mass=None):
+    """A fluid block on a cubic lattice in the corner of a box: the dam break
+    of the benchmark configuration.  h = 2*spacing, cell = h, rho0 = m/d^3."""
+    rng = np.random.default_rng(seed)
+    d = np.float32(spacing)
+    s = Scene(name=f"pbf_{nx}x{ny}x{nz}")
+    s.particle_radius = float(d / 2)
+    s.kernel_radius = float(2 * d)
+    s.cell_size = float(2 * d)
+    s.grid_dim = grid_dim
+    m = float(mass) if mass is not None else float(1000.0 * d ** 3)
+    s.rest_density = m / float(d) ** 3
+    if box is None:
+        box = (max(4.0, nx * d + 1.0), max(4.0, ny * d + 1.0), max(4.0, nz * d + 1.0))
+    box_planes(s, (0, 0, 0), box)
+    s.add_fluid_block((nx, ny, nz), (d, d, d), (d, d, d), m, jitter=jitter_frac * d, rng=rng)
+    return s
+
+
+def config0_dam_break(seed=0):
+    """32^3 = 32,768 fluid particles, d = 0.1, jitter +-0.01d, box [0,4]^3."""
+    return pbf_scene(32, 32, 32, 0.1, seed=seed, box=(4.0, 4.0, 4.0), jitter_frac=0.01)
+
+
+def config1_mixed(seed=0, fluid=(128, 64, 128), cloth=256, cubes=64, cube_dim=8):
+    """1,048,576 fluid particles (128x64x128 block), a 256x256 cloth under
+    wind, 64 rigid cubes of 8^3 particles; box [0,25.6]x[0,12.8]x[0,25.6]."""
+    rng = np.random.default_rng(seed)
+    d = np.float32(0.1)
+    s = Scene(name="mixed")
+    s.particle_radius = float(d / 2)
+    s.kernel_radius = float(2 * d)
+    s.cell_size = float(2 * d)
+    s.grid_dim = 64
+    m = float(1000.0 * d ** 3)
+    s.rest_density = m / float(d) ** 3
+    box = (fluid[0] * d + 0.2, 16.0, fluid[2] * d + 0.2)
+    box_planes(s, (0, 0, 0), box)
+    s.add_fluid_block(fluid, (d, d, d), (d, d, d), m, jitter=0.01 * d, rng=rng)
+    if cloth:
+        y = float(fluid[1] * d + 2.0)
+        span = (box[0] - 0.2) / cloth
+        s.add_cloth((0.1, y, 0.1), (span, 0, 0), (0, 0, span), cloth, cloth, m,
+                    stretch=1.0, shear=0.5, bend=0.1)
+    ncube = int(round(cubes ** 0.5))
+    for c in range(cubes):
+        cx, cz = c % ncube, c // ncube
+        start = (1.0 + cx * (box[0] - 2.0) / ncube, fluid[1] * d + 4.0 + (c % 3) * 1.0,
+                 1.0 + cz * (box[2] - 2.0) / ncube)
+        s.add_rigid_box((cube_dim,) * 3, start, (d, d, d), m)
+    return s

@@ -1,0 +1,154 @@
+"""Python mirror of the reference's ParticleSolver interface over the C ABI.
+
+Method names follow brasstower/particlesolver.cuh (update, queryOriginalParticleId,
+queryNewParticleId, getParticlePosition) so host code written against the
+reference ports line for line.  Every call goes through libbrasspan.so; there
+is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .scenes import Scene
+
+
+def make_params(scene: Scene | None = None, mode: int = abi.BP_MODE_REFERENCE, stage_mask: int | None = None,
+                **overrides) -> abi.BpParams:
+    """bp_params with the reference's literals, the scene's geometry, then overrides."""
+    lib = abi.load()
+    p = abi.BpParams()
+    radius = scene.particle_radius if scene is not None else 0.05
+    lib.bp_params_init(C.byref(p), C.c_float(radius))
+    if scene is not None:
+        p.kernel_radius = scene.kernel_radius
+        p.cell_size = scene.cell_size
+        p.grid_dim = scene.grid_dim
+        p.rest_density = scene.rest_density
+    p.mode = mode
+    if stage_mask is not None:
+        p.stage_mask = stage_mask
+    for k, v in overrides.items():
+        if isinstance(getattr(p, k), C.Array):
+            arr = getattr(p, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(p, k, v)
+    return p
+
+
+class ParticleSolver:
+    """One solver handle on the current CUDA device."""
+
+    def __init__(self, scene: Scene, params: abi.BpParams | None = None, stream: int | None = None):
+        self.lib = abi.load()
+        self.scene = scene
+        self.params = params if params is not None else make_params(scene)
+        desc, self._keep = abi.scene_desc(scene)
+        h = C.c_void_p()
+        abi.check(self.lib, self.lib.bp_solver_create(C.byref(desc), C.byref(self.params),
+                                                      C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.handle = h
+        self.n = scene.num_particles
+
+    # -- reference interface ------------------------------------------------------
+    def update(self, num_substeps: int, dt: float, iterations: int = 2, picked_original_id: int = -1,
+               picked_position=(0.0, 0.0, 0.0), picked_velocity=(0.0, 0.0, 0.0)):
+        pp = (C.c_float * 3)(*picked_position)
+        pv = (C.c_float * 3)(*picked_velocity)
+        abi.check(self.lib, self.lib.bp_solver_update(self.handle, num_substeps, C.c_float(dt), iterations,
+                                                      picked_original_id, pp, pv))
+
+    def step(self, dt: float, substeps: int, iterations: int):
+        abi.check(self.lib, self.lib.bp_solver_step(self.handle, C.c_float(dt), substeps, iterations))
+
+    def queryOriginalParticleId(self, sorted_index: int) -> int:
+        out = C.c_int32()
+        abi.check(self.lib, self.lib.bp_solver_query_original_particle_id(self.handle, sorted_index, C.byref(out)))
+        return out.value
+
+    def queryNewParticleId(self, original_id: int) -> int:
+        out = C.c_int32()
+        abi.check(self.lib, self.lib.bp_solver_query_new_particle_id(self.handle, original_id, C.byref(out)))
+        return out.value
+
+    def getParticlePosition(self, sorted_index: int) -> np.ndarray:
+        out = (C.c_float * 3)()
+        abi.check(self.lib, self.lib.bp_solver_get_particle_position(self.handle, sorted_index, out))
+        return np.array(out[:], np.float32)
+
+    # -- state access ----------------------------------------------------------------
+    def positions(self, order: int = abi.BP_ORDER_ORIGINAL) -> np.ndarray:
+        out = np.empty((self.n, 3), np.float32)
+        abi.check(self.lib, self.lib.bp_solver_copy_positions(
+            self.handle, out.ctypes.data_as(C.POINTER(C.c_float)), order))
+        return out
+
+    def velocities(self, order: int = abi.BP_ORDER_ORIGINAL) -> np.ndarray:
+        out = np.empty((self.n, 3), np.float32)
+        abi.check(self.lib, self.lib.bp_solver_copy_velocities(
+            self.handle, out.ctypes.data_as(C.POINTER(C.c_float)), order))
+        return out
+
+    def set_state(self, positions=None, velocities=None, order: int = abi.BP_ORDER_ORIGINAL):
+        x = None if positions is None else np.ascontiguousarray(positions, np.float32)
+        v = None if velocities is None else np.ascontiguousarray(velocities, np.float32)
+        abi.check(self.lib, self.lib.bp_solver_set_state(
+            self.handle, None if x is None else x.ctypes.data_as(C.POINTER(C.c_float)),
+            None if v is None else v.ctypes.data_as(C.POINTER(C.c_float)), order))
+
+    _DTYPES = {
+        abi.BP_FIELD_POSITIONS: (np.float32, 4), abi.BP_FIELD_NEW_POSITIONS: (np.float32, 4),
+        abi.BP_FIELD_VELOCITIES: (np.float32, 4), abi.BP_FIELD_MAP_TO_ORIGINAL: (np.int32, 1),
+        abi.BP_FIELD_MAP_TO_NEW: (np.int32, 1), abi.BP_FIELD_LAMBDAS: (np.float32, 1),
+        abi.BP_FIELD_DENSITIES: (np.float32, 1), abi.BP_FIELD_SORTED_CELL_IDS: (np.int32, 1),
+        abi.BP_FIELD_CELL_OFFSETS: (np.int32, 1), abi.BP_FIELD_RIGID_ROTATIONS: (np.float32, 4),
+        abi.BP_FIELD_RIGID_CMS: (np.float32, 4), abi.BP_FIELD_INV_SCALED_MASSES: (np.float32, 1),
+    }
+
+    def field_ptr(self, field: int) -> tuple[int, int]:
+        ptr = C.c_void_p()
+        nbytes = C.c_size_t()
+        abi.check(self.lib, self.lib.bp_solver_field(self.handle, field, C.byref(ptr), C.byref(nbytes)))
+        return ptr.value or 0, nbytes.value
+
+    def field(self, field: int) -> np.ndarray:
+        dt, width = self._DTYPES[field]
+        _, nbytes = self.field_ptr(field)
+        out = np.empty(nbytes // 4, dt)
+        if nbytes:
+            abi.check(self.lib, self.lib.bp_solver_copy_field(self.handle, field, out.ctypes.data, nbytes))
+        return out.reshape(-1, width) if width > 1 else out
+
+    def device_errors(self) -> int:
+        out = C.c_uint32()
+        abi.check(self.lib, self.lib.bp_solver_device_errors(self.handle, C.byref(out)))
+        return out.value
+
+    def last_launch_count(self) -> int:
+        out = C.c_int64()
+        abi.check(self.lib, self.lib.bp_solver_last_launch_count(self.handle, C.byref(out)))
+        return out.value
+
+    def pack_particle_infos(self, device_ptr: int):
+        abi.check(self.lib, self.lib.bp_solver_pack_particle_infos(self.handle, C.c_void_p(device_ptr)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.bp_solver_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -1,0 +1,250 @@
+/*
+ * brasspan.h -- C ABI of the GB300-native unified particle solver step.
+ *
+ * This is the drop-in boundary for brass-pan's `ParticleSolver`
+ * (brasstower/particlesolver.cuh).  Every entry point is plain C: opaque
+ * handles, plain pointers and sizes, integer status codes, no exceptions and
+ * no C++ or PyTorch types.  Each declaration names the reference interface it
+ * replaces (file:line inside the brass-pan project).
+ *
+ * Memory: the solver owns its device memory (bp_solver_destroy frees it).
+ * Arrays are kept in cell-sorted order between steps, exactly like the
+ * reference keeps devPositions & co. permuted (particlesolver.cuh:758-764);
+ * original ids map through bp_solver_query_* or bp_solver_copy_* with
+ * BP_ORDER_ORIGINAL.
+ *
+ * Streams: each solver is bound to the CUDA stream given at creation (NULL =
+ * legacy default stream, as the reference uses).  Calls on one solver are not
+ * thread-safe; different solvers are independent.  bp_solver_update only
+ * enqueues work (a CUDA graph replay after the first call of a given shape);
+ * the copy / query / error entry points synchronise the stream.
+ */
+#ifndef BRASSPAN_H
+#define BRASSPAN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BP_ABI_VERSION 1
+
+typedef enum bp_status {
+    BP_OK = 0,
+    BP_ERR_INVALID_ARGUMENT = 1, /* NULL handle, negative count, bad id, ... */
+    BP_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+    BP_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed */
+    BP_ERR_CAPACITY = 4,         /* a size is beyond a documented limit */
+    BP_ERR_DEVICE_CHECK = 5,     /* a device-side check fired during the last step */
+    BP_ERR_NO_DEVICE = 6         /* no CUDA device visible */
+} bp_status;
+
+/* Bits of the device error word (bp_solver_device_errors). */
+#define BP_DEVERR_NONFINITE 0x1u     /* a predicted position became NaN/Inf */
+#define BP_DEVERR_RIGID_SIZE 0x2u    /* reserved */
+#define BP_DEVERR_BAD_INDEX 0x4u     /* a constraint referenced an id outside [0, N) */
+
+/* Parameter presets. */
+typedef enum bp_mode {
+    /* Reproduces the reference kernels as written, quirks included
+     * (density over j >= i, precomputed lambda denominator, per-pair clamp,
+     * Akinci spline inner branch, wind without a wind vector, ...). */
+    BP_MODE_REFERENCE = 0,
+    /* Textbook position-based fluids (Macklin & Mueller 2013): density over
+     * all neighbours, lambda = -C / (sum |grad C|^2 + eps), s_corr active,
+     * no per-pair clamp, wind relative to a wind vector. */
+    BP_MODE_TEXTBOOK = 1
+} bp_mode;
+
+/* Stage switches (bp_params.stage_mask).  BP_STAGE_ALL is the reference's
+ * update() with its commented-out constraint block (particlesolver.cuh:881-993)
+ * and wind block (:838-858) enabled. */
+#define BP_STAGE_PLANES 0x001
+#define BP_STAGE_WIND 0x002
+#define BP_STAGE_PARTICLE_COLLISION 0x004
+#define BP_STAGE_FLUID 0x008
+#define BP_STAGE_DISTANCE 0x010
+#define BP_STAGE_SHAPE_MATCHING 0x020
+#define BP_STAGE_IMMOVABLE 0x040
+#define BP_STAGE_VORTICITY 0x080
+#define BP_STAGE_AKINCI 0x100
+#define BP_STAGE_XSPH 0x200
+#define BP_STAGE_ALL 0x3ff
+/* The stages the reference's update() runs as shipped (only planes and the
+ * velocity post-passes are live there). */
+#define BP_STAGE_REFERENCE_AS_SHIPPED \
+    (BP_STAGE_PLANES | BP_STAGE_VORTICITY | BP_STAGE_AKINCI | BP_STAGE_XSPH)
+
+/* Every literal of the reference's step as a field.  bp_params_init fills the
+ * reference's values; comments give the reference location of each. */
+typedef struct bp_params {
+    int32_t mode;                /* bp_mode */
+    int32_t stage_mask;          /* BP_STAGE_* */
+    float gravity[3];            /* (0,-9.8,0), added as g*dt*dt to the prediction (particlesolver.cuh:56) */
+    float particle_radius;       /* solid radius: planes and contacts (scene.h:500) */
+    float kernel_radius;         /* SPH smoothing length h (fluid.cuh:11) */
+    float cell_size;             /* hash cell edge; the reference uses 2.3*radius == h (particlesolver.cuh:221) */
+    int32_t grid_dim;            /* D, power of two in [4, 512]: D^3 cells (particlesolver.cuh:222 uses 512) */
+    float rest_density;          /* rho0 (scene.h OldSceneFormat::fluidRestDensity) */
+    float solid_density_scale;   /* 2.0 (particlesolver.cuh:909) */
+    float lambda_denominator;    /* 15000, reference mode (fluid.cuh:153) */
+    float relaxation;            /* epsilon of the exact lambda, textbook mode (fluid.cuh:155) */
+    float scorr_k;               /* 0.0001 (particlesolver.cuh:926) */
+    int32_t scorr_n;             /* 4 (particlesolver.cuh:927) */
+    float scorr_dq;              /* s_corr reference distance as a fraction of h: 0.03 (fluid.cuh:208) */
+    float delta_clamp;           /* per-pair |delta p| clamp: 5.0 (fluid.cuh:214); <= 0 disables */
+    float vorticity_eps;         /* 0.001 (particlesolver.cuh:1017) */
+    float surface_tension;       /* Akinci gamma 0.5 (particlesolver.cuh:1043) */
+    float xsph_c;                /* 0.0002 (particlesolver.cuh:1055) */
+    float friction_static;       /* 0.5 (cubrasstower.cuh:18) */
+    float friction_dynamic;      /* 0.0 (cubrasstower.cuh:19) */
+    float mass_scaling_k;        /* 2 (cubrasstower.cuh:20) */
+    float wind_velocity[3];      /* textbook mode only: the wind vector */
+    float wind_drag;             /* 10 (wind.cuh:40) */
+    float wind_lift;             /* 100 (wind.cuh:43) */
+    int32_t rotation_iterations; /* 20 (shapematching.cuh:72) */
+    int32_t reserved[8];
+} bp_params;
+
+/* Fills `p` with the reference's literals for a scene of the given particle
+ * radius (h = cell = 2.3 * radius, D = 512, rho0 = 1200 as initFluidScene). */
+void bp_params_init(bp_params *p, float particle_radius);
+
+/* Scene description in original particle order (host pointers, copied at
+ * creation).  Replaces the reference's `Scene` vectors (scene.h:455-535) and
+ * the OldSceneFormat objects (scene.h:39-435). */
+typedef struct bp_scene_desc {
+    int32_t num_particles;
+    const float *positions;            /* [N][3] */
+    const float *velocities;           /* [N][3] or NULL for zero */
+    const float *masses;               /* [N], > 0 */
+    const int32_t *phases;             /* [N]: < 0 fluid, > 0 solid (never 0) */
+    const int32_t *group_ids;          /* [N] or NULL (render grouping only) */
+    int32_t num_planes;
+    const float *planes;               /* [P][6]: origin xyz, unit normal xyz */
+    int32_t num_distance_constraints;
+    const int32_t *distance_pairs;     /* [M][2] original ids */
+    const float *distance_params;      /* [M][2]: rest length, stiffness */
+    int32_t num_wind_faces;
+    const int32_t *wind_faces;         /* [F][3] original ids */
+    int32_t num_rigid_bodies;
+    const int32_t *rigid_ranges;       /* [B][2]: [first, last+1) original ids */
+    const float *rigid_rest_positions; /* [N][3] by original id; each body's rest shape has its centre at 0 */
+    int32_t num_immovables;
+    const int32_t *immovables;         /* [K] original ids */
+} bp_scene_desc;
+
+typedef struct bp_solver bp_solver;
+
+/* ParticleSolver(const shared_ptr<Scene>&) / ParticleSolver(shared_ptr<OldSceneFormat>)
+ * (particlesolver.cuh:148-215, :218-342).  `stream` is a cudaStream_t or NULL. */
+bp_status bp_solver_create(const bp_scene_desc *scene, const bp_params *params, void *stream,
+                           bp_solver **out);
+
+/* The reference never frees its buffers ("TODO:: implement object's destroyer",
+ * particlesolver.cuh:1074); this releases everything the solver owns. */
+bp_status bp_solver_destroy(bp_solver *s);
+
+/* ParticleSolver::update(numSubTimeStep, deltaTime, pickedOriginalParticleId,
+ * pickedParticlePosition, pickedParticleVelocity) (particlesolver.cuh:772-1072),
+ * with the solver-iteration count, hard-coded to 2 there (:862), as a
+ * parameter.  picked_original_id < 0 disables picking; picked_* may then be NULL. */
+bp_status bp_solver_update(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
+                           int32_t picked_original_id, const float *picked_position,
+                           const float *picked_velocity);
+
+/* update() without picking. */
+bp_status bp_solver_step(bp_solver *s, float dt, int32_t num_substeps, int32_t iterations);
+
+/* Replaces the parameters (takes effect at the next update). */
+bp_status bp_solver_set_params(bp_solver *s, const bp_params *params);
+
+/* queryOriginalParticleId / queryNewParticleId (particlesolver.cuh:352-366). */
+bp_status bp_solver_query_original_particle_id(bp_solver *s, int32_t sorted_index, int32_t *out);
+bp_status bp_solver_query_new_particle_id(bp_solver *s, int32_t original_id, int32_t *out);
+
+/* getParticlePosition(sorted index) (particlesolver.cuh:378-386). */
+bp_status bp_solver_get_particle_position(bp_solver *s, int32_t sorted_index, float out_xyz[3]);
+
+typedef enum bp_order { BP_ORDER_SORTED = 0, BP_ORDER_ORIGINAL = 1 } bp_order;
+
+/* Host copies of the state ([N][3] floats), synchronising the solver's stream. */
+bp_status bp_solver_copy_positions(bp_solver *s, float *host_xyz, int32_t order);
+bp_status bp_solver_copy_velocities(bp_solver *s, float *host_xyz, int32_t order);
+/* Overwrites positions and velocities (host [N][3], either may be NULL). */
+bp_status bp_solver_set_state(bp_solver *s, const float *host_positions,
+                              const float *host_velocities, int32_t order);
+
+typedef enum bp_field {
+    BP_FIELD_POSITIONS = 0,      /* float4 [N]: committed x, w = mass */
+    BP_FIELD_NEW_POSITIONS = 1,  /* float4 [N]: predicted p, w = phase (int bits) */
+    BP_FIELD_VELOCITIES = 2,     /* float4 [N] */
+    BP_FIELD_MAP_TO_ORIGINAL = 3,/* int32 [N]: sorted index -> original id */
+    BP_FIELD_MAP_TO_NEW = 4,     /* int32 [N]: original id -> sorted index */
+    BP_FIELD_LAMBDAS = 5,        /* float [N] */
+    BP_FIELD_DENSITIES = 6,      /* float [N] */
+    BP_FIELD_SORTED_CELL_IDS = 7,/* int32 [N] */
+    BP_FIELD_CELL_OFFSETS = 8,   /* int32 [D^3+1]: first sorted index of each cell */
+    BP_FIELD_RIGID_ROTATIONS = 9,/* float4 [B] quaternion (x,y,z,w) */
+    BP_FIELD_RIGID_CMS = 10,     /* float4 [B] */
+    BP_FIELD_INV_SCALED_MASSES = 11, /* float [N] */
+    BP_FIELD_COUNT = 12
+} bp_field;
+
+/* Device pointer and byte size of a field (valid until the next update;
+ * fields are swapped between buffers inside update, like the reference's
+ * std::swap calls at particlesolver.cuh:758-764,1048,1060). */
+bp_status bp_solver_field(bp_solver *s, int32_t field, void **device_ptr, size_t *bytes);
+/* Synchronous host copy of a whole field. */
+bp_status bp_solver_copy_field(bp_solver *s, int32_t field, void *host_dst, size_t bytes);
+
+/* Headless stand-in for the render hand-off mapParticleInfos (main.cu:273-282):
+ * writes N records {float x, y, z; int32 phase} (16 bytes each, sorted order)
+ * into a caller-owned device buffer, on the solver's stream. */
+bp_status bp_solver_pack_particle_infos(bp_solver *s, void *device_out);
+
+/* Reads and clears the device error word (BP_DEVERR_* bits). */
+bp_status bp_solver_device_errors(bp_solver *s, uint32_t *out_bits);
+
+/* Number of kernels the last bp_solver_update enqueued. */
+bp_status bp_solver_last_launch_count(bp_solver *s, int64_t *out);
+
+/* ---- Stand-alone hash grid on caller-owned device buffers ---------------
+ * Replaces updateGrid() (particlesolver.cuh:712-765): updateGridId
+ * (kernel/grid.cuh:30-47), the CUB stable radix sort (particlesolver.cuh:721-738)
+ * and findStartEndId (kernel/grid.cuh:70-99).  positions are [N][3] floats.
+ * cell_start/cell_end hold D^3 int32 each and, as in the reference, must be
+ * -1 everywhere before the call (set once, then restored by bp_grid_reset);
+ * only the entries of occupied cells are written. */
+bp_status bp_grid_workspace_size(int32_t num_particles, int32_t grid_dim, size_t *bytes);
+bp_status bp_grid_build(void *stream, int32_t num_particles, const float *d_positions,
+                        float cell_size, int32_t grid_dim, int32_t *d_cell_ids,
+                        int32_t *d_sorted_cell_ids, int32_t *d_sorted_particle_ids,
+                        int32_t *d_cell_start, int32_t *d_cell_end, void *d_workspace,
+                        size_t workspace_bytes);
+/* resetStartEndId (kernel/grid.cuh:101-132). */
+bp_status bp_grid_reset(void *stream, int32_t num_particles, const int32_t *d_sorted_cell_ids,
+                        int32_t *d_cell_start, int32_t *d_cell_end);
+
+/* Neighbour counts in the reference's 27-cell walk (the loop structure of
+ * kernel/fluid.cuh:104-141): for each particle i of the cell-sorted positions
+ * [N][3], the number of j (i itself included) stored in the 27 cells around
+ * the cell of p_i with |p_i - p_j|^2 <= h^2.  start/end as from bp_grid_build. */
+bp_status bp_grid_neighbor_counts(void *stream, int32_t num_particles, const float *d_sorted_positions,
+                                  float cell_size, int32_t grid_dim, float kernel_radius,
+                                  const int32_t *d_cell_start, const int32_t *d_cell_end,
+                                  int32_t *d_counts);
+
+/* Last error message of this thread ("" if none). */
+const char *bp_last_error_string(void);
+
+/* ABI version and build description. */
+int32_t bp_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BRASSPAN_H */

@@ -1,0 +1,240 @@
+"""Python handle on the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+* `OracleSolver`: the C restatement in oracle.c (liboracle.so), any mode.
+* `RefSolver`: the reference's own kernels compiled for the host through
+  oracle/refshim (oracle/_ref/libbrassref.so); only where the reference
+  checkout was present at build time, reference parameters only.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this
+module, as the checker or the timed CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import importlib.util
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent
+ORACLE_LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libbrassref.so"
+REF_SRC = Path(os.environ.get("BRASSPAN_REFERENCE", "/root/reference")) / "brasstower"
+
+
+def _abi():
+    mod = sys.modules.get("brasspan_gb300")
+    if mod is not None:
+        return mod.abi
+    mod = sys.modules.get("_brasspan_abi")
+    if mod is None:
+        spec = importlib.util.spec_from_file_location("_brasspan_abi", REPO / "brass-pan_gb300" / "abi.py")
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules["_brasspan_abi"] = mod
+        spec.loader.exec_module(mod)
+    return mod
+
+
+def build_oracle(force: bool = False) -> Path:
+    args = ["make", "-s", "-C", str(HERE), "all"]
+    if force:
+        args.insert(1, "-B")
+    subprocess.run(args, check=True)
+    return ORACLE_LIB
+
+
+def build_ref(force: bool = False) -> Path | None:
+    """Compiles oracle/_ref from the reference checkout; None when it is absent."""
+    if not REF_SRC.is_dir():
+        return None
+    args = ["make", "-s", "-C", str(HERE), "ref", f"REF={REF_SRC}"]
+    if force:
+        args.insert(1, "-B")
+    subprocess.run(args, check=True)
+    return REF_LIB
+
+
+_or = None
+_ref = None
+
+
+def oracle_lib():
+    global _or
+    if _or is None:
+        if not ORACLE_LIB.exists():
+            build_oracle()
+        lib = C.CDLL(str(ORACLE_LIB))
+        abi = _abi()
+        vp, i32, f32 = C.c_void_p, C.c_int32, C.c_float
+        lib.or_create.restype = vp
+        lib.or_create.argtypes = [C.POINTER(abi.BpSceneDesc), C.POINTER(abi.BpParams)]
+        lib.or_destroy.argtypes = [vp]
+        lib.or_set_params.argtypes = [vp, C.POINTER(abi.BpParams)]
+        lib.or_update.argtypes = [vp, i32, f32, i32, i32, vp, vp]
+        lib.or_get.argtypes = [vp, i32, vp]
+        lib.or_set_state.argtypes = [vp, vp, vp]
+        lib.or_set_threads.argtypes = [i32]
+        lib.or_grid_build.argtypes = [i32, vp, f32, i32, vp, vp, vp, vp, vp]
+        lib.or_neighbor_counts.argtypes = [i32, vp, f32, i32, f32, vp, vp, vp]
+        _or = lib
+    return _or
+
+
+def ref_lib():
+    """The host build of the reference kernels, or None if it was not built."""
+    global _ref
+    if _ref is None:
+        if not REF_LIB.exists():
+            if build_ref() is None:
+                return None
+        lib = C.CDLL(str(REF_LIB))
+        abi = _abi()
+        vp, i32, f32 = C.c_void_p, C.c_int32, C.c_float
+        lib.ref_create.restype = vp
+        lib.ref_create.argtypes = [C.POINTER(abi.BpSceneDesc), f32, f32, f32, i32, f32]
+        lib.ref_destroy.argtypes = [vp]
+        lib.ref_update.argtypes = [vp, i32, f32, i32, i32, i32, vp, vp]
+        lib.ref_get.argtypes = [vp, i32, vp]
+        lib.ref_set_threads.argtypes = [i32]
+        lib.ref_grid_build.argtypes = [i32, vp, f32, i32, vp, vp, vp, vp, vp]
+        lib.ref_neighbor_counts.argtypes = [i32, vp, f32, i32, f32, vp, vp, vp]
+        _ref = lib
+    return _ref
+
+
+# field ids shared by or_get / ref_get
+F_X, F_P, F_V, F_TO_ORIG, F_TO_NEW, F_LAMBDA, F_DENSITY, F_INVSCALED, F_SORTED_CELL, F_ROT, F_CM, \
+    F_OMEGA, F_NORMAL, F_MASS, F_PHASE = range(15)
+
+
+class _Base:
+    n: int
+    nb: int
+
+    def _get(self, field):
+        shapes = {F_X: (self.n, 3), F_P: (self.n, 3), F_V: (self.n, 3), F_OMEGA: (self.n, 3),
+                  F_NORMAL: (self.n, 3), F_ROT: (self.nb, 4), F_CM: (self.nb, 3)}
+        ints = {F_TO_ORIG, F_TO_NEW, F_SORTED_CELL, F_PHASE}
+        shape = shapes.get(field, (self.n,))
+        out = np.zeros(shape, np.int32 if field in ints else np.float32)
+        if out.size:
+            self._getter(self.h, field, out.ctypes.data)
+        return out
+
+    def get(self, field):
+        return self._get(field)
+
+    def positions(self, original_order=True):
+        x = self._get(F_X)
+        if not original_order:
+            return x
+        out = np.empty_like(x)
+        out[self._get(F_TO_ORIG)] = x
+        return out
+
+    def velocities(self, original_order=True):
+        v = self._get(F_V)
+        if not original_order:
+            return v
+        out = np.empty_like(v)
+        out[self._get(F_TO_ORIG)] = v
+        return out
+
+    def update(self, num_substeps, dt, iterations=2, picked=-1, picked_position=None, picked_velocity=None):
+        pp = None if picked_position is None else np.ascontiguousarray(picked_position, np.float32)
+        pv = None if picked_velocity is None else np.ascontiguousarray(picked_velocity, np.float32)
+        self._update(num_substeps, dt, iterations, picked, pp, pv)
+
+
+class OracleSolver(_Base):
+    """oracle.c: the restatement, deterministic when single-threaded."""
+
+    def __init__(self, scene, params, threads: int = 1):
+        self.lib = oracle_lib()
+        self.lib.or_set_threads(threads)
+        abi = _abi()
+        desc, keep = abi.scene_desc(scene)
+        self.params = params
+        self.h = self.lib.or_create(C.byref(desc), C.byref(params))
+        self.n = scene.num_particles
+        self.nb = int(len(scene.rigid_ranges))
+        self._getter = self.lib.or_get
+
+    def set_threads(self, threads):
+        self.lib.or_set_threads(threads)
+
+    def _update(self, nsub, dt, iters, picked, pp, pv):
+        self.lib.or_update(self.h, nsub, C.c_float(dt), iters, picked,
+                           None if pp is None else pp.ctypes.data, None if pv is None else pv.ctypes.data)
+
+    def set_state(self, x_sorted=None, v_sorted=None):
+        x = None if x_sorted is None else np.ascontiguousarray(x_sorted, np.float32)
+        v = None if v_sorted is None else np.ascontiguousarray(v_sorted, np.float32)
+        self.lib.or_set_state(self.h, None if x is None else x.ctypes.data, None if v is None else v.ctypes.data)
+
+    def __del__(self):
+        try:
+            self.lib.or_destroy(self.h)
+        except Exception:
+            pass
+
+
+class RefSolver(_Base):
+    """The reference's own kernels on the host (reference parameters only)."""
+
+    def __init__(self, scene, params, threads: int = 1):
+        self.lib = ref_lib()
+        if self.lib is None:
+            raise RuntimeError("reference build unavailable (no reference checkout at build time)")
+        self.lib.ref_set_threads(threads)
+        abi = _abi()
+        desc, keep = abi.scene_desc(scene)
+        self.mask = params.stage_mask
+        self.h = self.lib.ref_create(C.byref(desc), C.c_float(params.particle_radius),
+                                     C.c_float(params.kernel_radius), C.c_float(params.cell_size),
+                                     params.grid_dim, C.c_float(params.rest_density))
+        self.n = scene.num_particles
+        self.nb = int(len(scene.rigid_ranges))
+        self._getter = self.lib.ref_get
+
+    def _update(self, nsub, dt, iters, picked, pp, pv):
+        self.lib.ref_update(self.h, nsub, C.c_float(dt), iters, self.mask, picked,
+                            None if pp is None else pp.ctypes.data, None if pv is None else pv.ctypes.data)
+
+    def __del__(self):
+        try:
+            self.lib.ref_destroy(self.h)
+        except Exception:
+            pass
+
+
+def grid_build(lib_kind: str, pos: np.ndarray, cell: float, D: int):
+    """updateGridId + stable sort + findStartEndId on the host; returns
+    (cell_ids, sorted_cell_ids, sorted_particle_ids, cell_start, cell_end)."""
+    pos = np.ascontiguousarray(pos, np.float32)
+    n = len(pos)
+    lib = oracle_lib() if lib_kind == "oracle" else ref_lib()
+    fn = lib.or_grid_build if lib_kind == "oracle" else lib.ref_grid_build
+    cid = np.zeros(n, np.int32)
+    scid = np.zeros(n, np.int32)
+    spid = np.zeros(n, np.int32)
+    cs = np.full(D ** 3, -1, np.int32)
+    ce = np.full(D ** 3, -1, np.int32)
+    fn(n, pos.ctypes.data, C.c_float(cell), D, cid.ctypes.data, scid.ctypes.data, spid.ctypes.data,
+       cs.ctypes.data, ce.ctypes.data)
+    return cid, scid, spid, cs, ce
+
+
+def neighbor_counts(lib_kind: str, sorted_pos, cell, D, h, cs, ce):
+    sorted_pos = np.ascontiguousarray(sorted_pos, np.float32)
+    n = len(sorted_pos)
+    lib = oracle_lib() if lib_kind == "oracle" else ref_lib()
+    fn = lib.or_neighbor_counts if lib_kind == "oracle" else lib.ref_neighbor_counts
+    out = np.zeros(n, np.int32)
+    fn(n, sorted_pos.ctypes.data, C.c_float(cell), D, C.c_float(h), np.ascontiguousarray(cs).ctypes.data,
+       np.ascontiguousarray(ce).ctypes.data, out.ctypes.data)
+    return out
