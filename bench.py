@@ -1,0 +1,374 @@
+"""Throughput benchmark: particle-substeps/s of the solver step on one GB300.
+
+A step is one call of update(2 substeps, dt = 1/60 s, 4 iterations) on the
+mixed-phase scene of the benchmark configuration (1,048,576 PBF fluid
+particles, a 256x256 cloth under wind, 64 rigid 8^3 cubes; 1,146,880
+particles), reference-mode parameters.  Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload mixed|fluid]
+
+Multi-GPU (torchrun, one rank per GPU): the scene does not shard, so every
+rank advances its own replica ("replicas only"); value = all ranks' particle
+substeps / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+DT = 1.0 / 60.0
+SUBSTEPS = 2
+ITERATIONS = 4
+
+# Algorithmic bytes per particle per launch (each per-particle input read
+# once, each output written once; neighbour re-reads are cache traffic).
+KERNEL_BYTES = {
+    "launch_lambda": 16 + 4 + 4 + 4,            # P, mass -> lambda, rho
+    "launch_deltap": 16 + 4 + 4 + 16 + 16,      # P, lambda, mass, Xs (planes) -> P'
+    "launch_post_a": 16 + 16 + 4 + 16 + 16,     # P, V, rho -> omega, normal
+    "launch_post_b": 16 + 16 + 16 + 16 + 16,    # P, V, Om, Nm -> V'
+    "launch_post_c": 16 + 16 + 16,              # P, V -> V'
+    "launch_particle_collision": 16 + 16 + 4 + 16,
+    "launch_reorder": 4 + 16 + 16 + 4 + 16 * 3 + 4 + 4 + 4 + 4,
+    "launch_hash_state": 16 + 16 + 4,
+}
+
+
+def load_peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def build_scene(bp, workload: str, seed: int = 0):
+    if workload == "mixed":
+        return bp.scenes.config1_mixed(seed=seed)
+    if workload == "fluid":
+        return bp.scenes.pbf_scene(128, 64, 128, spacing=0.1, seed=seed, box=(12.9, 16.0, 12.9))
+    if workload == "small":
+        return bp.scenes.pbf_scene(32, 32, 32, spacing=0.1, seed=seed, box=(4.0, 4.0, 4.0))
+    raise SystemExit(f"unknown workload {workload}")
+
+
+def workload_name(workload, n):
+    return {"mixed": "mixed-phase: 128x64x128 PBF fluid + 256^2 cloth (wind) + 64 rigid 8^3 cubes",
+            "fluid": "PBF dam break 128x64x128", "small": "PBF dam break 32^3"}[workload] + f", N={n}"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def traffic_for(kernel: str, n: int):
+    """dram bytes per launch for `kernel` from the committed ncu summary, scaled
+    to n particles (traffic grows with the particle count)."""
+    p = REPO / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    e = d.get(kernel)
+    if not e:
+        return None
+    return float(e["dram_bytes_per_launch"]) * n / float(e["particles"])
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import __graft_entry__ as entry
+
+    entry.build()
+    bp = entry.load_package()
+    scene = build_scene(bp, args.workload, seed=rank)
+    n = scene.num_particles
+    params = bp.make_params(scene)
+    stream = torch.cuda.Stream()
+    solver = bp.ParticleSolver(scene, params, stream=stream.cuda_stream)
+
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            solver.update(SUBSTEPS, DT, ITERATIONS)
+        stream.synchronize()
+        launches_per_step = solver.last_launch_count()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clocks:
+            for k in range(args.steps):
+                flush.fill_(k & 0xFF)  # evict the state from L2 between timed steps
+                starts[k].record(stream)
+                solver.update(SUBSTEPS, DT, ITERATIONS)
+                ends[k].record(stream)
+            torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    total_units = float(n) * SUBSTEPS * args.steps * world
+    value = total_units / (ms_max / 1e3)
+
+    # end to end through the C ABI with host buffers: pinned host state in,
+    # one update, positions out, every step
+    x0 = torch.from_numpy(solver.positions()).pin_memory()
+    v0 = torch.from_numpy(solver.velocities()).pin_memory()
+    xout = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+    import ctypes as C
+
+    lib = solver.lib
+    fp = C.POINTER(C.c_float)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        bp.abi.check(lib, lib.bp_solver_set_state(solver.handle, C.cast(x0.data_ptr(), fp), C.cast(v0.data_ptr(), fp),
+                                                  bp.abi.BP_ORDER_ORIGINAL))
+        solver.update(SUBSTEPS, DT, ITERATIONS)
+        bp.abi.check(lib, lib.bp_solver_copy_positions(solver.handle, C.cast(xout.data_ptr(), fp),
+                                                       bp.abi.BP_ORDER_ORIGINAL))
+    e2e_s = time.perf_counter() - t0
+    e2e_t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = total_units / float(e2e_t.item())
+
+    # per-kernel device time of real updates (CUDA events on the solver's stream)
+    prof_steps = 3
+    agg: dict[str, list] = {}
+    for _ in range(prof_steps):
+        flush.fill_(7)
+        torch.cuda.synchronize()
+        for name, (cnt, tot) in solver.profile(SUBSTEPS, DT, ITERATIONS).items():
+            a = agg.setdefault(name, [0, 0.0])
+            a[0] += cnt
+            a[1] += tot
+    top = max(agg.items(), key=lambda kv: kv[1][1])
+    top_name, (top_launches, top_ms) = top
+    avg_ms = top_ms / top_launches
+    peak, peak_kind = load_peaks()
+    bytes_per = KERNEL_BYTES.get(top_name)
+    achieved = (bytes_per * n / (avg_ms / 1e3) / 1e9) if bytes_per else None
+    traffic = traffic_for(top_name, n)
+    step_ms_total = sum(v[1] for v in agg.values()) / prof_steps
+    solver.close()
+
+    result = None
+    if rank == 0:
+        cpu = None if args.no_cpu_baseline else cpu_baseline(bp, args.workload, steps=1)
+        clk = clocks.summary()
+        result = {
+            "metric": "particle-substeps/s",
+            "value": value,
+            "unit": "particle-substeps/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic (seeded lattice scenes, no dataset)",
+            "config": {"workload": workload_name(args.workload, n), "particles": n, "substeps": SUBSTEPS,
+                       "iterations": ITERATIONS, "dt": DT, "mode": "reference", "grid": "64^3 cells, cell = h = 0.2",
+                       "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_value, "unit": "particle-substeps/s",
+                    "h2d_bytes_per_step": int(2 * n * 12), "d2h_bytes_per_step": int(n * 12)},
+            "gpu_launches": int(launches_per_step * args.steps),
+            "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "bytes_per_particle": bytes_per, "avg_launch_ms": avg_ms},
+            "stages_ms_per_step": {k: round(v[1] / prof_steps, 4) for k, v in
+                                   sorted(agg.items(), key=lambda kv: -kv[1][1])},
+            "profiled_ms_per_step": step_ms_total,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return result
+
+
+def cpu_baseline(bp, workload, steps=1):
+    """The oracle port (the reference's step restated in C, OpenMP over all
+    host cores) on a bounded sample: `steps` substeps of the same scene."""
+    import oracle
+
+    threads = os.cpu_count() or 1
+    scene = build_scene(bp, workload, seed=0)
+    params = bp.make_params(scene)
+    kind = "port"
+    o = oracle.OracleSolver(scene, params, threads=threads)
+    o.update(1, DT / SUBSTEPS, ITERATIONS)  # warm-up substep (first-touch of the grid tables)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.update(1, DT / SUBSTEPS, ITERATIONS)
+    dt = time.perf_counter() - t0
+    return {"value": scene.num_particles * steps / dt, "unit": "particle-substeps/s", "cores": threads,
+            "kind": kind, "sample": f"{steps} substep(s) of the same scene ({scene.num_particles} particles) "
+                                    f"after 1 warm-up substep, {threads} OpenMP threads"}
+
+
+def run_reference(args):
+    """Reference arm: the reference's step on the host cores (the oracle port,
+    or the reference's own kernels where they were compiled here), rank 0 only."""
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return None
+    import __graft_entry__ as entry
+
+    entry.load_package()
+    bp = sys.modules["brasspan_gb300"]
+    if not bp.abi.LIB_PATH.exists():
+        entry.build()
+    import oracle
+
+    threads = os.cpu_count() or 1
+    scene = build_scene(bp, args.workload, seed=0)
+    params = bp.make_params(scene)
+    solver = oracle.OracleSolver(scene, params, threads=threads)
+    kind = "port"
+    n = scene.num_particles
+    # each step is a bounded sample of the workload: one substep
+    for _ in range(min(args.warmup, 1)):
+        solver.update(1, DT / SUBSTEPS, ITERATIONS)
+    budget_s = 150.0
+    t0 = time.perf_counter()
+    done = 0
+    for _ in range(args.steps):
+        solver.update(1, DT / SUBSTEPS, ITERATIONS)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    value = n * done / dt
+    sample = (f"{done} timed substep(s) (one per step, capped at {budget_s:.0f} s) of the same scene "
+              f"({n} particles) after {min(args.warmup, 1)} warm-up substep, {threads} OpenMP threads")
+    result = {
+        "impl": "reference",
+        "metric": "particle-substeps/s",
+        "value": value,
+        "unit": "particle-substeps/s",
+        "n_gpus": world,
+        "steps": done,
+        "warmup": min(args.warmup, 1),
+        "ms_per_step": dt * 1e3 / max(done, 1),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded lattice scenes, no dataset)",
+        "config": {"workload": workload_name(args.workload, n), "particles": n, "substeps": SUBSTEPS,
+                   "iterations": ITERATIONS, "dt": DT, "mode": "reference"},
+        "cpu_baseline": {"value": value, "unit": "particle-substeps/s", "cores": threads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "particle-substeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(result), flush=True)
+    return result
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["mixed", "fluid", "small"], default="mixed")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

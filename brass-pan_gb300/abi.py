@@ -104,6 +104,10 @@ class BpSceneDesc(C.Structure):
     ]
 
 
+class BpStageTime(C.Structure):
+    _fields_ = [("name", C.c_char * 48), ("launches", C.c_int32), ("total_ms", C.c_float)]
+
+
 def _fptr(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
 
@@ -162,7 +166,7 @@ EXPORTS = [
     "bp_solver_set_params", "bp_solver_query_original_particle_id", "bp_solver_query_new_particle_id",
     "bp_solver_get_particle_position", "bp_solver_copy_positions", "bp_solver_copy_velocities",
     "bp_solver_set_state", "bp_solver_field", "bp_solver_copy_field", "bp_solver_pack_particle_infos",
-    "bp_solver_device_errors", "bp_solver_last_launch_count", "bp_grid_workspace_size", "bp_grid_build",
+    "bp_solver_device_errors", "bp_solver_last_launch_count", "bp_solver_profile", "bp_grid_workspace_size", "bp_grid_build",
     "bp_grid_reset", "bp_grid_neighbor_counts", "bp_last_error_string", "bp_abi_version",
 ]
 
@@ -196,6 +200,7 @@ def load(path: Path | None = None):
         "bp_solver_pack_particle_infos": (i32, [vp, vp]),
         "bp_solver_device_errors": (i32, [vp, C.POINTER(C.c_uint32)]),
         "bp_solver_last_launch_count": (i32, [vp, C.POINTER(C.c_int64)]),
+        "bp_solver_profile": (i32, [vp, i32, f32, i32, i32, C.POINTER(BpStageTime), pi]),
         "bp_grid_workspace_size": (i32, [i32, i32, C.POINTER(sz)]),
         "bp_grid_build": (i32, [vp, i32, vp, f32, i32, vp, vp, vp, vp, vp, vp, sz]),
         "bp_grid_reset": (i32, [vp, i32, vp, vp, vp]),

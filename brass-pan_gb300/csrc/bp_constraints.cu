@@ -26,11 +26,11 @@ __global__ void k_planes(SimConsts C, const float4 *__restrict__ Xs, float4 *__r
     P[i] = make_float4(p.x, p.y, p.z, p4.w);
 }
 
-void launch_planes(cudaStream_t st, const SimConsts &C, const float4 *Xs, float4 *P, int64_t *launches)
+void launch_planes(cudaStream_t st, const SimConsts &C, const float4 *Xs, float4 *P, LaunchLog *L)
 {
     if (C.n <= 0 || C.nplanes <= 0) return;
     k_planes<<<(C.n + 255) / 256, 256, 0, st>>>(C, Xs, P);
-    ++*launches;
+    L->done(__func__);
 }
 
 __global__ void k_commit(SimConsts C, const float4 *__restrict__ P, const float4 *__restrict__ Xs,
@@ -49,11 +49,11 @@ __global__ void k_commit(SimConsts C, const float4 *__restrict__ P, const float4
 }
 
 void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs, const float4 *Vs,
-                   const int *orig_s, float4 *Xc, float4 *Vc, int *orig_c, int64_t *launches)
+                   const int *orig_s, float4 *Xc, float4 *Vc, int *orig_c, LaunchLog *L)
 {
     if (C.n <= 0) return;
     k_commit<<<(C.n + 255) / 256, 256, 0, st>>>(C, P, Xs, Vs, orig_s, Xc, Vc, orig_c);
-    ++*launches;
+    L->done(__func__);
 }
 
 // Solid contacts: pairs of different phase with at least one solid, closer
@@ -113,11 +113,11 @@ __global__ void __launch_bounds__(128) k_particle_collision(SimConsts C, const f
 }
 
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
-                               const float *w, const int *off, float4 *Pout, int64_t *launches)
+                               const float *w, const int *off, float4 *Pout, LaunchLog *L)
 {
     if (C.n <= 0) return;
     k_particle_collision<<<(C.n + 127) / 128, 128, 0, st>>>(C, P, Xs, w, off, Pout);
-    ++*launches;
+    L->done(__func__);
 }
 
 // ---- distance constraints ----
@@ -161,16 +161,17 @@ __global__ void k_distance_apply(int nn_, const int *__restrict__ node_ids, cons
 }
 
 void launch_distance(cudaStream_t st, const SimConsts &C, const DistanceArgs &a, float4 *P, const float *w,
-                     const int *to_new, unsigned *err, int64_t *launches)
+                     const int *to_new, unsigned *err, LaunchLog *L)
 {
     (void)C;
     (void)err;
     if (a.num_edges <= 0) return;
     k_distance_edges<<<(a.num_edges + 255) / 256, 256, 0, st>>>(a.num_edges, a.pairs, a.params, P, w, to_new,
                                                                 a.edge_k);
+    L->done("k_distance_edges");
     k_distance_apply<<<(a.num_nodes + 255) / 256, 256, 0, st>>>(a.num_nodes, a.node_ids, a.node_ptr, a.node_inc,
                                                                 a.edge_k, w, to_new, P);
-    *launches += 2;
+    L->done("k_distance_apply");
 }
 
 // ---- wind ----
@@ -220,13 +221,14 @@ __global__ void k_wind_apply(int nn_, const int *__restrict__ node_ids, const in
 }
 
 void launch_wind(cudaStream_t st, const SimConsts &C, const WindArgs &a, float4 *P, const float4 *Vs,
-                 const float *mass, const int *to_new, int64_t *launches)
+                 const float *mass, const int *to_new, LaunchLog *L)
 {
     if (a.num_faces <= 0) return;
     k_wind_faces<<<(a.num_faces + 255) / 256, 256, 0, st>>>(C, a.num_faces, a.faces, P, Vs, to_new, a.face_move);
+    L->done("k_wind_faces");
     k_wind_apply<<<(a.num_nodes + 255) / 256, 256, 0, st>>>(a.num_nodes, a.node_ids, a.node_ptr, a.node_inc,
                                                             a.face_move, mass, to_new, P);
-    *launches += 2;
+    L->done("k_wind_apply");
 }
 
 // ---- shape matching ----
@@ -349,11 +351,11 @@ __global__ void __launch_bounds__(kSmThreads) k_shape_matching(SimConsts C, Rigi
 }
 
 void launch_shape_matching(cudaStream_t st, const SimConsts &C, const RigidArgs &a, float4 *P,
-                           const int *to_new, int64_t *launches)
+                           const int *to_new, LaunchLog *L)
 {
     if (a.num_bodies <= 0) return;
     k_shape_matching<<<a.num_bodies, kSmThreads, 0, st>>>(C, a, P, to_new);
-    ++*launches;
+    L->done(__func__);
 }
 
 __global__ void k_immovable(int k, const int *__restrict__ ids, const int *__restrict__ to_new,
@@ -367,11 +369,11 @@ __global__ void k_immovable(int k, const int *__restrict__ ids, const int *__res
 }
 
 void launch_immovable(cudaStream_t st, int k, const int *ids, const int *to_new, const float4 *Xs, float4 *P,
-                      int64_t *launches)
+                      LaunchLog *L)
 {
     if (k <= 0) return;
     k_immovable<<<(k + 255) / 256, 256, 0, st>>>(k, ids, to_new, Xs, P);
-    ++*launches;
+    L->done(__func__);
 }
 
 // setParticle (particlesolver.cuh:388-393) on the picked particle.
@@ -390,10 +392,10 @@ __global__ void k_pick(int id_orig, const int *__restrict__ to_new, float4 *pos,
 }
 
 void launch_pick(cudaStream_t st, int id_orig, const int *to_new, float4 *pos, float3 p, int set_pos, float4 *vel,
-                 float3 v, int64_t *launches)
+                 float3 v, LaunchLog *L)
 {
     k_pick<<<1, 1, 0, st>>>(id_orig, to_new, pos, p, set_pos, vel, v);
-    ++*launches;
+    L->done(__func__);
 }
 
 // {x, y, z, phase} records for a renderer.
@@ -411,6 +413,40 @@ void launch_pack_infos(cudaStream_t st, int n, const float4 *X, const float4 *V,
     k_pack_infos<<<(n + 255) / 256, 256, 0, st>>>(n, X, V, (float4 *)out);
 }
 
+__global__ void k_gather_xyz(int n, const float4 *__restrict__ src, const int *__restrict__ map,
+                             float *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v = src[i];
+    const int o = map ? map[i] : i;
+    out[3 * o] = v.x;
+    out[3 * o + 1] = v.y;
+    out[3 * o + 2] = v.z;
+}
+
+void launch_gather_xyz(cudaStream_t st, int n, const float4 *src, const int *map, float *out)
+{
+    if (n <= 0) return;
+    k_gather_xyz<<<(n + 255) / 256, 256, 0, st>>>(n, src, map, out);
+}
+
+__global__ void k_scatter_xyz(int n, const float *__restrict__ in, const int *__restrict__ map,
+                              float4 *__restrict__ dst)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = map ? map[k] : k;
+    const float4 o = dst[i];
+    dst[i] = make_float4(in[3 * k], in[3 * k + 1], in[3 * k + 2], o.w);
+}
+
+void launch_scatter_xyz(cudaStream_t st, int n, const float *in, const int *map, float4 *dst)
+{
+    if (n <= 0) return;
+    k_scatter_xyz<<<(n + 255) / 256, 256, 0, st>>>(n, in, map, dst);
+}
+
 // Device error word: NaN / Inf positions.
 __global__ void k_check_finite(int n, const float4 *__restrict__ X, unsigned *err)
 {
@@ -421,11 +457,11 @@ __global__ void k_check_finite(int n, const float4 *__restrict__ X, unsigned *er
     if (__any_sync(__activemask(), bad) && bad) atomicOr(err, BP_DEVERR_NONFINITE);
 }
 
-void launch_check_finite(cudaStream_t st, int n, const float4 *X, unsigned *err, int64_t *launches)
+void launch_check_finite(cudaStream_t st, int n, const float4 *X, unsigned *err, LaunchLog *L)
 {
     if (n <= 0) return;
     k_check_finite<<<(n + 255) / 256, 256, 0, st>>>(n, X, err);
-    ++*launches;
+    L->done(__func__);
 }
 
 }  // namespace bp

@@ -75,11 +75,11 @@ __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const floa
 }
 
 void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const float *mass, const int *off,
-                   float *lam, float *rho, int64_t *launches)
+                   float *lam, float *rho, LaunchLog *L)
 {
     if (C.n <= 0) return;
     k_lambda<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, mass, off, lam, rho);
-    ++*launches;
+    L->done(__func__);
 }
 
 // Position correction.  Reference mode: the pair (a, b), a < b, contributes
@@ -129,11 +129,11 @@ __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs 
     a.Pout[k] = make_float4(p.x, p.y, p.z, pk4.w);
 }
 
-void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, int64_t *launches)
+void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, LaunchLog *L)
 {
     if (C.n <= 0) return;
     k_deltap<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, a);
-    ++*launches;
+    L->done(__func__);
 }
 
 // Pass A: vorticity omega_i (fluidOmega) and Akinci normal n_i (fluidNormal)
@@ -249,25 +249,25 @@ __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const floa
 }
 
 void launch_post_a(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float *rho,
-                   const int *off, float4 *Om, float4 *Nm, int64_t *launches)
+                   const int *off, float4 *Om, float4 *Nm, LaunchLog *L)
 {
     if (C.n <= 0) return;
     k_post_a<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, V, rho, off, Om, Nm);
-    ++*launches;
+    L->done(__func__);
 }
 void launch_post_b(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float4 *Om,
-                   const float4 *Nm, const int *off, float4 *Vout, int64_t *launches)
+                   const float4 *Nm, const int *off, float4 *Vout, LaunchLog *L)
 {
     if (C.n <= 0) return;
     k_post_b<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, V, Om, Nm, off, Vout);
-    ++*launches;
+    L->done(__func__);
 }
 void launch_post_c(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
-                   float4 *Vout, int64_t *launches)
+                   float4 *Vout, LaunchLog *L)
 {
     if (C.n <= 0) return;
     k_post_c<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, V, off, Vout);
-    ++*launches;
+    L->done(__func__);
 }
 
 // Neighbour counts on the solver's grid: j in the 27 cells with r^2 <= h^2 (self included).
@@ -285,11 +285,11 @@ __global__ void k_neighbor_counts(SimConsts C, const float4 *__restrict__ P, con
 }
 
 void launch_neighbor_counts(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, int *counts,
-                            int64_t *launches)
+                            LaunchLog *L)
 {
     if (C.n <= 0) return;
     k_neighbor_counts<<<(C.n + 127) / 128, 128, 0, st>>>(C, P, off, counts);
-    ++*launches;
+    L->done(__func__);
 }
 
 // Same count on caller buffers in the reference's start/end format.

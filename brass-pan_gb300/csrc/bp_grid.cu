@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(
 }
 
 void radix_sort_pairs(cudaStream_t st, int n, int D, const int *keys_in, const int *vals_in, int *keys_out,
-                      int *vals_out, const SortScratch &s, bool hist_ready, int64_t *launches)
+                      int *vals_out, const SortScratch &s, bool hist_ready, LaunchLog *L)
 {
     if (n <= 0) return;
     const int tiles = sort_tiles(n);
@@ -197,12 +197,13 @@ void radix_sort_pairs(cudaStream_t st, int n, int D, const int *keys_in, const i
         int *vdst = (p == passes - 1) ? vals_out : s.vals_alt[p & 1];
         if (!(p == 0 && hist_ready)) {
             k_radix_upsweep<<<tiles, kSortThreads, 0, st>>>(ksrc, n, shift, s.hist, tiles);
-            ++*launches;
+            L->done("k_radix_upsweep");
         }
         k_radix_scan<<<kRadixBins, 256, 0, st>>>(s.hist, tiles, s.digit_total);
+        L->done("k_radix_scan");
         k_radix_downsweep<<<tiles, kSortThreads, 0, st>>>(ksrc, vsrc, n, shift, s.hist, s.digit_total, tiles,
                                                           kdst, vdst);
-        *launches += 2;
+        L->done("k_radix_downsweep");
         ksrc = kdst;
         vsrc = vdst;
     }
@@ -268,21 +269,21 @@ __global__ void __launch_bounds__(kSortThreads) k_hash_state(SimConsts C, const 
 }
 
 void launch_hash_f3(cudaStream_t st, int n, const float *pos3, float cell, int D, int *keys, int *hist,
-                    int64_t *launches)
+                    LaunchLog *L)
 {
     if (n <= 0) return;
     const int tiles = sort_tiles(n);
     k_hash_f3<<<tiles, kSortThreads, 0, st>>>(n, pos3, cell, D, keys, hist, tiles);
-    ++*launches;
+    L->done(__func__);
 }
 
 void launch_hash_state(cudaStream_t st, const SimConsts &C, const float4 *X, const float4 *V, int *keys,
-                       int *hist, int64_t *launches)
+                       int *hist, LaunchLog *L)
 {
     if (C.n <= 0) return;
     const int tiles = sort_tiles(C.n);
     k_hash_state<<<tiles, kSortThreads, 0, st>>>(C, X, V, keys, hist, tiles);
-    ++*launches;
+    L->done(__func__);
 }
 
 // ------------------------------------------------------------------------
@@ -326,24 +327,24 @@ __global__ void k_cell_offsets(int n, int ncells, const int *__restrict__ sorted
     off[c] = lo;
 }
 
-void launch_find_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end, int64_t *launches)
+void launch_find_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end, LaunchLog *L)
 {
     if (n <= 0) return;
     k_find_start_end<<<(n + 255) / 256, 256, 0, st>>>(n, sorted, start, end);
-    ++*launches;
+    L->done(__func__);
 }
 
-void launch_reset_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end, int64_t *launches)
+void launch_reset_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end, LaunchLog *L)
 {
     if (n <= 0) return;
     k_reset_start_end<<<(n + 255) / 256, 256, 0, st>>>(n, sorted, start, end);
-    ++*launches;
+    L->done(__func__);
 }
 
-void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, int64_t *launches)
+void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, LaunchLog *L)
 {
     k_cell_offsets<<<(ncells + 1 + 255) / 256, 256, 0, st>>>(n, ncells, sorted, off);
-    ++*launches;
+    L->done(__func__);
 }
 
 // ------------------------------------------------------------------------
@@ -381,11 +382,11 @@ __global__ void __launch_bounds__(256) k_reorder(SimConsts C, ReorderArgs a)
     a.to_new[id] = i;
 }
 
-void launch_reorder(cudaStream_t st, const SimConsts &C, const ReorderArgs &a, int64_t *launches)
+void launch_reorder(cudaStream_t st, const SimConsts &C, const ReorderArgs &a, LaunchLog *L)
 {
     if (C.n <= 0) return;
     k_reorder<<<(C.n + 255) / 256, 256, 0, st>>>(C, a);
-    ++*launches;
+    L->done(__func__);
 }
 
 }  // namespace bp

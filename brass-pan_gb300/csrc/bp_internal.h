@@ -9,6 +9,26 @@
 
 namespace bp {
 
+// Counts kernel launches and, when `events` is set (bp_solver_profile),
+// records a CUDA event after each one so per-stage device time can be read
+// back without a profiler.
+struct LaunchLog {
+    int64_t count = 0;
+    cudaStream_t stream = nullptr;
+    int max_events = 0;
+    int num_events = 0;
+    cudaEvent_t *events = nullptr;
+    const char **names = nullptr;
+    void done(const char *name)
+    {
+        ++count;
+        if (events && num_events < max_events) {
+            cudaEventRecord(events[num_events], stream);
+            names[num_events++] = name;
+        }
+    }
+};
+
 // ---- stable LSD radix sort of (cell key, particle index) pairs -------------
 // 9-bit digits; a tile of 4096 keys per CTA (512 threads x 8 keys).
 constexpr int kRadixBits = 9;
@@ -39,17 +59,17 @@ void sort_scratch_carve(void *base, int n, int D, SortScratch *s);
 // keys_in: cell keys (pass 0 histogram already in s.hist when hist_ready);
 // vals_in == nullptr means the identity permutation.
 void radix_sort_pairs(cudaStream_t st, int n, int D, const int *keys_in, const int *vals_in, int *keys_out,
-                      int *vals_out, const SortScratch &s, bool hist_ready, int64_t *launches);
+                      int *vals_out, const SortScratch &s, bool hist_ready, LaunchLog *L);
 
 // ---- grid kernels launched by the solver and the stand-alone API ----
 void launch_hash_f3(cudaStream_t st, int n, const float *pos3, float cell, int D, int *keys, int *hist,
-                    int64_t *launches);
+                    LaunchLog *L);
 void launch_hash_state(cudaStream_t st, const SimConsts &C, const float4 *X, const float4 *V, int *keys,
-                       int *hist, int64_t *launches);
-void launch_find_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end, int64_t *launches);
+                       int *hist, LaunchLog *L);
+void launch_find_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end, LaunchLog *L);
 void launch_reset_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end,
-                            int64_t *launches);
-void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, int64_t *launches);
+                            LaunchLog *L);
+void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, LaunchLog *L);
 
 struct ReorderArgs {
     const int *order;      // sorted position -> old index
@@ -62,11 +82,11 @@ struct ReorderArgs {
     int stabilize;         // run planeStabilize twice
     int collide;           // also run iteration 0's plane collision
 };
-void launch_reorder(cudaStream_t st, const SimConsts &C, const ReorderArgs &a, int64_t *launches);
+void launch_reorder(cudaStream_t st, const SimConsts &C, const ReorderArgs &a, LaunchLog *L);
 
 // ---- fluid kernels ----
 void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const float *mass, const int *off,
-                   float *lam, float *rho, int64_t *launches);
+                   float *lam, float *rho, LaunchLog *L);
 struct DeltaArgs {
     const float4 *P;
     const float *mass, *lam;
@@ -79,24 +99,24 @@ struct DeltaArgs {
     const int *orig_s;
     int *orig_c;
 };
-void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, int64_t *launches);
+void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, LaunchLog *L);
 void launch_post_a(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float *rho,
-                   const int *off, float4 *Om, float4 *Nm, int64_t *launches);
+                   const int *off, float4 *Om, float4 *Nm, LaunchLog *L);
 void launch_post_b(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float4 *Om,
-                   const float4 *Nm, const int *off, float4 *Vout, int64_t *launches);
+                   const float4 *Nm, const int *off, float4 *Vout, LaunchLog *L);
 void launch_post_c(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
-                   float4 *Vout, int64_t *launches);
+                   float4 *Vout, LaunchLog *L);
 void launch_neighbor_counts(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, int *counts,
-                            int64_t *launches);
+                            LaunchLog *L);
 void launch_neighbor_counts_f3(cudaStream_t st, int n, const float *pos3, float cell, int D, float h,
                                const int *start, const int *end, int *counts);
 
 // ---- per-particle and constraint kernels ----
-void launch_planes(cudaStream_t st, const SimConsts &C, const float4 *Xs, float4 *P, int64_t *launches);
+void launch_planes(cudaStream_t st, const SimConsts &C, const float4 *Xs, float4 *P, LaunchLog *L);
 void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs, const float4 *Vs,
-                   const int *orig_s, float4 *Xc, float4 *Vc, int *orig_c, int64_t *launches);
+                   const int *orig_s, float4 *Xc, float4 *Vc, int *orig_c, LaunchLog *L);
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
-                               const float *w, const int *off, float4 *Pout, int64_t *launches);
+                               const float *w, const int *off, float4 *Pout, LaunchLog *L);
 struct DistanceArgs {
     int num_edges;
     const int2 *pairs;       // original ids
@@ -108,7 +128,7 @@ struct DistanceArgs {
     float4 *edge_k;          // per-edge correction vector
 };
 void launch_distance(cudaStream_t st, const SimConsts &C, const DistanceArgs &a, float4 *P, const float *w,
-                     const int *to_new, unsigned *err, int64_t *launches);
+                     const int *to_new, unsigned *err, LaunchLog *L);
 struct WindArgs {
     int num_faces;
     const int *faces;        // [F][3] original ids
@@ -119,7 +139,7 @@ struct WindArgs {
     float4 *face_move;
 };
 void launch_wind(cudaStream_t st, const SimConsts &C, const WindArgs &a, float4 *P, const float4 *Vs,
-                 const float *mass, const int *to_new, int64_t *launches);
+                 const float *mass, const int *to_new, LaunchLog *L);
 struct RigidArgs {
     int num_bodies;
     const int2 *ranges;      // original ids
@@ -127,12 +147,16 @@ struct RigidArgs {
     float4 *rot, *cm;
 };
 void launch_shape_matching(cudaStream_t st, const SimConsts &C, const RigidArgs &a, float4 *P,
-                           const int *to_new, int64_t *launches);
+                           const int *to_new, LaunchLog *L);
 void launch_immovable(cudaStream_t st, int k, const int *ids, const int *to_new, const float4 *Xs, float4 *P,
-                      int64_t *launches);
+                      LaunchLog *L);
 void launch_pick(cudaStream_t st, int id_orig, const int *to_new, float4 *pos, float3 p, int set_pos, float4 *vel,
-                 float3 v, int64_t *launches);
+                 float3 v, LaunchLog *L);
 void launch_pack_infos(cudaStream_t st, int n, const float4 *X, const float4 *V, void *out);
-void launch_check_finite(cudaStream_t st, int n, const float4 *X, unsigned *err, int64_t *launches);
+// out[3*o..] = src[i].xyz with o = map ? map[i] : i (sorted -> original when map = orig ids)
+void launch_gather_xyz(cudaStream_t st, int n, const float4 *src, const int *map, float *out);
+// dst[i].xyz = in[3*k..] with i = map ? map[k] : k, w kept (original -> sorted when map = to_new)
+void launch_scatter_xyz(cudaStream_t st, int n, const float *in, const int *map, float4 *dst);
+void launch_check_finite(cudaStream_t st, int n, const float4 *X, unsigned *err, LaunchLog *L);
 
 }  // namespace bp

@@ -55,6 +55,7 @@ struct bp_solver {
     int *orig_c = nullptr, *orig_s = nullptr, *to_new = nullptr, *group = nullptr;
     int *keys = nullptr, *sorted_keys = nullptr, *order = nullptr, *off = nullptr;
     float *mass = nullptr, *lam = nullptr, *rho = nullptr, *w = nullptr;
+    float *staging = nullptr;  // 2 x N x 3 floats for host copies
     unsigned *err = nullptr;
     SortScratch sort{};
 
@@ -316,7 +317,8 @@ extern "C" bp_status bp_solver_create(const bp_scene_desc *sc, const bp_params *
         (st = s->alloc(&s->orig_s, N)) || (st = s->alloc(&s->to_new, N)) || (st = s->alloc(&s->group, N)) ||
         (st = s->alloc(&s->keys, N)) || (st = s->alloc(&s->sorted_keys, N)) || (st = s->alloc(&s->order, N)) ||
         (st = s->alloc(&s->off, ncells + 1)) || (st = s->alloc(&s->mass, N)) || (st = s->alloc(&s->lam, N)) ||
-        (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)))
+        (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)) ||
+        (st = s->alloc(&s->staging, 6 * N)))
         return bail(st);
     {
         char *scratch = nullptr;
@@ -449,7 +451,7 @@ extern "C" bp_status bp_solver_set_params(bp_solver *s, const bp_params *prm)
 
 // Enqueues one substep; returns the number of kernels launched.
 static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int picked, float3 ppos,
-                            int64_t *L)
+                            LaunchLog *L)
 {
     const cudaStream_t st = s->stream;
     const int mask = s->prm.stage_mask;
@@ -546,7 +548,7 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
 }
 
 static bp_status enqueue_update(bp_solver *s, int nsub, float dt, int iterations, int picked, float3 ppos,
-                                float3 pvel, int64_t *L)
+                                float3 pvel, LaunchLog *L)
 {
     const float sdt = dt / (float)nsub;
     const SimConsts C = make_consts(s, sdt);
@@ -567,11 +569,12 @@ extern "C" bp_status bp_solver_update(bp_solver *s, int32_t nsub, float dt, int3
     if (picked >= 0 && !ppos) return fail(BP_ERR_INVALID_ARGUMENT, "picked_position is NULL");
     const float3 pp = ppos ? make_float3(ppos[0], ppos[1], ppos[2]) : make_float3(0.f, 0.f, 0.f);
     const float3 pv = pvel ? make_float3(pvel[0], pvel[1], pvel[2]) : make_float3(0.f, 0.f, 0.f);
-    int64_t L = 0;
+    LaunchLog L;
+    L.stream = s->stream;
     if (picked >= 0) {
         enqueue_update(s, nsub, dt, iterations, picked, pp, pv, &L);
         BP_CUDA(cudaGetLastError());
-        s->last_launches = L;
+        s->last_launches = L.count;
         return BP_OK;
     }
     const bool hit = s->exec && s->g_sub == nsub && s->g_iter == iterations && s->g_dt == dt &&
@@ -593,10 +596,57 @@ extern "C" bp_status bp_solver_update(bp_solver *s, int32_t nsub, float dt, int3
         s->g_iter = iterations;
         s->g_dt = dt;
         s->g_params_version = s->params_version;
-        s->graph_launches = L;
+        s->graph_launches = L.count;
     }
     BP_CUDA(cudaGraphLaunch(s->exec, s->stream));
     s->last_launches = s->graph_launches;
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_profile(bp_solver *s, int32_t nsub, float dt, int32_t iterations,
+                                       int32_t capacity, bp_stage_time *out, int32_t *count)
+{
+    if (!s || !count || capacity < 0 || (capacity > 0 && !out)) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (nsub <= 0 || !(dt > 0.f) || iterations < 0) return fail(BP_ERR_INVALID_ARGUMENT, "bad step arguments");
+    *count = 0;
+    if (s->n <= 0) return BP_OK;
+    const int maxev = 4096;
+    std::vector<cudaEvent_t> ev(maxev + 1);
+    std::vector<const char *> names(maxev);
+    for (auto &e : ev) BP_CUDA(cudaEventCreate(&e));
+    LaunchLog L;
+    L.stream = s->stream;
+    L.events = ev.data() + 1;
+    L.names = names.data();
+    L.max_events = maxev;
+    BP_CUDA(cudaEventRecord(ev[0], s->stream));
+    enqueue_update(s, nsub, dt, iterations, -1, make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), &L);
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    std::vector<bp_stage_time> agg;
+    for (int k = 0; k < L.num_events; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+        bool found = false;
+        for (auto &a : agg)
+            if (!strcmp(a.name, names[k])) {
+                a.total_ms += ms;
+                a.launches += 1;
+                found = true;
+            }
+        if (!found) {
+            bp_stage_time t;
+            memset(&t, 0, sizeof(t));
+            strncpy(t.name, names[k], sizeof(t.name) - 1);
+            t.total_ms = ms;
+            t.launches = 1;
+            agg.push_back(t);
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    const int m = (int)agg.size() < capacity ? (int)agg.size() : capacity;
+    for (int k = 0; k < m; ++k) out[k] = agg[k];
+    *count = (int)agg.size();
+    s->last_launches = L.count;
     return BP_OK;
 }
 
@@ -639,26 +689,18 @@ extern "C" bp_status bp_solver_get_particle_position(bp_solver *s, int32_t idx, 
     return BP_OK;
 }
 
+// Host <-> device state copies move 12 bytes per particle and array: the
+// (sorted <-> original) permutation and the float4 packing happen on the GPU
+// through the solver's staging buffer.
 static bp_status copy_xyz(bp_solver *s, const float4 *src, float *dst, int order)
 {
     if (!s || !dst) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
     if (order != BP_ORDER_SORTED && order != BP_ORDER_ORIGINAL) return fail(BP_ERR_INVALID_ARGUMENT, "bad order");
     const int n = s->n;
     if (n == 0) return BP_OK;
-    std::vector<float4> tmp(n);
-    std::vector<int> ids;
-    BP_CUDA(cudaMemcpyAsync(tmp.data(), src, n * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
-    if (order == BP_ORDER_ORIGINAL) {
-        ids.resize(n);
-        BP_CUDA(cudaMemcpyAsync(ids.data(), s->orig_c, n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-    }
+    launch_gather_xyz(s->stream, n, src, order == BP_ORDER_ORIGINAL ? s->orig_c : nullptr, s->staging);
+    BP_CUDA(cudaMemcpyAsync(dst, s->staging, (size_t)n * 12, cudaMemcpyDeviceToHost, s->stream));
     BP_CUDA(cudaStreamSynchronize(s->stream));
-    for (int i = 0; i < n; ++i) {
-        const int o = order == BP_ORDER_ORIGINAL ? ids[i] : i;
-        dst[3 * o] = tmp[i].x;
-        dst[3 * o + 1] = tmp[i].y;
-        dst[3 * o + 2] = tmp[i].z;
-    }
     return BP_OK;
 }
 
@@ -678,19 +720,15 @@ extern "C" bp_status bp_solver_set_state(bp_solver *s, const float *hx, const fl
     if (order != BP_ORDER_SORTED && order != BP_ORDER_ORIGINAL) return fail(BP_ERR_INVALID_ARGUMENT, "bad order");
     const int n = s->n;
     if (n == 0) return BP_OK;
-    std::vector<float4> X(n), V(n);
-    std::vector<int> ids(n);
-    BP_CUDA(cudaMemcpyAsync(X.data(), s->Xc, n * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
-    BP_CUDA(cudaMemcpyAsync(V.data(), s->Vc, n * sizeof(float4), cudaMemcpyDeviceToHost, s->stream));
-    BP_CUDA(cudaMemcpyAsync(ids.data(), s->orig_c, n * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-    BP_CUDA(cudaStreamSynchronize(s->stream));
-    for (int i = 0; i < n; ++i) {
-        const int o = order == BP_ORDER_ORIGINAL ? ids[i] : i;
-        if (hx) X[i] = make_float4(hx[3 * o], hx[3 * o + 1], hx[3 * o + 2], X[i].w);
-        if (hv) V[i] = make_float4(hv[3 * o], hv[3 * o + 1], hv[3 * o + 2], V[i].w);
+    const int *map = order == BP_ORDER_ORIGINAL ? s->to_new : nullptr;
+    if (hx) {
+        BP_CUDA(cudaMemcpyAsync(s->staging, hx, (size_t)n * 12, cudaMemcpyHostToDevice, s->stream));
+        launch_scatter_xyz(s->stream, n, s->staging, map, s->Xc);
     }
-    BP_CUDA(cudaMemcpyAsync(s->Xc, X.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
-    BP_CUDA(cudaMemcpyAsync(s->Vc, V.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
+    if (hv) {
+        BP_CUDA(cudaMemcpyAsync(s->staging + 3 * (size_t)n, hv, (size_t)n * 12, cudaMemcpyHostToDevice, s->stream));
+        launch_scatter_xyz(s->stream, n, s->staging + 3 * (size_t)n, map, s->Vc);
+    }
     BP_CUDA(cudaStreamSynchronize(s->stream));
     return BP_OK;
 }
@@ -779,7 +817,8 @@ extern "C" bp_status bp_grid_build(void *stream, int32_t n, const float *pos, fl
     cudaStream_t st = (cudaStream_t)stream;
     SortScratch sc;
     sort_scratch_carve(ws, n, D, &sc);
-    int64_t L = 0;
+    LaunchLog L;
+    L.stream = st;
     launch_hash_f3(st, n, pos, cell, D, cell_ids, sc.hist, &L);
     radix_sort_pairs(st, n, D, cell_ids, nullptr, sorted_cell_ids, sorted_ids, sc, true, &L);
     launch_find_start_end(st, n, sorted_cell_ids, start, end, &L);
@@ -792,7 +831,8 @@ extern "C" bp_status bp_grid_reset(void *stream, int32_t n, const int32_t *sorte
     if (n < 0) return fail(BP_ERR_INVALID_ARGUMENT, "n < 0");
     if (n == 0) return BP_OK;
     if (!sorted || !start || !end) return fail(BP_ERR_INVALID_ARGUMENT, "NULL buffer");
-    int64_t L = 0;
+    LaunchLog L;
+    L.stream = (cudaStream_t)stream;
     launch_reset_start_end((cudaStream_t)stream, n, sorted, start, end, &L);
     BP_CUDA(cudaGetLastError());
     return BP_OK;

@@ -133,6 +133,15 @@ class ParticleSolver:
         abi.check(self.lib, self.lib.bp_solver_last_launch_count(self.handle, C.byref(out)))
         return out.value
 
+    def profile(self, num_substeps: int, dt: float, iterations: int) -> dict[str, tuple[int, float]]:
+        """One real update with a CUDA event after every kernel: {kernel: (launches, total ms)}."""
+        cap = 64
+        buf = (abi.BpStageTime * cap)()
+        count = C.c_int32()
+        abi.check(self.lib, self.lib.bp_solver_profile(self.handle, num_substeps, C.c_float(dt), iterations, cap,
+                                                       buf, C.byref(count)))
+        return {buf[k].name.decode(): (buf[k].launches, buf[k].total_ms) for k in range(min(cap, count.value))}
+
     def pack_particle_infos(self, device_ptr: int):
         abi.check(self.lib, self.lib.bp_solver_pack_particle_infos(self.handle, C.c_void_p(device_ptr)))
 

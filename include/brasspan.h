@@ -211,6 +211,19 @@ bp_status bp_solver_device_errors(bp_solver *s, uint32_t *out_bits);
 /* Number of kernels the last bp_solver_update enqueued. */
 bp_status bp_solver_last_launch_count(bp_solver *s, int64_t *out);
 
+/* Per-stage device time of one update (no graph; a CUDA event after every
+ * kernel on the solver's stream).  Replaces the reference's only timing, the
+ * ms/frame in the window title (main.cu:418-428).  Writes up to `capacity`
+ * entries, one per kernel name, and the number of distinct names to *count.
+ * The update is real: it advances the state like bp_solver_update. */
+typedef struct bp_stage_time {
+    char name[48];
+    int32_t launches;
+    float total_ms;
+} bp_stage_time;
+bp_status bp_solver_profile(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
+                            int32_t capacity, bp_stage_time *out, int32_t *count);
+
 /* ---- Stand-alone hash grid on caller-owned device buffers ---------------
  * Replaces updateGrid() (particlesolver.cuh:712-765): updateGridId
  * (kernel/grid.cuh:30-47), the CUB stable radix sort (particlesolver.cuh:721-738)

@@ -77,6 +77,7 @@ def oracle_lib():
         lib.or_update.argtypes = [vp, i32, f32, i32, i32, vp, vp]
         lib.or_get.argtypes = [vp, i32, vp]
         lib.or_set_state.argtypes = [vp, vp, vp]
+        lib.or_set_full_state.argtypes = [vp, vp, vp, vp, vp]
         lib.or_set_threads.argtypes = [i32]
         lib.or_grid_build.argtypes = [i32, vp, f32, i32, vp, vp, vp, vp, vp]
         lib.or_neighbor_counts.argtypes = [i32, vp, f32, i32, f32, vp, vp, vp]
@@ -170,6 +171,15 @@ class OracleSolver(_Base):
     def _update(self, nsub, dt, iters, picked, pp, pv):
         self.lib.or_update(self.h, nsub, C.c_float(dt), iters, picked,
                            None if pp is None else pp.ctypes.data, None if pv is None else pv.ctypes.data)
+
+    def adopt(self, x_sorted, v_sorted, to_orig, rotations=None):
+        """Takes over another solver's state, arrangement included."""
+        x = np.ascontiguousarray(x_sorted, np.float32)
+        v = np.ascontiguousarray(v_sorted, np.float32)
+        t = np.ascontiguousarray(to_orig, np.int32)
+        r = None if rotations is None else np.ascontiguousarray(rotations, np.float32)
+        self.lib.or_set_full_state(self.h, x.ctypes.data, v.ctypes.data, t.ctypes.data,
+                                   None if r is None else r.ctypes.data)
 
     def set_state(self, x_sorted=None, v_sorted=None):
         x = None if x_sorted is None else np.ascontiguousarray(x_sorted, np.float32)

@@ -306,6 +306,44 @@ int or_set_state(or_solver *s, const float *x, const float *v)
     return 0;
 }
 
+/* Adopts a complete state in another solver's sorted arrangement: positions
+ * and velocities [N][3] in that order, its sorted->original map, and
+ * optionally the rigid-body quaternions [B][4]; per-particle constants follow
+ * the new arrangement.  Used to restart both solvers from identical inputs. */
+int or_set_full_state(or_solver *s, const float *x, const float *v, const int *to_orig, const float *rot)
+{
+    const int n = s->n;
+    float *m0 = (float *)malloc(sizeof(float) * (size_t)(n > 0 ? n : 1));
+    int *ph0 = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int *g0 = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int i = 0; i < n; ++i) {
+        m0[s->to_orig[i]] = s->m[i];
+        ph0[s->to_orig[i]] = s->phase[i];
+        g0[s->to_orig[i]] = s->group[i];
+    }
+    for (int i = 0; i < n; ++i) {
+        const int o = to_orig[i];
+        s->to_orig[i] = o;
+        s->to_new[o] = i;
+        s->m[i] = m0[o];
+        s->phase[i] = ph0[o];
+        s->group[i] = g0[o];
+        s->x[i] = v3(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+        s->v[i] = v3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+    }
+    if (rot)
+        for (int b = 0; b < s->nb; ++b) {
+            s->rot[b].x = rot[4 * b];
+            s->rot[b].y = rot[4 * b + 1];
+            s->rot[b].z = rot[4 * b + 2];
+            s->rot[b].w = rot[4 * b + 3];
+        }
+    free(m0);
+    free(ph0);
+    free(g0);
+    return 0;
+}
+
 #define SWAP(a, b) do { void *t_ = (void *)(a); (a) = (b); (b) = t_; } while (0)
 
 /* updateGrid (PS:712-765): hash, stable sort, start/end, 7-array reorder */

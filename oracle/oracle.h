@@ -42,6 +42,7 @@ int or_update(or_solver *s, int num_substeps, float dt, int iterations, int pick
  * 11 omega, 12 normal (float [N][3]); 13 mass (float [N]); 14 phase (int [N]). */
 int or_get(or_solver *s, int field, void *out);
 int or_set_state(or_solver *s, const float *x, const float *v); /* sorted order */
+int or_set_full_state(or_solver *s, const float *x, const float *v, const int *to_orig, const float *rot);
 
 /* Stand-alone grid on host arrays (kernel/grid.cuh:30-99 + stable sort).
  * cell_start/cell_end: D^3 entries, -1 on entry; occupied cells are written. */

@@ -1,0 +1,270 @@
+"""The solver step on the GPU through the C ABI against the oracle.
+
+Parity bar: from identical inputs, one substep of the GPU solver and of the
+oracle (the reference's step restated, pinned bit-exact to the reference's
+own kernels) agree to max |x_gpu - x_oracle| <= 1e-4 * h, velocities to
+1e-4 * h / dt; the neighbour search inside the step (cell keys, stable sorted
+order) is identical.  The GPU sums pair terms in a different order than the
+reference's atomics, so fp32 rounding differs; nothing else may."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, fluid_scene, small_mixed_scene
+
+import sys
+
+sys.path.insert(0, str(GOLDEN))
+from make_golden import scene_from_npz  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+DT = 1.0 / 60.0
+
+
+def gpu_state(bp, s):
+    abi = bp.abi
+    X = s.field(abi.BP_FIELD_POSITIONS)
+    V = s.field(abi.BP_FIELD_VELOCITIES)
+    to_orig = s.field(abi.BP_FIELD_MAP_TO_ORIGINAL)
+    rot = s.field(abi.BP_FIELD_RIGID_ROTATIONS) if len(s.scene.rigid_ranges) else None
+    return X[:, :3].copy(), V[:, :3].copy(), to_orig, rot
+
+
+def lockstep(bp, oracle, scene, params, substeps=6, iterations=4, sub_per_call=1):
+    """Runs GPU and oracle substep by substep, re-synchronising the oracle on
+    the GPU state before each one; returns per-substep max errors."""
+    g = bp.ParticleSolver(scene, params)
+    o = oracle.OracleSolver(scene, params)
+    h = scene.kernel_radius
+    sdt = DT / 2
+    errs = []
+    for k in range(substeps):
+        x, v, to_orig, rot = gpu_state(bp, g)
+        o.adopt(x, v, to_orig, rot)
+        g.update(sub_per_call, sdt * sub_per_call, iterations)
+        o.update(sub_per_call, sdt * sub_per_call, iterations)
+        ex = np.abs(g.positions() - o.positions()).max()
+        ev = np.abs(g.velocities() - o.velocities()).max()
+        keys_equal = np.array_equal(g.field(bp.abi.BP_FIELD_SORTED_CELL_IDS), o.get(oracle.F_SORTED_CELL))
+        order_equal = np.array_equal(g.field(bp.abi.BP_FIELD_MAP_TO_ORIGINAL), o.get(oracle.F_TO_ORIG))
+        errs.append((ex, ev, keys_equal, order_equal))
+    g.close()
+    return errs, h, sdt
+
+
+def assert_parity(errs, h, sdt):
+    for k, (ex, ev, keys_equal, order_equal) in enumerate(errs):
+        assert keys_equal and order_equal, f"substep {k}: neighbour search differs"
+        assert ex <= 1e-4 * h, f"substep {k}: max position error {ex:.3e} > {1e-4 * h:.3e}"
+        assert ev <= 1e-4 * h / sdt, f"substep {k}: max velocity error {ev:.3e}"
+
+
+def test_fluid_substep_parity(bp, gpu, oracle):
+    scene = fluid_scene(bp, (14, 14, 14), seed=1, grid_dim=32)
+    errs, h, sdt = lockstep(bp, oracle, scene, bp.make_params(scene), substeps=8)
+    assert_parity(errs, h, sdt)
+
+
+def test_mixed_substep_parity(bp, gpu, oracle):
+    scene = small_mixed_scene(bp, seed=2)
+    errs, h, sdt = lockstep(bp, oracle, scene, bp.make_params(scene), substeps=8)
+    assert_parity(errs, h, sdt)
+
+
+@pytest.mark.parametrize("iterations", [1, 2, 3])
+def test_mixed_parity_iteration_counts(bp, gpu, oracle, iterations):
+    scene = small_mixed_scene(bp, seed=3)
+    errs, h, sdt = lockstep(bp, oracle, scene, bp.make_params(scene), substeps=3, iterations=iterations)
+    assert_parity(errs, h, sdt)
+
+
+@pytest.mark.parametrize("mask_name", ["as_shipped", "no_akinci", "fluid_only", "constraints_only"])
+def test_stage_subsets_parity(bp, gpu, oracle, mask_name):
+    a = bp.abi
+    masks = {
+        "as_shipped": a.BP_STAGE_REFERENCE_AS_SHIPPED | a.BP_STAGE_FLUID,
+        "no_akinci": a.BP_STAGE_ALL & ~a.BP_STAGE_AKINCI,   # s_corr on, no C clamp
+        "fluid_only": a.BP_STAGE_PLANES | a.BP_STAGE_FLUID,
+        "constraints_only": a.BP_STAGE_PLANES | a.BP_STAGE_DISTANCE | a.BP_STAGE_WIND | a.BP_STAGE_SHAPE_MATCHING
+        | a.BP_STAGE_IMMOVABLE | a.BP_STAGE_PARTICLE_COLLISION,
+    }
+    scene = small_mixed_scene(bp, seed=4)
+    params = bp.make_params(scene, stage_mask=masks[mask_name])
+    errs, h, sdt = lockstep(bp, oracle, scene, params, substeps=4)
+    assert_parity(errs, h, sdt)
+
+
+def test_textbook_mode_parity(bp, gpu, oracle):
+    scene = fluid_scene(bp, (12, 12, 12), seed=5, grid_dim=32)
+    params = bp.make_params(scene, mode=bp.abi.BP_MODE_TEXTBOOK, relaxation=600.0, scorr_k=0.1, scorr_dq=0.2,
+                            xsph_c=0.01)
+    errs, h, sdt = lockstep(bp, oracle, scene, params, substeps=4)
+    assert_parity(errs, h, sdt)
+
+
+def test_two_substeps_per_call_parity(bp, gpu, oracle):
+    scene = small_mixed_scene(bp, seed=7)
+    errs, h, sdt = lockstep(bp, oracle, scene, bp.make_params(scene), substeps=3, sub_per_call=2)
+    assert_parity(errs, h, sdt)
+
+
+@pytest.mark.parametrize("name", ["step_fluid.npz", "step_mixed.npz", "step_mixed_as_shipped.npz"])
+def test_first_frame_matches_reference_golden(bp, gpu, name):
+    """One frame from the fixture scene against the reference's own kernels."""
+    z = np.load(GOLDEN / name)
+    scene = scene_from_npz(z, bp.scenes)
+    params = bp.make_params(scene)
+    params.stage_mask = int(z["stage_mask"])
+    g = bp.ParticleSolver(scene, params)
+    g.update(2, DT, 4)
+    h = scene.kernel_radius
+    np.testing.assert_array_less(np.abs(g.positions() - z["x1"]).max(), 2e-4 * h)
+    np.testing.assert_array_equal(g.field(bp.abi.BP_FIELD_MAP_TO_ORIGINAL), z["to_orig1"])
+    np.testing.assert_array_equal(g.field(bp.abi.BP_FIELD_SORTED_CELL_IDS), z["sorted_cell1"])
+    g.close()
+
+
+def test_density_statistics_100_frames(bp, gpu, oracle):
+    """Free-running for 100 frames, the fluid's density error statistics agree
+    with the oracle's (trajectories decorrelate; the statistics must not)."""
+    scene = fluid_scene(bp, (10, 10, 10), seed=8, grid_dim=32)
+    params = bp.make_params(scene)
+    g = bp.ParticleSolver(scene, params)
+    o = oracle.OracleSolver(scene, params, threads=4)
+    stats_g, stats_o = [], []
+    for f in range(100):
+        g.update(2, DT, 4)
+        o.update(2, DT, 4)
+        if f >= 50:
+            rg = g.field(bp.abi.BP_FIELD_DENSITIES)
+            ro = o.get(oracle.F_DENSITY)
+            stats_g.append(rg.mean())
+            stats_o.append(ro.mean())
+    mg, mo = float(np.mean(stats_g)), float(np.mean(stats_o))
+    assert abs(mg - mo) / mo < 0.02, (mg, mo)
+    assert np.isfinite(g.positions()).all()
+    g.close()
+
+
+def test_runs_are_bitwise_deterministic(bp, gpu):
+    scene = small_mixed_scene(bp, seed=9)
+    outs = []
+    for _ in range(2):
+        g = bp.ParticleSolver(scene, bp.make_params(scene))
+        for _ in range(5):
+            g.update(2, DT, 4)
+        outs.append((g.positions(), g.velocities()))
+        g.close()
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
+def test_graph_replay_equals_recapture(bp, gpu):
+    scene = small_mixed_scene(bp, seed=10)
+    p = bp.make_params(scene)
+    a = bp.ParticleSolver(scene, p)
+    b = bp.ParticleSolver(scene, p)
+    for _ in range(4):
+        a.update(2, DT, 4)                  # captured once, then replayed
+        b.lib.bp_solver_set_params(b.handle, p)  # forces a new capture every call
+        b.update(2, DT, 4)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    assert a.last_launch_count() > 10
+    a.close()
+    b.close()
+
+
+def test_picking_matches_oracle(bp, gpu, oracle):
+    scene = fluid_scene(bp, (6, 6, 6), seed=2, grid_dim=16)
+    params = bp.make_params(scene)
+    g = bp.ParticleSolver(scene, params)
+    o = oracle.OracleSolver(scene, params)
+    pp = np.array([0.5, 1.5, 0.5], np.float32)
+    pv = np.array([1.0, 0.0, 0.0], np.float32)
+    g.update(2, DT, 3, picked_original_id=7, picked_position=pp, picked_velocity=pv)
+    o.update(2, DT, 3, picked=7, picked_position=pp, picked_velocity=pv)
+    h = scene.kernel_radius
+    assert np.abs(g.positions() - o.positions()).max() <= 1e-4 * h
+    np.testing.assert_allclose(g.velocities()[7], pv)
+    g.close()
+
+
+def test_api_queries_and_copies(bp, gpu):
+    abi = bp.abi
+    scene = small_mixed_scene(bp, seed=12)
+    g = bp.ParticleSolver(scene, bp.make_params(scene))
+    g.update(2, DT, 2)
+    to_orig = g.field(abi.BP_FIELD_MAP_TO_ORIGINAL)
+    to_new = g.field(abi.BP_FIELD_MAP_TO_NEW)
+    n = scene.num_particles
+    assert sorted(to_orig.tolist()) == list(range(n))
+    np.testing.assert_array_equal(to_new[to_orig], np.arange(n))
+    for i in (0, 5, n - 1):
+        assert g.queryOriginalParticleId(i) == to_orig[i]
+        assert g.queryNewParticleId(int(to_orig[i])) == i
+    xs = g.positions(abi.BP_ORDER_SORTED)
+    xo = g.positions(abi.BP_ORDER_ORIGINAL)
+    np.testing.assert_array_equal(xo[to_orig], xs)
+    np.testing.assert_array_equal(g.getParticlePosition(3), xs[3])
+    np.testing.assert_array_equal(g.getParticlePosition(n + 5), np.zeros(3, np.float32))
+    # set_state round trip
+    g.set_state(xo + 1.0, np.zeros_like(xo))
+    np.testing.assert_allclose(g.positions(), xo + 1.0)
+    # render records
+    out = gpu.empty((n, 4), dtype=gpu.float32, device="cuda:0")
+    g.pack_particle_infos(out.data_ptr())
+    gpu.cuda.synchronize()
+    rec = out.cpu().numpy()
+    np.testing.assert_array_equal(rec[:, :3], g.positions(abi.BP_ORDER_SORTED))
+    np.testing.assert_array_equal(rec[:, 3].view(np.int32), scene.phases[to_orig])
+    # cell offsets are a prefix table of the sorted keys
+    off = g.field(abi.BP_FIELD_CELL_OFFSETS)
+    keys = g.field(abi.BP_FIELD_SORTED_CELL_IDS)
+    assert (np.diff(keys) >= 0).all()
+    idx = np.arange(n)
+    assert (off[keys] <= idx).all() and (idx < off[keys + 1]).all()
+    assert g.device_errors() == 0
+    g.close()
+
+
+def test_nonfinite_state_sets_device_error(bp, gpu):
+    scene = fluid_scene(bp, (4, 4, 4), seed=1, grid_dim=16)
+    g = bp.ParticleSolver(scene, bp.make_params(scene))
+    x = g.positions()
+    x[3] = np.nan
+    g.set_state(x)
+    g.update(1, DT, 1)
+    assert g.device_errors() & bp.abi.BP_DEVERR_NONFINITE
+    g.close()
+
+
+def test_empty_scene_update_is_noop(bp, gpu):
+    scene = bp.scenes.Scene()
+    scene.grid_dim = 16
+    scene.kernel_radius = scene.cell_size = 0.2
+    g = bp.ParticleSolver(scene, bp.make_params(scene))
+    g.update(2, DT, 4)
+    assert g.positions().shape == (0, 3)
+    g.close()
+
+
+def test_million_particles_properties(bp, gpu):
+    """Full-size fluid block (1,048,576 particles): size-independent checks."""
+    abi = bp.abi
+    scene = bp.scenes.pbf_scene(128, 64, 128, spacing=0.1, seed=0, box=(12.9, 16.0, 12.9))
+    g = bp.ParticleSolver(scene, bp.make_params(scene))
+    g.update(2, DT, 4)
+    n = scene.num_particles
+    keys = g.field(abi.BP_FIELD_SORTED_CELL_IDS)
+    to_orig = g.field(abi.BP_FIELD_MAP_TO_ORIGINAL)
+    to_new = g.field(abi.BP_FIELD_MAP_TO_NEW)
+    off = g.field(abi.BP_FIELD_CELL_OFFSETS)
+    assert (np.diff(keys) >= 0).all()
+    np.testing.assert_array_equal(to_new[to_orig], np.arange(n))
+    assert off[0] == 0 and off[-1] == n and (np.diff(off) >= 0).all()
+    x = g.positions()
+    assert np.isfinite(x).all() and g.device_errors() == 0
+    assert x[:, 1].min() >= 0.0 - 1e-3
+    g.close()
