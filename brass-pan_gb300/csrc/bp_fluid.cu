@@ -222,10 +222,12 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
     Vout[i] = make_float4(v.x, v.y, v.z, vi4.w);
 }
 
-// Pass C: XSPH viscosity (fluidXSph): same phase, j != i, r^2 <= h^2 (r = 0 included).
+// Pass C: XSPH viscosity (fluidXSph): same phase, j != i, r^2 <= h^2 (r = 0
+// included).  Textbook mode weights each neighbour by its volume m_j / rho_j.
 __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
-                                                         const int *__restrict__ off, float4 *__restrict__ Vout)
+                                                         const int *__restrict__ off, const float *__restrict__ mass,
+                                                         const float *__restrict__ rho, float4 *__restrict__ Vout)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= C.n) return;
@@ -242,7 +244,11 @@ __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const floa
         const float4 pj4 = P[j];
         if (j == i || phase_of(pj4) != phi) return;
         const float d2 = len2(pi - f3(pj4));
-        if (d2 <= C.h2) vn += (f3(V[j]) - vi) * poly6(C, d2);
+        if (d2 <= C.h2) {
+            float wgt = poly6(C, d2);
+            if (C.textbook) wgt = wgt * (__ldg(mass + j) / __ldg(rho + j));
+            vn += (f3(V[j]) - vi) * wgt;
+        }
     });
     const float3 v = vi + C.xsph_c * vn;
     Vout[i] = make_float4(v.x, v.y, v.z, vi4.w);
@@ -263,10 +269,10 @@ void launch_post_b(cudaStream_t st, const SimConsts &C, const float4 *P, const f
     L->done(__func__);
 }
 void launch_post_c(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
-                   float4 *Vout, LaunchLog *L)
+                   const float *mass, const float *rho, float4 *Vout, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    k_post_c<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, V, off, Vout);
+    k_post_c<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, V, off, mass, rho, Vout);
     L->done(__func__);
 }
 

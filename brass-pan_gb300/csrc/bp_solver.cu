@@ -168,6 +168,7 @@ static SimConsts make_consts(const bp_solver *s, float sdt)
     C.c_spiky = -45.f / 3.141592f / powf(h, 6.f);
     C.c_akinci = 32.0f / 3.141592f / powf(h, 9.f);
     C.c_akinci_off = powf(h, 6.0f) / 64.0f;
+    if (p.mode == BP_MODE_TEXTBOOK) C.c_akinci_off = C.c_akinci * C.c_akinci_off;  // Akinci 2013 spline
     C.rho0 = p.rest_density;
     C.inv_rho0 = 1.0f / p.rest_density;
     C.solid_scale = p.solid_density_scale;
@@ -540,9 +541,9 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
     if (post_ab) {
         launch_post_a(st, C, cur, s->Vc, s->rho, s->off, s->Om, s->Nm, L);
         launch_post_b(st, C, cur, s->Vc, s->Om, s->Nm, s->off, C.use_xsph ? s->Vs : s->Vc, L);
-        if (C.use_xsph) launch_post_c(st, C, cur, s->Vs, s->off, s->Vc, L);
+        if (C.use_xsph) launch_post_c(st, C, cur, s->Vs, s->off, s->mass, s->rho, s->Vc, L);
     } else if (C.use_xsph) {
-        launch_post_c(st, C, cur, s->Vc, s->off, s->Vs, L);
+        launch_post_c(st, C, cur, s->Vc, s->off, s->mass, s->rho, s->Vs, L);
         cudaMemcpyAsync(s->Vc, s->Vs, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
     }
 }

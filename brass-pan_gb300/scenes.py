@@ -232,8 +232,12 @@ def config0_dam_break(seed=0):
 
 
 def config1_mixed(seed=0, fluid=(128, 64, 128), cloth=256, cubes=64, cube_dim=8):
-    """1,048,576 fluid particles (128x64x128 block), a 256x256 cloth under
-    wind, 64 rigid cubes of 8^3 particles; box [0,25.6]x[0,12.8]x[0,25.6]."""
+    """1,048,576 fluid particles (128x64x128 block, d = 0.1) in the corner of
+    the box [0,25.8] x [0,16] x [0,25.8]; a 256x256 cloth at spacing d (the
+    contact distance 2r, so the cloth does not fight its own contacts) 2 m
+    above the fluid under wind, with stretch/shear/bend stiffness 1.0/0.5/0.1;
+    64 rigid 8^3 cubes on an 8x8 lattice 2-4 m above the cloth.  The 2^18-cell
+    table (D = 64, cell 0.2 m) wraps every 12.8 m, as in the configuration."""
     rng = np.random.default_rng(seed)
     d = np.float32(0.1)
     s = Scene(name="mixed")
@@ -243,18 +247,16 @@ def config1_mixed(seed=0, fluid=(128, 64, 128), cloth=256, cubes=64, cube_dim=8)
     s.grid_dim = 64
     m = float(1000.0 * d ** 3)
     s.rest_density = m / float(d) ** 3
-    box = (fluid[0] * d + 0.2, 16.0, fluid[2] * d + 0.2)
+    side = max(fluid[0], fluid[2], cloth) * float(d) + 0.2
+    box = (side, 16.0, side)
     box_planes(s, (0, 0, 0), box)
     s.add_fluid_block(fluid, (d, d, d), (d, d, d), m, jitter=0.01 * d, rng=rng)
+    y = float(fluid[1] * d + 2.0)
     if cloth:
-        y = float(fluid[1] * d + 2.0)
-        span = (box[0] - 0.2) / cloth
-        s.add_cloth((0.1, y, 0.1), (span, 0, 0), (0, 0, span), cloth, cloth, m,
-                    stretch=1.0, shear=0.5, bend=0.1)
+        s.add_cloth((0.15, y, 0.15), (d, 0, 0), (0, 0, d), cloth, cloth, m, stretch=1.0, shear=0.5, bend=0.1)
     ncube = int(round(cubes ** 0.5))
     for c in range(cubes):
         cx, cz = c % ncube, c // ncube
-        start = (1.0 + cx * (box[0] - 2.0) / ncube, fluid[1] * d + 4.0 + (c % 3) * 1.0,
-                 1.0 + cz * (box[2] - 2.0) / ncube)
+        start = (0.5 + cx * (box[0] - 1.0) / ncube, y + 2.0 + (c % 3) * 1.0, 0.5 + cz * (box[2] - 1.0) / ncube)
         s.add_rigid_box((cube_dim,) * 3, start, (d, d, d), m)
     return s

@@ -68,14 +68,17 @@ typedef struct {
     float c1, c2, c3, c4, h, h2, half_h;
 } sph_consts;
 
-/* SetKernelRadius (K/fluid.cuh:11-27): pi is the literal 3.141592 */
-static sph_consts make_sph(float h)
+/* SetKernelRadius (K/fluid.cuh:11-27): pi is the literal 3.141592.  Textbook
+ * mode scales the Akinci spline's inner offset h^6/64 by the spline constant
+ * as in Akinci et al. 2013 (the reference leaves it unscaled, quirk Q7). */
+static sph_consts make_sph(float h, int textbook)
 {
     sph_consts k;
     k.c1 = 315.f / 64.f / 3.141592f / powf(h, 9.0f);
     k.c2 = -45.f / 3.141592f / powf(h, 6.f);
     k.c3 = 32.0f / 3.141592f / powf(h, 9.f);
     k.c4 = powf(h, 6.0f) / 64.0f;
+    if (textbook) k.c4 = k.c3 * k.c4;
     k.h2 = h * h;
     k.half_h = h * 0.5f;
     k.h = h;
@@ -749,10 +752,12 @@ static void fluid_vorticity(or_solver *s, const sph_consts *k, float dt)
     }
 }
 
-/* fluidXSph (K/fluid.cuh:338-385) -> out */
+/* fluidXSph (K/fluid.cuh:338-385) -> out.  Textbook mode weights each
+ * neighbour by its volume m_j / rho_j (Macklin & Mueller 2013, eq. 17). */
 static void fluid_xsph(or_solver *s, const sph_consts *k, f3 *out)
 {
     const float c = s->prm.xsph_c, cell = s->prm.cell_size;
+    const int textbook = s->prm.mode == BP_MODE_TEXTBOOK;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < s->n; ++i) {
         const int phi = s->phase[i];
@@ -763,7 +768,11 @@ static void fluid_xsph(or_solver *s, const sph_consts *k, f3 *out)
         FOR_EACH_CANDIDATE(s, pi, j) {
             if (!(i != j && phi == s->phase[j])) continue;
             const float d2 = vlen2(vsub(pi, s->p[j]));
-            if (d2 <= k->h2) vn = vadd(vn, vmul(vsub(s->v[j], vi), poly6(k, d2)));
+            if (d2 <= k->h2) {
+                float wgt = poly6(k, d2);
+                if (textbook) wgt = wgt * (s->m[j] / s->rho[j]);
+                vn = vadd(vn, vmul(vsub(s->v[j], vi), wgt));
+            }
         }
         out[i] = vadd(vi, smul(c, vn));
     }
@@ -835,7 +844,7 @@ int or_update(or_solver *s, int nsub, float dt, int iterations, int picked, cons
     const bp_params *P = &s->prm;
     const int mask = P->stage_mask;
     const float sdt = dt / (float)nsub;
-    const sph_consts k = make_sph(P->kernel_radius);
+    const sph_consts k = make_sph(P->kernel_radius, P->mode == BP_MODE_TEXTBOOK);
     const float r = P->particle_radius;
     const f3 g = v3(P->gravity[0], P->gravity[1], P->gravity[2]);
     const f3 ppos = pp ? v3(pp[0], pp[1], pp[2]) : v3(0, 0, 0);
