@@ -77,7 +77,8 @@ class BpParams(C.Structure):
         ("wind_drag", C.c_float),
         ("wind_lift", C.c_float),
         ("rotation_iterations", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("neighbor_skin", C.c_float),
+        ("reserved", C.c_int32 * 7),
     ]
 
 

@@ -45,6 +45,21 @@ struct SimConsts {
     int nplanes;
     float4 plane_o[kMaxPlanes];
     float4 plane_n[kMaxPlanes];
+    // Neighbour bitmasks of the current substep (nl_mask == nullptr: off).
+    // For each particle and each of its 9 column runs, bit t of
+    // nl_mask[col * n + i] marks candidate off[start] + t within h + skin of
+    // it at build time; nl_cell is the cell the masks were built for (-1: the
+    // particle always walks its 27 cells), nl_pos the positions at build,
+    // and *nl_disp the largest squared displacement since the build (float
+    // bits).  A masked walk is taken only while the particle is still in
+    // nl_cell and *nl_disp <= (skin/2)^2, which guarantees that every pair
+    // within h is flagged.
+    unsigned long long *nl_mask;
+    int *nl_cell;
+    float4 *nl_pos;
+    unsigned *nl_disp;
+    float nl_hs2;        // (h + skin)^2
+    float nl_half_skin2; // (skin / 2)^2
 };
 
 // ---- small vector helpers (own code; component-wise, left-to-right dot) ----
@@ -172,6 +187,65 @@ __device__ __forceinline__ void for_each_candidate_from(float3 pi, int lo, const
             }
         }
     }
+}
+
+// True when particle i may walk its neighbour bitmasks instead of its 27 cells.
+__device__ __forceinline__ bool masks_usable(const SimConsts &C, int i, int3 c)
+{
+    if (!C.nl_mask) return false;
+    if (*C.nl_disp > __float_as_uint(C.nl_half_skin2)) return false;
+    return __ldg(C.nl_cell + i) == cell_addr(c.x, c.y, c.z, C.D, C.mask);
+}
+
+// Candidate walk of particle i: the set bits of its neighbour masks when
+// they are valid, else the 27-cell walk.  Both visit candidates column by
+// column in ascending sorted index, so every pair sum accumulates in the same
+// order either way; only indices j >= lo are visited.
+template <class F>
+__device__ __forceinline__ void for_each_neighbor(int i, float3 pi, int lo, const int *__restrict__ off,
+                                                  const SimConsts &C, F &&f)
+{
+    const int3 c = cell_of(pi, C);
+    if (masks_usable(C, i, c)) {
+        // One loop over all set bits of the 9 masks (advancing to the next
+        // column when the current one is exhausted), so the lanes of a warp
+        // diverge only on their total neighbour count.
+        const unsigned m = C.mask;
+        const unsigned D = (unsigned)C.D;
+        const unsigned z0 = (unsigned)(c.z - 1) & m;  // no wrap: masks are never built across it
+        int col = -1, b = 0;
+        unsigned long long bits = 0ull;
+#pragma unroll 1
+        while (true) {
+            while (bits == 0ull) {
+                if (++col == 9) return;
+                bits = C.nl_mask[(size_t)col * C.n + i];
+                if (bits) {
+                    const int dx = col / 3 - 1, dy = col % 3 - 1;
+                    b = __ldg(off + ((unsigned)(c.x + dx) & m) * D * D + ((unsigned)(c.y + dy) & m) * D + z0);
+                    if (lo > b) bits = (lo - b >= 64) ? 0ull : bits & (~0ull << (lo - b));
+                }
+            }
+            const int t = __ffsll((long long)bits) - 1;
+            bits &= bits - 1;
+            f(b + t);
+        }
+    }
+    if (lo > 0)
+        for_each_candidate_from(pi, lo, off, C, f);
+    else
+        for_each_candidate(pi, off, C, f);
+}
+
+// Records how far particle i has moved from its position at mask build;
+// writers of P call it with the new position (inactive lanes pass false).
+__device__ __forceinline__ void track_displacement(const SimConsts &C, int i, float3 p, bool active)
+{
+    if (!C.nl_mask) return;
+    const float d2 = active ? len2(p - f3(C.nl_pos[i])) : 0.f;
+    const unsigned am = __activemask();
+    const unsigned u = __reduce_max_sync(am, __float_as_uint(d2));  // NaN bits exceed every finite value
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(am) - 1) && u > 0u) atomicMax(C.nl_disp, u);
 }
 
 // Plane walls: planeStabilize / particlePlaneCollisionConstraint

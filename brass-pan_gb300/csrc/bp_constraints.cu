@@ -24,6 +24,7 @@ __global__ void k_planes(SimConsts C, const float4 *__restrict__ Xs, float4 *__r
     float3 p = f3(p4);
     plane_collide(C, f3(Xs[i]), p);
     P[i] = make_float4(p.x, p.y, p.z, p4.w);
+    track_displacement(C, i, p, true);
 }
 
 void launch_planes(cudaStream_t st, const SimConsts &C, const float4 *Xs, float4 *P, LaunchLog *L)
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(128) k_particle_collision(SimConsts C, const f
     const float r = C.radius;
     float3 sd = make_float3(0.f, 0.f, 0.f), sf = make_float3(0.f, 0.f, 0.f);
     int count = 0;
-    for_each_candidate(xip, off, C, [&](int j) {
+    for_each_neighbor(i, xip, 0, off, C, [&](int j) {
         const float4 pj4 = P[j];
         const int phj = phase_of(pj4);
         if (!(j != i && phi != phj && (phi > 0 || phj > 0))) return;
@@ -110,6 +111,7 @@ __global__ void __launch_bounds__(128) k_particle_collision(SimConsts C, const f
     const float3 d = (count == 0) ? sd : sd + sf / (float)count;
     const float3 p = xip + d;
     Pout[i] = make_float4(p.x, p.y, p.z, pi4.w);
+    track_displacement(C, i, p, true);
 }
 
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
@@ -142,7 +144,7 @@ __global__ void k_distance_edges(int m, const int2 *__restrict__ pairs, const fl
     edge_k[e] = make_float4(k.x, k.y, k.z, 0.f);
 }
 
-__global__ void k_distance_apply(int nn_, const int *__restrict__ node_ids, const int *__restrict__ ptr,
+__global__ void k_distance_apply(SimConsts C, int nn_, const int *__restrict__ node_ids, const int *__restrict__ ptr,
                                  const int *__restrict__ inc, const float4 *__restrict__ edge_k,
                                  const float *__restrict__ w, const int *__restrict__ to_new, float4 *__restrict__ P)
 {
@@ -157,19 +159,20 @@ __global__ void k_distance_apply(int nn_, const int *__restrict__ node_ids, cons
         d += (code & 1) ? wi * k : -wi * k;
     }
     const float4 p4 = P[i];
-    P[i] = make_float4(p4.x + d.x, p4.y + d.y, p4.z + d.z, p4.w);
+    const float3 p = make_float3(p4.x + d.x, p4.y + d.y, p4.z + d.z);
+    P[i] = make_float4(p.x, p.y, p.z, p4.w);
+    track_displacement(C, i, p, true);
 }
 
 void launch_distance(cudaStream_t st, const SimConsts &C, const DistanceArgs &a, float4 *P, const float *w,
                      const int *to_new, unsigned *err, LaunchLog *L)
 {
-    (void)C;
     (void)err;
     if (a.num_edges <= 0) return;
     k_distance_edges<<<(a.num_edges + 255) / 256, 256, 0, st>>>(a.num_edges, a.pairs, a.params, P, w, to_new,
                                                                 a.edge_k);
     L->done("k_distance_edges");
-    k_distance_apply<<<(a.num_nodes + 255) / 256, 256, 0, st>>>(a.num_nodes, a.node_ids, a.node_ptr, a.node_inc,
+    k_distance_apply<<<(a.num_nodes + 255) / 256, 256, 0, st>>>(C, a.num_nodes, a.node_ids, a.node_ptr, a.node_inc,
                                                                 a.edge_k, w, to_new, P);
     L->done("k_distance_apply");
 }
@@ -206,7 +209,7 @@ __global__ void k_wind_faces(SimConsts C, int nf, const int *__restrict__ faces,
     move[f] = make_float4(mv.x, mv.y, mv.z, 0.f);
 }
 
-__global__ void k_wind_apply(int nn_, const int *__restrict__ node_ids, const int *__restrict__ ptr,
+__global__ void k_wind_apply(SimConsts C, int nn_, const int *__restrict__ node_ids, const int *__restrict__ ptr,
                              const int *__restrict__ inc, const float4 *__restrict__ move,
                              const float *__restrict__ mass, const int *__restrict__ to_new, float4 *__restrict__ P)
 {
@@ -217,7 +220,9 @@ __global__ void k_wind_apply(int nn_, const int *__restrict__ node_ids, const in
     float3 d = make_float3(0.f, 0.f, 0.f);
     for (int q = ptr[t]; q < ptr[t + 1]; ++q) d += f3(move[inc[q]]) / m;
     const float4 p4 = P[i];
-    P[i] = make_float4(p4.x + d.x, p4.y + d.y, p4.z + d.z, p4.w);
+    const float3 p = make_float3(p4.x + d.x, p4.y + d.y, p4.z + d.z);
+    P[i] = make_float4(p.x, p.y, p.z, p4.w);
+    track_displacement(C, i, p, true);
 }
 
 void launch_wind(cudaStream_t st, const SimConsts &C, const WindArgs &a, float4 *P, const float4 *Vs,
@@ -226,7 +231,7 @@ void launch_wind(cudaStream_t st, const SimConsts &C, const WindArgs &a, float4 
     if (a.num_faces <= 0) return;
     k_wind_faces<<<(a.num_faces + 255) / 256, 256, 0, st>>>(C, a.num_faces, a.faces, P, Vs, to_new, a.face_move);
     L->done("k_wind_faces");
-    k_wind_apply<<<(a.num_nodes + 255) / 256, 256, 0, st>>>(a.num_nodes, a.node_ids, a.node_ptr, a.node_inc,
+    k_wind_apply<<<(a.num_nodes + 255) / 256, 256, 0, st>>>(C, a.num_nodes, a.node_ids, a.node_ptr, a.node_inc,
                                                             a.face_move, mass, to_new, P);
     L->done("k_wind_apply");
 }
@@ -347,6 +352,7 @@ __global__ void __launch_bounds__(kSmThreads) k_shape_matching(SimConsts C, Rigi
         const float3 g = ((R.c0 * q.x + R.c1 * q.y) + R.c2 * q.z) + cmv;
         const float4 p4 = P[id];
         P[id] = make_float4(g.x, g.y, g.z, p4.w);
+        track_displacement(C, id, g, true);
     }
 }
 
@@ -358,7 +364,7 @@ void launch_shape_matching(cudaStream_t st, const SimConsts &C, const RigidArgs 
     L->done(__func__);
 }
 
-__global__ void k_immovable(int k, const int *__restrict__ ids, const int *__restrict__ to_new,
+__global__ void k_immovable(SimConsts C, int k, const int *__restrict__ ids, const int *__restrict__ to_new,
                             const float4 *__restrict__ Xs, float4 *__restrict__ P)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -366,13 +372,14 @@ __global__ void k_immovable(int k, const int *__restrict__ ids, const int *__res
     const int i = to_new[ids[t]];
     const float4 x = Xs[i];
     P[i] = make_float4(x.x, x.y, x.z, P[i].w);
+    track_displacement(C, i, f3(x), true);
 }
 
-void launch_immovable(cudaStream_t st, int k, const int *ids, const int *to_new, const float4 *Xs, float4 *P,
-                      LaunchLog *L)
+void launch_immovable(cudaStream_t st, const SimConsts &C, int k, const int *ids, const int *to_new,
+                      const float4 *Xs, float4 *P, LaunchLog *L)
 {
     if (k <= 0) return;
-    k_immovable<<<(k + 255) / 256, 256, 0, st>>>(k, ids, to_new, Xs, P);
+    k_immovable<<<(k + 255) / 256, 256, 0, st>>>(C, k, ids, to_new, Xs, P);
     L->done(__func__);
 }
 

@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const floa
     const float3 pi = f3(pi4);
     float density = 0.f;
     if (!C.textbook) {
-        for_each_candidate_from(pi, i, off, C, [&](int j) {
+        for_each_neighbor(i, pi, i, off, C, [&](int j) {
             const float4 pj = P[j];
             const float d2 = len2(pi - f3(pj));
             if (d2 <= C.h2) {
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const floa
     } else {
         float sum_g2 = 0.f;
         float3 gi = make_float3(0.f, 0.f, 0.f);
-        for_each_candidate(pi, off, C, [&](int j) {
+        for_each_neighbor(i, pi, 0, off, C, [&](int j) {
             const float4 pj = P[j];
             const float3 diff = pi - f3(pj);
             const float d2 = len2(diff);
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs 
     float3 sum = make_float3(0.f, 0.f, 0.f);
     if (!(C.textbook && phk > 0)) {
         const float lk = a.lam[k];
-        for_each_candidate(pk, a.off, C, [&](int j) {
+        for_each_neighbor(k, pk, 0, a.off, C, [&](int j) {
             if (j == k) return;
             const float4 pj4 = a.P[j];
             const float3 diff = pk - f3(pj4);
@@ -127,6 +127,57 @@ __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs 
         a.orig_c[k] = a.orig_s[k];
     }
     a.Pout[k] = make_float4(p.x, p.y, p.z, pk4.w);
+    track_displacement(C, k, p, true);
+}
+
+// Neighbour bitmasks for the rest of the substep (see SimConsts::nl_mask):
+// one 27-cell walk at the positions of the first iteration.  Particles whose
+// column runs wrap around the table in z, or hold more than 64 candidates,
+// keep walking their cells.
+__global__ void __launch_bounds__(kScanThreads) k_build_masks(SimConsts C, const float4 *__restrict__ P,
+                                                              const int *__restrict__ off)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C.n) return;
+    const float4 pi4 = P[i];
+    const float3 pi = f3(pi4);
+    C.nl_pos[i] = pi4;
+    const int3 c = cell_of(pi, C);
+    const unsigned m = C.mask;
+    const unsigned D = (unsigned)C.D;
+    const unsigned z0 = (unsigned)(c.z - 1) & m;
+    const unsigned z2 = (unsigned)(c.z + 1) & m;
+    bool ok = z0 < z2;
+    int col = 0;
+#pragma unroll 1
+    for (int dx = -1; dx <= 1; ++dx) {
+        const unsigned bx = ((unsigned)(c.x + dx) & m) * D * D;
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy, ++col) {
+            unsigned long long bits = 0ull;
+            if (ok) {
+                const unsigned base = bx + ((unsigned)(c.y + dy) & m) * D;
+                const int b = __ldg(off + base + z0), e = __ldg(off + base + z2 + 1);
+                if (e - b > 64) {
+                    ok = false;
+                } else {
+#pragma unroll 1
+                    for (int j = b; j < e; ++j)
+                        if (len2(pi - f3(P[j])) <= C.nl_hs2) bits |= 1ull << (j - b);
+                }
+            }
+            C.nl_mask[(size_t)col * C.n + i] = bits;
+        }
+    }
+    C.nl_cell[i] = ok ? cell_addr(c.x, c.y, c.z, C.D, C.mask) : -1;
+}
+
+void launch_build_masks(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, LaunchLog *L)
+{
+    if (C.n <= 0 || !C.nl_mask) return;
+    cudaMemsetAsync(C.nl_disp, 0, sizeof(unsigned), st);
+    k_build_masks<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, off);
+    L->done(__func__);
 }
 
 void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, LaunchLog *L)
@@ -153,7 +204,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const floa
     const float3 vi = f3(V[i]);
     float3 om = make_float3(0.f, 0.f, 0.f), nn = make_float3(0.f, 0.f, 0.f);
     const bool want_om = C.use_vort, want_n = C.use_akinci;
-    for_each_candidate(pi, off, C, [&](int j) {
+    for_each_neighbor(i, pi, 0, off, C, [&](int j) {
         const float4 pj4 = P[j];
         if (j == i || phase_of(pj4) != phi) return;
         const float3 diff = pi - f3(pj4);
@@ -194,7 +245,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
     const float rhoi = ni4.w;
     float3 eta = make_float3(0.f, 0.f, 0.f), ft = make_float3(0.f, 0.f, 0.f);
     const bool want_v = C.use_vort, want_t = C.use_akinci;
-    for_each_candidate(pi, off, C, [&](int j) {
+    for_each_neighbor(i, pi, 0, off, C, [&](int j) {
         const float4 pj4 = P[j];
         if (j == i || phase_of(pj4) != phi) return;
         const float3 pj = f3(pj4);
@@ -240,7 +291,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const floa
     }
     const float3 pi = f3(pi4), vi = f3(vi4);
     float3 vn = make_float3(0.f, 0.f, 0.f);
-    for_each_candidate(pi, off, C, [&](int j) {
+    for_each_neighbor(i, pi, 0, off, C, [&](int j) {
         const float4 pj4 = P[j];
         if (j == i || phase_of(pj4) != phi) return;
         const float d2 = len2(pi - f3(pj4));

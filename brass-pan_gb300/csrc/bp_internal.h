@@ -100,6 +100,7 @@ struct DeltaArgs {
     int *orig_c;
 };
 void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, LaunchLog *L);
+void launch_build_masks(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, LaunchLog *L);
 void launch_post_a(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float *rho,
                    const int *off, float4 *Om, float4 *Nm, LaunchLog *L);
 void launch_post_b(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float4 *Om,
@@ -148,7 +149,7 @@ struct RigidArgs {
 };
 void launch_shape_matching(cudaStream_t st, const SimConsts &C, const RigidArgs &a, float4 *P,
                            const int *to_new, LaunchLog *L);
-void launch_immovable(cudaStream_t st, int k, const int *ids, const int *to_new, const float4 *Xs, float4 *P,
+void launch_immovable(cudaStream_t st, const SimConsts &C, int k, const int *ids, const int *to_new, const float4 *Xs, float4 *P,
                       LaunchLog *L);
 void launch_pick(cudaStream_t st, int id_orig, const int *to_new, float4 *pos, float3 p, int set_pos, float4 *vel,
                  float3 v, LaunchLog *L);

@@ -56,6 +56,10 @@ struct bp_solver {
     int *keys = nullptr, *sorted_keys = nullptr, *order = nullptr, *off = nullptr;
     float *mass = nullptr, *lam = nullptr, *rho = nullptr, *w = nullptr;
     float *staging = nullptr;  // 2 x N x 3 floats for host copies
+    unsigned long long *nl_mask = nullptr;  // neighbour masks [9][N]
+    int *nl_cell = nullptr;
+    float4 *nl_pos = nullptr;
+    unsigned *nl_disp = nullptr;
     unsigned *err = nullptr;
     SortScratch sort{};
 
@@ -134,6 +138,7 @@ extern "C" void bp_params_init(bp_params *p, float r)
     p->wind_drag = 10.0f;
     p->wind_lift = 100.0f;
     p->rotation_iterations = 20;
+    p->neighbor_skin = 0.1f;
 }
 
 static bp_status check_params(const bp_params *p)
@@ -203,6 +208,16 @@ static SimConsts make_consts(const bp_solver *s, float sdt)
     C.rot_iters = p.rotation_iterations;
     C.dt = sdt;
     C.inv_dt = 1.0f / sdt;
+    if (p.neighbor_skin > 0.f) {
+        C.nl_mask = s->nl_mask;
+        C.nl_cell = s->nl_cell;
+        C.nl_pos = s->nl_pos;
+        C.nl_disp = s->nl_disp;
+        const float hs = h * (1.0f + p.neighbor_skin);
+        const float half_skin = 0.5f * h * p.neighbor_skin;
+        C.nl_hs2 = hs * hs;
+        C.nl_half_skin2 = half_skin * half_skin;
+    }
     C.nplanes = (p.stage_mask & BP_STAGE_PLANES) ? s->nplanes : 0;
     for (int k = 0; k < s->nplanes; ++k) {
         C.plane_o[k] = make_float4(s->planes[k][0], s->planes[k][1], s->planes[k][2], 0.f);
@@ -319,7 +334,8 @@ extern "C" bp_status bp_solver_create(const bp_scene_desc *sc, const bp_params *
         (st = s->alloc(&s->keys, N)) || (st = s->alloc(&s->sorted_keys, N)) || (st = s->alloc(&s->order, N)) ||
         (st = s->alloc(&s->off, ncells + 1)) || (st = s->alloc(&s->mass, N)) || (st = s->alloc(&s->lam, N)) ||
         (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)) ||
-        (st = s->alloc(&s->staging, 6 * N)))
+        (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->nl_mask, 9 * N)) ||
+        (st = s->alloc(&s->nl_cell, N)) || (st = s->alloc(&s->nl_pos, N)) || (st = s->alloc(&s->nl_disp, 1)))
         return bail(st);
     {
         char *scratch = nullptr;
@@ -492,6 +508,8 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
 
     float4 *cur = s->Pa, *other = s->Pb;
     if (wind) launch_wind(st, C, s->wind, cur, s->Vs, s->mass, s->to_new, L);
+    const bool scans = pcoll || fluid || C.use_vort || C.use_akinci || C.use_xsph;
+    if (scans && C.nl_mask) launch_build_masks(st, C, cur, s->off, L);
 
     bool planes_done = fuse_first_planes;
     bool committed = false;
@@ -532,7 +550,7 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
         }
         if (distance) launch_distance(st, C, s->dist, cur, s->w, s->to_new, s->err, L);
         if (rigid) launch_shape_matching(st, C, s->rigid, cur, s->to_new, L);
-        if (immov) launch_immovable(st, s->nimm, s->imm, s->to_new, s->Xs, cur, L);
+        if (immov) launch_immovable(st, C, s->nimm, s->imm, s->to_new, s->Xs, cur, L);
     }
     if (!committed) launch_commit(st, C, cur, s->Xs, s->Vs, s->orig_s, s->Xc, s->Vc, s->orig_c, L);
     s->Pcur = cur;
@@ -552,7 +570,8 @@ static bp_status enqueue_update(bp_solver *s, int nsub, float dt, int iterations
                                 float3 pvel, LaunchLog *L)
 {
     const float sdt = dt / (float)nsub;
-    const SimConsts C = make_consts(s, sdt);
+    SimConsts C = make_consts(s, sdt);
+    if (picked >= 0) C.nl_mask = nullptr;  // the picked particle teleports: walk the cells
     for (int k = 0; k < nsub; ++k) enqueue_substep(s, C, iterations, picked, ppos, L);
     if (picked >= 0) launch_pick(s->stream, picked, s->to_new, s->Xc, ppos, 0, s->Vc, pvel, L);
     launch_check_finite(s->stream, s->n, s->Xc, s->err, L);

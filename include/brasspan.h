@@ -105,7 +105,9 @@ typedef struct bp_params {
     float wind_drag;             /* 10 (wind.cuh:40) */
     float wind_lift;             /* 100 (wind.cuh:43) */
     int32_t rotation_iterations; /* 20 (shapematching.cuh:72) */
-    int32_t reserved[8];
+    float neighbor_skin;         /* skin of the per-substep neighbour masks, as a fraction of h
+                                    (0 disables them; results are identical either way): 0.1 */
+    int32_t reserved[7];
 } bp_params;
 
 /* Fills `p` with the reference's literals for a scene of the given particle

@@ -163,6 +163,23 @@ def test_runs_are_bitwise_deterministic(bp, gpu):
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
+@pytest.mark.parametrize("skin", [0.1, 0.02, 0.001])
+def test_neighbor_masks_are_bit_identical_to_cell_walks(bp, gpu, skin):
+    """The per-substep neighbour masks (any skin, including one so small that
+    the displacement guard falls back to cell walks mid-substep) give exactly
+    the results of walking the 27 cells."""
+    scene = small_mixed_scene(bp, seed=13)
+    outs = []
+    for s in (0.0, skin):
+        g = bp.ParticleSolver(scene, bp.make_params(scene, neighbor_skin=s))
+        for _ in range(4):
+            g.update(2, DT, 4)
+        outs.append((g.positions(), g.velocities()))
+        g.close()
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
 def test_graph_replay_equals_recapture(bp, gpu):
     scene = small_mixed_scene(bp, seed=10)
     p = bp.make_params(scene)
