@@ -27,10 +27,11 @@ struct SimConsts {
     float h, h2, half_h, c_poly6, c_spiky, c_akinci, c_akinci_off;
     // PBF
     float rho0, inv_rho0, solid_scale, lambda_den, relaxation;
-    float scorr_k, scorr_n, scorr_wq;  // wq = poly6((dq*h)^2)
+    float scorr_k, scorr_inv_wq;       // 1 / poly6((dq*h)^2)
+    int scorr_ni;                      // exponent n
     int scorr_on;                      // reference: s_corr only when Akinci is off
     int clamp_c;                       // reference: C = max(C, 0) when Akinci is on
-    float delta_clamp;                 // <= 0: no clamp
+    float delta_clamp, delta_clamp2;   // <= 0: no clamp
     int textbook;
     // post passes
     float vort_eps, tension, xsph_c;
@@ -58,9 +59,14 @@ struct SimConsts {
     int *nl_cell;
     float4 *nl_pos;
     unsigned *nl_disp;
-    float nl_hs2;        // (h + skin)^2
-    float nl_half_skin2; // (skin / 2)^2
+    unsigned char *nl_flags; // kFlagContact: a contact partner within 2r + skin at build
+    unsigned *nl_stats;      // profiling only: [0] masked walks, [1] cell walks
+    float nl_hs2;            // (h + skin)^2
+    float nl_half_skin2;     // (skin / 2)^2
+    float nl_contact2;       // (2r + skin)^2
 };
+
+constexpr unsigned char kFlagContact = 1;
 
 // ---- small vector helpers (own code; component-wise, left-to-right dot) ----
 
@@ -94,6 +100,19 @@ __device__ __forceinline__ float3 spiky_grad(const SimConsts &C, float3 v, float
     const float r = sqrtf(r2);
     const float t = C.h - r;
     return (C.c_spiky * t * t * v) / r;
+}
+// Same gradient through one reciprocal square root (r2 > 0): the hot loops'
+// form.  Differs from the IEEE sqrt-and-divide form above by a few ulp.
+__device__ __forceinline__ float3 spiky_grad_r(const SimConsts &C, float3 v, float r2, float inv_r)
+{
+    const float t = C.h - r2 * inv_r;
+    return (C.c_spiky * t * t * inv_r) * v;
+}
+__device__ __forceinline__ float ipowf(float x, int n)
+{
+    float r = 1.0f;
+    for (int k = 0; k < n; ++k) r *= x;
+    return r;
 }
 __device__ __forceinline__ float akinci_spline(const SimConsts &C, float r)
 {
@@ -206,7 +225,9 @@ __device__ __forceinline__ void for_each_neighbor(int i, float3 pi, int lo, cons
                                                   const SimConsts &C, F &&f)
 {
     const int3 c = cell_of(pi, C);
-    if (masks_usable(C, i, c)) {
+    const bool usable = masks_usable(C, i, c);
+    if (C.nl_stats) atomicAdd(C.nl_stats + (usable ? 0 : 1), 1u);
+    if (usable) {
         // One loop over all set bits of the 9 masks (advancing to the next
         // column when the current one is exhausted), so the lanes of a warp
         // diverge only on their total neighbour count.

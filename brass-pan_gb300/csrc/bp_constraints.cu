@@ -76,7 +76,11 @@ __global__ void __launch_bounds__(128) k_particle_collision(SimConsts C, const f
     const float r = C.radius;
     float3 sd = make_float3(0.f, 0.f, 0.f), sf = make_float3(0.f, 0.f, 0.f);
     int count = 0;
-    for_each_neighbor(i, xip, 0, off, C, [&](int j) {
+    // No contact partner within 2r + skin at mask build and the masks still
+    // valid: no pair can be closer than 2r now, the walk would find nothing.
+    const bool none = C.nl_mask && C.nl_flags && !(C.nl_flags[i] & kFlagContact) &&
+                      masks_usable(C, i, cell_of(xip, C));
+    if (!none) for_each_neighbor(i, xip, 0, off, C, [&](int j) {
         const float4 pj4 = P[j];
         const int phj = phase_of(pj4);
         if (!(j != i && phi != phj && (phi > 0 || phj > 0))) return;

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const floa
                 const float ld = mj * poly6(C, d2);
                 density += (phase_of(pj) < 0) ? ld : C.solid_scale * ld;
                 if (d2 > 0.f) {
-                    const float3 g = (-mj * spiky_grad(C, diff, d2)) / C.rho0;
+                    const float3 g = (-mj * C.inv_rho0) * spiky_grad_r(C, diff, d2, rsqrtf(d2));
                     sum_g2 += dot3(g, g);
                     gi -= g;
                 }
@@ -106,11 +106,11 @@ __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs 
                 const bool inc = C.textbook ? true : ((j > k) ? (phk < 0) : (phase_of(pj4) < 0));
                 if (!inc) return;
                 float sl = lk + __ldg(a.lam + j);
-                if (C.scorr_on) sl += -C.scorr_k * powf(poly6(C, d2) / C.scorr_wq, C.scorr_n);
-                float3 delta = sl * spiky_grad(C, diff, d2);
-                if (C.delta_clamp > 0.f) {
-                    const float len = len3(delta);
-                    delta = (len < C.delta_clamp) ? delta : (delta * fminf(len, C.delta_clamp)) / len;
+                if (C.scorr_on) sl += -C.scorr_k * ipowf(poly6(C, d2) * C.scorr_inv_wq, C.scorr_ni);
+                float3 delta = sl * spiky_grad_r(C, diff, d2, rsqrtf(d2));
+                if (C.delta_clamp > 0.f) {  // per-pair clamp; the length is only needed past it
+                    const float l2 = len2(delta);
+                    if (!(l2 < C.delta_clamp2)) delta = delta * (C.delta_clamp * rsqrtf(l2));
                 }
                 sum += __ldg(a.mass + j) * delta;
             }
@@ -141,6 +141,7 @@ __global__ void __launch_bounds__(kScanThreads) k_build_masks(SimConsts C, const
     if (i >= C.n) return;
     const float4 pi4 = P[i];
     const float3 pi = f3(pi4);
+    const int phi = phase_of(pi4);
     C.nl_pos[i] = pi4;
     const int3 c = cell_of(pi, C);
     const unsigned m = C.mask;
@@ -148,6 +149,7 @@ __global__ void __launch_bounds__(kScanThreads) k_build_masks(SimConsts C, const
     const unsigned z0 = (unsigned)(c.z - 1) & m;
     const unsigned z2 = (unsigned)(c.z + 1) & m;
     bool ok = z0 < z2;
+    unsigned char flags = 0;
     int col = 0;
 #pragma unroll 1
     for (int dx = -1; dx <= 1; ++dx) {
@@ -162,14 +164,21 @@ __global__ void __launch_bounds__(kScanThreads) k_build_masks(SimConsts C, const
                     ok = false;
                 } else {
 #pragma unroll 1
-                    for (int j = b; j < e; ++j)
-                        if (len2(pi - f3(P[j])) <= C.nl_hs2) bits |= 1ull << (j - b);
+                    for (int j = b; j < e; ++j) {
+                        const float4 pj4 = P[j];
+                        const float d2 = len2(pi - f3(pj4));
+                        if (d2 <= C.nl_hs2) bits |= 1ull << (j - b);
+                        const int phj = phase_of(pj4);
+                        if (d2 <= C.nl_contact2 && j != i && phi != phj && (phi > 0 || phj > 0))
+                            flags |= kFlagContact;
+                    }
                 }
             }
             C.nl_mask[(size_t)col * C.n + i] = bits;
         }
     }
     C.nl_cell[i] = ok ? cell_addr(c.x, c.y, c.z, C.D, C.mask) : -1;
+    C.nl_flags[i] = flags;
 }
 
 void launch_build_masks(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, LaunchLog *L)
@@ -210,9 +219,9 @@ __global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const floa
         const float3 diff = pi - f3(pj4);
         const float d2 = len2(diff);
         if (d2 <= C.h2 && d2 > 0.f) {
-            const float3 g = spiky_grad(C, diff, d2);
+            const float3 g = spiky_grad_r(C, diff, d2, rsqrtf(d2));
             if (want_om) om += cross3(f3(V[j]) - vi, g);
-            if (want_n) nn += (1.0f / __ldg(rho + j)) * g;
+            if (want_n) nn += __frcp_rn(__ldg(rho + j)) * g;
         }
     });
     Om[i] = make_float4(om.x, om.y, om.z, len3(om));
@@ -252,13 +261,14 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
         const float3 diff = pi - pj;
         const float d2 = len2(diff);
         if (d2 <= C.h2 && d2 > 0.f) {
-            if (want_v) eta += Om[j].w * spiky_grad(C, diff, d2);
+            const float inv_r = rsqrtf(d2);
+            if (want_v) eta += Om[j].w * spiky_grad_r(C, diff, d2, inv_r);
             if (want_t) {
                 const float4 nj4 = Nm[j];
-                const float dist = sqrtf(d2);
-                const float3 fco = (-C.tension * akinci_spline(C, dist) * (pi - pj)) / dist;
+                const float dist = d2 * inv_r;
+                const float3 fco = (-C.tension * akinci_spline(C, dist) * inv_r) * diff;
                 const float3 fcu = -C.tension * (ni - f3(nj4));
-                const float kij = 2.0f * C.rho0 / (rhoi + nj4.w);
+                const float kij = (2.0f * C.rho0) * __frcp_rn(rhoi + nj4.w);
                 ft += kij * (fco + fcu);
             }
         }

@@ -60,6 +60,8 @@ struct bp_solver {
     int *nl_cell = nullptr;
     float4 *nl_pos = nullptr;
     unsigned *nl_disp = nullptr;
+    unsigned char *nl_flags = nullptr;
+    unsigned *nl_stats = nullptr;
     unsigned *err = nullptr;
     SortScratch sort{};
 
@@ -152,6 +154,8 @@ static bp_status check_params(const bp_params *p)
     if (p->kernel_radius > p->cell_size * 1.0001f)
         return fail(BP_ERR_INVALID_ARGUMENT, "kernel_radius must not exceed cell_size (27-cell search)");
     if (p->rotation_iterations < 0) return fail(BP_ERR_INVALID_ARGUMENT, "rotation_iterations < 0");
+    if (p->scorr_n < 0 || p->scorr_n > 16) return fail(BP_ERR_INVALID_ARGUMENT, "scorr_n must be in [0, 16]");
+    if (!(p->neighbor_skin >= 0.f)) return fail(BP_ERR_INVALID_ARGUMENT, "neighbor_skin < 0");
     return BP_OK;
 }
 
@@ -184,13 +188,14 @@ static SimConsts make_consts(const bp_solver *s, float sdt)
     C.scorr_on = C.textbook || !akinci;
     C.clamp_c = akinci;
     C.scorr_k = p.scorr_k;
-    C.scorr_n = (float)p.scorr_n;
+    C.scorr_ni = p.scorr_n;
     {
         const float dq = powf(p.scorr_dq * h, 2.f);
         const float t = C.h2 - dq;
-        C.scorr_wq = C.c_poly6 * t * t * t;
+        C.scorr_inv_wq = 1.0f / (C.c_poly6 * t * t * t);
     }
     C.delta_clamp = C.textbook ? -1.f : p.delta_clamp;  // textbook PBF has no per-pair clamp
+    C.delta_clamp2 = C.delta_clamp * C.delta_clamp;
     C.vort_eps = p.vorticity_eps;
     C.tension = p.surface_tension;
     C.xsph_c = p.xsph_c;
@@ -213,10 +218,13 @@ static SimConsts make_consts(const bp_solver *s, float sdt)
         C.nl_cell = s->nl_cell;
         C.nl_pos = s->nl_pos;
         C.nl_disp = s->nl_disp;
+        C.nl_flags = s->nl_flags;
         const float hs = h * (1.0f + p.neighbor_skin);
         const float half_skin = 0.5f * h * p.neighbor_skin;
+        const float contact = 2.0f * p.particle_radius + h * p.neighbor_skin;
         C.nl_hs2 = hs * hs;
         C.nl_half_skin2 = half_skin * half_skin;
+        C.nl_contact2 = contact * contact;
     }
     C.nplanes = (p.stage_mask & BP_STAGE_PLANES) ? s->nplanes : 0;
     for (int k = 0; k < s->nplanes; ++k) {
@@ -335,7 +343,8 @@ extern "C" bp_status bp_solver_create(const bp_scene_desc *sc, const bp_params *
         (st = s->alloc(&s->off, ncells + 1)) || (st = s->alloc(&s->mass, N)) || (st = s->alloc(&s->lam, N)) ||
         (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)) ||
         (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->nl_mask, 9 * N)) ||
-        (st = s->alloc(&s->nl_cell, N)) || (st = s->alloc(&s->nl_pos, N)) || (st = s->alloc(&s->nl_disp, 1)))
+        (st = s->alloc(&s->nl_cell, N)) || (st = s->alloc(&s->nl_pos, N)) || (st = s->alloc(&s->nl_disp, 1)) ||
+        (st = s->alloc(&s->nl_flags, N)) || (st = s->alloc(&s->nl_stats, 2)))
         return bail(st);
     {
         char *scratch = nullptr;
@@ -567,11 +576,12 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
 }
 
 static bp_status enqueue_update(bp_solver *s, int nsub, float dt, int iterations, int picked, float3 ppos,
-                                float3 pvel, LaunchLog *L)
+                                float3 pvel, LaunchLog *L, bool walk_stats = false)
 {
     const float sdt = dt / (float)nsub;
     SimConsts C = make_consts(s, sdt);
     if (picked >= 0) C.nl_mask = nullptr;  // the picked particle teleports: walk the cells
+    if (walk_stats) C.nl_stats = s->nl_stats;
     for (int k = 0; k < nsub; ++k) enqueue_substep(s, C, iterations, picked, ppos, L);
     if (picked >= 0) launch_pick(s->stream, picked, s->to_new, s->Xc, ppos, 0, s->Vc, pvel, L);
     launch_check_finite(s->stream, s->n, s->Xc, s->err, L);
@@ -666,6 +676,26 @@ extern "C" bp_status bp_solver_profile(bp_solver *s, int32_t nsub, float dt, int
     const int m = (int)agg.size() < capacity ? (int)agg.size() : capacity;
     for (int k = 0; k < m; ++k) out[k] = agg[k];
     *count = (int)agg.size();
+    s->last_launches = L.count;
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_walk_stats(bp_solver *s, int32_t nsub, float dt, int32_t iterations,
+                                          uint64_t out_walks[2])
+{
+    if (!s || !out_walks) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (nsub <= 0 || !(dt > 0.f) || iterations < 0) return fail(BP_ERR_INVALID_ARGUMENT, "bad step arguments");
+    out_walks[0] = out_walks[1] = 0;
+    if (s->n <= 0) return BP_OK;
+    LaunchLog L;
+    L.stream = s->stream;
+    BP_CUDA(cudaMemsetAsync(s->nl_stats, 0, 2 * sizeof(unsigned), s->stream));
+    enqueue_update(s, nsub, dt, iterations, -1, make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), &L, true);
+    unsigned h[2];
+    BP_CUDA(cudaMemcpyAsync(h, s->nl_stats, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    out_walks[0] = h[0];
+    out_walks[1] = h[1];
     s->last_launches = L.count;
     return BP_OK;
 }

@@ -226,6 +226,12 @@ typedef struct bp_stage_time {
 bp_status bp_solver_profile(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
                             int32_t capacity, bp_stage_time *out, int32_t *count);
 
+/* One real update that also counts the neighbour walks of every scan pass:
+ * out_walks[0] walks over the per-substep neighbour masks, out_walks[1]
+ * walks over the 27 cells (mask not valid for the particle). */
+bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
+                               uint64_t out_walks[2]);
+
 /* ---- Stand-alone hash grid on caller-owned device buffers ---------------
  * Replaces updateGrid() (particlesolver.cuh:712-765): updateGridId
  * (kernel/grid.cuh:30-47), the CUB stable radix sort (particlesolver.cuh:721-738)
