@@ -233,7 +233,7 @@ def run_ours(args):
     achieved = (bytes_per * n / (avg_ms / 1e3) / 1e9) if bytes_per else None
     traffic = traffic_for(top_name, n)
     step_ms_total = sum(v[1] for v in agg.values()) / prof_steps
-    masked, cell_walks = solver.walk_stats(SUBSTEPS, DT, ITERATIONS)
+    walks = solver.walk_stats(SUBSTEPS, DT, ITERATIONS)
     solver.close()
 
     result = None
@@ -266,7 +266,7 @@ def run_ours(args):
             "stages_ms_per_step": {k: round(v[1] / prof_steps, 4) for k, v in
                                    sorted(agg.items(), key=lambda kv: -kv[1][1])},
             "profiled_ms_per_step": step_ms_total,
-            "neighbor_walks": {"masked": masked, "cells": cell_walks},
+            "neighbor_walks": walks,
             "cpu_baseline": cpu,
             "clocks": clk,
         }

@@ -208,12 +208,20 @@ __device__ __forceinline__ void for_each_candidate_from(float3 pi, int lo, const
     }
 }
 
-// True when particle i may walk its neighbour bitmasks instead of its 27 cells.
+// 0 when particle i may walk its neighbour bitmasks instead of its 27 cells;
+// otherwise why not: 1 no masks for it, 2 it changed cell, 3 some particle
+// moved more than half the skin since the build.
+__device__ __forceinline__ int masks_state(const SimConsts &C, int i, int3 c)
+{
+    const int built = __ldg(C.nl_cell + i);
+    if (built < 0) return 1;
+    if (built != cell_addr(c.x, c.y, c.z, C.D, C.mask)) return 2;
+    if (*C.nl_disp > __float_as_uint(C.nl_half_skin2)) return 3;
+    return 0;
+}
 __device__ __forceinline__ bool masks_usable(const SimConsts &C, int i, int3 c)
 {
-    if (!C.nl_mask) return false;
-    if (*C.nl_disp > __float_as_uint(C.nl_half_skin2)) return false;
-    return __ldg(C.nl_cell + i) == cell_addr(c.x, c.y, c.z, C.D, C.mask);
+    return C.nl_mask && masks_state(C, i, c) == 0;
 }
 
 // Candidate walk of particle i: the set bits of its neighbour masks when
@@ -225,9 +233,9 @@ __device__ __forceinline__ void for_each_neighbor(int i, float3 pi, int lo, cons
                                                   const SimConsts &C, F &&f)
 {
     const int3 c = cell_of(pi, C);
-    const bool usable = masks_usable(C, i, c);
-    if (C.nl_stats) atomicAdd(C.nl_stats + (usable ? 0 : 1), 1u);
-    if (usable) {
+    const int state = C.nl_mask ? masks_state(C, i, c) : 1;
+    if (C.nl_stats) atomicAdd(C.nl_stats + state, 1u);
+    if (state == 0) {
         // One loop over all set bits of the 9 masks (advancing to the next
         // column when the current one is exhausted), so the lanes of a warp
         // diverge only on their total neighbour count.

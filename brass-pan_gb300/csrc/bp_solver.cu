@@ -344,7 +344,7 @@ extern "C" bp_status bp_solver_create(const bp_scene_desc *sc, const bp_params *
         (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)) ||
         (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->nl_mask, 9 * N)) ||
         (st = s->alloc(&s->nl_cell, N)) || (st = s->alloc(&s->nl_pos, N)) || (st = s->alloc(&s->nl_disp, 1)) ||
-        (st = s->alloc(&s->nl_flags, N)) || (st = s->alloc(&s->nl_stats, 2)))
+        (st = s->alloc(&s->nl_flags, N)) || (st = s->alloc(&s->nl_stats, 4)))
         return bail(st);
     {
         char *scratch = nullptr;
@@ -517,8 +517,14 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
 
     float4 *cur = s->Pa, *other = s->Pb;
     if (wind) launch_wind(st, C, s->wind, cur, s->Vs, s->mass, s->to_new, L);
+    // masks are built at the positions the first scan sees: after the wind
+    // and iteration 0's plane collision, which move particles the most
     const bool scans = pcoll || fluid || C.use_vort || C.use_akinci || C.use_xsph;
-    if (scans && C.nl_mask) launch_build_masks(st, C, cur, s->off, L);
+    bool masks_built = !(scans && C.nl_mask);
+    if (!masks_built && (fuse_first_planes || !planes || iterations == 0)) {
+        launch_build_masks(st, C, cur, s->off, L);
+        masks_built = true;
+    }
 
     bool planes_done = fuse_first_planes;
     bool committed = false;
@@ -526,6 +532,10 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
         if (picking) launch_pick(st, picked, s->to_new, cur, ppos, 1, nullptr, make_float3(0.f, 0.f, 0.f), L);
         if (planes && !planes_done) launch_planes(st, C, s->Xs, cur, L);
         planes_done = false;
+        if (!masks_built) {
+            launch_build_masks(st, C, cur, s->off, L);
+            masks_built = true;
+        }
         if (pcoll) {
             launch_particle_collision(st, C, cur, s->Xs, s->w, s->off, other, L);
             std::swap(cur, other);
@@ -681,21 +691,20 @@ extern "C" bp_status bp_solver_profile(bp_solver *s, int32_t nsub, float dt, int
 }
 
 extern "C" bp_status bp_solver_walk_stats(bp_solver *s, int32_t nsub, float dt, int32_t iterations,
-                                          uint64_t out_walks[2])
+                                          uint64_t out_walks[4])
 {
     if (!s || !out_walks) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
     if (nsub <= 0 || !(dt > 0.f) || iterations < 0) return fail(BP_ERR_INVALID_ARGUMENT, "bad step arguments");
-    out_walks[0] = out_walks[1] = 0;
+    for (int k = 0; k < 4; ++k) out_walks[k] = 0;
     if (s->n <= 0) return BP_OK;
     LaunchLog L;
     L.stream = s->stream;
-    BP_CUDA(cudaMemsetAsync(s->nl_stats, 0, 2 * sizeof(unsigned), s->stream));
+    BP_CUDA(cudaMemsetAsync(s->nl_stats, 0, 4 * sizeof(unsigned), s->stream));
     enqueue_update(s, nsub, dt, iterations, -1, make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), &L, true);
-    unsigned h[2];
+    unsigned h[4];
     BP_CUDA(cudaMemcpyAsync(h, s->nl_stats, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
     BP_CUDA(cudaStreamSynchronize(s->stream));
-    out_walks[0] = h[0];
-    out_walks[1] = h[1];
+    for (int k = 0; k < 4; ++k) out_walks[k] = h[k];
     s->last_launches = L.count;
     return BP_OK;
 }

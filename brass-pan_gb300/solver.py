@@ -142,11 +142,12 @@ class ParticleSolver:
                                                        buf, C.byref(count)))
         return {buf[k].name.decode(): (buf[k].launches, buf[k].total_ms) for k in range(min(cap, count.value))}
 
-    def walk_stats(self, num_substeps: int, dt: float, iterations: int) -> tuple[int, int]:
-        """One real update counting (masked walks, 27-cell walks) over all scan passes."""
-        out = (C.c_uint64 * 2)()
+    def walk_stats(self, num_substeps: int, dt: float, iterations: int) -> dict[str, int]:
+        """One real update counting the neighbour walks of all scan passes by kind."""
+        out = (C.c_uint64 * 4)()
         abi.check(self.lib, self.lib.bp_solver_walk_stats(self.handle, num_substeps, C.c_float(dt), iterations, out))
-        return int(out[0]), int(out[1])
+        return {"masked": int(out[0]), "cells_no_mask": int(out[1]), "cells_moved_cell": int(out[2]),
+                "cells_displaced": int(out[3])}
 
     def pack_particle_infos(self, device_ptr: int):
         abi.check(self.lib, self.lib.bp_solver_pack_particle_infos(self.handle, C.c_void_p(device_ptr)))

@@ -227,10 +227,12 @@ bp_status bp_solver_profile(bp_solver *s, int32_t num_substeps, float dt, int32_
                             int32_t capacity, bp_stage_time *out, int32_t *count);
 
 /* One real update that also counts the neighbour walks of every scan pass:
- * out_walks[0] walks over the per-substep neighbour masks, out_walks[1]
- * walks over the 27 cells (mask not valid for the particle). */
+ * out_walks[0] walks over the per-substep neighbour masks; 27-cell walks
+ * because [1] no mask was built for the particle (a column run wraps around
+ * the table or holds more than 64 candidates), [2] the particle left the cell
+ * its masks were built for, [3] some particle moved more than half the skin. */
 bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
-                               uint64_t out_walks[2]);
+                               uint64_t out_walks[4]);
 
 /* ---- Stand-alone hash grid on caller-owned device buffers ---------------
  * Replaces updateGrid() (particlesolver.cuh:712-765): updateGridId
