@@ -47,20 +47,21 @@ struct SimConsts {
     float4 plane_o[kMaxPlanes];
     float4 plane_n[kMaxPlanes];
     // Neighbour bitmasks of the current substep (nl_mask == nullptr: off).
-    // For each particle and each of its 9 column runs, bit t of
-    // nl_mask[col * n + i] marks candidate off[start] + t within h + skin of
-    // it at build time; nl_cell is the cell the masks were built for (-1: the
-    // particle always walks its 27 cells), nl_pos the positions at build,
-    // and *nl_disp the largest squared displacement since the build (float
-    // bits).  A masked walk is taken only while the particle is still in
-    // nl_cell and *nl_disp <= (skin/2)^2, which guarantees that every pair
-    // within h is flagged.
-    unsigned long long *nl_mask;
+    // For each particle and each of its 9 column runs, bit t of the column's
+    // two words marks candidate off[start] + t within h + skin of it at build
+    // time; nl_cell is the cell the masks were built for (-1: the particle
+    // always walks its 27 cells), nl_pos the positions at build.  A masked
+    // walk is taken while the particle is still in nl_cell and within half
+    // the skin of nl_pos; columns holding a particle that moved further are
+    // walked whole (see for_each_neighbor).
+    unsigned long long *nl_mask;       // [18][n]: column c uses words 2c and 2c+1 (128 candidates)
     int *nl_cell;
     float4 *nl_pos;
-    unsigned *nl_disp;
+    unsigned long long *nl_outlier;    // per (x, y) column of cells, nl_zwords words of z bits
+    int nl_zwords;                     // ceil(D / 64)
+    const int *cell_keys;              // stored cell of every sorted particle
     unsigned char *nl_flags; // kFlagContact: a contact partner within 2r + skin at build
-    unsigned *nl_stats;      // profiling only: [0] masked walks, [1] cell walks
+    unsigned *nl_stats;      // profiling only: walks by masks_state
     float nl_hs2;            // (h + skin)^2
     float nl_half_skin2;     // (skin / 2)^2
     float nl_contact2;       // (2r + skin)^2
@@ -208,52 +209,93 @@ __device__ __forceinline__ void for_each_candidate_from(float3 pi, int lo, const
     }
 }
 
+// Is any of the cells (x, y, z0..z0+2) flagged as holding an outlier (a
+// particle that moved more than half the skin since the masks were built)?
+__device__ __forceinline__ bool column_has_outlier(const SimConsts &C, unsigned x, unsigned y, unsigned z0)
+{
+    const unsigned long long *w = C.nl_outlier + (size_t)(x * (unsigned)C.D + y) * C.nl_zwords;
+    const unsigned k = z0 >> 6, s = z0 & 63u;
+    unsigned long long bits = __ldcg(w + k) >> s;
+    if (s > 61u && k + 1 < (unsigned)C.nl_zwords) bits |= __ldcg(w + k + 1) << (64u - s);
+    return (bits & 7ull) != 0ull;
+}
+
+// Does any column run around the cell of p hold an outlier?
+__device__ __forceinline__ bool contact_outlier_near(const SimConsts &C, float3 p)
+{
+    const int3 c = cell_of(p, C);
+    const unsigned m = C.mask;
+    const unsigned z0 = (unsigned)(c.z - 1) & m;
+    for (int col = 0; col < 9; ++col)
+        if (column_has_outlier(C, (unsigned)(c.x + col / 3 - 1) & m, (unsigned)(c.y + col % 3 - 1) & m, z0))
+            return true;
+    return false;
+}
+
 // 0 when particle i may walk its neighbour bitmasks instead of its 27 cells;
-// otherwise why not: 1 no masks for it, 2 it changed cell, 3 some particle
-// moved more than half the skin since the build.
-__device__ __forceinline__ int masks_state(const SimConsts &C, int i, int3 c)
+// otherwise why not: 1 no masks for it, 2 it changed cell, 3 it moved more
+// than half the skin since the build (an outlier).
+__device__ __forceinline__ int masks_state(const SimConsts &C, int i, int3 c, float3 pi)
 {
     const int built = __ldg(C.nl_cell + i);
     if (built < 0) return 1;
     if (built != cell_addr(c.x, c.y, c.z, C.D, C.mask)) return 2;
-    if (*C.nl_disp > __float_as_uint(C.nl_half_skin2)) return 3;
+    if (len2(pi - f3(C.nl_pos[i])) > C.nl_half_skin2) return 3;
     return 0;
 }
-__device__ __forceinline__ bool masks_usable(const SimConsts &C, int i, int3 c)
+__device__ __forceinline__ bool masks_usable(const SimConsts &C, int i, int3 c, float3 pi)
 {
-    return C.nl_mask && masks_state(C, i, c) == 0;
+    return C.nl_mask && masks_state(C, i, c, pi) == 0;
 }
 
 // Candidate walk of particle i: the set bits of its neighbour masks when
-// they are valid, else the 27-cell walk.  Both visit candidates column by
-// column in ascending sorted index, so every pair sum accumulates in the same
-// order either way; only indices j >= lo are visited.
+// they are valid, else the 27-cell walk.  A masked walk takes a column run
+// whole (every candidate, as the cell walk does) when one of its three cells
+// holds an outlier, because an outlier may have come within h without being
+// flagged; a pair of non-outliers moved by at most the skin in total, so
+// their masks flag every pair within h.  Both walks visit candidates column
+// by column in ascending sorted index, so every pair sum accumulates in the
+// same order either way; only indices j >= lo are visited.
 template <class F>
 __device__ __forceinline__ void for_each_neighbor(int i, float3 pi, int lo, const int *__restrict__ off,
                                                   const SimConsts &C, F &&f)
 {
     const int3 c = cell_of(pi, C);
-    const int state = C.nl_mask ? masks_state(C, i, c) : 1;
+    const int state = C.nl_mask ? masks_state(C, i, c, pi) : 1;
     if (C.nl_stats) atomicAdd(C.nl_stats + state, 1u);
     if (state == 0) {
-        // One loop over all set bits of the 9 masks (advancing to the next
-        // column when the current one is exhausted), so the lanes of a warp
-        // diverge only on their total neighbour count.
+        // One loop over all set bits of the 9 columns x 2 words (moving on
+        // when a word is exhausted), so the lanes of a warp diverge only on
+        // their total neighbour count.
         const unsigned m = C.mask;
         const unsigned D = (unsigned)C.D;
         const unsigned z0 = (unsigned)(c.z - 1) & m;  // no wrap: masks are never built across it
         int col = -1, b = 0;
-        unsigned long long bits = 0ull;
+        unsigned long long bits = 0ull, next = 0ull;
+        bool second = true;
 #pragma unroll 1
         while (true) {
             while (bits == 0ull) {
-                if (++col == 9) return;
-                bits = C.nl_mask[(size_t)col * C.n + i];
-                if (bits) {
-                    const int dx = col / 3 - 1, dy = col % 3 - 1;
-                    b = __ldg(off + ((unsigned)(c.x + dx) & m) * D * D + ((unsigned)(c.y + dy) & m) * D + z0);
-                    if (lo > b) bits = (lo - b >= 64) ? 0ull : bits & (~0ull << (lo - b));
+                if (!second) {  // second word of the current column
+                    second = true;
+                    bits = next;
+                    b += 64;
+                } else {
+                    if (++col == 9) return;
+                    second = false;
+                    const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
+                    const unsigned base = x * D * D + y * D + z0;
+                    b = __ldg(off + base);
+                    if (column_has_outlier(C, x, y, z0)) {
+                        const int len = __ldg(off + base + 3) - b;  // <= 128: the masks were built
+                        bits = len >= 64 ? ~0ull : ((1ull << len) - 1ull);
+                        next = len > 64 ? (len >= 128 ? ~0ull : ((1ull << (len - 64)) - 1ull)) : 0ull;
+                    } else {
+                        bits = C.nl_mask[(size_t)(2 * col) * C.n + i];
+                        next = C.nl_mask[(size_t)(2 * col + 1) * C.n + i];
+                    }
                 }
+                if (lo > b) bits = (lo - b >= 64) ? 0ull : bits & (~0ull << (lo - b));
             }
             const int t = __ffsll((long long)bits) - 1;
             bits &= bits - 1;
@@ -266,15 +308,18 @@ __device__ __forceinline__ void for_each_neighbor(int i, float3 pi, int lo, cons
         for_each_candidate(pi, off, C, f);
 }
 
-// Records how far particle i has moved from its position at mask build;
-// writers of P call it with the new position (inactive lanes pass false).
+// Records that particle i moved more than half the skin since the mask
+// build: flags its stored cell (the cell its sorted index belongs to) so
+// walks over that cell's column take every candidate.  Writers of P call it
+// with the new position.
 __device__ __forceinline__ void track_displacement(const SimConsts &C, int i, float3 p, bool active)
 {
-    if (!C.nl_mask) return;
-    const float d2 = active ? len2(p - f3(C.nl_pos[i])) : 0.f;
-    const unsigned am = __activemask();
-    const unsigned u = __reduce_max_sync(am, __float_as_uint(d2));  // NaN bits exceed every finite value
-    if ((threadIdx.x & 31) == (unsigned)(__ffs(am) - 1) && u > 0u) atomicMax(C.nl_disp, u);
+    if (!C.nl_mask || !active) return;
+    if (!(len2(p - f3(C.nl_pos[i])) <= C.nl_half_skin2)) {  // NaN counts as moved
+        const unsigned key = (unsigned)__ldg(C.cell_keys + i);
+        const unsigned col = key / (unsigned)C.D, z = key % (unsigned)C.D;
+        atomicOr(C.nl_outlier + (size_t)col * C.nl_zwords + (z >> 6), 1ull << (z & 63u));
+    }
 }
 
 // Plane walls: planeStabilize / particlePlaneCollisionConstraint

@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(128) k_particle_collision(SimConsts C, const f
     // No contact partner within 2r + skin at mask build and the masks still
     // valid: no pair can be closer than 2r now, the walk would find nothing.
     const bool none = C.nl_mask && C.nl_flags && !(C.nl_flags[i] & kFlagContact) &&
-                      masks_usable(C, i, cell_of(xip, C));
+                      masks_usable(C, i, cell_of(xip, C), xip) && !contact_outlier_near(C, xip);
     if (!none) for_each_neighbor(i, xip, 0, off, C, [&](int j) {
         const float4 pj4 = P[j];
         const int phj = phase_of(pj4);

@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs 
 
 // Neighbour bitmasks for the rest of the substep (see SimConsts::nl_mask):
 // one 27-cell walk at the positions of the first iteration.  Particles whose
-// column runs wrap around the table in z, or hold more than 64 candidates,
+// column runs wrap around the table in z, or hold more than 128 candidates,
 // keep walking their cells.
 __global__ void __launch_bounds__(kScanThreads) k_build_masks(SimConsts C, const float4 *__restrict__ P,
                                                               const int *__restrict__ off)
@@ -156,25 +156,26 @@ __global__ void __launch_bounds__(kScanThreads) k_build_masks(SimConsts C, const
         const unsigned bx = ((unsigned)(c.x + dx) & m) * D * D;
 #pragma unroll 1
         for (int dy = -1; dy <= 1; ++dy, ++col) {
-            unsigned long long bits = 0ull;
+            unsigned long long bits[2] = {0ull, 0ull};
             if (ok) {
                 const unsigned base = bx + ((unsigned)(c.y + dy) & m) * D;
                 const int b = __ldg(off + base + z0), e = __ldg(off + base + z2 + 1);
-                if (e - b > 64) {
+                if (e - b > 128) {
                     ok = false;
                 } else {
 #pragma unroll 1
                     for (int j = b; j < e; ++j) {
                         const float4 pj4 = P[j];
                         const float d2 = len2(pi - f3(pj4));
-                        if (d2 <= C.nl_hs2) bits |= 1ull << (j - b);
+                        if (d2 <= C.nl_hs2) bits[(j - b) >> 6] |= 1ull << ((j - b) & 63);
                         const int phj = phase_of(pj4);
                         if (d2 <= C.nl_contact2 && j != i && phi != phj && (phi > 0 || phj > 0))
                             flags |= kFlagContact;
                     }
                 }
             }
-            C.nl_mask[(size_t)col * C.n + i] = bits;
+            C.nl_mask[(size_t)(2 * col) * C.n + i] = bits[0];
+            C.nl_mask[(size_t)(2 * col + 1) * C.n + i] = bits[1];
         }
     }
     C.nl_cell[i] = ok ? cell_addr(c.x, c.y, c.z, C.D, C.mask) : -1;
@@ -184,7 +185,7 @@ __global__ void __launch_bounds__(kScanThreads) k_build_masks(SimConsts C, const
 void launch_build_masks(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, LaunchLog *L)
 {
     if (C.n <= 0 || !C.nl_mask) return;
-    cudaMemsetAsync(C.nl_disp, 0, sizeof(unsigned), st);
+    cudaMemsetAsync(C.nl_outlier, 0, (size_t)C.D * C.D * C.nl_zwords * sizeof(unsigned long long), st);
     k_build_masks<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, off);
     L->done(__func__);
 }

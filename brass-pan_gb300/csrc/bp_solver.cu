@@ -56,10 +56,10 @@ struct bp_solver {
     int *keys = nullptr, *sorted_keys = nullptr, *order = nullptr, *off = nullptr;
     float *mass = nullptr, *lam = nullptr, *rho = nullptr, *w = nullptr;
     float *staging = nullptr;  // 2 x N x 3 floats for host copies
-    unsigned long long *nl_mask = nullptr;  // neighbour masks [9][N]
+    unsigned long long *nl_mask = nullptr;  // neighbour masks [18][N]
     int *nl_cell = nullptr;
     float4 *nl_pos = nullptr;
-    unsigned *nl_disp = nullptr;
+    unsigned long long *nl_outlier = nullptr;  // outlier cell bits [D*D][ceil(D/64)]
     unsigned char *nl_flags = nullptr;
     unsigned *nl_stats = nullptr;
     unsigned *err = nullptr;
@@ -217,7 +217,9 @@ static SimConsts make_consts(const bp_solver *s, float sdt)
         C.nl_mask = s->nl_mask;
         C.nl_cell = s->nl_cell;
         C.nl_pos = s->nl_pos;
-        C.nl_disp = s->nl_disp;
+        C.nl_outlier = s->nl_outlier;
+        C.nl_zwords = (p.grid_dim + 63) / 64;
+        C.cell_keys = s->sorted_keys;
         C.nl_flags = s->nl_flags;
         const float hs = h * (1.0f + p.neighbor_skin);
         const float half_skin = 0.5f * h * p.neighbor_skin;
@@ -342,8 +344,8 @@ extern "C" bp_status bp_solver_create(const bp_scene_desc *sc, const bp_params *
         (st = s->alloc(&s->keys, N)) || (st = s->alloc(&s->sorted_keys, N)) || (st = s->alloc(&s->order, N)) ||
         (st = s->alloc(&s->off, ncells + 1)) || (st = s->alloc(&s->mass, N)) || (st = s->alloc(&s->lam, N)) ||
         (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)) ||
-        (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->nl_mask, 9 * N)) ||
-        (st = s->alloc(&s->nl_cell, N)) || (st = s->alloc(&s->nl_pos, N)) || (st = s->alloc(&s->nl_disp, 1)) ||
+        (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->nl_mask, 18 * N)) ||
+        (st = s->alloc(&s->nl_cell, N)) || (st = s->alloc(&s->nl_pos, N)) || (st = s->alloc(&s->nl_outlier, (size_t)D * D * ((D + 63) / 64))) ||
         (st = s->alloc(&s->nl_flags, N)) || (st = s->alloc(&s->nl_stats, 4)))
         return bail(st);
     {
