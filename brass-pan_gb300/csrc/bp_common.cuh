@@ -60,14 +60,16 @@ struct SimConsts {
     unsigned long long *nl_outlier;    // per (x, y) column of cells, nl_zwords words of z bits
     int nl_zwords;                     // ceil(D / 64)
     const int *cell_keys;              // stored cell of every sorted particle
-    unsigned char *nl_flags; // kFlagContact: a contact partner within 2r + skin at build
+    unsigned short *nl_flags; // kFlagContact: a contact partner within 2r + skin at build;
+                              // kFlagWide << col: column run col holds more than 64 candidates
     unsigned *nl_stats;      // profiling only: walks by masks_state
     float nl_hs2;            // (h + skin)^2
     float nl_half_skin2;     // (skin / 2)^2
     float nl_contact2;       // (2r + skin)^2
 };
 
-constexpr unsigned char kFlagContact = 1;
+constexpr unsigned short kFlagContact = 1;
+constexpr unsigned short kFlagWide = 2;
 
 // ---- small vector helpers (own code; component-wise, left-to-right dot) ----
 
@@ -215,8 +217,10 @@ __device__ __forceinline__ bool column_has_outlier(const SimConsts &C, unsigned 
 {
     const unsigned long long *w = C.nl_outlier + (size_t)(x * (unsigned)C.D + y) * C.nl_zwords;
     const unsigned k = z0 >> 6, s = z0 & 63u;
-    unsigned long long bits = __ldcg(w + k) >> s;
-    if (s > 61u && k + 1 < (unsigned)C.nl_zwords) bits |= __ldcg(w + k + 1) << (64u - s);
+    // flags written by earlier kernels; a flag set during this kernel concerns
+    // positions this kernel does not read, so a stale read is harmless
+    unsigned long long bits = __ldg(w + k) >> s;
+    if (s > 61u && k + 1 < (unsigned)C.nl_zwords) bits |= __ldg(w + k + 1) << (64u - s);
     return (bits & 7ull) != 0ull;
 }
 
@@ -273,6 +277,7 @@ __device__ __forceinline__ void for_each_neighbor(int i, float3 pi, int lo, cons
         int col = -1, b = 0;
         unsigned long long bits = 0ull, next = 0ull;
         bool second = true;
+        const unsigned wide = __ldg(C.nl_flags + i);
 #pragma unroll 1
         while (true) {
             while (bits == 0ull) {
@@ -291,8 +296,8 @@ __device__ __forceinline__ void for_each_neighbor(int i, float3 pi, int lo, cons
                         bits = len >= 64 ? ~0ull : ((1ull << len) - 1ull);
                         next = len > 64 ? (len >= 128 ? ~0ull : ((1ull << (len - 64)) - 1ull)) : 0ull;
                     } else {
-                        bits = C.nl_mask[(size_t)(2 * col) * C.n + i];
-                        next = C.nl_mask[(size_t)(2 * col + 1) * C.n + i];
+                        bits = __ldg(C.nl_mask + (size_t)(2 * col) * C.n + i);
+                        next = (wide & (kFlagWide << col)) ? __ldg(C.nl_mask + (size_t)(2 * col + 1) * C.n + i) : 0ull;
                     }
                 }
                 if (lo > b) bits = (lo - b >= 64) ? 0ull : bits & (~0ull << (lo - b));

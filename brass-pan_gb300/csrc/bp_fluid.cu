@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kScanThreads) k_build_masks(SimConsts C, const
     const unsigned z0 = (unsigned)(c.z - 1) & m;
     const unsigned z2 = (unsigned)(c.z + 1) & m;
     bool ok = z0 < z2;
-    unsigned char flags = 0;
+    unsigned short flags = 0;
     int col = 0;
 #pragma unroll 1
     for (int dx = -1; dx <= 1; ++dx) {
@@ -163,6 +163,7 @@ __global__ void __launch_bounds__(kScanThreads) k_build_masks(SimConsts C, const
                 if (e - b > 128) {
                     ok = false;
                 } else {
+                    if (e - b > 64) flags |= (unsigned short)(kFlagWide << col);
 #pragma unroll 1
                     for (int j = b; j < e; ++j) {
                         const float4 pj4 = P[j];

@@ -60,7 +60,7 @@ struct bp_solver {
     int *nl_cell = nullptr;
     float4 *nl_pos = nullptr;
     unsigned long long *nl_outlier = nullptr;  // outlier cell bits [D*D][ceil(D/64)]
-    unsigned char *nl_flags = nullptr;
+    unsigned short *nl_flags = nullptr;
     unsigned *nl_stats = nullptr;
     unsigned *err = nullptr;
     SortScratch sort{};
