@@ -13,6 +13,7 @@
 // thread per constraint computes its correction once, then one thread per
 // affected particle sums its incident corrections in a fixed (CSR) order.
 #include "bp_internal.h"
+#include "bp_walk.cuh"
 
 namespace bp {
 
@@ -61,12 +62,16 @@ void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // than two radii; mass-weighted projection plus friction averaged over the
 // counted contacts; only particle i moves (the reference's j update is
 // commented out).  Reads P, writes Pout = P + delta.
-__global__ void __launch_bounds__(128) k_particle_collision(SimConsts C, const float4 *__restrict__ P,
-                                                            const float4 *__restrict__ Xs,
-                                                            const float *__restrict__ w,
-                                                            const int *__restrict__ off, float4 *__restrict__ Pout)
+__global__ void __launch_bounds__(kWalkThreads) k_particle_collision(SimConsts C, const float4 *__restrict__ P,
+                                                                     const float4 *__restrict__ Xs,
+                                                                     const float *__restrict__ w,
+                                                                     const int *__restrict__ off,
+                                                                     float4 *__restrict__ Pout)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ StageShared S;
+    const int i0 = blockIdx.x * kWalkThreads;
+    const int g = stage_block(C, P, off, i0, S);
+    const int i = i0 + threadIdx.x;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
     const float3 xip = f3(pi4);
@@ -80,8 +85,7 @@ __global__ void __launch_bounds__(128) k_particle_collision(SimConsts C, const f
     // valid: no pair can be closer than 2r now, the walk would find nothing.
     const bool none = C.nl_mask && C.nl_flags && !(C.nl_flags[i] & kFlagContact) &&
                       masks_usable(C, i, cell_of(xip, C), xip) && !contact_outlier_near(C, xip);
-    if (!none) for_each_neighbor(i, xip, 0, off, C, [&](int j) {
-        const float4 pj4 = P[j];
+    if (!none) walk_neighbors(i, xip, 0, P, off, C, &S, g, [&](int j, float4 pj4) {
         const int phj = phase_of(pj4);
         if (!(j != i && phi != phj && (phi > 0 || phj > 0))) return;
         const float3 xjp = f3(pj4);
@@ -122,7 +126,7 @@ void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4
                                const float *w, const int *off, float4 *Pout, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    k_particle_collision<<<(C.n + 127) / 128, 128, 0, st>>>(C, P, Xs, w, off, Pout);
+    k_particle_collision<<<(C.n + kWalkThreads - 1) / kWalkThreads, kWalkThreads, 0, st>>>(C, P, Xs, w, off, Pout);
     L->done(__func__);
 }
 

@@ -14,10 +14,11 @@
 // term for (k, j) is bit-identical to the reference's term for (j, k) up to
 // sign, because the spiky gradient is odd in the difference vector.
 #include "bp_internal.h"
+#include "bp_walk.cuh"
 
 namespace bp {
 
-constexpr int kScanThreads = 128;
+constexpr int kScanThreads = kWalkThreads;  // scan kernels stage their neighbourhood (bp_walk.cuh)
 
 // Reference mode (Q1): density sums only sorted indices j >= i; solid
 // neighbours count x solid_scale; C = rho/rho0 - 1, clamped at 0 when Akinci
@@ -27,7 +28,10 @@ __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const floa
                                                          const int *__restrict__ off, float *__restrict__ lam,
                                                          float *__restrict__ rho)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ StageShared S;
+    const int i0 = blockIdx.x * kScanThreads;
+    const int g = stage_block(C, P, off, i0, S);
+    const int i = i0 + threadIdx.x;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
     if (phase_of(pi4) > 0) {  // solids carry lambda 0 (read by the position pass)
@@ -37,8 +41,7 @@ __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const floa
     const float3 pi = f3(pi4);
     float density = 0.f;
     if (!C.textbook) {
-        for_each_neighbor(i, pi, i, off, C, [&](int j) {
-            const float4 pj = P[j];
+        walk_neighbors(i, pi, i, P, off, C, &S, g, [&](int j, float4 pj) {
             const float d2 = len2(pi - f3(pj));
             if (d2 <= C.h2) {
                 const float ld = __ldg(mass + j) * poly6(C, d2);
@@ -51,8 +54,7 @@ __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const floa
     } else {
         float sum_g2 = 0.f;
         float3 gi = make_float3(0.f, 0.f, 0.f);
-        for_each_neighbor(i, pi, 0, off, C, [&](int j) {
-            const float4 pj = P[j];
+        walk_neighbors(i, pi, 0, P, off, C, &S, g, [&](int j, float4 pj) {
             const float3 diff = pi - f3(pj);
             const float d2 = len2(diff);
             if (d2 <= C.h2) {
@@ -89,7 +91,10 @@ void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // every neighbour; solids do not move.
 __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs a)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ StageShared S;
+    const int i0 = blockIdx.x * kScanThreads;
+    const int g = stage_block(C, a.P, a.off, i0, S);
+    const int k = i0 + threadIdx.x;
     if (k >= C.n) return;
     const float4 pk4 = a.P[k];
     const int phk = phase_of(pk4);
@@ -97,9 +102,8 @@ __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs 
     float3 sum = make_float3(0.f, 0.f, 0.f);
     if (!(C.textbook && phk > 0)) {
         const float lk = a.lam[k];
-        for_each_neighbor(k, pk, 0, a.off, C, [&](int j) {
+        walk_neighbors(k, pk, 0, a.P, a.off, C, &S, g, [&](int j, float4 pj4) {
             if (j == k) return;
-            const float4 pj4 = a.P[j];
             const float3 diff = pk - f3(pj4);
             const float d2 = len2(diff);
             if (d2 <= C.h2 && d2 > 0.f) {
@@ -206,7 +210,10 @@ __global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const floa
                                                          const float *__restrict__ rho, const int *__restrict__ off,
                                                          float4 *__restrict__ Om, float4 *__restrict__ Nm)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ StageShared S;
+    const int i0 = blockIdx.x * kScanThreads;
+    const int g = stage_block(C, P, off, i0, S);
+    const int i = i0 + threadIdx.x;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
     const int phi = phase_of(pi4);
@@ -215,8 +222,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const floa
     const float3 vi = f3(V[i]);
     float3 om = make_float3(0.f, 0.f, 0.f), nn = make_float3(0.f, 0.f, 0.f);
     const bool want_om = C.use_vort, want_n = C.use_akinci;
-    for_each_neighbor(i, pi, 0, off, C, [&](int j) {
-        const float4 pj4 = P[j];
+    walk_neighbors(i, pi, 0, P, off, C, &S, g, [&](int j, float4 pj4) {
         if (j == i || phase_of(pj4) != phi) return;
         const float3 diff = pi - f3(pj4);
         const float d2 = len2(diff);
@@ -241,7 +247,10 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
                                                          const float4 *__restrict__ Nm,
                                                          const int *__restrict__ off, float4 *__restrict__ Vout)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ StageShared S;
+    const int i0 = blockIdx.x * kScanThreads;
+    const int g = stage_block(C, P, off, i0, S);
+    const int i = i0 + threadIdx.x;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
     const float4 vi4 = V[i];
@@ -256,8 +265,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
     const float rhoi = ni4.w;
     float3 eta = make_float3(0.f, 0.f, 0.f), ft = make_float3(0.f, 0.f, 0.f);
     const bool want_v = C.use_vort, want_t = C.use_akinci;
-    for_each_neighbor(i, pi, 0, off, C, [&](int j) {
-        const float4 pj4 = P[j];
+    walk_neighbors(i, pi, 0, P, off, C, &S, g, [&](int j, float4 pj4) {
         if (j == i || phase_of(pj4) != phi) return;
         const float3 pj = f3(pj4);
         const float3 diff = pi - pj;
@@ -292,7 +300,10 @@ __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const floa
                                                          const int *__restrict__ off, const float *__restrict__ mass,
                                                          const float *__restrict__ rho, float4 *__restrict__ Vout)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ StageShared S;
+    const int i0 = blockIdx.x * kScanThreads;
+    const int g = stage_block(C, P, off, i0, S);
+    const int i = i0 + threadIdx.x;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
     const float4 vi4 = V[i];
@@ -303,8 +314,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const floa
     }
     const float3 pi = f3(pi4), vi = f3(vi4);
     float3 vn = make_float3(0.f, 0.f, 0.f);
-    for_each_neighbor(i, pi, 0, off, C, [&](int j) {
-        const float4 pj4 = P[j];
+    walk_neighbors(i, pi, 0, P, off, C, &S, g, [&](int j, float4 pj4) {
         if (j == i || phase_of(pj4) != phi) return;
         const float d2 = len2(pi - f3(pj4));
         if (d2 <= C.h2) {

@@ -213,13 +213,13 @@ static SimConsts make_consts(const bp_solver *s, float sdt)
     C.rot_iters = p.rotation_iterations;
     C.dt = sdt;
     C.inv_dt = 1.0f / sdt;
+    C.cell_keys = s->sorted_keys;  // stored cell of every particle (staged walks, masks)
     if (p.neighbor_skin > 0.f) {
         C.nl_mask = s->nl_mask;
         C.nl_cell = s->nl_cell;
         C.nl_pos = s->nl_pos;
         C.nl_outlier = s->nl_outlier;
         C.nl_zwords = (p.grid_dim + 63) / 64;
-        C.cell_keys = s->sorted_keys;
         C.nl_flags = s->nl_flags;
         const float hs = h * (1.0f + p.neighbor_skin);
         const float half_skin = 0.5f * h * p.neighbor_skin;

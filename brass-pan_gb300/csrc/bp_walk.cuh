@@ -1,0 +1,194 @@
+// bp_walk.cuh -- neighbour walks of the scan kernels, staged in shared memory.
+//
+// A CTA of kWalkThreads threads handles kWalkThreads consecutive particles of
+// the cell-sorted arrays.  Because cells are addressed x-major, those
+// particles lie in one or two (x, y) columns of the grid, over a run of z
+// cells; the 27-cell neighbourhoods of all of them are covered by at most 9
+// column runs per column (split in two where z wraps around the table).
+// stage_block() copies those runs of P into shared memory with coalesced
+// loads; every candidate read of the walk then comes from shared memory.
+// A CTA whose runs would not fit (three or more columns, or more than
+// kStageCap particles) and particles that left their stored cell read P from
+// global memory instead.
+//
+// Every walk visits the candidates of the 27 cells column by column, in
+// ascending sorted index within a column, or the subset of them flagged in
+// the particle's neighbour masks (see SimConsts::nl_mask); the pair sums of
+// the scan kernels therefore accumulate in the same order on every path.
+#pragma once
+
+#include "bp_common.cuh"
+
+namespace bp {
+
+constexpr int kWalkThreads = 256;
+constexpr int kStageCap = 2816;       // staged particles per CTA (44 KB)
+constexpr int kStageSegs = 2 * 9 * 2; // groups x columns x pieces
+
+struct StageShared {
+    float4 pos[kStageCap];
+    int gstart[kStageSegs];
+    int len[kStageSegs];
+    int sbase[kStageSegs];
+    int keys[kWalkThreads];
+    int first1;  // first thread of the second column group
+    int ngroups;
+    int ok;
+};
+
+// Collective: every thread of the CTA must call it (before any early exit).
+// Returns the calling thread's column group (0 or 1), or -1 when the CTA does
+// not use shared memory or the thread has no particle.
+__device__ __forceinline__ int stage_block(const SimConsts &C, const float4 *__restrict__ P,
+                                           const int *__restrict__ off, int i0, StageShared &S)
+{
+    const int t = threadIdx.x;
+    const int i = i0 + t;
+    const bool valid = i < C.n;
+    const unsigned D = (unsigned)C.D, m = C.mask;
+    const int key = valid ? __ldg(C.cell_keys + i) : -1;
+    S.keys[t] = key;
+    if (t == 0) S.first1 = kWalkThreads;
+    __syncthreads();
+    const bool boundary = valid && (t == 0 || (unsigned)key / D != (unsigned)S.keys[t - 1] / D);
+    const int G = __syncthreads_count(boundary);
+    if (boundary && t > 0) S.first1 = t;  // unique when G == 2
+    __syncthreads();
+    if (G < 1 || G > 2) return -1;
+    const int nvalid = min(kWalkThreads, C.n - i0);
+    if (t < G * 9) {
+        const int g = t / 9, k = t % 9;
+        const int tf = g == 0 ? 0 : S.first1;
+        const int tl = g == G - 1 ? nvalid - 1 : S.first1 - 1;
+        const unsigned kf = (unsigned)S.keys[tf], kl = (unsigned)S.keys[tl];
+        const unsigned colid = kf / D;
+        const unsigned x = colid / D, y = colid % D;
+        const int zlo = (int)(kf % D) - 1, zhi = (int)(kl % D) + 1;
+        const unsigned nx = (x + (unsigned)(k / 3) - 1u) & m, ny = (y + (unsigned)(k % 3) - 1u) & m;
+        const unsigned base = (nx * D + ny) * D;
+        const int a = max(zlo, 0), b = min(zhi, (int)D - 1);
+        const int sa = __ldg(off + base + a), ea = __ldg(off + base + b + 1);
+        int sb = 0, eb = 0;
+        if (zlo < 0 && zhi <= (int)D - 1) {  // wraps below: cell D-1
+            sb = __ldg(off + base + D - 1);
+            eb = __ldg(off + base + D);
+        } else if (zhi > (int)D - 1 && zlo >= 0) {  // wraps above: cell 0
+            sb = __ldg(off + base);
+            eb = __ldg(off + base + 1);
+        }
+        S.gstart[2 * t] = sa;
+        S.len[2 * t] = ea - sa;
+        S.gstart[2 * t + 1] = sb;
+        S.len[2 * t + 1] = eb - sb;
+    }
+    __syncthreads();
+    if (t == 0) {
+        int total = 0;
+        for (int s = 0; s < 2 * G * 9; ++s) {
+            S.sbase[s] = total;
+            total += S.len[s];
+        }
+        S.ok = total <= kStageCap;
+        S.ngroups = G;
+    }
+    __syncthreads();
+    if (!S.ok) return -1;
+    for (int s = 0; s < 2 * G * 9; ++s) {
+        const int gs = S.gstart[s], l = S.len[s], sb = S.sbase[s];
+        for (int u = t; u < l; u += kWalkThreads) S.pos[sb + u] = P[gs + u];
+    }
+    __syncthreads();
+    if (!valid) return -1;
+    return (G == 2 && t >= S.first1) ? 1 : 0;
+}
+
+// Shared-memory index of candidate run [b, e) of column k for group g, or -1.
+__device__ __forceinline__ int staged_index(const StageShared &S, int g, int k, int b, int e)
+{
+    const int s = 2 * (g * 9 + k);
+    if (b >= S.gstart[s] && e <= S.gstart[s] + S.len[s]) return S.sbase[s] + (b - S.gstart[s]);
+    if (b >= S.gstart[s + 1] && e <= S.gstart[s + 1] + S.len[s + 1]) return S.sbase[s + 1] + (b - S.gstart[s + 1]);
+    return -1;
+}
+
+// Walk of particle i (sorted index) at position pi over the candidates
+// j >= lo of its 27 cells; calls f(j, P[j]).  S / g come from stage_block
+// (S == nullptr: no staging).
+template <class F>
+__device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const float4 *__restrict__ P,
+                                               const int *__restrict__ off, const SimConsts &C,
+                                               const StageShared *S, int g, F &&f)
+{
+    const int3 c = cell_of(pi, C);
+    const unsigned m = C.mask;
+    const unsigned D = (unsigned)C.D;
+    const int addr = cell_addr(c.x, c.y, c.z, C.D, C.mask);
+    const bool staged = S != nullptr && g >= 0 && addr == __ldg(C.cell_keys + i);
+    const int state = C.nl_mask ? masks_state(C, i, c, pi) : 1;
+    if (C.nl_stats) atomicAdd(C.nl_stats + state, 1u);
+    const unsigned z0 = (unsigned)(c.z - 1) & m;
+    const unsigned z2 = (unsigned)(c.z + 1) & m;
+
+    if (state == 0) {
+        // One loop over all set bits of the 9 columns x 2 words (moving on
+        // when a word is exhausted), so the lanes of a warp diverge only on
+        // their total neighbour count.  No column wraps here: masks are never
+        // built for particles whose column runs wrap.
+        int col = -1, b = 0, sidx = -1;
+        unsigned long long bits = 0ull, next = 0ull;
+        bool second = true;
+        const unsigned wide = __ldg(C.nl_flags + i);
+#pragma unroll 1
+        while (true) {
+            while (bits == 0ull) {
+                if (!second) {  // second word of the current column
+                    second = true;
+                    bits = next;
+                    b += 64;
+                    if (sidx >= 0) sidx += 64;
+                } else {
+                    if (++col == 9) return;
+                    second = false;
+                    const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
+                    const unsigned base = x * D * D + y * D + z0;
+                    b = __ldg(off + base);
+                    const int e = __ldg(off + base + 3);
+                    sidx = staged ? staged_index(*S, g, col, b, e) : -1;
+                    if (column_has_outlier(C, x, y, z0)) {
+                        const int len = e - b;  // <= 128: the masks were built
+                        bits = len >= 64 ? ~0ull : ((1ull << len) - 1ull);
+                        next = len > 64 ? (len >= 128 ? ~0ull : ((1ull << (len - 64)) - 1ull)) : 0ull;
+                    } else {
+                        bits = __ldg(C.nl_mask + (size_t)(2 * col) * C.n + i);
+                        next = (wide & (kFlagWide << col)) ? __ldg(C.nl_mask + (size_t)(2 * col + 1) * C.n + i)
+                                                           : 0ull;
+                    }
+                }
+                if (lo > b) bits = (lo - b >= 64) ? 0ull : bits & (~0ull << (lo - b));
+            }
+            const int t = __ffsll((long long)bits) - 1;
+            bits &= bits - 1;
+            const int j = b + t;
+            f(j, sidx >= 0 ? S->pos[sidx + t] : P[j]);
+        }
+    }
+
+    // 27-cell walk: 9 column runs, split where z wraps around the table
+#pragma unroll 1
+    for (int col = 0; col < 9; ++col) {
+        const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
+        const unsigned base = x * D * D + y * D;
+        const bool wrap = !(z0 < z2);
+#pragma unroll 1
+        for (int piece = 0; piece < (wrap ? 2 : 1); ++piece) {
+            const unsigned za = (wrap && piece == 1) ? 0u : z0;
+            const unsigned zb = wrap ? (piece == 0 ? D - 1 : z2) : z2;
+            const int b = __ldg(off + base + za), e = __ldg(off + base + zb + 1);
+            const int sidx = staged ? staged_index(*S, g, col, b, e) : -1;
+#pragma unroll 1
+            for (int j = max(b, lo); j < e; ++j) f(j, sidx >= 0 ? S->pos[sidx + (j - b)] : P[j]);
+        }
+    }
+}
+
+}  // namespace bp
