@@ -161,6 +161,10 @@ def run_ours(args):
     scene = build_scene(bp, args.workload, seed=rank)
     n = scene.num_particles
     params = bp.make_params(scene)
+    if args.skin is not None:
+        params.neighbor_skin = args.skin
+    if args.no_stage:
+        params.walk_options |= bp.abi.BP_WALK_NO_STAGING
     stream = torch.cuda.Stream()
     solver = bp.ParticleSolver(scene, params, stream=stream.cuda_stream)
 
@@ -255,6 +259,7 @@ def run_ours(args):
             "data": "synthetic (seeded lattice scenes, no dataset)",
             "config": {"workload": workload_name(args.workload, n), "particles": n, "substeps": SUBSTEPS,
                        "iterations": ITERATIONS, "dt": DT, "mode": "reference", "grid": "64^3 cells, cell = h = 0.2",
+                       "neighbor_skin": float(params.neighbor_skin), "staging": not args.no_stage,
                        "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "particle-substeps/s",
                     "h2d_bytes_per_step": int(2 * n * 12), "d2h_bytes_per_step": int(n * 12)},
@@ -363,6 +368,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["mixed", "fluid", "small"], default="mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skin", type=float, default=None, help="neighbour-mask skin (fraction of h); 0 disables")
+    ap.add_argument("--no-stage", action="store_true", help="read neighbours from global memory only")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -43,6 +43,7 @@ BP_ORDER_SORTED = 0
 BP_ORDER_ORIGINAL = 1
 
 BP_DEVERR_NONFINITE = 0x1
+BP_WALK_NO_STAGING = 0x1
 
 (BP_FIELD_POSITIONS, BP_FIELD_NEW_POSITIONS, BP_FIELD_VELOCITIES, BP_FIELD_MAP_TO_ORIGINAL,
  BP_FIELD_MAP_TO_NEW, BP_FIELD_LAMBDAS, BP_FIELD_DENSITIES, BP_FIELD_SORTED_CELL_IDS,
@@ -78,7 +79,8 @@ class BpParams(C.Structure):
         ("wind_lift", C.c_float),
         ("rotation_iterations", C.c_int32),
         ("neighbor_skin", C.c_float),
-        ("reserved", C.c_int32 * 7),
+        ("walk_options", C.c_int32),
+        ("reserved", C.c_int32 * 6),
     ]
 
 

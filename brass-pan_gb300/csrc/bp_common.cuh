@@ -44,6 +44,7 @@ struct SimConsts {
     int rot_iters;
     float dt, inv_dt;
     int nplanes;
+    int stage;        // scan kernels stage their neighbourhood in shared memory
     float4 plane_o[kMaxPlanes];
     float4 plane_n[kMaxPlanes];
     // Neighbour bitmasks of the current substep (nl_mask == nullptr: off).

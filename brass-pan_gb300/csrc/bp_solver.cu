@@ -214,6 +214,7 @@ static SimConsts make_consts(const bp_solver *s, float sdt)
     C.dt = sdt;
     C.inv_dt = 1.0f / sdt;
     C.cell_keys = s->sorted_keys;  // stored cell of every particle (staged walks, masks)
+    C.stage = (p.walk_options & BP_WALK_NO_STAGING) ? 0 : 1;
     if (p.neighbor_skin > 0.f) {
         C.nl_mask = s->nl_mask;
         C.nl_cell = s->nl_cell;

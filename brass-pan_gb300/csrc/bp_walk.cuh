@@ -42,6 +42,7 @@ struct StageShared {
 __device__ __forceinline__ int stage_block(const SimConsts &C, const float4 *__restrict__ P,
                                            const int *__restrict__ off, int i0, StageShared &S)
 {
+    if (!C.stage) return -1;  // uniform across the grid: no barrier skipped unevenly
     const int t = threadIdx.x;
     const int i = i0 + t;
     const bool valid = i < C.n;
@@ -113,7 +114,8 @@ __device__ __forceinline__ int staged_index(const StageShared &S, int g, int k, 
 
 // Walk of particle i (sorted index) at position pi over the candidates
 // j >= lo of its 27 cells; calls f(j, P[j]).  S / g come from stage_block
-// (S == nullptr: no staging).
+// (S == nullptr: no staging).  The loop has a single call site of f, so the
+// pair arithmetic is compiled once and is the same on every path.
 template <class F>
 __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const float4 *__restrict__ P,
                                                const int *__restrict__ off, const SimConsts &C,
@@ -122,40 +124,41 @@ __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const f
     const int3 c = cell_of(pi, C);
     const unsigned m = C.mask;
     const unsigned D = (unsigned)C.D;
-    const int addr = cell_addr(c.x, c.y, c.z, C.D, C.mask);
-    const bool staged = S != nullptr && g >= 0 && addr == __ldg(C.cell_keys + i);
+    const bool staged = S != nullptr && g >= 0 && cell_addr(c.x, c.y, c.z, C.D, C.mask) == __ldg(C.cell_keys + i);
     const int state = C.nl_mask ? masks_state(C, i, c, pi) : 1;
     if (C.nl_stats) atomicAdd(C.nl_stats + state, 1u);
+    const bool masked = state == 0;  // masks are never built for particles whose column runs wrap
     const unsigned z0 = (unsigned)(c.z - 1) & m;
     const unsigned z2 = (unsigned)(c.z + 1) & m;
+    const bool wrap = !(z0 < z2);
+    const unsigned wide = masked ? __ldg(C.nl_flags + i) : 0u;
 
-    if (state == 0) {
-        // One loop over all set bits of the 9 columns x 2 words (moving on
-        // when a word is exhausted), so the lanes of a warp diverge only on
-        // their total neighbour count.  No column wraps here: masks are never
-        // built for particles whose column runs wrap.
-        int col = -1, b = 0, sidx = -1;
-        unsigned long long bits = 0ull, next = 0ull;
-        bool second = true;
-        const unsigned wide = __ldg(C.nl_flags + i);
+    int col = -1, piece = 0, npieces = 0;
+    int cb = 0;                           // first candidate of the current run
+    const float4 *src = P;                // src[j - cb] is candidate j's position
+    int j = 0, e = 0;                     // cell walk cursor over [j, e)
+    unsigned long long bits = 0ull, next = 0ull;
+    int word = 0;                         // masked walk: word of the current column
 #pragma unroll 1
-        while (true) {
+    while (true) {
+        int jc;
+        if (masked) {
             while (bits == 0ull) {
-                if (!second) {  // second word of the current column
-                    second = true;
+                if (word == 0 && next != 0ull) {
+                    word = 1;
                     bits = next;
-                    b += 64;
-                    if (sidx >= 0) sidx += 64;
+                    next = 0ull;
                 } else {
                     if (++col == 9) return;
-                    second = false;
+                    word = 0;
                     const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
                     const unsigned base = x * D * D + y * D + z0;
-                    b = __ldg(off + base);
-                    const int e = __ldg(off + base + 3);
-                    sidx = staged ? staged_index(*S, g, col, b, e) : -1;
+                    cb = __ldg(off + base);
+                    const int ce = __ldg(off + base + 3);
+                    const int sidx = staged ? staged_index(*S, g, col, cb, ce) : -1;
+                    src = sidx >= 0 ? S->pos + sidx : P + cb;
                     if (column_has_outlier(C, x, y, z0)) {
-                        const int len = e - b;  // <= 128: the masks were built
+                        const int len = ce - cb;  // <= 128: the masks were built
                         bits = len >= 64 ? ~0ull : ((1ull << len) - 1ull);
                         next = len > 64 ? (len >= 128 ? ~0ull : ((1ull << (len - 64)) - 1ull)) : 0ull;
                     } else {
@@ -164,30 +167,31 @@ __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const f
                                                            : 0ull;
                     }
                 }
-                if (lo > b) bits = (lo - b >= 64) ? 0ull : bits & (~0ull << (lo - b));
+                const int wb = cb + 64 * word;  // index of bit 0 of the current word
+                if (lo > wb) bits = (lo - wb >= 64) ? 0ull : bits & (~0ull << (lo - wb));
             }
-            const int t = __ffsll((long long)bits) - 1;
+            jc = cb + 64 * word + __ffsll((long long)bits) - 1;
             bits &= bits - 1;
-            const int j = b + t;
-            f(j, sidx >= 0 ? S->pos[sidx + t] : P[j]);
+        } else {
+            while (j >= e) {
+                if (++piece >= npieces) {
+                    if (++col == 9) return;
+                    piece = 0;
+                    npieces = wrap ? 2 : 1;
+                }
+                const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
+                const unsigned base = x * D * D + y * D;
+                const unsigned za = (wrap && piece == 1) ? 0u : z0;
+                const unsigned zb = wrap ? (piece == 0 ? D - 1 : z2) : z2;
+                cb = __ldg(off + base + za);
+                e = __ldg(off + base + zb + 1);
+                const int sidx = staged ? staged_index(*S, g, col, cb, e) : -1;
+                src = sidx >= 0 ? S->pos + sidx : P + cb;
+                j = max(cb, lo);
+            }
+            jc = j++;
         }
-    }
-
-    // 27-cell walk: 9 column runs, split where z wraps around the table
-#pragma unroll 1
-    for (int col = 0; col < 9; ++col) {
-        const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
-        const unsigned base = x * D * D + y * D;
-        const bool wrap = !(z0 < z2);
-#pragma unroll 1
-        for (int piece = 0; piece < (wrap ? 2 : 1); ++piece) {
-            const unsigned za = (wrap && piece == 1) ? 0u : z0;
-            const unsigned zb = wrap ? (piece == 0 ? D - 1 : z2) : z2;
-            const int b = __ldg(off + base + za), e = __ldg(off + base + zb + 1);
-            const int sidx = staged ? staged_index(*S, g, col, b, e) : -1;
-#pragma unroll 1
-            for (int j = max(b, lo); j < e; ++j) f(j, sidx >= 0 ? S->pos[sidx + (j - b)] : P[j]);
-        }
+        f(jc, src[jc - cb]);
     }
 }
 

@@ -77,6 +77,10 @@ typedef enum bp_mode {
 #define BP_STAGE_REFERENCE_AS_SHIPPED \
     (BP_STAGE_PLANES | BP_STAGE_VORTICITY | BP_STAGE_AKINCI | BP_STAGE_XSPH)
 
+/* bp_params.walk_options: read every neighbour from global memory instead of
+ * staging each block's neighbourhood in shared memory (results are identical). */
+#define BP_WALK_NO_STAGING 0x1
+
 /* Every literal of the reference's step as a field.  bp_params_init fills the
  * reference's values; comments give the reference location of each. */
 typedef struct bp_params {
@@ -107,7 +111,8 @@ typedef struct bp_params {
     int32_t rotation_iterations; /* 20 (shapematching.cuh:72) */
     float neighbor_skin;         /* skin of the per-substep neighbour masks, as a fraction of h
                                     (0 disables them; results are identical either way): 0.1 */
-    int32_t reserved[7];
+    int32_t walk_options;        /* BP_WALK_* tuning switches of the neighbour walks: 0 */
+    int32_t reserved[6];
 } bp_params;
 
 /* Fills `p` with the reference's literals for a scene of the given particle
