@@ -72,57 +72,82 @@ struct SimConsts {
 constexpr unsigned short kFlagContact = 1;
 constexpr unsigned short kFlagWide = 2;
 
-// ---- small vector helpers (own code; component-wise, left-to-right dot) ----
+// ---- small vector helpers (own code) ----
+// Every operation is an explicitly rounded intrinsic, so the compiler never
+// fuses or reorders arithmetic differently in two inlined copies of the same
+// expression: a pair term evaluates to the same bits wherever it is used.
 
 __device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
-__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b)
+{
+    return make_float3(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z));
+}
+__device__ __forceinline__ float3 operator-(float3 a, float3 b)
+{
+    return make_float3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
 __device__ __forceinline__ float3 operator-(float3 a) { return make_float3(-a.x, -a.y, -a.z); }
-__device__ __forceinline__ float3 operator*(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
-__device__ __forceinline__ float3 operator/(float3 a, float s) { return make_float3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float3 operator*(float3 a, float s)
+{
+    return make_float3(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s));
+}
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return a * s; }
+__device__ __forceinline__ float3 operator/(float3 a, float s)
+{
+    return make_float3(__fdiv_rn(a.x, s), __fdiv_rn(a.y, s), __fdiv_rn(a.z, s));
+}
 __device__ __forceinline__ void operator+=(float3 &a, float3 b) { a = a + b; }
 __device__ __forceinline__ void operator-=(float3 &a, float3 b) { a = a - b; }
-__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// a + s * b with one rounding per component
+__device__ __forceinline__ float3 fma3(float s, float3 b, float3 a)
+{
+    return make_float3(__fmaf_rn(s, b.x, a.x), __fmaf_rn(s, b.y, a.y), __fmaf_rn(s, b.z, a.z));
+}
+__device__ __forceinline__ float dot3(float3 a, float3 b)
+{
+    return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)));
+}
 __device__ __forceinline__ float3 cross3(float3 a, float3 b)
 {
-    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+    return make_float3(__fmaf_rn(a.y, b.z, -__fmul_rn(a.z, b.y)), __fmaf_rn(a.z, b.x, -__fmul_rn(a.x, b.z)),
+                       __fmaf_rn(a.x, b.y, -__fmul_rn(a.y, b.x)));
 }
 __device__ __forceinline__ float len2(float3 a) { return dot3(a, a); }
-__device__ __forceinline__ float len3(float3 a) { return sqrtf(dot3(a, a)); }
+__device__ __forceinline__ float len3(float3 a) { return __fsqrt_rn(dot3(a, a)); }
 __device__ __forceinline__ int phase_of(float4 a) { return __float_as_int(a.w); }
 
 // ---- SPH kernels (same formulas as K/fluid.cuh:31-74) ----
 
 __device__ __forceinline__ float poly6(const SimConsts &C, float r2)
 {
-    const float t = C.h2 - r2;
-    return C.c_poly6 * t * t * t;
+    const float t = __fsub_rn(C.h2, r2);
+    return __fmul_rn(__fmul_rn(__fmul_rn(C.c_poly6, t), t), t);
 }
 __device__ __forceinline__ float3 spiky_grad(const SimConsts &C, float3 v, float r2)
 {
-    const float r = sqrtf(r2);
-    const float t = C.h - r;
-    return (C.c_spiky * t * t * v) / r;
+    const float r = __fsqrt_rn(r2);
+    const float t = __fsub_rn(C.h, r);
+    return (__fmul_rn(__fmul_rn(C.c_spiky, t), t) * v) / r;
 }
 // Same gradient through one reciprocal square root (r2 > 0): the hot loops'
 // form.  Differs from the IEEE sqrt-and-divide form above by a few ulp.
 __device__ __forceinline__ float3 spiky_grad_r(const SimConsts &C, float3 v, float r2, float inv_r)
 {
-    const float t = C.h - r2 * inv_r;
-    return (C.c_spiky * t * t * inv_r) * v;
+    const float t = __fmaf_rn(-r2, inv_r, C.h);
+    return __fmul_rn(__fmul_rn(__fmul_rn(C.c_spiky, t), t), inv_r) * v;
 }
 __device__ __forceinline__ float ipowf(float x, int n)
 {
     float r = 1.0f;
-    for (int k = 0; k < n; ++k) r *= x;
+    for (int k = 0; k < n; ++k) r = __fmul_rn(r, x);
     return r;
 }
 __device__ __forceinline__ float akinci_spline(const SimConsts &C, float r)
 {
-    const float t = (C.h - r) * r;
-    const float t3 = t * t * t;
-    return (r >= C.half_h) ? C.c_akinci * t3 : 2.0f * C.c_akinci * t3 - C.c_akinci_off;
+    const float t = __fmul_rn(__fsub_rn(C.h, r), r);
+    const float t3 = __fmul_rn(__fmul_rn(t, t), t);
+    return (r >= C.half_h) ? __fmul_rn(C.c_akinci, t3)
+                           : __fsub_rn(__fmul_rn(__fmul_rn(2.0f, C.c_akinci), t3), C.c_akinci_off);
 }
 
 // ---- hash grid (same cell function as K/grid.cuh:9-28) ----

@@ -92,11 +92,11 @@ __global__ void __launch_bounds__(kWalkThreads) k_particle_collision(SimConsts C
         const float3 diff = xip - xjp;
         const float d2 = len2(diff);
         if (!(d2 < r * r * 4.0f && d2 > 1e-5f)) return;
-        const float dist = sqrtf(d2);
+        const float dist = __fsqrt_rn(d2);
         const float wj = w[j];
-        const float w1 = wi / (wi + wj);
-        const float w2 = wj / (wi + wj);
-        const float3 proj = diff * (2.0f * r / dist - 1.0f);
+        const float w1 = __fdiv_rn(wi, __fadd_rn(wi, wj));
+        const float w2 = __fdiv_rn(wj, __fadd_rn(wi, wj));
+        const float3 proj = diff * __fsub_rn(__fdiv_rn(2.0f * r, dist), 1.0f);
         const float3 dxi = w1 * proj;
         const float3 xistar = dxi + xip;
         sd += dxi;
@@ -110,10 +110,10 @@ __global__ void __launch_bounds__(kWalkThreads) k_particle_collision(SimConsts C
             const float3 nn = diff / dist;
             const float3 tdx = t1 - dot3(t1, nn) * nn;
             const float tl2 = len2(tdx);
-            if (tl2 <= (C.fs * C.fs) * dxi2)
+            if (tl2 <= __fmul_rn(C.fs * C.fs, dxi2))
                 sf -= w1 * tdx;
             else
-                sf -= (w1 * tdx) * fminf(C.fd * sqrtf(dxi2 / tl2), 1.0f);
+                sf -= (w1 * tdx) * fminf(__fmul_rn(C.fd, __fsqrt_rn(__fdiv_rn(dxi2, tl2))), 1.0f);
         }
     });
     const float3 d = (count == 0) ? sd : sd + sf / (float)count;

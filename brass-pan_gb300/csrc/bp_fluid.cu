@@ -44,8 +44,8 @@ __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const floa
         walk_neighbors(i, pi, i, P, off, C, &S, g, [&](int j, float4 pj) {
             const float d2 = len2(pi - f3(pj));
             if (d2 <= C.h2) {
-                const float ld = __ldg(mass + j) * poly6(C, d2);
-                density += (phase_of(pj) < 0) ? ld : C.solid_scale * ld;
+                const float ld = __fmul_rn(__ldg(mass + j), poly6(C, d2));
+                density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
             }
         });
         float c = density / C.rho0 - 1.0f;
@@ -59,11 +59,11 @@ __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const floa
             const float d2 = len2(diff);
             if (d2 <= C.h2) {
                 const float mj = __ldg(mass + j);
-                const float ld = mj * poly6(C, d2);
-                density += (phase_of(pj) < 0) ? ld : C.solid_scale * ld;
+                const float ld = __fmul_rn(mj, poly6(C, d2));
+                density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
                 if (d2 > 0.f) {
-                    const float3 g = (-mj * C.inv_rho0) * spiky_grad_r(C, diff, d2, rsqrtf(d2));
-                    sum_g2 += dot3(g, g);
+                    const float3 g = __fmul_rn(-mj, C.inv_rho0) * spiky_grad_r(C, diff, d2, rsqrtf(d2));
+                    sum_g2 = __fadd_rn(sum_g2, dot3(g, g));
                     gi -= g;
                 }
             }
@@ -109,14 +109,15 @@ __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs 
             if (d2 <= C.h2 && d2 > 0.f) {
                 const bool inc = C.textbook ? true : ((j > k) ? (phk < 0) : (phase_of(pj4) < 0));
                 if (!inc) return;
-                float sl = lk + __ldg(a.lam + j);
-                if (C.scorr_on) sl += -C.scorr_k * ipowf(poly6(C, d2) * C.scorr_inv_wq, C.scorr_ni);
+                float sl = __fadd_rn(lk, __ldg(a.lam + j));
+                if (C.scorr_on)
+                    sl = __fsub_rn(sl, __fmul_rn(C.scorr_k, ipowf(__fmul_rn(poly6(C, d2), C.scorr_inv_wq), C.scorr_ni)));
                 float3 delta = sl * spiky_grad_r(C, diff, d2, rsqrtf(d2));
                 if (C.delta_clamp > 0.f) {  // per-pair clamp; the length is only needed past it
                     const float l2 = len2(delta);
-                    if (!(l2 < C.delta_clamp2)) delta = delta * (C.delta_clamp * rsqrtf(l2));
+                    if (!(l2 < C.delta_clamp2)) delta = delta * __fmul_rn(C.delta_clamp, rsqrtf(l2));
                 }
-                sum += __ldg(a.mass + j) * delta;
+                sum = fma3(__ldg(a.mass + j), delta, sum);
             }
         });
     }
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const floa
         if (d2 <= C.h2 && d2 > 0.f) {
             const float3 g = spiky_grad_r(C, diff, d2, rsqrtf(d2));
             if (want_om) om += cross3(f3(V[j]) - vi, g);
-            if (want_n) nn += __frcp_rn(__ldg(rho + j)) * g;
+            if (want_n) nn = fma3(__frcp_rn(__ldg(rho + j)), g, nn);
         }
     });
     Om[i] = make_float4(om.x, om.y, om.z, len3(om));
@@ -272,14 +273,14 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
         const float d2 = len2(diff);
         if (d2 <= C.h2 && d2 > 0.f) {
             const float inv_r = rsqrtf(d2);
-            if (want_v) eta += Om[j].w * spiky_grad_r(C, diff, d2, inv_r);
+            if (want_v) eta = fma3(Om[j].w, spiky_grad_r(C, diff, d2, inv_r), eta);
             if (want_t) {
                 const float4 nj4 = Nm[j];
-                const float dist = d2 * inv_r;
-                const float3 fco = (-C.tension * akinci_spline(C, dist) * inv_r) * diff;
-                const float3 fcu = -C.tension * (ni - f3(nj4));
-                const float kij = (2.0f * C.rho0) * __frcp_rn(rhoi + nj4.w);
-                ft += kij * (fco + fcu);
+                const float dist = __fmul_rn(d2, inv_r);
+                const float3 fco = __fmul_rn(__fmul_rn(-C.tension, akinci_spline(C, dist)), inv_r) * diff;
+                const float3 fcu = (-C.tension) * (ni - f3(nj4));
+                const float kij = __fmul_rn(2.0f * C.rho0, __frcp_rn(__fadd_rn(rhoi, nj4.w)));
+                ft = fma3(kij, fco + fcu, ft);
             }
         }
     });
@@ -319,8 +320,8 @@ __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const floa
         const float d2 = len2(pi - f3(pj4));
         if (d2 <= C.h2) {
             float wgt = poly6(C, d2);
-            if (C.textbook) wgt = wgt * (__ldg(mass + j) / __ldg(rho + j));
-            vn += (f3(V[j]) - vi) * wgt;
+            if (C.textbook) wgt = __fmul_rn(wgt, __fdiv_rn(__ldg(mass + j), __ldg(rho + j)));
+            vn = fma3(wgt, f3(V[j]) - vi, vn);
         }
     });
     const float3 v = vi + C.xsph_c * vn;

@@ -114,8 +114,10 @@ __device__ __forceinline__ int staged_index(const StageShared &S, int g, int k, 
 
 // Walk of particle i (sorted index) at position pi over the candidates
 // j >= lo of its 27 cells; calls f(j, P[j]).  S / g come from stage_block
-// (S == nullptr: no staging).  The loop has a single call site of f, so the
-// pair arithmetic is compiled once and is the same on every path.
+// (S == nullptr or g < 0: no staging).  Masked walks take each column's set
+// bits in ascending order; a column holding an outlier is walked whole.  The
+// pair arithmetic of the callers uses explicitly rounded operations, so the
+// two inlined copies of f (masked and cell walk) produce the same bits.
 template <class F>
 __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const float4 *__restrict__ P,
                                                const int *__restrict__ off, const SimConsts &C,
@@ -127,71 +129,60 @@ __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const f
     const bool staged = S != nullptr && g >= 0 && cell_addr(c.x, c.y, c.z, C.D, C.mask) == __ldg(C.cell_keys + i);
     const int state = C.nl_mask ? masks_state(C, i, c, pi) : 1;
     if (C.nl_stats) atomicAdd(C.nl_stats + state, 1u);
-    const bool masked = state == 0;  // masks are never built for particles whose column runs wrap
     const unsigned z0 = (unsigned)(c.z - 1) & m;
     const unsigned z2 = (unsigned)(c.z + 1) & m;
-    const bool wrap = !(z0 < z2);
-    const unsigned wide = masked ? __ldg(C.nl_flags + i) : 0u;
 
-    int col = -1, piece = 0, npieces = 0;
-    int cb = 0;                           // first candidate of the current run
-    const float4 *src = P;                // src[j - cb] is candidate j's position
-    int j = 0, e = 0;                     // cell walk cursor over [j, e)
-    unsigned long long bits = 0ull, next = 0ull;
-    int word = 0;                         // masked walk: word of the current column
+    if (state == 0) {  // masks are never built for particles whose column runs wrap
+        const unsigned wide = __ldg(C.nl_flags + i);
 #pragma unroll 1
-    while (true) {
-        int jc;
-        if (masked) {
-            while (bits == 0ull) {
-                if (word == 0 && next != 0ull) {
-                    word = 1;
-                    bits = next;
-                    next = 0ull;
-                } else {
-                    if (++col == 9) return;
-                    word = 0;
-                    const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
-                    const unsigned base = x * D * D + y * D + z0;
-                    cb = __ldg(off + base);
-                    const int ce = __ldg(off + base + 3);
-                    const int sidx = staged ? staged_index(*S, g, col, cb, ce) : -1;
-                    src = sidx >= 0 ? S->pos + sidx : P + cb;
-                    if (column_has_outlier(C, x, y, z0)) {
-                        const int len = ce - cb;  // <= 128: the masks were built
-                        bits = len >= 64 ? ~0ull : ((1ull << len) - 1ull);
-                        next = len > 64 ? (len >= 128 ? ~0ull : ((1ull << (len - 64)) - 1ull)) : 0ull;
-                    } else {
-                        bits = __ldg(C.nl_mask + (size_t)(2 * col) * C.n + i);
-                        next = (wide & (kFlagWide << col)) ? __ldg(C.nl_mask + (size_t)(2 * col + 1) * C.n + i)
-                                                           : 0ull;
-                    }
-                }
-                const int wb = cb + 64 * word;  // index of bit 0 of the current word
+        for (int col = 0; col < 9; ++col) {
+            const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
+            const unsigned base = x * D * D + y * D + z0;
+            const int cb = __ldg(off + base);
+            const int ce = __ldg(off + base + 3);
+            unsigned long long w[2];
+            if (column_has_outlier(C, x, y, z0)) {
+                const int len = ce - cb;  // <= 128: the masks were built
+                w[0] = len >= 64 ? ~0ull : ((1ull << len) - 1ull);
+                w[1] = len > 64 ? (len >= 128 ? ~0ull : ((1ull << (len - 64)) - 1ull)) : 0ull;
+            } else {
+                w[0] = __ldg(C.nl_mask + (size_t)(2 * col) * C.n + i);
+                w[1] = (wide & (kFlagWide << col)) ? __ldg(C.nl_mask + (size_t)(2 * col + 1) * C.n + i) : 0ull;
+            }
+            if (!(w[0] | w[1])) continue;
+            const int sidx = staged ? staged_index(*S, g, col, cb, ce) : -1;
+            const float4 *src = sidx >= 0 ? S->pos + sidx : P + cb;
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                unsigned long long bits = w[k];
+                const int wb = cb + 64 * k;
                 if (lo > wb) bits = (lo - wb >= 64) ? 0ull : bits & (~0ull << (lo - wb));
-            }
-            jc = cb + 64 * word + __ffsll((long long)bits) - 1;
-            bits &= bits - 1;
-        } else {
-            while (j >= e) {
-                if (++piece >= npieces) {
-                    if (++col == 9) return;
-                    piece = 0;
-                    npieces = wrap ? 2 : 1;
+                while (bits) {
+                    const int t = 64 * k + __ffsll((long long)bits) - 1;
+                    bits &= bits - 1;
+                    f(cb + t, src[t]);
                 }
-                const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
-                const unsigned base = x * D * D + y * D;
-                const unsigned za = (wrap && piece == 1) ? 0u : z0;
-                const unsigned zb = wrap ? (piece == 0 ? D - 1 : z2) : z2;
-                cb = __ldg(off + base + za);
-                e = __ldg(off + base + zb + 1);
-                const int sidx = staged ? staged_index(*S, g, col, cb, e) : -1;
-                src = sidx >= 0 ? S->pos + sidx : P + cb;
-                j = max(cb, lo);
             }
-            jc = j++;
         }
-        f(jc, src[jc - cb]);
+        return;
+    }
+
+    // 27-cell walk: 9 column runs, split where z wraps around the table
+    const bool wrap = !(z0 < z2);
+#pragma unroll 1
+    for (int col = 0; col < 9; ++col) {
+        const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
+        const unsigned base = x * D * D + y * D;
+#pragma unroll 1
+        for (int piece = 0; piece < (wrap ? 2 : 1); ++piece) {
+            const unsigned za = (wrap && piece == 1) ? 0u : z0;
+            const unsigned zb = wrap ? (piece == 0 ? D - 1 : z2) : z2;
+            const int b = __ldg(off + base + za), e = __ldg(off + base + zb + 1);
+            const int sidx = staged ? staged_index(*S, g, col, b, e) : -1;
+            const float4 *src = sidx >= 0 ? S->pos + sidx : P + b;
+#pragma unroll 1
+            for (int j = max(b, lo); j < e; ++j) f(j, src[j - b]);
+        }
     }
 }
 
