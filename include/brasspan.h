@@ -110,7 +110,7 @@ typedef struct bp_params {
     float wind_lift;             /* 100 (wind.cuh:43) */
     int32_t rotation_iterations; /* 20 (shapematching.cuh:72) */
     float neighbor_skin;         /* skin of the per-substep neighbour masks, as a fraction of h
-                                    (0 disables them; results are identical either way): 0.1 */
+                                    (0 disables them; results are identical either way): 0 */
     int32_t walk_options;        /* BP_WALK_* tuning switches of the neighbour walks: 0 */
     int32_t reserved[6];
 } bp_params;

@@ -172,12 +172,27 @@ def test_neighbor_masks_are_bit_identical_to_cell_walks(bp, gpu, skin):
     outs = []
     for s in (0.0, skin):
         g = bp.ParticleSolver(scene, bp.make_params(scene, neighbor_skin=s))
+        assert g.params.neighbor_skin == np.float32(s)
         for _ in range(4):
             g.update(2, DT, 4)
         outs.append((g.positions(), g.velocities()))
         g.close()
     np.testing.assert_array_equal(outs[0][0], outs[1][0])
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("options", [0, 1])
+def test_shared_memory_staging_is_bit_identical(bp, gpu, options):
+    """Staging each block's neighbourhood in shared memory changes nothing."""
+    scene = small_mixed_scene(bp, seed=14)
+    outs = []
+    for walk in (bp.abi.BP_WALK_NO_STAGING, options * 0):
+        g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=walk, neighbor_skin=0.1 * options))
+        for _ in range(4):
+            g.update(2, DT, 4)
+        outs.append(g.positions())
+        g.close()
+    np.testing.assert_array_equal(outs[0], outs[1])
 
 
 def test_graph_replay_equals_recapture(bp, gpu):
