@@ -160,4 +160,7 @@ void launch_gather_xyz(cudaStream_t st, int n, const float4 *src, const int *map
 void launch_scatter_xyz(cudaStream_t st, int n, const float *in, const int *map, float4 *dst);
 void launch_check_finite(cudaStream_t st, int n, const float4 *X, unsigned *err, LaunchLog *L);
 
+// Sets the message bp_last_error_string returns on this thread.
+void set_last_error(const char *msg);
+
 }  // namespace bp

@@ -38,6 +38,9 @@ bool is_pow2(int d) { return d > 0 && (d & (d - 1)) == 0; }
 
 }  // namespace
 
+// The message bp_last_error_string returns, for entry points in other files.
+void bp::set_last_error(const char *msg) { g_err = msg; }
+
 struct bp_solver {
     int n = 0;
     bp_params prm{};

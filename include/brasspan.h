@@ -256,6 +256,29 @@ bp_status bp_grid_build(void *stream, int32_t num_particles, const float *d_posi
 bp_status bp_grid_reset(void *stream, int32_t num_particles, const int32_t *d_sorted_cell_ids,
                         int32_t *d_cell_start, int32_t *d_cell_end);
 
+/* bp_grid_build without a workspace and without any allocation.  This entry
+ * point has no counterpart in the reference.  It is for callers that cannot
+ * call cudaMalloc when they need a grid: a plug-in inside a host application
+ * that owns all device memory through its own pools, a real-time loop whose
+ * budget forbids allocation after start-up, or code that must not
+ * synchronise the device, as cudaMalloc and cudaFree may do.
+ *
+ * The sort's scratch is a fixed 4.2 MB array in the library's device memory,
+ * held on every GPU that loads the library until the process exits, so
+ * num_particles is at most 262144; larger inputs return BP_ERR_CAPACITY.
+ * Inputs, outputs and their contract are those of bp_grid_build (cell_start /
+ * cell_end -1 before the call; grid_dim a power of two in 4..1024).
+ *
+ * The first call on a device, with that device current, looks up the array's
+ * address on that device; make that first call before any stream capture.
+ * All calls on a device share the one array: calls whose work overlaps on the
+ * GPU (on different streams, or from different threads without ordering)
+ * race and give wrong results.  Order them on one stream. */
+bp_status bp_grid_build_static(void *stream, int32_t num_particles, const float *d_positions,
+                               float cell_size, int32_t grid_dim, int32_t *d_cell_ids,
+                               int32_t *d_sorted_cell_ids, int32_t *d_sorted_particle_ids,
+                               int32_t *d_cell_start, int32_t *d_cell_end);
+
 /* Neighbour counts in the reference's 27-cell walk (the loop structure of
  * kernel/fluid.cuh:104-141): for each particle i of the cell-sorted positions
  * [N][3], the number of j (i itself included) stored in the 27 cells around
