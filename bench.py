@@ -3,10 +3,13 @@
 A step is one call of update(2 substeps, dt = 1/60 s, 4 iterations) on the
 mixed-phase scene of the benchmark configuration (1,048,576 PBF fluid
 particles, a 256x256 cloth under wind, 64 rigid 8^3 cubes; 1,146,880
-particles), reference-mode parameters.  Prints one JSON line.
+particles), reference-mode parameters.  Prints one JSON line; unless
+--no-batch, its "batched" object times the batched ensemble (256 PBF dam
+breaks of 4096..262144 particles in one solver) against looping one solver
+per scene over the same scenes.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload mixed|fluid]
+                  [--workload mixed|fluid|small|batch] [--no-batch]
 
 Multi-GPU (torchrun, one rank per GPU): the scene does not shard, so every
 rank advances its own replica ("replicas only"); value = all ranks' particle
@@ -61,12 +64,58 @@ def build_scene(bp, workload: str, seed: int = 0):
         return bp.scenes.pbf_scene(128, 64, 128, spacing=0.1, seed=seed, box=(12.9, 16.0, 12.9))
     if workload == "small":
         return bp.scenes.pbf_scene(32, 32, 32, spacing=0.1, seed=seed, box=(4.0, 4.0, 4.0))
+    if workload == "batch":  # CPU-side sample of the ensemble: its largest member
+        return max(bp.scenes.config3_ensemble(seed=seed), key=lambda sc: sc.num_particles)
     raise SystemExit(f"unknown workload {workload}")
 
 
 def workload_name(workload, n):
     return {"mixed": "mixed-phase: 128x64x128 PBF fluid + 256^2 cloth (wind) + 64 rigid 8^3 cubes",
-            "fluid": "PBF dam break 128x64x128", "small": "PBF dam break 32^3"}[workload] + f", N={n}"
+            "fluid": "PBF dam break 128x64x128", "small": "PBF dam break 32^3",
+            "batch": "batched ensemble: 256 PBF dam breaks, log-uniform 4096..262144 particles"}[workload] + f", N={n}"
+
+
+def timed_steps(torch, stream, flush, steps, fn):
+    """CUDA-event time (ms) of `steps` calls of fn on `stream`, L2 flushed before each."""
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for k in range(steps):
+        flush.fill_(k & 0xFF)
+        starts[k].record(stream)
+        fn()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in zip(starts, ends))
+
+
+def run_batch(bp, torch, stream, flush, steps, warmup, seed=0):
+    """The batched ensemble (256 scenes in one solver) against looping one
+    solver per scene over the same scenes on the same stream."""
+    scenes = bp.scenes.config3_ensemble(seed=seed)
+    n = sum(s.num_particles for s in scenes)
+    batch = bp.BatchSolver(scenes, stream=stream.cuda_stream)
+    singles = [bp.ParticleSolver(s, stream=stream.cuda_stream) for s in scenes]
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            batch.update(SUBSTEPS, DT, ITERATIONS)
+            for g in singles:
+                g.update(SUBSTEPS, DT, ITERATIONS)
+        launches_batch = batch.last_launch_count()
+        launches_loop = sum(g.last_launch_count() for g in singles)
+        ms_batch = timed_steps(torch, stream, flush, steps, lambda: batch.update(SUBSTEPS, DT, ITERATIONS))
+        ms_loop = timed_steps(torch, stream, flush, steps,
+                              lambda: [g.update(SUBSTEPS, DT, ITERATIONS) for g in singles])
+    errors = batch.device_errors()
+    batch.close()
+    for g in singles:
+        g.close()
+    units = float(n) * SUBSTEPS * steps
+    return {"workload": workload_name("batch", n), "scenes": len(scenes), "particles": n,
+            "value": units / (ms_batch / 1e3), "loop_value": units / (ms_loop / 1e3),
+            "batched_vs_loop": ms_loop / ms_batch, "ms_per_step": ms_batch / steps,
+            "loop_ms_per_step": ms_loop / steps, "launches_per_step": launches_batch,
+            "loop_launches_per_step": launches_loop, "device_errors": errors, "steps": steps}
 
 
 class ClockSampler:
@@ -158,15 +207,27 @@ def run_ours(args):
 
     entry.build()
     bp = entry.load_package()
-    scene = build_scene(bp, args.workload, seed=rank)
-    n = scene.num_particles
-    params = bp.make_params(scene)
-    if args.skin is not None:
-        params.neighbor_skin = args.skin
-    if args.no_stage:
-        params.walk_options |= bp.abi.BP_WALK_NO_STAGING
     stream = torch.cuda.Stream()
-    solver = bp.ParticleSolver(scene, params, stream=stream.cuda_stream)
+
+    def tuned(p):
+        if args.skin is not None:
+            p.neighbor_skin = args.skin
+        if args.no_stage:
+            p.walk_options |= bp.abi.BP_WALK_NO_STAGING
+        if args.no_split:
+            p.walk_options |= bp.abi.BP_WALK_NO_SPLIT
+        return p
+
+    if args.workload == "batch":
+        scenes = bp.scenes.config3_ensemble(seed=rank)
+        solver = bp.BatchSolver(scenes, [tuned(bp.make_params(s)) for s in scenes], stream=stream.cuda_stream)
+        params = solver.params
+        n = solver.n
+    else:
+        scene = build_scene(bp, args.workload, seed=rank)
+        n = scene.num_particles
+        params = tuned(bp.make_params(scene))
+        solver = bp.ParticleSolver(scene, params, stream=stream.cuda_stream)
 
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     with torch.cuda.stream(stream):
@@ -239,6 +300,10 @@ def run_ours(args):
     step_ms_total = sum(v[1] for v in agg.values()) / prof_steps
     walks = solver.walk_stats(SUBSTEPS, DT, ITERATIONS)
     solver.close()
+    batched = None
+    if args.workload == "batch" or (args.workload == "mixed" and not args.no_batch):
+        # the ensemble against a loop of one solver per scene (bounded: 3 timed steps)
+        batched = run_batch(bp, torch, stream, flush, steps=min(args.steps, 3), warmup=3, seed=rank)
 
     result = None
     if rank == 0:
@@ -258,8 +323,10 @@ def run_ours(args):
             "dtype": "f32",
             "data": "synthetic (seeded lattice scenes, no dataset)",
             "config": {"workload": workload_name(args.workload, n), "particles": n, "substeps": SUBSTEPS,
-                       "iterations": ITERATIONS, "dt": DT, "mode": "reference", "grid": "64^3 cells, cell = h = 0.2",
-                       "neighbor_skin": float(params.neighbor_skin), "staging": not args.no_stage,
+                       "iterations": ITERATIONS, "dt": DT, "mode": "reference",
+                       "grid": ("one grid per scene (16^3..64^3 cells), cell = h = 0.2" if args.workload == "batch"
+                                else "64^3 cells, cell = h = 0.2"),
+                       "neighbor_skin": float(params.neighbor_skin), "staging": not args.no_stage, "split_walks": not args.no_split,
                        "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "particle-substeps/s",
                     "h2d_bytes_per_step": int(2 * n * 12), "d2h_bytes_per_step": int(n * 12)},
@@ -275,6 +342,8 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "clocks": clk,
         }
+        if batched is not None:
+            result["batched"] = batched
         print(json.dumps(result), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -368,8 +437,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["mixed", "fluid", "small"], default="mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--skin", type=float, default=None, help="neighbour-mask skin (fraction of h); 0 disables")
     ap.add_argument("--no-stage", action="store_true", help="read neighbours from global memory only")
+    ap.add_argument("--no-split", action="store_true", help="evaluate pair terms as candidates are tested")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -7,6 +7,6 @@ __graft_entry__.py registers it as the module `brasspan_gb300`.
 from . import abi, scenes
 from .abi import BrassPanError
 from .scenes import Scene
-from .solver import ParticleSolver, make_params
+from .solver import BatchSolver, ParticleSolver, make_params
 
-__all__ = ["abi", "scenes", "Scene", "ParticleSolver", "make_params", "BrassPanError"]
+__all__ = ["abi", "scenes", "Scene", "ParticleSolver", "BatchSolver", "make_params", "BrassPanError"]

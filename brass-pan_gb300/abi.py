@@ -44,6 +44,7 @@ BP_ORDER_ORIGINAL = 1
 
 BP_DEVERR_NONFINITE = 0x1
 BP_WALK_NO_STAGING = 0x1
+BP_WALK_NO_SPLIT = 0x2
 
 (BP_FIELD_POSITIONS, BP_FIELD_NEW_POSITIONS, BP_FIELD_VELOCITIES, BP_FIELD_MAP_TO_ORIGINAL,
  BP_FIELD_MAP_TO_NEW, BP_FIELD_LAMBDAS, BP_FIELD_DENSITIES, BP_FIELD_SORTED_CELL_IDS,
@@ -170,7 +171,7 @@ EXPORTS = [
     "bp_solver_get_particle_position", "bp_solver_copy_positions", "bp_solver_copy_velocities",
     "bp_solver_set_state", "bp_solver_field", "bp_solver_copy_field", "bp_solver_pack_particle_infos",
     "bp_solver_device_errors", "bp_solver_last_launch_count", "bp_solver_profile", "bp_solver_walk_stats", "bp_grid_workspace_size", "bp_grid_build",
-    "bp_grid_reset", "bp_grid_build_static", "bp_grid_neighbor_counts", "bp_last_error_string", "bp_abi_version",
+    "bp_grid_reset", "bp_grid_build_static", "bp_batch_create", "bp_batch_step", "bp_batch_scene_range", "bp_grid_neighbor_counts", "bp_last_error_string", "bp_abi_version",
 ]
 
 
@@ -209,6 +210,9 @@ def load(path: Path | None = None):
         "bp_grid_build": (i32, [vp, i32, vp, f32, i32, vp, vp, vp, vp, vp, vp, sz]),
         "bp_grid_reset": (i32, [vp, i32, vp, vp, vp]),
         "bp_grid_build_static": (i32, [vp, i32, vp, f32, i32, vp, vp, vp, vp, vp]),
+        "bp_batch_create": (i32, [i32, vp, vp, vp, vp]),
+        "bp_batch_step": (i32, [vp, f32, i32, i32]),
+        "bp_batch_scene_range": (i32, [vp, i32, vp, vp]),
         "bp_grid_neighbor_counts": (i32, [vp, i32, vp, f32, i32, f32, vp, vp, vp]),
         "bp_last_error_string": (C.c_char_p, []),
         "bp_abi_version": (i32, []),

@@ -17,6 +17,20 @@ namespace bp {
 
 constexpr int kMaxPlanes = 16;
 
+// One scene of a batched ensemble.  The scenes share one key space: scene s
+// owns cell keys [base, base + D^3), so one stable sort keeps every scene's
+// particles contiguous and in the order a solver of that scene alone gives.
+struct SceneConsts {
+    int D;             // grid dimension of this scene (power of two)
+    unsigned mask;     // D - 1
+    int base;          // first cell key of this scene
+    int nplanes;
+    float rho0, inv_rho0;
+    float gx, gy, gz;  // gravity
+    float4 plane_o[kMaxPlanes];
+    float4 plane_n[kMaxPlanes];
+};
+
 // Constants of one substep, passed by value to every kernel (graph friendly).
 struct SimConsts {
     int n;
@@ -45,6 +59,7 @@ struct SimConsts {
     float dt, inv_dt;
     int nplanes;
     int stage;        // scan kernels stage their neighbourhood in shared memory
+    int split;        // scan kernels test candidates in chunks before the pair terms
     float4 plane_o[kMaxPlanes];
     float4 plane_n[kMaxPlanes];
     // Neighbour bitmasks of the current substep (nl_mask == nullptr: off).
@@ -54,7 +69,7 @@ struct SimConsts {
     // always walks its 27 cells), nl_pos the positions at build.  A masked
     // walk is taken while the particle is still in nl_cell and within half
     // the skin of nl_pos; columns holding a particle that moved further are
-    // walked whole (see for_each_neighbor).
+    // walked whole (see walk_neighbors).
     unsigned long long *nl_mask;       // [18][n]: column c uses words 2c and 2c+1 (128 candidates)
     int *nl_cell;
     float4 *nl_pos;
@@ -67,6 +82,11 @@ struct SimConsts {
     float nl_hs2;            // (h + skin)^2
     float nl_half_skin2;     // (skin / 2)^2
     float nl_contact2;       // (2r + skin)^2
+    // Batched ensembles (nullptr: one scene, described by the fields above).
+    // scene_of[i] is the scene of particle i; it holds for sorted and
+    // original indices alike, because every scene keeps its segment.
+    const SceneConsts *scn;
+    const int *scene_of;
 };
 
 constexpr unsigned short kFlagContact = 1;
@@ -167,74 +187,33 @@ __device__ __forceinline__ int cell_addr(int x, int y, int z, int D, unsigned ma
                  ((unsigned)z & mask));
 }
 
-// Walk the 27 cells around the cell of `pi`.  Cells are addressed x-major
-// (x*D*D + y*D + z), so for a fixed (x, y) column the three z cells are
-// consecutive addresses and their particles are one contiguous run of the
-// sorted arrays: [off[base+z-1], off[base+z+2]).  The walk therefore visits
-// 9 column runs (split in two where z wraps around the table), using the
-// dense prefix table `off` of D^3+1 entries.
-template <class F>
-__device__ __forceinline__ void for_each_candidate(float3 pi, const int *__restrict__ off, const SimConsts &C,
-                                                   F &&f)
+// The grid a particle's walks use: its scene's dimension, and the cell
+// offsets from its scene's first key on (off[0] is that scene's first cell).
+struct GridView {
+    int D;
+    unsigned mask;
+    int base;
+    const int *off;
+};
+__device__ __forceinline__ int scene_index(const SimConsts &C, int i)
 {
-    const int3 c = cell_of(pi, C);
-    const unsigned m = C.mask;
-    const unsigned D = (unsigned)C.D;
-    const unsigned z0 = (unsigned)(c.z - 1) & m;
-    const unsigned z2 = (unsigned)(c.z + 1) & m;
-#pragma unroll 1
-    for (int dx = -1; dx <= 1; ++dx) {
-        const unsigned bx = ((unsigned)(c.x + dx) & m) * D * D;
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; ++dy) {
-            const unsigned base = bx + ((unsigned)(c.y + dy) & m) * D;
-            if (z0 < z2) {
-                const int b = __ldg(off + base + z0), e = __ldg(off + base + z2 + 1);
-#pragma unroll 1
-                for (int j = b; j < e; ++j) f(j);
-            } else {
-                const int b1 = __ldg(off + base + z0), e1 = __ldg(off + base + D);
-#pragma unroll 1
-                for (int j = b1; j < e1; ++j) f(j);
-                const int b2 = __ldg(off + base), e2 = __ldg(off + base + z2 + 1);
-#pragma unroll 1
-                for (int j = b2; j < e2; ++j) f(j);
-            }
-        }
-    }
+    return C.scene_of ? __ldg(C.scene_of + i) : -1;
 }
-
-// Same walk restricted to sorted indices j >= lo (used by the reference-mode
-// density, which only sums j >= i).
-template <class F>
-__device__ __forceinline__ void for_each_candidate_from(float3 pi, int lo, const int *__restrict__ off,
-                                                        const SimConsts &C, F &&f)
+__device__ __forceinline__ GridView grid_view(const SimConsts &C, int s, const int *off)
 {
-    const int3 c = cell_of(pi, C);
-    const unsigned m = C.mask;
-    const unsigned D = (unsigned)C.D;
-    const unsigned z0 = (unsigned)(c.z - 1) & m;
-    const unsigned z2 = (unsigned)(c.z + 1) & m;
-#pragma unroll 1
-    for (int dx = -1; dx <= 1; ++dx) {
-        const unsigned bx = ((unsigned)(c.x + dx) & m) * D * D;
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; ++dy) {
-            const unsigned base = bx + ((unsigned)(c.y + dy) & m) * D;
-            if (z0 < z2) {
-                const int b = max(__ldg(off + base + z0), lo), e = __ldg(off + base + z2 + 1);
-#pragma unroll 1
-                for (int j = b; j < e; ++j) f(j);
-            } else {
-                const int b1 = max(__ldg(off + base + z0), lo), e1 = __ldg(off + base + D);
-#pragma unroll 1
-                for (int j = b1; j < e1; ++j) f(j);
-                const int b2 = max(__ldg(off + base), lo), e2 = __ldg(off + base + z2 + 1);
-#pragma unroll 1
-                for (int j = b2; j < e2; ++j) f(j);
-            }
-        }
-    }
+    if (s < 0) return GridView{C.D, C.mask, 0, off};
+    const SceneConsts &S = C.scn[s];
+    const int base = S.base;
+    return GridView{S.D, S.mask, base, off + base};
+}
+__device__ __forceinline__ float rest_density(const SimConsts &C, int s) { return s < 0 ? C.rho0 : C.scn[s].rho0; }
+__device__ __forceinline__ float inv_rest_density(const SimConsts &C, int s)
+{
+    return s < 0 ? C.inv_rho0 : C.scn[s].inv_rho0;
+}
+__device__ __forceinline__ float3 gravity_of(const SimConsts &C, int s)
+{
+    return s < 0 ? C.gravity : make_float3(C.scn[s].gx, C.scn[s].gy, C.scn[s].gz);
 }
 
 // Is any of the cells (x, y, z0..z0+2) flagged as holding an outlier (a
@@ -278,67 +257,6 @@ __device__ __forceinline__ bool masks_usable(const SimConsts &C, int i, int3 c, 
     return C.nl_mask && masks_state(C, i, c, pi) == 0;
 }
 
-// Candidate walk of particle i: the set bits of its neighbour masks when
-// they are valid, else the 27-cell walk.  A masked walk takes a column run
-// whole (every candidate, as the cell walk does) when one of its three cells
-// holds an outlier, because an outlier may have come within h without being
-// flagged; a pair of non-outliers moved by at most the skin in total, so
-// their masks flag every pair within h.  Both walks visit candidates column
-// by column in ascending sorted index, so every pair sum accumulates in the
-// same order either way; only indices j >= lo are visited.
-template <class F>
-__device__ __forceinline__ void for_each_neighbor(int i, float3 pi, int lo, const int *__restrict__ off,
-                                                  const SimConsts &C, F &&f)
-{
-    const int3 c = cell_of(pi, C);
-    const int state = C.nl_mask ? masks_state(C, i, c, pi) : 1;
-    if (C.nl_stats) atomicAdd(C.nl_stats + state, 1u);
-    if (state == 0) {
-        // One loop over all set bits of the 9 columns x 2 words (moving on
-        // when a word is exhausted), so the lanes of a warp diverge only on
-        // their total neighbour count.
-        const unsigned m = C.mask;
-        const unsigned D = (unsigned)C.D;
-        const unsigned z0 = (unsigned)(c.z - 1) & m;  // no wrap: masks are never built across it
-        int col = -1, b = 0;
-        unsigned long long bits = 0ull, next = 0ull;
-        bool second = true;
-        const unsigned wide = __ldg(C.nl_flags + i);
-#pragma unroll 1
-        while (true) {
-            while (bits == 0ull) {
-                if (!second) {  // second word of the current column
-                    second = true;
-                    bits = next;
-                    b += 64;
-                } else {
-                    if (++col == 9) return;
-                    second = false;
-                    const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
-                    const unsigned base = x * D * D + y * D + z0;
-                    b = __ldg(off + base);
-                    if (column_has_outlier(C, x, y, z0)) {
-                        const int len = __ldg(off + base + 3) - b;  // <= 128: the masks were built
-                        bits = len >= 64 ? ~0ull : ((1ull << len) - 1ull);
-                        next = len > 64 ? (len >= 128 ? ~0ull : ((1ull << (len - 64)) - 1ull)) : 0ull;
-                    } else {
-                        bits = __ldg(C.nl_mask + (size_t)(2 * col) * C.n + i);
-                        next = (wide & (kFlagWide << col)) ? __ldg(C.nl_mask + (size_t)(2 * col + 1) * C.n + i) : 0ull;
-                    }
-                }
-                if (lo > b) bits = (lo - b >= 64) ? 0ull : bits & (~0ull << (lo - b));
-            }
-            const int t = __ffsll((long long)bits) - 1;
-            bits &= bits - 1;
-            f(b + t);
-        }
-    }
-    if (lo > 0)
-        for_each_candidate_from(pi, lo, off, C, f);
-    else
-        for_each_candidate(pi, off, C, f);
-}
-
 // Records that particle i moved more than half the skin since the mask
 // build: flags its stored cell (the cell its sorted index belongs to) so
 // walks over that cell's column take every candidate.  Writers of P call it
@@ -355,20 +273,25 @@ __device__ __forceinline__ void track_displacement(const SimConsts &C, int i, fl
 
 // Plane walls: planeStabilize / particlePlaneCollisionConstraint
 // (K/particleplane.cuh:3-58) for one particle, planes in scene order.
-__device__ __forceinline__ void plane_stabilize(const SimConsts &C, float3 &x, float3 &p)
+// In a batched ensemble, scene s uses its own planes (s >= 0).
+template <class Planes>
+__device__ __forceinline__ void plane_stabilize_with(const SimConsts &C, int np, Planes planes, float3 &x, float3 &p)
 {
-    for (int k = 0; k < C.nplanes; ++k) {
-        const float3 o = f3(C.plane_o[k]), nn = f3(C.plane_n[k]);
+    for (int k = 0; k < np; ++k) {
+        float3 o, nn;
+        planes(k, o, nn);
         const float d = dot3(o - x, nn) + C.radius;
         if (d <= 0.f) continue;
         x += d * nn;
         p += d * nn;
     }
 }
-__device__ __forceinline__ void plane_collide(const SimConsts &C, float3 x, float3 &p)
+template <class Planes>
+__device__ __forceinline__ void plane_collide_with(const SimConsts &C, int np, Planes planes, float3 x, float3 &p)
 {
-    for (int k = 0; k < C.nplanes; ++k) {
-        const float3 o = f3(C.plane_o[k]), nn = f3(C.plane_n[k]);
+    for (int k = 0; k < np; ++k) {
+        float3 o, nn;
+        planes(k, o, nn);
         const float d = dot3(o - p, nn) + C.radius;
         if (d <= 0.f) continue;
         const float3 diff = p - x;
@@ -382,6 +305,29 @@ __device__ __forceinline__ void plane_collide(const SimConsts &C, float3 x, floa
             p = resolved - tdx;
         else
             p = resolved - tdx * fminf(C.fd * -dn / dtl, 1.0f);
+    }
+}
+// Planes of scene s (s < 0: the solver's one scene).
+__device__ __forceinline__ void plane_stabilize(const SimConsts &C, int s, float3 &x, float3 &p)
+{
+    if (s < 0) {
+        plane_stabilize_with(
+            C, C.nplanes, [&](int k, float3 &o, float3 &n) { o = f3(C.plane_o[k]); n = f3(C.plane_n[k]); }, x, p);
+    } else {
+        const SceneConsts &S = C.scn[s];
+        plane_stabilize_with(
+            C, S.nplanes, [&](int k, float3 &o, float3 &n) { o = f3(S.plane_o[k]); n = f3(S.plane_n[k]); }, x, p);
+    }
+}
+__device__ __forceinline__ void plane_collide(const SimConsts &C, int s, float3 x, float3 &p)
+{
+    if (s < 0) {
+        plane_collide_with(
+            C, C.nplanes, [&](int k, float3 &o, float3 &n) { o = f3(C.plane_o[k]); n = f3(C.plane_n[k]); }, x, p);
+    } else {
+        const SceneConsts &S = C.scn[s];
+        plane_collide_with(
+            C, S.nplanes, [&](int k, float3 &o, float3 &n) { o = f3(S.plane_o[k]); n = f3(S.plane_n[k]); }, x, p);
     }
 }
 

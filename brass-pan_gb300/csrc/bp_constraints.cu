@@ -23,7 +23,7 @@ __global__ void k_planes(SimConsts C, const float4 *__restrict__ Xs, float4 *__r
     if (i >= C.n) return;
     const float4 p4 = P[i];
     float3 p = f3(p4);
-    plane_collide(C, f3(Xs[i]), p);
+    plane_collide(C, scene_index(C, i), f3(Xs[i]), p);
     P[i] = make_float4(p.x, p.y, p.z, p4.w);
     track_displacement(C, i, p, true);
 }
@@ -62,6 +62,7 @@ void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // than two radii; mass-weighted projection plus friction averaged over the
 // counted contacts; only particle i moves (the reference's j update is
 // commented out).  Reads P, writes Pout = P + delta.
+template <bool Split>
 __global__ void __launch_bounds__(kWalkThreads) k_particle_collision(SimConsts C, const float4 *__restrict__ P,
                                                                      const float4 *__restrict__ Xs,
                                                                      const float *__restrict__ w,
@@ -75,47 +76,61 @@ __global__ void __launch_bounds__(kWalkThreads) k_particle_collision(SimConsts C
     if (i >= C.n) return;
     const float4 pi4 = P[i];
     const float3 xip = f3(pi4);
-    const float3 xi = f3(Xs[i]);
     const int phi = phase_of(pi4);
-    const float wi = w[i];
     const float r = C.radius;
-    float3 sd = make_float3(0.f, 0.f, 0.f), sf = make_float3(0.f, 0.f, 0.f);
-    int count = 0;
+    const GridView v = grid_view(C, scene_index(C, i), off);
+    // A fluid particle only meets solids.  If it walks its CTA's staged runs
+    // and they hold no solid, the walk would find nothing.
+    bool none = phi < 0 && walks_staged(C, v, i, cell_of(xip, C), &S, g) && !S.has_solid;
     // No contact partner within 2r + skin at mask build and the masks still
     // valid: no pair can be closer than 2r now, the walk would find nothing.
-    const bool none = C.nl_mask && C.nl_flags && !(C.nl_flags[i] & kFlagContact) &&
-                      masks_usable(C, i, cell_of(xip, C), xip) && !contact_outlier_near(C, xip);
-    if (!none) walk_neighbors(i, xip, 0, P, off, C, &S, g, [&](int j, float4 pj4) {
-        const int phj = phase_of(pj4);
-        if (!(j != i && phi != phj && (phi > 0 || phj > 0))) return;
-        const float3 xjp = f3(pj4);
-        const float3 diff = xip - xjp;
-        const float d2 = len2(diff);
-        if (!(d2 < r * r * 4.0f && d2 > 1e-5f)) return;
-        const float dist = __fsqrt_rn(d2);
-        const float wj = w[j];
-        const float w1 = __fdiv_rn(wi, __fadd_rn(wi, wj));
-        const float w2 = __fdiv_rn(wj, __fadd_rn(wi, wj));
-        const float3 proj = diff * __fsub_rn(__fdiv_rn(2.0f * r, dist), 1.0f);
-        const float3 dxi = w1 * proj;
-        const float3 xistar = dxi + xip;
-        sd += dxi;
-        const float3 dxj = -w2 * proj;
-        const float dxi2 = len2(dxi);
-        if (dxi2 > r * r * 0.001f * 0.001f) {
-            count += 1;
-            const float3 xj = f3(Xs[j]);
-            const float3 xjstar = dxj + xjp;
-            const float3 t1 = (xistar - xi) - (xjstar - xj);
-            const float3 nn = diff / dist;
-            const float3 tdx = t1 - dot3(t1, nn) * nn;
-            const float tl2 = len2(tdx);
-            if (tl2 <= __fmul_rn(C.fs * C.fs, dxi2))
-                sf -= w1 * tdx;
-            else
-                sf -= (w1 * tdx) * fminf(__fmul_rn(C.fd, __fsqrt_rn(__fdiv_rn(dxi2, tl2))), 1.0f);
-        }
-    });
+    none = none || (C.nl_mask && C.nl_flags && !(C.nl_flags[i] & kFlagContact) &&
+                    masks_usable(C, i, cell_of(xip, C), xip) && !contact_outlier_near(C, xip));
+    if (none) {  // p = x + 0, rounded as the walk's result would be
+        const float3 p = xip + make_float3(0.f, 0.f, 0.f);
+        Pout[i] = make_float4(p.x, p.y, p.z, pi4.w);
+        track_displacement(C, i, p, true);
+        return;
+    }
+    const float3 xi = f3(Xs[i]);
+    const float wi = w[i];
+    float3 sd = make_float3(0.f, 0.f, 0.f), sf = make_float3(0.f, 0.f, 0.f);
+    int count = 0;
+    walk_neighbors<Split>(
+        i, xip, 0, P, v, C, &S, g,
+        [&](int j, float4 pj4) {
+            const int phj = phase_of(pj4);
+            const float d2 = len2(xip - f3(pj4));
+            return j != i && phi != phj && (phi > 0 || phj > 0) && d2 < r * r * 4.0f && d2 > 1e-5f;
+        },
+        [&](int j, float4 pj4) {
+            const float3 xjp = f3(pj4);
+            const float3 diff = xip - xjp;
+            const float d2 = len2(diff);
+            const float dist = __fsqrt_rn(d2);
+            const float wj = w[j];
+            const float w1 = __fdiv_rn(wi, __fadd_rn(wi, wj));
+            const float w2 = __fdiv_rn(wj, __fadd_rn(wi, wj));
+            const float3 proj = diff * __fsub_rn(__fdiv_rn(2.0f * r, dist), 1.0f);
+            const float3 dxi = w1 * proj;
+            const float3 xistar = dxi + xip;
+            sd += dxi;
+            const float3 dxj = -w2 * proj;
+            const float dxi2 = len2(dxi);
+            if (dxi2 > r * r * 0.001f * 0.001f) {
+                count += 1;
+                const float3 xj = f3(Xs[j]);
+                const float3 xjstar = dxj + xjp;
+                const float3 t1 = (xistar - xi) - (xjstar - xj);
+                const float3 nn = diff / dist;
+                const float3 tdx = t1 - dot3(t1, nn) * nn;
+                const float tl2 = len2(tdx);
+                if (tl2 <= __fmul_rn(C.fs * C.fs, dxi2))
+                    sf -= w1 * tdx;
+                else
+                    sf -= (w1 * tdx) * fminf(__fmul_rn(C.fd, __fsqrt_rn(__fdiv_rn(dxi2, tl2))), 1.0f);
+            }
+        });
     const float3 d = (count == 0) ? sd : sd + sf / (float)count;
     const float3 p = xip + d;
     Pout[i] = make_float4(p.x, p.y, p.z, pi4.w);
@@ -126,7 +141,11 @@ void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4
                                const float *w, const int *off, float4 *Pout, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    k_particle_collision<<<(C.n + kWalkThreads - 1) / kWalkThreads, kWalkThreads, 0, st>>>(C, P, Xs, w, off, Pout);
+    const int grid = (C.n + kWalkThreads - 1) / kWalkThreads;
+    if (C.split)
+        k_particle_collision<true><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, Pout);
+    else
+        k_particle_collision<false><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, Pout);
     L->done(__func__);
 }
 

@@ -23,6 +23,7 @@ constexpr int kScanThreads = kWalkThreads;  // scan kernels stage their neighbou
 // Reference mode (Q1): density sums only sorted indices j >= i; solid
 // neighbours count x solid_scale; C = rho/rho0 - 1, clamped at 0 when Akinci
 // is on; lambda = -C / lambda_den.  Textbook mode: all j, exact denominator.
+template <bool Split>
 __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const float4 *__restrict__ P,
                                                          const float *__restrict__ mass,
                                                          const int *__restrict__ off, float *__restrict__ lam,
@@ -38,37 +39,40 @@ __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const floa
         lam[i] = 0.f;
         return;
     }
+    const int sc = scene_index(C, i);
+    const GridView v = grid_view(C, sc, off);
+    const float rho0 = rest_density(C, sc);
     const float3 pi = f3(pi4);
     float density = 0.f;
     if (!C.textbook) {
-        walk_neighbors(i, pi, i, P, off, C, &S, g, [&](int j, float4 pj) {
-            const float d2 = len2(pi - f3(pj));
-            if (d2 <= C.h2) {
-                const float ld = __fmul_rn(__ldg(mass + j), poly6(C, d2));
+        walk_neighbors<Split>(
+            i, pi, i, P, v, C, &S, g, [&](int, float4 pj) { return len2(pi - f3(pj)) <= C.h2; },
+            [&](int j, float4 pj) {
+                const float ld = __fmul_rn(__ldg(mass + j), poly6(C, len2(pi - f3(pj))));
                 density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
-            }
-        });
-        float c = density / C.rho0 - 1.0f;
+            });
+        float c = density / rho0 - 1.0f;
         if (C.clamp_c) c = fmaxf(c, 0.0f);
         lam[i] = -c / C.lambda_den;
     } else {
+        const float inv_rho0 = inv_rest_density(C, sc);
         float sum_g2 = 0.f;
         float3 gi = make_float3(0.f, 0.f, 0.f);
-        walk_neighbors(i, pi, 0, P, off, C, &S, g, [&](int j, float4 pj) {
-            const float3 diff = pi - f3(pj);
-            const float d2 = len2(diff);
-            if (d2 <= C.h2) {
+        walk_neighbors<Split>(
+            i, pi, 0, P, v, C, &S, g, [&](int, float4 pj) { return len2(pi - f3(pj)) <= C.h2; },
+            [&](int j, float4 pj) {
+                const float3 diff = pi - f3(pj);
+                const float d2 = len2(diff);
                 const float mj = __ldg(mass + j);
                 const float ld = __fmul_rn(mj, poly6(C, d2));
                 density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
                 if (d2 > 0.f) {
-                    const float3 g = __fmul_rn(-mj, C.inv_rho0) * spiky_grad_r(C, diff, d2, rsqrtf(d2));
+                    const float3 g = __fmul_rn(-mj, inv_rho0) * spiky_grad_r(C, diff, d2, rsqrtf(d2));
                     sum_g2 = __fadd_rn(sum_g2, dot3(g, g));
                     gi -= g;
                 }
-            }
-        });
-        float c = density / C.rho0 - 1.0f;
+            });
+        float c = density / rho0 - 1.0f;
         if (C.clamp_c) c = fmaxf(c, 0.0f);
         sum_g2 += dot3(gi, gi);
         lam[i] = -c / (sum_g2 + C.relaxation);
@@ -76,11 +80,18 @@ __global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const floa
     rho[i] = density;
 }
 
+// Kernels with a split walk (test, then body over the hits) and a fused one.
+#define BP_LAUNCH_SPLIT(kernel, grid, block, st, ...)                     \
+    do {                                                                  \
+        if (C.split) kernel<true><<<grid, block, 0, st>>>(__VA_ARGS__);   \
+        else kernel<false><<<grid, block, 0, st>>>(__VA_ARGS__);          \
+    } while (0)
+
 void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const float *mass, const int *off,
                    float *lam, float *rho, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    k_lambda<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, mass, off, lam, rho);
+    BP_LAUNCH_SPLIT(k_lambda, (C.n + kScanThreads - 1) / kScanThreads, kScanThreads, st, C, P, mass, off, lam, rho);
     L->done(__func__);
 }
 
@@ -89,6 +100,7 @@ void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // only visit b > a), to both ends.  In gather form particle k includes j when
 // the lower-indexed of (k, j) is fluid.  Textbook mode: fluid k gathers over
 // every neighbour; solids do not move.
+template <bool Split>
 __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs a)
 {
     __shared__ StageShared S;
@@ -99,16 +111,20 @@ __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs 
     const float4 pk4 = a.P[k];
     const int phk = phase_of(pk4);
     const float3 pk = f3(pk4);
+    const int sc = scene_index(C, k);
     float3 sum = make_float3(0.f, 0.f, 0.f);
     if (!(C.textbook && phk > 0)) {
         const float lk = a.lam[k];
-        walk_neighbors(k, pk, 0, a.P, a.off, C, &S, g, [&](int j, float4 pj4) {
-            if (j == k) return;
-            const float3 diff = pk - f3(pj4);
-            const float d2 = len2(diff);
-            if (d2 <= C.h2 && d2 > 0.f) {
+        walk_neighbors<Split>(
+            k, pk, 0, a.P, grid_view(C, sc, a.off), C, &S, g,
+            [&](int j, float4 pj4) {
+                const float d2 = len2(pk - f3(pj4));
                 const bool inc = C.textbook ? true : ((j > k) ? (phk < 0) : (phase_of(pj4) < 0));
-                if (!inc) return;
+                return j != k && d2 <= C.h2 && d2 > 0.f && inc;
+            },
+            [&](int j, float4 pj4) {
+                const float3 diff = pk - f3(pj4);
+                const float d2 = len2(diff);
                 float sl = __fadd_rn(lk, __ldg(a.lam + j));
                 if (C.scorr_on)
                     sl = __fsub_rn(sl, __fmul_rn(C.scorr_k, ipowf(__fmul_rn(poly6(C, d2), C.scorr_inv_wq), C.scorr_ni)));
@@ -118,12 +134,11 @@ __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs 
                     if (!(l2 < C.delta_clamp2)) delta = delta * __fmul_rn(C.delta_clamp, rsqrtf(l2));
                 }
                 sum = fma3(__ldg(a.mass + j), delta, sum);
-            }
-        });
+            });
     }
-    float3 p = pk + sum * C.inv_rho0;
+    float3 p = pk + sum * inv_rest_density(C, sc);
     if (a.epilogue == 1) {
-        plane_collide(C, f3(a.Xs[k]), p);
+        plane_collide(C, sc, f3(a.Xs[k]), p);
     } else if (a.epilogue == 2) {  // updateVelocity + updatePositions (PS:71-81, 121-137)
         const float4 xs = a.Xs[k];
         const float3 v = (p - f3(xs)) * C.inv_dt;
@@ -199,13 +214,14 @@ void launch_build_masks(cudaStream_t st, const SimConsts &C, const float4 *P, co
 void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    k_deltap<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, a);
+    BP_LAUNCH_SPLIT(k_deltap, (C.n + kScanThreads - 1) / kScanThreads, kScanThreads, st, C, a);
     L->done(__func__);
 }
 
 // Pass A: vorticity omega_i (fluidOmega) and Akinci normal n_i (fluidNormal)
 // in one walk over same-phase neighbours with 0 < r^2 <= h^2.
 // Om[i] = (omega, |omega|); Nm[i] = (h * n, rho_i).
+template <bool Split>
 __global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
                                                          const float *__restrict__ rho, const int *__restrict__ off,
@@ -223,16 +239,19 @@ __global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const floa
     const float3 vi = f3(V[i]);
     float3 om = make_float3(0.f, 0.f, 0.f), nn = make_float3(0.f, 0.f, 0.f);
     const bool want_om = C.use_vort, want_n = C.use_akinci;
-    walk_neighbors(i, pi, 0, P, off, C, &S, g, [&](int j, float4 pj4) {
-        if (j == i || phase_of(pj4) != phi) return;
-        const float3 diff = pi - f3(pj4);
-        const float d2 = len2(diff);
-        if (d2 <= C.h2 && d2 > 0.f) {
+    walk_neighbors<Split>(
+        i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, &S, g,
+        [&](int j, float4 pj4) {
+            const float d2 = len2(pi - f3(pj4));
+            return j != i && phase_of(pj4) == phi && d2 <= C.h2 && d2 > 0.f;
+        },
+        [&](int j, float4 pj4) {
+            const float3 diff = pi - f3(pj4);
+            const float d2 = len2(diff);
             const float3 g = spiky_grad_r(C, diff, d2, rsqrtf(d2));
             if (want_om) om += cross3(f3(V[j]) - vi, g);
             if (want_n) nn = fma3(__frcp_rn(__ldg(rho + j)), g, nn);
-        }
-    });
+        });
     Om[i] = make_float4(om.x, om.y, om.z, len3(om));
     const float3 n = C.h * nn;
     Nm[i] = make_float4(n.x, n.y, n.z, rho[i]);
@@ -242,6 +261,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const floa
 // (fluidAkinciTension), both on the same neighbours.  v' = v + eps (N x w) dt,
 // v'' = v' + F dt, exactly the reference's sequence (in-place update followed
 // by newVelocities = velocities + F dt).  Solids pass through.
+template <bool Split>
 __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
                                                          const float4 *__restrict__ Om,
@@ -260,18 +280,23 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
         Vout[i] = vi4;
         return;
     }
+    const int sc = scene_index(C, i);
+    const float two_rho0 = 2.0f * rest_density(C, sc);
     const float3 pi = f3(pi4);
     const float4 ni4 = Nm[i];
     const float3 ni = f3(ni4);
     const float rhoi = ni4.w;
     float3 eta = make_float3(0.f, 0.f, 0.f), ft = make_float3(0.f, 0.f, 0.f);
     const bool want_v = C.use_vort, want_t = C.use_akinci;
-    walk_neighbors(i, pi, 0, P, off, C, &S, g, [&](int j, float4 pj4) {
-        if (j == i || phase_of(pj4) != phi) return;
-        const float3 pj = f3(pj4);
-        const float3 diff = pi - pj;
-        const float d2 = len2(diff);
-        if (d2 <= C.h2 && d2 > 0.f) {
+    walk_neighbors<Split>(
+        i, pi, 0, P, grid_view(C, sc, off), C, &S, g,
+        [&](int j, float4 pj4) {
+            const float d2 = len2(pi - f3(pj4));
+            return j != i && phase_of(pj4) == phi && d2 <= C.h2 && d2 > 0.f;
+        },
+        [&](int j, float4 pj4) {
+            const float3 diff = pi - f3(pj4);
+            const float d2 = len2(diff);
             const float inv_r = rsqrtf(d2);
             if (want_v) eta = fma3(Om[j].w, spiky_grad_r(C, diff, d2, inv_r), eta);
             if (want_t) {
@@ -279,11 +304,10 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
                 const float dist = __fmul_rn(d2, inv_r);
                 const float3 fco = __fmul_rn(__fmul_rn(-C.tension, akinci_spline(C, dist)), inv_r) * diff;
                 const float3 fcu = (-C.tension) * (ni - f3(nj4));
-                const float kij = __fmul_rn(2.0f * C.rho0, __frcp_rn(__fadd_rn(rhoi, nj4.w)));
+                const float kij = __fmul_rn(two_rho0, __frcp_rn(__fadd_rn(rhoi, nj4.w)));
                 ft = fma3(kij, fco + fcu, ft);
             }
-        }
-    });
+        });
     float3 v = f3(vi4);
     if (want_v && len2(eta) > 1e-3f) {
         const float inv = 1.0f / sqrtf(dot3(eta, eta));
@@ -296,6 +320,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
 
 // Pass C: XSPH viscosity (fluidXSph): same phase, j != i, r^2 <= h^2 (r = 0
 // included).  Textbook mode weights each neighbour by its volume m_j / rho_j.
+template <bool Split>
 __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
                                                          const int *__restrict__ off, const float *__restrict__ mass,
@@ -315,15 +340,14 @@ __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const floa
     }
     const float3 pi = f3(pi4), vi = f3(vi4);
     float3 vn = make_float3(0.f, 0.f, 0.f);
-    walk_neighbors(i, pi, 0, P, off, C, &S, g, [&](int j, float4 pj4) {
-        if (j == i || phase_of(pj4) != phi) return;
-        const float d2 = len2(pi - f3(pj4));
-        if (d2 <= C.h2) {
-            float wgt = poly6(C, d2);
+    walk_neighbors<Split>(
+        i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, &S, g,
+        [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; },
+        [&](int j, float4 pj4) {
+            float wgt = poly6(C, len2(pi - f3(pj4)));
             if (C.textbook) wgt = __fmul_rn(wgt, __fdiv_rn(__ldg(mass + j), __ldg(rho + j)));
             vn = fma3(wgt, f3(V[j]) - vi, vn);
-        }
-    });
+        });
     const float3 v = vi + C.xsph_c * vn;
     Vout[i] = make_float4(v.x, v.y, v.z, vi4.w);
 }
@@ -332,43 +356,21 @@ void launch_post_a(cudaStream_t st, const SimConsts &C, const float4 *P, const f
                    const int *off, float4 *Om, float4 *Nm, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    k_post_a<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, V, rho, off, Om, Nm);
+    BP_LAUNCH_SPLIT(k_post_a, (C.n + kScanThreads - 1) / kScanThreads, kScanThreads, st, C, P, V, rho, off, Om, Nm);
     L->done(__func__);
 }
 void launch_post_b(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float4 *Om,
                    const float4 *Nm, const int *off, float4 *Vout, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    k_post_b<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, V, Om, Nm, off, Vout);
+    BP_LAUNCH_SPLIT(k_post_b, (C.n + kScanThreads - 1) / kScanThreads, kScanThreads, st, C, P, V, Om, Nm, off, Vout);
     L->done(__func__);
 }
 void launch_post_c(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
                    const float *mass, const float *rho, float4 *Vout, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    k_post_c<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, V, off, mass, rho, Vout);
-    L->done(__func__);
-}
-
-// Neighbour counts on the solver's grid: j in the 27 cells with r^2 <= h^2 (self included).
-__global__ void k_neighbor_counts(SimConsts C, const float4 *__restrict__ P, const int *__restrict__ off,
-                                  int *__restrict__ counts)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= C.n) return;
-    const float3 pi = f3(P[i]);
-    int cnt = 0;
-    for_each_candidate(pi, off, C, [&](int j) {
-        if (len2(pi - f3(P[j])) <= C.h2) ++cnt;
-    });
-    counts[i] = cnt;
-}
-
-void launch_neighbor_counts(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, int *counts,
-                            LaunchLog *L)
-{
-    if (C.n <= 0) return;
-    k_neighbor_counts<<<(C.n + 127) / 128, 128, 0, st>>>(C, P, off, counts);
+    BP_LAUNCH_SPLIT(k_post_c, (C.n + kScanThreads - 1) / kScanThreads, kScanThreads, st, C, P, V, off, mass, rho, Vout);
     L->done(__func__);
 }
 

@@ -215,21 +215,18 @@ void radix_sort_pairs(cudaStream_t st, int n, int D, const int *keys_in, const i
 
 // Tile layout identical to the sort (4096 keys per CTA) so the pass-0
 // histogram is produced here and the first upsweep is skipped.
-template <class Pos>
-__device__ __forceinline__ void hash_tile(int n, float cell, int D, Pos pos, int *__restrict__ keys,
-                                          int *__restrict__ hist, int tiles)
+template <class Key>
+__device__ __forceinline__ void hash_tile(int n, Key key_of, int *__restrict__ keys, int *__restrict__ hist, int tiles)
 {
     __shared__ int h[kRadixBins];
     for (int d = threadIdx.x; d < kRadixBins; d += kSortThreads) h[d] = 0;
     __syncthreads();
-    const unsigned m = (unsigned)D - 1u;
     const int base = blockIdx.x * kSortTile;
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
         const int idx = base + k * kSortThreads + threadIdx.x;
         if (idx < n) {
-            const float3 p = pos(idx);
-            const int key = cell_addr(cell_coord(p.x, cell), cell_coord(p.y, cell), cell_coord(p.z, cell), D, m);
+            const int key = key_of(idx);
             keys[idx] = key;
             atomicAdd(&h[key & (kRadixBins - 1)], 1);
         }
@@ -238,34 +235,53 @@ __device__ __forceinline__ void hash_tile(int n, float cell, int D, Pos pos, int
     for (int d = threadIdx.x; d < kRadixBins; d += kSortThreads) hist[(size_t)d * tiles + blockIdx.x] = h[d];
 }
 
+__device__ __forceinline__ int hash_key(float3 p, float cell, int D, unsigned m)
+{
+    return cell_addr(cell_coord(p.x, cell), cell_coord(p.y, cell), cell_coord(p.z, cell), D, m);
+}
+
 __global__ void __launch_bounds__(kSortThreads) k_hash_f3(int n, const float *__restrict__ pos3, float cell, int D,
                                                           int *__restrict__ keys, int *__restrict__ hist, int tiles)
 {
-    hash_tile(n, cell, D,
-              [&](int i) { return make_float3(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2]); }, keys, hist,
-              tiles);
+    const unsigned m = (unsigned)D - 1u;
+    hash_tile(
+        n,
+        [&](int i) { return hash_key(make_float3(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2]), cell, D, m); },
+        keys, hist, tiles);
 }
 
 // predictPositions + applyGravity (PS:59-69, 49-57) feeding the hash; the
 // rounding is pinned (no fused multiply-add) so that the prediction, and with
 // it every cell key, is bit-identical to a host evaluation of x + v*dt + (g*dt)*dt.
-__device__ __forceinline__ float3 predict(float3 x, float3 v, const SimConsts &C)
+__device__ __forceinline__ float3 predict(float3 x, float3 v, float3 gr, const SimConsts &C)
 {
     float3 p;
     p.x = __fadd_rn(x.x, __fmul_rn(v.x, C.dt));
     p.y = __fadd_rn(x.y, __fmul_rn(v.y, C.dt));
     p.z = __fadd_rn(x.z, __fmul_rn(v.z, C.dt));
-    p.x = __fadd_rn(p.x, __fmul_rn(__fmul_rn(C.gravity.x, C.dt), C.dt));
-    p.y = __fadd_rn(p.y, __fmul_rn(__fmul_rn(C.gravity.y, C.dt), C.dt));
-    p.z = __fadd_rn(p.z, __fmul_rn(__fmul_rn(C.gravity.z, C.dt), C.dt));
+    p.x = __fadd_rn(p.x, __fmul_rn(__fmul_rn(gr.x, C.dt), C.dt));
+    p.y = __fadd_rn(p.y, __fmul_rn(__fmul_rn(gr.y, C.dt), C.dt));
+    p.z = __fadd_rn(p.z, __fmul_rn(__fmul_rn(gr.z, C.dt), C.dt));
     return p;
 }
 
+// Cell key of the predicted position; in a batched ensemble the key of the
+// particle's scene grid, offset by the scene's first key.  Every particle of
+// a scene keeps its scene's index segment, so X/V index i has scene_of[i].
 __global__ void __launch_bounds__(kSortThreads) k_hash_state(SimConsts C, const float4 *__restrict__ X,
                                                              const float4 *__restrict__ V, int *__restrict__ keys,
                                                              int *__restrict__ hist, int tiles)
 {
-    hash_tile(C.n, C.cell, C.D, [&](int i) { return predict(f3(X[i]), f3(V[i]), C); }, keys, hist, tiles);
+    hash_tile(
+        C.n,
+        [&](int i) {
+            const int s = scene_index(C, i);
+            const float3 p = predict(f3(X[i]), f3(V[i]), gravity_of(C, s), C);
+            if (s < 0) return hash_key(p, C.cell, C.D, C.mask);
+            const SceneConsts &S = C.scn[s];
+            return S.base + hash_key(p, C.cell, S.D, S.mask);
+        },
+        keys, hist, tiles);
 }
 
 void launch_hash_f3(cudaStream_t st, int n, const float *pos3, float cell, int D, int *keys, int *hist,
@@ -363,17 +379,18 @@ __global__ void __launch_bounds__(256) k_reorder(SimConsts C, ReorderArgs a)
     const float4 X = a.Xc[o];
     const float4 V = a.Vc[o];
     const int id = a.orig_c[o];
+    const int s = scene_index(C, i);
     float3 x = f3(X), v = f3(V);
-    float3 p = predict(x, v, C);
+    float3 p = predict(x, v, gravity_of(C, s), C);
     if (a.inv_scaled) {
         const float scale = powf(2.7182818284f, -C.mass_k * x.y);
         a.inv_scaled[i] = 1.0f / (scale * X.w);
     }
     if (a.stabilize) {
-        plane_stabilize(C, x, p);
-        plane_stabilize(C, x, p);
+        plane_stabilize(C, s, x, p);
+        plane_stabilize(C, s, x, p);
     }
-    if (a.collide) plane_collide(C, x, p);
+    if (a.collide) plane_collide(C, s, x, p);
     a.Xs[i] = make_float4(x.x, x.y, x.z, X.w);
     a.Vs[i] = V;
     a.P[i] = make_float4(p.x, p.y, p.z, V.w);

@@ -107,8 +107,6 @@ void launch_post_b(cudaStream_t st, const SimConsts &C, const float4 *P, const f
                    const float4 *Nm, const int *off, float4 *Vout, LaunchLog *L);
 void launch_post_c(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
                    const float *mass, const float *rho, float4 *Vout, LaunchLog *L);
-void launch_neighbor_counts(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, int *counts,
-                            LaunchLog *L);
 void launch_neighbor_counts_f3(cudaStream_t st, int n, const float *pos3, float cell, int D, float h,
                                const int *start, const int *end, int *counts);
 

@@ -5,6 +5,7 @@
 // block (:881-993) and wind block (:838-858) enabled and the iteration count
 // as a parameter.  The whole call is captured once into a CUDA graph per
 // (substeps, iterations, dt, parameters) and replayed afterwards.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -69,6 +70,13 @@ struct bp_solver {
     SortScratch sort{};
 
     bool has_solid = false;
+    size_t ncells = 0;   // cells of the key space (D^3 for one scene)
+    int sort_dim = 0;    // a grid dimension whose key width covers every key (sort passes)
+    // batched ensembles (num_scenes == 0: one scene)
+    int num_scenes = 0;
+    std::vector<int> scene_first;  // num_scenes + 1 particle offsets
+    SceneConsts *scn = nullptr;
+    int *scene_of = nullptr;
     DistanceArgs dist{};
     WindArgs wind{};
     RigidArgs rigid{};
@@ -217,7 +225,10 @@ static SimConsts make_consts(const bp_solver *s, float sdt)
     C.dt = sdt;
     C.inv_dt = 1.0f / sdt;
     C.cell_keys = s->sorted_keys;  // stored cell of every particle (staged walks, masks)
+    C.scn = s->scn;
+    C.scene_of = s->scene_of;
     C.stage = (p.walk_options & BP_WALK_NO_STAGING) ? 0 : 1;
+    C.split = (p.walk_options & BP_WALK_NO_SPLIT) ? 0 : 1;
     if (p.neighbor_skin > 0.f) {
         C.nl_mask = s->nl_mask;
         C.nl_cell = s->nl_cell;
@@ -304,7 +315,17 @@ static bp_status validate_scene(const bp_scene_desc *sc)
     return BP_OK;
 }
 
-extern "C" bp_status bp_solver_create(const bp_scene_desc *sc, const bp_params *prm, void *stream, bp_solver **out)
+// The scenes of a batched ensemble: per-scene grids and constants.
+struct BatchSpec {
+    std::vector<int> first;             // particle offsets, num_scenes + 1
+    std::vector<SceneConsts> scenes;
+    size_t ncells = 0;
+    int sort_dim = 0;
+    int max_planes = 0;
+};
+
+static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, void *stream, const BatchSpec *batch,
+                               bp_solver **out)
 {
     if (!out) return fail(BP_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
@@ -340,7 +361,10 @@ extern "C" bp_status bp_solver_create(const bp_scene_desc *sc, const bp_params *
 
     const size_t N = (size_t)(n > 0 ? n : 1);
     const int D = prm->grid_dim;
-    const size_t ncells = (size_t)D * D * D;
+    const size_t ncells = batch ? batch->ncells : (size_t)D * D * D;
+    s->ncells = ncells;
+    s->sort_dim = batch ? batch->sort_dim : D;
+    const size_t NM = batch ? 1 : N;  // neighbour masks: single scenes only
     if ((st = s->alloc(&s->Xc, N)) || (st = s->alloc(&s->Vc, N)) || (st = s->alloc(&s->Xs, N)) ||
         (st = s->alloc(&s->Vs, N)) || (st = s->alloc(&s->Pa, N)) || (st = s->alloc(&s->Pb, N)) ||
         (st = s->alloc(&s->Om, N)) || (st = s->alloc(&s->Nm, N)) || (st = s->alloc(&s->orig_c, N)) ||
@@ -348,14 +372,14 @@ extern "C" bp_status bp_solver_create(const bp_scene_desc *sc, const bp_params *
         (st = s->alloc(&s->keys, N)) || (st = s->alloc(&s->sorted_keys, N)) || (st = s->alloc(&s->order, N)) ||
         (st = s->alloc(&s->off, ncells + 1)) || (st = s->alloc(&s->mass, N)) || (st = s->alloc(&s->lam, N)) ||
         (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)) ||
-        (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->nl_mask, 18 * N)) ||
-        (st = s->alloc(&s->nl_cell, N)) || (st = s->alloc(&s->nl_pos, N)) || (st = s->alloc(&s->nl_outlier, (size_t)D * D * ((D + 63) / 64))) ||
-        (st = s->alloc(&s->nl_flags, N)) || (st = s->alloc(&s->nl_stats, 4)))
+        (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->nl_mask, NM * 18)) ||
+        (st = s->alloc(&s->nl_cell, NM)) || (st = s->alloc(&s->nl_pos, NM)) || (st = s->alloc(&s->nl_outlier, (size_t)D * D * ((D + 63) / 64))) ||
+        (st = s->alloc(&s->nl_flags, NM)) || (st = s->alloc(&s->nl_stats, 4)))
         return bail(st);
     {
         char *scratch = nullptr;
-        if ((st = s->alloc(&scratch, sort_scratch_bytes((int)N, D)))) return bail(st);
-        sort_scratch_carve(scratch, (int)N, D, &s->sort);
+        if ((st = s->alloc(&scratch, sort_scratch_bytes((int)N, s->sort_dim)))) return bail(st);
+        sort_scratch_carve(scratch, (int)N, s->sort_dim, &s->sort);
     }
 
     // initial state in original order (sorted order == identity)
@@ -457,8 +481,150 @@ extern "C" bp_status bp_solver_create(const bp_scene_desc *sc, const bp_params *
         s->nimm = sc->num_immovables;
         if ((st = s->upload(&s->imm, sc->immovables, s->nimm))) return bail(st);
     }
+    if (batch) {
+        const int S = (int)batch->scenes.size();
+        std::vector<int> of(N, 0);
+        for (int k = 0; k < S; ++k)
+            for (int i = batch->first[k]; i < batch->first[k + 1]; ++i) of[i] = k;
+        if ((st = s->upload(&s->scn, batch->scenes.data(), S)) || (st = s->upload(&s->scene_of, of.data(), N)))
+            return bail(st);
+        s->num_scenes = S;
+        s->scene_first = batch->first;
+        s->nplanes = batch->max_planes;  // each scene's own planes are in its table entry
+    }
     BP_CUDA(cudaDeviceSynchronize());
     *out = s;
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_create(const bp_scene_desc *sc, const bp_params *prm, void *stream, bp_solver **out)
+{
+    return create_solver(sc, prm, stream, nullptr, out);
+}
+
+// Parameters that scenes of one batch may not differ in: everything except
+// rest density, gravity and grid dimension.
+static bool same_shared_params(const bp_params &a, const bp_params &b)
+{
+    bp_params x = a, y = b;
+    for (bp_params *p : {&x, &y}) {
+        p->rest_density = 0.f;
+        p->gravity[0] = p->gravity[1] = p->gravity[2] = 0.f;
+        p->grid_dim = 0;
+    }
+    return memcmp(&x, &y, sizeof(bp_params)) == 0;
+}
+
+extern "C" bp_status bp_batch_create(int32_t num_scenes, const bp_scene_desc *scenes, const bp_params *params,
+                                     void *stream, bp_solver **out)
+{
+    if (!out) return fail(BP_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (num_scenes <= 0 || !scenes || !params) return fail(BP_ERR_INVALID_ARGUMENT, "no scenes");
+    bp_status st;
+    BatchSpec spec;
+    spec.first.assign(num_scenes + 1, 0);
+    spec.scenes.resize(num_scenes);
+    int64_t total = 0;
+    size_t cells = 0;
+    for (int k = 0; k < num_scenes; ++k) {
+        if ((st = validate_scene(&scenes[k])) != BP_OK) return st;
+        if ((st = check_params(&params[k])) != BP_OK) return st;
+        if (!same_shared_params(params[0], params[k]))
+            return fail(BP_ERR_INVALID_ARGUMENT,
+                        "scenes of a batch differ only in rest_density, gravity and grid_dim");
+        if (params[k].neighbor_skin > 0.f)
+            return fail(BP_ERR_INVALID_ARGUMENT, "neighbour masks (neighbor_skin > 0) are not available in a batch");
+        spec.first[k] = (int)total;
+        total += scenes[k].num_particles;
+        if (total > (1 << 28)) return fail(BP_ERR_CAPACITY, "a batch holds at most 2^28 particles");
+        SceneConsts &c = spec.scenes[k];
+        memset(&c, 0, sizeof(c));
+        const int D = params[k].grid_dim;
+        c.D = D;
+        c.mask = (unsigned)D - 1u;
+        c.base = (int)cells;
+        cells += (size_t)D * D * D;
+        if (cells >= ((size_t)1 << 30)) return fail(BP_ERR_CAPACITY, "a batch's grids hold at most 2^30 cells");
+        c.rho0 = params[k].rest_density;
+        c.inv_rho0 = 1.0f / params[k].rest_density;
+        c.gx = params[k].gravity[0];
+        c.gy = params[k].gravity[1];
+        c.gz = params[k].gravity[2];
+        c.nplanes = scenes[k].num_planes;
+        for (int q = 0; q < c.nplanes; ++q) {
+            const float *pl = scenes[k].planes + 6 * q;
+            c.plane_o[q] = make_float4(pl[0], pl[1], pl[2], 0.f);
+            c.plane_n[q] = make_float4(pl[3], pl[4], pl[5], 0.f);
+        }
+        spec.max_planes = std::max(spec.max_planes, c.nplanes);
+    }
+    spec.first[num_scenes] = (int)total;
+    spec.ncells = cells;
+    spec.sort_dim = 4;
+    while ((size_t)spec.sort_dim * spec.sort_dim * spec.sort_dim < cells) spec.sort_dim *= 2;
+
+    // one scene description: the scenes' particles and constraints concatenated, ids offset
+    const int n = (int)total;
+    std::vector<float> pos(3 * (size_t)n), vel(3 * (size_t)n, 0.f), mass(n), rest;
+    std::vector<int32_t> phase(n), group(n, 0), pairs, faces, ranges, imm;
+    std::vector<float> dparams;
+    bool any_rigid = false;
+    for (int k = 0; k < num_scenes; ++k) any_rigid |= scenes[k].num_rigid_bodies > 0;
+    if (any_rigid) rest.assign(3 * (size_t)n, 0.f);
+    for (int k = 0; k < num_scenes; ++k) {
+        const bp_scene_desc &d = scenes[k];
+        const int o = spec.first[k], m = d.num_particles;
+        if (m == 0) continue;
+        std::copy(d.positions, d.positions + 3 * (size_t)m, pos.begin() + 3 * (size_t)o);
+        if (d.velocities) std::copy(d.velocities, d.velocities + 3 * (size_t)m, vel.begin() + 3 * (size_t)o);
+        std::copy(d.masses, d.masses + m, mass.begin() + o);
+        std::copy(d.phases, d.phases + m, phase.begin() + o);
+        if (d.group_ids) std::copy(d.group_ids, d.group_ids + m, group.begin() + o);
+        for (int e = 0; e < 2 * d.num_distance_constraints; ++e) pairs.push_back(d.distance_pairs[e] + o);
+        dparams.insert(dparams.end(), d.distance_params, d.distance_params + 2 * (size_t)d.num_distance_constraints);
+        for (int e = 0; e < 3 * d.num_wind_faces; ++e) faces.push_back(d.wind_faces[e] + o);
+        for (int e = 0; e < 2 * d.num_rigid_bodies; ++e) ranges.push_back(d.rigid_ranges[e] + o);
+        if (d.num_rigid_bodies > 0)
+            std::copy(d.rigid_rest_positions, d.rigid_rest_positions + 3 * (size_t)m, rest.begin() + 3 * (size_t)o);
+        for (int e = 0; e < d.num_immovables; ++e) imm.push_back(d.immovables[e] + o);
+    }
+    bp_scene_desc all;
+    memset(&all, 0, sizeof(all));
+    all.num_particles = n;
+    all.positions = pos.data();
+    all.velocities = vel.data();
+    all.masses = mass.data();
+    all.phases = phase.data();
+    all.group_ids = group.data();
+    all.num_distance_constraints = (int)(pairs.size() / 2);
+    all.distance_pairs = pairs.data();
+    all.distance_params = dparams.data();
+    all.num_wind_faces = (int)(faces.size() / 3);
+    all.wind_faces = faces.data();
+    all.num_rigid_bodies = (int)(ranges.size() / 2);
+    all.rigid_ranges = ranges.data();
+    all.rigid_rest_positions = any_rigid ? rest.data() : nullptr;
+    all.num_immovables = (int)imm.size();
+    all.immovables = imm.data();
+    bp_params shared = params[0];
+    shared.grid_dim = 4;  // unused: every particle walks its scene's grid
+    return create_solver(&all, &shared, stream, &spec, out);
+}
+
+extern "C" bp_status bp_batch_step(bp_solver *s, float dt, int32_t num_substeps, int32_t iterations)
+{
+    if (s && s->num_scenes == 0) return fail(BP_ERR_INVALID_ARGUMENT, "not a batch (use bp_solver_step)");
+    return bp_solver_step(s, dt, num_substeps, iterations);
+}
+
+extern "C" bp_status bp_batch_scene_range(const bp_solver *s, int32_t scene, int32_t *first, int32_t *count)
+{
+    if (!s || !first || !count) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (s->num_scenes == 0) return fail(BP_ERR_INVALID_ARGUMENT, "not a batch");
+    if (scene < 0 || scene >= s->num_scenes) return fail(BP_ERR_INVALID_ARGUMENT, "scene out of range");
+    *first = s->scene_first[scene];
+    *count = s->scene_first[scene + 1] - s->scene_first[scene];
     return BP_OK;
 }
 
@@ -475,8 +641,18 @@ extern "C" bp_status bp_solver_set_params(bp_solver *s, const bp_params *prm)
     if (!s) return fail(BP_ERR_INVALID_ARGUMENT, "solver is NULL");
     bp_status st = check_params(prm);
     if (st != BP_OK) return st;
-    if (prm->grid_dim != s->prm.grid_dim) return fail(BP_ERR_INVALID_ARGUMENT, "grid_dim cannot change after creation");
-    s->prm = *prm;
+    if (s->num_scenes > 0) {
+        // a batch keeps each scene's grid, rest density and gravity from creation
+        if (prm->neighbor_skin > 0.f)
+            return fail(BP_ERR_INVALID_ARGUMENT, "neighbour masks (neighbor_skin > 0) are not available in a batch");
+        const int D = s->prm.grid_dim;
+        s->prm = *prm;
+        s->prm.grid_dim = D;
+    } else {
+        if (prm->grid_dim != s->prm.grid_dim)
+            return fail(BP_ERR_INVALID_ARGUMENT, "grid_dim cannot change after creation");
+        s->prm = *prm;
+    }
     s->params_version++;
     return BP_OK;
 }
@@ -496,13 +672,11 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
     const bool immov = (mask & BP_STAGE_IMMOVABLE) && s->nimm > 0;
     const bool picking = picked >= 0;
     const bool tail = distance || rigid || immov;  // stages after the fluid position pass
-    const int D = s->prm.grid_dim;
-
     if (picking) launch_pick(st, picked, s->to_new, s->Xc, ppos, 1, s->Vc, make_float3(0.f, 0.f, 0.f), L);
 
     launch_hash_state(st, C, s->Xc, s->Vc, s->keys, s->sort.hist, L);
-    radix_sort_pairs(st, s->n, D, s->keys, nullptr, s->sorted_keys, s->order, s->sort, true, L);
-    launch_cell_offsets(st, s->n, D * D * D, s->sorted_keys, s->off, L);
+    radix_sort_pairs(st, s->n, s->sort_dim, s->keys, nullptr, s->sorted_keys, s->order, s->sort, true, L);
+    launch_cell_offsets(st, s->n, (int)s->ncells, s->sorted_keys, s->off, L);
 
     const bool fuse_first_planes = planes && !wind && !picking && iterations > 0;
     ReorderArgs ra;
@@ -802,7 +976,6 @@ extern "C" bp_status bp_solver_field(bp_solver *s, int32_t field, void **ptr, si
 {
     if (!s || !ptr || !bytes) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
     const size_t n = (size_t)s->n;
-    const int D = s->prm.grid_dim;
     switch (field) {
     case BP_FIELD_POSITIONS: *ptr = s->Xc; *bytes = n * 16; break;
     case BP_FIELD_NEW_POSITIONS: *ptr = s->Pcur; *bytes = n * 16; break;
@@ -812,7 +985,7 @@ extern "C" bp_status bp_solver_field(bp_solver *s, int32_t field, void **ptr, si
     case BP_FIELD_LAMBDAS: *ptr = s->lam; *bytes = n * 4; break;
     case BP_FIELD_DENSITIES: *ptr = s->rho; *bytes = n * 4; break;
     case BP_FIELD_SORTED_CELL_IDS: *ptr = s->sorted_keys; *bytes = n * 4; break;
-    case BP_FIELD_CELL_OFFSETS: *ptr = s->off; *bytes = ((size_t)D * D * D + 1) * 4; break;
+    case BP_FIELD_CELL_OFFSETS: *ptr = s->off; *bytes = (s->ncells + 1) * 4; break;
     case BP_FIELD_RIGID_ROTATIONS: *ptr = s->rigid.rot; *bytes = (size_t)s->rigid.num_bodies * 16; break;
     case BP_FIELD_RIGID_CMS: *ptr = s->rigid.cm; *bytes = (size_t)s->rigid.num_bodies * 16; break;
     case BP_FIELD_INV_SCALED_MASSES: *ptr = s->w; *bytes = n * 4; break;

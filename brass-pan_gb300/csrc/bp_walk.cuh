@@ -15,6 +15,15 @@
 // ascending sorted index within a column, or the subset of them flagged in
 // the particle's neighbour masks (see SimConsts::nl_mask); the pair sums of
 // the scan kernels therefore accumulate in the same order on every path.
+//
+// A walk takes two functions: test(j, pj), the cheap pair filter (distance,
+// phases), and body(j, pj), the pair term.  Split walks first test a chunk of
+// up to 32 candidates into a bit mask and then run the body over the set
+// bits only, so a warp issues the body about as often as its busiest lane
+// has neighbours, instead of once per candidate of the longest run.
+//
+// In a batched ensemble the walk uses the grid of the particle's own scene
+// (GridView); a CTA whose particles belong to two scenes is not staged.
 #pragma once
 
 #include "bp_common.cuh"
@@ -34,22 +43,32 @@ struct StageShared {
     int first1;  // first thread of the second column group
     int ngroups;
     int ok;
+    int scene;
+    int has_solid;  // a staged particle has a positive (solid) phase
 };
 
 // Collective: every thread of the CTA must call it (before any early exit).
 // Returns the calling thread's column group (0 or 1), or -1 when the CTA does
 // not use shared memory or the thread has no particle.
 __device__ __forceinline__ int stage_block(const SimConsts &C, const float4 *__restrict__ P,
-                                           const int *__restrict__ off, int i0, StageShared &S)
+                                           const int *__restrict__ off_all, int i0, StageShared &S)
 {
     if (!C.stage) return -1;  // uniform across the grid: no barrier skipped unevenly
     const int t = threadIdx.x;
     const int i = i0 + t;
     const bool valid = i < C.n;
-    const unsigned D = (unsigned)C.D, m = C.mask;
-    const int key = valid ? __ldg(C.cell_keys + i) : -1;
+    if (t == 0) {
+        S.scene = scene_index(C, i0);
+        S.first1 = kWalkThreads;
+        S.has_solid = 0;
+    }
+    __syncthreads();
+    const int s0 = S.scene;
+    if (!__syncthreads_and(!valid || scene_index(C, i) == s0)) return -1;
+    const GridView v = grid_view(C, s0, off_all);
+    const unsigned D = (unsigned)v.D, m = v.mask;
+    const int key = valid ? __ldg(C.cell_keys + i) - v.base : -1;
     S.keys[t] = key;
-    if (t == 0) S.first1 = kWalkThreads;
     __syncthreads();
     const bool boundary = valid && (t == 0 || (unsigned)key / D != (unsigned)S.keys[t - 1] / D);
     const int G = __syncthreads_count(boundary);
@@ -68,14 +87,14 @@ __device__ __forceinline__ int stage_block(const SimConsts &C, const float4 *__r
         const unsigned nx = (x + (unsigned)(k / 3) - 1u) & m, ny = (y + (unsigned)(k % 3) - 1u) & m;
         const unsigned base = (nx * D + ny) * D;
         const int a = max(zlo, 0), b = min(zhi, (int)D - 1);
-        const int sa = __ldg(off + base + a), ea = __ldg(off + base + b + 1);
+        const int sa = __ldg(v.off + base + a), ea = __ldg(v.off + base + b + 1);
         int sb = 0, eb = 0;
         if (zlo < 0 && zhi <= (int)D - 1) {  // wraps below: cell D-1
-            sb = __ldg(off + base + D - 1);
-            eb = __ldg(off + base + D);
+            sb = __ldg(v.off + base + D - 1);
+            eb = __ldg(v.off + base + D);
         } else if (zhi > (int)D - 1 && zlo >= 0) {  // wraps above: cell 0
-            sb = __ldg(off + base);
-            eb = __ldg(off + base + 1);
+            sb = __ldg(v.off + base);
+            eb = __ldg(v.off + base + 1);
         }
         S.gstart[2 * t] = sa;
         S.len[2 * t] = ea - sa;
@@ -94,10 +113,16 @@ __device__ __forceinline__ int stage_block(const SimConsts &C, const float4 *__r
     }
     __syncthreads();
     if (!S.ok) return -1;
+    bool solid = false;
     for (int s = 0; s < 2 * G * 9; ++s) {
         const int gs = S.gstart[s], l = S.len[s], sb = S.sbase[s];
-        for (int u = t; u < l; u += kWalkThreads) S.pos[sb + u] = P[gs + u];
+        for (int u = t; u < l; u += kWalkThreads) {
+            const float4 q = P[gs + u];
+            solid |= phase_of(q) > 0;
+            S.pos[sb + u] = q;
+        }
     }
+    if (solid) S.has_solid = 1;
     __syncthreads();
     if (!valid) return -1;
     return (G == 2 && t >= S.first1) ? 1 : 0;
@@ -112,21 +137,60 @@ __device__ __forceinline__ int staged_index(const StageShared &S, int g, int k, 
     return -1;
 }
 
+// Does particle i walk its CTA's staged runs (it is still in its stored cell)?
+__device__ __forceinline__ bool walks_staged(const SimConsts &C, const GridView &v, int i, int3 c,
+                                             const StageShared *S, int g)
+{
+    return S != nullptr && g >= 0 && cell_addr(c.x, c.y, c.z, v.D, v.mask) + v.base == __ldg(C.cell_keys + i);
+}
+
+// Candidates [jb, e) of one run, read from src[j - b]: the test of each pair,
+// then the body of those that pass, in ascending j.
+template <bool Split, class T, class B>
+__device__ __forceinline__ void walk_run(int jb, int b, int e, const float4 *src, T &test, B &body)
+{
+    if constexpr (!Split) {
+#pragma unroll 1
+        for (int j = jb; j < e; ++j) {
+            const float4 pj = src[j - b];
+            if (test(j, pj)) body(j, pj);
+        }
+    } else {
+#pragma unroll 1
+        for (int j0 = jb; j0 < e; j0 += 32) {
+            const int cnt = min(32, e - j0);
+            const float4 *s = src + (j0 - b);
+            unsigned bits = 0u;
+#pragma unroll 4
+            for (int t = 0; t < cnt; ++t)
+                if (test(j0 + t, s[t])) bits |= 1u << t;
+#pragma unroll 1
+            while (bits) {
+                const int t = __ffs(bits) - 1;
+                bits &= bits - 1u;
+                body(j0 + t, s[t]);
+            }
+        }
+    }
+}
+
 // Walk of particle i (sorted index) at position pi over the candidates
-// j >= lo of its 27 cells; calls f(j, P[j]).  S / g come from stage_block
-// (S == nullptr or g < 0: no staging).  Masked walks take each column's set
-// bits in ascending order; a column holding an outlier is walked whole.  The
-// pair arithmetic of the callers uses explicitly rounded operations, so the
-// two inlined copies of f (masked and cell walk) produce the same bits.
-template <class F>
+// j >= lo of its 27 cells on grid v: body(j, P[j]) for every j with
+// test(j, P[j]).  S / g come from stage_block (S == nullptr or g < 0: no
+// staging).  Masked walks take each column's set bits in ascending order; a
+// column holding an outlier is walked whole.  The pair arithmetic of the
+// callers uses explicitly rounded operations, so every inlined copy of the
+// pair functions produces the same bits.
+template <bool Split, class T, class B>
 __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const float4 *__restrict__ P,
-                                               const int *__restrict__ off, const SimConsts &C,
-                                               const StageShared *S, int g, F &&f)
+                                               const GridView &v, const SimConsts &C, const StageShared *S, int g,
+                                               T &&test, B &&body)
 {
     const int3 c = cell_of(pi, C);
-    const unsigned m = C.mask;
-    const unsigned D = (unsigned)C.D;
-    const bool staged = S != nullptr && g >= 0 && cell_addr(c.x, c.y, c.z, C.D, C.mask) == __ldg(C.cell_keys + i);
+    const unsigned m = v.mask;
+    const unsigned D = (unsigned)v.D;
+    const int *__restrict__ off = v.off;
+    const bool staged = walks_staged(C, v, i, c, S, g);
     const int state = C.nl_mask ? masks_state(C, i, c, pi) : 1;
     if (C.nl_stats) atomicAdd(C.nl_stats + state, 1u);
     const unsigned z0 = (unsigned)(c.z - 1) & m;
@@ -160,7 +224,8 @@ __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const f
                 while (bits) {
                     const int t = 64 * k + __ffsll((long long)bits) - 1;
                     bits &= bits - 1;
-                    f(cb + t, src[t]);
+                    const float4 pj = src[t];
+                    if (test(cb + t, pj)) body(cb + t, pj);
                 }
             }
         }
@@ -180,8 +245,7 @@ __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const f
             const int b = __ldg(off + base + za), e = __ldg(off + base + zb + 1);
             const int sidx = staged ? staged_index(*S, g, col, b, e) : -1;
             const float4 *src = sidx >= 0 ? S->pos + sidx : P + b;
-#pragma unroll 1
-            for (int j = max(b, lo); j < e; ++j) f(j, src[j - b]);
+            walk_run<Split>(max(b, lo), b, e, src, test, body);
         }
     }
 }

@@ -44,6 +44,7 @@ class Scene:
     cell_size: float = 0.115
     grid_dim: int = 512
     rest_density: float = 1200.0
+    gravity: tuple = (0.0, -9.8, 0.0)
     name: str = "scene"
 
     @property
@@ -260,3 +261,37 @@ def config1_mixed(seed=0, fluid=(128, 64, 128), cloth=256, cubes=64, cube_dim=8)
         start = (0.5 + cx * (box[0] - 1.0) / ncube, y + 2.0 + (c % 3) * 1.0, 0.5 + cz * (box[2] - 1.0) / ncube)
         s.add_rigid_box((cube_dim,) * 3, start, (d, d, d), m)
     return s
+
+
+def ensemble_member(n_target, spacing=0.1, seed=0, rest_scale=1.0, gravity=9.8):
+    """One scene of the batched ensemble: a dam break of about n_target fluid
+    particles (an a x b x a block, b = a/2) in the corner of a box 1.5 times the
+    block's footprint and twice its height; the grid covers the box (D the next
+    power of two of its cells per axis).  Returns the scene and the
+    rest-density and gravity of the member."""
+    d = float(np.float32(spacing))
+    a = max(2, int(round((2.0 * n_target) ** (1.0 / 3.0))))
+    b = max(1, int(round(n_target / (a * a))))
+    box = (1.5 * a * d + 0.2, 2.0 * b * d + 0.2, 1.5 * a * d + 0.2)
+    cells = int(np.ceil(max(box) / (2 * d)))
+    D = 16
+    while D < cells:
+        D *= 2
+    s = pbf_scene(a, b, a, spacing=spacing, seed=seed, box=box, grid_dim=D)
+    s.name = f"ensemble_{a}x{b}x{a}"
+    s.rest_density = s.rest_density * float(rest_scale)
+    s.gravity = (0.0, -float(gravity), 0.0)
+    return s
+
+
+def config3_ensemble(seed=0, num_scenes=256, lo=4096, hi=262144):
+    """The batched ensemble: num_scenes dam breaks whose particle counts are
+    drawn log-uniform in [lo, hi], rest density scaled uniform in [0.8, 1.2],
+    gravity magnitude uniform in [5, 15], boxes scaled to the particle count."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(num_scenes):
+        n = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        out.append(ensemble_member(n, seed=seed * 100003 + k, rest_scale=rng.uniform(0.8, 1.2),
+                                   gravity=rng.uniform(5.0, 15.0)))
+    return out

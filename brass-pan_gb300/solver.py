@@ -27,6 +27,8 @@ def make_params(scene: Scene | None = None, mode: int = abi.BP_MODE_REFERENCE, s
         p.cell_size = scene.cell_size
         p.grid_dim = scene.grid_dim
         p.rest_density = scene.rest_density
+        for k in range(3):
+            p.gravity[k] = scene.gravity[k]
     p.mode = mode
     if stage_mask is not None:
         p.stage_mask = stage_mask
@@ -168,3 +170,47 @@ class ParticleSolver:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class BatchSolver(ParticleSolver):
+    """Many independent scenes stepped together (bp_batch_create).
+
+    The handle is a solver over the scenes' particles in scene order; every
+    ParticleSolver method applies to all of them at once, and scene_positions /
+    scene_velocities slice one scene out."""
+
+    def __init__(self, scenes: list[Scene], params: list[abi.BpParams] | None = None, stream: int | None = None):
+        self.lib = abi.load()
+        self.scenes = list(scenes)
+        self.scene = None
+        plist = params if params is not None else [make_params(s) for s in self.scenes]
+        self.params_list = list(plist)
+        self.params = self.params_list[0]
+        descs = (abi.BpSceneDesc * len(self.scenes))()
+        self._keep = []
+        for k, s in enumerate(self.scenes):
+            d, keep = abi.scene_desc(s)
+            descs[k] = d
+            self._keep.append(keep)
+        parr = (abi.BpParams * len(self.params_list))(*self.params_list)
+        h = C.c_void_p()
+        abi.check(self.lib, self.lib.bp_batch_create(len(self.scenes), descs, parr,
+                                                     C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.handle = h
+        self.n = sum(s.num_particles for s in self.scenes)
+        self.ranges = []
+        for k in range(len(self.scenes)):
+            first, count = C.c_int32(), C.c_int32()
+            abi.check(self.lib, self.lib.bp_batch_scene_range(self.handle, k, C.byref(first), C.byref(count)))
+            self.ranges.append((first.value, count.value))
+
+    def step(self, dt: float, substeps: int, iterations: int):
+        abi.check(self.lib, self.lib.bp_batch_step(self.handle, C.c_float(dt), substeps, iterations))
+
+    def scene_positions(self, k: int) -> np.ndarray:
+        first, count = self.ranges[k]
+        return self.positions()[first:first + count]
+
+    def scene_velocities(self, k: int) -> np.ndarray:
+        first, count = self.ranges[k]
+        return self.velocities()[first:first + count]

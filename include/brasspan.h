@@ -77,9 +77,13 @@ typedef enum bp_mode {
 #define BP_STAGE_REFERENCE_AS_SHIPPED \
     (BP_STAGE_PLANES | BP_STAGE_VORTICITY | BP_STAGE_AKINCI | BP_STAGE_XSPH)
 
-/* bp_params.walk_options: read every neighbour from global memory instead of
- * staging each block's neighbourhood in shared memory (results are identical). */
+/* bp_params.walk_options (results are identical under every combination):
+ * BP_WALK_NO_STAGING reads every neighbour from global memory instead of
+ * staging each block's neighbourhood in shared memory; BP_WALK_NO_SPLIT
+ * evaluates each pair term as its candidate is tested instead of testing a
+ * chunk of candidates first and evaluating the pair terms of the hits. */
 #define BP_WALK_NO_STAGING 0x1
+#define BP_WALK_NO_SPLIT 0x2
 
 /* Every literal of the reference's step as a field.  bp_params_init fills the
  * reference's values; comments give the reference location of each. */
@@ -238,6 +242,27 @@ bp_status bp_solver_profile(bp_solver *s, int32_t num_substeps, float dt, int32_
  * its masks were built for, [3] some particle moved more than half the skin. */
 bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
                                uint64_t out_walks[4]);
+
+/* ---- Batched ensembles ----------------------------------------------------
+ * No counterpart in the reference, which steps one scene per solver.  Many
+ * independent scenes advance together, one kernel launch per stage over all
+ * of their particles: each scene keeps its own hash grid (params[k].grid_dim)
+ * inside one shared key space, its own rest density, gravity and planes, and
+ * every other parameter is shared (params[k] may differ from params[0] only
+ * in rest_density, gravity and grid_dim; neighbour masks are not available).
+ * Scene k's particles, stepped in a batch, follow exactly the trajectory a
+ * solver of scene k alone gives.
+ *
+ * The batch is a bp_solver: its particles are the scenes' particles in scene
+ * order (scene k's particle i has original id first_k + i, first_k from
+ * bp_batch_scene_range), and every bp_solver_* entry point applies to it.
+ * Capacity: 2^28 particles, 2^30 grid cells in total. */
+bp_status bp_batch_create(int32_t num_scenes, const bp_scene_desc *scenes, const bp_params *params,
+                          void *stream, bp_solver **out);
+/* bp_solver_step of a batch (BP_ERR_INVALID_ARGUMENT for a single-scene solver). */
+bp_status bp_batch_step(bp_solver *batch, float dt, int32_t num_substeps, int32_t iterations);
+/* First original id and particle count of scene `scene`. */
+bp_status bp_batch_scene_range(const bp_solver *batch, int32_t scene, int32_t *first, int32_t *count);
 
 /* ---- Stand-alone hash grid on caller-owned device buffers ---------------
  * Replaces updateGrid() (particlesolver.cuh:712-765): updateGridId

@@ -126,3 +126,55 @@ def test_create_without_device_reports_no_device(bp):
     s = bp.scenes.pbf_scene(3, 3, 3)
     st, _ = _create(bp, s, bp.make_params(s))
     assert st == bp.abi.BP_ERR_NO_DEVICE
+
+
+def _create_batch(bp, scenes, params):
+    lib = bp.abi.load()
+    descs = (bp.abi.BpSceneDesc * len(scenes))()
+    keep = []
+    for k, s in enumerate(scenes):
+        d, kk = bp.abi.scene_desc(s)
+        descs[k] = d
+        keep.append(kk)
+    parr = (bp.abi.BpParams * len(params))(*params)
+    h = C.c_void_p()
+    st = lib.bp_batch_create(len(scenes), descs, parr, None, C.byref(h))
+    if st == bp.abi.BP_OK:
+        lib.bp_solver_destroy(h)
+    return st, lib.bp_last_error_string().decode()
+
+
+@pytest.mark.skipif(cuda_available(), reason="checks the argument validation that runs before the device check")
+def test_batch_create_validates_scene_parameters(bp):
+    a = bp.scenes.ensemble_member(200, seed=1)
+    b = bp.scenes.ensemble_member(500, seed=2, rest_scale=0.9, gravity=12.0)
+    pa, pb = bp.make_params(a), bp.make_params(b)
+    assert pa.grid_dim != pb.grid_dim or pa.rest_density != pb.rest_density
+    # rest density, gravity and grid dimension may differ: the call gets as far as the device
+    assert _create_batch(bp, [a, b], [pa, pb])[0] == bp.abi.BP_ERR_NO_DEVICE
+    # anything else may not
+    pc = bp.make_params(b, xsph_c=0.01)
+    st, msg = _create_batch(bp, [a, b], [pa, pc])
+    assert st == bp.abi.BP_ERR_INVALID_ARGUMENT and "differ only" in msg
+    pd = bp.make_params(b, neighbor_skin=0.1)
+    assert _create_batch(bp, [a, b], [pa, pd])[0] == bp.abi.BP_ERR_INVALID_ARGUMENT
+    assert _create_batch(bp, [], [])[0] == bp.abi.BP_ERR_INVALID_ARGUMENT
+
+
+def test_batch_entry_points_reject_null_handles(bp):
+    lib = bp.abi.load()
+    first, count = C.c_int32(), C.c_int32()
+    assert lib.bp_batch_scene_range(None, 0, C.byref(first), C.byref(count)) == bp.abi.BP_ERR_INVALID_ARGUMENT
+    assert lib.bp_batch_step(None, C.c_float(0.01), 1, 1) == bp.abi.BP_ERR_INVALID_ARGUMENT
+
+
+def test_ensemble_members_follow_the_configuration(bp):
+    scenes = bp.scenes.config3_ensemble(seed=0, num_scenes=16)
+    n = np.array([s.num_particles for s in scenes])
+    assert n.min() >= 0.8 * 4096 and n.max() <= 1.1 * 262144
+    rho = np.array([s.rest_density for s in scenes]) / 1000.0
+    g = np.array([-s.gravity[1] for s in scenes])
+    assert (rho >= 0.8 - 1e-6).all() and (rho <= 1.2 + 1e-6).all()
+    assert (g >= 5.0).all() and (g <= 15.0).all()
+    for s in scenes:  # the grid covers the box without aliasing
+        assert s.grid_dim * s.cell_size >= s.planes[:, :3].max() - 1e-6

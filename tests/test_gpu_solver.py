@@ -181,18 +181,25 @@ def test_neighbor_masks_are_bit_identical_to_cell_walks(bp, gpu, skin):
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
-@pytest.mark.parametrize("options", [0, 1])
-def test_shared_memory_staging_is_bit_identical(bp, gpu, options):
-    """Staging each block's neighbourhood in shared memory changes nothing."""
+@pytest.mark.parametrize("skin", [0.0, 0.1])
+@pytest.mark.parametrize("walk", ["no_staging", "no_split", "neither"])
+def test_walk_variants_are_bit_identical(bp, gpu, walk, skin):
+    """Staging each block's neighbourhood in shared memory and testing
+    candidates in chunks before the pair terms change nothing: every walk
+    variant gives the default walk's bits."""
+    abi = bp.abi
+    options = {"no_staging": abi.BP_WALK_NO_STAGING, "no_split": abi.BP_WALK_NO_SPLIT,
+               "neither": abi.BP_WALK_NO_STAGING | abi.BP_WALK_NO_SPLIT}[walk]
     scene = small_mixed_scene(bp, seed=14)
     outs = []
-    for walk in (bp.abi.BP_WALK_NO_STAGING, options * 0):
-        g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=walk, neighbor_skin=0.1 * options))
+    for w in (0, options):
+        g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=w, neighbor_skin=skin))
         for _ in range(4):
             g.update(2, DT, 4)
-        outs.append(g.positions())
+        outs.append((g.positions(), g.velocities()))
         g.close()
-    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
 def test_graph_replay_equals_recapture(bp, gpu):
