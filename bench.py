@@ -216,6 +216,8 @@ def run_ours(args):
             p.walk_options |= bp.abi.BP_WALK_NO_STAGING
         if args.no_split:
             p.walk_options |= bp.abi.BP_WALK_NO_SPLIT
+        if args.no_lists:
+            p.walk_options |= bp.abi.BP_WALK_NO_LISTS
         return p
 
     if args.workload == "batch":
@@ -327,6 +329,7 @@ def run_ours(args):
                        "grid": ("one grid per scene (16^3..64^3 cells), cell = h = 0.2" if args.workload == "batch"
                                 else "64^3 cells, cell = h = 0.2"),
                        "neighbor_skin": float(params.neighbor_skin), "staging": not args.no_stage, "split_walks": not args.no_split,
+                       "post_lists": not args.no_lists,
                        "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "particle-substeps/s",
                     "h2d_bytes_per_step": int(2 * n * 12), "d2h_bytes_per_step": int(n * 12)},
@@ -441,6 +444,7 @@ def main():
     ap.add_argument("--skin", type=float, default=None, help="neighbour-mask skin (fraction of h); 0 disables")
     ap.add_argument("--no-stage", action="store_true", help="read neighbours from global memory only")
     ap.add_argument("--no-split", action="store_true", help="evaluate pair terms as candidates are tested")
+    ap.add_argument("--no-lists", action="store_true", help="post passes B and C walk their cells")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -82,6 +82,14 @@ struct SimConsts {
     float nl_hs2;            // (h + skin)^2
     float nl_half_skin2;     // (skin / 2)^2
     float nl_contact2;       // (2r + skin)^2
+    // Neighbour lists of the velocity post passes, written by pass A and read
+    // by passes B and C (positions do not change between them): for fluid
+    // particle i, nbr[k * n + i] for k < nbr_count[i] are the same-phase j != i
+    // with r^2 <= h^2, in walk order; nbr_count[i] < 0 when they did not fit
+    // in nbr_cap entries (the later passes then walk the cells).
+    int *nbr;
+    int *nbr_count;
+    int nbr_cap;
     // Batched ensembles (nullptr: one scene, described by the fields above).
     // scene_of[i] is the scene of particle i; it holds for sorted and
     // original indices alike, because every scene keeps its segment.

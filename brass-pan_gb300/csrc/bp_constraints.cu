@@ -67,11 +67,12 @@ __global__ void __launch_bounds__(kWalkThreads) k_particle_collision(SimConsts C
                                                                      const float4 *__restrict__ Xs,
                                                                      const float *__restrict__ w,
                                                                      const int *__restrict__ off,
+                                                                     const int *__restrict__ tile_solid,
                                                                      float4 *__restrict__ Pout)
 {
     __shared__ StageShared S;
     const int i0 = blockIdx.x * kWalkThreads;
-    const int g = stage_block(C, P, off, i0, S);
+    const int g = stage_block(C, P, off, i0, S, tile_solid);
     const int i = i0 + threadIdx.x;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
@@ -79,9 +80,11 @@ __global__ void __launch_bounds__(kWalkThreads) k_particle_collision(SimConsts C
     const int phi = phase_of(pi4);
     const float r = C.radius;
     const GridView v = grid_view(C, scene_index(C, i), off);
-    // A fluid particle only meets solids.  If it walks its CTA's staged runs
-    // and they hold no solid, the walk would find nothing.
-    bool none = phi < 0 && walks_staged(C, v, i, cell_of(xip, C), &S, g) && !S.has_solid;
+    // A fluid particle only meets solids.  If it walks its CTA's runs (it is
+    // in its stored cell) and they hold no solid, the walk would find nothing.
+    const int3 ci = cell_of(xip, C);
+    const bool in_cell = cell_addr(ci.x, ci.y, ci.z, v.D, v.mask) + v.base == __ldg(C.cell_keys + i);
+    bool none = phi < 0 && in_cell && (g == kNoSolidNear || (g >= 0 && !S.has_solid));
     // No contact partner within 2r + skin at mask build and the masks still
     // valid: no pair can be closer than 2r now, the walk would find nothing.
     none = none || (C.nl_mask && C.nl_flags && !(C.nl_flags[i] & kFlagContact) &&
@@ -138,14 +141,14 @@ __global__ void __launch_bounds__(kWalkThreads) k_particle_collision(SimConsts C
 }
 
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
-                               const float *w, const int *off, float4 *Pout, LaunchLog *L)
+                               const float *w, const int *off, const int *tile_solid, float4 *Pout, LaunchLog *L)
 {
     if (C.n <= 0) return;
     const int grid = (C.n + kWalkThreads - 1) / kWalkThreads;
     if (C.split)
-        k_particle_collision<true><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, Pout);
+        k_particle_collision<true><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, tile_solid, Pout);
     else
-        k_particle_collision<false><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, Pout);
+        k_particle_collision<false><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, tile_solid, Pout);
     L->done(__func__);
 }
 

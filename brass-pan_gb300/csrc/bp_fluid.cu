@@ -239,22 +239,38 @@ __global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const floa
     const float3 vi = f3(V[i]);
     float3 om = make_float3(0.f, 0.f, 0.f), nn = make_float3(0.f, 0.f, 0.f);
     const bool want_om = C.use_vort, want_n = C.use_akinci;
+    int cnt = 0;
+    // the walk takes the passes' common neighbours (r = 0 included, as pass C
+    // wants them) and records them for passes B and C
     walk_neighbors<Split>(
         i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, &S, g,
+        [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; },
         [&](int j, float4 pj4) {
-            const float d2 = len2(pi - f3(pj4));
-            return j != i && phase_of(pj4) == phi && d2 <= C.h2 && d2 > 0.f;
-        },
-        [&](int j, float4 pj4) {
+            if (C.nbr && cnt < C.nbr_cap) C.nbr[(size_t)cnt * C.n + i] = j;
+            ++cnt;
             const float3 diff = pi - f3(pj4);
             const float d2 = len2(diff);
+            if (!(d2 > 0.f)) return;
             const float3 g = spiky_grad_r(C, diff, d2, rsqrtf(d2));
             if (want_om) om += cross3(f3(V[j]) - vi, g);
             if (want_n) nn = fma3(__frcp_rn(__ldg(rho + j)), g, nn);
         });
+    if (C.nbr) C.nbr_count[i] = cnt <= C.nbr_cap ? cnt : -1;
     Om[i] = make_float4(om.x, om.y, om.z, len3(om));
     const float3 n = C.h * nn;
     Nm[i] = make_float4(n.x, n.y, n.z, rho[i]);
+}
+
+// Passes B and C: the number of recorded neighbours of particle i, or
+// kWalkCells when it must walk its cells (no lists, or they overflowed).
+// Solids and indices past the end need neither (0).
+constexpr int kWalkCells = -1;
+__device__ __forceinline__ int post_list_count(const SimConsts &C, const float4 *__restrict__ P, int i)
+{
+    if (i >= C.n || phase_of(P[i]) >= 0) return 0;
+    if (!C.nbr) return kWalkCells;
+    const int cnt = __ldg(C.nbr_count + i);
+    return cnt >= 0 ? cnt : kWalkCells;
 }
 
 // Pass B: vorticity confinement (fluidVorticity) then Akinci tension
@@ -270,8 +286,9 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
 {
     __shared__ StageShared S;
     const int i0 = blockIdx.x * kScanThreads;
-    const int g = stage_block(C, P, off, i0, S);
     const int i = i0 + threadIdx.x;
+    const int cnt = post_list_count(C, P, i);
+    const int g = __syncthreads_or(cnt == kWalkCells) ? stage_block(C, P, off, i0, S) : -1;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
     const float4 vi4 = V[i];
@@ -288,26 +305,32 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
     const float rhoi = ni4.w;
     float3 eta = make_float3(0.f, 0.f, 0.f), ft = make_float3(0.f, 0.f, 0.f);
     const bool want_v = C.use_vort, want_t = C.use_akinci;
-    walk_neighbors<Split>(
-        i, pi, 0, P, grid_view(C, sc, off), C, &S, g,
-        [&](int j, float4 pj4) {
-            const float d2 = len2(pi - f3(pj4));
-            return j != i && phase_of(pj4) == phi && d2 <= C.h2 && d2 > 0.f;
-        },
-        [&](int j, float4 pj4) {
-            const float3 diff = pi - f3(pj4);
-            const float d2 = len2(diff);
-            const float inv_r = rsqrtf(d2);
-            if (want_v) eta = fma3(Om[j].w, spiky_grad_r(C, diff, d2, inv_r), eta);
-            if (want_t) {
-                const float4 nj4 = Nm[j];
-                const float dist = __fmul_rn(d2, inv_r);
-                const float3 fco = __fmul_rn(__fmul_rn(-C.tension, akinci_spline(C, dist)), inv_r) * diff;
-                const float3 fcu = (-C.tension) * (ni - f3(nj4));
-                const float kij = __fmul_rn(two_rho0, __frcp_rn(__fadd_rn(rhoi, nj4.w)));
-                ft = fma3(kij, fco + fcu, ft);
-            }
-        });
+    auto body = [&](int j, float4 pj4) {
+        const float3 diff = pi - f3(pj4);
+        const float d2 = len2(diff);
+        if (!(d2 > 0.f)) return;
+        const float inv_r = rsqrtf(d2);
+        if (want_v) eta = fma3(Om[j].w, spiky_grad_r(C, diff, d2, inv_r), eta);
+        if (want_t) {
+            const float4 nj4 = Nm[j];
+            const float dist = __fmul_rn(d2, inv_r);
+            const float3 fco = __fmul_rn(__fmul_rn(-C.tension, akinci_spline(C, dist)), inv_r) * diff;
+            const float3 fcu = (-C.tension) * (ni - f3(nj4));
+            const float kij = __fmul_rn(two_rho0, __frcp_rn(__fadd_rn(rhoi, nj4.w)));
+            ft = fma3(kij, fco + fcu, ft);
+        }
+    };
+    if (cnt != kWalkCells) {
+        for (int k = 0; k < cnt; ++k) {
+            const int j = __ldg(C.nbr + (size_t)k * C.n + i);
+            body(j, P[j]);
+        }
+    } else {
+        walk_neighbors<Split>(
+            i, pi, 0, P, grid_view(C, sc, off), C, &S, g,
+            [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; },
+            body);
+    }
     float3 v = f3(vi4);
     if (want_v && len2(eta) > 1e-3f) {
         const float inv = 1.0f / sqrtf(dot3(eta, eta));
@@ -328,8 +351,9 @@ __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const floa
 {
     __shared__ StageShared S;
     const int i0 = blockIdx.x * kScanThreads;
-    const int g = stage_block(C, P, off, i0, S);
     const int i = i0 + threadIdx.x;
+    const int cnt = post_list_count(C, P, i);
+    const int g = __syncthreads_or(cnt == kWalkCells) ? stage_block(C, P, off, i0, S) : -1;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
     const float4 vi4 = V[i];
@@ -340,14 +364,22 @@ __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const floa
     }
     const float3 pi = f3(pi4), vi = f3(vi4);
     float3 vn = make_float3(0.f, 0.f, 0.f);
-    walk_neighbors<Split>(
-        i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, &S, g,
-        [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; },
-        [&](int j, float4 pj4) {
-            float wgt = poly6(C, len2(pi - f3(pj4)));
-            if (C.textbook) wgt = __fmul_rn(wgt, __fdiv_rn(__ldg(mass + j), __ldg(rho + j)));
-            vn = fma3(wgt, f3(V[j]) - vi, vn);
-        });
+    auto body = [&](int j, float4 pj4) {
+        float wgt = poly6(C, len2(pi - f3(pj4)));
+        if (C.textbook) wgt = __fmul_rn(wgt, __fdiv_rn(__ldg(mass + j), __ldg(rho + j)));
+        vn = fma3(wgt, f3(V[j]) - vi, vn);
+    };
+    if (cnt != kWalkCells) {
+        for (int k = 0; k < cnt; ++k) {
+            const int j = __ldg(C.nbr + (size_t)k * C.n + i);
+            body(j, P[j]);
+        }
+    } else {
+        walk_neighbors<Split>(
+            i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, &S, g,
+            [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; },
+            body);
+    }
     const float3 v = vi + C.xsph_c * vn;
     Vout[i] = make_float4(v.x, v.y, v.z, vi4.w);
 }

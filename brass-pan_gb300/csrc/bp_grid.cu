@@ -393,6 +393,7 @@ __global__ void __launch_bounds__(256) k_reorder(SimConsts C, ReorderArgs a)
     if (a.collide) plane_collide(C, s, x, p);
     a.Xs[i] = make_float4(x.x, x.y, x.z, X.w);
     a.Vs[i] = V;
+    if (a.tile_solid && phase_of(V) > 0) a.tile_solid[i >> 8] = 1;
     a.P[i] = make_float4(p.x, p.y, p.z, V.w);
     a.mass[i] = X.w;
     a.orig_s[i] = id;

@@ -81,6 +81,7 @@ struct ReorderArgs {
     float *inv_scaled;     // nullptr: not needed
     int stabilize;         // run planeStabilize twice
     int collide;           // also run iteration 0's plane collision
+    int *tile_solid;       // nullptr, or flags set for 256-particle tiles holding a solid (cleared before)
 };
 void launch_reorder(cudaStream_t st, const SimConsts &C, const ReorderArgs &a, LaunchLog *L);
 
@@ -114,8 +115,9 @@ void launch_neighbor_counts_f3(cudaStream_t st, int n, const float *pos3, float 
 void launch_planes(cudaStream_t st, const SimConsts &C, const float4 *Xs, float4 *P, LaunchLog *L);
 void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs, const float4 *Vs,
                    const int *orig_s, float4 *Xc, float4 *Vc, int *orig_c, LaunchLog *L);
+// tile_solid: nullptr, or one flag per 256 sorted particles (the tile holds a solid)
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
-                               const float *w, const int *off, float4 *Pout, LaunchLog *L);
+                               const float *w, const int *off, const int *tile_solid, float4 *Pout, LaunchLog *L);
 struct DistanceArgs {
     int num_edges;
     const int2 *pairs;       // original ids

@@ -42,6 +42,8 @@ bool is_pow2(int d) { return d > 0 && (d & (d - 1)) == 0; }
 // The message bp_last_error_string returns, for entry points in other files.
 void bp::set_last_error(const char *msg) { g_err = msg; }
 
+constexpr int kPostListCap = 64;  // recorded neighbours per particle for the post passes
+
 struct bp_solver {
     int n = 0;
     bp_params prm{};
@@ -67,6 +69,8 @@ struct bp_solver {
     unsigned short *nl_flags = nullptr;
     unsigned *nl_stats = nullptr;
     unsigned *err = nullptr;
+    int *tile_solid = nullptr;  // per 256 sorted particles: the tile holds a solid
+    int *nbr = nullptr, *nbr_count = nullptr;  // post-pass neighbour lists [kPostListCap][N], counts
     SortScratch sort{};
 
     bool has_solid = false;
@@ -400,6 +404,9 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         if (sc->group_ids) grp[i] = sc->group_ids[i];
     }
     s->has_solid = has_solid;
+    if ((st = s->alloc(&s->tile_solid, (N + 255) / 256)) || (st = s->alloc(&s->nbr, N * kPostListCap)) ||
+        (st = s->alloc(&s->nbr_count, N)))
+        return bail(st);
     if (n > 0) {
         BP_CUDA(cudaMemcpy(s->Xc, X.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
         BP_CUDA(cudaMemcpy(s->Vc, V.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
@@ -693,6 +700,8 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
     ra.inv_scaled = (distance || pcoll) ? s->w : nullptr;
     ra.stabilize = planes;
     ra.collide = fuse_first_planes;
+    ra.tile_solid = pcoll ? s->tile_solid : nullptr;
+    if (pcoll) cudaMemsetAsync(s->tile_solid, 0, ((s->n + 255) / 256) * sizeof(int), st);
     launch_reorder(st, C, ra, L);
 
     float4 *cur = s->Pa, *other = s->Pb;
@@ -717,7 +726,7 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
             masks_built = true;
         }
         if (pcoll) {
-            launch_particle_collision(st, C, cur, s->Xs, s->w, s->off, other, L);
+            launch_particle_collision(st, C, cur, s->Xs, s->w, s->off, s->tile_solid, other, L);
             std::swap(cur, other);
         }
         if (fluid) {
@@ -756,9 +765,16 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
 
     const bool post_ab = C.use_vort || C.use_akinci;
     if (post_ab) {
-        launch_post_a(st, C, cur, s->Vc, s->rho, s->off, s->Om, s->Nm, L);
-        launch_post_b(st, C, cur, s->Vc, s->Om, s->Nm, s->off, C.use_xsph ? s->Vs : s->Vc, L);
-        if (C.use_xsph) launch_post_c(st, C, cur, s->Vs, s->off, s->mass, s->rho, s->Vc, L);
+        // pass A records each fluid particle's neighbours for passes B and C
+        SimConsts Cl = C;
+        if (!(s->prm.walk_options & BP_WALK_NO_LISTS)) {
+            Cl.nbr = s->nbr;
+            Cl.nbr_count = s->nbr_count;
+            Cl.nbr_cap = kPostListCap;
+        }
+        launch_post_a(st, Cl, cur, s->Vc, s->rho, s->off, s->Om, s->Nm, L);
+        launch_post_b(st, Cl, cur, s->Vc, s->Om, s->Nm, s->off, C.use_xsph ? s->Vs : s->Vc, L);
+        if (C.use_xsph) launch_post_c(st, Cl, cur, s->Vs, s->off, s->mass, s->rho, s->Vc, L);
     } else if (C.use_xsph) {
         launch_post_c(st, C, cur, s->Vc, s->off, s->mass, s->rho, s->Vs, L);
         cudaMemcpyAsync(s->Vc, s->Vs, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);

@@ -44,14 +44,22 @@ struct StageShared {
     int ngroups;
     int ok;
     int scene;
-    int has_solid;  // a staged particle has a positive (solid) phase
+    int has_solid;  // a solid lies in the CTA's runs (tile_solid) or among the staged particles
 };
+
+constexpr int kNoSolidNear = -2;
 
 // Collective: every thread of the CTA must call it (before any early exit).
 // Returns the calling thread's column group (0 or 1), or -1 when the CTA does
 // not use shared memory or the thread has no particle.
+//
+// With `tile_solid` (one flag per 256 sorted particles: the tile holds a
+// solid), a CTA of fluid particles whose runs touch no solid tile skips the
+// staging and returns kNoSolidNear to every thread: none of its particles
+// that stayed in their stored cell can meet a solid.
 __device__ __forceinline__ int stage_block(const SimConsts &C, const float4 *__restrict__ P,
-                                           const int *__restrict__ off_all, int i0, StageShared &S)
+                                           const int *__restrict__ off_all, int i0, StageShared &S,
+                                           const int *__restrict__ tile_solid = nullptr)
 {
     if (!C.stage) return -1;  // uniform across the grid: no barrier skipped unevenly
     const int t = threadIdx.x;
@@ -100,6 +108,17 @@ __device__ __forceinline__ int stage_block(const SimConsts &C, const float4 *__r
         S.len[2 * t] = ea - sa;
         S.gstart[2 * t + 1] = sb;
         S.len[2 * t + 1] = eb - sb;
+        if (tile_solid) {
+            bool solid = false;
+            for (int q = sa >> 8; q <= (ea - 1) >> 8 && ea > sa && !solid; ++q) solid = __ldg(tile_solid + q) != 0;
+            for (int q = sb >> 8; q <= (eb - 1) >> 8 && eb > sb && !solid; ++q) solid = __ldg(tile_solid + q) != 0;
+            if (solid) S.has_solid = 1;
+        }
+    }
+    if (tile_solid) {
+        const bool own_solid = valid && phase_of(P[i]) > 0;
+        // uniform: S.has_solid was written before the barrier
+        if (!__syncthreads_or(own_solid) && !S.has_solid) return kNoSolidNear;
     }
     __syncthreads();
     if (t == 0) {

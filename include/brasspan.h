@@ -81,9 +81,12 @@ typedef enum bp_mode {
  * BP_WALK_NO_STAGING reads every neighbour from global memory instead of
  * staging each block's neighbourhood in shared memory; BP_WALK_NO_SPLIT
  * evaluates each pair term as its candidate is tested instead of testing a
- * chunk of candidates first and evaluating the pair terms of the hits. */
+ * chunk of candidates first and evaluating the pair terms of the hits;
+ * BP_WALK_NO_LISTS makes the second and third velocity post passes walk
+ * their cells instead of reading the neighbour lists the first one records. */
 #define BP_WALK_NO_STAGING 0x1
 #define BP_WALK_NO_SPLIT 0x2
+#define BP_WALK_NO_LISTS 0x4
 
 /* Every literal of the reference's step as a field.  bp_params_init fills the
  * reference's values; comments give the reference location of each. */

@@ -182,14 +182,16 @@ def test_neighbor_masks_are_bit_identical_to_cell_walks(bp, gpu, skin):
 
 
 @pytest.mark.parametrize("skin", [0.0, 0.1])
-@pytest.mark.parametrize("walk", ["no_staging", "no_split", "neither"])
+@pytest.mark.parametrize("walk", ["no_staging", "no_split", "no_lists", "none"])
 def test_walk_variants_are_bit_identical(bp, gpu, walk, skin):
-    """Staging each block's neighbourhood in shared memory and testing
-    candidates in chunks before the pair terms change nothing: every walk
-    variant gives the default walk's bits."""
+    """Staging each block's neighbourhood in shared memory, testing
+    candidates in chunks before the pair terms and the post passes'
+    neighbour lists change nothing: every walk variant gives the default
+    walk's bits."""
     abi = bp.abi
     options = {"no_staging": abi.BP_WALK_NO_STAGING, "no_split": abi.BP_WALK_NO_SPLIT,
-               "neither": abi.BP_WALK_NO_STAGING | abi.BP_WALK_NO_SPLIT}[walk]
+               "no_lists": abi.BP_WALK_NO_LISTS,
+               "none": abi.BP_WALK_NO_STAGING | abi.BP_WALK_NO_SPLIT | abi.BP_WALK_NO_LISTS}[walk]
     scene = small_mixed_scene(bp, seed=14)
     outs = []
     for w in (0, options):
