@@ -6,10 +6,12 @@ particles, a 256x256 cloth under wind, 64 rigid 8^3 cubes; 1,146,880
 particles), reference-mode parameters.  Prints one JSON line; unless
 --no-batch, its "batched" object times the batched ensemble (256 PBF dam
 breaks of 4096..262144 particles in one solver) against looping one solver
-per scene over the same scenes.
+per scene over the same scenes; unless --no-adjoint, its "adjoint" object
+times forward + backward() of differentiable rollouts against the forward
+alone (wall clock, host arrays in and out).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload mixed|fluid|small|batch] [--no-batch]
+                  [--workload mixed|fluid|small|batch] [--no-batch] [--no-adjoint]
 
 Multi-GPU (torchrun, one rank per GPU): the scene does not shard, so every
 rank advances its own replica ("replicas only"); value = all ranks' particle
@@ -87,6 +89,60 @@ def timed_steps(torch, stream, flush, steps, fn):
         ends[k].record(stream)
     torch.cuda.synchronize()
     return sum(a.elapsed_time(b) for a, b in zip(starts, ends))
+
+
+def run_adjoint(bp, torch, stream, frames=120, every=10):
+    """Differentiable rollouts: a 128x128 cloth flag pinned along one edge
+    under wind (4, 0, 0) m/s (loss: squared distance of the final positions to
+    a seeded target) and a 64x32x32 = 65,536-particle PBF block (loss: final
+    centre of mass), each for `frames` updates of 2 substeps x 4 iterations,
+    checkpoints every `every` substeps.  Times one forward rollout and one
+    forward rollout recorded on a tape plus backward()."""
+    abi = bp.abi
+    out = {}
+    cloth = bp.scenes.flag_scene(n=128, seed=4)
+    cloth_stages = abi.BP_STAGE_PLANES | abi.BP_STAGE_WIND | abi.BP_STAGE_DISTANCE | abi.BP_STAGE_IMMOVABLE
+    # no mass scaling: exp(2 y) over a 13 m tall flag would span 11 orders of magnitude
+    cloth_params = bp.make_params(cloth, mode=abi.BP_MODE_TEXTBOOK, stage_mask=cloth_stages,
+                                  wind_velocity=(4.0, 0.0, 0.0), wind_drag=1.0, wind_lift=0.3, mass_scaling_k=0.0)
+    fluid = bp.scenes.pbf_scene(64, 32, 32, spacing=0.1, seed=4, box=(9.6, 8.0, 4.8), grid_dim=64)
+    fluid_params = bp.make_params(fluid, stage_mask=abi.BP_STAGE_FLUID | abi.BP_STAGE_PLANES | abi.BP_STAGE_XSPH)
+    rng = np.random.default_rng(4)
+    for name, scene, params in (("cloth_flag_128x128", cloth, cloth_params), ("pbf_block_65536", fluid, fluid_params)):
+        n = scene.num_particles
+        if name.startswith("cloth"):
+            target = scene.positions + rng.normal(0.0, 0.05, (n, 3)).astype(np.float32)
+        s = bp.ParticleSolver(scene, params, stream=stream.cuda_stream)
+        x0, v0 = s.positions(), s.velocities()
+        with torch.cuda.stream(stream):
+            s.update(SUBSTEPS, DT, ITERATIONS)  # graph capture outside the timed region
+            s.set_state(x0, v0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(frames):
+                s.update(SUBSTEPS, DT, ITERATIONS)
+            x = s.positions()
+            fwd = time.perf_counter() - t0
+            s.set_state(x0, v0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.tape_begin(every)
+            for _ in range(frames):
+                s.update(SUBSTEPS, DT, ITERATIONS)
+            x = s.positions()
+            if name.startswith("cloth"):
+                gx = (2.0 / n) * (x - target)
+            else:
+                gx = np.zeros((n, 3), np.float32)
+                gx[:] = 1.0 / n
+            g = s.backward(gx)
+            both = time.perf_counter() - t0
+            s.tape_end()
+        s.close()
+        out[name] = {"particles": n, "substeps": frames * SUBSTEPS, "checkpoint_every": every,
+                     "forward_ms": fwd * 1e3, "forward_adjoint_ms": both * 1e3, "ratio": both / fwd,
+                     "grad_finite": bool(np.isfinite(g["velocities"]).all())}
+    return out
 
 
 def run_batch(bp, torch, stream, flush, steps, warmup, seed=0):
@@ -306,6 +362,9 @@ def run_ours(args):
     if args.workload == "batch" or (args.workload == "mixed" and not args.no_batch):
         # the ensemble against a loop of one solver per scene (bounded: 3 timed steps)
         batched = run_batch(bp, torch, stream, flush, steps=min(args.steps, 3), warmup=3, seed=rank)
+    adjoint = None
+    if args.workload == "mixed" and not args.no_adjoint:
+        adjoint = run_adjoint(bp, torch, stream)
 
     result = None
     if rank == 0:
@@ -347,6 +406,8 @@ def run_ours(args):
         }
         if batched is not None:
             result["batched"] = batched
+        if adjoint is not None:
+            result["adjoint"] = adjoint
         print(json.dumps(result), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -441,6 +502,7 @@ def main():
     ap.add_argument("--workload", choices=["mixed", "fluid", "small"], default="mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint measurement")
     ap.add_argument("--skin", type=float, default=None, help="neighbour-mask skin (fraction of h); 0 disables")
     ap.add_argument("--no-stage", action="store_true", help="read neighbours from global memory only")
     ap.add_argument("--no-split", action="store_true", help="evaluate pair terms as candidates are tested")

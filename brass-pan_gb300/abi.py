@@ -113,6 +113,12 @@ class BpStageTime(C.Structure):
     _fields_ = [("name", C.c_char * 48), ("launches", C.c_int32), ("total_ms", C.c_float)]
 
 
+class BpGradients(C.Structure):
+    _fields_ = [("positions", C.POINTER(C.c_float)), ("velocities", C.POINTER(C.c_float)),
+                ("wind_velocity", C.POINTER(C.c_float)), ("distance_stiffness", C.POINTER(C.c_float)),
+                ("distance_rest_length", C.POINTER(C.c_float))]
+
+
 def _fptr(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
 
@@ -172,7 +178,8 @@ EXPORTS = [
     "bp_solver_get_particle_position", "bp_solver_copy_positions", "bp_solver_copy_velocities",
     "bp_solver_set_state", "bp_solver_field", "bp_solver_copy_field", "bp_solver_pack_particle_infos",
     "bp_solver_device_errors", "bp_solver_last_launch_count", "bp_solver_profile", "bp_solver_walk_stats", "bp_grid_workspace_size", "bp_grid_build",
-    "bp_grid_reset", "bp_grid_build_static", "bp_batch_create", "bp_batch_step", "bp_batch_scene_range", "bp_grid_neighbor_counts", "bp_last_error_string", "bp_abi_version",
+    "bp_grid_reset", "bp_grid_build_static", "bp_batch_create", "bp_batch_step", "bp_batch_scene_range",
+    "bp_solver_tape_begin", "bp_solver_backward", "bp_solver_tape_end", "bp_grid_neighbor_counts", "bp_last_error_string", "bp_abi_version",
 ]
 
 
@@ -212,6 +219,9 @@ def load(path: Path | None = None):
         "bp_grid_reset": (i32, [vp, i32, vp, vp, vp]),
         "bp_grid_build_static": (i32, [vp, i32, vp, f32, i32, vp, vp, vp, vp, vp]),
         "bp_batch_create": (i32, [i32, vp, vp, vp, vp]),
+        "bp_solver_tape_begin": (i32, [vp, i32]),
+        "bp_solver_backward": (i32, [vp, vp, vp, vp]),
+        "bp_solver_tape_end": (i32, [vp]),
         "bp_batch_step": (i32, [vp, f32, i32, i32]),
         "bp_batch_scene_range": (i32, [vp, i32, vp, vp]),
         "bp_grid_neighbor_counts": (i32, [vp, i32, vp, f32, i32, f32, vp, vp, vp]),

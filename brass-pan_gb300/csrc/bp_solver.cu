@@ -13,7 +13,7 @@
 #include <string>
 #include <vector>
 
-#include "bp_internal.h"
+#include "bp_solver_state.h"
 
 using namespace bp;
 
@@ -41,89 +41,6 @@ bool is_pow2(int d) { return d > 0 && (d & (d - 1)) == 0; }
 
 // The message bp_last_error_string returns, for entry points in other files.
 void bp::set_last_error(const char *msg) { g_err = msg; }
-
-constexpr int kPostListCap = 64;  // recorded neighbours per particle for the post passes
-
-struct bp_solver {
-    int n = 0;
-    bp_params prm{};
-    int nplanes = 0;
-    float planes[kMaxPlanes][6];
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int device = 0;
-
-    std::vector<void *> allocs;
-
-    float4 *Xc = nullptr, *Vc = nullptr, *Xs = nullptr, *Vs = nullptr, *Pa = nullptr, *Pb = nullptr;
-    float4 *Om = nullptr, *Nm = nullptr;
-    float4 *Pcur = nullptr;  // predicted positions after the last substep
-    int *orig_c = nullptr, *orig_s = nullptr, *to_new = nullptr, *group = nullptr;
-    int *keys = nullptr, *sorted_keys = nullptr, *order = nullptr, *off = nullptr;
-    float *mass = nullptr, *lam = nullptr, *rho = nullptr, *w = nullptr;
-    float *staging = nullptr;  // 2 x N x 3 floats for host copies
-    unsigned long long *nl_mask = nullptr;  // neighbour masks [18][N]
-    int *nl_cell = nullptr;
-    float4 *nl_pos = nullptr;
-    unsigned long long *nl_outlier = nullptr;  // outlier cell bits [D*D][ceil(D/64)]
-    unsigned short *nl_flags = nullptr;
-    unsigned *nl_stats = nullptr;
-    unsigned *err = nullptr;
-    int *tile_solid = nullptr;  // per 256 sorted particles: the tile holds a solid
-    int *nbr = nullptr, *nbr_count = nullptr;  // post-pass neighbour lists [kPostListCap][N], counts
-    SortScratch sort{};
-
-    bool has_solid = false;
-    size_t ncells = 0;   // cells of the key space (D^3 for one scene)
-    int sort_dim = 0;    // a grid dimension whose key width covers every key (sort passes)
-    // batched ensembles (num_scenes == 0: one scene)
-    int num_scenes = 0;
-    std::vector<int> scene_first;  // num_scenes + 1 particle offsets
-    SceneConsts *scn = nullptr;
-    int *scene_of = nullptr;
-    DistanceArgs dist{};
-    WindArgs wind{};
-    RigidArgs rigid{};
-    int nimm = 0;
-    int *imm = nullptr;
-
-    // graph cache
-    cudaGraphExec_t exec = nullptr;
-    int g_sub = -1, g_iter = -1;
-    float g_dt = 0.f;
-    uint64_t g_params_version = ~0ull;
-    uint64_t params_version = 0;
-    int64_t graph_launches = 0;
-    int64_t last_launches = 0;
-
-    ~bp_solver()
-    {
-        if (exec) cudaGraphExecDestroy(exec);
-        for (void *p : allocs) cudaFree(p);
-        if (own_stream && stream) cudaStreamDestroy(stream);
-    }
-
-    template <class T>
-    bp_status alloc(T **ptr, size_t count)
-    {
-        void *p = nullptr;
-        const size_t bytes = count * sizeof(T) > 0 ? count * sizeof(T) : 16;
-        cudaError_t e = cudaMalloc(&p, bytes);
-        if (e != cudaSuccess)
-            return fail(BP_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-        allocs.push_back(p);
-        *ptr = (T *)p;
-        return BP_OK;
-    }
-    template <class T>
-    bp_status upload(T **ptr, const void *host, size_t count)
-    {
-        bp_status st = alloc(ptr, count);
-        if (st != BP_OK) return st;
-        if (count) BP_CUDA(cudaMemcpy(*ptr, host, count * sizeof(T), cudaMemcpyHostToDevice));
-        return BP_OK;
-    }
-};
 
 extern "C" void bp_params_init(bp_params *p, float r)
 {
@@ -175,7 +92,7 @@ static bp_status check_params(const bp_params *p)
 }
 
 // Substep constants: SetKernelRadius (K/fluid.cuh:11-27) evaluated on the host.
-static SimConsts make_consts(const bp_solver *s, float sdt)
+SimConsts bp::make_consts(const bp_solver *s, float sdt)
 {
     const bp_params &p = s->prm;
     SimConsts C;
@@ -665,8 +582,8 @@ extern "C" bp_status bp_solver_set_params(bp_solver *s, const bp_params *prm)
 }
 
 // Enqueues one substep; returns the number of kernels launched.
-static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int picked, float3 ppos,
-                            LaunchLog *L)
+void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int picked, float3 ppos, LaunchLog *L,
+                         SubstepTape *tape)
 {
     const cudaStream_t st = s->stream;
     const int mask = s->prm.stage_mask;
@@ -685,7 +602,7 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
     radix_sort_pairs(st, s->n, s->sort_dim, s->keys, nullptr, s->sorted_keys, s->order, s->sort, true, L);
     launch_cell_offsets(st, s->n, (int)s->ncells, s->sorted_keys, s->off, L);
 
-    const bool fuse_first_planes = planes && !wind && !picking && iterations > 0;
+    const bool fuse_first_planes = planes && !wind && !picking && iterations > 0 && !tape;
     ReorderArgs ra;
     ra.order = s->order;
     ra.Xc = s->Xc;
@@ -703,9 +620,13 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
     ra.tile_solid = pcoll ? s->tile_solid : nullptr;
     if (pcoll) cudaMemsetAsync(s->tile_solid, 0, ((s->n + 255) / 256) * sizeof(int), st);
     launch_reorder(st, C, ra, L);
+    if (tape) tape->vs_slot = tape->snap4(s->Vs);
 
     float4 *cur = s->Pa, *other = s->Pb;
-    if (wind) launch_wind(st, C, s->wind, cur, s->Vs, s->mass, s->to_new, L);
+    if (wind) {
+        if (tape) tape->push(TS_WIND, cur);
+        launch_wind(st, C, s->wind, cur, s->Vs, s->mass, s->to_new, L);
+    }
     // masks are built at the positions the first scan sees: after the wind
     // and iteration 0's plane collision, which move particles the most
     const bool scans = pcoll || fluid || C.use_vort || C.use_akinci || C.use_xsph;
@@ -719,18 +640,27 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
     bool committed = false;
     for (int it = 0; it < iterations; ++it) {
         if (picking) launch_pick(st, picked, s->to_new, cur, ppos, 1, nullptr, make_float3(0.f, 0.f, 0.f), L);
-        if (planes && !planes_done) launch_planes(st, C, s->Xs, cur, L);
+        if (planes && !planes_done) {
+            if (tape) tape->push(TS_PLANES, cur);
+            launch_planes(st, C, s->Xs, cur, L);
+        }
         planes_done = false;
         if (!masks_built) {
             launch_build_masks(st, C, cur, s->off, L);
             masks_built = true;
         }
         if (pcoll) {
+            if (tape) tape->push(TS_PCOLL, cur);
             launch_particle_collision(st, C, cur, s->Xs, s->w, s->off, s->tile_solid, other, L);
             std::swap(cur, other);
         }
         if (fluid) {
             launch_lambda(st, C, cur, s->mass, s->off, s->lam, s->rho, L);
+            if (tape) {
+                const int aux = tape->snap1(s->lam);
+                tape->snap1(s->rho);
+                tape->push(TS_FLUID, cur, aux);
+            }
             DeltaArgs da;
             da.P = cur;
             da.mass = s->mass;
@@ -744,7 +674,7 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
             da.Vs = s->Vs;
             da.orig_s = s->orig_s;
             da.orig_c = s->orig_c;
-            if (!tail) {
+            if (!tail && !tape) {
                 if (it == iterations - 1) {
                     da.epilogue = 2;
                     committed = true;
@@ -756,14 +686,28 @@ static void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, in
             launch_deltap(st, C, da, L);
             std::swap(cur, other);
         }
-        if (distance) launch_distance(st, C, s->dist, cur, s->w, s->to_new, s->err, L);
-        if (rigid) launch_shape_matching(st, C, s->rigid, cur, s->to_new, L);
-        if (immov) launch_immovable(st, C, s->nimm, s->imm, s->to_new, s->Xs, cur, L);
+        if (distance) {
+            if (tape) tape->push(TS_DISTANCE, cur);
+            launch_distance(st, C, s->dist, cur, s->w, s->to_new, s->err, L);
+        }
+        if (rigid) {
+            if (tape) tape->push(TS_SHAPE, cur);
+            launch_shape_matching(st, C, s->rigid, cur, s->to_new, L);
+        }
+        if (immov) {
+            if (tape) tape->push(TS_IMMOVABLE, cur);
+            launch_immovable(st, C, s->nimm, s->imm, s->to_new, s->Xs, cur, L);
+        }
     }
-    if (!committed) launch_commit(st, C, cur, s->Xs, s->Vs, s->orig_s, s->Xc, s->Vc, s->orig_c, L);
+    if (!committed) {
+        if (tape) tape->push(TS_COMMIT, cur);
+        launch_commit(st, C, cur, s->Xs, s->Vs, s->orig_s, s->Xc, s->Vc, s->orig_c, L);
+    }
     s->Pcur = cur;
 
     const bool post_ab = C.use_vort || C.use_akinci;
+    if (tape && post_ab) tape->push(TS_POST_AB, s->Vc);
+    if (tape && !post_ab && C.use_xsph) tape->push(TS_XSPH, s->Vc);
     if (post_ab) {
         // pass A records each fluid particle's neighbours for passes B and C
         SimConsts Cl = C;
@@ -805,6 +749,10 @@ extern "C" bp_status bp_solver_update(bp_solver *s, int32_t nsub, float dt, int3
     if (picked >= 0 && !ppos) return fail(BP_ERR_INVALID_ARGUMENT, "picked_position is NULL");
     const float3 pp = ppos ? make_float3(ppos[0], ppos[1], ppos[2]) : make_float3(0.f, 0.f, 0.f);
     const float3 pv = pvel ? make_float3(pvel[0], pvel[1], pvel[2]) : make_float3(0.f, 0.f, 0.f);
+    if (s->tape) {
+        const bp_status st = tape_record_update(s, nsub, dt, iterations, picked >= 0);
+        if (st != BP_OK) return st;
+    }
     LaunchLog L;
     L.stream = s->stream;
     if (picked >= 0) {
@@ -843,6 +791,7 @@ extern "C" bp_status bp_solver_profile(bp_solver *s, int32_t nsub, float dt, int
                                        int32_t capacity, bp_stage_time *out, int32_t *count)
 {
     if (!s || !count || capacity < 0 || (capacity > 0 && !out)) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (s->tape) return fail(BP_ERR_INVALID_ARGUMENT, "not available while a tape records");
     if (nsub <= 0 || !(dt > 0.f) || iterations < 0) return fail(BP_ERR_INVALID_ARGUMENT, "bad step arguments");
     *count = 0;
     if (s->n <= 0) return BP_OK;
@@ -890,6 +839,7 @@ extern "C" bp_status bp_solver_walk_stats(bp_solver *s, int32_t nsub, float dt, 
                                           uint64_t out_walks[4])
 {
     if (!s || !out_walks) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (s->tape) return fail(BP_ERR_INVALID_ARGUMENT, "not available while a tape records");
     if (nsub <= 0 || !(dt > 0.f) || iterations < 0) return fail(BP_ERR_INVALID_ARGUMENT, "bad step arguments");
     for (int k = 0; k < 4; ++k) out_walks[k] = 0;
     if (s->n <= 0) return BP_OK;
@@ -973,6 +923,7 @@ extern "C" bp_status bp_solver_set_state(bp_solver *s, const float *hx, const fl
 {
     if (!s) return fail(BP_ERR_INVALID_ARGUMENT, "solver is NULL");
     if (order != BP_ORDER_SORTED && order != BP_ORDER_ORIGINAL) return fail(BP_ERR_INVALID_ARGUMENT, "bad order");
+    if (s->tape && !s->tape_empty()) return fail(BP_ERR_INVALID_ARGUMENT, "the state cannot change while a tape records");
     const int n = s->n;
     if (n == 0) return BP_OK;
     const int *map = order == BP_ORDER_ORIGINAL ? s->to_new : nullptr;

@@ -1,0 +1,174 @@
+// bp_solver_state.h -- the solver handle's state, shared by the step
+// orchestration (bp_solver.cu) and the adjoint driver (bp_backward.cu).
+#pragma once
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bp_internal.h"
+
+namespace bp {
+struct SubstepTape;
+struct Tape;
+
+// Sets the message bp_last_error_string returns and passes the status on.
+inline bp_status fail_with(bp_status st, const std::string &msg)
+{
+    set_last_error(msg.c_str());
+    return st;
+}
+}  // namespace bp
+
+#define BP_CUDA_OR_FAIL(call)                                                                        \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return bp::fail_with(e_ == cudaErrorMemoryAllocation ? BP_ERR_OUT_OF_MEMORY : BP_ERR_CUDA, \
+                                 std::string(#call) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+using namespace bp;
+
+namespace bp {
+void destroy_tape(Tape *t);  // frees a recording (bp_backward.cu)
+
+// Stages of a substep as recorded for the adjoint.
+enum TapeStage : int {
+    TS_WIND,
+    TS_PLANES,
+    TS_PCOLL,
+    TS_FLUID,
+    TS_DISTANCE,
+    TS_SHAPE,
+    TS_IMMOVABLE,
+    TS_COMMIT,
+    TS_XSPH,
+    TS_POST_AB
+};
+struct TapeRec {
+    int stage;
+    int slot;  // snapshot of the stage's input: positions, or velocities for TS_XSPH
+    int aux;   // TS_FLUID: snapshot of lambda (aux) and density (aux + 1)
+};
+
+// The intermediates of one substep re-run for its adjoint: each stage's
+// input, copied into a pool of device buffers that persists across substeps.
+struct SubstepTape {
+    bp_solver *s = nullptr;
+    std::vector<float4 *> pool4;
+    std::vector<float *> pool1;
+    int used4 = 0, used1 = 0;
+    std::vector<TapeRec> recs;
+    int vs_slot = -1;  // velocities after the reorder
+    bool ok = true;    // false after a failed allocation
+    void reset()
+    {
+        used4 = used1 = 0;
+        recs.clear();
+        vs_slot = -1;
+    }
+    int snap4(const float4 *src);
+    int snap1(const float *src);
+    void push(int stage, const float4 *src, int aux = -1) { recs.push_back(TapeRec{stage, snap4(src), aux}); }
+};
+}  // namespace bp
+
+constexpr int kPostListCap = 64;  // recorded neighbours per particle for the post passes
+
+struct bp_solver {
+    int n = 0;
+    bp_params prm{};
+    int nplanes = 0;
+    float planes[kMaxPlanes][6];
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0;
+
+    std::vector<void *> allocs;
+
+    float4 *Xc = nullptr, *Vc = nullptr, *Xs = nullptr, *Vs = nullptr, *Pa = nullptr, *Pb = nullptr;
+    float4 *Om = nullptr, *Nm = nullptr;
+    float4 *Pcur = nullptr;  // predicted positions after the last substep
+    int *orig_c = nullptr, *orig_s = nullptr, *to_new = nullptr, *group = nullptr;
+    int *keys = nullptr, *sorted_keys = nullptr, *order = nullptr, *off = nullptr;
+    float *mass = nullptr, *lam = nullptr, *rho = nullptr, *w = nullptr;
+    float *staging = nullptr;  // 2 x N x 3 floats for host copies
+    unsigned long long *nl_mask = nullptr;  // neighbour masks [18][N]
+    int *nl_cell = nullptr;
+    float4 *nl_pos = nullptr;
+    unsigned long long *nl_outlier = nullptr;  // outlier cell bits [D*D][ceil(D/64)]
+    unsigned short *nl_flags = nullptr;
+    unsigned *nl_stats = nullptr;
+    unsigned *err = nullptr;
+    int *tile_solid = nullptr;  // per 256 sorted particles: the tile holds a solid
+    int *nbr = nullptr, *nbr_count = nullptr;  // post-pass neighbour lists [kPostListCap][N], counts
+    SortScratch sort{};
+
+    bool has_solid = false;
+    size_t ncells = 0;   // cells of the key space (D^3 for one scene)
+    int sort_dim = 0;    // a grid dimension whose key width covers every key (sort passes)
+    // batched ensembles (num_scenes == 0: one scene)
+    int num_scenes = 0;
+    std::vector<int> scene_first;  // num_scenes + 1 particle offsets
+    SceneConsts *scn = nullptr;
+    int *scene_of = nullptr;
+    DistanceArgs dist{};
+    WindArgs wind{};
+    RigidArgs rigid{};
+    int nimm = 0;
+    int *imm = nullptr;
+
+    // graph cache
+    cudaGraphExec_t exec = nullptr;
+    int g_sub = -1, g_iter = -1;
+    float g_dt = 0.f;
+    uint64_t g_params_version = ~0ull;
+    uint64_t params_version = 0;
+    int64_t graph_launches = 0;
+    int64_t last_launches = 0;
+
+    bp::Tape *tape = nullptr;  // recording for bp_solver_backward (nullptr: not recording)
+    bool tape_empty() const;   // no update recorded yet
+
+    ~bp_solver()
+    {
+        if (tape) bp::destroy_tape(tape);
+        if (exec) cudaGraphExecDestroy(exec);
+        for (void *p : allocs) cudaFree(p);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+
+    template <class T>
+    bp_status alloc(T **ptr, size_t count)
+    {
+        void *p = nullptr;
+        const size_t bytes = count * sizeof(T) > 0 ? count * sizeof(T) : 16;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess)
+            return bp::fail_with(BP_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs.push_back(p);
+        *ptr = (T *)p;
+        return BP_OK;
+    }
+    template <class T>
+    bp_status upload(T **ptr, const void *host, size_t count)
+    {
+        bp_status st = alloc(ptr, count);
+        if (st != BP_OK) return st;
+        if (count) BP_CUDA_OR_FAIL(cudaMemcpy(*ptr, host, count * sizeof(T), cudaMemcpyHostToDevice));
+        return BP_OK;
+    }
+};
+
+
+namespace bp {
+// Substep constants of solver s for substep length sdt.
+SimConsts make_consts(const bp_solver *s, float sdt);
+// Records an update about to be enqueued while s->tape is open.
+bp_status tape_record_update(bp_solver *s, int nsub, float dt, int iterations, bool picked);
+// Enqueues one substep on s->stream.  With a tape, the fused epilogues are
+// replaced by their separate kernels and every stage's input is recorded.
+void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int picked, float3 ppos, LaunchLog *L,
+                     SubstepTape *tape = nullptr);
+}  // namespace bp

@@ -51,6 +51,10 @@ class Scene:
     def num_particles(self) -> int:
         return int(len(self.positions))
 
+    @property
+    def num_distance_constraints(self) -> int:
+        return int(len(self.distance_pairs))
+
     # -- internal append -------------------------------------------------------
     def _append(self, pos, mass, phases, rest=None):
         pos = np.asarray(pos, np.float32).reshape(-1, 3)
@@ -295,3 +299,29 @@ def config3_ensemble(seed=0, num_scenes=256, lo=4096, hi=262144):
         out.append(ensemble_member(n, seed=seed * 100003 + k, rest_scale=rng.uniform(0.8, 1.2),
                                    gravity=rng.uniform(5.0, 15.0)))
     return out
+
+
+def flag_scene(n=128, spacing=0.1, angle_deg=20.0, seed=0, mass=1.0, stretch=0.25, shear=0.1, bend=0.05,
+               floor=-30.0):
+    """A cloth flag of n x n particles pinned along its vertical edge (the
+    pole), its plane turned by angle_deg about the vertical so that a wind
+    along +x meets it, over a distant floor.  Returns the scene; the pole's
+    particles are immovable.  The distance constraints are projected Jacobi
+    style (all corrections from the same positions, summed), so the summed
+    stiffness around a particle must stay small: a pinned flag with the
+    stiffnesses 1.0 / 0.5 / 0.1 diverges within a few frames."""
+    d = float(np.float32(spacing))
+    s = Scene(name=f"flag_{n}x{n}")
+    s.particle_radius = d / 2
+    s.kernel_radius = 2 * d
+    s.cell_size = 2 * d
+    s.grid_dim = 64
+    s.rest_density = 1000.0
+    a = np.deg2rad(angle_deg)
+    s.add_plane((0.0, floor, 0.0), (0.0, 1.0, 0.0))
+    ox = (d * float(np.cos(a)), 0.0, d * float(np.sin(a)))
+    s.add_cloth((0.0, n * d + 1.0, 0.0), ox, (0.0, -d, 0.0), n, n, mass, stretch=stretch, shear=shear, bend=bend)
+    s.make_immovable(np.arange(n) * n)  # y = 0 of every row: the pole
+    rng = np.random.default_rng(seed)
+    s.velocities = rng.uniform(-0.05, 0.05, (s.num_particles, 3)).astype(np.float32)
+    return s

@@ -151,6 +151,35 @@ class ParticleSolver:
         return {"masked": int(out[0]), "cells_no_mask": int(out[1]), "cells_moved_cell": int(out[2]),
                 "cells_displaced": int(out[3])}
 
+    # -- differentiable rollouts ------------------------------------------------------
+    def tape_begin(self, checkpoint_every: int = 10):
+        """Record the following updates for backward()."""
+        abi.check(self.lib, self.lib.bp_solver_tape_begin(self.handle, checkpoint_every))
+
+    def tape_end(self):
+        abi.check(self.lib, self.lib.bp_solver_tape_end(self.handle))
+
+    def backward(self, grad_positions=None, grad_velocities=None) -> dict[str, np.ndarray]:
+        """Gradients of a loss of the final state (dL/dx, dL/dv: [N][3], original
+        order) with respect to the state at tape_begin and the parameters."""
+        fp = C.POINTER(C.c_float)
+
+        def arr(a):
+            return None if a is None else np.ascontiguousarray(a, np.float32).reshape(self.n, 3)
+
+        gx, gv = arr(grad_positions), arr(grad_velocities)
+        m = int(self.scene.num_distance_constraints) if self.scene is not None else 0
+        out = {"positions": np.zeros((self.n, 3), np.float32), "velocities": np.zeros((self.n, 3), np.float32),
+               "wind_velocity": np.zeros(3, np.float32), "distance_stiffness": np.zeros(m, np.float32),
+               "distance_rest_length": np.zeros(m, np.float32)}
+        g = abi.BpGradients()
+        for k, v in out.items():
+            setattr(g, k, v.ctypes.data_as(fp) if v.size else None)
+        abi.check(self.lib, self.lib.bp_solver_backward(
+            self.handle, None if gx is None else gx.ctypes.data_as(fp),
+            None if gv is None else gv.ctypes.data_as(fp), C.byref(g)))
+        return out
+
     def pack_particle_infos(self, device_ptr: int):
         abi.check(self.lib, self.lib.bp_solver_pack_particle_infos(self.handle, C.c_void_p(device_ptr)))
 

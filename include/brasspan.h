@@ -246,6 +246,35 @@ bp_status bp_solver_profile(bp_solver *s, int32_t num_substeps, float dt, int32_
 bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
                                uint64_t out_walks[4]);
 
+/* ---- Differentiable rollouts ------------------------------------------------
+ * No counterpart in the reference.  bp_solver_tape_begin starts recording the
+ * following bp_solver_update calls (no picking); the state is checkpointed at
+ * the start of an update once `checkpoint_every` substeps have passed since
+ * the last checkpoint.  bp_solver_backward then returns the gradient of a
+ * scalar loss L(x_T, v_T) of the final state with respect to the state when
+ * recording began and to parameters, given dL/dx_T and dL/dv_T ([N][3] host
+ * arrays in original order; either may be NULL for zero).  It re-runs the
+ * substeps between checkpoints (the neighbour sets of the adjoint are those
+ * of the re-run forward pass) and restores the solver's state afterwards, so
+ * stepping may continue; the tape stays open until bp_solver_tape_end.
+ *
+ * Stages with an adjoint: planes, wind, distance constraints, immovables,
+ * the velocity update, and in reference mode the fluid density / lambda /
+ * position correction and XSPH.  Recordings that used particle collisions
+ * between solids, shape matching, vorticity or Akinci tension, or textbook
+ * fluid passes return BP_ERR_INVALID_ARGUMENT from bp_solver_backward. */
+typedef struct bp_gradients {
+    float *positions;            /* [N][3] dL/dx at tape begin, original order, or NULL */
+    float *velocities;           /* [N][3] dL/dv at tape begin, or NULL */
+    float *wind_velocity;        /* [3] dL/d wind_velocity (textbook wind), or NULL */
+    float *distance_stiffness;   /* [M] dL/d stiffness of each distance constraint, or NULL */
+    float *distance_rest_length; /* [M] dL/d rest length, or NULL */
+} bp_gradients;
+bp_status bp_solver_tape_begin(bp_solver *s, int32_t checkpoint_every);
+bp_status bp_solver_backward(bp_solver *s, const float *grad_positions, const float *grad_velocities,
+                             bp_gradients *out);
+bp_status bp_solver_tape_end(bp_solver *s);
+
 /* ---- Batched ensembles ----------------------------------------------------
  * No counterpart in the reference, which steps one scene per solver.  Many
  * independent scenes advance together, one kernel launch per stage over all

@@ -42,7 +42,7 @@ def test_library_exports_every_declared_symbol(bp):
 
 def test_struct_layout_matches_header(bp, tmp_path):
     abi = bp.abi
-    fields = {"bp_params": abi.BpParams, "bp_scene_desc": abi.BpSceneDesc}
+    fields = {"bp_params": abi.BpParams, "bp_scene_desc": abi.BpSceneDesc, "bp_gradients": abi.BpGradients}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "brasspan.h"', "int main(void){"]
     for cname, py in fields.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')

@@ -1,0 +1,190 @@
+"""Adjoint of the solver step (bp_solver_backward) on the GPU through the C ABI.
+
+Gradients of a loss of the final state are compared with central finite
+differences of the same forward solver (directional derivatives along random
+directions, so every component of a gradient vector takes part), on short
+rollouts where the dynamics are smooth.  The forward runs in fp32, so a
+perturbed rollout rounds differently everywhere and the loss carries about
+1e-5 of absolute noise; the steps below are large enough that this noise and
+the O(eps^2) truncation both stay under the 0.5 % tolerance (measured: 0.02 %
+for positions and velocities, at most 0.4 % for wind and stiffness).
+Checkpoint spacing must not change the result, and the solver's state must be
+as it was after backward."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DT = 1.0 / 60.0
+FD_REL = 5e-3  # |fd - adjoint| <= FD_REL * scale, scale = max(|fd|, |adjoint|, floor)
+
+
+def cloth_case(bp, n=10):
+    abi = bp.abi
+    scene = bp.scenes.flag_scene(n=n, seed=3, mass=0.05)  # light, so that the wind moves it
+    stages = abi.BP_STAGE_PLANES | abi.BP_STAGE_WIND | abi.BP_STAGE_DISTANCE | abi.BP_STAGE_IMMOVABLE
+    params = bp.make_params(scene, mode=abi.BP_MODE_TEXTBOOK, stage_mask=stages, wind_velocity=(4.0, 0.0, 1.0),
+                            wind_drag=1.0, wind_lift=0.3)
+    return scene, params
+
+
+def fluid_case(bp, n=6):
+    abi = bp.abi
+    scene = bp.scenes.pbf_scene(n, n, n, spacing=0.1, seed=5, box=(1.2, 2.0, 1.2), grid_dim=16)
+    rng = np.random.default_rng(6)
+    scene.velocities = rng.uniform(-0.2, 0.2, (scene.num_particles, 3)).astype(np.float32)
+    stages = abi.BP_STAGE_FLUID | abi.BP_STAGE_PLANES | abi.BP_STAGE_XSPH
+    return scene, bp.make_params(scene, stage_mask=stages)
+
+
+def rollout(bp, scene, params, updates, substeps=2, iterations=4):
+    s = bp.ParticleSolver(scene, params)
+    for _ in range(updates):
+        s.update(substeps, DT, iterations)
+    x, v = s.positions(), s.velocities()
+    s.close()
+    return x, v
+
+
+def loss_weights(n, seed=11):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal((n, 3)).astype(np.float32), rng.standard_normal((n, 3)).astype(np.float32) * 0.1
+
+
+def loss(x, v, wx, wv):
+    return float(np.sum(x.astype(np.float64) * wx) + np.sum(v.astype(np.float64) * wv))
+
+
+def adjoint(bp, scene, params, updates, wx, wv, every=2, substeps=2, iterations=4):
+    s = bp.ParticleSolver(scene, params)
+    s.tape_begin(every)
+    for _ in range(updates):
+        s.update(substeps, DT, iterations)
+    g = s.backward(wx, wv)
+    s.close()
+    return g
+
+
+def check_dir(fd, ad, floor):
+    scale = max(abs(fd), abs(ad), floor)
+    assert abs(fd - ad) <= FD_REL * scale, f"finite difference {fd:.6e} vs adjoint {ad:.6e}"
+
+
+def test_cloth_gradients_match_finite_differences(bp, gpu):
+    import copy
+
+    scene, params = cloth_case(bp)
+    updates = 3
+    wx, wv = loss_weights(scene.num_particles)
+    g = adjoint(bp, scene, params, updates, wx, wv)
+    rng = np.random.default_rng(21)
+
+    def L(sc, pr):
+        return loss(*rollout(bp, sc, pr, updates), wx, wv)
+
+    pairs = []  # (what, eps, finite difference, adjoint)
+    # wind velocity (textbook wind is relative to it)
+    for eps in (0.2,):
+        for k in range(3):
+            pp, pm = copy.copy(params), copy.copy(params)
+            pp.wind_velocity[k] += eps
+            pm.wind_velocity[k] -= eps
+            pairs.append((f"wind[{k}]", eps, (L(scene, pp) - L(scene, pm)) / (2 * eps), float(g["wind_velocity"][k])))
+    # stiffness of every distance constraint, along one random direction
+    d = rng.standard_normal(scene.num_distance_constraints).astype(np.float32)
+    d /= np.linalg.norm(d)
+    for eps in (4e-2,):
+        sp, sm = copy.deepcopy(scene), copy.deepcopy(scene)
+        sp.distance_params[:, 1] += eps * d
+        sm.distance_params[:, 1] -= eps * d
+        pairs.append(("stiffness", eps, (L(sp, params) - L(sm, params)) / (2 * eps),
+                      float(g["distance_stiffness"] @ d)))
+    # initial velocities and positions
+    for key, e0 in (("velocities", 4e-2), ("positions", 4e-3)):
+        d = rng.standard_normal((scene.num_particles, 3)).astype(np.float32)
+        d /= np.linalg.norm(d)
+        for eps in (e0,):
+            sp, sm = copy.deepcopy(scene), copy.deepcopy(scene)
+            setattr(sp, key, (getattr(scene, key) + eps * d).astype(np.float32))
+            setattr(sm, key, (getattr(scene, key) - eps * d).astype(np.float32))
+            pairs.append((key, eps, (L(sp, params) - L(sm, params)) / (2 * eps), float(np.sum(g[key] * d))))
+    report = "; ".join(f"{w}@{e:g} {fd:.5e}/{ad:.5e}" for w, e, fd, ad in pairs)
+    print(report)
+    floor = 1e-2 * max(abs(a) for _, _, _, a in pairs)
+    bad = [f"{w}@{e:g}: fd {fd:.6e} adjoint {ad:.6e}" for w, e, fd, ad in pairs
+           if abs(fd - ad) > FD_REL * max(abs(fd), abs(ad), floor)]
+    assert not bad, "; ".join(bad) + " | all: " + report
+
+
+def test_fluid_gradients_match_finite_differences(bp, gpu):
+    """Reference-mode position-based fluid with planes and XSPH: gradient of the
+    final centre of mass with respect to the initial velocity field."""
+    import copy
+
+    scene, params = fluid_case(bp)
+    n = scene.num_particles
+    updates = 2
+    wx = np.zeros((n, 3), np.float32)
+    wx[:, 0] = 1.0 / n  # loss: x of the centre of mass
+    wx[:, 1] = 0.5 / n
+    wv = np.zeros((n, 3), np.float32)
+    g = adjoint(bp, scene, params, updates, wx, wv, iterations=3)
+    rng = np.random.default_rng(31)
+    for trial in range(2):
+        d = rng.standard_normal((n, 3)).astype(np.float32)
+        d /= np.linalg.norm(d)
+        eps = 2e-2
+        sp, sm = copy.deepcopy(scene), copy.deepcopy(scene)
+        sp.velocities = (scene.velocities + eps * d).astype(np.float32)
+        sm.velocities = (scene.velocities - eps * d).astype(np.float32)
+        fd = (loss(*rollout(bp, sp, params, updates, iterations=3), wx, wv) -
+              loss(*rollout(bp, sm, params, updates, iterations=3), wx, wv)) / (2 * eps)
+        check_dir(fd, float(np.sum(g["velocities"] * d)), 1e-4)
+
+
+def test_checkpoint_spacing_does_not_change_gradients(bp, gpu):
+    scene, params = cloth_case(bp, n=8)
+    wx, wv = loss_weights(scene.num_particles, seed=5)
+    ref = adjoint(bp, scene, params, 4, wx, wv, every=1)
+    for every in (3, 100):
+        g = adjoint(bp, scene, params, 4, wx, wv, every=every)
+        for k in ref:
+            np.testing.assert_array_equal(ref[k], g[k], err_msg=f"{k}, checkpoint every {every}")
+
+
+def test_backward_restores_the_state(bp, gpu):
+    scene, params = cloth_case(bp, n=8)
+    wx, wv = loss_weights(scene.num_particles)
+    a = bp.ParticleSolver(scene, params)
+    b = bp.ParticleSolver(scene, params)
+    a.tape_begin(2)
+    for s in (a, b):
+        for _ in range(3):
+            s.update(2, DT, 4)
+    a.backward(wx, wv)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.velocities(), b.velocities())
+    for s in (a, b):
+        s.update(2, DT, 4)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    a.tape_end()
+    a.close()
+    b.close()
+
+
+def test_backward_rejects_stages_without_adjoint(bp, gpu):
+    abi = bp.abi
+    scene, _ = fluid_case(bp, n=4)
+    s = bp.ParticleSolver(scene, bp.make_params(scene))  # vorticity and Akinci on
+    s.tape_begin(1)
+    s.update(1, DT, 2)
+    with pytest.raises(bp.BrassPanError):
+        s.backward(np.ones((scene.num_particles, 3), np.float32))
+    s.close()
+    t = bp.ParticleSolver(scene, bp.make_params(scene))
+    with pytest.raises(bp.BrassPanError):
+        t.backward(np.ones((scene.num_particles, 3), np.float32))  # nothing recorded
+    t.close()
+    assert abi.BP_STAGE_VORTICITY
