@@ -6,10 +6,12 @@
 // update once `checkpoint_every` substeps have passed since the last
 // checkpoint.  bp_solver_backward walks the recorded substeps backwards: per
 // segment between checkpoints it re-runs the forward substeps from the
-// checkpoint, keeping each substep's start state; then, last substep first,
-// it re-runs the substep once more recording every stage's input
-// (SubstepTape) and applies the adjoint kernels of the stages in reverse
-// order (bp_adjoint.cu).  The neighbour sets of the adjoint walks are those
+// checkpoint, keeping each substep's start state, every stage's input
+// (SubstepTape) and the grid the substep ran with; then, last substep first,
+// it applies the adjoint kernels of the stages in reverse order
+// (bp_adjoint.cu).  Each position in a segment has its own buffers, so its
+// recording re-run and its adjoint are each captured once as a CUDA graph and
+// replayed for every segment.  The neighbour sets of the adjoint walks are those
 // of the re-run forward pass.  Finally the solver's state is put back as it
 // was before the call.
 #include <algorithm>
@@ -62,6 +64,14 @@ struct StateBuf {
     int *orig = nullptr;
 };
 
+// What a substep leaves in the solver's buffers that its adjoint reads: the
+// reordered positions, the order and maps, masses, the cell keys and offsets.
+struct SubCtx {
+    float4 *Xs = nullptr;
+    int *order = nullptr, *to_new = nullptr, *keys = nullptr, *off = nullptr;
+    float *mass = nullptr, *w = nullptr;
+};
+
 }  // namespace
 
 struct Tape {
@@ -77,13 +87,14 @@ struct Tape {
     int since = 0;
     bool picked = false;
     DevPool pool;
-    std::vector<StateBuf> seg;  // start states of a segment's substeps
-    StateBuf start;             // the start state of the substep being differentiated
-    SubstepTape sub;
-    // CUDA graphs of one plain substep and of one taped substep + its adjoint,
-    // for the substep configuration in key_fwd / key_bwd
-    cudaGraphExec_t g_fwd = nullptr, g_bwd = nullptr;
-    std::vector<char> key_fwd, key_bwd, key_warm;
+    // per position in a segment: the substep's start state, its stage records,
+    // the grid and order it ran with, and the CUDA graphs of its recording
+    // re-run and of its adjoint (captured for the configuration in the keys)
+    std::vector<StateBuf> seg;
+    std::vector<SubstepTape *> tapes;
+    std::vector<SubCtx> ctxs;
+    std::vector<cudaGraphExec_t> g_fwd, g_bwd;
+    std::vector<std::vector<char>> key_fwd, key_bwd, key_warm;
     // adjoint buffers
     bool grads_ready = false;
     float4 *gX = nullptr, *gV = nullptr, *gXn = nullptr, *gVn = nullptr, *gP = nullptr, *gP2 = nullptr;
@@ -96,10 +107,15 @@ struct Tape {
 void destroy_tape(Tape *t)
 {
     if (!t) return;
-    if (t->g_fwd) cudaGraphExecDestroy(t->g_fwd);
-    if (t->g_bwd) cudaGraphExecDestroy(t->g_bwd);
-    for (float4 *p : t->sub.pool4) cudaFree(p);
-    for (float *p : t->sub.pool1) cudaFree(p);
+    for (cudaGraphExec_t g : t->g_fwd)
+        if (g) cudaGraphExecDestroy(g);
+    for (cudaGraphExec_t g : t->g_bwd)
+        if (g) cudaGraphExecDestroy(g);
+    for (SubstepTape *st : t->tapes) {
+        for (float4 *p : st->pool4) cudaFree(p);
+        for (float *p : st->pool1) cudaFree(p);
+        delete st;
+    }
     delete t;
 }
 
@@ -168,6 +184,36 @@ void load_state(bp_solver *s, const StateBuf &b)
         cudaMemcpyAsync(s->rigid.rot, b.rot, nb * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream);
         cudaMemcpyAsync(s->rigid.cm, b.cm, nb * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream);
     }
+}
+
+bool alloc_ctx(Tape &t, const bp_solver *s, SubCtx &c)
+{
+    const size_t n = (size_t)s->n;
+    c.Xs = t.pool.get<float4>(n);
+    c.order = t.pool.get<int>(n);
+    c.to_new = t.pool.get<int>(n);
+    c.keys = t.pool.get<int>(n);
+    c.off = t.pool.get<int>(s->ncells + 1);
+    c.mass = t.pool.get<float>(n);
+    c.w = t.pool.get<float>(n);
+    return c.Xs && c.order && c.to_new && c.keys && c.off && c.mass && c.w;
+}
+
+// direction: true saves the solver's buffers into c, false loads them back
+void copy_ctx(bp_solver *s, const SubCtx &c, bool save)
+{
+    const size_t n = (size_t)s->n;
+    auto cp = [&](void *solver_buf, void *ctx_buf, size_t bytes) {
+        cudaMemcpyAsync(save ? ctx_buf : solver_buf, save ? solver_buf : ctx_buf, bytes, cudaMemcpyDeviceToDevice,
+                        s->stream);
+    };
+    cp(s->Xs, c.Xs, n * sizeof(float4));
+    cp(s->order, c.order, n * sizeof(int));
+    cp(s->to_new, c.to_new, n * sizeof(int));
+    cp(s->sorted_keys, c.keys, n * sizeof(int));
+    cp(s->off, c.off, (s->ncells + 1) * sizeof(int));
+    cp(s->mass, c.mass, n * sizeof(float));
+    cp(s->w, c.w, n * sizeof(float));
 }
 
 // Every buffer a caller can observe after an update, saved around backward.
@@ -264,13 +310,12 @@ bp_status ensure_grads(Tape &t, const bp_solver *s)
 // state (start.X, start.V, in the previous order) on exit.  Every buffer
 // keeps its role (results are copied back rather than swapped), so the
 // sequence can be captured once and replayed for every substep.
-void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &start)
+void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &start, const SubstepTape &T)
 {
     const cudaStream_t st = s->stream;
     SimConsts C = u.C;  // the adjoint walks take the 27 cells
     C.nl_mask = nullptr;
     C.nl_stats = nullptr;
-    SubstepTape &T = t.sub;
     const bp_params &p = u.prm;
     const bool planes = stage_on(p, BP_STAGE_PLANES) && s->nplanes > 0;
     const bool distance = stage_on(p, BP_STAGE_DISTANCE) && s->dist.num_edges > 0;
@@ -385,7 +430,6 @@ extern "C" bp_status bp_solver_tape_begin(bp_solver *s, int32_t checkpoint_every
     s->tape = new (std::nothrow) Tape();
     if (!s->tape) return fail_with(BP_ERR_OUT_OF_MEMORY, "tape");
     s->tape->every = checkpoint_every;
-    s->tape->sub.s = s;
     return BP_OK;
 }
 
@@ -437,7 +481,6 @@ extern "C" bp_status bp_solver_backward(bp_solver *s, const float *grad_position
         snap.restore(s);
         return fail_with(e, msg);
     };
-    if (!t.start.X && !alloc_state(t, s, t.start)) return bail(BP_ERR_OUT_OF_MEMORY, "backward: start state");
     int seg_end = (int)t.subs.size();
     while (seg_end > 0) {
         int seg_begin = seg_end - 1;
@@ -445,41 +488,54 @@ extern "C" bp_status bp_solver_backward(bp_solver *s, const float *grad_position
         const int len = seg_end - seg_begin;
         while ((int)t.seg.size() < len) {
             StateBuf b;
-            if (!alloc_state(t, s, b)) return bail(BP_ERR_OUT_OF_MEMORY, "backward: segment states");
+            SubCtx c;
+            SubstepTape *tp = new (std::nothrow) SubstepTape();
+            if (!tp || !alloc_state(t, s, b) || !alloc_ctx(t, s, c)) {
+                delete tp;
+                return bail(BP_ERR_OUT_OF_MEMORY, "backward: segment buffers");
+            }
+            tp->s = s;
             t.seg.push_back(b);
+            t.ctxs.push_back(c);
+            t.tapes.push_back(tp);
+            t.g_fwd.push_back(nullptr);
+            t.g_bwd.push_back(nullptr);
+            t.key_fwd.emplace_back();
+            t.key_bwd.emplace_back();
+            t.key_warm.emplace_back();
         }
-        // forward from the checkpoint, keeping each substep's start state
+        // forward from the checkpoint, recording every substep: its start
+        // state, each stage's input and the grid it ran with
         load_state(s, t.ckpts[t.subs[seg_begin].ckpt]);
         for (int k = seg_begin; k < seg_end; ++k) {
-            save_state(s, t.seg[k - seg_begin]);
-            if (k + 1 < seg_end) {
-                const Tape::Sub &u = t.subs[k];
-                s->prm = u.prm;
-                const bp_status e = replay(s, t.g_fwd, t.key_fwd, u, [&] {
-                    enqueue_substep(s, u.C, u.iterations, -1, make_float3(0.f, 0.f, 0.f), &L);
-                });
-                if (e != BP_OK) return bail(e, "backward: forward graph");
-            }
-        }
-        // last substep first: re-run it recording every stage input, then its adjoint
-        for (int k = seg_end - 1; k >= seg_begin; --k) {
+            const int q = k - seg_begin;
             const Tape::Sub &u = t.subs[k];
             s->prm = u.prm;
-            load_state(s, t.seg[k - seg_begin]);
-            save_state(s, t.start);
             auto body = [&] {
-                t.sub.reset();
-                enqueue_substep(s, u.C, u.iterations, -1, make_float3(0.f, 0.f, 0.f), &L, &t.sub);
-                adjoint_substep(s, t, u, t.start);
+                save_state(s, t.seg[q]);
+                t.tapes[q]->reset();
+                enqueue_substep(s, u.C, u.iterations, -1, make_float3(0.f, 0.f, 0.f), &L, t.tapes[q]);
+                copy_ctx(s, t.ctxs[q], true);
             };
-            if (sub_key(u) != t.key_warm) {  // a new configuration runs once directly, growing
-                body();                       // the record pool outside any capture
-                if (!t.sub.ok) return bail(BP_ERR_OUT_OF_MEMORY, "backward: stage records");
-                t.key_warm = sub_key(u);
-                continue;
+            if (sub_key(u) != t.key_warm[q]) {  // a new configuration runs once directly, growing
+                body();                          // the record pool outside any capture
+                if (!t.tapes[q]->ok) return bail(BP_ERR_OUT_OF_MEMORY, "backward: stage records");
+                t.key_warm[q] = sub_key(u);
+            } else {
+                const bp_status e = replay(s, t.g_fwd[q], t.key_fwd[q], u, body);
+                if (e != BP_OK) return bail(e, "backward: recording graph");
             }
-            const bp_status e = replay(s, t.g_bwd, t.key_bwd, u, body);
-            if (e != BP_OK || !t.sub.ok) return bail(e != BP_OK ? e : BP_ERR_OUT_OF_MEMORY, "backward: adjoint graph");
+        }
+        // last substep first: the adjoint of each, on the grid it ran with
+        for (int k = seg_end - 1; k >= seg_begin; --k) {
+            const int q = k - seg_begin;
+            const Tape::Sub &u = t.subs[k];
+            s->prm = u.prm;
+            const bp_status e = replay(s, t.g_bwd[q], t.key_bwd[q], u, [&] {
+                copy_ctx(s, t.ctxs[q], false);
+                adjoint_substep(s, t, u, t.seg[q], *t.tapes[q]);
+            });
+            if (e != BP_OK) return bail(e, "backward: adjoint graph");
         }
         seg_end = seg_begin;
     }
