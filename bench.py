@@ -238,16 +238,19 @@ def dist_info():
 
 
 def traffic_for(kernel: str, n: int):
-    """dram bytes per launch for `kernel` from the committed ncu summary, scaled
-    to n particles (traffic grows with the particle count)."""
-    p = REPO / "profiles" / "traffic.json"
+    """DRAM bytes per launch of `kernel` from its committed ncu summary
+    (profiles/k_<name>_fluid_1048576.md, a 1,048,576-particle launch), scaled
+    to n particles: the traffic grows with the particle count."""
+    import re
+
+    name = kernel.replace("launch_", "k_")
+    p = REPO / "profiles" / f"{name}_fluid_1048576.md"
     if not p.exists():
         return None
-    d = json.loads(p.read_text())
-    e = d.get(kernel)
-    if not e:
+    m = re.search(r"DRAM traffic of the launch: ([0-9.]+) MB", p.read_text())
+    if not m:
         return None
-    return float(e["dram_bytes_per_launch"]) * n / float(e["particles"])
+    return float(m.group(1)) * 1e6 * n / 1048576.0
 
 
 def run_ours(args):
