@@ -282,9 +282,67 @@ public:
     }
     bp_solver *handle() { return s_; }
 
+    // Differentiable rollouts (no counterpart in the reference): record the
+    // following updates, then gradients of a loss of the final state.
+    struct Gradients {
+        std::vector<float> positions, velocities, windVelocity, distanceStiffness, distanceRestLength;
+    };
+    void tapeBegin(int checkpointEvery) { check(bp_solver_tape_begin(s_, checkpointEvery)); }
+    void tapeEnd() { check(bp_solver_tape_end(s_)); }
+    // dLdx, dLdv: [N][3] in original order (either may be empty for zero);
+    // numDistanceConstraints sizes the per-constraint gradients
+    Gradients backward(const std::vector<float> &dLdx, const std::vector<float> &dLdv, int numDistanceConstraints)
+    {
+        Gradients g;
+        g.positions.assign(3 * (size_t)n_, 0.f);
+        g.velocities.assign(3 * (size_t)n_, 0.f);
+        g.windVelocity.assign(3, 0.f);
+        g.distanceStiffness.assign((size_t)numDistanceConstraints, 0.f);
+        g.distanceRestLength.assign((size_t)numDistanceConstraints, 0.f);
+        bp_gradients out;
+        out.positions = g.positions.data();
+        out.velocities = g.velocities.data();
+        out.wind_velocity = g.windVelocity.data();
+        out.distance_stiffness = numDistanceConstraints ? g.distanceStiffness.data() : nullptr;
+        out.distance_rest_length = numDistanceConstraints ? g.distanceRestLength.data() : nullptr;
+        check(bp_solver_backward(s_, dLdx.empty() ? nullptr : dLdx.data(), dLdv.empty() ? nullptr : dLdv.data(),
+                                 &out));
+        return g;
+    }
+
 private:
     bp_solver *s_ = nullptr;
     int n_ = 0;
+};
+
+// Many independent scenes stepped together (no counterpart in the reference).
+class BatchSolver {
+public:
+    BatchSolver(const std::vector<const Scene *> &scenes, void *stream = nullptr)
+    {
+        std::vector<bp_scene_desc> d;
+        std::vector<bp_params> p;
+        for (const Scene *sc : scenes) {
+            d.push_back(sc->desc());
+            p.push_back(sc->params());
+        }
+        check(bp_batch_create((int32_t)d.size(), d.data(), p.data(), stream, &s_));
+    }
+    ~BatchSolver() { bp_solver_destroy(s_); }
+    BatchSolver(const BatchSolver &) = delete;
+    BatchSolver &operator=(const BatchSolver &) = delete;
+    void step(float dt, int numSubTimeStep, int iterations) { check(bp_batch_step(s_, dt, numSubTimeStep, iterations)); }
+    // first original id and particle count of one scene
+    std::pair<int, int> sceneRange(int scene) const
+    {
+        int32_t first, count;
+        check(bp_batch_scene_range(s_, scene, &first, &count));
+        return {first, count};
+    }
+    bp_solver *handle() { return s_; }
+
+private:
+    bp_solver *s_ = nullptr;
 };
 
 }  // namespace brasspan
