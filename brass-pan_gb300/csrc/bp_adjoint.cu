@@ -11,7 +11,8 @@
 // Supported stages: prediction and reorder, planes (stabilisation and
 // collision), wind, reference-mode fluid density / lambda / position
 // correction (with s_corr and the per-pair clamp), distance constraints,
-// immovables, the velocity update and reference-mode XSPH.
+// shape matching (rotation differentiated at its fixed point), immovables,
+// the velocity update and reference-mode XSPH.
 #include "bp_dual.cuh"
 #include "bp_internal.h"
 #include "bp_walk.cuh"
@@ -501,6 +502,150 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_xsph(SimConsts C, const fl
     gX[i] = f4(add3(ld3(gX, i), gp));
 }
 
+// ---- shape matching (alpha = 1): g_i = R q_i + cm ----
+// cm = mean(p_i), A = sum (p_i - cm) q_i^T, R the rotation the extraction
+// converged to (recorded).  R is differentiated implicitly through its fixed
+// point, where R^T A = S is symmetric: dR = R [w]x with (tr(S) I - S) w =
+// vee(R^T dA - dA^T R).  Hence A-bar = R [z]x with z = (tr(S) I - S)^-1
+// vee(R^T R-bar - R-bar^T R), R-bar = sum g-bar_i q_i^T.
+
+struct M3 {
+    float m[3][3];  // row-major
+};
+__device__ __forceinline__ M3 quat_mat(float4 q)
+{
+    const float x = q.x, y = q.y, z = q.z, w = q.w;
+    M3 r;
+    r.m[0][0] = 1 - 2 * y * y - 2 * z * z;
+    r.m[1][0] = 2 * x * y + 2 * w * z;
+    r.m[2][0] = 2 * x * z - 2 * w * y;
+    r.m[0][1] = 2 * x * y - 2 * w * z;
+    r.m[1][1] = 1 - 2 * x * x - 2 * z * z;
+    r.m[2][1] = 2 * y * z + 2 * w * x;
+    r.m[0][2] = 2 * x * z + 2 * w * y;
+    r.m[1][2] = 2 * y * z - 2 * w * x;
+    r.m[2][2] = 1 - 2 * x * x - 2 * y * y;
+    return r;
+}
+
+constexpr int kAdjSmThreads = 256;
+
+template <int NV>
+__device__ __forceinline__ void adj_block_sum(float (&v)[NV], float (*red)[kAdjSmThreads / 32])
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        float s = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) red[k][warp] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        float s = 0.f;
+        for (int q = 0; q < kAdjSmThreads / 32; ++q) s += red[k][q];
+        v[k] = s;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kAdjSmThreads) k_adj_shape_matching(RigidArgs a, const float4 *__restrict__ rotq,
+                                                                      const float4 *__restrict__ Pin,
+                                                                      const int *__restrict__ to_new,
+                                                                      float4 *__restrict__ gP)
+{
+    __shared__ float red[12][kAdjSmThreads / 32];
+    __shared__ float s_abar[9], s_cmb[3];
+    const int b = blockIdx.x;
+    const int2 rg = a.ranges[b];
+    const int np = rg.y - rg.x;
+    float c[3] = {0.f, 0.f, 0.f};
+    for (int t = threadIdx.x; t < np; t += kAdjSmThreads) {
+        const float3 p = ld3(Pin, to_new[rg.x + t]);
+        c[0] += p.x;
+        c[1] += p.y;
+        c[2] += p.z;
+    }
+    adj_block_sum<3>(c, red);
+    const float3 cm = make_float3(c[0] / np, c[1] / np, c[2] / np);
+    // A (row-major), R-bar, sum of g-bar, sum of q
+    float acc[12] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float acc2[12] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int t = threadIdx.x; t < np; t += kAdjSmThreads) {
+        const int id = to_new[rg.x + t];
+        const float3 q = f3(a.rest[rg.x + t]);
+        const float3 pc = sub3(ld3(Pin, id), cm);
+        const float3 g = ld3(gP, id);
+        const float pv[3] = {pc.x, pc.y, pc.z}, qv[3] = {q.x, q.y, q.z}, gv[3] = {g.x, g.y, g.z};
+        for (int r = 0; r < 3; ++r)
+            for (int k = 0; k < 3; ++k) {
+                acc[3 * r + k] += pv[r] * qv[k];   // A
+                acc2[3 * r + k] += gv[r] * qv[k];  // R-bar
+            }
+        acc[9] += g.x;
+        acc[10] += g.y;
+        acc[11] += g.z;
+        acc2[9] += q.x;
+        acc2[10] += q.y;
+        acc2[11] += q.z;
+    }
+    adj_block_sum<12>(acc, red);
+    adj_block_sum<12>(acc2, red);
+    if (threadIdx.x == 0) {
+        const M3 R = quat_mat(rotq[b]);
+        float S[3][3], X[3][3];  // S = R^T A, X = R^T R-bar
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                float s = 0.f, x = 0.f;
+                for (int k = 0; k < 3; ++k) {
+                    s += R.m[k][i] * acc[3 * k + j];
+                    x += R.m[k][i] * acc2[3 * k + j];
+                }
+                S[i][j] = s;
+                X[i][j] = x;
+            }
+        const float u[3] = {X[2][1] - X[1][2], X[0][2] - X[2][0], X[1][0] - X[0][1]};
+        const float tr = S[0][0] + S[1][1] + S[2][2];
+        float G[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) G[i][j] = (i == j ? tr : 0.f) - 0.5f * (S[i][j] + S[j][i]);
+        // z = G^-1 u by the adjugate
+        const float c00 = G[1][1] * G[2][2] - G[1][2] * G[2][1], c01 = G[1][2] * G[2][0] - G[1][0] * G[2][2],
+                    c02 = G[1][0] * G[2][1] - G[1][1] * G[2][0];
+        const float det = G[0][0] * c00 + G[0][1] * c01 + G[0][2] * c02;
+        float z[3] = {0.f, 0.f, 0.f};
+        if (fabsf(det) > 1e-20f) {
+            const float inv = 1.0f / det;
+            const float Gi[3][3] = {{c00 * inv, (G[0][2] * G[2][1] - G[0][1] * G[2][2]) * inv,
+                                     (G[0][1] * G[1][2] - G[0][2] * G[1][1]) * inv},
+                                    {c01 * inv, (G[0][0] * G[2][2] - G[0][2] * G[2][0]) * inv,
+                                     (G[0][2] * G[1][0] - G[0][0] * G[1][2]) * inv},
+                                    {c02 * inv, (G[0][1] * G[2][0] - G[0][0] * G[2][1]) * inv,
+                                     (G[0][0] * G[1][1] - G[0][1] * G[1][0]) * inv}};
+            for (int i = 0; i < 3; ++i) z[i] = Gi[i][0] * u[0] + Gi[i][1] * u[1] + Gi[i][2] * u[2];
+        }
+        const float Z[3][3] = {{0.f, -z[2], z[1]}, {z[2], 0.f, -z[0]}, {-z[1], z[0], 0.f}};
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                s_abar[3 * i + j] = R.m[i][0] * Z[0][j] + R.m[i][1] * Z[1][j] + R.m[i][2] * Z[2][j];
+        // cm-bar: from the goals (sum g-bar) and from A through p_i - cm (-A-bar sum q)
+        for (int i = 0; i < 3; ++i)
+            s_cmb[i] = acc[9 + i] - (s_abar[3 * i] * acc2[9] + s_abar[3 * i + 1] * acc2[10] + s_abar[3 * i + 2] * acc2[11]);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < np; t += kAdjSmThreads) {
+        const int id = to_new[rg.x + t];
+        const float3 q = f3(a.rest[rg.x + t]);
+        float3 g;
+        g.x = s_abar[0] * q.x + s_abar[1] * q.y + s_abar[2] * q.z + s_cmb[0] / np;
+        g.y = s_abar[3] * q.x + s_abar[4] * q.y + s_abar[5] * q.z + s_cmb[1] / np;
+        g.z = s_abar[6] * q.x + s_abar[7] * q.y + s_abar[8] * q.z + s_cmb[2] / np;
+        gP[id] = f4(g);
+    }
+}
+
 // ---- launchers ----
 
 static int blocks(int n, int t = 256) { return (n + t - 1) / t; }
@@ -555,6 +700,12 @@ void adj_fluid(cudaStream_t st, const SimConsts &C, const float4 *Pin, const flo
     if (C.n <= 0) return;
     k_adj_deltap<<<blocks(C.n, kWalkThreads), kWalkThreads, 0, st>>>(C, Pin, mass, lam, off, gOut, gLam, gPart);
     k_adj_lambda<<<blocks(C.n, kWalkThreads), kWalkThreads, 0, st>>>(C, Pin, mass, rho, off, gLam, gPart, gOut, gIn);
+}
+void adj_shape_matching(cudaStream_t st, const RigidArgs &a, const float4 *rot, const float4 *Pin, const int *to_new,
+                        float4 *gP)
+{
+    if (a.num_bodies <= 0) return;
+    k_adj_shape_matching<<<a.num_bodies, kAdjSmThreads, 0, st>>>(a, rot, Pin, to_new, gP);
 }
 void adj_xsph(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
               const float4 *gVout, float4 *gVin, float4 *gX)

@@ -38,6 +38,8 @@ void adj_fluid(cudaStream_t st, const SimConsts &C, const float4 *Pin, const flo
                const float *rho, const int *off, const float4 *gOut, float *gLam, float4 *gPart, float4 *gIn);
 void adj_xsph(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
               const float4 *gVout, float4 *gVin, float4 *gX);
+void adj_shape_matching(cudaStream_t st, const RigidArgs &a, const float4 *rot, const float4 *Pin, const int *to_new,
+                        float4 *gP);
 
 namespace {
 
@@ -119,8 +121,9 @@ void destroy_tape(Tape *t)
     delete t;
 }
 
-int SubstepTape::snap4(const float4 *src)
+int SubstepTape::snap4(const float4 *src, size_t count)
 {
+    if (count == 0) count = (size_t)s->n;
     if (used4 == (int)pool4.size()) {
         void *p = nullptr;
         if (cudaMalloc(&p, (size_t)std::max(s->n, 1) * sizeof(float4)) != cudaSuccess) {
@@ -129,7 +132,7 @@ int SubstepTape::snap4(const float4 *src)
         }
         pool4.push_back((float4 *)p);
     }
-    cudaMemcpyAsync(pool4[used4], src, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream);
+    cudaMemcpyAsync(pool4[used4], src, count * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream);
     return used4++;
 }
 
@@ -263,8 +266,6 @@ bp_status check_supported(const bp_solver *s, const Tape &t)
         const bp_params &p = u.prm;
         if (stage_on(p, BP_STAGE_PARTICLE_COLLISION) && s->has_solid)
             return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: particle collisions have no adjoint");
-        if (stage_on(p, BP_STAGE_SHAPE_MATCHING) && s->rigid.num_bodies > 0)
-            return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: shape matching has no adjoint");
         if (stage_on(p, BP_STAGE_VORTICITY) || stage_on(p, BP_STAGE_AKINCI))
             return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: vorticity and Akinci tension have no adjoint");
         if (p.mode == BP_MODE_TEXTBOOK && (stage_on(p, BP_STAGE_FLUID) || stage_on(p, BP_STAGE_XSPH)))
@@ -347,6 +348,9 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
             break;
         case TS_PLANES:
             adj_planes(st, C, s->Xs, T.pool4[rec.slot], t.gP, t.gXs);
+            break;
+        case TS_SHAPE:
+            adj_shape_matching(st, s->rigid, T.pool4[rec.aux], T.pool4[rec.slot], s->to_new, t.gP);
             break;
         case TS_WIND:
             adj_wind(st, C, s->wind, T.pool4[rec.slot], T.pool4[T.vs_slot], s->mass, s->to_new, t.gP, t.gVs, t.FG,

@@ -693,6 +693,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         if (rigid) {
             if (tape) tape->push(TS_SHAPE, cur);
             launch_shape_matching(st, C, s->rigid, cur, s->to_new, L);
+            if (tape) tape->recs.back().aux = tape->snap4(s->rigid.rot, (size_t)s->rigid.num_bodies);
         }
         if (immov) {
             if (tape) tape->push(TS_IMMOVABLE, cur);

@@ -49,7 +49,7 @@ enum TapeStage : int {
 struct TapeRec {
     int stage;
     int slot;  // snapshot of the stage's input: positions, or velocities for TS_XSPH
-    int aux;   // TS_FLUID: snapshot of lambda (aux) and density (aux + 1)
+    int aux;   // TS_FLUID: snapshot of lambda (aux) and density (aux + 1); TS_SHAPE: the rotations after it
 };
 
 // The intermediates of one substep re-run for its adjoint: each stage's
@@ -68,7 +68,7 @@ struct SubstepTape {
         recs.clear();
         vs_slot = -1;
     }
-    int snap4(const float4 *src);
+    int snap4(const float4 *src, size_t count = 0);  // count 0: one per particle (count <= particles)
     int snap1(const float *src);
     void push(int stage, const float4 *src, int aux = -1) { recs.push_back(TapeRec{stage, snap4(src), aux}); }
 };

@@ -144,6 +144,57 @@ def test_fluid_gradients_match_finite_differences(bp, gpu):
         check_dir(fd, float(np.sum(g["velocities"] * d)), 1e-4)
 
 
+def rigid_case(bp):
+    abi = bp.abi
+    sc = bp.scenes
+    s = sc.Scene(name="rigid_air")
+    s.particle_radius, s.kernel_radius, s.cell_size, s.grid_dim, s.rest_density = 0.05, 0.2, 0.2, 32, 1000.0
+    s.add_plane((0.0, -20.0, 0.0), (0.0, 1.0, 0.0))
+    s.add_rigid_box((3, 3, 3), (0.0, 2.0, 0.0), (0.1, 0.1, 0.1), 1.0)
+    s.add_rigid_box((4, 2, 3), (1.0, 2.5, 0.3), (0.1, 0.1, 0.1), 1.0)
+    rng = np.random.default_rng(8)
+    s.velocities = rng.uniform(-0.5, 0.5, (s.num_particles, 3)).astype(np.float32)  # spins the boxes
+    return s, bp.make_params(s, stage_mask=abi.BP_STAGE_PLANES | abi.BP_STAGE_SHAPE_MATCHING)
+
+
+def test_rigid_gradients_match_finite_differences(bp, gpu):
+    """Shape matching, its rotation differentiated at the fixed point of the
+    extraction: initial velocities and positions of two spinning boxes."""
+    import copy
+
+    scene, params = rigid_case(bp)
+    updates = 3
+    wx, wv = loss_weights(scene.num_particles, seed=12)
+    g = adjoint(bp, scene, params, updates, wx, wv)
+    rng = np.random.default_rng(41)
+    pairs = []
+    # The extraction stops once its rotation step is below 3e-5 rad, so the
+    # forward map has jumps of that size: small steps (and deforming position
+    # directions) put those jumps into the quotient.  Velocities along a random
+    # direction with a 0.16 step, positions along rigid per-body translations.
+    body = np.zeros(scene.num_particles, np.int64)
+    for b, (r0, r1) in enumerate(scene.rigid_ranges):
+        body[r0:r1] = b
+    for key, eps0 in (("velocities", 0.16), ("positions", 0.016)):
+        if key == "velocities":
+            d = rng.standard_normal((scene.num_particles, 3)).astype(np.float32)
+        else:
+            d = rng.standard_normal((len(scene.rigid_ranges), 3)).astype(np.float32)[body]
+        d /= np.linalg.norm(d)
+        for eps in (eps0,):
+            sp, sm = copy.deepcopy(scene), copy.deepcopy(scene)
+            setattr(sp, key, (getattr(scene, key) + eps * d).astype(np.float32))
+            setattr(sm, key, (getattr(scene, key) - eps * d).astype(np.float32))
+            fd = (loss(*rollout(bp, sp, params, updates), wx, wv) -
+                  loss(*rollout(bp, sm, params, updates), wx, wv)) / (2 * eps)
+            pairs.append((f"{key}@{eps:g}", fd, float(np.sum(g[key] * d))))
+    report = "; ".join(f"{w} {fd:.5e}/{ad:.5e}" for w, fd, ad in pairs)
+    print(report)
+    floor = 1e-2 * max(abs(a) for _, _, a in pairs)
+    bad = [w for w, fd, ad in pairs if abs(fd - ad) > FD_REL * max(abs(fd), abs(ad), floor)]
+    assert not bad, report
+
+
 def test_checkpoint_spacing_does_not_change_gradients(bp, gpu):
     scene, params = cloth_case(bp, n=8)
     wx, wv = loss_weights(scene.num_particles, seed=5)
