@@ -63,7 +63,7 @@ void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // counted contacts; only particle i moves (the reference's j update is
 // commented out).  Reads P, writes Pout = P + delta.
 template <bool Split>
-__global__ void __launch_bounds__(kWalkThreads) k_particle_collision(SimConsts C, const float4 *__restrict__ P,
+__global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS) k_particle_collision(SimConsts C, const float4 *__restrict__ P,
                                                                      const float4 *__restrict__ Xs,
                                                                      const float *__restrict__ w,
                                                                      const int *__restrict__ off,

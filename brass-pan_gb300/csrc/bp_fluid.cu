@@ -24,7 +24,7 @@ constexpr int kScanThreads = kWalkThreads;  // scan kernels stage their neighbou
 // neighbours count x solid_scale; C = rho/rho0 - 1, clamped at 0 when Akinci
 // is on; lambda = -C / lambda_den.  Textbook mode: all j, exact denominator.
 template <bool Split>
-__global__ void __launch_bounds__(kScanThreads) k_lambda(SimConsts C, const float4 *__restrict__ P,
+__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(SimConsts C, const float4 *__restrict__ P,
                                                          const float *__restrict__ mass,
                                                          const int *__restrict__ off, float *__restrict__ lam,
                                                          float *__restrict__ rho)
@@ -101,7 +101,7 @@ void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // the lower-indexed of (k, j) is fluid.  Textbook mode: fluid k gathers over
 // every neighbour; solids do not move.
 template <bool Split>
-__global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs a)
+__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_deltap(SimConsts C, DeltaArgs a)
 {
     __shared__ StageShared S;
     const int i0 = blockIdx.x * kScanThreads;
@@ -117,12 +117,12 @@ __global__ void __launch_bounds__(kScanThreads) k_deltap(SimConsts C, DeltaArgs 
         const float lk = a.lam[k];
         walk_neighbors<Split>(
             k, pk, 0, a.P, grid_view(C, sc, a.off), C, &S, g,
-            [&](int j, float4 pj4) {
+            [&](int, float4 pj4) {  // r = 0 excludes k itself
                 const float d2 = len2(pk - f3(pj4));
-                const bool inc = C.textbook ? true : ((j > k) ? (phk < 0) : (phase_of(pj4) < 0));
-                return j != k && d2 <= C.h2 && d2 > 0.f && inc;
+                return d2 <= C.h2 && d2 > 0.f;
             },
             [&](int j, float4 pj4) {
+                if (!C.textbook && !((j > k) ? (phk < 0) : (phase_of(pj4) < 0))) return;
                 const float3 diff = pk - f3(pj4);
                 const float d2 = len2(diff);
                 float sl = __fadd_rn(lk, __ldg(a.lam + j));
@@ -222,7 +222,7 @@ void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, Laun
 // in one walk over same-phase neighbours with 0 < r^2 <= h^2.
 // Om[i] = (omega, |omega|); Nm[i] = (h * n, rho_i).
 template <bool Split>
-__global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const float4 *__restrict__ P,
+__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
                                                          const float *__restrict__ rho, const int *__restrict__ off,
                                                          float4 *__restrict__ Om, float4 *__restrict__ Nm)
@@ -244,8 +244,9 @@ __global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const floa
     // wants them) and records them for passes B and C
     walk_neighbors<Split>(
         i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, &S, g,
-        [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; },
+        [&](int, float4 pj4) { return len2(pi - f3(pj4)) <= C.h2; },
         [&](int j, float4 pj4) {
+            if (j == i || phase_of(pj4) != phi) return;
             if (C.nbr && cnt < C.nbr_cap) C.nbr[(size_t)cnt * C.n + i] = j;
             ++cnt;
             const float3 diff = pi - f3(pj4);
@@ -259,6 +260,32 @@ __global__ void __launch_bounds__(kScanThreads) k_post_a(SimConsts C, const floa
     Om[i] = make_float4(om.x, om.y, om.z, len3(om));
     const float3 n = C.h * nn;
     Nm[i] = make_float4(n.x, n.y, n.z, rho[i]);
+}
+
+// Passes B and C over the recorded neighbours of particle i, in order.  Four
+// entries at a time: their indices and positions are loaded before the
+// first of the four pair terms, so the dependent gathers overlap.
+template <class B>
+__device__ __forceinline__ void for_each_listed(const SimConsts &C, int i, int cnt, const float4 *__restrict__ P,
+                                                B &body)
+{
+    const int *__restrict__ list = C.nbr + i;
+    const size_t stride = (size_t)C.n;
+    int k = 0;
+    for (; k + 4 <= cnt; k += 4) {
+        int j[4];
+        float4 pj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) j[q] = __ldg(list + (size_t)(k + q) * stride);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pj[q] = P[j[q]];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) body(j[q], pj[q]);
+    }
+    for (; k < cnt; ++k) {
+        const int j = __ldg(list + (size_t)k * stride);
+        body(j, P[j]);
+    }
 }
 
 // Passes B and C: the number of recorded neighbours of particle i, or
@@ -278,7 +305,7 @@ __device__ __forceinline__ int post_list_count(const SimConsts &C, const float4 
 // v'' = v' + F dt, exactly the reference's sequence (in-place update followed
 // by newVelocities = velocities + F dt).  Solids pass through.
 template <bool Split>
-__global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const float4 *__restrict__ P,
+__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_b(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
                                                          const float4 *__restrict__ Om,
                                                          const float4 *__restrict__ Nm,
@@ -321,10 +348,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
         }
     };
     if (cnt != kWalkCells) {
-        for (int k = 0; k < cnt; ++k) {
-            const int j = __ldg(C.nbr + (size_t)k * C.n + i);
-            body(j, P[j]);
-        }
+        for_each_listed(C, i, cnt, P, body);
     } else {
         walk_neighbors<Split>(
             i, pi, 0, P, grid_view(C, sc, off), C, &S, g,
@@ -344,7 +368,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_b(SimConsts C, const floa
 // Pass C: XSPH viscosity (fluidXSph): same phase, j != i, r^2 <= h^2 (r = 0
 // included).  Textbook mode weights each neighbour by its volume m_j / rho_j.
 template <bool Split>
-__global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const float4 *__restrict__ P,
+__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_c(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
                                                          const int *__restrict__ off, const float *__restrict__ mass,
                                                          const float *__restrict__ rho, float4 *__restrict__ Vout)
@@ -370,10 +394,7 @@ __global__ void __launch_bounds__(kScanThreads) k_post_c(SimConsts C, const floa
         vn = fma3(wgt, f3(V[j]) - vi, vn);
     };
     if (cnt != kWalkCells) {
-        for (int k = 0; k < cnt; ++k) {
-            const int j = __ldg(C.nbr + (size_t)k * C.n + i);
-            body(j, P[j]);
-        }
+        for_each_listed(C, i, cnt, P, body);
     } else {
         walk_neighbors<Split>(
             i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, &S, g,

@@ -31,7 +31,15 @@
 namespace bp {
 
 constexpr int kWalkThreads = 256;
-constexpr int kStageCap = 2816;       // staged particles per CTA (44 KB)
+// Staged particles per CTA (44 KB at 2816) and the CTAs per SM the scan
+// kernels are compiled for (registers per thread <= 65536 / (256 x that)).
+#ifndef BP_STAGE_CAP
+#define BP_STAGE_CAP 2816
+#endif
+#ifndef BP_SCAN_MIN_BLOCKS
+#define BP_SCAN_MIN_BLOCKS 1
+#endif
+constexpr int kStageCap = BP_STAGE_CAP;
 constexpr int kStageSegs = 2 * 9 * 2; // groups x columns x pieces
 
 struct StageShared {
