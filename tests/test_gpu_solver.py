@@ -96,6 +96,24 @@ def test_stage_subsets_parity(bp, gpu, oracle, mask_name):
     assert_parity(errs, h, sdt)
 
 
+def test_large_rigid_bodies_parity(bp, gpu, oracle):
+    """Shape matching of bodies far beyond the reference kernel's 64-particle
+    limit (a 512-particle cube and a 1000-particle slab, as in the mixed and
+    shape-matching configurations), falling onto the floor and onto each other
+    with particle collisions, in lockstep with the oracle."""
+    sc = bp.scenes
+    s = sc.Scene(name="big_rigid")
+    s.particle_radius, s.kernel_radius, s.cell_size, s.grid_dim, s.rest_density = 0.05, 0.2, 0.2, 32, 1000.0
+    sc.box_planes(s, (0, 0, 0), (3.0, 4.0, 3.0))
+    s.add_rigid_box((8, 8, 8), (0.6, 0.3, 0.6), (0.1, 0.1, 0.1), 1.0)
+    s.add_rigid_box((10, 4, 25), (0.3, 1.4, 0.2), (0.1, 0.1, 0.1), 1.0)
+    rng = np.random.default_rng(17)
+    s.velocities = np.repeat(rng.uniform(-1.0, 1.0, (1, 3)), s.num_particles, axis=0).astype(np.float32)
+    s.velocities[:512] += rng.uniform(-0.2, 0.2, (512, 3)).astype(np.float32)  # spin the cube
+    assert [r1 - r0 for r0, r1 in s.rigid_ranges] == [512, 1000]
+    assert_parity(*lockstep(bp, oracle, s, bp.make_params(s), substeps=6))
+
+
 def test_textbook_mode_parity(bp, gpu, oracle):
     # s_corr k = 0.001: with m = 1 kg and rho0 = 1000 kg/m^3 the paper's k = 0.1
     # outweighs lambda ~50x and the block explodes (on the oracle as well)
