@@ -1,9 +1,12 @@
 """Throughput benchmark: particle-substeps/s of the solver step on one GB300.
 
-A step is one call of update(2 substeps, dt = 1/60 s, 4 iterations) on the
-mixed-phase scene of the benchmark configuration (1,048,576 PBF fluid
+A step is one call of update(2 substeps, dt = 1/60 s, 4 iterations) (one
+frame) on the mixed-phase scene of the benchmark configuration (1,048,576 PBF fluid
 particles, a 256x256 cloth under wind, 64 rigid 8^3 cubes; 1,146,880
-particles), reference-mode parameters.  Prints one JSON line; unless
+particles), reference-mode parameters.  By default the timed region is the
+configuration's 200 frames after 3 warm-up frames: throughput falls as the
+dam break spreads into cells the 64^3 table aliases and the fluid
+compresses, so short runs overstate it.  Prints one JSON line; unless
 --no-batch, its "batched" object times the batched ensemble (256 PBF dam
 breaks of 4096..262144 particles in one solver) against looping one solver
 per scene over the same scenes; unless --no-adjoint, its "adjoint" object
@@ -11,7 +14,7 @@ times forward + backward() of differentiable rollouts against the forward
 alone (wall clock, host arrays in and out).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload mixed|fluid|small|batch] [--no-batch] [--no-adjoint]
+                  [--workload mixed|fluid|small|batch|rigid] [--no-batch] [--no-adjoint]
 
 Multi-GPU (torchrun, one rank per GPU): the scene does not shard, so every
 rank advances its own replica ("replicas only"); value = all ranks' particle
@@ -66,6 +69,8 @@ def build_scene(bp, workload: str, seed: int = 0):
         return bp.scenes.pbf_scene(128, 64, 128, spacing=0.1, seed=seed, box=(12.9, 16.0, 12.9))
     if workload == "small":
         return bp.scenes.pbf_scene(32, 32, 32, spacing=0.1, seed=seed, box=(4.0, 4.0, 4.0))
+    if workload == "rigid":
+        return bp.scenes.config2_shape_stress(seed=seed)
     if workload == "batch":  # CPU-side sample of the ensemble: its largest member
         return max(bp.scenes.config3_ensemble(seed=seed), key=lambda sc: sc.num_particles)
     raise SystemExit(f"unknown workload {workload}")
@@ -74,7 +79,8 @@ def build_scene(bp, workload: str, seed: int = 0):
 def workload_name(workload, n):
     return {"mixed": "mixed-phase: 128x64x128 PBF fluid + 256^2 cloth (wind) + 64 rigid 8^3 cubes",
             "fluid": "PBF dam break 128x64x128", "small": "PBF dam break 32^3",
-            "batch": "batched ensemble: 256 PBF dam breaks, log-uniform 4096..262144 particles"}[workload] + f", N={n}"
+            "batch": "batched ensemble: 256 PBF dam breaks, log-uniform 4096..262144 particles",
+            "rigid": "shape-matching stress: 4096 rigid bodies of 27..1000 particles with contacts"}[workload] + f", N={n}"
 
 
 def timed_steps(torch, stream, flush, steps, fn):
@@ -287,7 +293,7 @@ def run_ours(args):
     else:
         scene = build_scene(bp, args.workload, seed=rank)
         n = scene.num_particles
-        params = tuned(bp.make_params(scene))
+        params = tuned(workload_params(bp, args.workload, scene))
         solver = bp.ParticleSolver(scene, params, stream=stream.cuda_stream)
 
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
@@ -360,6 +366,7 @@ def run_ours(args):
     traffic = traffic_for(top_name, n)
     step_ms_total = sum(v[1] for v in agg.values()) / prof_steps
     walks = solver.walk_stats(SUBSTEPS, DT, ITERATIONS)
+    device_errors = solver.device_errors()  # non-finite state anywhere in the run
     solver.close()
     batched = None
     if args.workload == "batch" or (args.workload == "mixed" and not args.no_batch):
@@ -389,7 +396,7 @@ def run_ours(args):
             "config": {"workload": workload_name(args.workload, n), "particles": n, "substeps": SUBSTEPS,
                        "iterations": ITERATIONS, "dt": DT, "mode": "reference",
                        "grid": ("one grid per scene (16^3..64^3 cells), cell = h = 0.2" if args.workload == "batch"
-                                else "64^3 cells, cell = h = 0.2"),
+                                else f"{params.grid_dim}^3 cells, cell = h = 0.2"),
                        "neighbor_skin": float(params.neighbor_skin), "staging": not args.no_stage, "split_walks": not args.no_split,
                        "post_lists": not args.no_lists,
                        "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
@@ -404,6 +411,7 @@ def run_ours(args):
                                    sorted(agg.items(), key=lambda kv: -kv[1][1])},
             "profiled_ms_per_step": step_ms_total,
             "neighbor_walks": walks,
+            "device_errors": device_errors,
             "cpu_baseline": cpu,
             "clocks": clk,
         }
@@ -417,6 +425,20 @@ def run_ours(args):
     return result
 
 
+def workload_params(bp, workload, scene):
+    """Parameters of a workload: the reference's literals, plus the stage set
+    of the shape-matching stress test (planes, contacts, shape matching).
+    The mixed scene runs without mass scaling: exp(2 y) at the cloth's and
+    cubes' heights (8 to 12 m) makes the contacts diverge within 120 frames."""
+    params = bp.make_params(scene)
+    if workload == "mixed":
+        params.mass_scaling_k = 0.0
+    if workload == "rigid":
+        params.stage_mask = (bp.abi.BP_STAGE_PLANES | bp.abi.BP_STAGE_PARTICLE_COLLISION |
+                             bp.abi.BP_STAGE_SHAPE_MATCHING)
+    return params
+
+
 def cpu_baseline(bp, workload, steps=1):
     """The oracle port (the reference's step restated in C, OpenMP over all
     host cores) on a bounded sample: `steps` substeps of the same scene."""
@@ -424,7 +446,7 @@ def cpu_baseline(bp, workload, steps=1):
 
     threads = os.cpu_count() or 1
     scene = build_scene(bp, workload, seed=0)
-    params = bp.make_params(scene)
+    params = workload_params(bp, workload, scene)
     kind = "port"
     o = oracle.OracleSolver(scene, params, threads=threads)
     o.update(1, DT / SUBSTEPS, ITERATIONS)  # warm-up substep (first-touch of the grid tables)
@@ -453,7 +475,7 @@ def run_reference(args):
 
     threads = os.cpu_count() or 1
     scene = build_scene(bp, args.workload, seed=0)
-    params = bp.make_params(scene)
+    params = workload_params(bp, args.workload, scene)
     solver = oracle.OracleSolver(scene, params, threads=threads)
     kind = "port"
     n = scene.num_particles
@@ -499,10 +521,10 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["mixed", "fluid", "small"], default="mixed")
+    ap.add_argument("--workload", choices=["mixed", "fluid", "small", "batch", "rigid"], default="mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint measurement")

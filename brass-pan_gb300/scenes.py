@@ -236,11 +236,13 @@ def config0_dam_break(seed=0):
     return pbf_scene(32, 32, 32, 0.1, seed=seed, box=(4.0, 4.0, 4.0), jitter_frac=0.01)
 
 
-def config1_mixed(seed=0, fluid=(128, 64, 128), cloth=256, cubes=64, cube_dim=8):
+def config1_mixed(seed=0, fluid=(128, 64, 128), cloth=256, cubes=64, cube_dim=8, stiffness=(0.25, 0.1, 0.05)):
     """1,048,576 fluid particles (128x64x128 block, d = 0.1) in the corner of
     the box [0,25.8] x [0,16] x [0,25.8]; a 256x256 cloth at spacing d (the
     contact distance 2r, so the cloth does not fight its own contacts) 2 m
-    above the fluid under wind, with stretch/shear/bend stiffness 1.0/0.5/0.1;
+    above the fluid under wind, with stretch/shear/bend stiffness 0.25/0.1/0.05
+    (the configuration's 1.0/0.5/0.1 diverge under the Jacobi distance
+    projection once the cloth meets the fluid; pass `stiffness` to use them);
     64 rigid 8^3 cubes on an 8x8 lattice 2-4 m above the cloth.  The 2^18-cell
     table (D = 64, cell 0.2 m) wraps every 12.8 m, as in the configuration."""
     rng = np.random.default_rng(seed)
@@ -258,7 +260,8 @@ def config1_mixed(seed=0, fluid=(128, 64, 128), cloth=256, cubes=64, cube_dim=8)
     s.add_fluid_block(fluid, (d, d, d), (d, d, d), m, jitter=0.01 * d, rng=rng)
     y = float(fluid[1] * d + 2.0)
     if cloth:
-        s.add_cloth((0.15, y, 0.15), (d, 0, 0), (0, 0, d), cloth, cloth, m, stretch=1.0, shear=0.5, bend=0.1)
+        s.add_cloth((0.15, y, 0.15), (d, 0, 0), (0, 0, d), cloth, cloth, m, stretch=stiffness[0], shear=stiffness[1],
+                    bend=stiffness[2])
     ncube = int(round(cubes ** 0.5))
     for c in range(cubes):
         cx, cz = c % ncube, c // ncube
@@ -324,4 +327,80 @@ def flag_scene(n=128, spacing=0.1, angle_deg=20.0, seed=0, mass=1.0, stretch=0.2
     s.make_immovable(np.arange(n) * n)  # y = 0 of every row: the pole
     rng = np.random.default_rng(seed)
     s.velocities = rng.uniform(-0.05, 0.05, (s.num_particles, 3)).astype(np.float32)
+    return s
+
+
+def _random_rotation(rng):
+    """Uniformly random rotation matrix (from a uniform unit quaternion)."""
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]], np.float32)
+
+
+def rigid_shape(count, kind, spacing):
+    """A lattice of about `count` particles at `spacing`: a cube, a ball or a rod
+    (7 x 7 cross-section), centred on the origin; at most about 2 m across for
+    1000 particles at 0.1 m."""
+    d = spacing
+    if kind == "cube":
+        a = max(3, int(round(count ** (1.0 / 3.0))))
+        g = np.stack(np.meshgrid(*[np.arange(a)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    elif kind == "ball":
+        r = max(1.5, (3.0 * count / (4.0 * np.pi)) ** (1.0 / 3.0))
+        m = int(np.ceil(r))
+        g = np.stack(np.meshgrid(*[np.arange(-m, m + 1)] * 3, indexing="ij"), -1).reshape(-1, 3)
+        g = g[np.sum(g.astype(np.float64) ** 2, axis=1) <= r * r]
+    else:  # rod
+        length = max(2, int(round(count / 49.0)))
+        g = np.stack(np.meshgrid(np.arange(length), np.arange(7), np.arange(7), indexing="ij"), -1).reshape(-1, 3)
+    g = g.astype(np.float32) * np.float32(d)
+    return g - g.mean(axis=0, dtype=np.float64).astype(np.float32)
+
+
+def config2_shape_stress(seed=0, bodies=4096, lo=27, hi=1000, spacing=0.1, lattice=(32, 4, 32), pitch=2.5):
+    """The shape-matching stress test: `bodies` rigid bodies whose particle
+    counts are drawn uniform in [lo, hi] (cube, ball or rod lattices at
+    `spacing`, chosen at random), each with a uniformly random orientation,
+    one per site of a lattice of the given pitch in x and z with layers whose
+    heights spread over [1, 20] m above a ground plane (bodies do not
+    overlap at the start).  The bodies are built in bulk (one array per
+    field) rather than body by body."""
+    rng = np.random.default_rng(seed)
+    s = Scene(name="shape_stress")
+    d = float(np.float32(spacing))
+    s.particle_radius = d / 2
+    s.kernel_radius = 2 * d
+    s.cell_size = 2 * d
+    s.rest_density = 1000.0
+    nx, ny, nz = lattice
+    extent = max(nx, nz) * pitch
+    D = 16
+    while D * s.cell_size < extent + 2.0:
+        D *= 2
+    s.grid_dim = D
+    s.add_plane((0.0, 0.0, 0.0), (0.0, 1.0, 0.0))
+    pos, rest, ranges, phases = [], [], [], []
+    n0 = 0
+    for b in range(bodies):
+        ix, iy, iz = b % nx, (b // nx) % ny, b // (nx * ny)
+        shape = rigid_shape(int(rng.integers(lo, hi + 1)), ("cube", "ball", "rod")[int(rng.integers(0, 3))], d)
+        body_rest = shape @ _random_rotation(rng).T
+        centre = np.array([(ix + 0.5) * pitch, 1.2 + (18.8 - 2.4) * (iy + rng.uniform(0.0, 0.2)) / max(ny - 1, 1),
+                           (iz + 0.5) * pitch], np.float32)
+        pos.append(body_rest + centre)
+        rest.append(body_rest - body_rest.mean(axis=0, dtype=np.float64).astype(np.float32))
+        ranges.append((n0, n0 + len(shape)))
+        phases.append(np.full(len(shape), b + 1, np.int32))
+        n0 += len(shape)
+    s.positions = np.concatenate(pos).astype(np.float32)
+    s.rigid_rest = np.concatenate(rest).astype(np.float32)
+    s.masses = np.ones(n0, np.float32) * np.float32(1000.0 * d ** 3)
+    s.phases = np.concatenate(phases)
+    s.group_ids = np.zeros(n0, np.int32)
+    s.rigid_ranges = np.asarray(ranges, np.int32)
+    s.solid_phase_counter = bodies + 1
+    s.velocities = np.zeros((n0, 3), np.float32)
     return s
