@@ -58,6 +58,109 @@ void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const f
     L->done(__func__);
 }
 
+// ---- the solids of the cell-sorted order, compacted ----
+// solid_prefix[i] = number of solids among sorted indices [0, i), for
+// i in [0, n]; solid_list holds their sorted indices in order.  A column run
+// [b, e) of the grid then holds the solids solid_list[prefix[b] .. prefix[e]).
+
+constexpr int kScanBlock = 1024;
+
+__global__ void __launch_bounds__(kScanBlock) k_solid_count(int n, const float4 *__restrict__ P, int *__restrict__ totals)
+{
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const bool solid = i < n && phase_of(P[i]) > 0;
+    const int c = __syncthreads_count(solid);
+    if (threadIdx.x == 0) totals[blockIdx.x] = c;
+}
+
+// Exclusive scan of the block totals in one CTA (fixed order: deterministic).
+__global__ void __launch_bounds__(kScanBlock) k_solid_scan_totals(int nb, int *__restrict__ totals, int *__restrict__ prefix, int n)
+{
+    __shared__ int part[kScanBlock];
+    const int per = (nb + kScanBlock - 1) / kScanBlock;
+    const int b0 = threadIdx.x * per, b1 = min(b0 + per, nb);
+    int sum = 0;
+    for (int b = b0; b < b1; ++b) sum += totals[b];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int o = 1; o < kScanBlock; o <<= 1) {  // inclusive Hillis-Steele scan
+        const int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int run = part[threadIdx.x] - sum;
+    for (int b = b0; b < b1; ++b) {
+        const int t = totals[b];
+        totals[b] = run;
+        run += t;
+    }
+    if (threadIdx.x == kScanBlock - 1) prefix[n] = part[kScanBlock - 1];
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_solid_scatter(int n, const float4 *__restrict__ P,
+                                                              const int *__restrict__ block_base,
+                                                              int *__restrict__ prefix, int *__restrict__ list)
+{
+    __shared__ int warp_sum[kScanBlock / 32];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const bool solid = i < n && phase_of(P[i]) > 0;
+    const unsigned ballot = __ballot_sync(0xffffffffu, solid);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_sum[warp] = __popc(ballot);
+    __syncthreads();
+    int before = 0;
+    for (int w = 0; w < warp; ++w) before += warp_sum[w];
+    const int pos = block_base[blockIdx.x] + before + __popc(ballot & ((1u << lane) - 1u));
+    if (i < n) {
+        prefix[i] = pos;
+        if (solid) list[pos] = i;
+    }
+}
+
+void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int *prefix, int *list, LaunchLog *L)
+{
+    if (n <= 0) return;
+    const int nb = (n + kScanBlock - 1) / kScanBlock;
+    k_solid_count<<<nb, kScanBlock, 0, st>>>(n, P, totals);
+    L->done("k_solid_count");
+    k_solid_scan_totals<<<1, kScanBlock, 0, st>>>(nb, totals, prefix, n);
+    L->done("k_solid_scan_totals");
+    k_solid_scatter<<<nb, kScanBlock, 0, st>>>(n, P, totals, prefix, list);
+    L->done("k_solid_scatter");
+}
+
+// The solids among the candidates of particle i's 27 cells, in walk order:
+// body(j, P[j]) for every solid j with test(j, P[j]).
+template <class T, class B>
+__device__ __forceinline__ void walk_solids(float3 pi, const float4 *__restrict__ P, const GridView &v,
+                                            const SimConsts &C, const int *__restrict__ prefix,
+                                            const int *__restrict__ list, T &&test, B &&body)
+{
+    const int3 c = cell_of(pi, C);
+    const unsigned m = v.mask, D = (unsigned)v.D;
+    const unsigned z0 = (unsigned)(c.z - 1) & m, z2 = (unsigned)(c.z + 1) & m;
+    const bool wrap = !(z0 < z2);
+#pragma unroll 1
+    for (int col = 0; col < 9; ++col) {
+        const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
+        const unsigned base = x * D * D + y * D;
+#pragma unroll 1
+        for (int piece = 0; piece < (wrap ? 2 : 1); ++piece) {
+            const unsigned za = (wrap && piece == 1) ? 0u : z0;
+            const unsigned zb = wrap ? (piece == 0 ? D - 1 : z2) : z2;
+            const int b = __ldg(v.off + base + za), e = __ldg(v.off + base + zb + 1);
+            const int kb = __ldg(prefix + b), ke = __ldg(prefix + e);
+#pragma unroll 1
+            for (int k = kb; k < ke; ++k) {
+                const int j = __ldg(list + k);
+                const float4 pj = P[j];
+                if (test(j, pj)) body(j, pj);
+            }
+        }
+    }
+}
+
 // Solid contacts: pairs of different phase with at least one solid, closer
 // than two radii; mass-weighted projection plus friction averaged over the
 // counted contacts; only particle i moves (the reference's j update is
@@ -68,6 +171,8 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS) k_particle_c
                                                                      const float *__restrict__ w,
                                                                      const int *__restrict__ off,
                                                                      const int *__restrict__ tile_solid,
+                                                                     const int *__restrict__ solid_prefix,
+                                                                     const int *__restrict__ solid_list,
                                                                      float4 *__restrict__ Pout)
 {
     __shared__ StageShared S;
@@ -99,14 +204,12 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS) k_particle_c
     const float wi = w[i];
     float3 sd = make_float3(0.f, 0.f, 0.f), sf = make_float3(0.f, 0.f, 0.f);
     int count = 0;
-    walk_neighbors<Split>(
-        i, xip, 0, P, v, C, &S, g,
-        [&](int j, float4 pj4) {
-            const int phj = phase_of(pj4);
-            const float d2 = len2(xip - f3(pj4));
-            return j != i && phi != phj && (phi > 0 || phj > 0) && d2 < r * r * 4.0f && d2 > 1e-5f;
-        },
-        [&](int j, float4 pj4) {
+    auto test = [&](int j, float4 pj4) {
+        const int phj = phase_of(pj4);
+        const float d2 = len2(xip - f3(pj4));
+        return j != i && phi != phj && (phi > 0 || phj > 0) && d2 < r * r * 4.0f && d2 > 1e-5f;
+    };
+    auto body = [&](int j, float4 pj4) {
             const float3 xjp = f3(pj4);
             const float3 diff = xip - xjp;
             const float d2 = len2(diff);
@@ -133,7 +236,11 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS) k_particle_c
                 else
                     sf -= (w1 * tdx) * fminf(__fmul_rn(C.fd, __fsqrt_rn(__fdiv_rn(dxi2, tl2))), 1.0f);
             }
-        });
+    };
+    // A fluid particle only meets solids: it walks the solids of its 27 cells
+    // (same candidates in the same order, the others contribute nothing).
+    if (phi < 0 && solid_prefix) walk_solids(xip, P, v, C, solid_prefix, solid_list, test, body);
+    else walk_neighbors<Split>(i, xip, 0, P, v, C, &S, g, test, body);
     const float3 d = (count == 0) ? sd : sd + sf / (float)count;
     const float3 p = xip + d;
     Pout[i] = make_float4(p.x, p.y, p.z, pi4.w);
@@ -141,14 +248,17 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS) k_particle_c
 }
 
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
-                               const float *w, const int *off, const int *tile_solid, float4 *Pout, LaunchLog *L)
+                               const float *w, const int *off, const int *tile_solid, const int *solid_prefix,
+                               const int *solid_list, float4 *Pout, LaunchLog *L)
 {
     if (C.n <= 0) return;
     const int grid = (C.n + kWalkThreads - 1) / kWalkThreads;
     if (C.split)
-        k_particle_collision<true><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, tile_solid, Pout);
+        k_particle_collision<true><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
+                                                                 solid_list, Pout);
     else
-        k_particle_collision<false><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, tile_solid, Pout);
+        k_particle_collision<false><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
+                                                                  solid_list, Pout);
     L->done(__func__);
 }
 

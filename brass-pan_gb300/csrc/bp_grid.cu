@@ -329,18 +329,26 @@ __global__ void k_reset_start_end(int n, const int *__restrict__ sorted, int *__
 }
 
 // Dense prefix: off[c] = number of particles whose key is below c, for
-// c in [0, ncells]; lower bound by binary search in the sorted keys.
-__global__ void k_cell_offsets(int n, int ncells, const int *__restrict__ sorted, int *__restrict__ off)
+// c in [0, ncells].  Each thread takes `per` consecutive cells: one binary
+// search for the first, then a forward scan over the keys of its cells.
+// Tables with many more cells than particles (mostly empty cells) take 8
+// cells per thread, so they cost one search per 8 cells; dense tables take
+// one, so no thread walks a long run of keys.
+__global__ void k_cell_offsets(int n, int ncells, int per, const int *__restrict__ sorted, int *__restrict__ off)
 {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c > ncells) return;
+    const long long c0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * per;
+    if (c0 > ncells) return;
     int lo = 0, hi = n;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (__ldg(sorted + mid) < c) lo = mid + 1;
+        if (__ldg(sorted + mid) < c0) lo = mid + 1;
         else hi = mid;
     }
-    off[c] = lo;
+    const long long c1 = min(c0 + per, (long long)ncells + 1);
+    for (long long c = c0; c < c1; ++c) {
+        while (lo < n && __ldg(sorted + lo) < c) ++lo;
+        off[c] = lo;
+    }
 }
 
 void launch_find_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end, LaunchLog *L)
@@ -359,7 +367,9 @@ void launch_reset_start_end(cudaStream_t st, int n, const int *sorted, int *star
 
 void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, LaunchLog *L)
 {
-    k_cell_offsets<<<(ncells + 1 + 255) / 256, 256, 0, st>>>(n, ncells, sorted, off);
+    const int per = ncells > 4LL * n ? 8 : 1;
+    const long long threads = ((long long)ncells + 1 + per - 1) / per;
+    k_cell_offsets<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(n, ncells, per, sorted, off);
     L->done(__func__);
 }
 

@@ -27,6 +27,15 @@ bp_status fail(bp_status st, const std::string &msg)
     return st;
 }
 
+// Inside create_solver: a failure frees the half-built solver first.
+#define BP_CUDA_BAIL(call)                                                                     \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return bail(fail(e_ == cudaErrorMemoryAllocation ? BP_ERR_OUT_OF_MEMORY : BP_ERR_CUDA, \
+                             std::string(#call) + ": " + cudaGetErrorString(e_)));             \
+    } while (0)
+
 #define BP_CUDA(call)                                                                          \
     do {                                                                                       \
         cudaError_t e_ = (call);                                                               \
@@ -321,27 +330,29 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         if (sc->group_ids) grp[i] = sc->group_ids[i];
     }
     s->has_solid = has_solid;
-    if ((st = s->alloc(&s->tile_solid, (N + 255) / 256)) || (st = s->alloc(&s->nbr, N * kPostListCap)) ||
+    if ((st = s->alloc(&s->tile_solid, (N + 255) / 256)) || (st = s->alloc(&s->solid_prefix, N + 1)) ||
+        (st = s->alloc(&s->solid_list, N)) || (st = s->alloc(&s->solid_totals, (N + 1023) / 1024)) ||
+        (st = s->alloc(&s->nbr, N * kPostListCap)) ||
         (st = s->alloc(&s->nbr_count, N)))
         return bail(st);
     if (n > 0) {
-        BP_CUDA(cudaMemcpy(s->Xc, X.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
-        BP_CUDA(cudaMemcpy(s->Vc, V.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
-        BP_CUDA(cudaMemcpy(s->Pa, P.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
-        BP_CUDA(cudaMemcpy(s->orig_c, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-        BP_CUDA(cudaMemcpy(s->to_new, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-        BP_CUDA(cudaMemcpy(s->group, grp.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+        BP_CUDA_BAIL(cudaMemcpy(s->Xc, X.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        BP_CUDA_BAIL(cudaMemcpy(s->Vc, V.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        BP_CUDA_BAIL(cudaMemcpy(s->Pa, P.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        BP_CUDA_BAIL(cudaMemcpy(s->orig_c, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+        BP_CUDA_BAIL(cudaMemcpy(s->to_new, ids.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+        BP_CUDA_BAIL(cudaMemcpy(s->group, grp.data(), n * sizeof(int), cudaMemcpyHostToDevice));
         std::vector<float> m(sc->masses, sc->masses + n);
-        BP_CUDA(cudaMemcpy(s->mass, m.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        BP_CUDA_BAIL(cudaMemcpy(s->mass, m.data(), n * sizeof(float), cudaMemcpyHostToDevice));
     }
     s->Pcur = s->Pa;
-    BP_CUDA(cudaMemset(s->lam, 0, N * sizeof(float)));
-    BP_CUDA(cudaMemset(s->rho, 0, N * sizeof(float)));
-    BP_CUDA(cudaMemset(s->Om, 0, N * sizeof(float4)));
-    BP_CUDA(cudaMemset(s->Nm, 0, N * sizeof(float4)));
-    BP_CUDA(cudaMemset(s->off, 0, (ncells + 1) * sizeof(int)));
-    BP_CUDA(cudaMemset(s->sorted_keys, 0, N * sizeof(int)));
-    BP_CUDA(cudaMemset(s->err, 0, sizeof(unsigned)));
+    BP_CUDA_BAIL(cudaMemset(s->lam, 0, N * sizeof(float)));
+    BP_CUDA_BAIL(cudaMemset(s->rho, 0, N * sizeof(float)));
+    BP_CUDA_BAIL(cudaMemset(s->Om, 0, N * sizeof(float4)));
+    BP_CUDA_BAIL(cudaMemset(s->Nm, 0, N * sizeof(float4)));
+    BP_CUDA_BAIL(cudaMemset(s->off, 0, (ncells + 1) * sizeof(int)));
+    BP_CUDA_BAIL(cudaMemset(s->sorted_keys, 0, N * sizeof(int)));
+    BP_CUDA_BAIL(cudaMemset(s->err, 0, sizeof(unsigned)));
 
     // distance constraints
     if (sc->num_distance_constraints > 0) {
@@ -416,7 +427,7 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         s->scene_first = batch->first;
         s->nplanes = batch->max_planes;  // each scene's own planes are in its table entry
     }
-    BP_CUDA(cudaDeviceSynchronize());
+    BP_CUDA_BAIL(cudaDeviceSynchronize());
     *out = s;
     return BP_OK;
 }
@@ -623,6 +634,8 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     if (tape) tape->vs_slot = tape->snap4(s->Vs);
 
     float4 *cur = s->Pa, *other = s->Pb;
+    // the sorted order is fixed for the substep: compact its solids once
+    if (pcoll) launch_solid_list(st, s->n, cur, s->solid_totals, s->solid_prefix, s->solid_list, L);
     if (wind) {
         if (tape) tape->push(TS_WIND, cur);
         launch_wind(st, C, s->wind, cur, s->Vs, s->mass, s->to_new, L);
@@ -651,7 +664,8 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         }
         if (pcoll) {
             if (tape) tape->push(TS_PCOLL, cur);
-            launch_particle_collision(st, C, cur, s->Xs, s->w, s->off, s->tile_solid, other, L);
+            launch_particle_collision(st, C, cur, s->Xs, s->w, s->off, s->tile_solid, s->solid_prefix, s->solid_list,
+                                      other, L);
             std::swap(cur, other);
         }
         if (fluid) {

@@ -102,6 +102,7 @@ struct bp_solver {
     unsigned *nl_stats = nullptr;
     unsigned *err = nullptr;
     int *tile_solid = nullptr;  // per 256 sorted particles: the tile holds a solid
+    int *solid_prefix = nullptr, *solid_list = nullptr, *solid_totals = nullptr;  // compacted solids
     int *nbr = nullptr, *nbr_count = nullptr;  // post-pass neighbour lists [kPostListCap][N], counts
     SortScratch sort{};
 
