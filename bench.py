@@ -292,6 +292,9 @@ def run_ours(args):
         n = solver.n
     else:
         scene = build_scene(bp, args.workload, seed=rank)
+        if args.load_state:  # continue a saved run (positions, velocities in original order)
+            z = np.load(args.load_state)
+            scene.positions, scene.velocities = z["x"].astype(np.float32), z["v"].astype(np.float32)
         n = scene.num_particles
         params = tuned(workload_params(bp, args.workload, scene))
         solver = bp.ParticleSolver(scene, params, stream=stream.cuda_stream)
@@ -317,6 +320,8 @@ def run_ours(args):
         if world > 1:
             torch.distributed.barrier()
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    if args.save_state and rank == 0:
+        np.savez(args.save_state, x=solver.positions(), v=solver.velocities())
     t = torch.tensor([ms], dtype=torch.float64, device="cuda")
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -528,6 +533,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint measurement")
+    ap.add_argument("--save-state", default=None, help="after the timed steps, save the state (npz) here")
+    ap.add_argument("--load-state", default=None, help="start from a state saved by --save-state")
     ap.add_argument("--skin", type=float, default=None, help="neighbour-mask skin (fraction of h); 0 disables")
     ap.add_argument("--no-stage", action="store_true", help="read neighbours from global memory only")
     ap.add_argument("--no-split", action="store_true", help="evaluate pair terms as candidates are tested")

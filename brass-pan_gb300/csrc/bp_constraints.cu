@@ -164,36 +164,24 @@ __device__ __forceinline__ void walk_solids(float3 pi, const float4 *__restrict_
 // Solid contacts: pairs of different phase with at least one solid, closer
 // than two radii; mass-weighted projection plus friction averaged over the
 // counted contacts; only particle i moves (the reference's j update is
-// commented out).  Reads P, writes Pout = P + delta.
+// commented out).  Reads P, writes Pout = P + delta.  A fluid particle only
+// meets solids, so it walks the compacted solids of its 27 cells (same
+// candidates in the same order; the others contribute nothing).
 template <bool Split>
-__global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS) k_particle_collision(SimConsts C, const float4 *__restrict__ P,
-                                                                     const float4 *__restrict__ Xs,
-                                                                     const float *__restrict__ w,
-                                                                     const int *__restrict__ off,
-                                                                     const int *__restrict__ tile_solid,
-                                                                     const int *__restrict__ solid_prefix,
-                                                                     const int *__restrict__ solid_list,
-                                                                     float4 *__restrict__ Pout)
+__device__ __forceinline__ void collide_one(const SimConsts &C, int i, const float4 *__restrict__ P,
+                                            const float4 *__restrict__ Xs, const float *__restrict__ w,
+                                            const GridView &v, const StageShared *S, int g,
+                                            const int *__restrict__ solid_prefix, const int *__restrict__ solid_list,
+                                            float4 *__restrict__ Pout)
 {
-    __shared__ StageShared S;
-    const int i0 = blockIdx.x * kWalkThreads;
-    const int g = stage_block(C, P, off, i0, S, tile_solid);
-    const int i = i0 + threadIdx.x;
-    if (i >= C.n) return;
     const float4 pi4 = P[i];
     const float3 xip = f3(pi4);
     const int phi = phase_of(pi4);
     const float r = C.radius;
-    const GridView v = grid_view(C, scene_index(C, i), off);
-    // A fluid particle only meets solids.  If it walks its CTA's runs (it is
-    // in its stored cell) and they hold no solid, the walk would find nothing.
-    const int3 ci = cell_of(xip, C);
-    const bool in_cell = cell_addr(ci.x, ci.y, ci.z, v.D, v.mask) + v.base == __ldg(C.cell_keys + i);
-    bool none = phi < 0 && in_cell && (g == kNoSolidNear || (g >= 0 && !S.has_solid));
     // No contact partner within 2r + skin at mask build and the masks still
     // valid: no pair can be closer than 2r now, the walk would find nothing.
-    none = none || (C.nl_mask && C.nl_flags && !(C.nl_flags[i] & kFlagContact) &&
-                    masks_usable(C, i, cell_of(xip, C), xip) && !contact_outlier_near(C, xip));
+    const bool none = C.nl_mask && C.nl_flags && !(C.nl_flags[i] & kFlagContact) &&
+                      masks_usable(C, i, cell_of(xip, C), xip) && !contact_outlier_near(C, xip);
     if (none) {  // p = x + 0, rounded as the walk's result would be
         const float3 p = xip + make_float3(0.f, 0.f, 0.f);
         Pout[i] = make_float4(p.x, p.y, p.z, pi4.w);
@@ -237,29 +225,86 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS) k_particle_c
                     sf -= (w1 * tdx) * fminf(__fmul_rn(C.fd, __fsqrt_rn(__fdiv_rn(dxi2, tl2))), 1.0f);
             }
     };
-    // A fluid particle only meets solids: it walks the solids of its 27 cells
-    // (same candidates in the same order, the others contribute nothing).
     if (phi < 0 && solid_prefix) walk_solids(xip, P, v, C, solid_prefix, solid_list, test, body);
-    else walk_neighbors<Split>(i, xip, 0, P, v, C, &S, g, test, body);
+    else walk_neighbors<Split>(i, xip, 0, P, v, C, S, g, test, body);
     const float3 d = (count == 0) ? sd : sd + sf / (float)count;
     const float3 p = xip + d;
     Pout[i] = make_float4(p.x, p.y, p.z, pi4.w);
     track_displacement(C, i, p, true);
 }
 
+// Fluid particles (and, without a solid list, everything), one CTA per 256
+// sorted particles.  A CTA of fluid whose runs touch no tile holding a solid
+// skips the walks: none of its particles that stayed in their stored cell
+// can meet a solid.
+template <bool Split>
+__global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS)
+    k_particle_collision(SimConsts C, const float4 *__restrict__ P, const float4 *__restrict__ Xs,
+                         const float *__restrict__ w, const int *__restrict__ off, const int *__restrict__ tile_solid,
+                         const int *__restrict__ solid_prefix, const int *__restrict__ solid_list,
+                         int solids_apart, float4 *__restrict__ Pout)
+{
+    __shared__ StageShared S;
+    const int i0 = blockIdx.x * kWalkThreads;
+    // With the solids apart, fluid threads walk the solid list, not the
+    // staged runs: only the runs' solid check is needed.
+    const int g = stage_block(C, P, off, i0, S, tile_solid, !solids_apart);
+    const int i = i0 + threadIdx.x;
+    if (i >= C.n) return;
+    const float4 pi4 = P[i];
+    const int phi = phase_of(pi4);
+    if (phi > 0 && solids_apart) return;  // k_particle_collision_solids
+    const GridView v = grid_view(C, scene_index(C, i), off);
+    const float3 xip = f3(pi4);
+    const int3 ci = cell_of(xip, C);
+    const bool in_cell = cell_addr(ci.x, ci.y, ci.z, v.D, v.mask) + v.base == __ldg(C.cell_keys + i);
+    if (phi < 0 && in_cell && (g == kNoSolidNear || (g >= 0 && !S.has_solid))) {
+        const float3 p = xip + make_float3(0.f, 0.f, 0.f);
+        Pout[i] = make_float4(p.x, p.y, p.z, pi4.w);
+        track_displacement(C, i, p, true);
+        return;
+    }
+    collide_one<Split>(C, i, P, Xs, w, v, &S, g, solid_prefix, solid_list, Pout);
+}
+
+// The solid particles, one thread each through the compacted list, so the
+// long walks of solids scattered through fluid run in full warps.
+template <bool Split>
+__global__ void __launch_bounds__(kWalkThreads)
+    k_particle_collision_solids(SimConsts C, int nsolid, const float4 *__restrict__ P,
+                                const float4 *__restrict__ Xs, const float *__restrict__ w,
+                                const int *__restrict__ off, const int *__restrict__ solid_list,
+                                float4 *__restrict__ Pout)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nsolid) return;
+    const int i = __ldg(solid_list + t);
+    collide_one<Split>(C, i, P, Xs, w, grid_view(C, scene_index(C, i), off), nullptr, -1, nullptr, nullptr, Pout);
+}
+
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
                                const float *w, const int *off, const int *tile_solid, const int *solid_prefix,
-                               const int *solid_list, float4 *Pout, LaunchLog *L)
+                               const int *solid_list, int nsolid, bool solids_apart, float4 *Pout, LaunchLog *L)
 {
     if (C.n <= 0) return;
     const int grid = (C.n + kWalkThreads - 1) / kWalkThreads;
+    const int apart = (solids_apart && solid_list && nsolid > 0) ? 1 : 0;
     if (C.split)
         k_particle_collision<true><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
-                                                                 solid_list, Pout);
+                                                                 solid_list, apart, Pout);
     else
         k_particle_collision<false><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
-                                                                  solid_list, Pout);
+                                                                  solid_list, apart, Pout);
     L->done(__func__);
+    if (apart) {
+        const int sg = (nsolid + kWalkThreads - 1) / kWalkThreads;
+        if (C.split)
+            k_particle_collision_solids<true><<<sg, kWalkThreads, 0, st>>>(C, nsolid, P, Xs, w, off, solid_list, Pout);
+        else
+            k_particle_collision_solids<false><<<sg, kWalkThreads, 0, st>>>(C, nsolid, P, Xs, w, off, solid_list,
+                                                                           Pout);
+        L->done("launch_particle_collision_solids");
+    }
 }
 
 // ---- distance constraints ----

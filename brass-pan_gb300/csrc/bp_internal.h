@@ -117,9 +117,10 @@ void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const f
                    const int *orig_s, float4 *Xc, float4 *Vc, int *orig_c, LaunchLog *L);
 // tile_solid: nullptr, or one flag per 256 sorted particles (the tile holds a solid);
 // solid_prefix / solid_list: nullptr, or the compacted solids (launch_solid_list)
+// solids_apart: the nsolid solids of the list walk in a second launch over the list.
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
                                const float *w, const int *off, const int *tile_solid, const int *solid_prefix,
-                               const int *solid_list, float4 *Pout, LaunchLog *L);
+                               const int *solid_list, int nsolid, bool solids_apart, float4 *Pout, LaunchLog *L);
 // solid_prefix[i] (i <= n): solids among sorted [0, i); solid_list: their sorted indices in order.
 // totals: (n + 1023) / 1024 ints of scratch.
 void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int *solid_prefix, int *solid_list,

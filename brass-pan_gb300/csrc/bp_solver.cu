@@ -330,6 +330,8 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         if (sc->group_ids) grp[i] = sc->group_ids[i];
     }
     s->has_solid = has_solid;
+    s->num_solids = 0;
+    for (int i = 0; i < n; ++i) s->num_solids += sc->phases[i] > 0;
     if ((st = s->alloc(&s->tile_solid, (N + 255) / 256)) || (st = s->alloc(&s->solid_prefix, N + 1)) ||
         (st = s->alloc(&s->solid_list, N)) || (st = s->alloc(&s->solid_totals, (N + 1023) / 1024)) ||
         (st = s->alloc(&s->nbr, N * kPostListCap)) ||
@@ -664,8 +666,11 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         }
         if (pcoll) {
             if (tape) tape->push(TS_PCOLL, cur);
+            // solids walk in a launch of their own, in full warps (measured
+            // faster than walking them in the staged CTAs, whether solids are
+            // scattered through fluid or the whole scene)
             launch_particle_collision(st, C, cur, s->Xs, s->w, s->off, s->tile_solid, s->solid_prefix, s->solid_list,
-                                      other, L);
+                                      s->num_solids, true, other, L);
             std::swap(cur, other);
         }
         if (fluid) {

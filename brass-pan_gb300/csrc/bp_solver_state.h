@@ -114,6 +114,7 @@ struct bp_solver {
     SortScratch sort{};
 
     bool has_solid = false;
+    int num_solids = 0;
     size_t ncells = 0;   // cells of the key space (D^3 for one scene)
     int sort_dim = 0;    // a grid dimension whose key width covers every key (sort passes)
     // batched ensembles (num_scenes == 0: one scene)

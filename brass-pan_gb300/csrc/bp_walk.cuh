@@ -65,9 +65,12 @@ constexpr int kNoSolidNear = -2;
 // solid), a CTA of fluid particles whose runs touch no solid tile skips the
 // staging and returns kNoSolidNear to every thread: none of its particles
 // that stayed in their stored cell can meet a solid.
+//
+// With copy == false only the runs and the solid check are made: the CTA
+// walks nothing from shared memory (the returned group is -1 or kNoSolidNear).
 __device__ __forceinline__ int stage_block(const SimConsts &C, const float4 *__restrict__ P,
                                            const int *__restrict__ off_all, int i0, StageShared &S,
-                                           const int *__restrict__ tile_solid = nullptr)
+                                           const int *__restrict__ tile_solid = nullptr, bool copy = true)
 {
     if (!C.stage) return -1;  // uniform across the grid: no barrier skipped unevenly
     const int t = threadIdx.x;
@@ -139,7 +142,7 @@ __device__ __forceinline__ int stage_block(const SimConsts &C, const float4 *__r
         S.ngroups = G;
     }
     __syncthreads();
-    if (!S.ok) return -1;
+    if (!S.ok || !copy) return -1;
     bool solid = false;
     for (int s = 0; s < 2 * G * 9; ++s) {
         const int gs = S.gstart[s], l = S.len[s], sb = S.sbase[s];
