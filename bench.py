@@ -243,20 +243,24 @@ def dist_info():
     return rank, world, local
 
 
-def traffic_for(kernel: str, n: int):
-    """DRAM bytes per launch of `kernel` from its committed ncu summary
-    (profiles/k_<name>_fluid_1048576.md, a 1,048,576-particle launch), scaled
-    to n particles: the traffic grows with the particle count."""
+def traffic_for(kernel: str, n: int, workload: str):
+    """DRAM bytes per launch of `kernel` from its committed ncu summary, scaled
+    to n particles (the traffic grows with the particle count): the late-frame
+    capture of the workload where there is one (the top kernel is profiled at
+    the end of the timed run), else the 1,048,576-particle fluid capture."""
     import re
 
     name = kernel.replace("launch_", "k_")
-    p = REPO / "profiles" / f"{name}_fluid_1048576.md"
-    if not p.exists():
-        return None
-    m = re.search(r"DRAM traffic of the launch: ([0-9.]+) MB", p.read_text())
-    if not m:
-        return None
-    return float(m.group(1)) * 1e6 * n / 1048576.0
+    for fname in (f"{name}_{workload}_late.md", f"{name}_fluid_1048576.md"):
+        p = REPO / "profiles" / fname
+        if not p.exists():
+            continue
+        text = p.read_text()
+        t = re.search(r"DRAM traffic of the launch: ([0-9.]+) MB", text)
+        parts = re.search(r"Particles: ([0-9]+)", text)
+        if t and parts:
+            return float(t.group(1)) * 1e6 * n / float(parts.group(1))
+    return None
 
 
 def run_ours(args):
@@ -368,7 +372,7 @@ def run_ours(args):
     peak, peak_kind = load_peaks()
     bytes_per = KERNEL_BYTES.get(top_name)
     achieved = (bytes_per * n / (avg_ms / 1e3) / 1e9) if bytes_per else None
-    traffic = traffic_for(top_name, n)
+    traffic = traffic_for(top_name, n, args.workload)
     step_ms_total = sum(v[1] for v in agg.values()) / prof_steps
     walks = solver.walk_stats(SUBSTEPS, DT, ITERATIONS)
     device_errors = solver.device_errors()  # non-finite state anywhere in the run
