@@ -6,7 +6,8 @@
   checkout was present at build time, reference parameters only.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this
-module, as the checker or the timed CPU baseline.
+module: as the oracle the GPU results are compared with, or as the timed CPU
+baseline.
 """
 from __future__ import annotations
 

@@ -3,7 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
  * cpu_baseline / reference arm of bench.py may load this library, and only as
- * the checker (or the timed CPU baseline), never as part of the product path.
+ * the oracle the GPU results are compared with (or as the timed CPU
+ * baseline), never as part of the product path.
  *
  * The state mirrors the reference's ParticleSolver device arrays
  * (brasstower/particlesolver.cuh:1075-1148): float3 arrays permuted into
