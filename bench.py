@@ -307,6 +307,11 @@ def run_ours(args):
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             solver.update(SUBSTEPS, DT, ITERATIONS)
+        tuned_walk = None
+        if not (args.no_autotune or args.no_stage or args.no_split or args.no_lists):
+            # keeps the fastest (bit-identical) walk variant
+            opt, trial_ms = solver.autotune(SUBSTEPS, DT, ITERATIONS)
+            tuned_walk = {"walk_options": opt, "trial_ms": [round(t, 3) for t in trial_ms]}
         stream.synchronize()
         launches_per_step = solver.last_launch_count()
         starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -406,8 +411,8 @@ def run_ours(args):
                        "iterations": ITERATIONS, "dt": DT, "mode": "reference",
                        "grid": ("one grid per scene (16^3..64^3 cells), cell = h = 0.2" if args.workload == "batch"
                                 else f"{params.grid_dim}^3 cells, cell = h = 0.2"),
-                       "neighbor_skin": float(params.neighbor_skin), "staging": not args.no_stage, "split_walks": not args.no_split,
-                       "post_lists": not args.no_lists,
+                       "neighbor_skin": float(params.neighbor_skin), "walk_options": int(solver.params.walk_options),
+                       "autotune": tuned_walk,
                        "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "particle-substeps/s",
                     "h2d_bytes_per_step": int(2 * n * 12), "d2h_bytes_per_step": int(n * 12)},
@@ -543,6 +548,7 @@ def main():
     ap.add_argument("--no-stage", action="store_true", help="read neighbours from global memory only")
     ap.add_argument("--no-split", action="store_true", help="evaluate pair terms as candidates are tested")
     ap.add_argument("--no-lists", action="store_true", help="post passes B and C walk their cells")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the walk options given instead of timing them")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -179,7 +179,7 @@ EXPORTS = [
     "bp_solver_set_state", "bp_solver_field", "bp_solver_copy_field", "bp_solver_pack_particle_infos",
     "bp_solver_device_errors", "bp_solver_last_launch_count", "bp_solver_profile", "bp_solver_walk_stats", "bp_grid_workspace_size", "bp_grid_build",
     "bp_grid_reset", "bp_grid_build_static", "bp_batch_create", "bp_batch_step", "bp_batch_scene_range",
-    "bp_solver_tape_begin", "bp_solver_backward", "bp_solver_tape_end", "bp_grid_neighbor_counts", "bp_last_error_string", "bp_abi_version",
+    "bp_solver_tape_begin", "bp_solver_backward", "bp_solver_tape_end", "bp_solver_autotune", "bp_grid_neighbor_counts", "bp_last_error_string", "bp_abi_version",
 ]
 
 
@@ -220,6 +220,7 @@ def load(path: Path | None = None):
         "bp_grid_build_static": (i32, [vp, i32, vp, f32, i32, vp, vp, vp, vp, vp]),
         "bp_batch_create": (i32, [i32, vp, vp, vp, vp]),
         "bp_solver_tape_begin": (i32, [vp, i32]),
+        "bp_solver_autotune": (i32, [vp, i32, f32, i32, vp, vp]),
         "bp_solver_backward": (i32, [vp, vp, vp, vp]),
         "bp_solver_tape_end": (i32, [vp]),
         "bp_batch_step": (i32, [vp, f32, i32, i32]),

@@ -20,7 +20,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libbrasspan.so"
 
 SOURCES = ["bp_grid.cu", "bp_fluid.cu", "bp_constraints.cu", "bp_solver.cu", "bp_grid_static.cu", "bp_adjoint.cu",
-           "bp_backward.cu"]
+           "bp_backward.cu", "bp_autotune.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-std=c++17", "-lineinfo", "--extended-lambda", "-Xcompiler", "-fPIC",

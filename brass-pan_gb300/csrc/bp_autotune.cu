@@ -1,0 +1,76 @@
+// bp_autotune.cu -- picks the neighbour-walk variant that runs fastest for a
+// solver's scene and step configuration.
+//
+// The walk variants (staging each CTA's neighbourhood in shared memory,
+// testing candidates in chunks before the pair terms, the post passes'
+// neighbour lists) give bit-identical results, so the choice only affects
+// speed.  Each candidate runs one update from the same state (the first call
+// of a configuration captures its CUDA graph; it is run once untimed), timed
+// with CUDA events on the solver's stream; the state is put back after every
+// trial and the fastest variant is kept in the solver's parameters.
+#include "bp_solver_state.h"
+
+using namespace bp;
+
+extern "C" bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
+                                        int32_t *out_walk_options, float *out_ms)
+{
+    if (!s) return fail_with(BP_ERR_INVALID_ARGUMENT, "solver is NULL");
+    if (num_substeps <= 0 || !(dt > 0.f) || iterations < 0)
+        return fail_with(BP_ERR_INVALID_ARGUMENT, "num_substeps > 0, dt > 0 and iterations >= 0 required");
+    if (s->tape) return fail_with(BP_ERR_INVALID_ARGUMENT, "not available while a tape records");
+    static const int32_t kCandidates[] = {0, BP_WALK_NO_SPLIT, BP_WALK_NO_LISTS, BP_WALK_NO_STAGING,
+                                          BP_WALK_NO_SPLIT | BP_WALK_NO_STAGING};
+    constexpr int kNum = (int)(sizeof(kCandidates) / sizeof(kCandidates[0]));
+    if (s->n <= 0) {
+        if (out_walk_options) *out_walk_options = s->prm.walk_options;
+        return BP_OK;
+    }
+    BP_CUDA_OR_FAIL(cudaStreamSynchronize(s->stream));
+    StateSnapshot snap;
+    bp_status st = snap.take(s);
+    if (st != BP_OK) return st;
+    cudaEvent_t e0, e1;
+    BP_CUDA_OR_FAIL(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail_with(BP_ERR_CUDA, "cudaEventCreate");
+    }
+    const int32_t keep = s->prm.walk_options & ~(BP_WALK_NO_SPLIT | BP_WALK_NO_LISTS | BP_WALK_NO_STAGING);
+    float best = -1.f;
+    int32_t best_opt = s->prm.walk_options;
+    for (int c = 0; c < kNum && st == BP_OK; ++c) {
+        bp_params p = s->prm;
+        p.walk_options = keep | kCandidates[c];
+        if ((st = bp_solver_set_params(s, &p)) != BP_OK) break;
+        // untimed: captures this variant's graph
+        if ((st = bp_solver_update(s, num_substeps, dt, iterations, -1, nullptr, nullptr)) != BP_OK) break;
+        snap.restore(s);
+        cudaEventRecord(e0, s->stream);
+        if ((st = bp_solver_update(s, num_substeps, dt, iterations, -1, nullptr, nullptr)) != BP_OK) break;
+        cudaEventRecord(e1, s->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            st = fail_with(BP_ERR_CUDA, "autotune: event");
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (out_ms) out_ms[c] = ms;
+        if (best < 0.f || ms < best) {
+            best = ms;
+            best_opt = p.walk_options;
+        }
+        snap.restore(s);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    snap.restore(s);
+    bp_params p = s->prm;
+    p.walk_options = best_opt;
+    const bp_status st2 = bp_solver_set_params(s, &p);
+    cudaStreamSynchronize(s->stream);
+    if (st != BP_OK) return st;
+    if (st2 != BP_OK) return st2;
+    if (out_walk_options) *out_walk_options = best_opt;
+    return BP_OK;
+}

@@ -219,43 +219,6 @@ void copy_ctx(bp_solver *s, const SubCtx &c, bool save)
     cp(s->w, c.w, n * sizeof(float));
 }
 
-// Every buffer a caller can observe after an update, saved around backward.
-struct Snapshot {
-    std::vector<std::pair<void *, size_t>> bufs;  // solver buffer, bytes
-    std::vector<void *> copies;
-    float4 *pcur = nullptr;
-    ~Snapshot()
-    {
-        for (void *p : copies) cudaFree(p);
-    }
-    bp_status take(bp_solver *s)
-    {
-        const size_t n = (size_t)s->n, nb = (size_t)s->rigid.num_bodies;
-        bufs = {{s->Xc, n * 16}, {s->Vc, n * 16}, {s->Xs, n * 16}, {s->Vs, n * 16}, {s->Pa, n * 16},
-                {s->Pb, n * 16}, {s->orig_c, n * 4}, {s->orig_s, n * 4}, {s->to_new, n * 4},
-                {s->sorted_keys, n * 4}, {s->order, n * 4}, {s->off, (s->ncells + 1) * 4}, {s->mass, n * 4},
-                {s->lam, n * 4}, {s->rho, n * 4}, {s->w, n * 4}};
-        if (nb) {
-            bufs.push_back({s->rigid.rot, nb * 16});
-            bufs.push_back({s->rigid.cm, nb * 16});
-        }
-        for (auto &b : bufs) {
-            void *p = nullptr;
-            if (cudaMalloc(&p, b.second) != cudaSuccess) return fail_with(BP_ERR_OUT_OF_MEMORY, "backward: snapshot");
-            copies.push_back(p);
-            cudaMemcpyAsync(p, b.first, b.second, cudaMemcpyDeviceToDevice, s->stream);
-        }
-        pcur = s->Pcur;
-        return BP_OK;
-    }
-    void restore(bp_solver *s)
-    {
-        for (size_t k = 0; k < bufs.size(); ++k)
-            cudaMemcpyAsync(bufs[k].first, copies[k], bufs[k].second, cudaMemcpyDeviceToDevice, s->stream);
-        s->Pcur = pcur;
-    }
-};
-
 bool stage_on(const bp_params &p, int bit) { return (p.stage_mask & bit) != 0; }
 
 // Which recorded configurations have an adjoint.
@@ -459,7 +422,7 @@ extern "C" bp_status bp_solver_backward(bp_solver *s, const float *grad_position
     const int n = s->n;
     const size_t N = (size_t)n;
     BP_CUDA_OR_FAIL(cudaStreamSynchronize(st));
-    Snapshot snap;
+    StateSnapshot snap;
     if ((stt = snap.take(s)) != BP_OK) return stt;
 
     // incoming gradients, original order -> the final state's sorted order

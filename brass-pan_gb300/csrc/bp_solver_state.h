@@ -181,3 +181,41 @@ bp_status tape_record_update(bp_solver *s, int nsub, float dt, int iterations, b
 void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int picked, float3 ppos, LaunchLog *L,
                      SubstepTape *tape = nullptr);
 }  // namespace bp
+
+// Every buffer a caller can observe after an update, copied aside and put
+// back (around backward() and the autotuner's trial updates).
+struct StateSnapshot {
+    std::vector<std::pair<void *, size_t>> bufs;  // solver buffer, bytes
+    std::vector<void *> copies;
+    float4 *pcur = nullptr;
+    ~StateSnapshot()
+    {
+        for (void *p : copies) cudaFree(p);
+    }
+    bp_status take(bp_solver *s)
+    {
+        const size_t n = (size_t)s->n, nb = (size_t)s->rigid.num_bodies;
+        bufs = {{s->Xc, n * 16}, {s->Vc, n * 16}, {s->Xs, n * 16}, {s->Vs, n * 16}, {s->Pa, n * 16},
+                {s->Pb, n * 16}, {s->orig_c, n * 4}, {s->orig_s, n * 4}, {s->to_new, n * 4},
+                {s->sorted_keys, n * 4}, {s->order, n * 4}, {s->off, (s->ncells + 1) * 4}, {s->mass, n * 4},
+                {s->lam, n * 4}, {s->rho, n * 4}, {s->w, n * 4}, {s->err, 4}};
+        if (nb) {
+            bufs.push_back({s->rigid.rot, nb * 16});
+            bufs.push_back({s->rigid.cm, nb * 16});
+        }
+        for (auto &b : bufs) {
+            void *p = nullptr;
+            if (cudaMalloc(&p, b.second) != cudaSuccess) return bp::fail_with(BP_ERR_OUT_OF_MEMORY, "state snapshot");
+            copies.push_back(p);
+            cudaMemcpyAsync(p, b.first, b.second, cudaMemcpyDeviceToDevice, s->stream);
+        }
+        pcur = s->Pcur;
+        return BP_OK;
+    }
+    void restore(bp_solver *s)
+    {
+        for (size_t k = 0; k < bufs.size(); ++k)
+            cudaMemcpyAsync(bufs[k].first, copies[k], bufs[k].second, cudaMemcpyDeviceToDevice, s->stream);
+        s->Pcur = pcur;
+    }
+};

@@ -151,6 +151,16 @@ class ParticleSolver:
         return {"masked": int(out[0]), "cells_no_mask": int(out[1]), "cells_moved_cell": int(out[2]),
                 "cells_displaced": int(out[3])}
 
+    def autotune(self, num_substeps: int, dt: float, iterations: int) -> tuple[int, list[float]]:
+        """Keep the fastest walk variant for this scene; returns it and the
+        trial times (ms) of the five candidates."""
+        opt = C.c_int32()
+        ms = (C.c_float * 5)()
+        abi.check(self.lib, self.lib.bp_solver_autotune(self.handle, num_substeps, C.c_float(dt), iterations,
+                                                        C.byref(opt), ms))
+        self.params.walk_options = opt.value
+        return opt.value, list(ms)
+
     # -- differentiable rollouts ------------------------------------------------------
     def tape_begin(self, checkpoint_every: int = 10):
         """Record the following updates for backward()."""

@@ -246,6 +246,16 @@ bp_status bp_solver_profile(bp_solver *s, int32_t num_substeps, float dt, int32_
 bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
                                uint64_t out_walks[4]);
 
+/* Picks the fastest neighbour-walk variant (BP_WALK_* combinations; all give
+ * identical results) for this solver's scene and step configuration: each
+ * candidate runs one update from the current state, timed with CUDA events,
+ * and the state is put back after every trial.  The choice is kept in the
+ * solver's parameters and written to *out_walk_options; out_ms (or NULL)
+ * receives the time of each of the 5 candidates (0, NO_SPLIT, NO_LISTS,
+ * NO_STAGING, NO_SPLIT | NO_STAGING).  No counterpart in the reference. */
+bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
+                             int32_t *out_walk_options, float *out_ms);
+
 /* ---- Differentiable rollouts ------------------------------------------------
  * No counterpart in the reference.  bp_solver_tape_begin starts recording the
  * following bp_solver_update calls (no picking); the state is checkpointed at

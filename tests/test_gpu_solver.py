@@ -222,6 +222,30 @@ def test_walk_variants_are_bit_identical(bp, gpu, walk, skin):
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
+def test_autotune_keeps_state_and_results(bp, gpu):
+    """The autotuner's trial updates leave the state as it was, and the variant
+    it keeps gives the same bits as the default walk."""
+    abi = bp.abi
+    scene = small_mixed_scene(bp, seed=21)
+    a = bp.ParticleSolver(scene, bp.make_params(scene))
+    b = bp.ParticleSolver(scene, bp.make_params(scene))
+    for s in (a, b):
+        s.update(2, DT, 4)
+    x0 = a.positions()
+    opt, ms = a.autotune(2, DT, 4)
+    np.testing.assert_array_equal(a.positions(), x0)
+    assert opt in (0, abi.BP_WALK_NO_SPLIT, abi.BP_WALK_NO_LISTS, abi.BP_WALK_NO_STAGING,
+                   abi.BP_WALK_NO_SPLIT | abi.BP_WALK_NO_STAGING)
+    assert all(t > 0 for t in ms)
+    for s in (a, b):
+        for _ in range(3):
+            s.update(2, DT, 4)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.velocities(), b.velocities())
+    a.close()
+    b.close()
+
+
 def test_graph_replay_equals_recapture(bp, gpu):
     scene = small_mixed_scene(bp, seed=10)
     p = bp.make_params(scene)
