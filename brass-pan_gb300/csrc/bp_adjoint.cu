@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const 
                                                              const float4 *__restrict__ gOut,
                                                              float *__restrict__ gLam, float4 *__restrict__ gPart)
 {
-    __shared__ StageShared S;
+    StageShared &S = stage_shared();
     const int g = stage_block(C, P, off, blockIdx.x * kWalkThreads, S);
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= C.n) return;
@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_lambda(SimConsts C, const 
                                                              const float4 *__restrict__ gPart,
                                                              const float4 *__restrict__ gOut, float4 *__restrict__ gIn)
 {
-    __shared__ StageShared S;
+    StageShared &S = stage_shared();
     const int g = stage_block(C, P, off, blockIdx.x * kWalkThreads, S);
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= C.n) return;
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_xsph(SimConsts C, const fl
                                                            const float4 *__restrict__ gVout, float4 *__restrict__ gVin,
                                                            float4 *__restrict__ gX)
 {
-    __shared__ StageShared S;
+    StageShared &S = stage_shared();
     const int g = stage_block(C, P, off, blockIdx.x * kWalkThreads, S);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= C.n) return;
@@ -698,8 +698,8 @@ void adj_fluid(cudaStream_t st, const SimConsts &C, const float4 *Pin, const flo
                const float *rho, const int *off, const float4 *gOut, float *gLam, float4 *gPart, float4 *gIn)
 {
     if (C.n <= 0) return;
-    k_adj_deltap<<<blocks(C.n, kWalkThreads), kWalkThreads, 0, st>>>(C, Pin, mass, lam, off, gOut, gLam, gPart);
-    k_adj_lambda<<<blocks(C.n, kWalkThreads), kWalkThreads, 0, st>>>(C, Pin, mass, rho, off, gLam, gPart, gOut, gIn);
+    k_adj_deltap<<<blocks(C.n, kWalkThreads), kWalkThreads, stage_bytes(C), st>>>(C, Pin, mass, lam, off, gOut, gLam, gPart);
+    k_adj_lambda<<<blocks(C.n, kWalkThreads), kWalkThreads, stage_bytes(C), st>>>(C, Pin, mass, rho, off, gLam, gPart, gOut, gIn);
 }
 void adj_shape_matching(cudaStream_t st, const RigidArgs &a, const float4 *rot, const float4 *Pin, const int *to_new,
                         float4 *gP)
@@ -711,7 +711,7 @@ void adj_xsph(cudaStream_t st, const SimConsts &C, const float4 *P, const float4
               const float4 *gVout, float4 *gVin, float4 *gX)
 {
     if (C.n <= 0) return;
-    k_adj_xsph<<<blocks(C.n, kWalkThreads), kWalkThreads, 0, st>>>(C, P, V, off, gVout, gVin, gX);
+    k_adj_xsph<<<blocks(C.n, kWalkThreads), kWalkThreads, stage_bytes(C), st>>>(C, P, V, off, gVout, gVin, gX);
 }
 
 }  // namespace bp

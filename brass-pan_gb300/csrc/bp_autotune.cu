@@ -19,8 +19,14 @@ extern "C" bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, floa
     if (num_substeps <= 0 || !(dt > 0.f) || iterations < 0)
         return fail_with(BP_ERR_INVALID_ARGUMENT, "num_substeps > 0, dt > 0 and iterations >= 0 required");
     if (s->tape) return fail_with(BP_ERR_INVALID_ARGUMENT, "not available while a tape records");
-    static const int32_t kCandidates[] = {0, BP_WALK_NO_SPLIT, BP_WALK_NO_LISTS, BP_WALK_NO_STAGING,
-                                          BP_WALK_NO_SPLIT | BP_WALK_NO_STAGING};
+    static const int32_t kCandidates[] = {0,
+                                          BP_WALK_NO_STAGING,
+                                          BP_WALK_NO_SPLIT,
+                                          BP_WALK_NO_LISTS,
+                                          BP_WALK_NO_STAGING | BP_WALK_NO_SPLIT,
+                                          BP_WALK_NO_STAGING | BP_WALK_NO_LISTS,
+                                          BP_WALK_NO_SPLIT | BP_WALK_NO_LISTS,
+                                          BP_WALK_NO_STAGING | BP_WALK_NO_SPLIT | BP_WALK_NO_LISTS};
     constexpr int kNum = (int)(sizeof(kCandidates) / sizeof(kCandidates[0]));
     if (s->n <= 0) {
         if (out_walk_options) *out_walk_options = s->prm.walk_options;

@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS)
                          const int *__restrict__ solid_prefix, const int *__restrict__ solid_list,
                          int solids_apart, float4 *__restrict__ Pout)
 {
-    __shared__ StageShared S;
+    StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kWalkThreads;
     // With the solids apart, fluid threads walk the solid list, not the
     // staged runs: only the runs' solid check is needed.
@@ -290,10 +290,10 @@ void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4
     const int grid = (C.n + kWalkThreads - 1) / kWalkThreads;
     const int apart = (solids_apart && solid_list && nsolid > 0) ? 1 : 0;
     if (C.split)
-        k_particle_collision<true><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
+        k_particle_collision<true><<<grid, kWalkThreads, stage_bytes(C), st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
                                                                  solid_list, apart, Pout);
     else
-        k_particle_collision<false><<<grid, kWalkThreads, 0, st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
+        k_particle_collision<false><<<grid, kWalkThreads, stage_bytes(C), st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
                                                                   solid_list, apart, Pout);
     L->done(__func__);
     if (apart) {

@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
                                                          const int *__restrict__ off, float *__restrict__ lam,
                                                          float *__restrict__ rho)
 {
-    __shared__ StageShared S;
+    StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
     const int g = stage_block(C, P, off, i0, S);
     const int i = i0 + threadIdx.x;
@@ -81,10 +81,10 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
 }
 
 // Kernels with a split walk (test, then body over the hits) and a fused one.
-#define BP_LAUNCH_SPLIT(kernel, grid, block, st, ...)                     \
-    do {                                                                  \
-        if (C.split) kernel<true><<<grid, block, 0, st>>>(__VA_ARGS__);   \
-        else kernel<false><<<grid, block, 0, st>>>(__VA_ARGS__);          \
+#define BP_LAUNCH_SPLIT(kernel, grid, block, st, ...)                                      \
+    do {                                                                                   \
+        if (C.split) kernel<true><<<grid, block, stage_bytes(C), st>>>(__VA_ARGS__);       \
+        else kernel<false><<<grid, block, stage_bytes(C), st>>>(__VA_ARGS__);              \
     } while (0)
 
 void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const float *mass, const int *off,
@@ -103,7 +103,7 @@ void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 template <bool Split>
 __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_deltap(SimConsts C, DeltaArgs a)
 {
-    __shared__ StageShared S;
+    StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
     const int g = stage_block(C, a.P, a.off, i0, S);
     const int k = i0 + threadIdx.x;
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
                                                          const float *__restrict__ rho, const int *__restrict__ off,
                                                          float4 *__restrict__ Om, float4 *__restrict__ Nm)
 {
-    __shared__ StageShared S;
+    StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
     const int g = stage_block(C, P, off, i0, S);
     const int i = i0 + threadIdx.x;
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_b(Sim
                                                          const float4 *__restrict__ Nm,
                                                          const int *__restrict__ off, float4 *__restrict__ Vout)
 {
-    __shared__ StageShared S;
+    StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
     const int i = i0 + threadIdx.x;
     const int cnt = post_list_count(C, P, i);
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_c(Sim
                                                          const int *__restrict__ off, const float *__restrict__ mass,
                                                          const float *__restrict__ rho, float4 *__restrict__ Vout)
 {
-    __shared__ StageShared S;
+    StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
     const int i = i0 + threadIdx.x;
     const int cnt = post_list_count(C, P, i);

@@ -82,6 +82,9 @@ extern "C" void bp_params_init(bp_params *p, float r)
     p->wind_lift = 100.0f;
     p->rotation_iterations = 20;
     p->neighbor_skin = 0.0f;  // masks measured slower than cell walks on GB300 (opt-in)
+    // staging each CTA's neighbourhood in shared memory measured slower than
+    // reading it through a full-size L1 (opt-in; bp_solver_autotune times both)
+    p->walk_options = BP_WALK_NO_STAGING;
 }
 
 static bp_status check_params(const bp_params *p)

@@ -57,6 +57,13 @@ struct StageShared {
 
 constexpr int kNoSolidNear = -2;
 
+// The staging buffer lives in dynamic shared memory, sized stage_bytes(C) at
+// launch: without staging the kernels take none, and the L1 cache keeps the
+// whole unified shared-memory / L1 array.
+extern __shared__ __align__(16) unsigned char bp_stage_smem[];
+__device__ __forceinline__ StageShared &stage_shared() { return *reinterpret_cast<StageShared *>(bp_stage_smem); }
+inline size_t stage_bytes(const SimConsts &C) { return C.stage ? sizeof(StageShared) : 0; }
+
 // Collective: every thread of the CTA must call it (before any early exit).
 // Returns the calling thread's column group (0 or 1), or -1 when the CTA does
 // not use shared memory or the thread has no particle.

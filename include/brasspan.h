@@ -118,7 +118,7 @@ typedef struct bp_params {
     int32_t rotation_iterations; /* 20 (shapematching.cuh:72) */
     float neighbor_skin;         /* skin of the per-substep neighbour masks, as a fraction of h
                                     (0 disables them; results are identical either way): 0 */
-    int32_t walk_options;        /* BP_WALK_* tuning switches of the neighbour walks: 0 */
+    int32_t walk_options;        /* BP_WALK_* tuning switches of the neighbour walks: BP_WALK_NO_STAGING */
     int32_t reserved[6];
 } bp_params;
 
@@ -251,8 +251,10 @@ bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int
  * candidate runs one update from the current state, timed with CUDA events,
  * and the state is put back after every trial.  The choice is kept in the
  * solver's parameters and written to *out_walk_options; out_ms (or NULL)
- * receives the time of each of the 5 candidates (0, NO_SPLIT, NO_LISTS,
- * NO_STAGING, NO_SPLIT | NO_STAGING).  No counterpart in the reference. */
+ * receives the time of each of the 8 combinations of the three BP_WALK_NO_*
+ * bits, in the order 0, NO_STAGING, NO_SPLIT, NO_LISTS, NO_STAGING|NO_SPLIT,
+ * NO_STAGING|NO_LISTS, NO_SPLIT|NO_LISTS, all three.  No counterpart in the
+ * reference. */
 bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
                              int32_t *out_walk_options, float *out_ms);
 
