@@ -23,7 +23,7 @@ constexpr int kScanThreads = kWalkThreads;  // scan kernels stage their neighbou
 // Reference mode (Q1): density sums only sorted indices j >= i; solid
 // neighbours count x solid_scale; C = rho/rho0 - 1, clamped at 0 when Akinci
 // is on; lambda = -C / lambda_den.  Textbook mode: all j, exact denominator.
-template <bool Split>
+template <bool Split, bool Stage>
 __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(SimConsts C, const float4 *__restrict__ P,
                                                          const float *__restrict__ mass,
                                                          const int *__restrict__ off, float *__restrict__ lam,
@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
 {
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
-    const int g = stage_block(C, P, off, i0, S);
+    const int g = Stage ? stage_block(C, P, off, i0, S) : -1;
     const int i = i0 + threadIdx.x;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
     float density = 0.f;
     if (!C.textbook) {
         walk_neighbors<Split>(
-            i, pi, i, P, v, C, &S, g, [&](int, float4 pj) { return len2(pi - f3(pj)) <= C.h2; },
+            i, pi, i, P, v, C, Stage ? &S : nullptr, g, [&](int, float4 pj) { return len2(pi - f3(pj)) <= C.h2; },
             [&](int j, float4 pj) {
                 const float ld = __fmul_rn(__ldg(mass + j), poly6(C, len2(pi - f3(pj))));
                 density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
         float sum_g2 = 0.f;
         float3 gi = make_float3(0.f, 0.f, 0.f);
         walk_neighbors<Split>(
-            i, pi, 0, P, v, C, &S, g, [&](int, float4 pj) { return len2(pi - f3(pj)) <= C.h2; },
+            i, pi, 0, P, v, C, Stage ? &S : nullptr, g, [&](int, float4 pj) { return len2(pi - f3(pj)) <= C.h2; },
             [&](int j, float4 pj) {
                 const float3 diff = pi - f3(pj);
                 const float d2 = len2(diff);
@@ -81,10 +81,15 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
 }
 
 // Kernels with a split walk (test, then body over the hits) and a fused one.
-#define BP_LAUNCH_SPLIT(kernel, grid, block, st, ...)                                      \
-    do {                                                                                   \
-        if (C.split) kernel<true><<<grid, block, stage_bytes(C), st>>>(__VA_ARGS__);       \
-        else kernel<false><<<grid, block, stage_bytes(C), st>>>(__VA_ARGS__);              \
+// Kernels instantiated for split / fused walks and staged / unstaged CTAs
+// (an unstaged instantiation carries none of the staging code or registers).
+#define BP_LAUNCH_SPLIT(kernel, grid, block, st, ...)                                                 \
+    do {                                                                                              \
+        const size_t smem_ = stage_bytes(C);                                                          \
+        if (C.split && C.stage) kernel<true, true><<<grid, block, smem_, st>>>(__VA_ARGS__);          \
+        else if (C.split) kernel<true, false><<<grid, block, smem_, st>>>(__VA_ARGS__);               \
+        else if (C.stage) kernel<false, true><<<grid, block, smem_, st>>>(__VA_ARGS__);               \
+        else kernel<false, false><<<grid, block, smem_, st>>>(__VA_ARGS__);                           \
     } while (0)
 
 void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const float *mass, const int *off,
@@ -100,12 +105,12 @@ void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // only visit b > a), to both ends.  In gather form particle k includes j when
 // the lower-indexed of (k, j) is fluid.  Textbook mode: fluid k gathers over
 // every neighbour; solids do not move.
-template <bool Split>
+template <bool Split, bool Stage>
 __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_deltap(SimConsts C, DeltaArgs a)
 {
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
-    const int g = stage_block(C, a.P, a.off, i0, S);
+    const int g = Stage ? stage_block(C, a.P, a.off, i0, S) : -1;
     const int k = i0 + threadIdx.x;
     if (k >= C.n) return;
     const float4 pk4 = a.P[k];
@@ -116,7 +121,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_deltap(Sim
     if (!(C.textbook && phk > 0)) {
         const float lk = a.lam[k];
         walk_neighbors<Split>(
-            k, pk, 0, a.P, grid_view(C, sc, a.off), C, &S, g,
+            k, pk, 0, a.P, grid_view(C, sc, a.off), C, Stage ? &S : nullptr, g,
             [&](int, float4 pj4) {  // r = 0 excludes k itself
                 const float d2 = len2(pk - f3(pj4));
                 return d2 <= C.h2 && d2 > 0.f;
@@ -221,7 +226,7 @@ void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, Laun
 // Pass A: vorticity omega_i (fluidOmega) and Akinci normal n_i (fluidNormal)
 // in one walk over same-phase neighbours with 0 < r^2 <= h^2.
 // Om[i] = (omega, |omega|); Nm[i] = (h * n, rho_i).
-template <bool Split>
+template <bool Split, bool Stage>
 __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
                                                          const float *__restrict__ rho, const int *__restrict__ off,
@@ -229,7 +234,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
 {
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
-    const int g = stage_block(C, P, off, i0, S);
+    const int g = Stage ? stage_block(C, P, off, i0, S) : -1;
     const int i = i0 + threadIdx.x;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
@@ -243,7 +248,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
     // the walk takes the passes' common neighbours (r = 0 included, as pass C
     // wants them) and records them for passes B and C
     walk_neighbors<Split>(
-        i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, &S, g,
+        i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, Stage ? &S : nullptr, g,
         [&](int, float4 pj4) { return len2(pi - f3(pj4)) <= C.h2; },
         [&](int j, float4 pj4) {
             if (j == i || phase_of(pj4) != phi) return;
@@ -304,7 +309,7 @@ __device__ __forceinline__ int post_list_count(const SimConsts &C, const float4 
 // (fluidAkinciTension), both on the same neighbours.  v' = v + eps (N x w) dt,
 // v'' = v' + F dt, exactly the reference's sequence (in-place update followed
 // by newVelocities = velocities + F dt).  Solids pass through.
-template <bool Split>
+template <bool Split, bool Stage>
 __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_b(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
                                                          const float4 *__restrict__ Om,
@@ -315,7 +320,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_b(Sim
     const int i0 = blockIdx.x * kScanThreads;
     const int i = i0 + threadIdx.x;
     const int cnt = post_list_count(C, P, i);
-    const int g = __syncthreads_or(cnt == kWalkCells) ? stage_block(C, P, off, i0, S) : -1;
+    const int g = (Stage && __syncthreads_or(cnt == kWalkCells)) ? stage_block(C, P, off, i0, S) : -1;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
     const float4 vi4 = V[i];
@@ -351,7 +356,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_b(Sim
         for_each_listed(C, i, cnt, P, body);
     } else {
         walk_neighbors<Split>(
-            i, pi, 0, P, grid_view(C, sc, off), C, &S, g,
+            i, pi, 0, P, grid_view(C, sc, off), C, Stage ? &S : nullptr, g,
             [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; },
             body);
     }
@@ -367,7 +372,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_b(Sim
 
 // Pass C: XSPH viscosity (fluidXSph): same phase, j != i, r^2 <= h^2 (r = 0
 // included).  Textbook mode weights each neighbour by its volume m_j / rho_j.
-template <bool Split>
+template <bool Split, bool Stage>
 __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_c(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
                                                          const int *__restrict__ off, const float *__restrict__ mass,
@@ -377,7 +382,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_c(Sim
     const int i0 = blockIdx.x * kScanThreads;
     const int i = i0 + threadIdx.x;
     const int cnt = post_list_count(C, P, i);
-    const int g = __syncthreads_or(cnt == kWalkCells) ? stage_block(C, P, off, i0, S) : -1;
+    const int g = (Stage && __syncthreads_or(cnt == kWalkCells)) ? stage_block(C, P, off, i0, S) : -1;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
     const float4 vi4 = V[i];
@@ -397,7 +402,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_c(Sim
         for_each_listed(C, i, cnt, P, body);
     } else {
         walk_neighbors<Split>(
-            i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, &S, g,
+            i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, Stage ? &S : nullptr, g,
             [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; },
             body);
     }
