@@ -95,7 +95,34 @@ struct SimConsts {
     // original indices alike, because every scene keeps its segment.
     const SceneConsts *scn;
     const int *scene_of;
+    // Alias classes (cls_perm == nullptr: off).  A table of D^3 cells wraps
+    // space: table cell (x, y, z) holds the particles of every real cell
+    // (x + aD, y + bD, z + cD).  At hash time each particle gets the parity
+    // bits of (a, b, c), its class (0..7).  cls_perm lists the sorted indices
+    // class by class, each class in ascending sorted index, cls_inv is its
+    // inverse and cls_off[k * cls_T + key] the dense prefix over (class, cell
+    // key).  A walk of real cell w visits only the particles of w's class in
+    // that table cell: any other one was hashed at least D - 2 cells from the
+    // walker along some axis, so it fails every distance test within h while
+    // no particle has moved further than the reach (D - 2) cell - h - margin
+    // from its hash-time position.  k_class_refresh gathers P into cls_pos
+    // before each walking launch and sets *cls_moved when some particle moved
+    // further; walks then take whole table cells for the rest of the substep.
+    const int *cls_perm;
+    const int *cls_inv;
+    const int *cls_of;      // class of each sorted particle
+    const int *cls_off;     // [8 * cls_T + 1]
+    const float4 *cls_pos;  // P in class order
+    const int *cls_moved;
+    int cls_T;              // cell keys of all scenes
 };
+
+// Class (0..7) of real cell c on a table of D cells per axis (D a power of two).
+__device__ __forceinline__ int alias_class(int x, int y, int z, int D)
+{
+    const int sh = __ffs(D) - 1;
+    return ((x >> sh) & 1) | (((y >> sh) & 1) << 1) | (((z >> sh) & 1) << 2);
+}
 
 constexpr unsigned short kFlagContact = 1;
 constexpr unsigned short kFlagWide = 2;

@@ -8,6 +8,8 @@
 //   reorderParticlesData (kernel/grid.cuh:134-163)
 //   + inverseMapping    (kernel/util.cuh:348-358) -> k_reorder (float4 records, fused predict,
 //                                                    mass scaling and plane stabilisation)
+#include <algorithm>
+
 #include "bp_internal.h"
 
 namespace bp {
@@ -52,8 +54,9 @@ void sort_scratch_carve(void *base, int n, int D, SortScratch *s)
 
 // Per-tile digit histogram, digit-major: hist[d * tiles + tile].
 __global__ void __launch_bounds__(kSortThreads) k_radix_upsweep(const int *__restrict__ keys, int n, int shift,
-                                                               int *__restrict__ hist, int tiles)
+                                                               int *__restrict__ hist, int tiles, Gate gate)
 {
+    if (gate_closed(gate)) return;
     __shared__ int h[kRadixBins];
     for (int d = threadIdx.x; d < kRadixBins; d += kSortThreads) h[d] = 0;
     __syncthreads();
@@ -68,8 +71,10 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_upsweep(const int *__res
 }
 
 // One CTA per digit: exclusive scan over the tiles, digit total on the side.
-__global__ void __launch_bounds__(256) k_radix_scan(int *__restrict__ hist, int tiles, int *__restrict__ digit_total)
+__global__ void __launch_bounds__(256) k_radix_scan(int *__restrict__ hist, int tiles, int *__restrict__ digit_total,
+                                                    Gate gate)
 {
+    if (gate_closed(gate)) return;
     __shared__ int warp_sums[8];
     int *row = hist + (size_t)blockIdx.x * tiles;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -111,8 +116,9 @@ __global__ void __launch_bounds__(256) k_radix_scan(int *__restrict__ hist, int 
 __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(
     const int *__restrict__ keys_in, const int *__restrict__ vals_in, int n, int shift,
     const int *__restrict__ hist, const int *__restrict__ digit_total, int tiles, int *__restrict__ keys_out,
-    int *__restrict__ vals_out)
+    int *__restrict__ vals_out, Gate gate)
 {
+    if (gate_closed(gate)) return;
     constexpr int W = kSortThreads / 32;
     constexpr int SEG = kSortTile / W;        // keys per warp
     constexpr int ROUNDS = SEG / 32;
@@ -185,7 +191,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_downsweep(
 }
 
 void radix_sort_pairs(cudaStream_t st, int n, int D, const int *keys_in, const int *vals_in, int *keys_out,
-                      int *vals_out, const SortScratch &s, bool hist_ready, LaunchLog *L)
+                      int *vals_out, const SortScratch &s, bool hist_ready, LaunchLog *L, Gate gate)
 {
     if (n <= 0) return;
     const int tiles = sort_tiles(n);
@@ -196,13 +202,13 @@ void radix_sort_pairs(cudaStream_t st, int n, int D, const int *keys_in, const i
         int *kdst = (p == passes - 1) ? keys_out : s.keys_alt[p & 1];
         int *vdst = (p == passes - 1) ? vals_out : s.vals_alt[p & 1];
         if (!(p == 0 && hist_ready)) {
-            k_radix_upsweep<<<tiles, kSortThreads, 0, st>>>(ksrc, n, shift, s.hist, tiles);
+            k_radix_upsweep<<<tiles, kSortThreads, 0, st>>>(ksrc, n, shift, s.hist, tiles, gate);
             L->done("k_radix_upsweep");
         }
-        k_radix_scan<<<kRadixBins, 256, 0, st>>>(s.hist, tiles, s.digit_total);
+        k_radix_scan<<<kRadixBins, 256, 0, st>>>(s.hist, tiles, s.digit_total, gate);
         L->done("k_radix_scan");
         k_radix_downsweep<<<tiles, kSortThreads, 0, st>>>(ksrc, vsrc, n, shift, s.hist, s.digit_total, tiles,
-                                                          kdst, vdst);
+                                                          kdst, vdst, gate);
         L->done("k_radix_downsweep");
         ksrc = kdst;
         vsrc = vdst;
@@ -334,8 +340,10 @@ __global__ void k_reset_start_end(int n, const int *__restrict__ sorted, int *__
 // Tables with many more cells than particles (mostly empty cells) take 8
 // cells per thread, so they cost one search per 8 cells; dense tables take
 // one, so no thread walks a long run of keys.
-__global__ void k_cell_offsets(int n, int ncells, int per, const int *__restrict__ sorted, int *__restrict__ off)
+__global__ void k_cell_offsets(int n, int ncells, int per, const int *__restrict__ sorted, int *__restrict__ off,
+                               Gate gate)
 {
+    if (gate_closed(gate)) return;
     const long long c0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * per;
     if (c0 > ncells) return;
     int lo = 0, hi = n;
@@ -365,11 +373,11 @@ void launch_reset_start_end(cudaStream_t st, int n, const int *sorted, int *star
     L->done(__func__);
 }
 
-void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, LaunchLog *L)
+void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, LaunchLog *L, Gate gate)
 {
     const int per = ncells > 4LL * n ? 8 : 1;
     const long long threads = ((long long)ncells + 1 + per - 1) / per;
-    k_cell_offsets<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(n, ncells, per, sorted, off);
+    k_cell_offsets<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(n, ncells, per, sorted, off, gate);
     L->done(__func__);
 }
 
@@ -392,6 +400,11 @@ __global__ void __launch_bounds__(256) k_reorder(SimConsts C, ReorderArgs a)
     const int s = scene_index(C, i);
     float3 x = f3(X), v = f3(V);
     float3 p = predict(x, v, gravity_of(C, s), C);
+    if (a.cls) {  // the hashed position: its real cell gives the class
+        const int3 c = cell_of(p, C);
+        a.cls[i] = alias_class(c.x, c.y, c.z, s < 0 ? C.D : C.scn[s].D);
+        a.pos0[i] = make_float4(p.x, p.y, p.z, 0.f);
+    }
     if (a.inv_scaled) {
         const float scale = powf(2.7182818284f, -C.mass_k * x.y);
         a.inv_scaled[i] = 1.0f / (scale * X.w);
@@ -414,6 +427,91 @@ void launch_reorder(cudaStream_t st, const SimConsts &C, const ReorderArgs &a, L
 {
     if (C.n <= 0) return;
     k_reorder<<<(C.n + 255) / 256, 256, 0, st>>>(C, a);
+    L->done(__func__);
+}
+
+// ------------------------------------------------------------------------
+// alias classes
+// ------------------------------------------------------------------------
+
+// Counts the particles whose class differs from their cell's first
+// particle's (about how many candidates the class walks would skip) and
+// opens the substep's classes (*moved = 0).
+__global__ void __launch_bounds__(256) k_class_count(int n, const int *__restrict__ sorted_keys,
+                                                     const int *__restrict__ off, ClassArrays a)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j == 0) *a.moved = 0;
+    bool differs = false;
+    if (j < n) differs = __ldg(a.cls + j) != __ldg(a.cls + __ldg(off + __ldg(sorted_keys + j)));
+    const unsigned votes = __ballot_sync(0xffffffffu, differs);
+    if ((threadIdx.x & 31) == 0 && votes) atomicAdd(a.mixed, __popc(votes));
+}
+
+// keys[q] holds the class of perm[q] on entry (the radix pass output).
+__global__ void __launch_bounds__(256) k_class_keys(int n, const int *__restrict__ sorted_keys, ClassArrays a,
+                                                    Gate gate)
+{
+    if (gate_closed(gate)) return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int j = a.perm[q];
+    a.keys[q] = a.keys[q] * a.T + __ldg(sorted_keys + j);
+    a.inv[j] = q;
+}
+
+static Gate class_gate(int n, const ClassArrays &a) { return Gate{a.mixed, (n + 31) / 32}; }
+
+void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const int *off, const ClassArrays &a,
+                        const SortScratch &s, LaunchLog *L)
+{
+    if (n <= 0) return;
+    cudaMemsetAsync(a.mixed, 0, sizeof(int), st);
+    k_class_count<<<(n + 255) / 256, 256, 0, st>>>(n, sorted_keys, off, a);
+    L->done("k_class_count");
+    // the rest runs only where the classes pay (see k_class_refresh)
+    const Gate gate = class_gate(n, a);
+    // one 9-bit digit covers the 3 class bits: a stable partition of the sorted order
+    radix_sort_pairs(st, n, 8, a.cls, nullptr, a.keys, a.perm, s, false, L, gate);
+    k_class_keys<<<(n + 255) / 256, 256, 0, st>>>(n, sorted_keys, a, gate);
+    L->done("k_class_keys");
+    launch_cell_offsets(st, n, 8 * a.T, a.keys, a.off, L, gate);
+}
+
+// Walks use the classes while at least 1/32 of the particles sit in a cell
+// holding another class (below that the extra indirection costs more than
+// the skipped candidates save) and no particle has left the reach.
+__global__ void __launch_bounds__(256) k_class_refresh(int n, const float4 *__restrict__ P, ClassArrays a, Gate gate)
+{
+    if (gate_closed(gate)) {  // uniform: written by an earlier kernel
+        if (blockIdx.x == 0 && threadIdx.x == 0) *a.moved = 1;
+        return;
+    }
+    bool far = false;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int j = __ldg(a.perm + q);
+        const float4 p = P[j];
+        a.pos[q] = p;
+        const float4 p0 = __ldg(a.pos0 + j);
+        const float dx = p.x - p0.x, dy = p.y - p0.y, dz = p.z - p0.z;
+        // NaN counts as moved; so do positions far enough out that the hash's
+        // float rounding exceeds the reach's margin
+        const bool inside = fabsf(p.x) < 4.0e4f && fabsf(p.y) < 4.0e4f && fabsf(p.z) < 4.0e4f;
+        far |= !(dx * dx + dy * dy + dz * dz <= a.reach2) || !inside;
+    }
+    if (far) *a.moved = 1;
+}
+
+void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L)
+{
+    if (n <= 0) return;
+    // a grid-stride loop over one resident wave (8 CTAs of 256 per SM): the
+    // common case is the gate's early exit
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = std::min((n + 255) / 256, std::max(sms, 1) * 8);
+    k_class_refresh<<<blocks, 256, 0, st>>>(n, P, a, class_gate(n, a));
     L->done(__func__);
 }
 

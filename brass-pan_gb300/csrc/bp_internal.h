@@ -56,10 +56,18 @@ struct SortScratch {
 size_t sort_scratch_bytes(int n, int D);
 void sort_scratch_carve(void *base, int n, int D, SortScratch *s);
 
+// A device-side switch for kernels captured in a graph: they do nothing
+// unless *word >= min (word == nullptr: always open).
+struct Gate {
+    const int *word = nullptr;
+    int min = 0;
+};
+__device__ __forceinline__ bool gate_closed(const Gate &g) { return g.word && *g.word < g.min; }
+
 // keys_in: cell keys (pass 0 histogram already in s.hist when hist_ready);
 // vals_in == nullptr means the identity permutation.
 void radix_sort_pairs(cudaStream_t st, int n, int D, const int *keys_in, const int *vals_in, int *keys_out,
-                      int *vals_out, const SortScratch &s, bool hist_ready, LaunchLog *L);
+                      int *vals_out, const SortScratch &s, bool hist_ready, LaunchLog *L, Gate gate = Gate{});
 
 // ---- grid kernels launched by the solver and the stand-alone API ----
 void launch_hash_f3(cudaStream_t st, int n, const float *pos3, float cell, int D, int *keys, int *hist,
@@ -69,7 +77,8 @@ void launch_hash_state(cudaStream_t st, const SimConsts &C, const float4 *X, con
 void launch_find_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end, LaunchLog *L);
 void launch_reset_start_end(cudaStream_t st, int n, const int *sorted, int *start, int *end,
                             LaunchLog *L);
-void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, LaunchLog *L);
+void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, LaunchLog *L,
+                         Gate gate = Gate{});
 
 struct ReorderArgs {
     const int *order;      // sorted position -> old index
@@ -82,8 +91,31 @@ struct ReorderArgs {
     int stabilize;         // run planeStabilize twice
     int collide;           // also run iteration 0's plane collision
     int *tile_solid;       // nullptr, or flags set for 256-particle tiles holding a solid (cleared before)
+    int *cls;              // nullptr, or the alias class of each sorted particle at hash time
+    float4 *pos0;          // with cls: the hash-time (predicted) position of each sorted particle
 };
 void launch_reorder(cudaStream_t st, const SimConsts &C, const ReorderArgs &a, LaunchLog *L);
+
+// ---- alias classes (SimConsts::cls_perm) ----
+struct ClassArrays {
+    int *cls;        // [n] class of each sorted particle (k_reorder)
+    float4 *pos0;    // [n] hash-time positions (k_reorder)
+    int *keys;       // [n] class-order keys: class * T + cell key
+    int *perm;       // [n] class order -> sorted index
+    int *inv;        // [n] sorted index -> class order
+    int *off;        // [8 T + 1]
+    float4 *pos;     // [n] P in class order
+    int *mixed;      // one word: particles whose class differs from their cell's first particle's
+    int *moved;      // one word
+    int T;           // cell keys of all scenes
+    float reach2;    // squared reach (see SimConsts::cls_perm)
+};
+// After k_reorder: class order (one radix pass), keys, inverse, offsets and
+// the count of particles in cells holding two classes (off: the cell offsets).
+void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const int *off, const ClassArrays &a,
+                        const SortScratch &s, LaunchLog *L);
+// Gathers P into class order and flags particles beyond the reach.
+void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L);
 
 // ---- fluid kernels ----
 void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const float *mass, const int *off,

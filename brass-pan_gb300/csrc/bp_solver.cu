@@ -103,6 +103,22 @@ static bp_status check_params(const bp_params *p)
     return BP_OK;
 }
 
+// How far a particle may move from its hash-time position while walks skip
+// the other alias classes of a table cell, or 0 when they may not skip them
+// (see SimConsts::cls_perm).  A skipped particle was hashed in a real cell at
+// least D cells from the walked one along some axis, so at least (D - 2)
+// cells from the walker's cell; the hash's float rounding moves each cell
+// boundary by less than 0.01 for |p| < 4e4 (checked by k_class_refresh), and
+// 1e-3 h keeps the distance test's own rounding clear.  Taped updates and
+// neighbour masks walk whole cells.
+static float class_reach(const bp_solver *s)
+{
+    const bp_params &p = s->prm;
+    if (!s->cls.perm || s->tape || p.neighbor_skin > 0.f || (p.walk_options & BP_WALK_NO_ALIAS_CLASSES)) return 0.f;
+    const float reach = (float)(s->cls_dmin - 2) * p.cell_size - p.kernel_radius - (0.02f + 1e-3f * p.kernel_radius);
+    return reach > 0.f ? reach : 0.f;
+}
+
 // Substep constants: SetKernelRadius (K/fluid.cuh:11-27) evaluated on the host.
 SimConsts bp::make_consts(const bp_solver *s, float sdt)
 {
@@ -175,6 +191,15 @@ SimConsts bp::make_consts(const bp_solver *s, float sdt)
         C.nl_hs2 = hs * hs;
         C.nl_half_skin2 = half_skin * half_skin;
         C.nl_contact2 = contact * contact;
+    }
+    if (class_reach(s) > 0.f) {
+        C.cls_perm = s->cls.perm;
+        C.cls_inv = s->cls.inv;
+        C.cls_of = s->cls.cls;
+        C.cls_off = s->cls.off;
+        C.cls_pos = s->cls.pos;
+        C.cls_moved = s->cls.moved;
+        C.cls_T = s->cls.T;
     }
     C.nplanes = (p.stage_mask & BP_STAGE_PLANES) ? s->nplanes : 0;
     for (int k = 0; k < s->nplanes; ++k) {
@@ -307,12 +332,23 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)) ||
         (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->nl_mask, NM * 18)) ||
         (st = s->alloc(&s->nl_cell, NM)) || (st = s->alloc(&s->nl_pos, NM)) || (st = s->alloc(&s->nl_outlier, (size_t)D * D * ((D + 63) / 64))) ||
-        (st = s->alloc(&s->nl_flags, NM)) || (st = s->alloc(&s->nl_stats, 4)))
+        (st = s->alloc(&s->nl_flags, NM)) || (st = s->alloc(&s->nl_stats, 5)))
         return bail(st);
     {
         char *scratch = nullptr;
         if ((st = s->alloc(&scratch, sort_scratch_bytes((int)N, s->sort_dim)))) return bail(st);
         sort_scratch_carve(scratch, (int)N, s->sort_dim, &s->sort);
+    }
+    if (ncells <= kClassMaxCells) {
+        ClassArrays &a = s->cls;
+        if ((st = s->alloc(&a.cls, N)) || (st = s->alloc(&a.pos0, N)) || (st = s->alloc(&a.keys, N)) ||
+            (st = s->alloc(&a.perm, N)) || (st = s->alloc(&a.inv, N)) || (st = s->alloc(&a.off, 8 * ncells + 1)) ||
+            (st = s->alloc(&a.pos, N)) || (st = s->alloc(&a.mixed, 1)) || (st = s->alloc(&a.moved, 1)))
+            return bail(st);
+        a.T = (int)ncells;
+        s->cls_dmin = D;
+        if (batch)
+            for (const SceneConsts &c : batch->scenes) s->cls_dmin = std::min(s->cls_dmin, c.D);
     }
 
     // initial state in original order (sorted order == identity)
@@ -635,7 +671,20 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     ra.collide = fuse_first_planes;
     ra.tile_solid = pcoll ? s->tile_solid : nullptr;
     if (pcoll) cudaMemsetAsync(s->tile_solid, 0, ((s->n + 255) / 256) * sizeof(int), st);
+    const bool classes = C.cls_perm != nullptr;
+    ClassArrays ca = s->cls;
+    {
+        const float r = class_reach(s);
+        ca.reach2 = r * r;
+    }
+    ra.cls = classes ? ca.cls : nullptr;
+    ra.pos0 = classes ? ca.pos0 : nullptr;
     launch_reorder(st, C, ra, L);
+    if (classes) launch_class_order(st, s->n, s->sorted_keys, s->off, ca, s->sort, L);
+    // walks read candidates in class order: gather P before each walking launch
+    auto refresh = [&](const float4 *P) {
+        if (classes) launch_class_refresh(st, s->n, P, ca, L);
+    };
     if (tape) tape->vs_slot = tape->snap4(s->Vs);
 
     float4 *cur = s->Pa, *other = s->Pb;
@@ -672,11 +721,13 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             // solids walk in a launch of their own, in full warps (measured
             // faster than walking them in the staged CTAs, whether solids are
             // scattered through fluid or the whole scene)
+            refresh(cur);
             launch_particle_collision(st, C, cur, s->Xs, s->w, s->off, s->tile_solid, s->solid_prefix, s->solid_list,
                                       s->num_solids, true, other, L);
             std::swap(cur, other);
         }
         if (fluid) {
+            refresh(cur);  // lambda and delta-p read the same positions
             launch_lambda(st, C, cur, s->mass, s->off, s->lam, s->rho, L);
             if (tape) {
                 const int aux = tape->snap1(s->lam);
@@ -731,6 +782,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     const bool post_ab = C.use_vort || C.use_akinci;
     if (tape && post_ab) tape->push(TS_POST_AB, s->Vc);
     if (tape && !post_ab && C.use_xsph) tape->push(TS_XSPH, s->Vc);
+    if (post_ab || C.use_xsph) refresh(cur);  // the post passes read the same positions
     if (post_ab) {
         // pass A records each fluid particle's neighbours for passes B and C
         SimConsts Cl = C;
@@ -859,21 +911,21 @@ extern "C" bp_status bp_solver_profile(bp_solver *s, int32_t nsub, float dt, int
 }
 
 extern "C" bp_status bp_solver_walk_stats(bp_solver *s, int32_t nsub, float dt, int32_t iterations,
-                                          uint64_t out_walks[4])
+                                          uint64_t out_walks[5])
 {
     if (!s || !out_walks) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
     if (s->tape) return fail(BP_ERR_INVALID_ARGUMENT, "not available while a tape records");
     if (nsub <= 0 || !(dt > 0.f) || iterations < 0) return fail(BP_ERR_INVALID_ARGUMENT, "bad step arguments");
-    for (int k = 0; k < 4; ++k) out_walks[k] = 0;
+    for (int k = 0; k < 5; ++k) out_walks[k] = 0;
     if (s->n <= 0) return BP_OK;
     LaunchLog L;
     L.stream = s->stream;
-    BP_CUDA(cudaMemsetAsync(s->nl_stats, 0, 4 * sizeof(unsigned), s->stream));
+    BP_CUDA(cudaMemsetAsync(s->nl_stats, 0, 5 * sizeof(unsigned), s->stream));
     enqueue_update(s, nsub, dt, iterations, -1, make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), &L, true);
-    unsigned h[4];
+    unsigned h[5];
     BP_CUDA(cudaMemcpyAsync(h, s->nl_stats, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
     BP_CUDA(cudaStreamSynchronize(s->stream));
-    for (int k = 0; k < 4; ++k) out_walks[k] = h[k];
+    for (int k = 0; k < 5; ++k) out_walks[k] = h[k];
     s->last_launches = L.count;
     return BP_OK;
 }

@@ -83,6 +83,10 @@ struct SubstepTape {
 #endif
 constexpr int kPostListCap = BP_POST_LIST_CAP;
 
+// Alias classes are kept for key spaces of at most this many cells (their
+// offsets take 8 entries per cell: 64 MB at 2^21 cells, a 128^3 table).
+constexpr size_t kClassMaxCells = size_t(1) << 21;
+
 struct bp_solver {
     int n = 0;
     bp_params prm{};
@@ -112,6 +116,10 @@ struct bp_solver {
     int *solid_prefix = nullptr, *solid_list = nullptr, *solid_totals = nullptr;  // compacted solids
     int *nbr = nullptr, *nbr_count = nullptr;  // post-pass neighbour lists [kPostListCap][N], counts
     SortScratch sort{};
+    // alias classes (SimConsts::cls_perm); cls.perm == nullptr: not allocated
+    // (key spaces above kClassMaxCells cells)
+    ClassArrays cls{};
+    int cls_dmin = 0;  // smallest grid dimension of the scenes
 
     bool has_solid = false;
     int num_solids = 0;

@@ -211,6 +211,84 @@ __device__ __forceinline__ void walk_run(int jb, int b, int e, const float4 *src
     }
 }
 
+// Candidates [qb, e) of one (class, cell) run in class order, read from
+// C.cls_pos.  test() sees a stand-in index that equals i only for particle i
+// itself (tests compare it with i and nothing else); the body gets the sorted
+// index, and skips sorted indices below jlo.
+template <bool Split, class T, class B>
+__device__ __forceinline__ void walk_run_cls(int qb, int e, int qi, int i, int jlo, const SimConsts &C, T &test,
+                                             B &body)
+{
+    const float4 *__restrict__ src = C.cls_pos;
+    const int *__restrict__ perm = C.cls_perm;
+    if constexpr (!Split) {
+#pragma unroll 1
+        for (int q = qb; q < e; ++q) {
+            const float4 pj = src[q];
+            if (test(q == qi ? i : -1 - q, pj)) {
+                const int j = __ldg(perm + q);
+                if (j >= jlo) body(j, pj);
+            }
+        }
+    } else {
+#pragma unroll 1
+        for (int q0 = qb; q0 < e; q0 += 32) {
+            const int cnt = min(32, e - q0);
+            const float4 *s = src + q0;
+            unsigned bits = 0u;
+#pragma unroll 4
+            for (int t = 0; t < cnt; ++t)
+                if (test(q0 + t == qi ? i : -1 - (q0 + t), s[t])) bits |= 1u << t;
+#pragma unroll 1
+            while (bits) {
+                const int t = __ffs(bits) - 1;
+                bits &= bits - 1u;
+                const int j = __ldg(perm + q0 + t);
+                if (j >= jlo) body(j, s[t]);
+            }
+        }
+    }
+}
+
+// The 27-cell walk of real cell c over the alias classes (SimConsts::cls_perm):
+// the same columns and pieces as the table walk, each piece restricted to the
+// class of the real cells it covers.  A piece never spans two classes: z
+// crosses a class boundary exactly where the table index wraps.  With lo > 0
+// (candidates j >= lo only), a piece of i's own class starts at i's class
+// position (class order keeps sorted order); other pieces filter in the body.
+template <bool Split, class T, class B>
+__device__ __forceinline__ void walk_classes(int i, int3 c, int lo, const GridView &v, const SimConsts &C, T &test,
+                                             B &body)
+{
+    const unsigned m = v.mask;
+    const unsigned D = (unsigned)v.D;
+    const int sh = __ffs(v.D) - 1;
+    const int qi = __ldg(C.cls_inv + i);
+    const int ki = lo > 0 ? __ldg(C.cls_of + i) : -1;
+    const unsigned z0 = (unsigned)(c.z - 1) & m;
+    const unsigned z2 = (unsigned)(c.z + 1) & m;
+    const bool wrap = !(z0 < z2);
+    const int kz0 = ((c.z - 1) >> sh) & 1, kz2 = ((c.z + 1) >> sh) & 1;
+    const int *__restrict__ off = C.cls_off + v.base;
+    const size_t keys = (size_t)C.cls_T;
+#pragma unroll 1
+    for (int col = 0; col < 9; ++col) {
+        const int xr = c.x + col / 3 - 1, yr = c.y + col % 3 - 1;
+        const unsigned base = ((unsigned)xr & m) * D * D + ((unsigned)yr & m) * D;
+        const int kxy = ((xr >> sh) & 1) | (((yr >> sh) & 1) << 1);
+#pragma unroll 1
+        for (int piece = 0; piece < (wrap ? 2 : 1); ++piece) {
+            const unsigned za = (wrap && piece == 1) ? 0u : z0;
+            const unsigned zb = wrap ? (piece == 0 ? D - 1 : z2) : z2;
+            const int k = kxy | ((piece == 1 ? kz2 : kz0) << 2);
+            const int *o = off + (size_t)k * keys + base;
+            const int b = __ldg(o + za), e = __ldg(o + zb + 1);
+            const bool own = k == ki;
+            walk_run_cls<Split>(own ? max(b, qi) : b, e, qi, i, (lo > 0 && !own) ? lo : 0, C, test, body);
+        }
+    }
+}
+
 // Walk of particle i (sorted index) at position pi over the candidates
 // j >= lo of its 27 cells on grid v: body(j, P[j]) for every j with
 // test(j, P[j]).  S / g come from stage_block (S == nullptr or g < 0: no
@@ -266,6 +344,12 @@ __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const f
                 }
             }
         }
+        return;
+    }
+
+    if (C.cls_perm && !staged && __ldg(C.cls_moved) == 0) {
+        if (C.nl_stats) atomicAdd(C.nl_stats + 4, 1u);
+        walk_classes<Split>(i, c, lo, v, C, test, body);
         return;
     }
 

@@ -83,10 +83,17 @@ typedef enum bp_mode {
  * evaluates each pair term as its candidate is tested instead of testing a
  * chunk of candidates first and evaluating the pair terms of the hits;
  * BP_WALK_NO_LISTS makes the second and third velocity post passes walk
- * their cells instead of reading the neighbour lists the first one records. */
+ * their cells instead of reading the neighbour lists the first one records;
+ * BP_WALK_NO_ALIAS_CLASSES makes unstaged walks test every particle of a
+ * table cell instead of only those of the real cell walked (a grid of D^3
+ * cells wraps space, so one table cell holds every real cell D cells apart;
+ * the split is kept for grids of at most 2^21 cells and used in a substep
+ * while at least 1/32 of the particles share a cell with another real cell's
+ * and no particle has moved (D - 2) cells - h from where it was hashed). */
 #define BP_WALK_NO_STAGING 0x1
 #define BP_WALK_NO_SPLIT 0x2
 #define BP_WALK_NO_LISTS 0x4
+#define BP_WALK_NO_ALIAS_CLASSES 0x8
 
 /* Every literal of the reference's step as a field.  bp_params_init fills the
  * reference's values; comments give the reference location of each. */
@@ -242,9 +249,10 @@ bp_status bp_solver_profile(bp_solver *s, int32_t num_substeps, float dt, int32_
  * out_walks[0] walks over the per-substep neighbour masks; 27-cell walks
  * because [1] no mask was built for the particle (a column run wraps around
  * the table or holds more than 64 candidates), [2] the particle left the cell
- * its masks were built for, [3] some particle moved more than half the skin. */
+ * its masks were built for, [3] some particle moved more than half the skin;
+ * [4] of the walks counted in [1], those restricted to the alias classes. */
 bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
-                               uint64_t out_walks[4]);
+                               uint64_t out_walks[5]);
 
 /* Picks the fastest neighbour-walk variant (BP_WALK_* combinations; all give
  * identical results) for this solver's scene and step configuration: each

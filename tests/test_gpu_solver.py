@@ -222,6 +222,66 @@ def test_walk_variants_are_bit_identical(bp, gpu, walk, skin):
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
+@pytest.mark.parametrize("walk", ["split", "no_split", "staging"])
+def test_alias_classes_are_bit_identical(bp, gpu, walk):
+    """An 8^3 table over a 3 x 4 x 3 m box: every table cell holds up to
+    eight real cells.  Walks restricted to the walked real cell's alias class
+    give the bits of walks over whole table cells."""
+    abi = bp.abi
+    base = {"split": abi.BP_WALK_NO_STAGING, "no_split": abi.BP_WALK_NO_STAGING | abi.BP_WALK_NO_SPLIT,
+            "staging": 0}[walk]
+    scene = small_mixed_scene(bp, seed=15, fluid=(20, 8, 20), grid_dim=8)
+    outs = []
+    for w in (base, base | abi.BP_WALK_NO_ALIAS_CLASSES):
+        g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=w))
+        walks = g.walk_stats(2, DT, 4)  # a real update
+        if w & abi.BP_WALK_NO_ALIAS_CLASSES:
+            assert walks["alias_classes"] == 0
+        elif walk != "staging":
+            assert walks["alias_classes"] > walks["cells_no_mask"] // 2, walks
+        for _ in range(5):
+            g.update(2, DT, 4)
+        outs.append((g.positions(), g.velocities()))
+        g.close()
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
+def test_alias_classes_parity_on_aliased_grid(bp, gpu, oracle):
+    scene = small_mixed_scene(bp, seed=16, fluid=(20, 8, 20), grid_dim=8)
+    assert_parity(*lockstep(bp, oracle, scene, bp.make_params(scene), substeps=4))
+
+
+def test_alias_classes_fall_back_past_the_reach(bp, gpu):
+    """Particles placed exactly one table period (8 cells, 1.6 m) below the
+    floor: the plane stabilisation lifts them into the table cell they were
+    hashed to, next to the fluid, but their hash-time class is the other one.
+    They moved further than the reach, so the walks take whole table cells
+    and find them; the bits equal those of class-free walks."""
+    abi = bp.abi
+    scene = fluid_scene(bp, (20, 6, 20), seed=23, grid_dim=8, box=(2.5, 3.0, 2.5))
+    x = scene.positions.copy()
+    low = np.argsort(x[:, 1])[:50]
+    x[low, 1] -= np.float32(8 * scene.cell_size)
+    scene.positions = x
+    outs = []
+    for w in (abi.BP_WALK_NO_STAGING, abi.BP_WALK_NO_STAGING | abi.BP_WALK_NO_ALIAS_CLASSES):
+        g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=w))
+        first = g.walk_stats(1, DT / 2, 4)  # a real update: the lift
+        assert first["alias_classes"] == 0, first
+        xs = [g.positions()]
+        later = g.walk_stats(1, DT / 2, 4)  # nothing moves that far now
+        if not w & abi.BP_WALK_NO_ALIAS_CLASSES:
+            assert later["alias_classes"] > 0, later
+        for _ in range(2):
+            g.update(2, DT, 4)
+        outs.append((xs[0], g.positions(), g.velocities()))
+        g.close()
+    assert np.all(outs[0][0][low, 1] > 0.0)  # lifted onto the floor
+    for a, b in zip(outs[0], outs[1]):
+        np.testing.assert_array_equal(a, b)
+
+
 def test_autotune_keeps_state_and_results(bp, gpu):
     """The autotuner's trial updates leave the state as it was, and the variant
     it keeps gives the same bits as the default walk."""
