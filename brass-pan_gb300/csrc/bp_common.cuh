@@ -82,11 +82,14 @@ struct SimConsts {
     float nl_hs2;            // (h + skin)^2
     float nl_half_skin2;     // (skin / 2)^2
     float nl_contact2;       // (2r + skin)^2
-    // Neighbour lists of the velocity post passes, written by pass A and read
-    // by passes B and C (positions do not change between them): for fluid
-    // particle i, nbr[k * n + i] for k < nbr_count[i] are the same-phase j != i
-    // with r^2 <= h^2, in walk order; nbr_count[i] < 0 when they did not fit
-    // in nbr_cap entries (the later passes then walk the cells).
+    // Neighbour lists, written by one pass and read by the following ones at
+    // the same positions: by lambda for the position pass (every j with
+    // r^2 <= h^2), by post pass A for passes B and C (same-phase j != i).
+    // Entry k of particle i is nbr[((k / 4) * n + i) * 4 + k % 4], in walk
+    // order, for k < nbr_count[i]: each group of four is one 16-byte record,
+    // so a warp writes and reads whole records.  nbr_count[i] < 0 when they
+    // did not fit in nbr_cap entries (a multiple of 4; the readers then walk
+    // the cells).
     int *nbr;
     int *nbr_count;
     int nbr_cap;

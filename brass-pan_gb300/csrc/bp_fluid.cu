@@ -20,9 +20,65 @@ namespace bp {
 
 constexpr int kScanThreads = kWalkThreads;  // scan kernels stage their neighbourhood (bp_walk.cuh)
 
+// Records particle i's neighbours (SimConsts::nbr): entries collect in four
+// registers and leave as one 16-byte store per four.
+struct ListWriter {
+    int4 *rec;      // record 0 of particle i; record r at rec[r * n]
+    size_t stride;  // n
+    int cap;
+    int cnt = 0;
+    int4 buf = make_int4(0, 0, 0, 0);
+    __device__ __forceinline__ ListWriter(const SimConsts &C, int i)
+        : rec(reinterpret_cast<int4 *>(C.nbr) + i), stride((size_t)C.n), cap(C.nbr_cap) {}
+    __device__ __forceinline__ void push(int j)
+    {
+        const int q = cnt & 3;
+        buf.x = q == 0 ? j : buf.x;
+        buf.y = q == 1 ? j : buf.y;
+        buf.z = q == 2 ? j : buf.z;
+        buf.w = q == 3 ? j : buf.w;
+        if (q == 3 && cnt < cap) rec[(size_t)(cnt >> 2) * stride] = buf;
+        ++cnt;
+    }
+    // Writes the last partial record; returns the count to store (-1: overflow).
+    __device__ __forceinline__ int finish()
+    {
+        if ((cnt & 3) && cnt < cap) rec[(size_t)(cnt >> 2) * stride] = buf;
+        return cnt <= cap ? cnt : -1;
+    }
+};
+
+// The recorded neighbours of particle i (SimConsts::nbr), in order.  Each
+// record's four indices come in one 16-byte load and their positions are
+// loaded before the first of the four pair terms, so the gathers overlap.
+template <class B>
+__device__ __forceinline__ void for_each_listed(const SimConsts &C, int i, int cnt, const float4 *__restrict__ P,
+                                                B &body)
+{
+    const int4 *__restrict__ rec = reinterpret_cast<const int4 *>(C.nbr) + i;
+    const size_t stride = (size_t)C.n;
+    for (int k = 0; k < cnt; k += 4) {
+        const int4 r = __ldg(rec + (size_t)(k >> 2) * stride);
+        const int m = min(4, cnt - k);
+        const int j[4] = {r.x, r.y, r.z, r.w};
+        float4 pj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (q < m) pj[q] = P[j[q]];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (q < m) body(j[q], pj[q]);
+    }
+}
+
 // Reference mode (Q1): density sums only sorted indices j >= i; solid
 // neighbours count x solid_scale; C = rho/rho0 - 1, clamped at 0 when Akinci
 // is on; lambda = -C / lambda_den.  Textbook mode: all j, exact denominator.
+//
+// With C.nbr (neighbour lists on) the walk also records, for the position
+// pass that reads the same positions, every j with r^2 <= h^2 in walk order
+// (all j, also below i; solids too in reference mode, whose position pass
+// gathers from fluid neighbours).
 template <bool Split, bool Stage>
 __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(SimConsts C, const float4 *__restrict__ P,
                                                          const float *__restrict__ mass,
@@ -35,22 +91,28 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
     const int i = i0 + threadIdx.x;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
-    if (phase_of(pi4) > 0) {  // solids carry lambda 0 (read by the position pass)
-        lam[i] = 0.f;
-        return;
-    }
+    const bool rec = C.nbr != nullptr;
+    const bool solid = phase_of(pi4) > 0;
+    if (solid) lam[i] = 0.f;  // solids carry lambda 0 (read by the position pass)
+    if (solid && (C.textbook || !rec)) return;
     const int sc = scene_index(C, i);
     const GridView v = grid_view(C, sc, off);
     const float rho0 = rest_density(C, sc);
     const float3 pi = f3(pi4);
     float density = 0.f;
+    ListWriter list(C, i);
     if (!C.textbook) {
         walk_neighbors<Split>(
-            i, pi, i, P, v, C, Stage ? &S : nullptr, g, [&](int, float4 pj) { return len2(pi - f3(pj)) <= C.h2; },
+            i, pi, rec ? 0 : i, P, v, C, Stage ? &S : nullptr, g,
+            [&](int, float4 pj) { return len2(pi - f3(pj)) <= C.h2; },
             [&](int j, float4 pj) {
+                if (rec) list.push(j);
+                if (solid || j < i) return;
                 const float ld = __fmul_rn(__ldg(mass + j), poly6(C, len2(pi - f3(pj))));
                 density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
             });
+        if (rec) C.nbr_count[i] = list.finish();
+        if (solid) return;
         float c = density / rho0 - 1.0f;
         if (C.clamp_c) c = fmaxf(c, 0.0f);
         lam[i] = -c / C.lambda_den;
@@ -61,6 +123,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
         walk_neighbors<Split>(
             i, pi, 0, P, v, C, Stage ? &S : nullptr, g, [&](int, float4 pj) { return len2(pi - f3(pj)) <= C.h2; },
             [&](int j, float4 pj) {
+                if (rec) list.push(j);
                 const float3 diff = pi - f3(pj);
                 const float d2 = len2(diff);
                 const float mj = __ldg(mass + j);
@@ -72,6 +135,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
                     gi -= g;
                 }
             });
+        if (rec) C.nbr_count[i] = list.finish();
         float c = density / rho0 - 1.0f;
         if (C.clamp_c) c = fmaxf(c, 0.0f);
         sum_g2 += dot3(gi, gi);
@@ -104,42 +168,56 @@ void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // when a is a fluid particle (only fluid threads run fluidPosition and they
 // only visit b > a), to both ends.  In gather form particle k includes j when
 // the lower-indexed of (k, j) is fluid.  Textbook mode: fluid k gathers over
-// every neighbour; solids do not move.
+// every neighbour; solids do not move.  With C.nbr the neighbours come from
+// the lists k_lambda recorded at the same positions (r^2 <= h^2, walk order);
+// particles whose list overflowed walk their cells.
 template <bool Split, bool Stage>
 __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_deltap(SimConsts C, DeltaArgs a)
 {
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
-    const int g = Stage ? stage_block(C, a.P, a.off, i0, S) : -1;
     const int k = i0 + threadIdx.x;
-    if (k >= C.n) return;
-    const float4 pk4 = a.P[k];
+    const bool valid = k < C.n;
+    const float4 pk4 = valid ? a.P[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int phk = phase_of(pk4);
+    const bool moves = valid && !(C.textbook && phk > 0);
+    const int listed = (moves && C.nbr) ? __ldg(C.nbr_count + k) : -1;
+    const bool walk = moves && listed < 0;
+    const int g = (Stage && __syncthreads_or(walk)) ? stage_block(C, a.P, a.off, i0, S) : -1;
+    if (!valid) return;
     const float3 pk = f3(pk4);
     const int sc = scene_index(C, k);
     float3 sum = make_float3(0.f, 0.f, 0.f);
-    if (!(C.textbook && phk > 0)) {
+    if (moves) {
         const float lk = a.lam[k];
-        walk_neighbors<Split>(
-            k, pk, 0, a.P, grid_view(C, sc, a.off), C, Stage ? &S : nullptr, g,
-            [&](int, float4 pj4) {  // r = 0 excludes k itself
-                const float d2 = len2(pk - f3(pj4));
-                return d2 <= C.h2 && d2 > 0.f;
-            },
-            [&](int j, float4 pj4) {
-                if (!C.textbook && !((j > k) ? (phk < 0) : (phase_of(pj4) < 0))) return;
-                const float3 diff = pk - f3(pj4);
-                const float d2 = len2(diff);
-                float sl = __fadd_rn(lk, __ldg(a.lam + j));
-                if (C.scorr_on)
-                    sl = __fsub_rn(sl, __fmul_rn(C.scorr_k, ipowf(__fmul_rn(poly6(C, d2), C.scorr_inv_wq), C.scorr_ni)));
-                float3 delta = sl * spiky_grad_r(C, diff, d2, rsqrtf(d2));
-                if (C.delta_clamp > 0.f) {  // per-pair clamp; the length is only needed past it
-                    const float l2 = len2(delta);
-                    if (!(l2 < C.delta_clamp2)) delta = delta * __fmul_rn(C.delta_clamp, rsqrtf(l2));
-                }
-                sum = fma3(__ldg(a.mass + j), delta, sum);
-            });
+        auto body = [&](int j, float4 pj4) {
+            if (!C.textbook && !((j > k) ? (phk < 0) : (phase_of(pj4) < 0))) return;
+            const float3 diff = pk - f3(pj4);
+            const float d2 = len2(diff);
+            float sl = __fadd_rn(lk, __ldg(a.lam + j));
+            if (C.scorr_on)
+                sl = __fsub_rn(sl, __fmul_rn(C.scorr_k, ipowf(__fmul_rn(poly6(C, d2), C.scorr_inv_wq), C.scorr_ni)));
+            float3 delta = sl * spiky_grad_r(C, diff, d2, rsqrtf(d2));
+            if (C.delta_clamp > 0.f) {  // per-pair clamp; the length is only needed past it
+                const float l2 = len2(delta);
+                if (!(l2 < C.delta_clamp2)) delta = delta * __fmul_rn(C.delta_clamp, rsqrtf(l2));
+            }
+            sum = fma3(__ldg(a.mass + j), delta, sum);
+        };
+        if (!walk) {
+            auto listed_body = [&](int j, float4 pj4) {  // r = 0 excludes k itself
+                if (len2(pk - f3(pj4)) > 0.f) body(j, pj4);
+            };
+            for_each_listed(C, k, listed, a.P, listed_body);
+        } else {
+            walk_neighbors<Split>(
+                k, pk, 0, a.P, grid_view(C, sc, a.off), C, Stage ? &S : nullptr, g,
+                [&](int, float4 pj4) {  // r = 0 excludes k itself
+                    const float d2 = len2(pk - f3(pj4));
+                    return d2 <= C.h2 && d2 > 0.f;
+                },
+                body);
+        }
     }
     float3 p = pk + sum * inv_rest_density(C, sc);
     if (a.epilogue == 1) {
@@ -244,7 +322,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
     const float3 vi = f3(V[i]);
     float3 om = make_float3(0.f, 0.f, 0.f), nn = make_float3(0.f, 0.f, 0.f);
     const bool want_om = C.use_vort, want_n = C.use_akinci;
-    int cnt = 0;
+    ListWriter list(C, i);
     // the walk takes the passes' common neighbours (r = 0 included, as pass C
     // wants them) and records them for passes B and C
     walk_neighbors<Split>(
@@ -252,8 +330,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
         [&](int, float4 pj4) { return len2(pi - f3(pj4)) <= C.h2; },
         [&](int j, float4 pj4) {
             if (j == i || phase_of(pj4) != phi) return;
-            if (C.nbr && cnt < C.nbr_cap) C.nbr[(size_t)cnt * C.n + i] = j;
-            ++cnt;
+            if (C.nbr) list.push(j);
             const float3 diff = pi - f3(pj4);
             const float d2 = len2(diff);
             if (!(d2 > 0.f)) return;
@@ -261,36 +338,10 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
             if (want_om) om += cross3(f3(V[j]) - vi, g);
             if (want_n) nn = fma3(__frcp_rn(__ldg(rho + j)), g, nn);
         });
-    if (C.nbr) C.nbr_count[i] = cnt <= C.nbr_cap ? cnt : -1;
+    if (C.nbr) C.nbr_count[i] = list.finish();
     Om[i] = make_float4(om.x, om.y, om.z, len3(om));
     const float3 n = C.h * nn;
     Nm[i] = make_float4(n.x, n.y, n.z, rho[i]);
-}
-
-// Passes B and C over the recorded neighbours of particle i, in order.  Four
-// entries at a time: their indices and positions are loaded before the
-// first of the four pair terms, so the dependent gathers overlap.
-template <class B>
-__device__ __forceinline__ void for_each_listed(const SimConsts &C, int i, int cnt, const float4 *__restrict__ P,
-                                                B &body)
-{
-    const int *__restrict__ list = C.nbr + i;
-    const size_t stride = (size_t)C.n;
-    int k = 0;
-    for (; k + 4 <= cnt; k += 4) {
-        int j[4];
-        float4 pj[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) j[q] = __ldg(list + (size_t)(k + q) * stride);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) pj[q] = P[j[q]];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) body(j[q], pj[q]);
-    }
-    for (; k < cnt; ++k) {
-        const int j = __ldg(list + (size_t)k * stride);
-        body(j, P[j]);
-    }
 }
 
 // Passes B and C: the number of recorded neighbours of particle i, or

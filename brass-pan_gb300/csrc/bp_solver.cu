@@ -703,6 +703,14 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         masks_built = true;
     }
 
+    // lambda records each particle's neighbours for the position pass (the
+    // same positions), which then reads them instead of walking cells
+    SimConsts Cf = C;
+    if (!(s->prm.walk_options & BP_WALK_NO_LISTS) && s->nbr) {
+        Cf.nbr = s->nbr;
+        Cf.nbr_count = s->nbr_count;
+        Cf.nbr_cap = kPostListCap;
+    }
     bool planes_done = fuse_first_planes;
     bool committed = false;
     for (int it = 0; it < iterations; ++it) {
@@ -728,7 +736,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         }
         if (fluid) {
             refresh(cur);  // lambda and delta-p read the same positions
-            launch_lambda(st, C, cur, s->mass, s->off, s->lam, s->rho, L);
+            launch_lambda(st, Cf, cur, s->mass, s->off, s->lam, s->rho, L);
             if (tape) {
                 const int aux = tape->snap1(s->lam);
                 tape->snap1(s->rho);
@@ -756,7 +764,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
                     planes_done = true;
                 }
             }
-            launch_deltap(st, C, da, L);
+            launch_deltap(st, Cf, da, L);
             std::swap(cur, other);
         }
         if (distance) {

@@ -82,6 +82,7 @@ struct SubstepTape {
 #define BP_POST_LIST_CAP 192
 #endif
 constexpr int kPostListCap = BP_POST_LIST_CAP;
+static_assert(kPostListCap % 4 == 0, "lists are stored as records of four entries");
 
 // Alias classes are kept for key spaces of at most this many cells (their
 // offsets take 8 entries per cell: 64 MB at 2^21 cells, a 128^3 table).

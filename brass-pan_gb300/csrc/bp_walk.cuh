@@ -33,11 +33,14 @@ namespace bp {
 constexpr int kWalkThreads = 256;
 // Staged particles per CTA (44 KB at 2816) and the CTAs per SM the scan
 // kernels are compiled for (registers per thread <= 65536 / (256 x that)).
+// Four CTAs (64 registers) measured 7 % faster on the mixed scene than the
+// three that the lambda and pass A kernels fall to at their natural 66-71
+// registers; five spill.
 #ifndef BP_STAGE_CAP
 #define BP_STAGE_CAP 2816
 #endif
 #ifndef BP_SCAN_MIN_BLOCKS
-#define BP_SCAN_MIN_BLOCKS 1
+#define BP_SCAN_MIN_BLOCKS 4
 #endif
 constexpr int kStageCap = BP_STAGE_CAP;
 constexpr int kStageSegs = 2 * 9 * 2; // groups x columns x pieces

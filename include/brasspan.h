@@ -82,8 +82,9 @@ typedef enum bp_mode {
  * staging each block's neighbourhood in shared memory; BP_WALK_NO_SPLIT
  * evaluates each pair term as its candidate is tested instead of testing a
  * chunk of candidates first and evaluating the pair terms of the hits;
- * BP_WALK_NO_LISTS makes the second and third velocity post passes walk
- * their cells instead of reading the neighbour lists the first one records;
+ * BP_WALK_NO_LISTS makes the position pass and the second and third
+ * velocity post passes walk their cells instead of reading the neighbour
+ * lists that the lambda pass and the first post pass record;
  * BP_WALK_NO_ALIAS_CLASSES makes unstaged walks test every particle of a
  * table cell instead of only those of the real cell walked (a grid of D^3
  * cells wraps space, so one table cell holds every real cell D cells apart;

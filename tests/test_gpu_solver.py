@@ -222,6 +222,32 @@ def test_walk_variants_are_bit_identical(bp, gpu, walk, skin):
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
+@pytest.mark.parametrize("walk", ["split", "no_split"])
+def test_lists_overflowing_their_capacity_are_bit_identical(bp, gpu, walk):
+    """A block packed at half spacing holds about 270 neighbours within h
+    per particle, past the 192 entries a list takes: those particles walk
+    their cells in the position and post passes, the others read lists, and
+    the bits equal walks everywhere."""
+    abi = bp.abi
+    base = abi.BP_WALK_NO_STAGING | (abi.BP_WALK_NO_SPLIT if walk == "no_split" else 0)
+    scene = fluid_scene(bp, (12, 12, 12), seed=31, grid_dim=32)
+    x = scene.positions.copy()
+    c = x.mean(axis=0)
+    dense = np.all(np.abs(x - c) < 0.35, axis=1)
+    x[dense] = c + (x[dense] - c) * np.float32(0.5)
+    scene.positions = x.astype(np.float32)
+    assert dense.sum() > 200
+    outs = []
+    for w in (base, base | abi.BP_WALK_NO_LISTS):
+        g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=w))
+        for _ in range(3):
+            g.update(2, DT, 4)
+        outs.append((g.positions(), g.velocities()))
+        g.close()
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
 @pytest.mark.parametrize("walk", ["split", "no_split", "staging"])
 def test_alias_classes_are_bit_identical(bp, gpu, walk):
     """An 8^3 table over a 3 x 4 x 3 m box: every table cell holds up to
