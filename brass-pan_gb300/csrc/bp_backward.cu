@@ -278,7 +278,8 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
 {
     const cudaStream_t st = s->stream;
     SimConsts C = u.C;  // the adjoint walks take the 27 cells
-    C.nl_mask = nullptr;
+    C.vl = nullptr;
+    C.nl_pos = nullptr;
     C.nl_stats = nullptr;
     const bp_params &p = u.prm;
     const bool planes = stage_on(p, BP_STAGE_PLANES) && s->nplanes > 0;

@@ -62,26 +62,30 @@ struct SimConsts {
     int split;        // scan kernels test candidates in chunks before the pair terms
     float4 plane_o[kMaxPlanes];
     float4 plane_n[kMaxPlanes];
-    // Neighbour bitmasks of the current substep (nl_mask == nullptr: off).
-    // For each particle and each of its 9 column runs, bit t of the column's
-    // two words marks candidate off[start] + t within h + skin of it at build
-    // time; nl_cell is the cell the masks were built for (-1: the particle
-    // always walks its 27 cells), nl_pos the positions at build.  A masked
-    // walk is taken while the particle is still in nl_cell and within half
-    // the skin of nl_pos; columns holding a particle that moved further are
-    // walked whole (see walk_neighbors).
-    unsigned long long *nl_mask;       // [18][n]: column c uses words 2c and 2c+1 (128 candidates)
+    // Verlet lists of the current substep (vl == nullptr: off).  The first
+    // lambda pass of a substep (vl_build) walks the cells with the radius
+    // h + skin and records, for each particle, every candidate within it in
+    // walk order (records of four, as SimConsts::nbr; vl_count[i] < 0: did not
+    // fit in vl_cap).  nl_cell is the cell the list was built for (-1: the
+    // particle always walks its cells, e.g. its column runs wrap around the
+    // table), nl_pos its position then.  A later walk of the substep reads the
+    // list instead of the cells while the particle is still in nl_cell,
+    // within half the skin of nl_pos, and no particle stored in its 27 cells
+    // moved further (writers of P flag their stored cell in nl_outlier): then
+    // every pair within h now was within h + skin at the build, and the list
+    // yields the walk's hits in the walk's order.
+    int *vl;
+    int *vl_count;
+    int vl_cap;
+    int vl_build;                      // this launch builds the lists
     int *nl_cell;
-    float4 *nl_pos;
+    float4 *nl_pos;                    // nullptr: writers do not track displacements
     unsigned long long *nl_outlier;    // per (x, y) column of cells, nl_zwords words of z bits
     int nl_zwords;                     // ceil(D / 64)
     const int *cell_keys;              // stored cell of every sorted particle
-    unsigned short *nl_flags; // kFlagContact: a contact partner within 2r + skin at build;
-                              // kFlagWide << col: column run col holds more than 64 candidates
-    unsigned *nl_stats;      // profiling only: walks by masks_state
+    unsigned *nl_stats;      // profiling only: walks by list_state, then alias-class walks
     float nl_hs2;            // (h + skin)^2
     float nl_half_skin2;     // (skin / 2)^2
-    float nl_contact2;       // (2r + skin)^2
     // Neighbour lists, written by one pass and read by the following ones at
     // the same positions: by lambda for the position pass (every j with
     // r^2 <= h^2), by post pass A for passes B and C (same-phase j != i).
@@ -126,9 +130,6 @@ __device__ __forceinline__ int alias_class(int x, int y, int z, int D)
     const int sh = __ffs(D) - 1;
     return ((x >> sh) & 1) | (((y >> sh) & 1) << 1) | (((z >> sh) & 1) << 2);
 }
-
-constexpr unsigned short kFlagContact = 1;
-constexpr unsigned short kFlagWide = 2;
 
 // ---- small vector helpers (own code) ----
 // Every operation is an explicitly rounded intrinsic, so the compiler never
@@ -255,7 +256,8 @@ __device__ __forceinline__ float3 gravity_of(const SimConsts &C, int s)
 }
 
 // Is any of the cells (x, y, z0..z0+2) flagged as holding an outlier (a
-// particle that moved more than half the skin since the masks were built)?
+// particle that moved more than half the skin since the lists were built)?
+// z0 + 2 < D: lists are only built where the column runs do not wrap.
 __device__ __forceinline__ bool column_has_outlier(const SimConsts &C, unsigned x, unsigned y, unsigned z0)
 {
     const unsigned long long *w = C.nl_outlier + (size_t)(x * (unsigned)C.D + y) * C.nl_zwords;
@@ -267,41 +269,30 @@ __device__ __forceinline__ bool column_has_outlier(const SimConsts &C, unsigned 
     return (bits & 7ull) != 0ull;
 }
 
-// Does any column run around the cell of p hold an outlier?
-__device__ __forceinline__ bool contact_outlier_near(const SimConsts &C, float3 p)
-{
-    const int3 c = cell_of(p, C);
-    const unsigned m = C.mask;
-    const unsigned z0 = (unsigned)(c.z - 1) & m;
-    for (int col = 0; col < 9; ++col)
-        if (column_has_outlier(C, (unsigned)(c.x + col / 3 - 1) & m, (unsigned)(c.y + col % 3 - 1) & m, z0))
-            return true;
-    return false;
-}
-
-// 0 when particle i may walk its neighbour bitmasks instead of its 27 cells;
-// otherwise why not: 1 no masks for it, 2 it changed cell, 3 it moved more
-// than half the skin since the build (an outlier).
-__device__ __forceinline__ int masks_state(const SimConsts &C, int i, int3 c, float3 pi)
+// 0 when particle i may read its Verlet list instead of walking its 27
+// cells; otherwise why not: 1 no list for it, 2 it changed cell, 3 it, or a
+// particle stored in its 27 cells, moved more than half the skin since the build.
+__device__ __forceinline__ int list_state(const SimConsts &C, int i, int3 c, float3 pi)
 {
     const int built = __ldg(C.nl_cell + i);
     if (built < 0) return 1;
     if (built != cell_addr(c.x, c.y, c.z, C.D, C.mask)) return 2;
     if (len2(pi - f3(C.nl_pos[i])) > C.nl_half_skin2) return 3;
+    const unsigned m = C.mask;
+    const unsigned z0 = (unsigned)(c.z - 1) & m;
+    for (int col = 0; col < 9; ++col)
+        if (column_has_outlier(C, (unsigned)(c.x + col / 3 - 1) & m, (unsigned)(c.y + col % 3 - 1) & m, z0))
+            return 3;
     return 0;
 }
-__device__ __forceinline__ bool masks_usable(const SimConsts &C, int i, int3 c, float3 pi)
-{
-    return C.nl_mask && masks_state(C, i, c, pi) == 0;
-}
 
-// Records that particle i moved more than half the skin since the mask
-// build: flags its stored cell (the cell its sorted index belongs to) so
-// walks over that cell's column take every candidate.  Writers of P call it
+// Records that particle i moved more than half the skin since the list
+// build: flags its stored cell (the cell its sorted index belongs to) so the
+// particles whose 27 cells include it walk their cells.  Writers of P call it
 // with the new position.
 __device__ __forceinline__ void track_displacement(const SimConsts &C, int i, float3 p, bool active)
 {
-    if (!C.nl_mask || !active) return;
+    if (!C.nl_pos || !active) return;
     if (!(len2(p - f3(C.nl_pos[i])) <= C.nl_half_skin2)) {  // NaN counts as moved
         const unsigned key = (unsigned)__ldg(C.cell_keys + i);
         const unsigned col = key / (unsigned)C.D, z = key % (unsigned)C.D;

@@ -178,16 +178,6 @@ __device__ __forceinline__ void collide_one(const SimConsts &C, int i, const flo
     const float3 xip = f3(pi4);
     const int phi = phase_of(pi4);
     const float r = C.radius;
-    // No contact partner within 2r + skin at mask build and the masks still
-    // valid: no pair can be closer than 2r now, the walk would find nothing.
-    const bool none = C.nl_mask && C.nl_flags && !(C.nl_flags[i] & kFlagContact) &&
-                      masks_usable(C, i, cell_of(xip, C), xip) && !contact_outlier_near(C, xip);
-    if (none) {  // p = x + 0, rounded as the walk's result would be
-        const float3 p = xip + make_float3(0.f, 0.f, 0.f);
-        Pout[i] = make_float4(p.x, p.y, p.z, pi4.w);
-        track_displacement(C, i, p, true);
-        return;
-    }
     const float3 xi = f3(Xs[i]);
     const float wi = w[i];
     float3 sd = make_float3(0.f, 0.f, 0.f), sf = make_float3(0.f, 0.f, 0.f);

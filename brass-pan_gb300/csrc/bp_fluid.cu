@@ -20,55 +20,16 @@ namespace bp {
 
 constexpr int kScanThreads = kWalkThreads;  // scan kernels stage their neighbourhood (bp_walk.cuh)
 
-// Records particle i's neighbours (SimConsts::nbr): entries collect in four
-// registers and leave as one 16-byte store per four.
-struct ListWriter {
-    int4 *rec;      // record 0 of particle i; record r at rec[r * n]
-    size_t stride;  // n
-    int cap;
-    int cnt = 0;
-    int4 buf = make_int4(0, 0, 0, 0);
-    __device__ __forceinline__ ListWriter(const SimConsts &C, int i)
-        : rec(reinterpret_cast<int4 *>(C.nbr) + i), stride((size_t)C.n), cap(C.nbr_cap) {}
-    __device__ __forceinline__ void push(int j)
-    {
-        const int q = cnt & 3;
-        buf.x = q == 0 ? j : buf.x;
-        buf.y = q == 1 ? j : buf.y;
-        buf.z = q == 2 ? j : buf.z;
-        buf.w = q == 3 ? j : buf.w;
-        if (q == 3 && cnt < cap) rec[(size_t)(cnt >> 2) * stride] = buf;
-        ++cnt;
-    }
-    // Writes the last partial record; returns the count to store (-1: overflow).
-    __device__ __forceinline__ int finish()
-    {
-        if ((cnt & 3) && cnt < cap) rec[(size_t)(cnt >> 2) * stride] = buf;
-        return cnt <= cap ? cnt : -1;
-    }
-};
-
-// The recorded neighbours of particle i (SimConsts::nbr), in order.  Each
-// record's four indices come in one 16-byte load and their positions are
-// loaded before the first of the four pair terms, so the gathers overlap.
-template <class B>
-__device__ __forceinline__ void for_each_listed(const SimConsts &C, int i, int cnt, const float4 *__restrict__ P,
-                                                B &body)
+// Ends the Verlet list build of particle i (SimConsts::vl): its count, and
+// the cell and position the list holds for (cell -1: no list, because it
+// overflowed or the particle's column runs wrap around the table).
+__device__ __forceinline__ void finish_verlet(const SimConsts &C, int i, float4 pi4, int cnt)
 {
-    const int4 *__restrict__ rec = reinterpret_cast<const int4 *>(C.nbr) + i;
-    const size_t stride = (size_t)C.n;
-    for (int k = 0; k < cnt; k += 4) {
-        const int4 r = __ldg(rec + (size_t)(k >> 2) * stride);
-        const int m = min(4, cnt - k);
-        const int j[4] = {r.x, r.y, r.z, r.w};
-        float4 pj[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (q < m) pj[q] = P[j[q]];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (q < m) body(j[q], pj[q]);
-    }
+    const int3 c = cell_of(f3(pi4), C);
+    const unsigned z0 = (unsigned)(c.z - 1) & C.mask, z2 = (unsigned)(c.z + 1) & C.mask;
+    C.vl_count[i] = cnt;
+    C.nl_pos[i] = pi4;
+    C.nl_cell[i] = (cnt >= 0 && z0 < z2) ? cell_addr(c.x, c.y, c.z, C.D, C.mask) : -1;
 }
 
 // Reference mode (Q1): density sums only sorted indices j >= i; solid
@@ -78,7 +39,8 @@ __device__ __forceinline__ void for_each_listed(const SimConsts &C, int i, int c
 // With C.nbr (neighbour lists on) the walk also records, for the position
 // pass that reads the same positions, every j with r^2 <= h^2 in walk order
 // (all j, also below i; solids too in reference mode, whose position pass
-// gathers from fluid neighbours).
+// gathers from fluid neighbours).  With C.vl_build it records the substep's
+// Verlet lists instead: every j within h + skin.
 template <bool Split, bool Stage>
 __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(SimConsts C, const float4 *__restrict__ P,
                                                          const float *__restrict__ mass,
@@ -91,27 +53,38 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
     const int i = i0 + threadIdx.x;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
-    const bool rec = C.nbr != nullptr;
+    const bool build = C.vl_build != 0;
+    const bool rec = build || C.nbr != nullptr;
     const bool solid = phase_of(pi4) > 0;
     if (solid) lam[i] = 0.f;  // solids carry lambda 0 (read by the position pass)
-    if (solid && (C.textbook || !rec)) return;
+    if (solid && (C.textbook || !rec)) {
+        if (build) C.nl_cell[i] = -1;
+        return;
+    }
     const int sc = scene_index(C, i);
     const GridView v = grid_view(C, sc, off);
     const float rho0 = rest_density(C, sc);
     const float3 pi = f3(pi4);
+    const float r2 = build ? C.nl_hs2 : C.h2;
     float density = 0.f;
-    ListWriter list(C, i);
+    ListWriter list(build ? C.vl : C.nbr, build ? C.vl_cap : C.nbr_cap, C.n, i);
+    auto finish = [&]() {
+        const int cnt = list.finish();
+        if (build) finish_verlet(C, i, pi4, cnt);
+        else C.nbr_count[i] = cnt;
+    };
     if (!C.textbook) {
         walk_neighbors<Split>(
             i, pi, rec ? 0 : i, P, v, C, Stage ? &S : nullptr, g,
-            [&](int, float4 pj) { return len2(pi - f3(pj)) <= C.h2; },
+            [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; },
             [&](int j, float4 pj) {
                 if (rec) list.push(j);
-                if (solid || j < i) return;
-                const float ld = __fmul_rn(__ldg(mass + j), poly6(C, len2(pi - f3(pj))));
+                const float d2 = len2(pi - f3(pj));
+                if (solid || j < i || (build && !(d2 <= C.h2))) return;
+                const float ld = __fmul_rn(__ldg(mass + j), poly6(C, d2));
                 density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
             });
-        if (rec) C.nbr_count[i] = list.finish();
+        if (rec) finish();
         if (solid) return;
         float c = density / rho0 - 1.0f;
         if (C.clamp_c) c = fmaxf(c, 0.0f);
@@ -121,11 +94,12 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
         float sum_g2 = 0.f;
         float3 gi = make_float3(0.f, 0.f, 0.f);
         walk_neighbors<Split>(
-            i, pi, 0, P, v, C, Stage ? &S : nullptr, g, [&](int, float4 pj) { return len2(pi - f3(pj)) <= C.h2; },
+            i, pi, 0, P, v, C, Stage ? &S : nullptr, g, [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; },
             [&](int j, float4 pj) {
                 if (rec) list.push(j);
                 const float3 diff = pi - f3(pj);
                 const float d2 = len2(diff);
+                if (build && !(d2 <= C.h2)) return;
                 const float mj = __ldg(mass + j);
                 const float ld = __fmul_rn(mj, poly6(C, d2));
                 density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
@@ -135,7 +109,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
                     gi -= g;
                 }
             });
-        if (rec) C.nbr_count[i] = list.finish();
+        if (rec) finish();
         float c = density / rho0 - 1.0f;
         if (C.clamp_c) c = fmaxf(c, 0.0f);
         sum_g2 += dot3(gi, gi);
@@ -208,7 +182,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_deltap(Sim
             auto listed_body = [&](int j, float4 pj4) {  // r = 0 excludes k itself
                 if (len2(pk - f3(pj4)) > 0.f) body(j, pj4);
             };
-            for_each_listed(C, k, listed, a.P, listed_body);
+            for_each_in_list(C.nbr, C.n, k, listed, a.P, listed_body);
         } else {
             walk_neighbors<Split>(
                 k, pk, 0, a.P, grid_view(C, sc, a.off), C, Stage ? &S : nullptr, g,
@@ -231,67 +205,6 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_deltap(Sim
     }
     a.Pout[k] = make_float4(p.x, p.y, p.z, pk4.w);
     track_displacement(C, k, p, true);
-}
-
-// Neighbour bitmasks for the rest of the substep (see SimConsts::nl_mask):
-// one 27-cell walk at the positions of the first iteration.  Particles whose
-// column runs wrap around the table in z, or hold more than 128 candidates,
-// keep walking their cells.
-__global__ void __launch_bounds__(kScanThreads) k_build_masks(SimConsts C, const float4 *__restrict__ P,
-                                                              const int *__restrict__ off)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= C.n) return;
-    const float4 pi4 = P[i];
-    const float3 pi = f3(pi4);
-    const int phi = phase_of(pi4);
-    C.nl_pos[i] = pi4;
-    const int3 c = cell_of(pi, C);
-    const unsigned m = C.mask;
-    const unsigned D = (unsigned)C.D;
-    const unsigned z0 = (unsigned)(c.z - 1) & m;
-    const unsigned z2 = (unsigned)(c.z + 1) & m;
-    bool ok = z0 < z2;
-    unsigned short flags = 0;
-    int col = 0;
-#pragma unroll 1
-    for (int dx = -1; dx <= 1; ++dx) {
-        const unsigned bx = ((unsigned)(c.x + dx) & m) * D * D;
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; ++dy, ++col) {
-            unsigned long long bits[2] = {0ull, 0ull};
-            if (ok) {
-                const unsigned base = bx + ((unsigned)(c.y + dy) & m) * D;
-                const int b = __ldg(off + base + z0), e = __ldg(off + base + z2 + 1);
-                if (e - b > 128) {
-                    ok = false;
-                } else {
-                    if (e - b > 64) flags |= (unsigned short)(kFlagWide << col);
-#pragma unroll 1
-                    for (int j = b; j < e; ++j) {
-                        const float4 pj4 = P[j];
-                        const float d2 = len2(pi - f3(pj4));
-                        if (d2 <= C.nl_hs2) bits[(j - b) >> 6] |= 1ull << ((j - b) & 63);
-                        const int phj = phase_of(pj4);
-                        if (d2 <= C.nl_contact2 && j != i && phi != phj && (phi > 0 || phj > 0))
-                            flags |= kFlagContact;
-                    }
-                }
-            }
-            C.nl_mask[(size_t)(2 * col) * C.n + i] = bits[0];
-            C.nl_mask[(size_t)(2 * col + 1) * C.n + i] = bits[1];
-        }
-    }
-    C.nl_cell[i] = ok ? cell_addr(c.x, c.y, c.z, C.D, C.mask) : -1;
-    C.nl_flags[i] = flags;
-}
-
-void launch_build_masks(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, LaunchLog *L)
-{
-    if (C.n <= 0 || !C.nl_mask) return;
-    cudaMemsetAsync(C.nl_outlier, 0, (size_t)C.D * C.D * C.nl_zwords * sizeof(unsigned long long), st);
-    k_build_masks<<<(C.n + kScanThreads - 1) / kScanThreads, kScanThreads, 0, st>>>(C, P, off);
-    L->done(__func__);
 }
 
 void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, LaunchLog *L)
@@ -322,7 +235,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
     const float3 vi = f3(V[i]);
     float3 om = make_float3(0.f, 0.f, 0.f), nn = make_float3(0.f, 0.f, 0.f);
     const bool want_om = C.use_vort, want_n = C.use_akinci;
-    ListWriter list(C, i);
+    ListWriter list(C.nbr, C.nbr_cap, C.n, i);
     // the walk takes the passes' common neighbours (r = 0 included, as pass C
     // wants them) and records them for passes B and C
     walk_neighbors<Split>(
@@ -404,7 +317,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_b(Sim
         }
     };
     if (cnt != kWalkCells) {
-        for_each_listed(C, i, cnt, P, body);
+        for_each_in_list(C.nbr, C.n, i, cnt, P, body);
     } else {
         walk_neighbors<Split>(
             i, pi, 0, P, grid_view(C, sc, off), C, Stage ? &S : nullptr, g,
@@ -450,7 +363,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_c(Sim
         vn = fma3(wgt, f3(V[j]) - vi, vn);
     };
     if (cnt != kWalkCells) {
-        for_each_listed(C, i, cnt, P, body);
+        for_each_in_list(C.nbr, C.n, i, cnt, P, body);
     } else {
         walk_neighbors<Split>(
             i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, Stage ? &S : nullptr, g,

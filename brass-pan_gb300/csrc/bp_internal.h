@@ -133,7 +133,6 @@ struct DeltaArgs {
     int *orig_c;
 };
 void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, LaunchLog *L);
-void launch_build_masks(cudaStream_t st, const SimConsts &C, const float4 *P, const int *off, LaunchLog *L);
 void launch_post_a(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float *rho,
                    const int *off, float4 *Om, float4 *Nm, LaunchLog *L);
 void launch_post_b(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float4 *Om,

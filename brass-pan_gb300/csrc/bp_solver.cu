@@ -114,7 +114,7 @@ static bp_status check_params(const bp_params *p)
 static float class_reach(const bp_solver *s)
 {
     const bp_params &p = s->prm;
-    if (!s->cls.perm || s->tape || p.neighbor_skin > 0.f || (p.walk_options & BP_WALK_NO_ALIAS_CLASSES)) return 0.f;
+    if (!s->cls.perm || s->tape || (p.walk_options & BP_WALK_NO_ALIAS_CLASSES)) return 0.f;
     const float reach = (float)(s->cls_dmin - 2) * p.cell_size - p.kernel_radius - (0.02f + 1e-3f * p.kernel_radius);
     return reach > 0.f ? reach : 0.f;
 }
@@ -178,19 +178,18 @@ SimConsts bp::make_consts(const bp_solver *s, float sdt)
     C.scene_of = s->scene_of;
     C.stage = (p.walk_options & BP_WALK_NO_STAGING) ? 0 : 1;
     C.split = (p.walk_options & BP_WALK_NO_SPLIT) ? 0 : 1;
-    if (p.neighbor_skin > 0.f) {
-        C.nl_mask = s->nl_mask;
+    if (p.neighbor_skin > 0.f && !s->tape && s->vl) {  // Verlet lists (enqueue_substep decides per launch)
+        C.vl = s->vl;
+        C.vl_count = s->vl_count;
+        C.vl_cap = kVerletCap;
         C.nl_cell = s->nl_cell;
         C.nl_pos = s->nl_pos;
         C.nl_outlier = s->nl_outlier;
         C.nl_zwords = (p.grid_dim + 63) / 64;
-        C.nl_flags = s->nl_flags;
         const float hs = h * (1.0f + p.neighbor_skin);
         const float half_skin = 0.5f * h * p.neighbor_skin;
-        const float contact = 2.0f * p.particle_radius + h * p.neighbor_skin;
         C.nl_hs2 = hs * hs;
         C.nl_half_skin2 = half_skin * half_skin;
-        C.nl_contact2 = contact * contact;
     }
     if (class_reach(s) > 0.f) {
         C.cls_perm = s->cls.perm;
@@ -322,7 +321,7 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
     const size_t ncells = batch ? batch->ncells : (size_t)D * D * D;
     s->ncells = ncells;
     s->sort_dim = batch ? batch->sort_dim : D;
-    const size_t NM = batch ? 1 : N;  // neighbour masks: single scenes only
+    const size_t NM = batch ? 1 : N;  // Verlet lists: single scenes only
     if ((st = s->alloc(&s->Xc, N)) || (st = s->alloc(&s->Vc, N)) || (st = s->alloc(&s->Xs, N)) ||
         (st = s->alloc(&s->Vs, N)) || (st = s->alloc(&s->Pa, N)) || (st = s->alloc(&s->Pb, N)) ||
         (st = s->alloc(&s->Om, N)) || (st = s->alloc(&s->Nm, N)) || (st = s->alloc(&s->orig_c, N)) ||
@@ -330,9 +329,9 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         (st = s->alloc(&s->keys, N)) || (st = s->alloc(&s->sorted_keys, N)) || (st = s->alloc(&s->order, N)) ||
         (st = s->alloc(&s->off, ncells + 1)) || (st = s->alloc(&s->mass, N)) || (st = s->alloc(&s->lam, N)) ||
         (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)) ||
-        (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->nl_mask, NM * 18)) ||
+        (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->vl, NM * kVerletCap)) ||
         (st = s->alloc(&s->nl_cell, NM)) || (st = s->alloc(&s->nl_pos, NM)) || (st = s->alloc(&s->nl_outlier, (size_t)D * D * ((D + 63) / 64))) ||
-        (st = s->alloc(&s->nl_flags, NM)) || (st = s->alloc(&s->nl_stats, 5)))
+        (st = s->alloc(&s->vl_count, NM)) || (st = s->alloc(&s->nl_stats, 5)))
         return bail(st);
     {
         char *scratch = nullptr;
@@ -510,7 +509,7 @@ extern "C" bp_status bp_batch_create(int32_t num_scenes, const bp_scene_desc *sc
             return fail(BP_ERR_INVALID_ARGUMENT,
                         "scenes of a batch differ only in rest_density, gravity and grid_dim");
         if (params[k].neighbor_skin > 0.f)
-            return fail(BP_ERR_INVALID_ARGUMENT, "neighbour masks (neighbor_skin > 0) are not available in a batch");
+            return fail(BP_ERR_INVALID_ARGUMENT, "Verlet lists (neighbor_skin > 0) are not available in a batch");
         spec.first[k] = (int)total;
         total += scenes[k].num_particles;
         if (total > (1 << 28)) return fail(BP_ERR_CAPACITY, "a batch holds at most 2^28 particles");
@@ -620,7 +619,7 @@ extern "C" bp_status bp_solver_set_params(bp_solver *s, const bp_params *prm)
     if (s->num_scenes > 0) {
         // a batch keeps each scene's grid, rest density and gravity from creation
         if (prm->neighbor_skin > 0.f)
-            return fail(BP_ERR_INVALID_ARGUMENT, "neighbour masks (neighbor_skin > 0) are not available in a batch");
+            return fail(BP_ERR_INVALID_ARGUMENT, "Verlet lists (neighbor_skin > 0) are not available in a batch");
         const int D = s->prm.grid_dim;
         s->prm = *prm;
         s->prm.grid_dim = D;
@@ -688,55 +687,59 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     if (tape) tape->vs_slot = tape->snap4(s->Vs);
 
     float4 *cur = s->Pa, *other = s->Pb;
-    // the sorted order is fixed for the substep: compact its solids once
-    if (pcoll) launch_solid_list(st, s->n, cur, s->solid_totals, s->solid_prefix, s->solid_list, L);
-    if (wind) {
-        if (tape) tape->push(TS_WIND, cur);
-        launch_wind(st, C, s->wind, cur, s->Vs, s->mass, s->to_new, L);
-    }
-    // masks are built at the positions the first scan sees: after the wind
-    // and iteration 0's plane collision, which move particles the most
-    const bool scans = pcoll || fluid || C.use_vort || C.use_akinci || C.use_xsph;
-    bool masks_built = !(scans && C.nl_mask);
-    if (!masks_built && (fuse_first_planes || !planes || iterations == 0)) {
-        launch_build_masks(st, C, cur, s->off, L);
-        masks_built = true;
-    }
-
-    // lambda records each particle's neighbours for the position pass (the
-    // same positions), which then reads them instead of walking cells
-    SimConsts Cf = C;
-    if (!(s->prm.walk_options & BP_WALK_NO_LISTS) && s->nbr) {
+    // Verlet lists (SimConsts::vl): iteration 0's lambda builds them and every
+    // later walk of the substep may read them; the kernels before the build
+    // neither read them nor track displacements.
+    const bool verlet = C.vl != nullptr && fluid && iterations > 0;
+    SimConsts Cpre = C;
+    Cpre.vl = nullptr;
+    Cpre.nl_pos = nullptr;
+    const SimConsts &Cpost = verlet ? C : Cpre;
+    // Without them lambda records each particle's neighbours within h for the
+    // position pass (the same positions), which then reads them instead of
+    // walking cells.
+    const bool lists = !(s->prm.walk_options & BP_WALK_NO_LISTS) && s->nbr;
+    SimConsts Cf = Cpost;
+    if (lists && !verlet) {
         Cf.nbr = s->nbr;
         Cf.nbr_count = s->nbr_count;
         Cf.nbr_cap = kPostListCap;
     }
+    SimConsts Cbuild = Cf;
+    Cbuild.vl_build = verlet ? 1 : 0;
+
+    // the sorted order is fixed for the substep: compact its solids once
+    if (pcoll) launch_solid_list(st, s->n, cur, s->solid_totals, s->solid_prefix, s->solid_list, L);
+    if (wind) {
+        if (tape) tape->push(TS_WIND, cur);
+        launch_wind(st, Cpre, s->wind, cur, s->Vs, s->mass, s->to_new, L);
+    }
+
     bool planes_done = fuse_first_planes;
     bool committed = false;
     for (int it = 0; it < iterations; ++it) {
+        const SimConsts &Cit = it == 0 ? Cpre : Cpost;  // stages before lambda
         if (picking) launch_pick(st, picked, s->to_new, cur, ppos, 1, nullptr, make_float3(0.f, 0.f, 0.f), L);
         if (planes && !planes_done) {
             if (tape) tape->push(TS_PLANES, cur);
-            launch_planes(st, C, s->Xs, cur, L);
+            launch_planes(st, Cit, s->Xs, cur, L);
         }
         planes_done = false;
-        if (!masks_built) {
-            launch_build_masks(st, C, cur, s->off, L);
-            masks_built = true;
-        }
         if (pcoll) {
             if (tape) tape->push(TS_PCOLL, cur);
             // solids walk in a launch of their own, in full warps (measured
             // faster than walking them in the staged CTAs, whether solids are
             // scattered through fluid or the whole scene)
             refresh(cur);
-            launch_particle_collision(st, C, cur, s->Xs, s->w, s->off, s->tile_solid, s->solid_prefix, s->solid_list,
-                                      s->num_solids, true, other, L);
+            launch_particle_collision(st, Cit, cur, s->Xs, s->w, s->off, s->tile_solid, s->solid_prefix,
+                                      s->solid_list, s->num_solids, true, other, L);
             std::swap(cur, other);
         }
         if (fluid) {
             refresh(cur);  // lambda and delta-p read the same positions
-            launch_lambda(st, Cf, cur, s->mass, s->off, s->lam, s->rho, L);
+            if (verlet && it == 0)
+                cudaMemsetAsync(s->nl_outlier, 0, (size_t)C.D * C.D * C.nl_zwords * sizeof(unsigned long long), st);
+            launch_lambda(st, it == 0 ? Cbuild : Cf, cur, s->mass, s->off, s->lam, s->rho, L);
             if (tape) {
                 const int aux = tape->snap1(s->lam);
                 tape->snap1(s->rho);
@@ -769,21 +772,21 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         }
         if (distance) {
             if (tape) tape->push(TS_DISTANCE, cur);
-            launch_distance(st, C, s->dist, cur, s->w, s->to_new, s->err, L);
+            launch_distance(st, Cpost, s->dist, cur, s->w, s->to_new, s->err, L);
         }
         if (rigid) {
             if (tape) tape->push(TS_SHAPE, cur);
-            launch_shape_matching(st, C, s->rigid, cur, s->to_new, L);
+            launch_shape_matching(st, Cpost, s->rigid, cur, s->to_new, L);
             if (tape) tape->recs.back().aux = tape->snap4(s->rigid.rot, (size_t)s->rigid.num_bodies);
         }
         if (immov) {
             if (tape) tape->push(TS_IMMOVABLE, cur);
-            launch_immovable(st, C, s->nimm, s->imm, s->to_new, s->Xs, cur, L);
+            launch_immovable(st, Cpost, s->nimm, s->imm, s->to_new, s->Xs, cur, L);
         }
     }
     if (!committed) {
         if (tape) tape->push(TS_COMMIT, cur);
-        launch_commit(st, C, cur, s->Xs, s->Vs, s->orig_s, s->Xc, s->Vc, s->orig_c, L);
+        launch_commit(st, Cpost, cur, s->Xs, s->Vs, s->orig_s, s->Xc, s->Vc, s->orig_c, L);
     }
     s->Pcur = cur;
 
@@ -793,8 +796,8 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     if (post_ab || C.use_xsph) refresh(cur);  // the post passes read the same positions
     if (post_ab) {
         // pass A records each fluid particle's neighbours for passes B and C
-        SimConsts Cl = C;
-        if (!(s->prm.walk_options & BP_WALK_NO_LISTS)) {
+        SimConsts Cl = Cpost;
+        if (lists) {
             Cl.nbr = s->nbr;
             Cl.nbr_count = s->nbr_count;
             Cl.nbr_cap = kPostListCap;
@@ -803,7 +806,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         launch_post_b(st, Cl, cur, s->Vc, s->Om, s->Nm, s->off, C.use_xsph ? s->Vs : s->Vc, L);
         if (C.use_xsph) launch_post_c(st, Cl, cur, s->Vs, s->off, s->mass, s->rho, s->Vc, L);
     } else if (C.use_xsph) {
-        launch_post_c(st, C, cur, s->Vc, s->off, s->mass, s->rho, s->Vs, L);
+        launch_post_c(st, Cpost, cur, s->Vc, s->off, s->mass, s->rho, s->Vs, L);
         cudaMemcpyAsync(s->Vc, s->Vs, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
     }
 }
@@ -813,7 +816,10 @@ static bp_status enqueue_update(bp_solver *s, int nsub, float dt, int iterations
 {
     const float sdt = dt / (float)nsub;
     SimConsts C = make_consts(s, sdt);
-    if (picked >= 0) C.nl_mask = nullptr;  // the picked particle teleports: walk the cells
+    if (picked >= 0) {  // the picked particle teleports: walk the cells
+        C.vl = nullptr;
+        C.nl_pos = nullptr;
+    }
     if (walk_stats) C.nl_stats = s->nl_stats;
     for (int k = 0; k < nsub; ++k) enqueue_substep(s, C, iterations, picked, ppos, L);
     if (picked >= 0) launch_pick(s->stream, picked, s->to_new, s->Xc, ppos, 0, s->Vc, pvel, L);

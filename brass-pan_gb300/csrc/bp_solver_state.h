@@ -84,6 +84,11 @@ struct SubstepTape {
 constexpr int kPostListCap = BP_POST_LIST_CAP;
 static_assert(kPostListCap % 4 == 0, "lists are stored as records of four entries");
 
+// Entries of a Verlet list (candidates within h + skin): about 1.3x the
+// neighbours within h at a skin of 0.1 h (particles beyond it walk their cells).
+constexpr int kVerletCap = 256;
+static_assert(kVerletCap % 4 == 0, "lists are stored as records of four entries");
+
 // Alias classes are kept for key spaces of at most this many cells (their
 // offsets take 8 entries per cell: 64 MB at 2^21 cells, a 128^3 table).
 constexpr size_t kClassMaxCells = size_t(1) << 21;
@@ -106,11 +111,10 @@ struct bp_solver {
     int *keys = nullptr, *sorted_keys = nullptr, *order = nullptr, *off = nullptr;
     float *mass = nullptr, *lam = nullptr, *rho = nullptr, *w = nullptr;
     float *staging = nullptr;  // 2 x N x 3 floats for host copies
-    unsigned long long *nl_mask = nullptr;  // neighbour masks [18][N]
+    int *vl = nullptr, *vl_count = nullptr;  // Verlet lists [kVerletCap][N] (records of four), counts
     int *nl_cell = nullptr;
     float4 *nl_pos = nullptr;
     unsigned long long *nl_outlier = nullptr;  // outlier cell bits [D*D][ceil(D/64)]
-    unsigned short *nl_flags = nullptr;
     unsigned *nl_stats = nullptr;
     unsigned *err = nullptr;
     int *tile_solid = nullptr;  // per 256 sorted particles: the tile holds a solid

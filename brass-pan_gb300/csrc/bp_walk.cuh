@@ -12,9 +12,9 @@
 // global memory instead.
 //
 // Every walk visits the candidates of the 27 cells column by column, in
-// ascending sorted index within a column, or the subset of them flagged in
-// the particle's neighbour masks (see SimConsts::nl_mask); the pair sums of
-// the scan kernels therefore accumulate in the same order on every path.
+// ascending sorted index within a column, or the subset of them recorded in
+// the particle's Verlet list (see SimConsts::vl); the pair sums of the scan
+// kernels therefore accumulate in the same order on every path.
 //
 // A walk takes two functions: test(j, pj), the cheap pair filter (distance,
 // phases), and body(j, pj), the pair term.  Split walks first test a chunk of
@@ -214,6 +214,60 @@ __device__ __forceinline__ void walk_run(int jb, int b, int e, const float4 *src
     }
 }
 
+// A neighbour list in records of four (SimConsts::nbr, SimConsts::vl): entry
+// k of particle i is base[((k / 4) * n + i) * 4 + k % 4].  The writer keeps
+// the current record in registers and stores each full one with a single
+// 16-byte store, so a warp writes whole records.
+struct ListWriter {
+    int4 *rec;      // record 0 of particle i; record r at rec[r * n]
+    size_t stride;  // n
+    int cap;        // a multiple of 4
+    int cnt = 0;
+    int4 buf = make_int4(0, 0, 0, 0);
+    __device__ __forceinline__ ListWriter(int *base, int cap_, int n, int i)
+        : rec(reinterpret_cast<int4 *>(base) + i), stride((size_t)n), cap(cap_) {}
+    __device__ __forceinline__ void push(int j)
+    {
+        const int q = cnt & 3;
+        buf.x = q == 0 ? j : buf.x;
+        buf.y = q == 1 ? j : buf.y;
+        buf.z = q == 2 ? j : buf.z;
+        buf.w = q == 3 ? j : buf.w;
+        if (q == 3 && cnt < cap) rec[(size_t)(cnt >> 2) * stride] = buf;
+        ++cnt;
+    }
+    // Writes the last partial record; returns the count to store (-1: overflow).
+    __device__ __forceinline__ int finish()
+    {
+        if ((cnt & 3) && cnt < cap) rec[(size_t)(cnt >> 2) * stride] = buf;
+        return cnt <= cap ? cnt : -1;
+    }
+};
+
+// The cnt entries of particle i's list, in order: f(j, P[j]).  Each record's
+// four indices come in one 16-byte load and their positions are loaded
+// before the first of the four calls, so the gathers overlap.
+template <class F>
+__device__ __forceinline__ void for_each_in_list(const int *base, int n, int i, int cnt,
+                                                 const float4 *__restrict__ P, F &&f)
+{
+    const int4 *__restrict__ rec = reinterpret_cast<const int4 *>(base) + i;
+    const size_t stride = (size_t)n;
+#pragma unroll 1
+    for (int k = 0; k < cnt; k += 4) {
+        const int4 r = __ldg(rec + (size_t)(k >> 2) * stride);
+        const int m = min(4, cnt - k);
+        const int j[4] = {r.x, r.y, r.z, r.w};
+        float4 pj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (q < m) pj[q] = P[j[q]];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (q < m) f(j[q], pj[q]);
+    }
+}
+
 // Candidates [qb, e) of one (class, cell) run in class order, read from
 // C.cls_pos.  test() sees a stand-in index that equals i only for particle i
 // itself (tests compare it with i and nothing else); the body gets the sorted
@@ -295,8 +349,8 @@ __device__ __forceinline__ void walk_classes(int i, int3 c, int lo, const GridVi
 // Walk of particle i (sorted index) at position pi over the candidates
 // j >= lo of its 27 cells on grid v: body(j, P[j]) for every j with
 // test(j, P[j]).  S / g come from stage_block (S == nullptr or g < 0: no
-// staging).  Masked walks take each column's set bits in ascending order; a
-// column holding an outlier is walked whole.  The pair arithmetic of the
+// staging).  A particle whose Verlet list is valid (list_state) tests the
+// list's entries instead, in their recorded (walk) order.  The pair arithmetic of the
 // callers uses explicitly rounded operations, so every inlined copy of the
 // pair functions produces the same bits.
 template <bool Split, class T, class B>
@@ -309,46 +363,16 @@ __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const f
     const unsigned D = (unsigned)v.D;
     const int *__restrict__ off = v.off;
     const bool staged = walks_staged(C, v, i, c, S, g);
-    const int state = C.nl_mask ? masks_state(C, i, c, pi) : 1;
+    const int state = (C.vl && !C.vl_build) ? list_state(C, i, c, pi) : 1;
     if (C.nl_stats) atomicAdd(C.nl_stats + state, 1u);
-    const unsigned z0 = (unsigned)(c.z - 1) & m;
-    const unsigned z2 = (unsigned)(c.z + 1) & m;
-
-    if (state == 0) {  // masks are never built for particles whose column runs wrap
-        const unsigned wide = __ldg(C.nl_flags + i);
-#pragma unroll 1
-        for (int col = 0; col < 9; ++col) {
-            const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
-            const unsigned base = x * D * D + y * D + z0;
-            const int cb = __ldg(off + base);
-            const int ce = __ldg(off + base + 3);
-            unsigned long long w[2];
-            if (column_has_outlier(C, x, y, z0)) {
-                const int len = ce - cb;  // <= 128: the masks were built
-                w[0] = len >= 64 ? ~0ull : ((1ull << len) - 1ull);
-                w[1] = len > 64 ? (len >= 128 ? ~0ull : ((1ull << (len - 64)) - 1ull)) : 0ull;
-            } else {
-                w[0] = __ldg(C.nl_mask + (size_t)(2 * col) * C.n + i);
-                w[1] = (wide & (kFlagWide << col)) ? __ldg(C.nl_mask + (size_t)(2 * col + 1) * C.n + i) : 0ull;
-            }
-            if (!(w[0] | w[1])) continue;
-            const int sidx = staged ? staged_index(*S, g, col, cb, ce) : -1;
-            const float4 *src = sidx >= 0 ? S->pos + sidx : P + cb;
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                unsigned long long bits = w[k];
-                const int wb = cb + 64 * k;
-                if (lo > wb) bits = (lo - wb >= 64) ? 0ull : bits & (~0ull << (lo - wb));
-                while (bits) {
-                    const int t = 64 * k + __ffsll((long long)bits) - 1;
-                    bits &= bits - 1;
-                    const float4 pj = src[t];
-                    if (test(cb + t, pj)) body(cb + t, pj);
-                }
-            }
-        }
+    if (state == 0) {  // four entries at a time (measured faster than testing chunks first)
+        for_each_in_list(C.vl, C.n, i, __ldg(C.vl_count + i), P, [&](int j, float4 pj) {
+            if (j >= lo && test(j, pj)) body(j, pj);
+        });
         return;
     }
+    const unsigned z0 = (unsigned)(c.z - 1) & m;
+    const unsigned z2 = (unsigned)(c.z + 1) & m;
 
     if (C.cls_perm && !staged && __ldg(C.cls_moved) == 0) {
         if (C.nl_stats) atomicAdd(C.nl_stats + 4, 1u);

@@ -148,7 +148,7 @@ class ParticleSolver:
         """One real update counting the neighbour walks of all scan passes by kind."""
         out = (C.c_uint64 * 5)()
         abi.check(self.lib, self.lib.bp_solver_walk_stats(self.handle, num_substeps, C.c_float(dt), iterations, out))
-        return {"masked": int(out[0]), "cells_no_mask": int(out[1]), "cells_moved_cell": int(out[2]),
+        return {"listed": int(out[0]), "cells_no_list": int(out[1]), "cells_moved_cell": int(out[2]),
                 "cells_displaced": int(out[3]), "alias_classes": int(out[4])}
 
     def autotune(self, num_substeps: int, dt: float, iterations: int) -> tuple[int, list[float]]:

@@ -124,7 +124,7 @@ typedef struct bp_params {
     float wind_drag;             /* 10 (wind.cuh:40) */
     float wind_lift;             /* 100 (wind.cuh:43) */
     int32_t rotation_iterations; /* 20 (shapematching.cuh:72) */
-    float neighbor_skin;         /* skin of the per-substep neighbour masks, as a fraction of h
+    float neighbor_skin;         /* skin of the per-substep Verlet lists, as a fraction of h
                                     (0 disables them; results are identical either way): 0 */
     int32_t walk_options;        /* BP_WALK_* tuning switches of the neighbour walks: BP_WALK_NO_STAGING */
     int32_t reserved[6];
@@ -247,11 +247,12 @@ bp_status bp_solver_profile(bp_solver *s, int32_t num_substeps, float dt, int32_
                             int32_t capacity, bp_stage_time *out, int32_t *count);
 
 /* One real update that also counts the neighbour walks of every scan pass:
- * out_walks[0] walks over the per-substep neighbour masks; 27-cell walks
- * because [1] no mask was built for the particle (a column run wraps around
- * the table or holds more than 64 candidates), [2] the particle left the cell
- * its masks were built for, [3] some particle moved more than half the skin;
- * [4] of the walks counted in [1], those restricted to the alias classes. */
+ * out_walks[0] walks over the per-substep Verlet lists; 27-cell walks
+ * because [1] no list was built for the particle (lists are off, the pass
+ * builds them, its column runs wrap around the table, or its list held more
+ * than 256 candidates), [2] the particle left the cell its list was built
+ * for, [3] it or a particle stored in its 27 cells moved more than half the
+ * skin; [4] of the cell walks, those restricted to the alias classes. */
 bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
                                uint64_t out_walks[5]);
 
@@ -303,7 +304,7 @@ bp_status bp_solver_tape_end(bp_solver *s);
  * of their particles: each scene keeps its own hash grid (params[k].grid_dim)
  * inside one shared key space, its own rest density, gravity and planes, and
  * every other parameter is shared (params[k] may differ from params[0] only
- * in rest_density, gravity and grid_dim; neighbour masks are not available).
+ * in rest_density, gravity and grid_dim; Verlet lists are not available).
  * Scene k's particles, stepped in a batch, follow exactly the trajectory a
  * solver of scene k alone gives.
  *

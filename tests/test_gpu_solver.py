@@ -181,17 +181,22 @@ def test_runs_are_bitwise_deterministic(bp, gpu):
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
-@pytest.mark.parametrize("skin", [0.1, 0.02, 0.001])
-def test_neighbor_masks_are_bit_identical_to_cell_walks(bp, gpu, skin):
-    """The per-substep neighbour masks (any skin, including one so small that
-    the displacement guard falls back to cell walks mid-substep) give exactly
-    the results of walking the 27 cells."""
+@pytest.mark.parametrize("skin", [0.3, 0.1, 0.02, 0.001])
+def test_verlet_lists_are_bit_identical_to_cell_walks(bp, gpu, skin):
+    """The per-substep Verlet lists (any skin, including one so small that
+    the displacement guard sends most walks back to the cells mid-substep)
+    give exactly the results of walking the 27 cells."""
     scene = small_mixed_scene(bp, seed=13)
     outs = []
     for s in (0.0, skin):
         g = bp.ParticleSolver(scene, bp.make_params(scene, neighbor_skin=s))
         assert g.params.neighbor_skin == np.float32(s)
-        for _ in range(4):
+        walks = g.walk_stats(2, DT, 4)  # a real update
+        if s >= 0.1:
+            assert walks["listed"] > walks["cells_displaced"], walks
+        if s == 0.001:
+            assert walks["cells_displaced"] > 0, walks
+        for _ in range(3):
             g.update(2, DT, 4)
         outs.append((g.positions(), g.velocities()))
         g.close()
@@ -222,12 +227,13 @@ def test_walk_variants_are_bit_identical(bp, gpu, walk, skin):
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
+@pytest.mark.parametrize("skin", [0.0, 0.1])
 @pytest.mark.parametrize("walk", ["split", "no_split"])
-def test_lists_overflowing_their_capacity_are_bit_identical(bp, gpu, walk):
+def test_lists_overflowing_their_capacity_are_bit_identical(bp, gpu, walk, skin):
     """A block packed at half spacing holds about 270 neighbours within h
-    per particle, past the 192 entries a list takes: those particles walk
-    their cells in the position and post passes, the others read lists, and
-    the bits equal walks everywhere."""
+    per particle, past the 192 entries a list takes (and the 256 of a Verlet
+    list): those particles walk their cells, the others read lists, and the
+    bits equal walks everywhere."""
     abi = bp.abi
     base = abi.BP_WALK_NO_STAGING | (abi.BP_WALK_NO_SPLIT if walk == "no_split" else 0)
     scene = fluid_scene(bp, (12, 12, 12), seed=31, grid_dim=32)
@@ -238,8 +244,8 @@ def test_lists_overflowing_their_capacity_are_bit_identical(bp, gpu, walk):
     scene.positions = x.astype(np.float32)
     assert dense.sum() > 200
     outs = []
-    for w in (base, base | abi.BP_WALK_NO_LISTS):
-        g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=w))
+    for w, sk in ((base, skin), (base | abi.BP_WALK_NO_LISTS, 0.0)):
+        g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=w, neighbor_skin=sk))
         for _ in range(3):
             g.update(2, DT, 4)
         outs.append((g.positions(), g.velocities()))
@@ -264,7 +270,7 @@ def test_alias_classes_are_bit_identical(bp, gpu, walk):
         if w & abi.BP_WALK_NO_ALIAS_CLASSES:
             assert walks["alias_classes"] == 0
         elif walk != "staging":
-            assert walks["alias_classes"] > walks["cells_no_mask"] // 2, walks
+            assert walks["alias_classes"] > walks["cells_no_list"] // 2, walks
         for _ in range(5):
             g.update(2, DT, 4)
         outs.append((g.positions(), g.velocities()))
