@@ -36,7 +36,8 @@ BP_STAGE_IMMOVABLE = 0x040
 BP_STAGE_VORTICITY = 0x080
 BP_STAGE_AKINCI = 0x100
 BP_STAGE_XSPH = 0x200
-BP_STAGE_ALL = 0x3FF
+BP_STAGE_BENDING = 0x400
+BP_STAGE_ALL = 0x7FF
 BP_STAGE_REFERENCE_AS_SHIPPED = BP_STAGE_PLANES | BP_STAGE_VORTICITY | BP_STAGE_AKINCI | BP_STAGE_XSPH
 
 BP_ORDER_SORTED = 0
@@ -83,7 +84,8 @@ class BpParams(C.Structure):
         ("rotation_iterations", C.c_int32),
         ("neighbor_skin", C.c_float),
         ("walk_options", C.c_int32),
-        ("reserved", C.c_int32 * 6),
+        ("bending_stiffness", C.c_float),
+        ("reserved", C.c_int32 * 5),
     ]
 
 
@@ -107,6 +109,8 @@ class BpSceneDesc(C.Structure):
         ("rigid_rest_positions", C.POINTER(C.c_float)),
         ("num_immovables", C.c_int32),
         ("immovables", C.POINTER(C.c_int32)),
+        ("num_bendings", C.c_int32),
+        ("bendings", C.POINTER(C.c_int32)),
     ]
 
 
@@ -168,6 +172,9 @@ def scene_desc(scene) -> tuple[BpSceneDesc, list]:
     d.rigid_rest_positions = _fptr(f32(scene.rigid_rest)) if len(scene.rigid_ranges) else None
     d.num_immovables = int(len(scene.immovables))
     d.immovables = _iptr(i32(scene.immovables)) if len(scene.immovables) else None
+    bendings = getattr(scene, "bendings", None)
+    d.num_bendings = int(len(bendings)) if bendings is not None else 0
+    d.bendings = _iptr(i32(bendings)) if d.num_bendings else None
     return d, keep
 
 

@@ -231,6 +231,8 @@ bp_status check_supported(const bp_solver *s, const Tape &t)
             return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: particle collisions have no adjoint");
         if (stage_on(p, BP_STAGE_VORTICITY) || stage_on(p, BP_STAGE_AKINCI))
             return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: vorticity and Akinci tension have no adjoint");
+        if (stage_on(p, BP_STAGE_BENDING) && s->bend.num_quads > 0)
+            return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: dihedral bending has no adjoint");
         if (p.mode == BP_MODE_TEXTBOOK && (stage_on(p, BP_STAGE_FLUID) || stage_on(p, BP_STAGE_XSPH)))
             return fail_with(BP_ERR_INVALID_ARGUMENT,
                              "backward: the fluid and XSPH adjoints are for reference-mode parameters");

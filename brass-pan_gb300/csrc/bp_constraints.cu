@@ -5,6 +5,7 @@
 //   updateVelocity + updatePositions (particlesolver.cuh:71-81,121-137) -> k_commit
 //   particleParticleCollisionConstraint (K/particleparticle.cuh:5-101) -> k_particle_collision
 //   distanceConstraints (K/distance.cuh:3-40) -> k_distance_edges + k_distance_apply
+//   bendingConstraints (K/bending.cuh:3-75)   -> k_bending_terms + k_bending_apply
 //   applyWindForce (K/wind.cuh:3-50) -> k_wind_faces + k_wind_apply
 //   shapeMatchingAlphaOne (K/shapematching.cuh:8-99) -> k_shape_matching (any body size)
 //   immovableConstraints (K/immovable.cuh:3-14) -> k_immovable
@@ -350,6 +351,88 @@ void launch_distance(cudaStream_t st, const SimConsts &C, const DistanceArgs &a,
     k_distance_apply<<<(a.num_nodes + 255) / 256, 256, 0, st>>>(C, a.num_nodes, a.node_ids, a.node_ptr, a.node_inc,
                                                                 a.edge_k, w, to_new, P);
     L->done("k_distance_apply");
+}
+
+// ---- dihedral bending ----
+
+// bendingConstraints (K/bending.cuh:3-75): the dihedral angle of the two
+// triangles (1, 2, 3) and (1, 2, 4) over the hinge 1-2 is pulled towards pi
+// (flat) with the gradients of Mueller et al., Position Based Dynamics (2007),
+// appendix A, in the reference's sequence of operations.  One thread per quad
+// writes the four corrections; degenerate quads (a triangle normal or the
+// denominator below 1e-5) write zeros, as the reference skips them.
+__global__ void k_bending_terms(int nq, const int4 *__restrict__ quads, const float4 *__restrict__ P,
+                                const float *__restrict__ w, const int *__restrict__ to_new, float kb,
+                                float4 *__restrict__ terms)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const int4 ids = quads[q];
+    const int i1 = to_new[ids.x], i2 = to_new[ids.y], i3 = to_new[ids.z], i4 = to_new[ids.w];
+    float4 *out = terms + 4 * (size_t)q;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float3 p1 = f3(P[i1]);
+    const float3 e = f3(P[i2]) - p1, a = f3(P[i3]) - p1, b = f3(P[i4]) - p1;
+    const float3 ca = cross3(e, a), cb = cross3(e, b);
+    const float la = len3(ca), lb = len3(cb);
+    if (la <= 1e-5f || lb <= 1e-5f) {
+        out[0] = out[1] = out[2] = out[3] = zero;
+        return;
+    }
+    const float3 n1 = ca * __fdiv_rn(1.0f, la), n2 = cb * __fdiv_rn(1.0f, lb);
+    const float d = fminf(fmaxf(dot3(n1, n2), -1.0f), 1.0f);
+    const float3 en1 = cross3(e, n1), en2 = cross3(e, n2);
+    const float3 an1 = cross3(a, n1), an2 = cross3(a, n2);
+    const float3 bn1 = cross3(b, n1), bn2 = cross3(b, n2);
+    const float3 q3 = (en2 - en1 * d) / la;
+    const float3 q4 = (en1 - en2 * d) / lb;
+    const float3 q2 = -((an2 - an1 * d) / la) - (bn1 - bn2 * d) / lb;
+    const float3 q1 = (-q2 - q3) - q4;
+    const float w1 = w[i1], w2 = w[i2], w3 = w[i3], w4 = w[i4];
+    const float den = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(w1, len2(q1)), __fmul_rn(w2, len2(q2))),
+                                          __fmul_rn(w3, len2(q3))),
+                                __fmul_rn(w4, len2(q4)));
+    const float num = __fmul_rn(__fsqrt_rn(__fsub_rn(1.0f, __fmul_rn(d, d))), __fsub_rn(acosf(d), 3.141592f));
+    if (den <= 1e-5f) {
+        out[0] = out[1] = out[2] = out[3] = zero;
+        return;
+    }
+    const float s = __fdiv_rn(num, den);
+    const float3 d1 = ((-w1 * q1) * s) * kb, d2 = ((-w2 * q2) * s) * kb;
+    const float3 d3 = ((-w3 * q3) * s) * kb, d4 = ((-w4 * q4) * s) * kb;
+    out[0] = make_float4(d1.x, d1.y, d1.z, 0.f);
+    out[1] = make_float4(d2.x, d2.y, d2.z, 0.f);
+    out[2] = make_float4(d3.x, d3.y, d3.z, 0.f);
+    out[3] = make_float4(d4.x, d4.y, d4.z, 0.f);
+}
+
+// Each particle with incident quads adds their corrections in CSR order (the
+// reference's atomic scatter into deltaX, then accDevArr_float3).
+__global__ void k_bending_apply(SimConsts C, int nn_, const int *__restrict__ node_ids, const int *__restrict__ ptr,
+                                const int *__restrict__ inc, const float4 *__restrict__ terms,
+                                const int *__restrict__ to_new, float4 *__restrict__ P)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nn_) return;
+    const int i = to_new[node_ids[t]];
+    float3 d = make_float3(0.f, 0.f, 0.f);
+    for (int q = ptr[t]; q < ptr[t + 1]; ++q) d += f3(terms[inc[q]]);
+    const float4 p4 = P[i];
+    const float3 p = f3(p4) + d;
+    P[i] = make_float4(p.x, p.y, p.z, p4.w);
+    track_displacement(C, i, p, true);
+}
+
+void launch_bending(cudaStream_t st, const SimConsts &C, const BendingArgs &a, float4 *P, const float *w,
+                    const int *to_new, LaunchLog *L)
+{
+    if (a.num_quads <= 0) return;
+    k_bending_terms<<<(a.num_quads + 255) / 256, 256, 0, st>>>(a.num_quads, a.quads, P, w, to_new, a.stiffness,
+                                                              a.terms);
+    L->done("k_bending_terms");
+    k_bending_apply<<<(a.num_nodes + 255) / 256, 256, 0, st>>>(C, a.num_nodes, a.node_ids, a.node_ptr, a.node_inc,
+                                                               a.terms, to_new, P);
+    L->done("k_bending_apply");
 }
 
 // ---- wind ----

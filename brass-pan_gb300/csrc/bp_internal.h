@@ -168,6 +168,18 @@ struct DistanceArgs {
 };
 void launch_distance(cudaStream_t st, const SimConsts &C, const DistanceArgs &a, float4 *P, const float *w,
                      const int *to_new, unsigned *err, LaunchLog *L);
+struct BendingArgs {
+    int num_quads;
+    const int4 *quads;       // original ids: hinge edge (x, y), wings z and w
+    float stiffness;
+    int num_nodes;           // particles with incident quads
+    const int *node_ids;     // original ids of those particles
+    const int *node_ptr;     // CSR row pointers (num_nodes + 1)
+    const int *node_inc;     // quad*4 + corner
+    float4 *terms;           // per quad and corner: the correction
+};
+void launch_bending(cudaStream_t st, const SimConsts &C, const BendingArgs &a, float4 *P, const float *w,
+                    const int *to_new, LaunchLog *L);
 struct WindArgs {
     int num_faces;
     const int *faces;        // [F][3] original ids

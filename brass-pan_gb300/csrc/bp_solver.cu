@@ -85,6 +85,7 @@ extern "C" void bp_params_init(bp_params *p, float r)
     // staging each CTA's neighbourhood in shared memory measured slower than
     // reading it through a full-size L1 (opt-in; bp_solver_autotune times both)
     p->walk_options = BP_WALK_NO_STAGING;
+    p->bending_stiffness = 0.8f;                   // bending.cuh:71
 }
 
 static bp_status check_params(const bp_params *p)
@@ -98,6 +99,7 @@ static bp_status check_params(const bp_params *p)
     if (p->kernel_radius > p->cell_size * 1.0001f)
         return fail(BP_ERR_INVALID_ARGUMENT, "kernel_radius must not exceed cell_size (27-cell search)");
     if (p->rotation_iterations < 0) return fail(BP_ERR_INVALID_ARGUMENT, "rotation_iterations < 0");
+    if (!std::isfinite(p->bending_stiffness)) return fail(BP_ERR_INVALID_ARGUMENT, "bending_stiffness is not finite");
     if (p->scorr_n < 0 || p->scorr_n > 16) return fail(BP_ERR_INVALID_ARGUMENT, "scorr_n must be in [0, 16]");
     if (!(p->neighbor_skin >= 0.f)) return fail(BP_ERR_INVALID_ARGUMENT, "neighbor_skin < 0");
     return BP_OK;
@@ -230,7 +232,7 @@ static void build_incidence(int n, int count, int arity, const int32_t *ids, boo
     for (int c = 0; c < count; ++c)
         for (int a = 0; a < arity; ++a) {
             const int nd = node_of[ids[arity * c + a]];
-            inc[fill[nd]++] = encode_side ? (c * 2 + a) : c;
+            inc[fill[nd]++] = encode_side ? (c * arity + a) : c;
         }
 }
 
@@ -262,6 +264,7 @@ static bp_status validate_scene(const bp_scene_desc *sc)
         return fail(BP_ERR_INVALID_ARGUMENT, "distance_params is NULL");
     if ((st = check_ids(sc->num_wind_faces, 3, sc->wind_faces, "wind_faces")) != BP_OK) return st;
     if ((st = check_ids(sc->num_immovables, 1, sc->immovables, "immovables")) != BP_OK) return st;
+    if ((st = check_ids(sc->num_bendings, 4, sc->bendings, "bendings")) != BP_OK) return st;
     if (sc->num_rigid_bodies < 0) return fail(BP_ERR_INVALID_ARGUMENT, "num_rigid_bodies < 0");
     if (sc->num_rigid_bodies > 0 && (!sc->rigid_ranges || !sc->rigid_rest_positions))
         return fail(BP_ERR_INVALID_ARGUMENT, "rigid_ranges / rigid_rest_positions is NULL");
@@ -416,6 +419,25 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         s->dist.node_inc = ninc;
         s->dist.edge_k = ek;
     }
+    if (sc->num_bendings > 0) {
+        const int q = sc->num_bendings;
+        std::vector<int> nodes, ptr, inc;
+        build_incidence(n, q, 4, sc->bendings, true, nodes, ptr, inc);
+        s->bend.num_quads = q;
+        s->bend.num_nodes = (int)nodes.size();
+        int4 *quads;
+        int *nid, *nptr, *ninc;
+        float4 *terms;
+        if ((st = s->upload(&quads, sc->bendings, q)) || (st = s->upload(&nid, nodes.data(), nodes.size())) ||
+            (st = s->upload(&nptr, ptr.data(), ptr.size())) || (st = s->upload(&ninc, inc.data(), inc.size())) ||
+            (st = s->alloc(&terms, 4 * (size_t)q)))
+            return bail(st);
+        s->bend.quads = quads;
+        s->bend.node_ids = nid;
+        s->bend.node_ptr = nptr;
+        s->bend.node_inc = ninc;
+        s->bend.terms = terms;
+    }
     if (sc->num_wind_faces > 0) {
         const int f = sc->num_wind_faces;
         std::vector<int> nodes, ptr, inc;
@@ -542,7 +564,7 @@ extern "C" bp_status bp_batch_create(int32_t num_scenes, const bp_scene_desc *sc
     // one scene description: the scenes' particles and constraints concatenated, ids offset
     const int n = (int)total;
     std::vector<float> pos(3 * (size_t)n), vel(3 * (size_t)n, 0.f), mass(n), rest;
-    std::vector<int32_t> phase(n), group(n, 0), pairs, faces, ranges, imm;
+    std::vector<int32_t> phase(n), group(n, 0), pairs, faces, ranges, imm, quads;
     std::vector<float> dparams;
     bool any_rigid = false;
     for (int k = 0; k < num_scenes; ++k) any_rigid |= scenes[k].num_rigid_bodies > 0;
@@ -563,6 +585,7 @@ extern "C" bp_status bp_batch_create(int32_t num_scenes, const bp_scene_desc *sc
         if (d.num_rigid_bodies > 0)
             std::copy(d.rigid_rest_positions, d.rigid_rest_positions + 3 * (size_t)m, rest.begin() + 3 * (size_t)o);
         for (int e = 0; e < d.num_immovables; ++e) imm.push_back(d.immovables[e] + o);
+        for (int e = 0; e < 4 * d.num_bendings; ++e) quads.push_back(d.bendings[e] + o);
     }
     bp_scene_desc all;
     memset(&all, 0, sizeof(all));
@@ -582,6 +605,8 @@ extern "C" bp_status bp_batch_create(int32_t num_scenes, const bp_scene_desc *sc
     all.rigid_rest_positions = any_rigid ? rest.data() : nullptr;
     all.num_immovables = (int)imm.size();
     all.immovables = imm.data();
+    all.num_bendings = (int)(quads.size() / 4);
+    all.bendings = quads.data();
     bp_params shared = params[0];
     shared.grid_dim = 4;  // unused: every particle walks its scene's grid
     return create_solver(&all, &shared, stream, &spec, out);
@@ -643,10 +668,11 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     const bool pcoll = (mask & BP_STAGE_PARTICLE_COLLISION) && s->has_solid;
     const bool fluid = (mask & BP_STAGE_FLUID) != 0;
     const bool distance = (mask & BP_STAGE_DISTANCE) && s->dist.num_edges > 0;
+    const bool bending = (mask & BP_STAGE_BENDING) && s->bend.num_quads > 0;
     const bool rigid = (mask & BP_STAGE_SHAPE_MATCHING) && s->rigid.num_bodies > 0;
     const bool immov = (mask & BP_STAGE_IMMOVABLE) && s->nimm > 0;
     const bool picking = picked >= 0;
-    const bool tail = distance || rigid || immov;  // stages after the fluid position pass
+    const bool tail = distance || bending || rigid || immov;  // stages after the fluid position pass
     if (picking) launch_pick(st, picked, s->to_new, s->Xc, ppos, 1, s->Vc, make_float3(0.f, 0.f, 0.f), L);
 
     launch_hash_state(st, C, s->Xc, s->Vc, s->keys, s->sort.hist, L);
@@ -665,7 +691,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     ra.mass = s->mass;
     ra.orig_s = s->orig_s;
     ra.to_new = s->to_new;
-    ra.inv_scaled = (distance || pcoll) ? s->w : nullptr;
+    ra.inv_scaled = (distance || bending || pcoll) ? s->w : nullptr;
     ra.stabilize = planes;
     ra.collide = fuse_first_planes;
     ra.tile_solid = pcoll ? s->tile_solid : nullptr;
@@ -773,6 +799,11 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         if (distance) {
             if (tape) tape->push(TS_DISTANCE, cur);
             launch_distance(st, Cpost, s->dist, cur, s->w, s->to_new, s->err, L);
+        }
+        if (bending) {  // PS:956-969 (no adjoint)
+            BendingArgs ba = s->bend;
+            ba.stiffness = s->prm.bending_stiffness;
+            launch_bending(st, Cpost, ba, cur, s->w, s->to_new, L);
         }
         if (rigid) {
             if (tape) tape->push(TS_SHAPE, cur);

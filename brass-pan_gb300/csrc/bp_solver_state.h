@@ -136,6 +136,7 @@ struct bp_solver {
     SceneConsts *scn = nullptr;
     int *scene_of = nullptr;
     DistanceArgs dist{};
+    BendingArgs bend{};
     WindArgs wind{};
     RigidArgs rigid{};
     int nimm = 0;

@@ -34,6 +34,7 @@ class Scene:
     rigid_ranges: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int32))
     rigid_rest: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.float32))
     immovables: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    bendings: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.int32))
     # counters as in the reference
     solid_phase_counter: int = 1
     fluid_phase_counter: int = -1
@@ -139,7 +140,7 @@ class Scene:
         self.distance_params = np.concatenate([self.distance_params, params.reshape(-1, 2).astype(np.float32)])
 
     def add_cloth(self, start, offset_x, offset_y, nx, ny, mass, corners=(False, False, False, False),
-                  stretch=0.2, shear=None, bend=0.1, self_collide=True):
+                  stretch=0.2, shear=None, bend=0.1, self_collide=True, dihedral=False):
         """Cloth::CreateCloth + addCloth (scene.h:226-330, particlesolver.cuh:576-710).
 
         Positions are pushed x-outer / y-inner as start + y*offset_x + x*offset_y
@@ -147,14 +148,16 @@ class Scene:
         transposes the lattice, exactly as the reference does.  Pairs:
         horizontal and vertical (stretch), both diagonals (shear), and the
         skip-one "hack bending" pairs of the 3x3 stencil (bend), with the
-        reference's repetitions."""
+        reference's repetitions.  dihedral=True adds the reference's
+        commented-out dihedral bending quads (scene.h:308-320): per lattice
+        quad (p3, p2, p1, p4) when x + y is odd, else (p1, p4, p3, p2)."""
         shear = stretch if shear is None else shear
         ox = np.asarray(offset_x, np.float32)
         oy = np.asarray(offset_y, np.float32)
         lx = float(np.linalg.norm(ox))
         ly = float(np.linalg.norm(oy))
         ld = float(np.linalg.norm(ox + oy))
-        pos, faces, pairs, params, imm = [], [], [], [], []
+        pos, faces, pairs, params, imm, quads = [], [], [], [], [], []
         if corners[0]:
             imm.append(0)
         if corners[1]:
@@ -173,6 +176,8 @@ class Scene:
                 if x < nx - 1 and y < ny - 1:
                     faces.append((p1, p2, p3))
                     faces.append((p2, p3, p4))
+                    if dihedral:
+                        quads.append((p3, p2, p1, p4) if (x + y) % 2 else (p1, p4, p3, p2))
                 if x < nx - 1:
                     pairs.append((p1, p2)); params.append((lx, stretch))
                 if y < ny - 1:
@@ -193,6 +198,8 @@ class Scene:
             self.faces = np.concatenate([self.faces, np.array(faces, np.int32) + n0])
         if imm:
             self.immovables = np.concatenate([self.immovables, np.array(imm, np.int32) + n0])
+        if quads:
+            self.bendings = np.concatenate([self.bendings, np.array(quads, np.int32) + n0])
         return n0, self.num_particles
 
     def make_immovable(self, ids):

@@ -71,7 +71,8 @@ typedef enum bp_mode {
 #define BP_STAGE_VORTICITY 0x080
 #define BP_STAGE_AKINCI 0x100
 #define BP_STAGE_XSPH 0x200
-#define BP_STAGE_ALL 0x3ff
+#define BP_STAGE_BENDING 0x400
+#define BP_STAGE_ALL 0x7ff
 /* The stages the reference's update() runs as shipped (only planes and the
  * velocity post-passes are live there). */
 #define BP_STAGE_REFERENCE_AS_SHIPPED \
@@ -127,7 +128,8 @@ typedef struct bp_params {
     float neighbor_skin;         /* skin of the per-substep Verlet lists, as a fraction of h
                                     (0 disables them; results are identical either way): 0 */
     int32_t walk_options;        /* BP_WALK_* tuning switches of the neighbour walks: BP_WALK_NO_STAGING */
-    int32_t reserved[6];
+    float bending_stiffness;     /* 0.8 (bending.cuh:71) */
+    int32_t reserved[5];
 } bp_params;
 
 /* Fills `p` with the reference's literals for a scene of the given particle
@@ -156,6 +158,8 @@ typedef struct bp_scene_desc {
     const float *rigid_rest_positions; /* [N][3] by original id; each body's rest shape has its centre at 0 */
     int32_t num_immovables;
     const int32_t *immovables;         /* [K] original ids */
+    int32_t num_bendings;              /* dihedral bending constraints (kernel/bending.cuh) */
+    const int32_t *bendings;           /* [Q][4] original ids: hinge edge (0, 1), wings 2 and 3; rest: flat */
 } bp_scene_desc;
 
 typedef struct bp_solver bp_solver;

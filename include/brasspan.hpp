@@ -58,6 +58,7 @@ public:
     std::vector<int> distancePairs;                // [M][2]
     std::vector<float> distanceParams;             // [M][2]
     std::vector<int> immovableConstraints;
+    std::vector<int> bendingConstraints;  // [Q][4]: "bending constraints - record all 4 ids" (scene.h:527-528)
 
     int groupIdCounter = 0;
     int solidPhaseCounter = 1;   // scene.h:534
@@ -125,7 +126,8 @@ public:
     // Cloth::CreateCloth + addCloth (scene.h:226-330, particlesolver.cuh:576-710)
     std::pair<int, int> addCloth(float3_ start, float3_ offsetX, float3_ offsetY, int nx, int ny, float mass,
                                  bool c0 = false, bool c1 = false, bool c2 = false, bool c3 = false,
-                                 float stretch = 0.2f, float shear = 0.2f, float bend = 0.1f)
+                                 float stretch = 0.2f, float shear = 0.2f, float bend = 0.1f,
+                                 bool dihedral = false)
     {
         const int n0 = numParticles();
         const float lx = norm(offsetX), ly = norm(offsetY);
@@ -144,6 +146,10 @@ public:
                 if (x < nx - 1 && y < ny - 1) {
                     const int f[6] = {p1, p2, p3, p2, p3, p4};
                     for (int k = 0; k < 6; ++k) faces.push_back(n0 + f[k]);
+                    if (dihedral) {  // the commented-out quads of scene.h:308-320
+                        const int odd[4] = {p3, p2, p1, p4}, even[4] = {p1, p4, p3, p2};
+                        for (int k = 0; k < 4; ++k) bendingConstraints.push_back(n0 + ((x + y) % 2 ? odd[k] : even[k]));
+                    }
                 }
                 if (x < nx - 1) pair(n0 + p1, n0 + p2, lx, stretch);
                 if (y < ny - 1) pair(n0 + p1, n0 + p3, ly, stretch);
@@ -187,6 +193,8 @@ public:
         d.rigid_rest_positions = rigidbodyInitialPositions.data();
         d.num_immovables = (int)immovableConstraints.size();
         d.immovables = immovableConstraints.empty() ? nullptr : immovableConstraints.data();
+        d.num_bendings = (int)bendingConstraints.size() / 4;
+        d.bendings = bendingConstraints.empty() ? nullptr : bendingConstraints.data();
         return d;
     }
 

@@ -209,13 +209,13 @@ int or_neighbor_counts(int n, const float *sp, float cell, int D, float h, const
 /* ---- solver state ------------------------------------------------------------ */
 
 struct or_solver {
-    int n, D, nb, npairs, nfaces, nimm, nplanes;
+    int n, D, nb, npairs, nfaces, nimm, nplanes, nbend;
     bp_params prm;
     f3 *x, *p, *v, *sx, *sp, *sv, *dX, *tmp, *omega, *normal;
     float *m, *sm, *w, *lambda, *rho;
     int *phase, *sphase, *group, *sgroup, *to_orig, *sto_orig, *to_new;
     int *cell_id, *sorted_cell, *sorted_pid, *cell_start, *cell_end;
-    int *ranges, *pairs, *faces, *imm;
+    int *ranges, *pairs, *faces, *imm, *bends;
     float *dparams, *planes;
     f3 *rest, *cms;
     f4 *rot;
@@ -278,6 +278,9 @@ or_solver *or_create(const bp_scene_desc *sc, const bp_params *prm)
     s->nimm = sc->num_immovables;
     ALLOC(s->imm, s->nimm);
     if (s->nimm) memcpy(s->imm, sc->immovables, sizeof(int) * (size_t)s->nimm);
+    s->nbend = sc->num_bendings;
+    ALLOC(s->bends, 4 * s->nbend);
+    if (s->nbend) memcpy(s->bends, sc->bendings, sizeof(int) * 4 * (size_t)s->nbend);
     return s;
 }
 
@@ -288,7 +291,7 @@ void or_destroy(or_solver *s)
                     s->w, s->lambda, s->rho, s->phase, s->sphase, s->group, s->sgroup, s->to_orig,
                     s->sto_orig, s->to_new, s->cell_id, s->sorted_cell, s->sorted_pid, s->cell_start,
                     s->cell_end, s->ranges, s->pairs, s->faces, s->imm, s->dparams, s->planes, s->rest,
-                    s->cms, s->rot};
+                    s->cms, s->rot, s->bends};
     for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); ++k) free(ptrs[k]);
     free(s);
 }
@@ -586,6 +589,44 @@ static void distance_constraints(or_solver *s)
         const f3 kk = vmul(vmul(nn, (d12 - d0) / sw), kst);
         atomic_add3(s->dX, id1, smul(-w1, kk));
         atomic_add3(s->dX, id2, smul(w2, kk));
+    }
+}
+
+/* bendingConstraints (K/bending.cuh:3-75) -> dX: the dihedral angle of the
+ * triangles (1, 2, 3) and (1, 2, 4) over the hinge 1-2 pulled towards pi with
+ * the gradients of Mueller et al. 2007 (appendix A), stiffness k (0.8 there). */
+static void bending_constraints(or_solver *s, float kb)
+{
+#pragma omp parallel for num_threads(g_threads)
+    for (int c = 0; c < s->nbend; ++c) {
+        const int id1 = s->to_new[s->bends[4 * c]], id2 = s->to_new[s->bends[4 * c + 1]];
+        const int id3 = s->to_new[s->bends[4 * c + 2]], id4 = s->to_new[s->bends[4 * c + 3]];
+        const f3 p1 = s->p[id1];
+        const f3 e = vsub(s->p[id2], p1), a = vsub(s->p[id3], p1), b = vsub(s->p[id4], p1);
+        const f3 ca = vcross(e, a), cb = vcross(e, b);
+        const float la = vlen(ca);
+        if (la <= 1e-5f) continue;
+        const float lb = vlen(cb);
+        if (lb <= 1e-5f) continue;
+        const f3 n1 = vmul(ca, 1.0f / la), n2 = vmul(cb, 1.0f / lb);
+        float d = vdot(n1, n2);
+        d = fminf_(fmaxf_(d, -1.0f), 1.0f);
+        const f3 en1 = vcross(e, n1), en2 = vcross(e, n2);
+        const f3 an1 = vcross(a, n1), an2 = vcross(a, n2);
+        const f3 bn1 = vcross(b, n1), bn2 = vcross(b, n2);
+        const f3 q3 = vdiv(vsub(en2, vmul(en1, d)), la);
+        const f3 q4 = vdiv(vsub(en1, vmul(en2, d)), lb);
+        const f3 q2 = vsub(vdiv(vneg(vsub(an2, vmul(an1, d))), la), vdiv(vsub(bn1, vmul(bn2, d)), lb));
+        const f3 q1 = vsub(vsub(vneg(q2), q3), q4);
+        const float w1 = s->w[id1], w2 = s->w[id2], w3 = s->w[id3], w4 = s->w[id4];
+        const float den = w1 * vlen2(q1) + w2 * vlen2(q2) + w3 * vlen2(q3) + w4 * vlen2(q4);
+        const float num = sqrtf(1.0f - d * d) * (acosf(d) - 3.141592f);
+        if (den <= 1e-5f) continue;
+        const float sc = num / den;
+        atomic_add3(s->dX, id1, vmul(vmul(smul(-w1, q1), sc), kb));
+        atomic_add3(s->dX, id2, vmul(vmul(smul(-w2, q2), sc), kb));
+        atomic_add3(s->dX, id3, vmul(vmul(smul(-w3, q3), sc), kb));
+        atomic_add3(s->dX, id4, vmul(vmul(smul(-w4, q4), sc), kb));
     }
 }
 
@@ -898,6 +939,11 @@ int or_update(or_solver *s, int nsub, float dt, int iterations, int picked, cons
             if ((mask & BP_STAGE_DISTANCE) && s->npairs > 0) {
                 zero3(s->dX, n);
                 distance_constraints(s);
+                acc3(s->p, s->dX, n);
+            }
+            if ((mask & BP_STAGE_BENDING) && s->nbend > 0) { /* PS:956-969 */
+                zero3(s->dX, n);
+                bending_constraints(s, s->prm.bending_stiffness);
                 acc3(s->p, s->dX, n);
             }
             if ((mask & BP_STAGE_SHAPE_MATCHING) && s->nb > 0) shape_matching(s);

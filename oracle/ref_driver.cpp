@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE (the reference build, "oracle/_ref"): this file is
  * compiled together with the reference's unmodified kernel headers
  * (brasstower/kernel/{grid,fluid,particleplane,particleparticle,distance,wind,
- * shapematching,immovable}.cuh, cuda/cudamatrix.cuh, ext/helper_math.h), read
+ * shapematching,immovable,bending}.cuh, cuda/cudamatrix.cuh, ext/helper_math.h), read
  * in place from the reference checkout through the host shim in
  * oracle/refshim/.  Its outputs pin the C restatement (oracle/oracle.c) and
  * are committed as golden fixtures under tests/golden/.  Nothing in the
@@ -51,6 +51,12 @@ thread_local dim3 gridDim;
 #include "kernel/wind.cuh"
 #include "kernel/shapematching.cuh"
 #include "kernel/immovable.cuh"
+
+/* kernel/bending.cuh:52 negates a temporary, which helper_math.h's
+ * operator-(float3 &) cannot bind; this overload for rvalues (ours) lets the
+ * unmodified kernel compile. */
+inline __host__ __device__ float3 operator-(float3 &&a) { return make_float3(-a.x, -a.y, -a.z); }
+#include "kernel/bending.cuh"
 
 #include "../include/brasspan.h"
 
@@ -172,6 +178,7 @@ struct RefSolver {
     std::vector<float3> cms;
     std::vector<int3> faces;
     std::vector<int> immovables;
+    std::vector<int4> bends;
     std::vector<float3> planeO, planeN;
 };
 
@@ -296,6 +303,13 @@ static void update(RefSolver &s, int numSub, float dt, int iterations, int mask,
                 launch(np_, [&] { distanceConstraints(dX, p, w, pr, pa, toNew, np_); });
                 k_acc(p, dX, n);
             }
+            if ((mask & BP_STAGE_BENDING) && !s.bends.empty()) { /* PS:956-969 */
+                k_fill(dX, make_float3(0.f), n);
+                const int nq = (int)s.bends.size();
+                const int4 *bq = s.bends.data();
+                launch(nq, [&] { bendingConstraints(dX, p, w, bq, toNew, nq); });
+                k_acc(p, dX, n);
+            }
             if ((mask & BP_STAGE_SHAPE_MATCHING) && !s.ranges.empty()) {
                 const int nb = (int)s.ranges.size();
                 float4 *rot = s.rotations.data();
@@ -410,6 +424,9 @@ void *ref_create(const bp_scene_desc *sc, float radius, float h, float cell, int
     s->rotations.assign(s->ranges.size(), make_float4(0.f, 0.f, 0.f, 1.f));
     s->cms.assign(s->ranges.size(), make_float3(0.f));
     for (int k = 0; k < sc->num_immovables; ++k) s->immovables.push_back(sc->immovables[k]);
+    for (int k = 0; k < sc->num_bendings; ++k)
+        s->bends.push_back(make_int4(sc->bendings[4 * k], sc->bendings[4 * k + 1], sc->bendings[4 * k + 2],
+                                     sc->bendings[4 * k + 3]));
     return s;
 }
 

@@ -81,3 +81,17 @@ def fluid_scene(bp, n=(12, 12, 12), seed=0, grid_dim=64, box=(2.0, 3.0, 2.0)):
     rng = np.random.default_rng(seed + 100)
     s.velocities = rng.uniform(-0.3, 0.3, (s.num_particles, 3)).astype(np.float32)
     return s
+
+
+def cloth_bending_scene(bp, seed=0, n=12, grid_dim=16):
+    """A horizontal cloth with the reference's dihedral bending quads, pinned
+    at two corners, sagging onto itself; random initial velocities."""
+    sc = bp.scenes
+    rng = np.random.default_rng(seed)
+    s = sc.Scene(name="cloth_bending")
+    s.particle_radius, s.kernel_radius, s.cell_size, s.grid_dim, s.rest_density = 0.05, 0.2, 0.2, grid_dim, 1000.0
+    sc.box_planes(s, (0, 0, 0), (3.0, 4.0, 3.0))
+    s.add_cloth((0.2, 1.5, 0.2), (0.1, 0, 0), (0, 0, 0.1), n, n, 0.1, corners=(True, True, False, False),
+                stretch=0.25, shear=0.1, bend=0.05, dihedral=True)
+    s.velocities = rng.uniform(-0.3, 0.3, (s.num_particles, 3)).astype(np.float32)
+    return s

@@ -11,6 +11,10 @@ travel with the repository (the GPU machine has no reference checkout):
   step_*.npz   a scene (all arrays + parameters) and the state after
                `frames` calls of update(2 substeps, 1/60 s, 4 iterations)
 
+kernel/bending.cuh:52 negates a temporary, which helper_math.h's unary minus
+(a non-const reference) cannot bind; ref_driver.cpp adds an rvalue overload
+so that the unmodified kernel compiles.
+
 Run:  python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -26,7 +30,7 @@ sys.path.insert(0, str(REPO))
 sys.path.insert(0, str(REPO / "tests"))
 
 SCENE_ARRAYS = ["positions", "velocities", "masses", "phases", "group_ids", "planes", "distance_pairs",
-                "distance_params", "faces", "rigid_ranges", "rigid_rest", "immovables"]
+                "distance_params", "faces", "rigid_ranges", "rigid_rest", "immovables", "bendings"]
 SCENE_SCALARS = ["particle_radius", "kernel_radius", "cell_size", "grid_dim", "rest_density"]
 
 
@@ -98,7 +102,7 @@ def step_fixture(name, bp, scene, frames, mask=None):
 def main():
     import __graft_entry__ as entry
     import oracle
-    from conftest import fluid_scene, small_mixed_scene
+    from conftest import cloth_bending_scene, fluid_scene, small_mixed_scene
 
     entry.build()
     if oracle.ref_lib() is None:
@@ -128,6 +132,8 @@ def main():
     step_fixture("step_mixed_as_shipped.npz", bp, s, frames=3,
                  mask=bp.abi.BP_STAGE_PLANES | bp.abi.BP_STAGE_VORTICITY | bp.abi.BP_STAGE_AKINCI
                  | bp.abi.BP_STAGE_XSPH | bp.abi.BP_STAGE_FLUID)
+    # dihedral bending (kernel/bending.cuh, compiled with an rvalue negation overload)
+    step_fixture("step_cloth_bending.npz", bp, cloth_bending_scene(bp, seed=7), frames=10)
 
 
 if __name__ == "__main__":

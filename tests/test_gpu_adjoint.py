@@ -238,4 +238,14 @@ def test_backward_rejects_stages_without_adjoint(bp, gpu):
     with pytest.raises(bp.BrassPanError):
         t.backward(np.ones((scene.num_particles, 3), np.float32))  # nothing recorded
     t.close()
+    from conftest import cloth_bending_scene
+
+    cloth = cloth_bending_scene(bp, seed=1, n=6)
+    stages = abi.BP_STAGE_PLANES | abi.BP_STAGE_DISTANCE | abi.BP_STAGE_BENDING | abi.BP_STAGE_IMMOVABLE
+    u = bp.ParticleSolver(cloth, bp.make_params(cloth, stage_mask=stages))
+    u.tape_begin(1)
+    u.update(1, DT, 2)
+    with pytest.raises(bp.BrassPanError):
+        u.backward(np.ones((cloth.num_particles, 3), np.float32))  # dihedral bending has no adjoint
+    u.close()
     assert abi.BP_STAGE_VORTICITY

@@ -11,7 +11,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, fluid_scene, small_mixed_scene
+from conftest import GOLDEN, cloth_bending_scene, fluid_scene, small_mixed_scene
 
 import sys
 
@@ -114,6 +114,23 @@ def test_large_rigid_bodies_parity(bp, gpu, oracle):
     assert_parity(*lockstep(bp, oracle, s, bp.make_params(s), substeps=6))
 
 
+def test_dihedral_bending_parity(bp, gpu, oracle):
+    """Dihedral bending (kernel/bending.cuh) on a sagging cloth with its
+    stretch, shear and skip-one pairs, self-collisions and pinned corners."""
+    scene = cloth_bending_scene(bp, seed=3)
+    assert len(scene.bendings) == 121
+    assert_parity(*lockstep(bp, oracle, scene, bp.make_params(scene), substeps=6))
+    # the stage does something: without it the cloth ends elsewhere
+    a = bp.ParticleSolver(scene, bp.make_params(scene))
+    b = bp.ParticleSolver(scene, bp.make_params(scene, stage_mask=bp.abi.BP_STAGE_ALL & ~bp.abi.BP_STAGE_BENDING))
+    for s in (a, b):
+        for _ in range(5):
+            s.update(2, DT, 4)
+    assert np.abs(a.positions() - b.positions()).max() > 1e-3
+    a.close()
+    b.close()
+
+
 def test_textbook_mode_parity(bp, gpu, oracle):
     # s_corr k = 0.001: with m = 1 kg and rho0 = 1000 kg/m^3 the paper's k = 0.1
     # outweighs lambda ~50x and the block explodes (on the oracle as well)
@@ -130,7 +147,8 @@ def test_two_substeps_per_call_parity(bp, gpu, oracle):
     assert_parity(errs, h, sdt)
 
 
-@pytest.mark.parametrize("name", ["step_fluid.npz", "step_mixed.npz", "step_mixed_as_shipped.npz"])
+@pytest.mark.parametrize("name", ["step_fluid.npz", "step_mixed.npz", "step_mixed_as_shipped.npz",
+                                  "step_cloth_bending.npz"])
 def test_first_frame_matches_reference_golden(bp, gpu, name):
     """One frame from the fixture scene against the reference's own kernels."""
     z = np.load(GOLDEN / name)
@@ -140,7 +158,11 @@ def test_first_frame_matches_reference_golden(bp, gpu, name):
     g = bp.ParticleSolver(scene, params)
     g.update(2, DT, 4)
     h = scene.kernel_radius
-    np.testing.assert_array_less(np.abs(g.positions() - z["x1"]).max(), 2e-4 * h)
+    # The self-colliding cloth (144 particles all in contact range of their
+    # lattice neighbours, plus bending and stretch) amplifies rounding over the
+    # frame's 8 constraint passes: 4.2e-5 measured there, so it gets 4e-4 h.
+    tol = 4e-4 if name == "step_cloth_bending.npz" else 2e-4
+    np.testing.assert_array_less(np.abs(g.positions() - z["x1"]).max(), tol * h)
     np.testing.assert_array_equal(g.field(bp.abi.BP_FIELD_MAP_TO_ORIGINAL), z["to_orig1"])
     np.testing.assert_array_equal(g.field(bp.abi.BP_FIELD_SORTED_CELL_IDS), z["sorted_cell1"])
     g.close()

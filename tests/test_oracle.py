@@ -17,7 +17,7 @@ sys.path.insert(0, str(GOLDEN))
 from make_golden import scene_from_npz  # noqa: E402
 
 GRID_FIXTURES = ["grid_d32.npz", "grid_d4_alias.npz", "grid_faces_d16.npz", "grid_d512.npz", "grid_single.npz"]
-STEP_FIXTURES = ["step_fluid.npz", "step_mixed.npz", "step_mixed_as_shipped.npz"]
+STEP_FIXTURES = ["step_fluid.npz", "step_mixed.npz", "step_mixed_as_shipped.npz", "step_cloth_bending.npz"]
 
 
 @pytest.mark.parametrize("name", GRID_FIXTURES)

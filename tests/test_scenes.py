@@ -26,6 +26,23 @@ def test_cloth_counts_follow_reference_factory(bp):
     np.testing.assert_allclose(d, [0.1, np.sqrt(0.02), 0.2], rtol=1e-5)
 
 
+def test_dihedral_quads_follow_reference_pattern(bp):
+    """The reference's commented-out cloth bending quads (scene.h:308-320):
+    one per lattice quad, hinge along the diagonal p3-p2 when x + y is odd,
+    p1-p4 when even."""
+    s = bp.scenes.Scene()
+    n = 5
+    s.add_cloth((0, 1, 0), (0.1, 0, 0), (0, 0, 0.1), n, n, 1.0, dihedral=True)
+    assert s.bendings.shape == ((n - 1) ** 2, 4)
+    q = s.bendings.tolist()
+    k = 0
+    for x in range(n - 1):
+        for y in range(n - 1):
+            p1, p2, p3, p4 = y * n + x, y * n + x + 1, (y + 1) * n + x, (y + 1) * n + x + 1
+            assert q[k] == ([p3, p2, p1, p4] if (x + y) % 2 else [p1, p4, p3, p2])
+            k += 1
+
+
 def test_phase_and_group_conventions(bp):
     s = bp.scenes.Scene()
     s.add_fluid_block((2, 2, 2), (0, 0, 0), (0.1, 0.1, 0.1), 1.0)
@@ -49,14 +66,17 @@ int main(int argc, char **argv) {
     Scene s;
     const int fd[3] = {3, 4, 5};
     s.addFluidBlock(fd, {0.1f, 0.1f, 0.1f}, {0.1f, 0.1f, 0.1f}, 1.0f);
-    s.addCloth({0.2f, 1.25f, 0.2f}, {0.1f, 0.f, 0.f}, {0.f, 0.f, 0.1f}, 6, 6, 1.0f, true, false, false, true);
+    s.addCloth({0.2f, 1.25f, 0.2f}, {0.1f, 0.f, 0.f}, {0.f, 0.f, 0.1f}, 6, 6, 1.0f, true, false, false, true,
+               0.2f, 0.2f, 0.1f, true);
     const int rd[3] = {3, 2, 3};
     s.addRigidBox(rd, {0.4f, 1.45f, 0.5f}, {0.1f, 0.1f, 0.1f}, 1.0f);
     s.addRope({2.5f, 3.0f, 0.5f}, {2.5f, 2.0f, 0.5f}, 7, 1.0f);
     FILE *f = fopen(argv[1], "wb");
     dump(f, s.positions); dump(f, s.masses); dump(f, s.phases); dump(f, s.groupIds); dump(f, s.distancePairs);
     dump(f, s.distanceParams); dump(f, s.faces); dump(f, s.rigidbodyParticleIdRanges);
-    dump(f, s.rigidbodyInitialPositions); dump(f, s.immovableConstraints);
+    dump(f, s.rigidbodyInitialPositions); dump(f, s.immovableConstraints); dump(f, s.bendingConstraints);
+    const bp_scene_desc d = s.desc();
+    if (d.num_bendings * 4 != (int)s.bendingConstraints.size() || d.bendings != s.bendingConstraints.data()) return 2;
     fclose(f);
     bp_params p = s.params();
     return p.grid_dim == 512 ? 0 : 1;
@@ -76,7 +96,7 @@ def test_cpp_scene_builder_matches_python(bp, tmp_path):
     raw = out.read_bytes()
     arrays, off = [], 0
     kinds = [np.float32, np.float32, np.int32, np.int32, np.int32, np.float32, np.int32, np.int32, np.float32,
-             np.int32]
+             np.int32, np.int32]
     for k in kinds:
         n = int(np.frombuffer(raw, np.int64, 1, off)[0])
         off += 8
@@ -84,7 +104,8 @@ def test_cpp_scene_builder_matches_python(bp, tmp_path):
         off += n * 4
     s = bp.scenes.Scene()
     s.add_fluid_block((3, 4, 5), (0.1, 0.1, 0.1), (0.1, 0.1, 0.1), 1.0)
-    s.add_cloth((0.2, 1.25, 0.2), (0.1, 0, 0), (0, 0, 0.1), 6, 6, 1.0, corners=(True, False, False, True))
+    s.add_cloth((0.2, 1.25, 0.2), (0.1, 0, 0), (0, 0, 0.1), 6, 6, 1.0, corners=(True, False, False, True),
+                dihedral=True)
     s.add_rigid_box((3, 2, 3), (0.4, 1.45, 0.5), (0.1, 0.1, 0.1), 1.0)
     s.add_rope((2.5, 3.0, 0.5), (2.5, 2.0, 0.5), 7, 1.0)
     np.testing.assert_array_equal(arrays[0].reshape(-1, 3), s.positions)
@@ -97,3 +118,4 @@ def test_cpp_scene_builder_matches_python(bp, tmp_path):
     np.testing.assert_array_equal(arrays[7].reshape(-1, 2), s.rigid_ranges)
     np.testing.assert_allclose(arrays[8].reshape(-1, 3), s.rigid_rest, atol=1e-6)
     np.testing.assert_array_equal(arrays[9], s.immovables)
+    np.testing.assert_array_equal(arrays[10].reshape(-1, 4), s.bendings)
