@@ -184,7 +184,8 @@ EXPORTS = [
     "bp_params_init", "bp_solver_create", "bp_solver_destroy", "bp_solver_update", "bp_solver_step",
     "bp_solver_set_params", "bp_solver_query_original_particle_id", "bp_solver_query_new_particle_id",
     "bp_solver_get_particle_position", "bp_solver_copy_positions", "bp_solver_copy_velocities",
-    "bp_solver_set_state", "bp_solver_field", "bp_solver_copy_field", "bp_solver_pack_particle_infos",
+    "bp_solver_set_state", "bp_solver_snapshot_size", "bp_solver_snapshot_save", "bp_solver_snapshot_load",
+    "bp_solver_field", "bp_solver_copy_field", "bp_solver_pack_particle_infos",
     "bp_solver_device_errors", "bp_solver_last_launch_count", "bp_solver_profile", "bp_solver_walk_stats", "bp_grid_workspace_size", "bp_grid_build",
     "bp_grid_reset", "bp_grid_build_static", "bp_batch_create", "bp_batch_step", "bp_batch_scene_range",
     "bp_solver_tape_begin", "bp_solver_backward", "bp_solver_tape_end", "bp_solver_autotune", "bp_grid_neighbor_counts", "bp_last_error_string", "bp_abi_version",
@@ -215,6 +216,9 @@ def load(path: Path | None = None):
         "bp_solver_copy_positions": (i32, [vp, pf, i32]),
         "bp_solver_copy_velocities": (i32, [vp, pf, i32]),
         "bp_solver_set_state": (i32, [vp, pf, pf, i32]),
+        "bp_solver_snapshot_size": (i32, [vp, C.POINTER(sz)]),
+        "bp_solver_snapshot_save": (i32, [vp, vp, sz]),
+        "bp_solver_snapshot_load": (i32, [vp, vp, sz]),
         "bp_solver_field": (i32, [vp, i32, C.POINTER(vp), C.POINTER(sz)]),
         "bp_solver_copy_field": (i32, [vp, i32, vp, sz]),
         "bp_solver_pack_particle_infos": (i32, [vp, vp]),

@@ -1059,6 +1059,75 @@ extern "C" bp_status bp_solver_set_state(bp_solver *s, const float *hx, const fl
     return BP_OK;
 }
 
+// Snapshot layout: header, then the state buffers in state_buffers() order.
+struct SnapshotHeader {
+    char magic[8];        // "BPSNAP1"
+    int64_t n, ncells, num_bodies;
+    int64_t pcur_is_b;    // which predicted-position buffer the last update ended in
+    int64_t payload;      // bytes after the header
+};
+static const char kSnapMagic[8] = {'B', 'P', 'S', 'N', 'A', 'P', '1', 0};
+
+static size_t snapshot_payload(bp_solver *s)
+{
+    size_t b = 0;
+    for (const auto &kv : state_buffers(s)) b += kv.second;
+    return b;
+}
+
+extern "C" bp_status bp_solver_snapshot_size(bp_solver *s, size_t *bytes)
+{
+    if (!s || !bytes) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    *bytes = sizeof(SnapshotHeader) + snapshot_payload(s);
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_snapshot_save(bp_solver *s, void *host, size_t bytes)
+{
+    if (!s || !host) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (s->tape) return fail(BP_ERR_INVALID_ARGUMENT, "not available while a tape records");
+    const size_t payload = snapshot_payload(s);
+    if (bytes < sizeof(SnapshotHeader) + payload) return fail(BP_ERR_CAPACITY, "snapshot buffer too small");
+    SnapshotHeader h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, kSnapMagic, sizeof(kSnapMagic));
+    h.n = s->n;
+    h.ncells = (int64_t)s->ncells;
+    h.num_bodies = s->rigid.num_bodies;
+    h.pcur_is_b = s->Pcur == s->Pb;
+    h.payload = (int64_t)payload;
+    memcpy(host, &h, sizeof(h));
+    char *dst = (char *)host + sizeof(h);
+    for (const auto &kv : state_buffers(s)) {
+        BP_CUDA(cudaMemcpyAsync(dst, kv.first, kv.second, cudaMemcpyDeviceToHost, s->stream));
+        dst += kv.second;
+    }
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_snapshot_load(bp_solver *s, const void *host, size_t bytes)
+{
+    if (!s || !host) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (s->tape) return fail(BP_ERR_INVALID_ARGUMENT, "not available while a tape records");
+    SnapshotHeader h;
+    if (bytes < sizeof(h)) return fail(BP_ERR_INVALID_ARGUMENT, "not a snapshot (too short)");
+    memcpy(&h, host, sizeof(h));
+    if (memcmp(h.magic, kSnapMagic, sizeof(kSnapMagic)) != 0) return fail(BP_ERR_INVALID_ARGUMENT, "not a snapshot");
+    const size_t payload = snapshot_payload(s);
+    if (h.n != s->n || h.ncells != (int64_t)s->ncells || h.num_bodies != s->rigid.num_bodies ||
+        h.payload != (int64_t)payload || bytes < sizeof(h) + payload)
+        return fail(BP_ERR_INVALID_ARGUMENT, "snapshot of a different scene (particles, grid or rigid bodies differ)");
+    const char *src = (const char *)host + sizeof(h);
+    for (const auto &kv : state_buffers(s)) {
+        BP_CUDA(cudaMemcpyAsync(kv.first, src, kv.second, cudaMemcpyHostToDevice, s->stream));
+        src += kv.second;
+    }
+    BP_CUDA(cudaStreamSynchronize(s->stream));
+    s->Pcur = h.pcur_is_b ? s->Pb : s->Pa;
+    return BP_OK;
+}
+
 extern "C" bp_status bp_solver_field(bp_solver *s, int32_t field, void **ptr, size_t *bytes)
 {
     if (!s || !ptr || !bytes) return fail(BP_ERR_INVALID_ARGUMENT, "NULL argument");

@@ -196,8 +196,27 @@ void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int picke
                      SubstepTape *tape = nullptr);
 }  // namespace bp
 
-// Every buffer a caller can observe after an update, copied aside and put
-// back (around backward() and the autotuner's trial updates).
+// Every buffer a caller can observe after an update (device pointer, bytes):
+// what a later update reads (committed state, its cell-sorted order, rigid
+// rotations) and what the queries return.
+inline std::vector<std::pair<void *, size_t>> state_buffers(bp_solver *s)
+{
+    const size_t n = (size_t)s->n, nb = (size_t)s->rigid.num_bodies;
+    std::vector<std::pair<void *, size_t>> bufs = {
+        {s->Xc, n * 16},          {s->Vc, n * 16},       {s->Xs, n * 16},   {s->Vs, n * 16},
+        {s->Pa, n * 16},          {s->Pb, n * 16},       {s->orig_c, n * 4}, {s->orig_s, n * 4},
+        {s->to_new, n * 4},       {s->sorted_keys, n * 4}, {s->order, n * 4}, {s->off, (s->ncells + 1) * 4},
+        {s->mass, n * 4},         {s->lam, n * 4},       {s->rho, n * 4},   {s->w, n * 4},
+        {s->err, 4}};
+    if (nb) {
+        bufs.push_back({s->rigid.rot, nb * 16});
+        bufs.push_back({s->rigid.cm, nb * 16});
+    }
+    return bufs;
+}
+
+// The state buffers copied aside on the device and put back (around
+// backward() and the autotuner's trial updates).
 struct StateSnapshot {
     std::vector<std::pair<void *, size_t>> bufs;  // solver buffer, bytes
     std::vector<void *> copies;
@@ -208,15 +227,7 @@ struct StateSnapshot {
     }
     bp_status take(bp_solver *s)
     {
-        const size_t n = (size_t)s->n, nb = (size_t)s->rigid.num_bodies;
-        bufs = {{s->Xc, n * 16}, {s->Vc, n * 16}, {s->Xs, n * 16}, {s->Vs, n * 16}, {s->Pa, n * 16},
-                {s->Pb, n * 16}, {s->orig_c, n * 4}, {s->orig_s, n * 4}, {s->to_new, n * 4},
-                {s->sorted_keys, n * 4}, {s->order, n * 4}, {s->off, (s->ncells + 1) * 4}, {s->mass, n * 4},
-                {s->lam, n * 4}, {s->rho, n * 4}, {s->w, n * 4}, {s->err, 4}};
-        if (nb) {
-            bufs.push_back({s->rigid.rot, nb * 16});
-            bufs.push_back({s->rigid.cm, nb * 16});
-        }
+        bufs = state_buffers(s);
         for (auto &b : bufs) {
             void *p = nullptr;
             if (cudaMalloc(&p, b.second) != cudaSuccess) return bp::fail_with(BP_ERR_OUT_OF_MEMORY, "state snapshot");

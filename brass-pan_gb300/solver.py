@@ -102,6 +102,19 @@ class ParticleSolver:
             self.handle, None if x is None else x.ctypes.data_as(C.POINTER(C.c_float)),
             None if v is None else v.ctypes.data_as(C.POINTER(C.c_float)), order))
 
+    def snapshot(self) -> bytes:
+        """Checkpoint: the whole state as bytes (bp_solver_snapshot_save)."""
+        size = C.c_size_t()
+        abi.check(self.lib, self.lib.bp_solver_snapshot_size(self.handle, C.byref(size)))
+        buf = C.create_string_buffer(size.value)
+        abi.check(self.lib, self.lib.bp_solver_snapshot_save(self.handle, buf, size.value))
+        return buf.raw
+
+    def restore(self, snap: bytes):
+        """Resume from snapshot() bytes of a solver of the same scene."""
+        buf = C.create_string_buffer(bytes(snap), len(snap))
+        abi.check(self.lib, self.lib.bp_solver_snapshot_load(self.handle, buf, len(snap)))
+
     _DTYPES = {
         abi.BP_FIELD_POSITIONS: (np.float32, 4), abi.BP_FIELD_NEW_POSITIONS: (np.float32, 4),
         abi.BP_FIELD_VELOCITIES: (np.float32, 4), abi.BP_FIELD_MAP_TO_ORIGINAL: (np.int32, 1),

@@ -199,9 +199,23 @@ typedef enum bp_order { BP_ORDER_SORTED = 0, BP_ORDER_ORIGINAL = 1 } bp_order;
 /* Host copies of the state ([N][3] floats), synchronising the solver's stream. */
 bp_status bp_solver_copy_positions(bp_solver *s, float *host_xyz, int32_t order);
 bp_status bp_solver_copy_velocities(bp_solver *s, float *host_xyz, int32_t order);
-/* Overwrites positions and velocities (host [N][3], either may be NULL). */
+/* Overwrites positions and velocities (host [N][3], either may be NULL).
+ * The cell-sorted order stays as it is; the reference's density sums depend
+ * on that order, so a run continued from set_state need not repeat the bits
+ * of one that was never interrupted (bp_solver_snapshot_* does). */
 bp_status bp_solver_set_state(bp_solver *s, const float *host_positions,
                               const float *host_velocities, int32_t order);
+
+/* Checkpoint / resume; no counterpart in the reference.  A snapshot is one
+ * host byte buffer holding everything a later update or query reads: the
+ * committed and predicted state in its cell-sorted order, the id maps, the
+ * grid, lambda and density, rigid rotations and centres, the device error
+ * word.  Loading it into a solver created from the same scene (same particle
+ * count, grid and rigid bodies; checked) continues the run bit for bit.
+ * Parameters are not part of it.  Neither call is allowed while a tape records. */
+bp_status bp_solver_snapshot_size(bp_solver *s, size_t *bytes);
+bp_status bp_solver_snapshot_save(bp_solver *s, void *host, size_t bytes);
+bp_status bp_solver_snapshot_load(bp_solver *s, const void *host, size_t bytes);
 
 typedef enum bp_field {
     BP_FIELD_POSITIONS = 0,      /* float4 [N]: committed x, w = mass */
