@@ -544,7 +544,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint measurement")
     ap.add_argument("--save-state", default=None, help="after the timed steps, save the state (npz) here")
     ap.add_argument("--load-state", default=None, help="start from a state saved by --save-state")
-    ap.add_argument("--skin", type=float, default=None, help="neighbour-mask skin (fraction of h); 0 disables")
+    ap.add_argument("--skin", type=float, default=None, help="Verlet-list skin (fraction of h); 0 disables")
     ap.add_argument("--no-stage", action="store_true", help="read neighbours from global memory only")
     ap.add_argument("--no-split", action="store_true", help="evaluate pair terms as candidates are tested")
     ap.add_argument("--no-lists", action="store_true", help="post passes B and C walk their cells")

@@ -81,7 +81,7 @@ extern "C" void bp_params_init(bp_params *p, float r)
     p->wind_drag = 10.0f;
     p->wind_lift = 100.0f;
     p->rotation_iterations = 20;
-    p->neighbor_skin = 0.0f;  // masks measured slower than cell walks on GB300 (opt-in)
+    p->neighbor_skin = 0.0f;  // Verlet lists measured slower than the lambda-recorded lists (opt-in)
     // staging each CTA's neighbourhood in shared memory measured slower than
     // reading it through a full-size L1 (opt-in; bp_solver_autotune times both)
     p->walk_options = BP_WALK_NO_STAGING;
@@ -111,8 +111,8 @@ static bp_status check_params(const bp_params *p)
 // least D cells from the walked one along some axis, so at least (D - 2)
 // cells from the walker's cell; the hash's float rounding moves each cell
 // boundary by less than 0.01 for |p| < 4e4 (checked by k_class_refresh), and
-// 1e-3 h keeps the distance test's own rounding clear.  Taped updates and
-// neighbour masks walk whole cells.
+// 1e-3 h keeps the distance test's own rounding clear.  Taped updates walk
+// whole cells (the adjoint re-runs do not record the classes).
 static float class_reach(const bp_solver *s)
 {
     const bp_params &p = s->prm;
@@ -175,7 +175,7 @@ SimConsts bp::make_consts(const bp_solver *s, float sdt)
     C.rot_iters = p.rotation_iterations;
     C.dt = sdt;
     C.inv_dt = 1.0f / sdt;
-    C.cell_keys = s->sorted_keys;  // stored cell of every particle (staged walks, masks)
+    C.cell_keys = s->sorted_keys;  // stored cell of every particle (staged walks, Verlet lists)
     C.scn = s->scn;
     C.scene_of = s->scene_of;
     C.stage = (p.walk_options & BP_WALK_NO_STAGING) ? 0 : 1;
