@@ -235,23 +235,36 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
     const float3 vi = f3(V[i]);
     float3 om = make_float3(0.f, 0.f, 0.f), nn = make_float3(0.f, 0.f, 0.f);
     const bool want_om = C.use_vort, want_n = C.use_akinci;
-    ListWriter list(C.nbr, C.nbr_cap, C.n, i);
-    // the walk takes the passes' common neighbours (r = 0 included, as pass C
-    // wants them) and records them for passes B and C
-    walk_neighbors<Split>(
-        i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, Stage ? &S : nullptr, g,
-        [&](int, float4 pj4) { return len2(pi - f3(pj4)) <= C.h2; },
-        [&](int j, float4 pj4) {
-            if (j == i || phase_of(pj4) != phi) return;
-            if (C.nbr) list.push(j);
-            const float3 diff = pi - f3(pj4);
-            const float d2 = len2(diff);
-            if (!(d2 > 0.f)) return;
-            const float3 g = spiky_grad_r(C, diff, d2, rsqrtf(d2));
-            if (want_om) om += cross3(f3(V[j]) - vi, g);
-            if (want_n) nn = fma3(__frcp_rn(__ldg(rho + j)), g, nn);
+    auto term = [&](int j, float4 pj4) {
+        const float3 diff = pi - f3(pj4);
+        const float d2 = len2(diff);
+        if (!(d2 > 0.f)) return;
+        const float3 g = spiky_grad_r(C, diff, d2, rsqrtf(d2));
+        if (want_om) om += cross3(f3(V[j]) - vi, g);
+        if (want_n) nn = fma3(__frcp_rn(__ldg(rho + j)), g, nn);
+    };
+    const GridView v = grid_view(C, scene_index(C, i), off);
+    auto test = [&](int, float4 pj4) { return len2(pi - f3(pj4)) <= C.h2; };
+    // The walk takes the passes' common neighbours (r = 0 included, as pass C
+    // wants them).  With lists on it only records them (for passes B and C as
+    // well), and the terms are then summed over the list four neighbours at a
+    // time, so their velocity and density gathers overlap; a list that
+    // overflowed is summed by walking again.
+    int cnt = -1;
+    if (C.nbr) {
+        ListWriter list(C.nbr, C.nbr_cap, C.n, i);
+        walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4 pj4) {
+            if (j != i && phase_of(pj4) == phi) list.push(j);
         });
-    if (C.nbr) C.nbr_count[i] = list.finish();
+        cnt = list.finish();
+        C.nbr_count[i] = cnt;
+        // the records just written come back through the coherent path (plain loads)
+        if (cnt >= 0) for_each_in_list<false>(C.nbr, C.n, i, cnt, P, term);
+    }
+    if (cnt < 0)
+        walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4 pj4) {
+            if (j != i && phase_of(pj4) == phi) term(j, pj4);
+        });
     Om[i] = make_float4(om.x, om.y, om.z, len3(om));
     const float3 n = C.h * nn;
     Nm[i] = make_float4(n.x, n.y, n.z, rho[i]);

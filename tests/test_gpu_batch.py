@@ -9,7 +9,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import small_mixed_scene
+from conftest import cloth_bending_scene, small_mixed_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -23,6 +23,7 @@ def members(bp):
         sc.ensemble_member(2000, seed=2, rest_scale=0.85, gravity=13.0),
         small_mixed_scene(bp, seed=3),
         sc.ensemble_member(900, seed=4, rest_scale=1.15, gravity=6.0),
+        cloth_bending_scene(bp, seed=5, n=8),  # dihedral bending quads, offset in the batch
     ]
     return scenes
 
