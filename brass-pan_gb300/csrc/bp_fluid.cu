@@ -74,17 +74,34 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
         else C.nbr_count[i] = cnt;
     };
     if (!C.textbook) {
-        walk_neighbors<Split>(
-            i, pi, rec ? 0 : i, P, v, C, Stage ? &S : nullptr, g,
-            [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; },
-            [&](int j, float4 pj) {
-                if (rec) list.push(j);
-                const float d2 = len2(pi - f3(pj));
-                if (solid || j < i || (build && !(d2 <= C.h2))) return;
-                const float ld = __fmul_rn(__ldg(mass + j), poly6(C, d2));
-                density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
-            });
-        if (rec) finish();
+        auto dens = [&](int j, float4 pj) {
+            const float ld = __fmul_rn(__ldg(mass + j), poly6(C, len2(pi - f3(pj))));
+            density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
+        };
+        auto test = [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; };
+        if (C.nbr && !build) {
+            // record first, then sum the density over the list's j >= i (the
+            // mass gathers overlap there); an overflowed list walks again
+            walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test,
+                                  [&](int j, float4) { list.push(j); });
+            const int cnt = list.finish();
+            C.nbr_count[i] = cnt;
+            if (solid) return;
+            if (cnt >= 0)
+                for_each_in_list<false>(C.nbr, C.n, i, cnt, P, [&](int j, float4 pj) {
+                    if (j >= i) dens(j, pj);
+                });
+            else
+                walk_neighbors<Split>(i, pi, i, P, v, C, Stage ? &S : nullptr, g, test, dens);
+        } else {
+            walk_neighbors<Split>(i, pi, rec ? 0 : i, P, v, C, Stage ? &S : nullptr, g, test,
+                                  [&](int j, float4 pj) {
+                                      if (rec) list.push(j);
+                                      if (solid || j < i || (build && !(len2(pi - f3(pj)) <= C.h2))) return;
+                                      dens(j, pj);
+                                  });
+            if (rec) finish();
+        }
         if (solid) return;
         float c = density / rho0 - 1.0f;
         if (C.clamp_c) c = fmaxf(c, 0.0f);
