@@ -110,23 +110,34 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
         const float inv_rho0 = inv_rest_density(C, sc);
         float sum_g2 = 0.f;
         float3 gi = make_float3(0.f, 0.f, 0.f);
-        walk_neighbors<Split>(
-            i, pi, 0, P, v, C, Stage ? &S : nullptr, g, [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; },
-            [&](int j, float4 pj) {
+        auto term = [&](int j, float4 pj) {
+            const float3 diff = pi - f3(pj);
+            const float d2 = len2(diff);
+            const float mj = __ldg(mass + j);
+            const float ld = __fmul_rn(mj, poly6(C, d2));
+            density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
+            if (d2 > 0.f) {
+                const float3 g = __fmul_rn(-mj, inv_rho0) * spiky_grad_r(C, diff, d2, rsqrtf(d2));
+                sum_g2 = __fadd_rn(sum_g2, dot3(g, g));
+                gi -= g;
+            }
+        };
+        auto test = [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; };
+        if (C.nbr && !build) {  // record first, then sum over the list (as above)
+            walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test,
+                                  [&](int j, float4) { list.push(j); });
+            const int cnt = list.finish();
+            C.nbr_count[i] = cnt;
+            if (cnt >= 0) for_each_in_list<false>(C.nbr, C.n, i, cnt, P, term);
+            else walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, term);
+        } else {
+            walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4 pj) {
                 if (rec) list.push(j);
-                const float3 diff = pi - f3(pj);
-                const float d2 = len2(diff);
-                if (build && !(d2 <= C.h2)) return;
-                const float mj = __ldg(mass + j);
-                const float ld = __fmul_rn(mj, poly6(C, d2));
-                density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
-                if (d2 > 0.f) {
-                    const float3 g = __fmul_rn(-mj, inv_rho0) * spiky_grad_r(C, diff, d2, rsqrtf(d2));
-                    sum_g2 = __fadd_rn(sum_g2, dot3(g, g));
-                    gi -= g;
-                }
+                if (build && !(len2(pi - f3(pj)) <= C.h2)) return;
+                term(j, pj);
             });
-        if (rec) finish();
+            if (rec) finish();
+        }
         float c = density / rho0 - 1.0f;
         if (C.clamp_c) c = fmaxf(c, 0.0f);
         sum_g2 += dot3(gi, gi);
