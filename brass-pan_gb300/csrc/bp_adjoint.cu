@@ -366,6 +366,24 @@ __device__ __forceinline__ float3 clamp_fwd(const SimConsts &C, float3 u)
     return mul3(u, C.delta_clamp / sqrtf(l2));
 }
 
+// The pairs of particle k that pass test, in walk order: term(j, P[j]).
+// With C.nbr the walk only records them and the terms are summed over the
+// list (four gathers at a time); without it, or past the list's capacity,
+// the terms run inside the walk.
+template <class T, class B>
+__device__ __forceinline__ void record_then_sum(const SimConsts &C, int k, float3 pk, const float4 *__restrict__ P,
+                                                const GridView &v, const StageShared *S, int g, T &test, B &term)
+{
+    int cnt = -1;
+    if (C.nbr) {
+        ListWriter list(C.nbr, C.nbr_cap, C.n, k);
+        walk_neighbors<true>(k, pk, 0, P, v, C, S, g, test, [&](int j, float4) { list.push(j); });
+        cnt = list.finish();
+        if (cnt >= 0) for_each_in_list<false>(C.nbr, C.n, k, cnt, P, term);
+    }
+    if (cnt < 0) walk_neighbors<true>(k, pk, 0, P, v, C, S, g, test, term);
+}
+
 // Walk A: lambda-bar and the position gradient of the correction terms.
 __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const float4 *__restrict__ P,
                                                              const float *__restrict__ mass,
@@ -386,15 +404,13 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const 
     const float3 gk = ld3(gOut, k);
     float lb = 0.f;
     float3 pb = make_float3(0.f, 0.f, 0.f);
-    walk_neighbors<true>(
-        k, pk, 0, P, grid_view(C, sc, off), C, &S, g,
-        [&](int j, float4 pj4) {
-            const float3 r = sub3(pk, f3(pj4));
-            const float d2 = dotf(r, r);
-            const bool inc = (j > k) ? (phk < 0) : (phase_of(pj4) < 0);
-            return j != k && d2 <= C.h2 && d2 > 0.f && inc;
-        },
-        [&](int j, float4 pj4) {
+    auto test = [&](int j, float4 pj4) {
+        const float3 r = sub3(pk, f3(pj4));
+        const float d2 = dotf(r, r);
+        const bool inc = (j > k) ? (phk < 0) : (phase_of(pj4) < 0);
+        return j != k && d2 <= C.h2 && d2 > 0.f && inc;
+    };
+    auto term = [&](int j, float4 pj4) {
             const float3 r = sub3(pk, f3(pj4));
             const float d2 = dotf(r, r);
             const float rl = sqrtf(d2);
@@ -419,7 +435,8 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const 
             const float3 rb2 = add3(mul3(spiky_hess_mul(sp, r, rl, u2b), s), mul3(dsc, sb2));
             lb += sb1 + sb2;
             pb = add3(pb, sub3(rb1, rb2));
-        });
+    };
+    record_then_sum(C, k, pk, P, grid_view(C, sc, off), &S, g, test, term);
     gLam[k] = lb;
     gPart[k] = f4(pb);
 }
@@ -449,16 +466,15 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_lambda(SimConsts C, const 
     const float rbk = rho_bar(k, phk);
     const float mk = mass[k] * (phk < 0 ? 1.f : C.solid_scale);
     float3 pb = make_float3(0.f, 0.f, 0.f);
-    walk_neighbors<true>(
-        k, pk, 0, P, grid_view(C, sc, off), C, &S, g,
-        [&](int j, float4 pj4) { return j != k && dotf(sub3(pk, f3(pj4)), sub3(pk, f3(pj4))) <= C.h2; },
-        [&](int j, float4 pj4) {
-            const int phj = phase_of(pj4);
-            const float3 r = sub3(pk, f3(pj4));
-            const float3 gw = poly6_grad(C, r, dotf(r, r));
-            if (j > k) pb = add3(pb, mul3(gw, rbk * mass[j] * (phj < 0 ? 1.f : C.solid_scale)));
-            else pb = add3(pb, mul3(gw, rho_bar(j, phj) * mk));
-        });
+    auto test = [&](int j, float4 pj4) { return j != k && dotf(sub3(pk, f3(pj4)), sub3(pk, f3(pj4))) <= C.h2; };
+    auto term = [&](int j, float4 pj4) {
+        const int phj = phase_of(pj4);
+        const float3 r = sub3(pk, f3(pj4));
+        const float3 gw = poly6_grad(C, r, dotf(r, r));
+        if (j > k) pb = add3(pb, mul3(gw, rbk * mass[j] * (phj < 0 ? 1.f : C.solid_scale)));
+        else pb = add3(pb, mul3(gw, rho_bar(j, phj) * mk));
+    };
+    record_then_sum(C, k, pk, P, grid_view(C, sc, off), &S, g, test, term);
     gIn[k] = f4(add3(add3(ld3(gOut, k), ld3(gPart, k)), pb));
 }
 

@@ -279,10 +279,15 @@ bp_status ensure_grads(Tape &t, const bp_solver *s)
 void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &start, const SubstepTape &T)
 {
     const cudaStream_t st = s->stream;
-    SimConsts C = u.C;  // the adjoint walks take the 27 cells
+    SimConsts C = u.C;  // the adjoint walks take the 27 cells, recording their pairs in the list buffer
     C.vl = nullptr;
     C.nl_pos = nullptr;
     C.nl_stats = nullptr;
+    if (!(u.prm.walk_options & BP_WALK_NO_LISTS)) {
+        C.nbr = s->nbr;
+        C.nbr_count = nullptr;  // the lists live only inside one launch
+        C.nbr_cap = kPostListCap;
+    }
     const bp_params &p = u.prm;
     const bool planes = stage_on(p, BP_STAGE_PLANES) && s->nplanes > 0;
     const bool distance = stage_on(p, BP_STAGE_DISTANCE) && s->dist.num_edges > 0;
