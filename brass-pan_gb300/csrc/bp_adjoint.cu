@@ -499,21 +499,20 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_xsph(SimConsts C, const fl
     }
     const float3 pi = f3(pi4), vi = ld3(V, i);
     float3 gv = go, gp = make_float3(0.f, 0.f, 0.f);
-    walk_neighbors<true>(
-        i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, &S, g,
-        [&](int j, float4 pj4) {
-            const float3 r = sub3(pi, f3(pj4));
-            return j != i && phase_of(pj4) == phi && dotf(r, r) <= C.h2;
-        },
-        [&](int j, float4 pj4) {
-            const float3 r = sub3(pi, f3(pj4));
-            const float d2 = dotf(r, r);
-            const float w = poly6(C, d2);
-            const float3 gj = ld3(gVout, j);
-            gv = add3(gv, mul3(sub3(gj, go), C.xsph_c * w));
-            const float3 dv = sub3(ld3(V, j), vi);
-            gp = add3(gp, mul3(poly6_grad(C, r, d2), C.xsph_c * dotf(dv, sub3(go, gj))));
-        });
+    auto test = [&](int j, float4 pj4) {
+        const float3 r = sub3(pi, f3(pj4));
+        return j != i && phase_of(pj4) == phi && dotf(r, r) <= C.h2;
+    };
+    auto term = [&](int j, float4 pj4) {
+        const float3 r = sub3(pi, f3(pj4));
+        const float d2 = dotf(r, r);
+        const float w = poly6(C, d2);
+        const float3 gj = ld3(gVout, j);
+        gv = add3(gv, mul3(sub3(gj, go), C.xsph_c * w));
+        const float3 dv = sub3(ld3(V, j), vi);
+        gp = add3(gp, mul3(poly6_grad(C, r, d2), C.xsph_c * dotf(dv, sub3(go, gj))));
+    };
+    record_then_sum(C, i, pi, P, grid_view(C, scene_index(C, i), off), &S, g, test, term);
     gVin[i] = f4(gv);
     gX[i] = f4(add3(ld3(gX, i), gp));
 }

@@ -305,7 +305,7 @@ constexpr int kWalkCells = -1;
 __device__ __forceinline__ int post_list_count(const SimConsts &C, const float4 *__restrict__ P, int i)
 {
     if (i >= C.n || phase_of(P[i]) >= 0) return 0;
-    if (!C.nbr) return kWalkCells;
+    if (!C.nbr || !C.nbr_count) return kWalkCells;
     const int cnt = __ldg(C.nbr_count + i);
     return cnt >= 0 ? cnt : kWalkCells;
 }
@@ -403,14 +403,19 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_c(Sim
         if (C.textbook) wgt = __fmul_rn(wgt, __fdiv_rn(__ldg(mass + j), __ldg(rho + j)));
         vn = fma3(wgt, f3(V[j]) - vi, vn);
     };
+    auto test = [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; };
+    const GridView gv = grid_view(C, scene_index(C, i), off);
+    int own = -1;
     if (cnt != kWalkCells) {
         for_each_in_list(C.nbr, C.n, i, cnt, P, body);
-    } else {
-        walk_neighbors<Split>(
-            i, pi, 0, P, grid_view(C, scene_index(C, i), off), C, Stage ? &S : nullptr, g,
-            [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; },
-            body);
+    } else if (C.nbr && !C.nbr_count) {
+        // no pass A before it: record the walk's pairs, then sum over them
+        ListWriter list(C.nbr, C.nbr_cap, C.n, i);
+        walk_neighbors<Split>(i, pi, 0, P, gv, C, Stage ? &S : nullptr, g, test, [&](int j, float4) { list.push(j); });
+        own = list.finish();
+        if (own >= 0) for_each_in_list<false>(C.nbr, C.n, i, own, P, body);
     }
+    if (cnt == kWalkCells && own < 0) walk_neighbors<Split>(i, pi, 0, P, gv, C, Stage ? &S : nullptr, g, test, body);
     const float3 v = vi + C.xsph_c * vn;
     Vout[i] = make_float4(v.x, v.y, v.z, vi4.w);
 }

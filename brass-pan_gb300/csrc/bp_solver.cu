@@ -837,7 +837,13 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         launch_post_b(st, Cl, cur, s->Vc, s->Om, s->Nm, s->off, C.use_xsph ? s->Vs : s->Vc, L);
         if (C.use_xsph) launch_post_c(st, Cl, cur, s->Vs, s->off, s->mass, s->rho, s->Vc, L);
     } else if (C.use_xsph) {
-        launch_post_c(st, Cpost, cur, s->Vc, s->off, s->mass, s->rho, s->Vs, L);
+        SimConsts Cx = Cpost;  // records its own pairs, then sums over them
+        if (lists) {
+            Cx.nbr = s->nbr;
+            Cx.nbr_count = nullptr;
+            Cx.nbr_cap = kPostListCap;
+        }
+        launch_post_c(st, Cx, cur, s->Vc, s->off, s->mass, s->rho, s->Vs, L);
         cudaMemcpyAsync(s->Vc, s->Vs, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
     }
 }
