@@ -243,24 +243,46 @@ def dist_info():
     return rank, world, local
 
 
-def traffic_for(kernel: str, n: int, workload: str):
-    """DRAM bytes per launch of `kernel` from its committed ncu summary, scaled
-    to n particles (the traffic grows with the particle count): the late-frame
-    capture of the workload where there is one (the top kernel is profiled at
-    the end of the timed run), else the 1,048,576-particle fluid capture."""
-    import re
-
+def profile_summary(kernel: str, workload: str):
+    """The committed ncu summary of `kernel` for this workload: the late-frame
+    capture where there is one (the top kernel is profiled at the end of the
+    timed run), else the 1,048,576-particle fluid capture.  Returns (text, file)."""
     name = kernel.replace("launch_", "k_")
     for fname in (f"{name}_{workload}_late.md", f"{name}_fluid_1048576.md"):
         p = REPO / "profiles" / fname
-        if not p.exists():
-            continue
-        text = p.read_text()
+        if p.exists():
+            return p.read_text(), fname
+    return None, None
+
+
+def traffic_for(kernel: str, n: int, workload: str):
+    """DRAM bytes per launch of `kernel` from its ncu summary, scaled to n
+    particles (the traffic grows with the particle count)."""
+    import re
+
+    text, _ = profile_summary(kernel, workload)
+    if text:
         t = re.search(r"DRAM traffic of the launch: ([0-9.]+) MB", text)
         parts = re.search(r"Particles: ([0-9]+)", text)
         if t and parts:
             return float(t.group(1)) * 1e6 * n / float(parts.group(1))
     return None
+
+
+def issue_for(kernel: str, workload: str):
+    """The scan kernels are bound by instruction issue, not by HBM: issue-slot
+    use and active lanes per warp instruction from the same ncu summary."""
+    import re
+
+    text, fname = profile_summary(kernel, workload)
+    if not text:
+        return None
+    busy = re.search(r"\| issue slots busy \| ([0-9.]+) %", text)
+    lanes = re.search(r"\| active threads per warp instruction \(of 32\) \| ([0-9.]+)", text)
+    if not (busy and lanes):
+        return None
+    return {"issue_slots_busy": round(float(busy.group(1)) / 100.0, 3),
+            "active_lanes_of_32": float(lanes.group(1)), "source": "profiles/" + fname}
 
 
 def run_ours(args):
@@ -420,7 +442,8 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                         "bytes_per_particle": bytes_per, "avg_launch_ms": avg_ms},
+                         "bytes_per_particle": bytes_per, "avg_launch_ms": avg_ms,
+                         "issue": issue_for(top_name, args.workload)},
             "stages_ms_per_step": {k: round(v[1] / prof_steps, 4) for k, v in
                                    sorted(agg.items(), key=lambda kv: -kv[1][1])},
             "profiled_ms_per_step": step_ms_total,
