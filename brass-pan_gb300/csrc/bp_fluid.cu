@@ -81,16 +81,27 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
         auto test = [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; };
         if (C.nbr && !build) {
             // record first, then sum the density over the list's j >= i (the
-            // mass gathers overlap there); an overflowed list walks again
-            walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test,
-                                  [&](int j, float4) { list.push(j); });
+            // mass gathers overlap there); an overflowed list walks again.
+            // Where no column run wraps around the table the walk visits j in
+            // ascending order, so the j >= i are the entries from i itself on.
+            int self = 0;
+            walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4) {
+                if (j == i) self = list.cnt;
+                list.push(j);
+            });
             const int cnt = list.finish();
             C.nbr_count[i] = cnt;
             if (solid) return;
+            const int3 c = cell_of(pi, C);
+            auto inner = [&](int a) {
+                const unsigned t = (unsigned)a & v.mask;
+                return t != 0u && t != v.mask;
+            };
+            const int first = (inner(c.x) && inner(c.y) && inner(c.z)) ? (self & ~3) : 0;
             if (cnt >= 0)
                 for_each_in_list<false>(C.nbr, C.n, i, cnt, P, [&](int j, float4 pj) {
                     if (j >= i) dens(j, pj);
-                });
+                }, first);
             else
                 walk_neighbors<Split>(i, pi, i, P, v, C, Stage ? &S : nullptr, g, test, dens);
         } else {

@@ -249,14 +249,15 @@ struct ListWriter {
 // before the first of the four calls, so the gathers overlap.  ReadOnly:
 // the list was written by an earlier kernel (read through the read-only
 // cache); false for records the calling thread has just written itself.
+// Entries from `first` on (a multiple of 4).
 template <bool ReadOnly = true, class F>
 __device__ __forceinline__ void for_each_in_list(const int *base, int n, int i, int cnt,
-                                                 const float4 *__restrict__ P, F &&f)
+                                                 const float4 *__restrict__ P, F &&f, int first = 0)
 {
     const int4 *rec = reinterpret_cast<const int4 *>(base) + i;
     const size_t stride = (size_t)n;
 #pragma unroll 1
-    for (int k = 0; k < cnt; k += 4) {
+    for (int k = first; k < cnt; k += 4) {
         const int4 *rp = rec + (size_t)(k >> 2) * stride;
         const int4 r = ReadOnly ? __ldg(rp) : *rp;
         const int m = min(4, cnt - k);
