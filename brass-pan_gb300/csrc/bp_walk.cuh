@@ -256,10 +256,15 @@ __device__ __forceinline__ void for_each_in_list(const int *base, int n, int i, 
 {
     const int4 *rec = reinterpret_cast<const int4 *>(base) + i;
     const size_t stride = (size_t)n;
+    auto load = [&](int k) {
+        const int4 *rp = rec + (size_t)(k >> 2) * stride;
+        return ReadOnly ? __ldg(rp) : *rp;
+    };
+    int4 next = first < cnt ? load(first) : make_int4(0, 0, 0, 0);
 #pragma unroll 1
     for (int k = first; k < cnt; k += 4) {
-        const int4 *rp = rec + (size_t)(k >> 2) * stride;
-        const int4 r = ReadOnly ? __ldg(rp) : *rp;
+        const int4 r = next;
+        if (k + 4 < cnt) next = load(k + 4);  // the next record loads while these four are summed
         const int m = min(4, cnt - k);
         const int j[4] = {r.x, r.y, r.z, r.w};
         float4 pj[4];
