@@ -725,13 +725,16 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     // position pass (the same positions), which then reads them instead of
     // walking cells.
     const bool lists = !(s->prm.walk_options & BP_WALK_NO_LISTS) && s->nbr;
+    // With Verlet lists the later lambda passes read them and record the exact
+    // lists as well; the pass that builds them does not, so the position pass
+    // right after it reads the Verlet lists instead.
     SimConsts Cf = Cpost;
-    if (lists && !verlet) {
+    if (lists) {
         Cf.nbr = s->nbr;
         Cf.nbr_count = s->nbr_count;
         Cf.nbr_cap = kPostListCap;
     }
-    SimConsts Cbuild = Cf;
+    SimConsts Cbuild = verlet ? Cpost : Cf;
     Cbuild.vl_build = verlet ? 1 : 0;
 
     // the sorted order is fixed for the substep: compact its solids once
@@ -793,7 +796,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
                     planes_done = true;
                 }
             }
-            launch_deltap(st, Cf, da, L);
+            launch_deltap(st, (verlet && it == 0) ? Cpost : Cf, da, L);
             std::swap(cur, other);
         }
         if (distance) {
