@@ -20,6 +20,16 @@ namespace bp {
 
 constexpr int kScanThreads = kWalkThreads;  // scan kernels stage their neighbourhood (bp_walk.cuh)
 
+// CTAs per SM the list-reading passes are compiled for: they mostly wait on
+// the lists' gathers, so they gain from more resident warps (position pass,
+// 4 -> 5: 3.4 -> 3.1 ms per frame late, 48 registers with a few bytes spilled).
+#ifndef BP_DELTAP_MIN_BLOCKS
+#define BP_DELTAP_MIN_BLOCKS 5
+#endif
+#ifndef BP_POSTBC_MIN_BLOCKS
+#define BP_POSTBC_MIN_BLOCKS BP_SCAN_MIN_BLOCKS
+#endif
+
 // Ends the Verlet list build of particle i (SimConsts::vl): its count, and
 // the cell and position the list holds for (cell -1: no list, because it
 // overflowed or the particle's column runs wrap around the table).
@@ -185,7 +195,7 @@ void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // the lists k_lambda recorded at the same positions (r^2 <= h^2, walk order);
 // particles whose list overflowed walk their cells.
 template <bool Split, bool Stage>
-__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_deltap(SimConsts C, DeltaArgs a)
+__global__ void __launch_bounds__(kScanThreads, BP_DELTAP_MIN_BLOCKS) k_deltap(SimConsts C, DeltaArgs a)
 {
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
@@ -326,7 +336,7 @@ __device__ __forceinline__ int post_list_count(const SimConsts &C, const float4 
 // v'' = v' + F dt, exactly the reference's sequence (in-place update followed
 // by newVelocities = velocities + F dt).  Solids pass through.
 template <bool Split, bool Stage>
-__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_b(SimConsts C, const float4 *__restrict__ P,
+__global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_b(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
                                                          const float4 *__restrict__ Om,
                                                          const float4 *__restrict__ Nm,
@@ -389,7 +399,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_b(Sim
 // Pass C: XSPH viscosity (fluidXSph): same phase, j != i, r^2 <= h^2 (r = 0
 // included).  Textbook mode weights each neighbour by its volume m_j / rho_j.
 template <bool Split, bool Stage>
-__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_c(SimConsts C, const float4 *__restrict__ P,
+__global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_c(SimConsts C, const float4 *__restrict__ P,
                                                          const float4 *__restrict__ V,
                                                          const int *__restrict__ off, const float *__restrict__ mass,
                                                          const float *__restrict__ rho, float4 *__restrict__ Vout)
