@@ -101,7 +101,9 @@ __global__ void __launch_bounds__(kScanBlock) k_solid_scan_totals(int nb, int *_
 
 __global__ void __launch_bounds__(kScanBlock) k_solid_scatter(int n, const float4 *__restrict__ P,
                                                               const int *__restrict__ block_base,
-                                                              int *__restrict__ prefix, int *__restrict__ list)
+                                                              int *__restrict__ prefix, int *__restrict__ list,
+                                                              const int *__restrict__ keys,
+                                                              unsigned long long *__restrict__ cells)
 {
     __shared__ int warp_sum[kScanBlock / 32];
     const int i = blockIdx.x * kScanBlock + threadIdx.x;
@@ -117,18 +119,65 @@ __global__ void __launch_bounds__(kScanBlock) k_solid_scatter(int n, const float
         prefix[i] = pos;
         if (solid) list[pos] = i;
     }
+    if (solid && cells) {
+        const unsigned key = (unsigned)__ldg(keys + i);
+        atomicOr(cells + (key >> 6), 1ull << (key & 63u));
+    }
 }
 
-void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int *prefix, int *list, LaunchLog *L)
+// near[c] = some cell of the 27 around table cell c (the same masked
+// neighbours a walk visits) stores a solid.  One thread per 64-bit word: with
+// D >= 64 a word is 64 consecutive z of one (x, y) row, dilated in z by
+// shifts and in x, y by the OR over the 9 rows; smaller grids test each bit.
+__global__ void __launch_bounds__(256) k_solid_dilate(int D, int nwords, const unsigned long long *__restrict__ cells,
+                                                      unsigned long long *__restrict__ near)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nwords) return;
+    const unsigned m = (unsigned)D - 1u, DD = (unsigned)D * (unsigned)D;
+    unsigned long long acc = 0ull;
+    if (D >= 64) {
+        const unsigned key0 = (unsigned)k * 64u, wpr = (unsigned)D / 64u;
+        const unsigned x = key0 / DD, y = (key0 / (unsigned)D) & m, zw = (key0 & m) / 64u;
+        const unsigned zp = (zw + wpr - 1u) % wpr, zn = (zw + 1u) % wpr;
+        for (int r = 0; r < 9; ++r) {
+            const unsigned rb = (((x + r / 3 - 1) & m) * DD + ((y + r % 3 - 1) & m) * (unsigned)D) / 64u;
+            const unsigned long long w = __ldg(cells + rb + zw);
+            acc |= w | (w << 1) | (w >> 1) | (__ldg(cells + rb + zp) >> 63) | (__ldg(cells + rb + zn) << 63);
+        }
+    } else {
+        for (int b = 0; b < 64; ++b) {
+            const unsigned key = (unsigned)k * 64u + (unsigned)b;
+            const unsigned x = key / DD, y = (key / (unsigned)D) & m, z = key & m;
+            bool any = false;
+            for (int t = 0; t < 27 && !any; ++t) {
+                const unsigned a = ((x + t / 9 - 1) & m) * DD + ((y + (t / 3) % 3 - 1) & m) * (unsigned)D +
+                                   ((z + t % 3 - 1) & m);
+                any = (__ldg(cells + (a >> 6)) >> (a & 63u)) & 1ull;
+            }
+            if (any) acc |= 1ull << b;
+        }
+    }
+    near[k] = acc;
+}
+
+void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int *prefix, int *list,
+                       const SolidCells &sc, LaunchLog *L)
 {
     if (n <= 0) return;
     const int nb = (n + kScanBlock - 1) / kScanBlock;
+    const int nwords = sc.cells ? (int)((size_t)sc.D * sc.D * sc.D / 64) : 0;
+    if (sc.cells) cudaMemsetAsync(sc.cells, 0, (size_t)nwords * sizeof(unsigned long long), st);
     k_solid_count<<<nb, kScanBlock, 0, st>>>(n, P, totals);
     L->done("k_solid_count");
     k_solid_scan_totals<<<1, kScanBlock, 0, st>>>(nb, totals, prefix, n);
     L->done("k_solid_scan_totals");
-    k_solid_scatter<<<nb, kScanBlock, 0, st>>>(n, P, totals, prefix, list);
+    k_solid_scatter<<<nb, kScanBlock, 0, st>>>(n, P, totals, prefix, list, sc.keys, sc.cells);
     L->done("k_solid_scatter");
+    if (sc.cells) {
+        k_solid_dilate<<<(nwords + 255) / 256, 256, 0, st>>>(sc.D, nwords, sc.cells, sc.near);
+        L->done("k_solid_dilate");
+    }
 }
 
 // The solids among the candidates of particle i's 27 cells, in walk order:
@@ -227,13 +276,16 @@ __device__ __forceinline__ void collide_one(const SimConsts &C, int i, const flo
 // Fluid particles (and, without a solid list, everything), one CTA per 256
 // sorted particles.  A CTA of fluid whose runs touch no tile holding a solid
 // skips the walks: none of its particles that stayed in their stored cell
-// can meet a solid.
+// can meet a solid.  So does a fluid particle whose current cell has no
+// solid stored in its 27 cells (solid_near, k_solid_dilate): its walk over
+// the solids would visit none.
 template <bool Split>
 __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS)
     k_particle_collision(SimConsts C, const float4 *__restrict__ P, const float4 *__restrict__ Xs,
                          const float *__restrict__ w, const int *__restrict__ off, const int *__restrict__ tile_solid,
                          const int *__restrict__ solid_prefix, const int *__restrict__ solid_list,
-                         int solids_apart, float4 *__restrict__ Pout)
+                         const unsigned long long *__restrict__ solid_near, int solids_apart,
+                         float4 *__restrict__ Pout)
 {
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kWalkThreads;
@@ -248,8 +300,10 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS)
     const GridView v = grid_view(C, scene_index(C, i), off);
     const float3 xip = f3(pi4);
     const int3 ci = cell_of(xip, C);
-    const bool in_cell = cell_addr(ci.x, ci.y, ci.z, v.D, v.mask) + v.base == __ldg(C.cell_keys + i);
-    if (phi < 0 && in_cell && (g == kNoSolidNear || (g >= 0 && !S.has_solid))) {
+    const int cur_key = cell_addr(ci.x, ci.y, ci.z, v.D, v.mask);
+    const bool in_cell = cur_key + v.base == __ldg(C.cell_keys + i);
+    const bool none_near = solid_near && !((__ldg(solid_near + (cur_key >> 6)) >> (cur_key & 63)) & 1ull);
+    if (phi < 0 && (none_near || (in_cell && (g == kNoSolidNear || (g >= 0 && !S.has_solid))))) {
         const float3 p = xip + make_float3(0.f, 0.f, 0.f);
         Pout[i] = make_float4(p.x, p.y, p.z, pi4.w);
         track_displacement(C, i, p, true);
@@ -275,17 +329,20 @@ __global__ void __launch_bounds__(kWalkThreads)
 
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
                                const float *w, const int *off, const int *tile_solid, const int *solid_prefix,
-                               const int *solid_list, int nsolid, bool solids_apart, float4 *Pout, LaunchLog *L)
+                               const int *solid_list, int nsolid, bool solids_apart,
+                               const unsigned long long *solid_near, float4 *Pout, LaunchLog *L)
 {
     if (C.n <= 0) return;
     const int grid = (C.n + kWalkThreads - 1) / kWalkThreads;
     const int apart = (solids_apart && solid_list && nsolid > 0) ? 1 : 0;
+    // the cell mask describes the walks over the compacted solids only
+    const unsigned long long *near = (apart && solid_prefix) ? solid_near : nullptr;
     if (C.split)
         k_particle_collision<true><<<grid, kWalkThreads, stage_bytes(C), st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
-                                                                 solid_list, apart, Pout);
+                                                                 solid_list, near, apart, Pout);
     else
         k_particle_collision<false><<<grid, kWalkThreads, stage_bytes(C), st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
-                                                                  solid_list, apart, Pout);
+                                                                  solid_list, near, apart, Pout);
     L->done(__func__);
     if (apart) {
         const int sg = (nsolid + kWalkThreads - 1) / kWalkThreads;

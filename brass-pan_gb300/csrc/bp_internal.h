@@ -149,13 +149,23 @@ void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // tile_solid: nullptr, or one flag per 256 sorted particles (the tile holds a solid);
 // solid_prefix / solid_list: nullptr, or the compacted solids (launch_solid_list)
 // solids_apart: the nsolid solids of the list walk in a second launch over the list.
+// solid_near: nullptr, or SolidCells::near of the same sorted order.
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
                                const float *w, const int *off, const int *tile_solid, const int *solid_prefix,
-                               const int *solid_list, int nsolid, bool solids_apart, float4 *Pout, LaunchLog *L);
+                               const int *solid_list, int nsolid, bool solids_apart,
+                               const unsigned long long *solid_near, float4 *Pout, LaunchLog *L);
+// Bit masks over the D^3 table cells of one scene (cells == nullptr: not built):
+// cells marks the stored cells (keys) of the solids, near the cells whose 27
+// cells hold one.
+struct SolidCells {
+    int D = 0;
+    const int *keys = nullptr;  // stored cell of every sorted particle
+    unsigned long long *cells = nullptr, *near = nullptr;  // D^3 / 64 words each
+};
 // solid_prefix[i] (i <= n): solids among sorted [0, i); solid_list: their sorted indices in order.
 // totals: (n + 1023) / 1024 ints of scratch.
 void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int *solid_prefix, int *solid_list,
-                       LaunchLog *L);
+                       const SolidCells &sc, LaunchLog *L);
 struct DistanceArgs {
     int num_edges;
     const int2 *pairs;       // original ids

@@ -378,6 +378,11 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         (st = s->alloc(&s->nbr, N * kPostListCap)) ||
         (st = s->alloc(&s->nbr_count, N)))
         return bail(st);
+    // fluid next to solids: the cell masks that let fluid far from every
+    // solid skip its walk over the solids (one scene's table)
+    if (!batch && s->num_solids > 0 && s->num_solids < n &&
+        ((st = s->alloc(&s->solid_cells, ncells / 64)) || (st = s->alloc(&s->solid_near, ncells / 64))))
+        return bail(st);
     if (n > 0) {
         BP_CUDA_BAIL(cudaMemcpy(s->Xc, X.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
         BP_CUDA_BAIL(cudaMemcpy(s->Vc, V.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
@@ -738,7 +743,16 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     Cbuild.vl_build = verlet ? 1 : 0;
 
     // the sorted order is fixed for the substep: compact its solids once
-    if (pcoll) launch_solid_list(st, s->n, cur, s->solid_totals, s->solid_prefix, s->solid_list, L);
+    if (pcoll) {
+        SolidCells sc;
+        if (s->solid_cells) {
+            sc.D = C.D;
+            sc.keys = s->sorted_keys;
+            sc.cells = s->solid_cells;
+            sc.near = s->solid_near;
+        }
+        launch_solid_list(st, s->n, cur, s->solid_totals, s->solid_prefix, s->solid_list, sc, L);
+    }
     if (wind) {
         if (tape) tape->push(TS_WIND, cur);
         launch_wind(st, Cpre, s->wind, cur, s->Vs, s->mass, s->to_new, L);
@@ -761,7 +775,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             // scattered through fluid or the whole scene)
             refresh(cur);
             launch_particle_collision(st, Cit, cur, s->Xs, s->w, s->off, s->tile_solid, s->solid_prefix,
-                                      s->solid_list, s->num_solids, true, other, L);
+                                      s->solid_list, s->num_solids, true, s->solid_near, other, L);
             std::swap(cur, other);
         }
         if (fluid) {

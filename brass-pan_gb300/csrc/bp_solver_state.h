@@ -119,6 +119,7 @@ struct bp_solver {
     unsigned *err = nullptr;
     int *tile_solid = nullptr;  // per 256 sorted particles: the tile holds a solid
     int *solid_prefix = nullptr, *solid_list = nullptr, *solid_totals = nullptr;  // compacted solids
+    unsigned long long *solid_cells = nullptr, *solid_near = nullptr;  // SolidCells masks (one scene with fluid)
     int *nbr = nullptr, *nbr_count = nullptr;  // post-pass neighbour lists [kPostListCap][N], counts
     SortScratch sort{};
     // alias classes (SimConsts::cls_perm); cls.perm == nullptr: not allocated

@@ -67,3 +67,27 @@ def test_batch_scene_ranges_and_step(bp, gpu):
         assert (xs >= -1e-3).all()
         assert (xs[:, [0, 2]] <= hi[[0, 2]] + 1e-3).all()
     batch.close()
+
+
+@pytest.mark.parametrize("grid_dim", [16, 64, 128])
+def test_solid_cell_masks_keep_collision_bits(bp, gpu, grid_dim):
+    """A single-scene solver lets fluid skip its walk over the solids where
+    no solid is stored in its 27 cells (a per-substep cell mask); a batch
+    walks them all.  The mixed scene sits across z cell 63/64 (x + 50000 over
+    the cell size, masked), so the mask's dilation wraps rows (64) and crosses
+    words (128); bodies fall onto the fluid within the frames run."""
+    s = small_mixed_scene(bp, seed=7, grid_dim=grid_dim)
+    dz = 9.3
+    s.positions[:, 2] += dz
+    s.planes[:, 2] += dz
+    p = bp.make_params(s)
+    single = bp.ParticleSolver(s, p)
+    batch = bp.BatchSolver([s], [p])
+    for _ in range(20):
+        single.update(2, DT, 4)
+        batch.update(2, DT, 4)
+    np.testing.assert_array_equal(batch.positions(), single.positions())
+    np.testing.assert_array_equal(batch.velocities(), single.velocities())
+    assert single.device_errors() == 0 and batch.device_errors() == 0
+    single.close()
+    batch.close()
