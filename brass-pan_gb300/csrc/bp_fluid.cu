@@ -60,8 +60,9 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
     const int g = Stage ? stage_block(C, P, off, i0, S) : -1;
-    const int i = i0 + threadIdx.x;
-    if (i >= C.n) return;
+    const int t = i0 + threadIdx.x;  // the slot of the position pass's list
+    if (t >= C.n) return;
+    const int i = Stage ? t : walker_index(C, t);
     const float4 pi4 = P[i];
     const bool build = C.vl_build != 0;
     const bool rec = build || C.nbr != nullptr;
@@ -77,11 +78,12 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
     const float3 pi = f3(pi4);
     const float r2 = build ? C.nl_hs2 : C.h2;
     float density = 0.f;
-    ListWriter list(build ? C.vl : C.nbr, build ? C.vl_cap : C.nbr_cap, C.n, i);
+    // Verlet lists are kept per particle, the position pass's lists per slot
+    ListWriter list(build ? C.vl : C.nbr, build ? C.vl_cap : C.nbr_cap, C.n, build ? i : t);
     auto finish = [&]() {
         const int cnt = list.finish();
         if (build) finish_verlet(C, i, pi4, cnt);
-        else C.nbr_count[i] = cnt;
+        else C.nbr_count[t] = cnt;
     };
     if (!C.textbook) {
         auto dens = [&](int j, float4 pj) {
@@ -100,7 +102,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
                 list.push(j);
             });
             const int cnt = list.finish();
-            C.nbr_count[i] = cnt;
+            C.nbr_count[t] = cnt;
             if (solid) return;
             const int3 c = cell_of(pi, C);
             auto inner = [&](int a) {
@@ -109,7 +111,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
             };
             const int first = (inner(c.x) && inner(c.y) && inner(c.z)) ? (self & ~3) : 0;
             if (cnt >= 0)
-                for_each_in_list<false>(C.nbr, C.n, i, cnt, P, [&](int j, float4 pj) {
+                for_each_in_list<false>(C.nbr, C.n, t, cnt, P, [&](int j, float4 pj) {
                     if (j >= i) dens(j, pj);
                 }, first);
             else
@@ -148,8 +150,8 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
             walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test,
                                   [&](int j, float4) { list.push(j); });
             const int cnt = list.finish();
-            C.nbr_count[i] = cnt;
-            if (cnt >= 0) for_each_in_list<false>(C.nbr, C.n, i, cnt, P, term);
+            C.nbr_count[t] = cnt;
+            if (cnt >= 0) for_each_in_list<false>(C.nbr, C.n, t, cnt, P, term);
             else walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, term);
         } else {
             walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4 pj) {
@@ -199,12 +201,13 @@ __global__ void __launch_bounds__(kScanThreads, BP_DELTAP_MIN_BLOCKS) k_deltap(S
 {
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
-    const int k = i0 + threadIdx.x;
-    const bool valid = k < C.n;
+    const int t = i0 + threadIdx.x;  // the slot of k's list (k_lambda)
+    const bool valid = t < C.n;
+    const int k = (Stage || !valid) ? t : walker_index(C, t);
     const float4 pk4 = valid ? a.P[k] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int phk = phase_of(pk4);
     const bool moves = valid && !(C.textbook && phk > 0);
-    const int listed = (moves && C.nbr) ? __ldg(C.nbr_count + k) : -1;
+    const int listed = (moves && C.nbr) ? __ldg(C.nbr_count + t) : -1;
     const bool walk = moves && listed < 0;
     const int g = (Stage && __syncthreads_or(walk)) ? stage_block(C, a.P, a.off, i0, S) : -1;
     if (!valid) return;
@@ -231,7 +234,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_DELTAP_MIN_BLOCKS) k_deltap(S
             auto listed_body = [&](int j, float4 pj4) {  // r = 0 excludes k itself
                 if (len2(pk - f3(pj4)) > 0.f) body(j, pj4);
             };
-            for_each_in_list(C.nbr, C.n, k, listed, a.P, listed_body);
+            for_each_in_list(C.nbr, C.n, t, listed, a.P, listed_body);
         } else {
             walk_neighbors<Split>(
                 k, pk, 0, a.P, grid_view(C, sc, a.off), C, Stage ? &S : nullptr, g,
@@ -275,8 +278,9 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
     const int g = Stage ? stage_block(C, P, off, i0, S) : -1;
-    const int i = i0 + threadIdx.x;
-    if (i >= C.n) return;
+    const int t = i0 + threadIdx.x;  // the slot of the list passes B and C read
+    if (t >= C.n) return;
+    const int i = Stage ? t : walker_index(C, t);
     const float4 pi4 = P[i];
     const int phi = phase_of(pi4);
     if (phi >= 0) return;
@@ -301,14 +305,14 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
     // overflowed is summed by walking again.
     int cnt = -1;
     if (C.nbr) {
-        ListWriter list(C.nbr, C.nbr_cap, C.n, i);
+        ListWriter list(C.nbr, C.nbr_cap, C.n, t);
         walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4 pj4) {
             if (j != i && phase_of(pj4) == phi) list.push(j);
         });
         cnt = list.finish();
-        C.nbr_count[i] = cnt;
+        C.nbr_count[t] = cnt;
         // the records just written come back through the coherent path (plain loads)
-        if (cnt >= 0) for_each_in_list<false>(C.nbr, C.n, i, cnt, P, term);
+        if (cnt >= 0) for_each_in_list<false>(C.nbr, C.n, t, cnt, P, term);
     }
     if (cnt < 0)
         walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4 pj4) {
@@ -319,15 +323,15 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
     Nm[i] = make_float4(n.x, n.y, n.z, rho[i]);
 }
 
-// Passes B and C: the number of recorded neighbours of particle i, or
-// kWalkCells when it must walk its cells (no lists, or they overflowed).
-// Solids and indices past the end need neither (0).
+// Passes B and C: the number of recorded neighbours of particle i (its list
+// in slot t, k_post_a), or kWalkCells when it must walk its cells (no lists,
+// or they overflowed).  Solids and indices past the end need neither (0).
 constexpr int kWalkCells = -1;
-__device__ __forceinline__ int post_list_count(const SimConsts &C, const float4 *__restrict__ P, int i)
+__device__ __forceinline__ int post_list_count(const SimConsts &C, const float4 *__restrict__ P, int i, int t)
 {
     if (i >= C.n || phase_of(P[i]) >= 0) return 0;
     if (!C.nbr || !C.nbr_count) return kWalkCells;
-    const int cnt = __ldg(C.nbr_count + i);
+    const int cnt = __ldg(C.nbr_count + t);
     return cnt >= 0 ? cnt : kWalkCells;
 }
 
@@ -344,8 +348,9 @@ __global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_b(S
 {
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
-    const int i = i0 + threadIdx.x;
-    const int cnt = post_list_count(C, P, i);
+    const int t = i0 + threadIdx.x;
+    const int i = (Stage || t >= C.n) ? t : walker_index(C, t);
+    const int cnt = post_list_count(C, P, i, t);
     const int g = (Stage && __syncthreads_or(cnt == kWalkCells)) ? stage_block(C, P, off, i0, S) : -1;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
@@ -379,7 +384,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_b(S
         }
     };
     if (cnt != kWalkCells) {
-        for_each_in_list(C.nbr, C.n, i, cnt, P, body);
+        for_each_in_list(C.nbr, C.n, t, cnt, P, body);
     } else {
         walk_neighbors<Split>(
             i, pi, 0, P, grid_view(C, sc, off), C, Stage ? &S : nullptr, g,
@@ -406,8 +411,9 @@ __global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_c(S
 {
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kScanThreads;
-    const int i = i0 + threadIdx.x;
-    const int cnt = post_list_count(C, P, i);
+    const int t = i0 + threadIdx.x;
+    const int i = (Stage || t >= C.n) ? t : walker_index(C, t);
+    const int cnt = post_list_count(C, P, i, t);
     const int g = (Stage && __syncthreads_or(cnt == kWalkCells)) ? stage_block(C, P, off, i0, S) : -1;
     if (i >= C.n) return;
     const float4 pi4 = P[i];
@@ -428,13 +434,13 @@ __global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_c(S
     const GridView gv = grid_view(C, scene_index(C, i), off);
     int own = -1;
     if (cnt != kWalkCells) {
-        for_each_in_list(C.nbr, C.n, i, cnt, P, body);
+        for_each_in_list(C.nbr, C.n, t, cnt, P, body);
     } else if (C.nbr && !C.nbr_count) {
         // no pass A before it: record the walk's pairs, then sum over them
-        ListWriter list(C.nbr, C.nbr_cap, C.n, i);
+        ListWriter list(C.nbr, C.nbr_cap, C.n, t);
         walk_neighbors<Split>(i, pi, 0, P, gv, C, Stage ? &S : nullptr, g, test, [&](int j, float4) { list.push(j); });
         own = list.finish();
-        if (own >= 0) for_each_in_list<false>(C.nbr, C.n, i, own, P, body);
+        if (own >= 0) for_each_in_list<false>(C.nbr, C.n, t, own, P, body);
     }
     if (cnt == kWalkCells && own < 0) walk_neighbors<Split>(i, pi, 0, P, gv, C, Stage ? &S : nullptr, g, test, body);
     const float3 v = vi + C.xsph_c * vn;

@@ -177,6 +177,16 @@ __device__ __forceinline__ int staged_index(const StageShared &S, int g, int k, 
     return -1;
 }
 
+// The particle that thread t (< n) of an unstaged walking kernel takes:
+// sorted particle t, or, while the walks use the alias classes, the t-th
+// particle of class order.  A warp's particles then share one class, so
+// their runs coincide instead of splitting between the classes interleaved
+// in a table cell.  Each particle's own result does not depend on the thread.
+__device__ __forceinline__ int walker_index(const SimConsts &C, int t)
+{
+    return (C.cls_perm && __ldg(C.cls_moved) == 0) ? __ldg(C.cls_perm + t) : t;
+}
+
 // Does particle i walk its CTA's staged runs (it is still in its stored cell)?
 __device__ __forceinline__ bool walks_staged(const SimConsts &C, const GridView &v, int i, int3 c,
                                              const StageShared *S, int g)
