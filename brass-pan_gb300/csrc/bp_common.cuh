@@ -122,7 +122,18 @@ struct SimConsts {
     const float4 *cls_pos;  // P in class order
     const int *cls_moved;
     int cls_T;              // cell keys of all scenes
+    // Class-order copies for the position pass's slot lists (k_lambda):
+    // masses (k_class_keys) and the lambdas k_lambda writes beside lam.
+    const float *cls_mass;
+    float *cls_lam;
 };
+
+// The walks use the alias classes for the rest of the substep (uniform
+// over a launch: the flag is written by k_class_refresh before it).
+__device__ __forceinline__ bool classes_on(const SimConsts &C)
+{
+    return C.cls_perm && __ldg(C.cls_moved) == 0;
+}
 
 // Class (0..7) of real cell c on a table of D cells per axis (D a power of two).
 __device__ __forceinline__ int alias_class(int x, int y, int z, int D)

@@ -66,8 +66,15 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
     const float4 pi4 = P[i];
     const bool build = C.vl_build != 0;
     const bool rec = build || C.nbr != nullptr;
+    // Slot lists: while the threads take class order (and no Verlet list can
+    // stand in for a walk) the list holds class positions, and the position
+    // pass gathers positions, masses and lambdas from the class-order copies.
+    const bool slots = !Stage && C.nbr && !build && !C.vl && classes_on(C);
     const bool solid = phase_of(pi4) > 0;
-    if (solid) lam[i] = 0.f;  // solids carry lambda 0 (read by the position pass)
+    if (solid) {  // solids carry lambda 0 (read by the position pass)
+        lam[i] = 0.f;
+        if (slots) C.cls_lam[t] = 0.f;
+    }
     if (solid && (C.textbook || !rec)) {
         if (build) C.nl_cell[i] = -1;
         return;
@@ -85,11 +92,31 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
         if (build) finish_verlet(C, i, pi4, cnt);
         else C.nbr_count[t] = cnt;
     };
+    auto record = [&](int &self) {  // entries: sorted indices, or class positions (slots)
+        auto push = [&](int j, float4) {
+            if (j == (slots ? t : i)) self = list.cnt;
+            list.push(j);
+        };
+        auto test = [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; };
+        if (slots) {  // the walk walk_neighbors takes here (no staging, no Verlet list)
+            if (C.nl_stats) {
+                atomicAdd(C.nl_stats + 1, 1u);
+                atomicAdd(C.nl_stats + 4, 1u);
+            }
+            walk_classes<Split, true>(i, cell_of(pi, C), 0, v, C, test, push);
+        } else {
+            walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, push);
+        }
+        const int cnt = list.finish();
+        C.nbr_count[t] = cnt;
+        return cnt;
+    };
     if (!C.textbook) {
-        auto dens = [&](int j, float4 pj) {
-            const float ld = __fmul_rn(__ldg(mass + j), poly6(C, len2(pi - f3(pj))));
+        auto dens_m = [&](float mj, float4 pj) {
+            const float ld = __fmul_rn(mj, poly6(C, len2(pi - f3(pj))));
             density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
         };
+        auto dens = [&](int j, float4 pj) { dens_m(__ldg(mass + j), pj); };
         auto test = [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; };
         if (C.nbr && !build) {
             // record first, then sum the density over the list's j >= i (the
@@ -97,25 +124,29 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
             // Where no column run wraps around the table the walk visits j in
             // ascending order, so the j >= i are the entries from i itself on.
             int self = 0;
-            walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4) {
-                if (j == i) self = list.cnt;
-                list.push(j);
-            });
-            const int cnt = list.finish();
-            C.nbr_count[t] = cnt;
+            const int cnt = record(self);
             if (solid) return;
             const int3 c = cell_of(pi, C);
             auto inner = [&](int a) {
-                const unsigned t = (unsigned)a & v.mask;
-                return t != 0u && t != v.mask;
+                const unsigned u = (unsigned)a & v.mask;
+                return u != 0u && u != v.mask;
             };
-            const int first = (inner(c.x) && inner(c.y) && inner(c.z)) ? (self & ~3) : 0;
-            if (cnt >= 0)
+            const bool ascending = inner(c.x) && inner(c.y) && inner(c.z);
+            const int first = ascending ? (self & ~3) : 0;
+            if (cnt >= 0 && slots) {
+                int e = first;  // entry index: ascending, the j >= i are the entries from self on
+                for_each_in_list<false>(C.nbr, C.n, t, cnt, C.cls_pos, [&](int q, float4 pj) {
+                    const bool upper = ascending ? e >= self : __ldg(C.cls_perm + q) >= i;
+                    ++e;
+                    if (upper) dens_m(__ldg(C.cls_mass + q), pj);
+                }, first);
+            } else if (cnt >= 0) {
                 for_each_in_list<false>(C.nbr, C.n, t, cnt, P, [&](int j, float4 pj) {
                     if (j >= i) dens(j, pj);
                 }, first);
-            else
+            } else {
                 walk_neighbors<Split>(i, pi, i, P, v, C, Stage ? &S : nullptr, g, test, dens);
+            }
         } else {
             walk_neighbors<Split>(i, pi, rec ? 0 : i, P, v, C, Stage ? &S : nullptr, g, test,
                                   [&](int j, float4 pj) {
@@ -129,14 +160,16 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
         float c = density / rho0 - 1.0f;
         if (C.clamp_c) c = fmaxf(c, 0.0f);
         lam[i] = -c / C.lambda_den;
+        if (slots) C.cls_lam[t] = lam[i];
     } else {
         const float inv_rho0 = inv_rest_density(C, sc);
         float sum_g2 = 0.f;
         float3 gi = make_float3(0.f, 0.f, 0.f);
+        const float *mw = slots ? C.cls_mass : mass;  // indexed by the list's entries
         auto term = [&](int j, float4 pj) {
             const float3 diff = pi - f3(pj);
             const float d2 = len2(diff);
-            const float mj = __ldg(mass + j);
+            const float mj = __ldg(mw + j);
             const float ld = __fmul_rn(mj, poly6(C, d2));
             density = __fadd_rn(density, (phase_of(pj) < 0) ? ld : __fmul_rn(C.solid_scale, ld));
             if (d2 > 0.f) {
@@ -147,12 +180,14 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
         };
         auto test = [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; };
         if (C.nbr && !build) {  // record first, then sum over the list (as above)
-            walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test,
-                                  [&](int j, float4) { list.push(j); });
-            const int cnt = list.finish();
-            C.nbr_count[t] = cnt;
-            if (cnt >= 0) for_each_in_list<false>(C.nbr, C.n, t, cnt, P, term);
-            else walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, term);
+            int self = 0;
+            const int cnt = record(self);
+            if (cnt >= 0) {
+                for_each_in_list<false>(C.nbr, C.n, t, cnt, slots ? C.cls_pos : P, term);
+            } else {
+                mw = mass;  // the walk gives sorted indices
+                walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, term);
+            }
         } else {
             walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4 pj) {
                 if (rec) list.push(j);
@@ -165,6 +200,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
         if (C.clamp_c) c = fmaxf(c, 0.0f);
         sum_g2 += dot3(gi, gi);
         lam[i] = -c / (sum_g2 + C.relaxation);
+        if (slots) C.cls_lam[t] = lam[i];
     }
     rho[i] = density;
 }
@@ -216,11 +252,10 @@ __global__ void __launch_bounds__(kScanThreads, BP_DELTAP_MIN_BLOCKS) k_deltap(S
     float3 sum = make_float3(0.f, 0.f, 0.f);
     if (moves) {
         const float lk = a.lam[k];
-        auto body = [&](int j, float4 pj4) {
-            if (!C.textbook && !((j > k) ? (phk < 0) : (phase_of(pj4) < 0))) return;
+        auto pair = [&](float4 pj4, float lj, float mj) {
             const float3 diff = pk - f3(pj4);
             const float d2 = len2(diff);
-            float sl = __fadd_rn(lk, __ldg(a.lam + j));
+            float sl = __fadd_rn(lk, lj);
             if (C.scorr_on)
                 sl = __fsub_rn(sl, __fmul_rn(C.scorr_k, ipowf(__fmul_rn(poly6(C, d2), C.scorr_inv_wq), C.scorr_ni)));
             float3 delta = sl * spiky_grad_r(C, diff, d2, rsqrtf(d2));
@@ -228,9 +263,29 @@ __global__ void __launch_bounds__(kScanThreads, BP_DELTAP_MIN_BLOCKS) k_deltap(S
                 const float l2 = len2(delta);
                 if (!(l2 < C.delta_clamp2)) delta = delta * __fmul_rn(C.delta_clamp, rsqrtf(l2));
             }
-            sum = fma3(__ldg(a.mass + j), delta, sum);
+            sum = fma3(mj, delta, sum);
         };
-        if (!walk) {
+        auto body = [&](int j, float4 pj4) {
+            if (!C.textbook && !((j > k) ? (phk < 0) : (phase_of(pj4) < 0))) return;
+            pair(pj4, __ldg(a.lam + j), __ldg(a.mass + j));
+        };
+        // slot lists (k_lambda) hold class positions q: the pair's data come
+        // from the class-order copies, the sorted index only where one of the
+        // two is a solid (the fluid-fluid pairs pass the rule either way)
+        const bool slots = !Stage && C.nbr && !C.vl && classes_on(C);
+        if (!walk && slots) {
+            for_each_in_list(C.nbr, C.n, t, listed, C.cls_pos, [&](int q, float4 pj4) {
+                if (!(len2(pk - f3(pj4)) > 0.f)) return;  // r = 0 excludes k itself
+                if (!C.textbook) {
+                    const bool fj = phase_of(pj4) < 0;
+                    if (!(phk < 0 && fj)) {
+                        const int j = __ldg(C.cls_perm + q);
+                        if (!((j > k) ? (phk < 0) : fj)) return;
+                    }
+                }
+                pair(pj4, __ldg(C.cls_lam + q), __ldg(C.cls_mass + q));
+            });
+        } else if (!walk) {
             auto listed_body = [&](int j, float4 pj4) {  // r = 0 excludes k itself
                 if (len2(pk - f3(pj4)) > 0.f) body(j, pj4);
             };

@@ -449,8 +449,8 @@ __global__ void __launch_bounds__(256) k_class_count(int n, const int *__restric
 }
 
 // keys[q] holds the class of perm[q] on entry (the radix pass output).
-__global__ void __launch_bounds__(256) k_class_keys(int n, const int *__restrict__ sorted_keys, ClassArrays a,
-                                                    Gate gate)
+__global__ void __launch_bounds__(256) k_class_keys(int n, const int *__restrict__ sorted_keys,
+                                                    const float *__restrict__ mass, ClassArrays a, Gate gate)
 {
     if (gate_closed(gate)) return;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -458,12 +458,13 @@ __global__ void __launch_bounds__(256) k_class_keys(int n, const int *__restrict
     const int j = a.perm[q];
     a.keys[q] = a.keys[q] * a.T + __ldg(sorted_keys + j);
     a.inv[j] = q;
+    a.mass[q] = __ldg(mass + j);
 }
 
 static Gate class_gate(int n, const ClassArrays &a) { return Gate{a.mixed, (n + 31) / 32}; }
 
-void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const int *off, const ClassArrays &a,
-                        const SortScratch &s, LaunchLog *L)
+void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const int *off, const float *mass,
+                        const ClassArrays &a, const SortScratch &s, LaunchLog *L)
 {
     if (n <= 0) return;
     cudaMemsetAsync(a.mixed, 0, sizeof(int), st);
@@ -473,7 +474,7 @@ void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const in
     const Gate gate = class_gate(n, a);
     // one 9-bit digit covers the 3 class bits: a stable partition of the sorted order
     radix_sort_pairs(st, n, 8, a.cls, nullptr, a.keys, a.perm, s, false, L, gate);
-    k_class_keys<<<(n + 255) / 256, 256, 0, st>>>(n, sorted_keys, a, gate);
+    k_class_keys<<<(n + 255) / 256, 256, 0, st>>>(n, sorted_keys, mass, a, gate);
     L->done("k_class_keys");
     launch_cell_offsets(st, n, 8 * a.T, a.keys, a.off, L, gate);
 }

@@ -107,13 +107,15 @@ struct ClassArrays {
     float4 *pos;     // [n] P in class order
     int *mixed;      // one word: particles whose class differs from their cell's first particle's
     int *moved;      // one word
+    float *mass;     // [n] masses in class order (k_class_keys)
+    float *lam;      // [n] lambdas in class order (k_lambda, slot lists)
     int T;           // cell keys of all scenes
     float reach2;    // squared reach (see SimConsts::cls_perm)
 };
 // After k_reorder: class order (one radix pass), keys, inverse, offsets and
 // the count of particles in cells holding two classes (off: the cell offsets).
-void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const int *off, const ClassArrays &a,
-                        const SortScratch &s, LaunchLog *L);
+void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const int *off, const float *mass,
+                        const ClassArrays &a, const SortScratch &s, LaunchLog *L);
 // Gathers P into class order and flags particles beyond the reach.
 void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L);
 

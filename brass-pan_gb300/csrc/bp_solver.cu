@@ -201,6 +201,8 @@ SimConsts bp::make_consts(const bp_solver *s, float sdt)
         C.cls_pos = s->cls.pos;
         C.cls_moved = s->cls.moved;
         C.cls_T = s->cls.T;
+        C.cls_mass = s->cls.mass;
+        C.cls_lam = s->cls.lam;
     }
     C.nplanes = (p.stage_mask & BP_STAGE_PLANES) ? s->nplanes : 0;
     for (int k = 0; k < s->nplanes; ++k) {
@@ -345,7 +347,8 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         ClassArrays &a = s->cls;
         if ((st = s->alloc(&a.cls, N)) || (st = s->alloc(&a.pos0, N)) || (st = s->alloc(&a.keys, N)) ||
             (st = s->alloc(&a.perm, N)) || (st = s->alloc(&a.inv, N)) || (st = s->alloc(&a.off, 8 * ncells + 1)) ||
-            (st = s->alloc(&a.pos, N)) || (st = s->alloc(&a.mixed, 1)) || (st = s->alloc(&a.moved, 1)))
+            (st = s->alloc(&a.pos, N)) || (st = s->alloc(&a.mixed, 1)) || (st = s->alloc(&a.moved, 1)) ||
+            (st = s->alloc(&a.mass, N)) || (st = s->alloc(&a.lam, N)))
             return bail(st);
         a.T = (int)ncells;
         s->cls_dmin = D;
@@ -710,7 +713,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     ra.cls = classes ? ca.cls : nullptr;
     ra.pos0 = classes ? ca.pos0 : nullptr;
     launch_reorder(st, C, ra, L);
-    if (classes) launch_class_order(st, s->n, s->sorted_keys, s->off, ca, s->sort, L);
+    if (classes) launch_class_order(st, s->n, s->sorted_keys, s->off, s->mass, ca, s->sort, L);
     // walks read candidates in class order: gather P before each walking launch
     auto refresh = [&](const float4 *P) {
         if (classes) launch_class_refresh(st, s->n, P, ca, L);

@@ -184,7 +184,7 @@ __device__ __forceinline__ int staged_index(const StageShared &S, int g, int k, 
 // in a table cell.  Each particle's own result does not depend on the thread.
 __device__ __forceinline__ int walker_index(const SimConsts &C, int t)
 {
-    return (C.cls_perm && __ldg(C.cls_moved) == 0) ? __ldg(C.cls_perm + t) : t;
+    return classes_on(C) ? __ldg(C.cls_perm + t) : t;
 }
 
 // Does particle i walk its CTA's staged runs (it is still in its stored cell)?
@@ -290,8 +290,9 @@ __device__ __forceinline__ void for_each_in_list(const int *base, int n, int i, 
 // Candidates [qb, e) of one (class, cell) run in class order, read from
 // C.cls_pos.  test() sees a stand-in index that equals i only for particle i
 // itself (tests compare it with i and nothing else); the body gets the sorted
-// index, and skips sorted indices below jlo.
-template <bool Split, class T, class B>
+// index, and skips sorted indices below jlo.  Slots: the body gets the class
+// position q instead (no sorted index is looked up; jlo must be 0).
+template <bool Split, bool Slots, class T, class B>
 __device__ __forceinline__ void walk_run_cls(int qb, int e, int qi, int i, int jlo, const SimConsts &C, T &test,
                                              B &body)
 {
@@ -302,8 +303,12 @@ __device__ __forceinline__ void walk_run_cls(int qb, int e, int qi, int i, int j
         for (int q = qb; q < e; ++q) {
             const float4 pj = src[q];
             if (test(q == qi ? i : -1 - q, pj)) {
-                const int j = __ldg(perm + q);
-                if (j >= jlo) body(j, pj);
+                if constexpr (Slots) {
+                    body(q, pj);
+                } else {
+                    const int j = __ldg(perm + q);
+                    if (j >= jlo) body(j, pj);
+                }
             }
         }
     } else {
@@ -319,8 +324,12 @@ __device__ __forceinline__ void walk_run_cls(int qb, int e, int qi, int i, int j
             while (bits) {
                 const int t = __ffs(bits) - 1;
                 bits &= bits - 1u;
-                const int j = __ldg(perm + q0 + t);
-                if (j >= jlo) body(j, s[t]);
+                if constexpr (Slots) {
+                    body(q0 + t, s[t]);
+                } else {
+                    const int j = __ldg(perm + q0 + t);
+                    if (j >= jlo) body(j, s[t]);
+                }
             }
         }
     }
@@ -332,7 +341,8 @@ __device__ __forceinline__ void walk_run_cls(int qb, int e, int qi, int i, int j
 // crosses a class boundary exactly where the table index wraps.  With lo > 0
 // (candidates j >= lo only), a piece of i's own class starts at i's class
 // position (class order keeps sorted order); other pieces filter in the body.
-template <bool Split, class T, class B>
+// Slots: the body gets class positions (walk_run_cls; lo must be 0).
+template <bool Split, bool Slots = false, class T, class B>
 __device__ __forceinline__ void walk_classes(int i, int3 c, int lo, const GridView &v, const SimConsts &C, T &test,
                                              B &body)
 {
@@ -360,7 +370,7 @@ __device__ __forceinline__ void walk_classes(int i, int3 c, int lo, const GridVi
             const int *o = off + (size_t)k * keys + base;
             const int b = __ldg(o + za), e = __ldg(o + zb + 1);
             const bool own = k == ki;
-            walk_run_cls<Split>(own ? max(b, qi) : b, e, qi, i, (lo > 0 && !own) ? lo : 0, C, test, body);
+            walk_run_cls<Split, Slots>(own ? max(b, qi) : b, e, qi, i, (lo > 0 && !own) ? lo : 0, C, test, body);
         }
     }
 }

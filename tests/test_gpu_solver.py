@@ -276,18 +276,20 @@ def test_lists_overflowing_their_capacity_are_bit_identical(bp, gpu, walk, skin)
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
-@pytest.mark.parametrize("walk", ["split", "no_split", "staging"])
+@pytest.mark.parametrize("walk", ["split", "no_split", "staging", "textbook"])
 def test_alias_classes_are_bit_identical(bp, gpu, walk):
     """An 8^3 table over a 3 x 4 x 3 m box: every table cell holds up to
     eight real cells.  Walks restricted to the walked real cell's alias class
-    give the bits of walks over whole table cells."""
+    give the bits of walks over whole table cells (with the threads in class
+    order and the position pass's lists in class positions)."""
     abi = bp.abi
     base = {"split": abi.BP_WALK_NO_STAGING, "no_split": abi.BP_WALK_NO_STAGING | abi.BP_WALK_NO_SPLIT,
-            "staging": 0}[walk]
+            "staging": 0, "textbook": abi.BP_WALK_NO_STAGING}[walk]
+    mode = abi.BP_MODE_TEXTBOOK if walk == "textbook" else abi.BP_MODE_REFERENCE
     scene = small_mixed_scene(bp, seed=15, fluid=(20, 8, 20), grid_dim=8)
     outs = []
     for w in (base, base | abi.BP_WALK_NO_ALIAS_CLASSES):
-        g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=w))
+        g = bp.ParticleSolver(scene, bp.make_params(scene, mode=mode, walk_options=w))
         walks = g.walk_stats(2, DT, 4)  # a real update
         if w & abi.BP_WALK_NO_ALIAS_CLASSES:
             assert walks["alias_classes"] == 0
