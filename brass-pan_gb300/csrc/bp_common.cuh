@@ -126,6 +126,13 @@ struct SimConsts {
     // masses (k_class_keys) and the lambdas k_lambda writes beside lam.
     const float *cls_mass;
     float *cls_lam;
+    // And for the post passes' slot lists (k_post_a), used where cls_post is
+    // set (a lambda pass of the substep wrote cls_rho): densities, committed
+    // velocities (gathered with the positions before pass A), pass A's
+    // vorticities and normals, pass B's velocities.
+    float *cls_rho;
+    float4 *cls_vel, *cls_om, *cls_nm, *cls_vb;
+    int cls_post;
 };
 
 // The walks use the alias classes for the rest of the substep (uniform

@@ -203,6 +203,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
         if (slots) C.cls_lam[t] = lam[i];
     }
     rho[i] = density;
+    if (slots) C.cls_rho[t] = density;
 }
 
 // Kernels with a split walk (test, then body over the hits) and a fused one.
@@ -321,6 +322,14 @@ void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, Laun
     L->done(__func__);
 }
 
+// The post passes keep class positions in their lists (SimConsts::cls_post):
+// pass A records them and every pass reads its neighbours' data from the
+// class-order copies, as k_lambda and k_deltap do.
+__device__ __forceinline__ bool post_slots(const SimConsts &C, bool stage)
+{
+    return !stage && C.cls_post && C.nbr && C.nbr_count && !C.vl && classes_on(C);
+}
+
 // Pass A: vorticity omega_i (fluidOmega) and Akinci normal n_i (fluidNormal)
 // in one walk over same-phase neighbours with 0 < r^2 <= h^2.
 // Om[i] = (omega, |omega|); Nm[i] = (h * n, rho_i).
@@ -343,14 +352,16 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
     const float3 vi = f3(V[i]);
     float3 om = make_float3(0.f, 0.f, 0.f), nn = make_float3(0.f, 0.f, 0.f);
     const bool want_om = C.use_vort, want_n = C.use_akinci;
-    auto term = [&](int j, float4 pj4) {
+    const bool slots = post_slots(C, Stage);
+    auto term_at = [&](const float4 *__restrict__ Vp, const float *__restrict__ rp, int j, float4 pj4) {
         const float3 diff = pi - f3(pj4);
         const float d2 = len2(diff);
         if (!(d2 > 0.f)) return;
         const float3 g = spiky_grad_r(C, diff, d2, rsqrtf(d2));
-        if (want_om) om += cross3(f3(V[j]) - vi, g);
-        if (want_n) nn = fma3(__frcp_rn(__ldg(rho + j)), g, nn);
+        if (want_om) om += cross3(f3(Vp[j]) - vi, g);
+        if (want_n) nn = fma3(__frcp_rn(__ldg(rp + j)), g, nn);
     };
+    auto term = [&](int j, float4 pj4) { term_at(V, rho, j, pj4); };
     const GridView v = grid_view(C, scene_index(C, i), off);
     auto test = [&](int, float4 pj4) { return len2(pi - f3(pj4)) <= C.h2; };
     // The walk takes the passes' common neighbours (r = 0 included, as pass C
@@ -361,21 +372,42 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
     int cnt = -1;
     if (C.nbr) {
         ListWriter list(C.nbr, C.nbr_cap, C.n, t);
-        walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4 pj4) {
-            if (j != i && phase_of(pj4) == phi) list.push(j);
-        });
+        if (slots) {  // the walk walk_neighbors takes here, recording class positions
+            if (C.nl_stats) {
+                atomicAdd(C.nl_stats + 1, 1u);
+                atomicAdd(C.nl_stats + 4, 1u);
+            }
+            auto push = [&](int q, float4 pj4) {
+                if (q != t && phase_of(pj4) == phi) list.push(q);
+            };
+            walk_classes<Split, true>(i, cell_of(pi, C), 0, v, C, test, push);
+        } else {
+            walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4 pj4) {
+                if (j != i && phase_of(pj4) == phi) list.push(j);
+            });
+        }
         cnt = list.finish();
         C.nbr_count[t] = cnt;
         // the records just written come back through the coherent path (plain loads)
-        if (cnt >= 0) for_each_in_list<false>(C.nbr, C.n, t, cnt, P, term);
+        if (cnt >= 0 && slots)
+            for_each_in_list<false>(C.nbr, C.n, t, cnt, C.cls_pos,
+                                    [&](int q, float4 pj4) { term_at(C.cls_vel, C.cls_rho, q, pj4); });
+        else if (cnt >= 0)
+            for_each_in_list<false>(C.nbr, C.n, t, cnt, P, term);
     }
     if (cnt < 0)
         walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4 pj4) {
             if (j != i && phase_of(pj4) == phi) term(j, pj4);
         });
-    Om[i] = make_float4(om.x, om.y, om.z, len3(om));
+    const float4 om4 = make_float4(om.x, om.y, om.z, len3(om));
     const float3 n = C.h * nn;
-    Nm[i] = make_float4(n.x, n.y, n.z, rho[i]);
+    const float4 nm4 = make_float4(n.x, n.y, n.z, rho[i]);
+    Om[i] = om4;
+    Nm[i] = nm4;
+    if (slots) {
+        C.cls_om[t] = om4;
+        C.cls_nm[t] = nm4;
+    }
 }
 
 // Passes B and C: the number of recorded neighbours of particle i (its list
@@ -423,14 +455,15 @@ __global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_b(S
     const float rhoi = ni4.w;
     float3 eta = make_float3(0.f, 0.f, 0.f), ft = make_float3(0.f, 0.f, 0.f);
     const bool want_v = C.use_vort, want_t = C.use_akinci;
-    auto body = [&](int j, float4 pj4) {
+    const bool slots = post_slots(C, Stage);
+    auto body_at = [&](const float4 *__restrict__ Omp, const float4 *__restrict__ Nmp, int j, float4 pj4) {
         const float3 diff = pi - f3(pj4);
         const float d2 = len2(diff);
         if (!(d2 > 0.f)) return;
         const float inv_r = rsqrtf(d2);
-        if (want_v) eta = fma3(Om[j].w, spiky_grad_r(C, diff, d2, inv_r), eta);
+        if (want_v) eta = fma3(Omp[j].w, spiky_grad_r(C, diff, d2, inv_r), eta);
         if (want_t) {
-            const float4 nj4 = Nm[j];
+            const float4 nj4 = Nmp[j];
             const float dist = __fmul_rn(d2, inv_r);
             const float3 fco = __fmul_rn(__fmul_rn(-C.tension, akinci_spline(C, dist)), inv_r) * diff;
             const float3 fcu = (-C.tension) * (ni - f3(nj4));
@@ -438,7 +471,11 @@ __global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_b(S
             ft = fma3(kij, fco + fcu, ft);
         }
     };
-    if (cnt != kWalkCells) {
+    auto body = [&](int j, float4 pj4) { body_at(Om, Nm, j, pj4); };
+    if (cnt != kWalkCells && slots) {
+        for_each_in_list(C.nbr, C.n, t, cnt, C.cls_pos,
+                         [&](int q, float4 pj4) { body_at(C.cls_om, C.cls_nm, q, pj4); });
+    } else if (cnt != kWalkCells) {
         for_each_in_list(C.nbr, C.n, t, cnt, P, body);
     } else {
         walk_neighbors<Split>(
@@ -453,7 +490,9 @@ __global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_b(S
         v += (C.vort_eps * cross3(nrm, f3(Om[i]))) * C.dt;
     }
     if (want_t) v = v + ft * C.dt;
-    Vout[i] = make_float4(v.x, v.y, v.z, vi4.w);
+    const float4 v4 = make_float4(v.x, v.y, v.z, vi4.w);
+    Vout[i] = v4;
+    if (slots) C.cls_vb[t] = v4;  // pass C's neighbour velocities
 }
 
 // Pass C: XSPH viscosity (fluidXSph): same phase, j != i, r^2 <= h^2 (r = 0
@@ -480,15 +519,20 @@ __global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_c(S
     }
     const float3 pi = f3(pi4), vi = f3(vi4);
     float3 vn = make_float3(0.f, 0.f, 0.f);
-    auto body = [&](int j, float4 pj4) {
+    auto body_at = [&](const float4 *__restrict__ Vp, const float *__restrict__ mp, const float *__restrict__ rp,
+                       int j, float4 pj4) {
         float wgt = poly6(C, len2(pi - f3(pj4)));
-        if (C.textbook) wgt = __fmul_rn(wgt, __fdiv_rn(__ldg(mass + j), __ldg(rho + j)));
-        vn = fma3(wgt, f3(V[j]) - vi, vn);
+        if (C.textbook) wgt = __fmul_rn(wgt, __fdiv_rn(__ldg(mp + j), __ldg(rp + j)));
+        vn = fma3(wgt, f3(Vp[j]) - vi, vn);
     };
+    auto body = [&](int j, float4 pj4) { body_at(V, mass, rho, j, pj4); };
     auto test = [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; };
     const GridView gv = grid_view(C, scene_index(C, i), off);
     int own = -1;
-    if (cnt != kWalkCells) {
+    if (cnt != kWalkCells && post_slots(C, Stage)) {  // V is pass B's output, kept in class order beside it
+        for_each_in_list(C.nbr, C.n, t, cnt, C.cls_pos,
+                         [&](int q, float4 pj4) { body_at(C.cls_vb, C.cls_mass, C.cls_rho, q, pj4); });
+    } else if (cnt != kWalkCells) {
         for_each_in_list(C.nbr, C.n, t, cnt, P, body);
     } else if (C.nbr && !C.nbr_count) {
         // no pass A before it: record the walk's pairs, then sum over them

@@ -482,7 +482,8 @@ void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const in
 // Walks use the classes while at least 1/32 of the particles sit in a cell
 // holding another class (below that the extra indirection costs more than
 // the skipped candidates save) and no particle has left the reach.
-__global__ void __launch_bounds__(256) k_class_refresh(int n, const float4 *__restrict__ P, ClassArrays a, Gate gate)
+__global__ void __launch_bounds__(256) k_class_refresh(int n, const float4 *__restrict__ P,
+                                                       const float4 *__restrict__ V, ClassArrays a, Gate gate)
 {
     if (gate_closed(gate)) {  // uniform: written by an earlier kernel
         if (blockIdx.x == 0 && threadIdx.x == 0) *a.moved = 1;
@@ -493,6 +494,7 @@ __global__ void __launch_bounds__(256) k_class_refresh(int n, const float4 *__re
         const int j = __ldg(a.perm + q);
         const float4 p = P[j];
         a.pos[q] = p;
+        if (V) a.vel[q] = V[j];
         const float4 p0 = __ldg(a.pos0 + j);
         const float dx = p.x - p0.x, dy = p.y - p0.y, dz = p.z - p0.z;
         // NaN counts as moved; so do positions far enough out that the hash's
@@ -503,7 +505,8 @@ __global__ void __launch_bounds__(256) k_class_refresh(int n, const float4 *__re
     if (far) *a.moved = 1;
 }
 
-void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L)
+void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L,
+                          const float4 *V)
 {
     if (n <= 0) return;
     // a grid-stride loop over one resident wave (8 CTAs of 256 per SM): the
@@ -512,7 +515,7 @@ void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassAr
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int blocks = std::min((n + 255) / 256, std::max(sms, 1) * 8);
-    k_class_refresh<<<blocks, 256, 0, st>>>(n, P, a, class_gate(n, a));
+    k_class_refresh<<<blocks, 256, 0, st>>>(n, P, V, a, class_gate(n, a));
     L->done(__func__);
 }
 

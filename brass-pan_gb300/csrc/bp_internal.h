@@ -109,6 +109,8 @@ struct ClassArrays {
     int *moved;      // one word
     float *mass;     // [n] masses in class order (k_class_keys)
     float *lam;      // [n] lambdas in class order (k_lambda, slot lists)
+    float *rho;      // [n] densities in class order (k_lambda, slot lists)
+    float4 *vel, *om, *nm, *vb;  // [n] each: the post passes' class-order copies (SimConsts::cls_vel ...)
     int T;           // cell keys of all scenes
     float reach2;    // squared reach (see SimConsts::cls_perm)
 };
@@ -117,7 +119,9 @@ struct ClassArrays {
 void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const int *off, const float *mass,
                         const ClassArrays &a, const SortScratch &s, LaunchLog *L);
 // Gathers P into class order and flags particles beyond the reach.
-void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L);
+// V != nullptr: also gathers V into a.vel (before the post passes).
+void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L,
+                          const float4 *V = nullptr);
 
 // ---- fluid kernels ----
 void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const float *mass, const int *off,

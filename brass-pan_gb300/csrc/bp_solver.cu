@@ -203,6 +203,11 @@ SimConsts bp::make_consts(const bp_solver *s, float sdt)
         C.cls_T = s->cls.T;
         C.cls_mass = s->cls.mass;
         C.cls_lam = s->cls.lam;
+        C.cls_rho = s->cls.rho;
+        C.cls_vel = s->cls.vel;
+        C.cls_om = s->cls.om;
+        C.cls_nm = s->cls.nm;
+        C.cls_vb = s->cls.vb;
     }
     C.nplanes = (p.stage_mask & BP_STAGE_PLANES) ? s->nplanes : 0;
     for (int k = 0; k < s->nplanes; ++k) {
@@ -348,7 +353,9 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         if ((st = s->alloc(&a.cls, N)) || (st = s->alloc(&a.pos0, N)) || (st = s->alloc(&a.keys, N)) ||
             (st = s->alloc(&a.perm, N)) || (st = s->alloc(&a.inv, N)) || (st = s->alloc(&a.off, 8 * ncells + 1)) ||
             (st = s->alloc(&a.pos, N)) || (st = s->alloc(&a.mixed, 1)) || (st = s->alloc(&a.moved, 1)) ||
-            (st = s->alloc(&a.mass, N)) || (st = s->alloc(&a.lam, N)))
+            (st = s->alloc(&a.mass, N)) || (st = s->alloc(&a.lam, N)) || (st = s->alloc(&a.rho, N)) ||
+            (st = s->alloc(&a.vel, N)) || (st = s->alloc(&a.om, N)) || (st = s->alloc(&a.nm, N)) ||
+            (st = s->alloc(&a.vb, N)))
             return bail(st);
         a.T = (int)ncells;
         s->cls_dmin = D;
@@ -844,7 +851,12 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     const bool post_ab = C.use_vort || C.use_akinci;
     if (tape && post_ab) tape->push(TS_POST_AB, s->Vc);
     if (tape && !post_ab && C.use_xsph) tape->push(TS_XSPH, s->Vc);
-    if (post_ab || C.use_xsph) refresh(cur);  // the post passes read the same positions
+    // The post passes keep class positions in their lists where lambda left
+    // its densities in class order (SimConsts::cls_post); the velocities are
+    // gathered into class order with the positions.
+    const bool post_slots = classes && lists && post_ab && fluid && iterations > 0 && !verlet;
+    if ((post_ab || C.use_xsph) && classes)  // the post passes read the same positions
+        launch_class_refresh(st, s->n, cur, ca, L, post_slots ? s->Vc : nullptr);
     if (post_ab) {
         // pass A records each fluid particle's neighbours for passes B and C
         SimConsts Cl = Cpost;
@@ -853,6 +865,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             Cl.nbr_count = s->nbr_count;
             Cl.nbr_cap = kPostListCap;
         }
+        Cl.cls_post = post_slots ? 1 : 0;
         launch_post_a(st, Cl, cur, s->Vc, s->rho, s->off, s->Om, s->Nm, L);
         launch_post_b(st, Cl, cur, s->Vc, s->Om, s->Nm, s->off, C.use_xsph ? s->Vs : s->Vc, L);
         if (C.use_xsph) launch_post_c(st, Cl, cur, s->Vs, s->off, s->mass, s->rho, s->Vc, L);
