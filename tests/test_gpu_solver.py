@@ -303,6 +303,25 @@ def test_alias_classes_are_bit_identical(bp, gpu, walk):
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
+def test_split_walks_match_one_thread_walks_on_aliased_grid(bp, gpu):
+    """Split walks (chunks of candidates tested before the pair terms)
+    against fused walks on the 8^3 table, where the walks take the alias
+    classes and the lists hold class positions: same bits."""
+    abi = bp.abi
+    scene = small_mixed_scene(bp, seed=17, fluid=(20, 8, 20), grid_dim=8)
+    outs = []
+    for w in (abi.BP_WALK_NO_STAGING, abi.BP_WALK_NO_STAGING | abi.BP_WALK_NO_SPLIT):
+        g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=w))
+        walks = g.walk_stats(2, DT, 4)  # a real update
+        assert walks["alias_classes"] > walks["cells_no_list"] // 2, walks
+        for _ in range(5):
+            g.update(2, DT, 4)
+        outs.append((g.positions(), g.velocities()))
+        g.close()
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
 def test_alias_classes_parity_on_aliased_grid(bp, gpu, oracle):
     scene = small_mixed_scene(bp, seed=16, fluid=(20, 8, 20), grid_dim=8)
     assert_parity(*lockstep(bp, oracle, scene, bp.make_params(scene), substeps=4))
