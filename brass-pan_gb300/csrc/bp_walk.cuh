@@ -42,6 +42,11 @@ constexpr int kWalkThreads = 256;
 #ifndef BP_SCAN_MIN_BLOCKS
 #define BP_SCAN_MIN_BLOCKS 4
 #endif
+// Candidate tests a split walk unrolls (loads in flight per thread).
+#ifndef BP_CHUNK_UNROLL
+#define BP_CHUNK_UNROLL 4
+#endif
+constexpr int kChunkUnroll = BP_CHUNK_UNROLL;
 constexpr int kStageCap = BP_STAGE_CAP;
 constexpr int kStageSegs = 2 * 9 * 2; // groups x columns x pieces
 
@@ -211,7 +216,7 @@ __device__ __forceinline__ void walk_run(int jb, int b, int e, const float4 *src
             const int cnt = min(32, e - j0);
             const float4 *s = src + (j0 - b);
             unsigned bits = 0u;
-#pragma unroll 4
+#pragma unroll kChunkUnroll
             for (int t = 0; t < cnt; ++t)
                 if (test(j0 + t, s[t])) bits |= 1u << t;
 #pragma unroll 1
@@ -317,7 +322,7 @@ __device__ __forceinline__ void walk_run_cls(int qb, int e, int qi, int i, int j
             const int cnt = min(32, e - q0);
             const float4 *s = src + q0;
             unsigned bits = 0u;
-#pragma unroll 4
+#pragma unroll kChunkUnroll
             for (int t = 0; t < cnt; ++t)
                 if (test(q0 + t == qi ? i : -1 - (q0 + t), s[t])) bits |= 1u << t;
 #pragma unroll 1
