@@ -283,6 +283,10 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
     C.vl = nullptr;
     C.nl_pos = nullptr;
     C.nl_stats = nullptr;
+    // nor the alias classes: their class-order positions are gathered only
+    // for the forward walks (the same candidates in the same order remain)
+    C.cls_perm = nullptr;
+    C.cls_post = 0;
     if (!(u.prm.walk_options & BP_WALK_NO_LISTS)) {
         C.nbr = s->nbr;
         C.nbr_count = nullptr;  // the lists live only inside one launch
