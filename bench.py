@@ -64,15 +64,15 @@ def load_peaks():
 
 def build_scene(bp, workload: str, seed: int = 0):
     if workload == "mixed":
-        return bp.scenes.config1_mixed(seed=seed)
+        return bp.scenes.mixed_phase_1m(seed=seed)
     if workload == "fluid":
         return bp.scenes.pbf_scene(128, 64, 128, spacing=0.1, seed=seed, box=(12.9, 16.0, 12.9))
     if workload == "small":
         return bp.scenes.pbf_scene(32, 32, 32, spacing=0.1, seed=seed, box=(4.0, 4.0, 4.0))
     if workload == "rigid":
-        return bp.scenes.config2_shape_stress(seed=seed)
+        return bp.scenes.rigid_body_pile(seed=seed)
     if workload == "batch":  # CPU-side sample of the ensemble: its largest member
-        return max(bp.scenes.config3_ensemble(seed=seed), key=lambda sc: sc.num_particles)
+        return max(bp.scenes.dam_break_ensemble(seed=seed), key=lambda sc: sc.num_particles)
     raise SystemExit(f"unknown workload {workload}")
 
 
@@ -154,7 +154,7 @@ def run_adjoint(bp, torch, stream, frames=120, every=10):
 def run_batch(bp, torch, stream, flush, steps, warmup, seed=0):
     """The batched ensemble (256 scenes in one solver) against looping one
     solver per scene over the same scenes on the same stream."""
-    scenes = bp.scenes.config3_ensemble(seed=seed)
+    scenes = bp.scenes.dam_break_ensemble(seed=seed)
     n = sum(s.num_particles for s in scenes)
     batch = bp.BatchSolver(scenes, stream=stream.cuda_stream)
     singles = [bp.ParticleSolver(s, stream=stream.cuda_stream) for s in scenes]
@@ -312,7 +312,7 @@ def run_ours(args):
         return p
 
     if args.workload == "batch":
-        scenes = bp.scenes.config3_ensemble(seed=rank)
+        scenes = bp.scenes.dam_break_ensemble(seed=rank)
         solver = bp.BatchSolver(scenes, [tuned(bp.make_params(s)) for s in scenes], stream=stream.cuda_stream)
         params = solver.params
         n = solver.n

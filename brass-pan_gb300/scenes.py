@@ -10,8 +10,8 @@ assign phases and ids (brasstower/particlesolver.cuh:395-710):
   (setDevArr_counterIncrement), rigid bodies one solid phase per body;
 * constraint ids are offset by the particle count before the object.
 
-The BASELINE benchmark scenes (`config0_dam_break`, `config1_mixed`) are
-built from the same factories with seeded jitter.
+The benchmark scenes (`dam_break_32k`, `mixed_phase_1m`, `dam_break_ensemble`,
+`rigid_body_pile`) are built from the same factories with seeded jitter.
 """
 from __future__ import annotations
 
@@ -238,12 +238,12 @@ def pbf_scene(nx, ny, nz, spacing=0.1, seed=0, box=None, jitter_frac=0.01, grid_
     return s
 
 
-def config0_dam_break(seed=0):
+def dam_break_32k(seed=0):
     """32^3 = 32,768 fluid particles, d = 0.1, jitter +-0.01d, box [0,4]^3."""
     return pbf_scene(32, 32, 32, 0.1, seed=seed, box=(4.0, 4.0, 4.0), jitter_frac=0.01)
 
 
-def config1_mixed(seed=0, fluid=(128, 64, 128), cloth=256, cubes=64, cube_dim=8, stiffness=(0.25, 0.1, 0.05)):
+def mixed_phase_1m(seed=0, fluid=(128, 64, 128), cloth=256, cubes=64, cube_dim=8, stiffness=(0.25, 0.1, 0.05)):
     """1,048,576 fluid particles (128x64x128 block, d = 0.1) in the corner of
     the box [0,25.8] x [0,16] x [0,25.8]; a 256x256 cloth at spacing d (the
     contact distance 2r, so the cloth does not fight its own contacts) 2 m
@@ -298,7 +298,7 @@ def ensemble_member(n_target, spacing=0.1, seed=0, rest_scale=1.0, gravity=9.8):
     return s
 
 
-def config3_ensemble(seed=0, num_scenes=256, lo=4096, hi=262144):
+def dam_break_ensemble(seed=0, num_scenes=256, lo=4096, hi=262144):
     """The batched ensemble: num_scenes dam breaks whose particle counts are
     drawn log-uniform in [lo, hi], rest density scaled uniform in [0.8, 1.2],
     gravity magnitude uniform in [5, 15], boxes scaled to the particle count."""
@@ -367,7 +367,7 @@ def rigid_shape(count, kind, spacing):
     return g - g.mean(axis=0, dtype=np.float64).astype(np.float32)
 
 
-def config2_shape_stress(seed=0, bodies=4096, lo=27, hi=1000, spacing=0.1, lattice=(32, 4, 32), pitch=2.5):
+def rigid_body_pile(seed=0, bodies=4096, lo=27, hi=1000, spacing=0.1, lattice=(32, 4, 32), pitch=2.5):
     """The shape-matching stress test: `bodies` rigid bodies whose particle
     counts are drawn uniform in [lo, hi] (cube, ball or rod lattices at
     `spacing`, chosen at random), each with a uniformly random orientation,

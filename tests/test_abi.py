@@ -169,7 +169,7 @@ def test_batch_entry_points_reject_null_handles(bp):
 
 
 def test_ensemble_members_follow_the_configuration(bp):
-    scenes = bp.scenes.config3_ensemble(seed=0, num_scenes=16)
+    scenes = bp.scenes.dam_break_ensemble(seed=0, num_scenes=16)
     n = np.array([s.num_particles for s in scenes])
     assert n.min() >= 0.8 * 4096 and n.max() <= 1.1 * 262144
     rho = np.array([s.rest_density for s in scenes]) / 1000.0
