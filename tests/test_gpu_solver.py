@@ -276,6 +276,34 @@ def test_lists_overflowing_their_capacity_are_bit_identical(bp, gpu, walk, skin)
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
+@pytest.mark.parametrize("mode", ["reference", "textbook"])
+def test_overflowing_class_position_lists_are_bit_identical(bp, gpu, mode):
+    """The overflow case on an 8^3 table, where the walks take the alias
+    classes and the lists hold class positions: particles past the list
+    capacity walk their cells with sorted indices, the rest read class
+    positions, and the bits equal walks everywhere."""
+    abi = bp.abi
+    m = abi.BP_MODE_TEXTBOOK if mode == "textbook" else abi.BP_MODE_REFERENCE
+    scene = fluid_scene(bp, (20, 8, 20), seed=37, grid_dim=8, box=(2.5, 3.0, 2.5))
+    x = scene.positions.copy()
+    c = x.mean(axis=0)
+    dense = np.all(np.abs(x - c) < 0.35, axis=1)
+    x[dense] = c + (x[dense] - c) * np.float32(0.5)
+    scene.positions = x.astype(np.float32)
+    assert dense.sum() > 200
+    outs = []
+    for w in (abi.BP_WALK_NO_STAGING, abi.BP_WALK_NO_STAGING | abi.BP_WALK_NO_LISTS):
+        g = bp.ParticleSolver(scene, bp.make_params(scene, mode=m, walk_options=w))
+        walks = g.walk_stats(1, DT / 2, 4)  # a real update
+        assert walks["alias_classes"] > 0, walks
+        for _ in range(3):
+            g.update(2, DT, 4)
+        outs.append((g.positions(), g.velocities()))
+        g.close()
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
 @pytest.mark.parametrize("walk", ["split", "no_split", "staging", "textbook"])
 def test_alias_classes_are_bit_identical(bp, gpu, walk):
     """An 8^3 table over a 3 x 4 x 3 m box: every table cell holds up to
