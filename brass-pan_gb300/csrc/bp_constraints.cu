@@ -181,9 +181,10 @@ void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int
 }
 
 // The solids among the candidates of particle i's 27 cells, in walk order:
-// body(j, P[j]) for every solid j with test(j, P[j]).
+// body(j, P[j]) for every solid j with test(-1, P[j]) (a fluid walker: no
+// candidate is itself).  spos[k] = P[list[k]] (k_gather_solids).
 template <class T, class B>
-__device__ __forceinline__ void walk_solids(float3 pi, const float4 *__restrict__ P, const GridView &v,
+__device__ __forceinline__ void walk_solids(float3 pi, const float4 *__restrict__ spos, const GridView &v,
                                             const SimConsts &C, const int *__restrict__ prefix,
                                             const int *__restrict__ list, T &&test, B &&body)
 {
@@ -203,9 +204,10 @@ __device__ __forceinline__ void walk_solids(float3 pi, const float4 *__restrict_
             const int kb = __ldg(prefix + b), ke = __ldg(prefix + e);
 #pragma unroll 1
             for (int k = kb; k < ke; ++k) {
-                const int j = __ldg(list + k);
-                const float4 pj = P[j];
-                if (test(j, pj)) body(j, pj);
+                // positions in list order (k_gather_solids); the sorted index
+                // only for a hit (the walker is fluid, so no candidate is itself)
+                const float4 pj = __ldg(spos + k);
+                if (test(-1, pj)) body(__ldg(list + k), pj);
             }
         }
     }
@@ -222,7 +224,7 @@ __device__ __forceinline__ void collide_one(const SimConsts &C, int i, const flo
                                             const float4 *__restrict__ Xs, const float *__restrict__ w,
                                             const GridView &v, const StageShared *S, int g,
                                             const int *__restrict__ solid_prefix, const int *__restrict__ solid_list,
-                                            float4 *__restrict__ Pout)
+                                            const float4 *__restrict__ solid_pos, float4 *__restrict__ Pout)
 {
     const float4 pi4 = P[i];
     const float3 xip = f3(pi4);
@@ -265,7 +267,7 @@ __device__ __forceinline__ void collide_one(const SimConsts &C, int i, const flo
                     sf -= (w1 * tdx) * fminf(__fmul_rn(C.fd, __fsqrt_rn(__fdiv_rn(dxi2, tl2))), 1.0f);
             }
     };
-    if (phi < 0 && solid_prefix) walk_solids(xip, P, v, C, solid_prefix, solid_list, test, body);
+    if (phi < 0 && solid_prefix) walk_solids(xip, solid_pos, v, C, solid_prefix, solid_list, test, body);
     else walk_neighbors<Split>(i, xip, 0, P, v, C, S, g, test, body);
     const float3 d = (count == 0) ? sd : sd + sf / (float)count;
     const float3 p = xip + d;
@@ -284,8 +286,8 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS)
     k_particle_collision(SimConsts C, const float4 *__restrict__ P, const float4 *__restrict__ Xs,
                          const float *__restrict__ w, const int *__restrict__ off, const int *__restrict__ tile_solid,
                          const int *__restrict__ solid_prefix, const int *__restrict__ solid_list,
-                         const unsigned long long *__restrict__ solid_near, int solids_apart,
-                         float4 *__restrict__ Pout)
+                         const float4 *__restrict__ solid_pos, const unsigned long long *__restrict__ solid_near,
+                         int solids_apart, float4 *__restrict__ Pout)
 {
     StageShared &S = stage_shared();
     const int i0 = blockIdx.x * kWalkThreads;
@@ -309,7 +311,16 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS)
         track_displacement(C, i, p, true);
         return;
     }
-    collide_one<Split>(C, i, P, Xs, w, v, &S, g, solid_prefix, solid_list, Pout);
+    collide_one<Split>(C, i, P, Xs, w, v, &S, g, solid_prefix, solid_list, solid_pos, Pout);
+}
+
+// The positions of the compacted solids, in list order, for the fluid
+// walkers' reads (sequential within a run instead of a gather per candidate).
+__global__ void __launch_bounds__(256) k_gather_solids(int nsolid, const int *__restrict__ list,
+                                                       const float4 *__restrict__ P, float4 *__restrict__ spos)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nsolid) spos[k] = P[__ldg(list + k)];
 }
 
 // The solid particles, one thread each through the compacted list, so the
@@ -324,25 +335,30 @@ __global__ void __launch_bounds__(kWalkThreads)
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nsolid) return;
     const int i = __ldg(solid_list + t);
-    collide_one<Split>(C, i, P, Xs, w, grid_view(C, scene_index(C, i), off), nullptr, -1, nullptr, nullptr, Pout);
+    collide_one<Split>(C, i, P, Xs, w, grid_view(C, scene_index(C, i), off), nullptr, -1, nullptr, nullptr, nullptr,
+                       Pout);
 }
 
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
                                const float *w, const int *off, const int *tile_solid, const int *solid_prefix,
                                const int *solid_list, int nsolid, bool solids_apart,
-                               const unsigned long long *solid_near, float4 *Pout, LaunchLog *L)
+                               const unsigned long long *solid_near, float4 *solid_pos, float4 *Pout, LaunchLog *L)
 {
     if (C.n <= 0) return;
     const int grid = (C.n + kWalkThreads - 1) / kWalkThreads;
     const int apart = (solids_apart && solid_list && nsolid > 0) ? 1 : 0;
     // the cell mask describes the walks over the compacted solids only
     const unsigned long long *near = (apart && solid_prefix) ? solid_near : nullptr;
+    if (solid_prefix && solid_list && nsolid > 0) {
+        k_gather_solids<<<(nsolid + 255) / 256, 256, 0, st>>>(nsolid, solid_list, P, solid_pos);
+        L->done("k_gather_solids");
+    }
     if (C.split)
         k_particle_collision<true><<<grid, kWalkThreads, stage_bytes(C), st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
-                                                                 solid_list, near, apart, Pout);
+                                                                 solid_list, solid_pos, near, apart, Pout);
     else
         k_particle_collision<false><<<grid, kWalkThreads, stage_bytes(C), st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
-                                                                  solid_list, near, apart, Pout);
+                                                                  solid_list, solid_pos, near, apart, Pout);
     L->done(__func__);
     if (apart) {
         const int sg = (nsolid + kWalkThreads - 1) / kWalkThreads;

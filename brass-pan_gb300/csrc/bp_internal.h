@@ -156,10 +156,11 @@ void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // solid_prefix / solid_list: nullptr, or the compacted solids (launch_solid_list)
 // solids_apart: the nsolid solids of the list walk in a second launch over the list.
 // solid_near: nullptr, or SolidCells::near of the same sorted order.
+// solid_pos: nsolid float4 of scratch (the listed solids' positions, gathered first).
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
                                const float *w, const int *off, const int *tile_solid, const int *solid_prefix,
                                const int *solid_list, int nsolid, bool solids_apart,
-                               const unsigned long long *solid_near, float4 *Pout, LaunchLog *L);
+                               const unsigned long long *solid_near, float4 *solid_pos, float4 *Pout, LaunchLog *L);
 // Bit masks over the D^3 table cells of one scene (cells == nullptr: not built):
 // cells marks the stored cells (keys) of the solids, near the cells whose 27
 // cells hold one.

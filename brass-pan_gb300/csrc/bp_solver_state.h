@@ -120,6 +120,7 @@ struct bp_solver {
     int *tile_solid = nullptr;  // per 256 sorted particles: the tile holds a solid
     int *solid_prefix = nullptr, *solid_list = nullptr, *solid_totals = nullptr;  // compacted solids
     unsigned long long *solid_cells = nullptr, *solid_near = nullptr;  // SolidCells masks (one scene with fluid)
+    float4 *solid_pos = nullptr;  // positions of the compacted solids (launch_particle_collision)
     int *nbr = nullptr, *nbr_count = nullptr;  // post-pass neighbour lists [kPostListCap][N], counts
     SortScratch sort{};
     // alias classes (SimConsts::cls_perm); cls.perm == nullptr: not allocated
