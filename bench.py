@@ -6,7 +6,9 @@ particles, a 256x256 cloth under wind, 64 rigid 8^3 cubes; 1,146,880
 particles), reference-mode parameters.  By default the timed region is the
 configuration's 200 frames after 3 warm-up frames: throughput falls as the
 dam break spreads into cells the 64^3 table aliases and the fluid
-compresses, so short runs overstate it.  Prints one JSON line; unless
+compresses, so short runs overstate it.  Its "e2e" object replays the
+same frames through the C ABI, each frame's state uploaded from pinned host
+memory and its positions and velocities read back.  Prints one JSON line; unless
 --no-batch, its "batched" object times the batched ensemble (256 PBF dam
 breaks of 4096..262144 particles in one solver) against looping one solver
 per scene over the same scenes; unless --no-adjoint, its "adjoint" object
