@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
             list.push(j);
         };
         auto test = [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; };
-        if (slots) {  // the walk walk_neighbors takes here (no staging, no Verlet list)
+        if (slots) {  // the class walk walk_neighbors would take (no staging, no Verlet list), counted alike
             if (C.nl_stats) {
                 atomicAdd(C.nl_stats + 1, 1u);
                 atomicAdd(C.nl_stats + 4, 1u);
@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
     int cnt = -1;
     if (C.nbr) {
         ListWriter list(C.nbr, C.nbr_cap, C.n, t);
-        if (slots) {  // the walk walk_neighbors takes here, recording class positions
+        if (slots) {  // the class walk walk_neighbors would take, recording class positions
             if (C.nl_stats) {
                 atomicAdd(C.nl_stats + 1, 1u);
                 atomicAdd(C.nl_stats + 4, 1u);
