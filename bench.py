@@ -64,17 +64,18 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def build_scene(bp, workload: str, seed: int = 0):
+def build_scene(scenes, workload: str, seed: int = 0):
+    """The workload's scene from the builders module `scenes`."""
     if workload == "mixed":
-        return bp.scenes.mixed_phase_1m(seed=seed)
+        return scenes.mixed_phase_1m(seed=seed)
     if workload == "fluid":
-        return bp.scenes.pbf_scene(128, 64, 128, spacing=0.1, seed=seed, box=(12.9, 16.0, 12.9))
+        return scenes.pbf_scene(128, 64, 128, spacing=0.1, seed=seed, box=(12.9, 16.0, 12.9))
     if workload == "small":
-        return bp.scenes.pbf_scene(32, 32, 32, spacing=0.1, seed=seed, box=(4.0, 4.0, 4.0))
+        return scenes.pbf_scene(32, 32, 32, spacing=0.1, seed=seed, box=(4.0, 4.0, 4.0))
     if workload == "rigid":
-        return bp.scenes.rigid_body_pile(seed=seed)
+        return scenes.rigid_body_pile(seed=seed)
     if workload == "batch":  # CPU-side sample of the ensemble: its largest member
-        return max(bp.scenes.dam_break_ensemble(seed=seed), key=lambda sc: sc.num_particles)
+        return max(scenes.dam_break_ensemble(seed=seed), key=lambda sc: sc.num_particles)
     raise SystemExit(f"unknown workload {workload}")
 
 
@@ -151,6 +152,40 @@ def run_adjoint(bp, torch, stream, frames=120, every=10):
                      "forward_ms": fwd * 1e3, "forward_adjoint_ms": both * 1e3, "ratio": both / fwd,
                      "grad_finite": bool(np.isfinite(g["velocities"]).all())}
     return out
+
+
+def run_reference_cuda(torch, scene, params, steps, warmup, flush, state=None):
+    """The reference's own step on this GPU: its kernel headers compiled by
+    nvcc for sm_103a and launched by the replay driver (oracle/ref_cuda.cu) on
+    the legacy default stream, same scene, parameters, update shape, warm-up
+    and L2 flush as the GPU arm; CUDA events around each update.  `state`
+    (positions, velocities in original order) replaces the scene's initial
+    state.  None when the reference's sources were not available to build it."""
+    import oracle
+
+    if oracle.ref_cuda_lib() is None:
+        return None
+    ref = oracle.RefCudaSolver(scene, params)
+    try:
+        if state is not None:
+            ref.set_state(*state)
+        t0 = time.perf_counter()
+        for _ in range(warmup):
+            ref.update(SUBSTEPS, DT, ITERATIONS)
+        ref.get(oracle.F_X)  # synchronises
+        per = (time.perf_counter() - t0) / max(warmup, 1)
+        k = max(1, min(steps, int(60.0 / max(per, 1e-6))))  # at most about a minute
+        ms = ref.time_updates(k, SUBSTEPS, DT, ITERATIONS, flush.data_ptr(), flush.numel())
+        x = ref.get(oracle.F_X)
+        finite = bool(np.isfinite(x).all())
+    finally:
+        ref.close()
+    n = scene.num_particles
+    return {"value": n * SUBSTEPS * k / (ms / 1e3), "unit": "particle-substeps/s", "ms_per_step": ms / k,
+            "steps": k, "warmup": warmup, "state_finite": finite,
+            "kind": "the reference's kernel headers (kernel/*.cuh) built unmodified for sm_103a, 128-thread "
+                    "launches on the legacy default stream, toolkit CUB radix sort, stage order of "
+                    "ParticleSolver::update with the constraint and wind blocks enabled"}
 
 
 def run_batch(bp, torch, stream, flush, steps, warmup, seed=0):
@@ -287,6 +322,17 @@ def issue_for(kernel: str, workload: str):
             "active_lanes_of_32": float(lanes.group(1)), "source": "profiles/" + fname}
 
 
+def workload_config(args, n, params, world):
+    """The config object both arms print (same keys, same values)."""
+    return {"workload": workload_name(args.workload, n), "particles": n, "substeps": SUBSTEPS,
+            "iterations": ITERATIONS, "dt": DT, "mode": "reference",
+            "grid": ("one grid per scene (16^3..64^3 cells), cell = h = 0.2" if args.workload == "batch"
+                     else f"{params.grid_dim}^3 cells, cell = h = 0.2"),
+            "neighbor_skin": float(params.neighbor_skin), "mass_scaling_k": float(params.mass_scaling_k),
+            "stage_mask": int(params.stage_mask),
+            "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"}
+
+
 def run_ours(args):
     import torch
 
@@ -319,7 +365,7 @@ def run_ours(args):
         params = solver.params
         n = solver.n
     else:
-        scene = build_scene(bp, args.workload, seed=rank)
+        scene = build_scene(bp.scenes, args.workload, seed=rank)
         if args.load_state:  # continue a saved run (positions, velocities in original order)
             z = np.load(args.load_state)
             scene.positions, scene.velocities = z["x"].astype(np.float32), z["v"].astype(np.float32)
@@ -407,6 +453,13 @@ def run_ours(args):
     walks = solver.walk_stats(SUBSTEPS, DT, ITERATIONS)
     device_errors = solver.device_errors()  # non-finite state anywhere in the run
     solver.close()
+    reference_cuda = None
+    if rank == 0 and args.workload != "batch" and not args.no_reference_cuda:
+        ref_scene = build_scene(bp.scenes, args.workload, seed=0)
+        reference_cuda = run_reference_cuda(torch, ref_scene, workload_params(bp, args.workload, ref_scene),
+                                            args.steps, args.warmup, flush)
+        if reference_cuda is not None:
+            reference_cuda["ours_over_reference"] = value / reference_cuda["value"]
     batched = None
     if args.workload == "batch" or (args.workload == "mixed" and not args.no_batch):
         # the ensemble against a loop of one solver per scene (bounded: 3 timed steps)
@@ -417,7 +470,7 @@ def run_ours(args):
 
     result = None
     if rank == 0:
-        cpu = None if args.no_cpu_baseline else cpu_baseline(bp, args.workload, steps=1)
+        cpu = None if args.no_cpu_baseline else cpu_baseline(args.workload)
         clk = clocks.summary()
         result = {
             "metric": "particle-substeps/s",
@@ -432,13 +485,8 @@ def run_ours(args):
             "vs_baseline": None,
             "dtype": "f32",
             "data": "synthetic (seeded lattice scenes, no dataset)",
-            "config": {"workload": workload_name(args.workload, n), "particles": n, "substeps": SUBSTEPS,
-                       "iterations": ITERATIONS, "dt": DT, "mode": "reference",
-                       "grid": ("one grid per scene (16^3..64^3 cells), cell = h = 0.2" if args.workload == "batch"
-                                else f"{params.grid_dim}^3 cells, cell = h = 0.2"),
-                       "neighbor_skin": float(params.neighbor_skin), "walk_options": int(solver.params.walk_options),
-                       "autotune": tuned_walk,
-                       "l2": "flushed (256 MB write) before every timed step", "parallelism": f"replicas x{world}"},
+            "config": dict(workload_config(args, n, params, world), walk_options=int(solver.params.walk_options),
+                           autotune=tuned_walk),
             "e2e": {"value": e2e_value, "unit": "particle-substeps/s",
                     "h2d_bytes_per_step": int(2 * n * 12), "d2h_bytes_per_step": int(2 * n * 12)},
             "gpu_launches": int(launches_per_step * args.steps),
@@ -455,6 +503,8 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "clocks": clk,
         }
+        if reference_cuda is not None:
+            result["reference_cuda"] = reference_cuda
         if batched is not None:
             result["batched"] = batched
         if adjoint is not None:
@@ -465,75 +515,94 @@ def run_ours(args):
     return result
 
 
-def workload_params(bp, workload, scene):
-    """Parameters of a workload: the reference's literals, plus the stage set
-    of the shape-matching stress test (planes, contacts, shape matching).
-    The mixed scene runs without mass scaling: exp(2 y) at the cloth's and
-    cubes' heights (8 to 12 m) makes the contacts diverge within 120 frames."""
-    params = bp.make_params(scene)
+def workload_overrides(abi, workload):
+    """Parameter overrides of a workload on top of the reference's literals:
+    the stage set of the shape-matching stress test (planes, contacts, shape
+    matching).  The mixed scene runs without mass scaling: exp(2 y) at the
+    cloth's and cubes' heights (8 to 12 m) makes the contacts diverge within
+    120 frames."""
     if workload == "mixed":
-        params.mass_scaling_k = 0.0
+        return {"mass_scaling_k": 0.0}
     if workload == "rigid":
-        params.stage_mask = (bp.abi.BP_STAGE_PLANES | bp.abi.BP_STAGE_PARTICLE_COLLISION |
-                             bp.abi.BP_STAGE_SHAPE_MATCHING)
-    return params
+        return {"stage_mask": abi.BP_STAGE_PLANES | abi.BP_STAGE_PARTICLE_COLLISION | abi.BP_STAGE_SHAPE_MATCHING}
+    return {}
 
 
-def cpu_baseline(bp, workload, steps=1):
-    """The oracle port (the reference's step restated in C, OpenMP over all
-    host cores) on a bounded sample: `steps` substeps of the same scene."""
+def workload_params(bp, workload, scene):
+    """bp_params of a workload through the product library."""
+    return bp.make_params(scene, **workload_overrides(bp.abi, workload))
+
+
+def reference_cpu_solver(oracle, scene, params, threads):
+    """The reference's step on the host: its own kernels compiled for the host
+    (oracle/_ref/libbrassref.so, kind "reference") where they were built,
+    else the C restatement (kind "port")."""
+    if oracle.ref_lib() is not None:
+        return oracle.RefSolver(scene, params, threads=threads), "reference"
+    return oracle.OracleSolver(scene, params, threads=threads), "port"
+
+
+def cpu_baseline(workload, warm_substeps=1, substeps=2):
+    """The reference's step on all host cores, on a bounded sample: one frame
+    (`substeps` substeps) of the same scene after `warm_substeps` warm-up
+    substeps, timed on the wall clock."""
     import oracle
 
     threads = os.cpu_count() or 1
-    scene = build_scene(bp, workload, seed=0)
-    params = workload_params(bp, workload, scene)
-    kind = "port"
-    o = oracle.OracleSolver(scene, params, threads=threads)
-    o.update(1, DT / SUBSTEPS, ITERATIONS)  # warm-up substep (first-touch of the grid tables)
+    scenes = oracle.scenes_module()
+    scene = build_scene(scenes, workload, seed=0)
+    params = oracle.reference_params(scene, **workload_overrides(oracle._abi(), workload))
+    solver, kind = reference_cpu_solver(oracle, scene, params, threads)
+    for _ in range(warm_substeps):  # first touch of the grid tables
+        solver.update(1, DT / SUBSTEPS, ITERATIONS)
     t0 = time.perf_counter()
-    for _ in range(steps):
-        o.update(1, DT / SUBSTEPS, ITERATIONS)
+    for _ in range(substeps):
+        solver.update(1, DT / SUBSTEPS, ITERATIONS)
     dt = time.perf_counter() - t0
-    return {"value": scene.num_particles * steps / dt, "unit": "particle-substeps/s", "cores": threads,
-            "kind": kind, "sample": f"{steps} substep(s) of the same scene ({scene.num_particles} particles) "
-                                    f"after 1 warm-up substep, {threads} OpenMP threads"}
+    what = ("the reference's kernels compiled for the host (OpenMP over the launch index)" if kind == "reference"
+            else "the C restatement of the reference's step")
+    return {"value": scene.num_particles * substeps / dt, "unit": "particle-substeps/s", "cores": threads,
+            "kind": kind, "sample": f"{substeps} substeps of the same scene ({scene.num_particles} particles) after "
+                                    f"{warm_substeps} warm-up substep: {what}, {threads} OpenMP threads"}
 
 
 def run_reference(args):
-    """Reference arm: the reference's step on the host cores (the oracle port,
-    or the reference's own kernels where they were compiled here), rank 0 only."""
+    """Reference arm: the reference's step on the host cores, rank 0 only.
+    It loads no product code: the scene comes from the pure-Python builders,
+    the parameters from the reference's literals (oracle.reference_params), and
+    the step from the reference's own kernels compiled for the host, else the
+    C restatement.  Same workload, frames and warm-up as the GPU arm: W
+    untimed updates, then K timed updates of 2 substeps (capped in time)."""
     rank, world, _ = dist_info()
     if rank != 0:
         return None
-    import __graft_entry__ as entry
-
-    entry.load_package()
-    bp = sys.modules["brasspan_gb300"]
-    if not bp.abi.LIB_PATH.exists():
-        entry.build()
     import oracle
 
+    oracle.build_oracle()
+    oracle.build_ref()  # no-op without the reference's sources
     threads = os.cpu_count() or 1
-    scene = build_scene(bp, args.workload, seed=0)
-    params = workload_params(bp, args.workload, scene)
-    solver = oracle.OracleSolver(scene, params, threads=threads)
-    kind = "port"
+    scenes = oracle.scenes_module()
+    scene = build_scene(scenes, args.workload, seed=0)
+    params = oracle.reference_params(scene, **workload_overrides(oracle._abi(), args.workload))
+    solver, kind = reference_cpu_solver(oracle, scene, params, threads)
     n = scene.num_particles
-    # each step is a bounded sample of the workload: one substep
-    for _ in range(min(args.warmup, 1)):
-        solver.update(1, DT / SUBSTEPS, ITERATIONS)
-    budget_s = 150.0
+    for _ in range(args.warmup):
+        solver.update(SUBSTEPS, DT, ITERATIONS)
+    budget_s = 240.0
     t0 = time.perf_counter()
     done = 0
     for _ in range(args.steps):
-        solver.update(1, DT / SUBSTEPS, ITERATIONS)
+        solver.update(SUBSTEPS, DT, ITERATIONS)
         done += 1
         if time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
-    value = n * done / dt
-    sample = (f"{done} timed substep(s) (one per step, capped at {budget_s:.0f} s) of the same scene "
-              f"({n} particles) after {min(args.warmup, 1)} warm-up substep, {threads} OpenMP threads")
+    value = n * SUBSTEPS * done / dt
+    what = ("the reference's kernels compiled for the host (OpenMP over the launch index)" if kind == "reference"
+            else "the C restatement of the reference's step")
+    sample = (f"{done} timed updates of {SUBSTEPS} substeps (frames {args.warmup + 1}..{args.warmup + done}; "
+              f"capped at {budget_s:.0f} s) of the same scene ({n} particles) after {args.warmup} warm-up updates: "
+              f"{what}, {threads} OpenMP threads")
     result = {
         "impl": "reference",
         "metric": "particle-substeps/s",
@@ -541,15 +610,14 @@ def run_reference(args):
         "unit": "particle-substeps/s",
         "n_gpus": world,
         "steps": done,
-        "warmup": min(args.warmup, 1),
+        "warmup": args.warmup,
         "ms_per_step": dt * 1e3 / max(done, 1),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded lattice scenes, no dataset)",
-        "config": {"workload": workload_name(args.workload, n), "particles": n, "substeps": SUBSTEPS,
-                   "iterations": ITERATIONS, "dt": DT, "mode": "reference"},
+        "config": workload_config(args, n, params, world),
         "cpu_baseline": {"value": value, "unit": "particle-substeps/s", "cores": threads, "kind": kind,
                          "sample": sample},
         "e2e": {"value": value, "unit": "particle-substeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -567,6 +635,7 @@ def main():
     ap.add_argument("--workload", choices=["mixed", "fluid", "small", "batch", "rigid"], default="mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--no-reference-cuda", action="store_true", help="skip timing the reference's CUDA step")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint measurement")
     ap.add_argument("--save-state", default=None, help="after the timed steps, save the state (npz) here")
     ap.add_argument("--load-state", default=None, help="start from a state saved by --save-state")

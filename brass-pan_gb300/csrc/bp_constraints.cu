@@ -316,11 +316,17 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS)
 
 // The positions of the compacted solids, in list order, for the fluid
 // walkers' reads (sequential within a run instead of a gather per candidate).
-__global__ void __launch_bounds__(256) k_gather_solids(int nsolid, const int *__restrict__ list,
-                                                       const float4 *__restrict__ P, float4 *__restrict__ spos)
+// The count is the device-side total of this substep's compaction
+// (prefix[n]): phases can change after creation (a snapshot, a write through
+// BP_FIELD_NEW_POSITIONS), so the launch's size, taken from the count at
+// creation, is covered by a grid-stride loop.
+__global__ void __launch_bounds__(256) k_gather_solids(int n, const int *__restrict__ prefix,
+                                                       const int *__restrict__ list, const float4 *__restrict__ P,
+                                                       float4 *__restrict__ spos)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < nsolid) spos[k] = P[__ldg(list + k)];
+    const int total = __ldg(prefix + n);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x)
+        spos[k] = P[__ldg(list + k)];
 }
 
 // The solid particles, one thread each through the compacted list, so the
@@ -329,14 +335,17 @@ template <bool Split>
 __global__ void __launch_bounds__(kWalkThreads)
     k_particle_collision_solids(SimConsts C, int nsolid, const float4 *__restrict__ P,
                                 const float4 *__restrict__ Xs, const float *__restrict__ w,
-                                const int *__restrict__ off, const int *__restrict__ solid_list,
-                                float4 *__restrict__ Pout)
+                                const int *__restrict__ off, const int *__restrict__ solid_prefix,
+                                const int *__restrict__ solid_list, float4 *__restrict__ Pout)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nsolid) return;
-    const int i = __ldg(solid_list + t);
-    collide_one<Split>(C, i, P, Xs, w, grid_view(C, scene_index(C, i), off), nullptr, -1, nullptr, nullptr, nullptr,
-                       Pout);
+    // the device-side count of this substep (see k_gather_solids); nsolid,
+    // the count at creation, only sized the launch
+    const int total = __ldg(solid_prefix + C.n);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const int i = __ldg(solid_list + t);
+        collide_one<Split>(C, i, P, Xs, w, grid_view(C, scene_index(C, i), off), nullptr, -1, nullptr, nullptr,
+                           nullptr, Pout);
+    }
 }
 
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
@@ -346,11 +355,11 @@ void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4
 {
     if (C.n <= 0) return;
     const int grid = (C.n + kWalkThreads - 1) / kWalkThreads;
-    const int apart = (solids_apart && solid_list && nsolid > 0) ? 1 : 0;
+    const int apart = (solids_apart && solid_prefix && solid_list && nsolid > 0) ? 1 : 0;
     // the cell mask describes the walks over the compacted solids only
     const unsigned long long *near = (apart && solid_prefix) ? solid_near : nullptr;
-    if (solid_prefix && solid_list && nsolid > 0) {
-        k_gather_solids<<<(nsolid + 255) / 256, 256, 0, st>>>(nsolid, solid_list, P, solid_pos);
+    if (solid_prefix && solid_list) {
+        k_gather_solids<<<(max(nsolid, 1) + 255) / 256, 256, 0, st>>>(C.n, solid_prefix, solid_list, P, solid_pos);
         L->done("k_gather_solids");
     }
     if (C.split)
@@ -363,10 +372,11 @@ void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4
     if (apart) {
         const int sg = (nsolid + kWalkThreads - 1) / kWalkThreads;
         if (C.split)
-            k_particle_collision_solids<true><<<sg, kWalkThreads, 0, st>>>(C, nsolid, P, Xs, w, off, solid_list, Pout);
+            k_particle_collision_solids<true><<<sg, kWalkThreads, 0, st>>>(C, nsolid, P, Xs, w, off, solid_prefix,
+                                                                          solid_list, Pout);
         else
-            k_particle_collision_solids<false><<<sg, kWalkThreads, 0, st>>>(C, nsolid, P, Xs, w, off, solid_list,
-                                                                           Pout);
+            k_particle_collision_solids<false><<<sg, kWalkThreads, 0, st>>>(C, nsolid, P, Xs, w, off, solid_prefix,
+                                                                           solid_list, Pout);
         L->done("launch_particle_collision_solids");
     }
 }

@@ -34,7 +34,9 @@ void *g_scratch_ptr[kMaxDevices] = {};
 
 // Device address of g_grid_scratch on the current device.  The host-side
 // symbol is only a stand-in; the address must be queried once per device,
-// with that device current.
+// with that device current.  It is kept until the process exits, so it goes
+// stale if the caller resets the device (cudaDeviceReset) after the first
+// call; the entry point's documentation rules that out.
 cudaError_t scratch_address(void **out)
 {
     int dev = 0;

@@ -156,7 +156,9 @@ void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // solid_prefix / solid_list: nullptr, or the compacted solids (launch_solid_list)
 // solids_apart: the nsolid solids of the list walk in a second launch over the list.
 // solid_near: nullptr, or SolidCells::near of the same sorted order.
-// solid_pos: nsolid float4 of scratch (the listed solids' positions, gathered first).
+// solid_pos: C.n + 1 float4 of scratch (the listed solids' positions, gathered
+// first); the kernels take the solid count from solid_prefix[C.n] (this
+// substep's compaction), nsolid (the count at creation) only sizes launches.
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
                                const float *w, const int *off, const int *tile_solid, const int *solid_prefix,
                                const int *solid_list, int nsolid, bool solids_apart,

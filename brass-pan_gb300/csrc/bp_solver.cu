@@ -384,7 +384,7 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
     s->num_solids = 0;
     for (int i = 0; i < n; ++i) s->num_solids += sc->phases[i] > 0;
     if ((st = s->alloc(&s->tile_solid, (N + 255) / 256)) || (st = s->alloc(&s->solid_prefix, N + 1)) ||
-        (st = s->alloc(&s->solid_pos, (size_t)s->num_solids + 1)) ||
+        (st = s->alloc(&s->solid_pos, N + 1)) ||  // phases may change after creation: room for every particle
         (st = s->alloc(&s->solid_list, N)) || (st = s->alloc(&s->solid_totals, (N + 1023) / 1024)) ||
         (st = s->alloc(&s->nbr, N * kPostListCap)) ||
         (st = s->alloc(&s->nbr_count, N)))

@@ -369,6 +369,10 @@ bp_status bp_grid_reset(void *stream, int32_t num_particles, const int32_t *d_so
  *
  * The first call on a device, with that device current, looks up the array's
  * address on that device; make that first call before any stream capture.
+ * The address is kept for the rest of the process: after cudaDeviceReset (or
+ * any other teardown of the device's primary context) it no longer points at
+ * the array, so do not call this entry point in a process that has reset the
+ * device since its first call there.
  * All calls on a device share the one array: calls whose work overlaps on the
  * GPU (on different streams, or from different threads without ordering)
  * race and give wrong results.  Order them on one stream. */

@@ -2,8 +2,15 @@
 
 * `OracleSolver`: the C restatement in oracle.c (liboracle.so), any mode.
 * `RefSolver`: the reference's own kernels compiled for the host through
-  oracle/refshim (oracle/_ref/libbrassref.so); only where the reference
-  checkout was present at build time, reference parameters only.
+  oracle/refshim (oracle/_ref/libbrassref.so); reference parameters only.
+* `RefCudaSolver`: the reference's own kernels compiled by nvcc for sm_103a
+  and launched by the replay driver oracle/ref_cuda.cu
+  (oracle/_ref/libbrassref_cuda.so); reference parameters only.
+
+The two reference builds read the reference's kernel headers from
+$BRASSPAN_REFERENCE/brasstower when that variable names a brass-pan checkout,
+else from the staged copy oracle/_ref/src/brasstower (`make -C oracle stage`);
+with neither, they are unavailable and the tests that need them skip.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this
 module: as the oracle the GPU results are compared with, or as the timed CPU
@@ -23,8 +30,32 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 ORACLE_LIB = HERE / "_build" / "liboracle.so"
+ORACLE64_LIB = HERE / "_build" / "liboracle64.so"
 REF_LIB = HERE / "_ref" / "libbrassref.so"
-REF_SRC = Path(os.environ.get("BRASSPAN_REFERENCE", "/root/reference")) / "brasstower"
+REF_CUDA_LIB = HERE / "_ref" / "libbrassref_cuda.so"
+STAGED_SRC = HERE / "_ref" / "src" / "brasstower"
+
+
+def ref_source() -> Path | None:
+    """Directory holding the reference's brasstower/ kernel headers, or None."""
+    env = os.environ.get("BRASSPAN_REFERENCE")
+    if env:
+        p = Path(env) / "brasstower"
+        if (p / "kernel" / "fluid.cuh").is_file():
+            return p
+    if (STAGED_SRC / "kernel" / "fluid.cuh").is_file():
+        return STAGED_SRC
+    return None
+
+
+def stage_reference() -> bool:
+    """Copies the reference headers the step needs into oracle/_ref/src
+    (git-ignored) when $BRASSPAN_REFERENCE names a checkout; True if a
+    staged copy exists afterwards."""
+    env = os.environ.get("BRASSPAN_REFERENCE")
+    if env and (Path(env) / "brasstower" / "kernel").is_dir():
+        subprocess.run(["make", "-s", "-C", str(HERE), "stage", f"BRASSPAN_REFERENCE={env}"], check=True)
+    return (STAGED_SRC / "kernel" / "fluid.cuh").is_file()
 
 
 def _abi():
@@ -49,18 +80,83 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def build_ref(force: bool = False) -> Path | None:
-    """Compiles oracle/_ref from the reference checkout; None when it is absent."""
-    if not REF_SRC.is_dir():
+    """Compiles the host build of the reference kernels; None without sources."""
+    src = ref_source()
+    if src is None:
         return None
-    args = ["make", "-s", "-C", str(HERE), "ref", f"REF={REF_SRC}"]
+    args = ["make", "-s", "-C", str(HERE), "ref", f"REF={src}"]
     if force:
         args.insert(1, "-B")
     subprocess.run(args, check=True)
     return REF_LIB
 
 
+def build_ref_cuda(force: bool = False) -> Path | None:
+    """Compiles the reference kernels for sm_103a with the replay driver
+    (needs nvcc, no GPU); None without sources."""
+    src = ref_source()
+    if src is None:
+        return None
+    args = ["make", "-s", "-C", str(HERE), "ref_cuda", f"REF={src}"]
+    if force:
+        args.insert(1, "-B")
+    subprocess.run(args, check=True)
+    return REF_CUDA_LIB
+
+
 _or = None
+_or64 = None
 _ref = None
+_refcu = None
+
+
+# The reference's literals (particlesolver.cuh, kernel/*.cuh, cubrasstower.cuh)
+# as bp_params fields: the values bp_params_init writes, restated here so that
+# the CPU reference arm can set up a run without loading the product library.
+REFERENCE_LITERALS = dict(
+    mode=0, stage_mask=0x7FF, solid_density_scale=2.0, lambda_denominator=15000.0, relaxation=300.0,
+    scorr_k=0.0001, scorr_n=4, scorr_dq=0.03, delta_clamp=5.0, vorticity_eps=0.001, surface_tension=0.5,
+    xsph_c=0.0002, friction_static=0.5, friction_dynamic=0.0, mass_scaling_k=2.0, wind_drag=10.0,
+    wind_lift=100.0, rotation_iterations=20, neighbor_skin=0.0, walk_options=1, bending_stiffness=0.8)
+
+
+def reference_params(scene, **overrides):
+    """bp_params of `scene` with the reference's literals (what
+    brasspan_gb300.make_params(scene) gives), then overrides; pure Python."""
+    abi = _abi()
+    p = abi.BpParams()
+    for k, v in REFERENCE_LITERALS.items():
+        setattr(p, k, v)
+    p.particle_radius = scene.particle_radius
+    p.kernel_radius = scene.kernel_radius
+    p.cell_size = scene.cell_size
+    p.grid_dim = scene.grid_dim
+    p.rest_density = scene.rest_density
+    for k in range(3):
+        p.gravity[k] = scene.gravity[k]
+    for k, v in overrides.items():
+        if isinstance(getattr(p, k), C.Array):
+            arr = getattr(p, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def scenes_module():
+    """brass-pan_gb300/scenes.py (pure Python scene builders) without
+    importing the package or loading its library."""
+    mod = sys.modules.get("brasspan_gb300")
+    if mod is not None:
+        return mod.scenes
+    mod = sys.modules.get("_brasspan_scenes")
+    if mod is None:
+        spec = importlib.util.spec_from_file_location("_brasspan_scenes", REPO / "brass-pan_gb300" / "scenes.py")
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules["_brasspan_scenes"] = mod
+        spec.loader.exec_module(mod)
+    return mod
 
 
 def oracle_lib():
@@ -98,6 +194,7 @@ def ref_lib():
         vp, i32, f32 = C.c_void_p, C.c_int32, C.c_float
         lib.ref_create.restype = vp
         lib.ref_create.argtypes = [C.POINTER(abi.BpSceneDesc), f32, f32, f32, i32, f32]
+        lib.ref_set_mass_scaling.argtypes = [vp, f32]
         lib.ref_destroy.argtypes = [vp]
         lib.ref_update.argtypes = [vp, i32, f32, i32, i32, i32, vp, vp]
         lib.ref_get.argtypes = [vp, i32, vp]
@@ -108,7 +205,30 @@ def ref_lib():
     return _ref
 
 
-# field ids shared by or_get / ref_get
+def ref_cuda_lib():
+    """The reference kernels built for sm_103a with the replay driver, or None
+    if they were not built (no reference sources) or no GPU is usable."""
+    global _refcu
+    if _refcu is None:
+        if not REF_CUDA_LIB.exists():
+            if build_ref_cuda() is None:
+                return None
+        lib = C.CDLL(str(REF_CUDA_LIB))
+        abi = _abi()
+        vp, i32, f32 = C.c_void_p, C.c_int32, C.c_float
+        lib.refcu_create.restype = vp
+        lib.refcu_create.argtypes = [C.POINTER(abi.BpSceneDesc), f32, f32, f32, i32, f32, f32]
+        lib.refcu_destroy.argtypes = [vp]
+        lib.refcu_update.argtypes = [vp, i32, f32, i32, i32, i32, vp, vp]
+        lib.refcu_time_updates.argtypes = [vp, i32, i32, f32, i32, i32, vp, C.c_size_t, C.POINTER(f32)]
+        lib.refcu_set_state.argtypes = [vp, vp, vp]
+        lib.refcu_get.argtypes = [vp, i32, vp]
+        lib.refcu_error.restype = i32
+        _refcu = lib
+    return _refcu
+
+
+# field ids shared by or_get / ref_get / refcu_get
 F_X, F_P, F_V, F_TO_ORIG, F_TO_NEW, F_LAMBDA, F_DENSITY, F_INVSCALED, F_SORTED_CELL, F_ROT, F_CM, \
     F_OMEGA, F_NORMAL, F_MASS, F_PHASE = range(15)
 
@@ -208,6 +328,7 @@ class RefSolver(_Base):
         self.h = self.lib.ref_create(C.byref(desc), C.c_float(params.particle_radius),
                                      C.c_float(params.kernel_radius), C.c_float(params.cell_size),
                                      params.grid_dim, C.c_float(params.rest_density))
+        self.lib.ref_set_mass_scaling(self.h, C.c_float(params.mass_scaling_k))
         self.n = scene.num_particles
         self.nb = int(len(scene.rigid_ranges))
         self._getter = self.lib.ref_get
@@ -219,6 +340,69 @@ class RefSolver(_Base):
     def __del__(self):
         try:
             self.lib.ref_destroy(self.h)
+        except Exception:
+            pass
+
+
+class RefCudaSolver(_Base):
+    """The reference's own kernels on the GPU (reference parameters only):
+    nvcc-built for sm_103a, launched on the legacy default stream in the
+    order of ParticleSolver::update, the stage mask and iteration count as
+    parameters.  Float atomics make its sums order-dependent run to run."""
+
+    def __init__(self, scene, params):
+        self.lib = ref_cuda_lib()
+        if self.lib is None:
+            raise RuntimeError("reference CUDA build unavailable (no reference sources at build time)")
+        abi = _abi()
+        desc, keep = abi.scene_desc(scene)
+        self.mask = params.stage_mask
+        self.h = self.lib.refcu_create(C.byref(desc), C.c_float(params.particle_radius),
+                                       C.c_float(params.kernel_radius), C.c_float(params.cell_size),
+                                       params.grid_dim, C.c_float(params.rest_density),
+                                       C.c_float(params.mass_scaling_k))
+        if not self.h:
+            raise RuntimeError(f"refcu_create failed (CUDA error {self.lib.refcu_error()})")
+        self.n = scene.num_particles
+        self.nb = int(len(scene.rigid_ranges))
+        self._getter = self._get_checked
+
+    def _get_checked(self, h, field, out):
+        err = self.lib.refcu_get(h, field, out)
+        if err:
+            raise RuntimeError(f"reference CUDA step failed (CUDA error {err})")
+
+    def _update(self, nsub, dt, iters, picked, pp, pv):
+        err = self.lib.refcu_update(self.h, nsub, C.c_float(dt), iters, self.mask, picked,
+                                    None if pp is None else pp.ctypes.data, None if pv is None else pv.ctypes.data)
+        if err:
+            raise RuntimeError(f"reference CUDA step failed (CUDA error {err})")
+
+    def time_updates(self, frames, nsub, dt, iters, flush_ptr=None, flush_bytes=0):
+        """Summed CUDA-event milliseconds of `frames` updates, L2 flushed by a
+        write of flush_bytes to the device buffer flush_ptr before each."""
+        ms = C.c_float(0.0)
+        err = self.lib.refcu_time_updates(self.h, frames, nsub, C.c_float(dt), iters, self.mask, flush_ptr,
+                                          flush_bytes, C.byref(ms))
+        if err:
+            raise RuntimeError(f"reference CUDA step failed (CUDA error {err})")
+        return float(ms.value)
+
+    def set_state(self, x_original, v_original):
+        x = np.ascontiguousarray(x_original, np.float32)
+        v = np.ascontiguousarray(v_original, np.float32)
+        err = self.lib.refcu_set_state(self.h, x.ctypes.data, v.ctypes.data)
+        if err:
+            raise RuntimeError(f"refcu_set_state failed (CUDA error {err})")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.refcu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 

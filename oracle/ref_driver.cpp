@@ -16,10 +16,10 @@
  * (identical result: LSD radix sort is stable), and the replay of
  * ParticleSolver::update() (particlesolver.cuh:772-1072) with the commented
  * constraint block (:881-993) and wind block (:838-858) enabled and the
- * solver-iteration count as a parameter.  The few one-line kernels defined
- * inside particlesolver.cuh (which cannot be parsed by a host compiler: it
- * uses <<<>>> launches, conio.h and MSVC-only exceptions) are restated below
- * with their line numbers.
+ * solver-iteration count and the mass-scaling k as parameters.  The few
+ * one-line kernels defined inside particlesolver.cuh (which cannot be parsed
+ * by a host compiler: it uses <<<>>> launches, conio.h and MSVC-only
+ * exceptions) are restated below with their line numbers.
  *
  * Defined behaviour where the reference reads uninitialised memory: the lambda
  * of a solid particle (fluid.cuh:207 reads lambdas[j] that fluidLambda never
@@ -166,6 +166,7 @@ static void k_acc(float3 *a, const float3 *d, int n) /* accDevArr_float3, kernel
 struct RefSolver {
     int n = 0;
     float radius = 0, h = 0, cell = 0, restDensity = 0;
+    float massScalingK = 2.0f; /* MASS_SCALING_CONSTANT (cubrasstower.cuh:20), passed at :809 */
     int D = 0;
     std::vector<float3> x, p, v, sx, sp, sv, dX, tmp, omegas, normals;
     std::vector<float> m, sm, invScaled, lambdas, densities;
@@ -251,7 +252,7 @@ static void update(RefSolver &s, int numSub, float dt, int iterations, int mask,
         k_applyGravity(s.p.data(), n, subDt);
         update_grid(s);
         k_inverseMapping(s.toNew.data(), s.toOrig.data(), n);
-        k_computeInvScaledMasses(s.invScaled.data(), s.m.data(), s.x.data(), 2.0f, n);
+        k_computeInvScaledMasses(s.invScaled.data(), s.m.data(), s.x.data(), s.massScalingK, n);
 
         float3 *x = s.x.data(), *p = s.p.data(), *v = s.v.data(), *dX = s.dX.data();
         const int *cst = s.cellStart.data(), *cen = s.cellEnd.data(), *ph = s.phase.data();
@@ -431,6 +432,10 @@ void *ref_create(const bp_scene_desc *sc, float radius, float h, float cell, int
 }
 
 void ref_destroy(void *h) { delete (RefSolver *)h; }
+
+/* The k of the inverse scaled masses (the literal MASS_SCALING_CONSTANT = 2
+ * at the reference's call site) as a parameter. */
+void ref_set_mass_scaling(void *h, float k) { ((RefSolver *)h)->massScalingK = k; }
 
 int ref_update(void *h, int numSub, float dt, int iterations, int mask, int picked, const float *pp,
                const float *pv)

@@ -106,3 +106,41 @@ def test_oracle_picking_matches_reference(bp, oracle):
         r.update(2, 1 / 60, 3, picked=7, picked_position=pp, picked_velocity=pv)
     np.testing.assert_array_equal(o.positions(), r.positions())
     np.testing.assert_array_equal(o.velocities(), r.velocities())
+
+
+def test_reference_params_match_product_literals(bp, oracle):
+    """oracle.reference_params (used by the CPU reference arm, which loads no
+    product code) gives exactly what make_params gives."""
+    for scene in (fluid_scene(bp, (4, 4, 4), seed=1), small_mixed_scene(bp, seed=1)):
+        a, b = bp.make_params(scene), oracle.reference_params(scene)
+        assert bytes(a) == bytes(b)
+        a, b = bp.make_params(scene, mass_scaling_k=0.0), oracle.reference_params(scene, mass_scaling_k=0.0)
+        assert bytes(a) == bytes(b)
+
+
+def test_reference_mass_scaling_parameter(bp, oracle):
+    """The reference replay takes the mass-scaling k as a parameter (the
+    literal 2 at its call site): k = 0 gives what the oracle gives at k = 0."""
+    if oracle.ref_lib() is None:
+        pytest.skip("reference sources absent")
+    scene = small_mixed_scene(bp, seed=12)
+    params = bp.make_params(scene, mass_scaling_k=0.0)
+    o = oracle.OracleSolver(scene, params)
+    r = oracle.RefSolver(scene, params)
+    o.update(2, 1.0 / 60.0, 4)
+    r.update(2, 1.0 / 60.0, 4)
+    np.testing.assert_array_equal(o.positions(), r.positions())
+    np.testing.assert_array_equal(o.get(oracle.F_INVSCALED), r.get(oracle.F_INVSCALED))
+
+
+def test_reference_cuda_build_exports(oracle):
+    """The reference's sm_103a build loads without a GPU and exports the
+    replay driver's entry points (its compute calls need the GPU)."""
+    if oracle.ref_source() is None:
+        pytest.skip("reference sources absent")
+    import ctypes
+
+    lib = ctypes.CDLL(str(oracle.build_ref_cuda()))
+    for name in ("refcu_create", "refcu_destroy", "refcu_update", "refcu_time_updates", "refcu_set_state",
+                 "refcu_get", "refcu_error"):
+        assert hasattr(lib, name), name
