@@ -159,12 +159,17 @@ def scenes_module():
     return mod
 
 
-def oracle_lib():
-    global _or
-    if _or is None:
-        if not ORACLE_LIB.exists():
+def oracle_lib(precision: int = 32):
+    """liboracle.so (fp32) or, precision=64, liboracle64.so (the FP64 host oracle)."""
+    global _or, _or64
+    cached = _or if precision == 32 else _or64
+    if cached is None:
+        path = ORACLE_LIB if precision == 32 else ORACLE64_LIB
+        if not path.exists():
             build_oracle()
-        lib = C.CDLL(str(ORACLE_LIB))
+        lib = C.CDLL(str(path))
+        if lib.or_real_size() != precision // 8:
+            raise RuntimeError(f"{path.name}: expected {precision}-bit reals")
         abi = _abi()
         vp, i32, f32 = C.c_void_p, C.c_int32, C.c_float
         lib.or_create.restype = vp
@@ -178,8 +183,14 @@ def oracle_lib():
         lib.or_set_threads.argtypes = [i32]
         lib.or_grid_build.argtypes = [i32, vp, f32, i32, vp, vp, vp, vp, vp]
         lib.or_neighbor_counts.argtypes = [i32, vp, f32, i32, f32, vp, vp, vp]
-        _or = lib
-    return _or
+        lib.or_set_wind.argtypes = [vp, vp]
+        lib.or_set_distance_params.argtypes = [vp, vp]
+        if precision == 32:
+            _or = lib
+        else:
+            _or64 = lib
+        cached = lib
+    return cached
 
 
 def ref_lib():
@@ -236,13 +247,14 @@ F_X, F_P, F_V, F_TO_ORIG, F_TO_NEW, F_LAMBDA, F_DENSITY, F_INVSCALED, F_SORTED_C
 class _Base:
     n: int
     nb: int
+    fdtype = np.float32  # element type of the float fields
 
     def _get(self, field):
         shapes = {F_X: (self.n, 3), F_P: (self.n, 3), F_V: (self.n, 3), F_OMEGA: (self.n, 3),
                   F_NORMAL: (self.n, 3), F_ROT: (self.nb, 4), F_CM: (self.nb, 3)}
         ints = {F_TO_ORIG, F_TO_NEW, F_SORTED_CELL, F_PHASE}
         shape = shapes.get(field, (self.n,))
-        out = np.zeros(shape, np.int32 if field in ints else np.float32)
+        out = np.zeros(shape, np.int32 if field in ints else self.fdtype)
         if out.size:
             self._getter(self.h, field, out.ctypes.data)
         return out
@@ -273,10 +285,13 @@ class _Base:
 
 
 class OracleSolver(_Base):
-    """oracle.c: the restatement, deterministic when single-threaded."""
+    """oracle.c: the restatement, deterministic when single-threaded.
+    precision=64 runs the FP64 host oracle (the same source in double): its
+    fields come back as float64 and its state inputs are taken as float64."""
 
-    def __init__(self, scene, params, threads: int = 1):
-        self.lib = oracle_lib()
+    def __init__(self, scene, params, threads: int = 1, precision: int = 32):
+        self.lib = oracle_lib(precision)
+        self.fdtype = np.float32 if precision == 32 else np.float64
         self.lib.or_set_threads(threads)
         abi = _abi()
         desc, keep = abi.scene_desc(scene)
@@ -295,17 +310,27 @@ class OracleSolver(_Base):
 
     def adopt(self, x_sorted, v_sorted, to_orig, rotations=None):
         """Takes over another solver's state, arrangement included."""
-        x = np.ascontiguousarray(x_sorted, np.float32)
-        v = np.ascontiguousarray(v_sorted, np.float32)
+        x = np.ascontiguousarray(x_sorted, self.fdtype)
+        v = np.ascontiguousarray(v_sorted, self.fdtype)
         t = np.ascontiguousarray(to_orig, np.int32)
-        r = None if rotations is None else np.ascontiguousarray(rotations, np.float32)
+        r = None if rotations is None else np.ascontiguousarray(rotations, self.fdtype)
         self.lib.or_set_full_state(self.h, x.ctypes.data, v.ctypes.data, t.ctypes.data,
                                    None if r is None else r.ctypes.data)
 
     def set_state(self, x_sorted=None, v_sorted=None):
-        x = None if x_sorted is None else np.ascontiguousarray(x_sorted, np.float32)
-        v = None if v_sorted is None else np.ascontiguousarray(v_sorted, np.float32)
+        x = None if x_sorted is None else np.ascontiguousarray(x_sorted, self.fdtype)
+        v = None if v_sorted is None else np.ascontiguousarray(v_sorted, self.fdtype)
         self.lib.or_set_state(self.h, None if x is None else x.ctypes.data, None if v is None else v.ctypes.data)
+
+    def set_wind(self, wind):
+        """The textbook wind vector, in this oracle's precision."""
+        w = np.ascontiguousarray(wind, self.fdtype)
+        self.lib.or_set_wind(self.h, w.ctypes.data)
+
+    def set_distance_params(self, params):
+        """(rest length, stiffness) of every distance constraint, [M][2]."""
+        p = np.ascontiguousarray(params, self.fdtype)
+        self.lib.or_set_distance_params(self.h, p.ctypes.data)
 
     def __del__(self):
         try:

@@ -15,7 +15,6 @@
  */
 #include "oracle.h"
 
-#include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -23,34 +22,43 @@
 #include <omp.h>
 #endif
 
+/* One source, two precisions: `real` is float (the restatement, bit-exact to
+ * the reference) or, built with ORACLE_REAL_DOUBLE, double (the FP64 host
+ * oracle: every state array, parameter copy and operation in double; the
+ * reference's float literals keep their float values).  <tgmath.h> makes
+ * sqrt, pow, sin, cos, acos and fabs follow the argument type, so the float
+ * build calls sqrtf & co. exactly as before. */
+typedef or_real real;
+#include <tgmath.h>
+
 static int g_threads = 1;
 void or_set_threads(int t) { g_threads = t > 0 ? t : 1; }
 int or_get_threads(void) { return g_threads; }
 
-/* ---- fp32 vector helpers (same operation order as the reference's float3
+/* ---- vector helpers (same operation order as the reference's float3
  * operators: component-wise, dot = x*x' + y*y' + z*z' left to right) ---- */
 
-typedef struct { float x, y, z; } f3;
-typedef struct { float x, y, z, w; } f4;
+typedef struct { real x, y, z; } f3;
+typedef struct { real x, y, z, w; } f4;
 
-static inline f3 v3(float x, float y, float z) { f3 r = {x, y, z}; return r; }
+static inline f3 v3(real x, real y, real z) { f3 r = {x, y, z}; return r; }
 static inline f3 vadd(f3 a, f3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
 static inline f3 vsub(f3 a, f3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
-static inline f3 vmul(f3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }   /* float3 * float */
-static inline f3 smul(float s, f3 a) { return v3(s * a.x, s * a.y, s * a.z); }   /* float * float3 */
-static inline f3 vdiv(f3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
+static inline f3 vmul(f3 a, real s) { return v3(a.x * s, a.y * s, a.z * s); }   /* float3 * scalar */
+static inline f3 smul(real s, f3 a) { return v3(s * a.x, s * a.y, s * a.z); }   /* scalar * float3 */
+static inline f3 vdiv(f3 a, real s) { return v3(a.x / s, a.y / s, a.z / s); }
 static inline f3 vneg(f3 a) { return v3(-a.x, -a.y, -a.z); }
-static inline float vdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline real vdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 static inline f3 vcross(f3 a, f3 b)
 {
     return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
-static inline float vlen2(f3 a) { return vdot(a, a); }
-static inline float vlen(f3 a) { return sqrtf(vdot(a, a)); }
+static inline real vlen2(f3 a) { return vdot(a, a); }
+static inline real vlen(f3 a) { return sqrt(vdot(a, a)); }
 /* normalize with rsqrt = 1/sqrt, the host form of the reference's helper */
-static inline f3 vnormalize(f3 a) { float inv = 1.0f / sqrtf(vdot(a, a)); return vmul(a, inv); }
-static inline float fminf_(float a, float b) { return a < b ? a : b; }
-static inline float fmaxf_(float a, float b) { return a > b ? a : b; }
+static inline f3 vnormalize(f3 a) { real inv = 1.0f / sqrt(vdot(a, a)); return vmul(a, inv); }
+static inline real fminf_(real a, real b) { return a < b ? a : b; }
+static inline real fmaxf_(real a, real b) { return a > b ? a : b; }
 
 static inline void atomic_add3(f3 *arr, int i, f3 d)
 {
@@ -65,19 +73,19 @@ static inline void atomic_add3(f3 *arr, int i, f3 d)
 /* ---- SPH kernels (K/fluid.cuh:11-74) --------------------------------------- */
 
 typedef struct {
-    float c1, c2, c3, c4, h, h2, half_h;
+    real c1, c2, c3, c4, h, h2, half_h;
 } sph_consts;
 
 /* SetKernelRadius (K/fluid.cuh:11-27): pi is the literal 3.141592.  Textbook
  * mode scales the Akinci spline's inner offset h^6/64 by the spline constant
  * as in Akinci et al. 2013 (the reference leaves it unscaled, quirk Q7). */
-static sph_consts make_sph(float h, int textbook)
+static sph_consts make_sph(real h, int textbook)
 {
     sph_consts k;
-    k.c1 = 315.f / 64.f / 3.141592f / powf(h, 9.0f);
-    k.c2 = -45.f / 3.141592f / powf(h, 6.f);
-    k.c3 = 32.0f / 3.141592f / powf(h, 9.f);
-    k.c4 = powf(h, 6.0f) / 64.0f;
+    k.c1 = 315.f / 64.f / 3.141592f / pow(h, 9.0f);
+    k.c2 = -45.f / 3.141592f / pow(h, 6.f);
+    k.c3 = 32.0f / 3.141592f / pow(h, 9.f);
+    k.c4 = pow(h, 6.0f) / 64.0f;
     if (textbook) k.c4 = k.c3 * k.c4;
     k.h2 = h * h;
     k.half_h = h * 0.5f;
@@ -85,23 +93,23 @@ static sph_consts make_sph(float h, int textbook)
     return k;
 }
 
-static inline float poly6(const sph_consts *k, float r2) /* K/fluid.cuh:31-43 */
+static inline real poly6(const sph_consts *k, real r2) /* K/fluid.cuh:31-43 */
 {
-    const float t = k->h2 - r2;
+    const real t = k->h2 - r2;
     return k->c1 * t * t * t;
 }
 
-static inline f3 spiky_grad(const sph_consts *k, f3 v, float r2) /* K/fluid.cuh:45-57 */
+static inline f3 spiky_grad(const sph_consts *k, f3 v, real r2) /* K/fluid.cuh:45-57 */
 {
-    const float r = sqrtf(r2);
-    const float t = k->h - r;
+    const real r = sqrt(r2);
+    const real t = k->h - r;
     return vdiv(smul(k->c2 * t * t, v), r);
 }
 
-static inline float akinci_spline(const sph_consts *k, float r) /* K/fluid.cuh:59-74 (quirk Q7 kept) */
+static inline real akinci_spline(const sph_consts *k, real r) /* K/fluid.cuh:59-74 (quirk Q7 kept) */
 {
-    const float t = (k->h - r) * r;
-    const float t3 = t * t * t;
+    const real t = (k->h - r) * r;
+    const real t3 = t * t * t;
     if (r >= k->half_h) return k->c3 * t3;
     return 2.0f * k->c3 * t3 - k->c4;
 }
@@ -110,12 +118,18 @@ static inline float akinci_spline(const sph_consts *k, float r) /* K/fluid.cuh:5
 
 typedef struct { int x, y, z; } i3;
 
-static inline i3 grid_pos(f3 p, float cell) /* calcGridPos, K/grid.cuh:9-13 */
+/* calcGridPos, K/grid.cuh:9-13.  The cell of a position is integer work that
+ * the reference defines in float arithmetic (p + 50000 keeps about 0.004 m of
+ * resolution), so both precisions compute it in float from the position
+ * rounded to float: the FP64 oracle then builds the grid the fp32 step builds
+ * and differs from it only in the floating-point sums. */
+static inline i3 grid_pos(f3 p, real cell)
 {
+    const float cf = (float)cell;
     i3 c;
-    c.x = (int)((p.x + 50000.0f) / cell);
-    c.y = (int)((p.y + 50000.0f) / cell);
-    c.z = (int)((p.z + 50000.0f) / cell);
+    c.x = (int)(((float)p.x + 50000.0f) / cf);
+    c.y = (int)(((float)p.y + 50000.0f) / cf);
+    c.z = (int)(((float)p.z + 50000.0f) / cf);
     return c;
 }
 
@@ -186,7 +200,7 @@ int or_grid_build(int n, const float *pos, float cell, int D, int *cell_ids, int
 int or_neighbor_counts(int n, const float *sp, float cell, int D, float h, const int *cs,
                        const int *ce, int *counts)
 {
-    const float h2 = h * h;
+    const real h2 = h * h;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < n; ++i) {
         const f3 pi = v3(sp[3 * i], sp[3 * i + 1], sp[3 * i + 2]);
@@ -211,12 +225,13 @@ int or_neighbor_counts(int n, const float *sp, float cell, int D, float h, const
 struct or_solver {
     int n, D, nb, npairs, nfaces, nimm, nplanes, nbend;
     bp_params prm;
+    real wind[3]; /* prm.wind_velocity, or an override in this precision (or_set_wind) */
     f3 *x, *p, *v, *sx, *sp, *sv, *dX, *tmp, *omega, *normal;
-    float *m, *sm, *w, *lambda, *rho;
+    real *m, *sm, *w, *lambda, *rho;
     int *phase, *sphase, *group, *sgroup, *to_orig, *sto_orig, *to_new;
     int *cell_id, *sorted_cell, *sorted_pid, *cell_start, *cell_end;
     int *ranges, *pairs, *faces, *imm, *bends;
-    float *dparams, *planes;
+    real *dparams, *planes;
     f3 *rest, *cms;
     f4 *rot;
 };
@@ -229,6 +244,7 @@ or_solver *or_create(const bp_scene_desc *sc, const bp_params *prm)
     const int n = sc->num_particles;
     s->n = n;
     s->prm = *prm;
+    for (int q = 0; q < 3; ++q) s->wind[q] = prm->wind_velocity[q];
     s->D = prm->grid_dim;
     ALLOC(s->x, n); ALLOC(s->p, n); ALLOC(s->v, n); ALLOC(s->sx, n); ALLOC(s->sp, n); ALLOC(s->sv, n);
     ALLOC(s->dX, n); ALLOC(s->tmp, n); ALLOC(s->omega, n); ALLOC(s->normal, n);
@@ -253,13 +269,13 @@ or_solver *or_create(const bp_scene_desc *sc, const bp_params *prm)
     }
     s->nplanes = sc->num_planes;
     ALLOC(s->planes, 6 * s->nplanes);
-    memcpy(s->planes, sc->planes, sizeof(float) * 6 * (size_t)s->nplanes);
+    for (int q = 0; q < 6 * s->nplanes; ++q) s->planes[q] = sc->planes[q];
     s->npairs = sc->num_distance_constraints;
     ALLOC(s->pairs, 2 * s->npairs);
     ALLOC(s->dparams, 2 * s->npairs);
-    if (s->npairs) {
+    if (s->npairs > 0) {
         memcpy(s->pairs, sc->distance_pairs, sizeof(int) * 2 * (size_t)s->npairs);
-        memcpy(s->dparams, sc->distance_params, sizeof(float) * 2 * (size_t)s->npairs);
+        for (int q = 0; q < 2 * s->npairs; ++q) s->dparams[q] = sc->distance_params[q];
     }
     s->nfaces = sc->num_wind_faces;
     ALLOC(s->faces, 3 * s->nfaces);
@@ -300,10 +316,25 @@ int or_set_params(or_solver *s, const bp_params *prm)
 {
     if (prm->grid_dim != s->D) return 1;
     s->prm = *prm;
+    for (int q = 0; q < 3; ++q) s->wind[q] = prm->wind_velocity[q];
     return 0;
 }
 
-int or_set_state(or_solver *s, const float *x, const float *v)
+int or_real_size(void) { return (int)sizeof(real); }
+
+int or_set_wind(or_solver *s, const real *wind)
+{
+    for (int q = 0; q < 3; ++q) s->wind[q] = wind[q];
+    return 0;
+}
+
+int or_set_distance_params(or_solver *s, const real *params)
+{
+    for (int q = 0; q < 2 * s->npairs; ++q) s->dparams[q] = params[q];
+    return 0;
+}
+
+int or_set_state(or_solver *s, const real *x, const real *v)
 {
     for (int i = 0; i < s->n; ++i) {
         if (x) s->x[i] = v3(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
@@ -316,10 +347,10 @@ int or_set_state(or_solver *s, const float *x, const float *v)
  * and velocities [N][3] in that order, its sorted->original map, and
  * optionally the rigid-body quaternions [B][4]; per-particle constants follow
  * the new arrangement.  Used to restart both solvers from identical inputs. */
-int or_set_full_state(or_solver *s, const float *x, const float *v, const int *to_orig, const float *rot)
+int or_set_full_state(or_solver *s, const real *x, const real *v, const int *to_orig, const real *rot)
 {
     const int n = s->n;
-    float *m0 = (float *)malloc(sizeof(float) * (size_t)(n > 0 ? n : 1));
+    real *m0 = (real *)malloc(sizeof(real) * (size_t)(n > 0 ? n : 1));
     int *ph0 = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
     int *g0 = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
     for (int i = 0; i < n; ++i) {
@@ -356,7 +387,7 @@ int or_set_full_state(or_solver *s, const float *x, const float *v, const int *t
 static void update_grid(or_solver *s)
 {
     const int n = s->n, D = s->D;
-    const float cell = s->prm.cell_size;
+    const real cell = s->prm.cell_size;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < n; ++i) {
         const i3 c = grid_pos(s->p[i], cell);
@@ -394,11 +425,11 @@ static inline f3 plane_o(const or_solver *s, int k) { return v3(s->planes[6 * k]
 static inline f3 plane_n(const or_solver *s, int k) { return v3(s->planes[6 * k + 3], s->planes[6 * k + 4], s->planes[6 * k + 5]); }
 
 /* planeStabilize (K/particleplane.cuh:3-19), both x and p move */
-static void plane_stabilize(or_solver *s, f3 o, f3 nrm, float r)
+static void plane_stabilize(or_solver *s, f3 o, f3 nrm, real r)
 {
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < s->n; ++i) {
-        const float d = vdot(vsub(o, s->x[i]), nrm) + r;
+        const real d = vdot(vsub(o, s->x[i]), nrm) + r;
         if (d <= 0) continue;
         s->x[i] = vadd(s->x[i], smul(d, nrm));
         s->p[i] = vadd(s->p[i], smul(d, nrm));
@@ -407,18 +438,18 @@ static void plane_stabilize(or_solver *s, f3 o, f3 nrm, float r)
 
 /* particlePlaneCollisionConstraint (K/particleplane.cuh:21-58), friction per
  * Macklin et al. 2014 eq. 24 with the reference's static/dynamic constants */
-static void plane_collision(or_solver *s, f3 o, f3 nrm, float r)
+static void plane_collision(or_solver *s, f3 o, f3 nrm, real r)
 {
-    const float fs = s->prm.friction_static, fd = s->prm.friction_dynamic;
+    const real fs = s->prm.friction_static, fd = s->prm.friction_dynamic;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < s->n; ++i) {
-        const float d = vdot(vsub(o, s->p[i]), nrm) + r;
+        const real d = vdot(vsub(o, s->p[i]), nrm) + r;
         if (d <= 0) continue;
         const f3 x = s->x[i];
         const f3 diff = vsub(s->p[i], x);
-        const float dn = vdot(diff, nrm);
+        const real dn = vdot(diff, nrm);
         const f3 dt = vsub(diff, smul(dn, nrm));
-        const float dtl = vlen(dt);
+        const real dtl = vlen(dt);
         const f3 resolved = vadd(smul(d, nrm), s->p[i]);
         const f3 dx = vsub(resolved, x);
         const f3 tdx = vsub(dx, smul(vdot(dx, nrm), nrm));
@@ -430,17 +461,17 @@ static void plane_collision(or_solver *s, f3 o, f3 nrm, float r)
 }
 
 /* particleParticleCollisionConstraint (K/particleparticle.cuh:5-101) -> dX */
-static void particle_collision(or_solver *s, float radius)
+static void particle_collision(or_solver *s, real radius)
 {
     const int n = s->n;
-    const float fs = s->prm.friction_static, fd = s->prm.friction_dynamic;
-    const float cell = s->prm.cell_size;
+    const real fs = s->prm.friction_static, fd = s->prm.friction_dynamic;
+    const real cell = s->prm.cell_size;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < n; ++i) {
         const f3 xi = s->x[i];
         const f3 xip = s->p[i];
         f3 sum_d = v3(0, 0, 0), sum_f = v3(0, 0, 0);
-        const float wi = s->w[i];
+        const real wi = s->w[i];
         const i3 c_ = grid_pos(xip, cell);
         const int phi = s->phase[i];
         int count = 0;
@@ -449,18 +480,18 @@ static void particle_collision(or_solver *s, float radius)
             if (!(i != j && phi != phj && (phi > 0 || phj > 0))) continue;
             const f3 xjp = s->p[j];
             const f3 diff = vsub(xip, xjp);
-            const float d2 = vlen2(diff);
+            const real d2 = vlen2(diff);
             if (!(d2 < radius * radius * 4.0f && d2 > 1e-5f)) continue;
-            const float dist = sqrtf(d2);
-            const float wj = s->w[j];
-            const float w1 = wi / (wi + wj);
-            const float w2 = wj / (wi + wj);
+            const real dist = sqrt(d2);
+            const real wj = s->w[j];
+            const real w1 = wi / (wi + wj);
+            const real w2 = wj / (wi + wj);
             const f3 proj = vmul(diff, 2.0f * radius / dist - 1.0f);
             const f3 dxi = smul(w1, proj);
             const f3 xistar = vadd(dxi, xip);
             sum_d = vadd(sum_d, dxi);
             const f3 dxj = smul(-w2, proj);
-            const float dxi2 = vlen2(dxi);
+            const real dxi2 = vlen2(dxi);
             if (dxi2 > radius * radius * 0.001f * 0.001f) {
                 count += 1;
                 const f3 xj = s->x[j];
@@ -468,17 +499,17 @@ static void particle_collision(or_solver *s, float radius)
                 const f3 t1 = vsub(vsub(xistar, xi), vsub(xjstar, xj));
                 const f3 nn = vdiv(diff, dist);
                 const f3 tdx = vsub(t1, smul(vdot(t1, nn), nn));
-                const float tl2 = vlen2(tdx);
+                const real tl2 = vlen2(tdx);
                 if (tl2 <= (fs * fs) * dxi2)
                     sum_f = vsub(sum_f, smul(w1, tdx));
                 else
-                    sum_f = vsub(sum_f, vmul(smul(w1, tdx), fminf_(fd * sqrtf(dxi2 / tl2), 1.0f)));
+                    sum_f = vsub(sum_f, vmul(smul(w1, tdx), fminf_(fd * sqrt(dxi2 / tl2), 1.0f)));
             }
         }
         if (count == 0)
             atomic_add3(s->dX, i, sum_d);
         else
-            atomic_add3(s->dX, i, vadd(sum_d, vdiv(sum_f, (float)count)));
+            atomic_add3(s->dX, i, vadd(sum_d, vdiv(sum_f, (real)count)));
     }
 }
 
@@ -488,25 +519,25 @@ static void particle_collision(or_solver *s, float radius)
 static void fluid_lambda(or_solver *s, const sph_consts *k)
 {
     const int n = s->n;
-    const float rho0 = s->prm.rest_density, solid = s->prm.solid_density_scale;
+    const real rho0 = s->prm.rest_density, solid = s->prm.solid_density_scale;
     const int textbook = s->prm.mode == BP_MODE_TEXTBOOK;
     const int clampC = (s->prm.stage_mask & BP_STAGE_AKINCI) != 0;
-    const float cell = s->prm.cell_size;
+    const real cell = s->prm.cell_size;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < n; ++i) {
         if (s->phase[i] > 0) continue;
         const f3 pi = s->p[i];
-        float density = 0.f, sum_g2 = 0.f;
+        real density = 0.f, sum_g2 = 0.f;
         f3 grad_i = v3(0, 0, 0);
         const i3 c_ = grid_pos(pi, cell);
         FOR_EACH_CANDIDATE(s, pi, j) {
             if (!textbook && !(i <= j)) continue;
             const f3 pj = s->p[j];
             const f3 diff = vsub(pi, pj);
-            const float d2 = vlen2(diff);
+            const real d2 = vlen2(diff);
             if (d2 <= k->h2) {
-                const float mj = s->m[j];
-                const float ld = mj * poly6(k, d2);
+                const real mj = s->m[j];
+                const real ld = mj * poly6(k, d2);
                 density += (s->phase[j] < 0) ? ld : solid * ld;
                 if (textbook && d2 > 0) {
                     const f3 g = vdiv(smul(-mj, spiky_grad(k, diff, d2)), rho0);
@@ -515,9 +546,9 @@ static void fluid_lambda(or_solver *s, const sph_consts *k)
                 }
             }
         }
-        float C = density / rho0 - 1.0f;
+        real C = density / rho0 - 1.0f;
         if (clampC) C = fmaxf_(C, 0.0f);
-        float lam;
+        real lam;
         if (textbook) {
             sum_g2 += vdot(grad_i, grad_i);
             lam = -C / (sum_g2 + s->prm.relaxation);
@@ -535,34 +566,34 @@ static void fluid_lambda(or_solver *s, const sph_consts *k)
 static void fluid_position(or_solver *s, const sph_consts *k)
 {
     const int n = s->n;
-    const float rho0 = s->prm.rest_density, K = s->prm.scorr_k;
+    const real rho0 = s->prm.rest_density, K = s->prm.scorr_k;
     const int N = s->prm.scorr_n;
     const int textbook = s->prm.mode == BP_MODE_TEXTBOOK;
     const int scorr = textbook || !(s->prm.stage_mask & BP_STAGE_AKINCI);
-    const float clampv = textbook ? -1.0f : s->prm.delta_clamp; /* textbook PBF: no per-pair clamp */
-    const float wq = poly6(k, powf(s->prm.scorr_dq * k->h, 2.f));
-    const float cell = s->prm.cell_size;
+    const real clampv = textbook ? -1.0f : s->prm.delta_clamp; /* textbook PBF: no per-pair clamp */
+    const real wq = poly6(k, pow(s->prm.scorr_dq * k->h, 2.f));
+    const real cell = s->prm.cell_size;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < n; ++i) {
         if (s->phase[i] > 0) continue;
         const f3 pi = s->p[i];
         f3 sum = v3(0, 0, 0);
         const i3 c_ = grid_pos(pi, cell);
-        const float mi = s->m[i];
-        const float li = s->lambda[i];
-        const float inv_rho = 1.0f / rho0;
+        const real mi = s->m[i];
+        const real li = s->lambda[i];
+        const real inv_rho = 1.0f / rho0;
         FOR_EACH_CANDIDATE(s, pi, j) {
             if (textbook ? (i == j) : !(i < j)) continue;
             const f3 pj = s->p[j];
             const f3 diff = vsub(pi, pj);
-            const float d2 = vlen2(diff);
+            const real d2 = vlen2(diff);
             if (d2 <= k->h2 && d2 > 0) {
-                const float mj = s->m[j];
-                float sl = li + s->lambda[j];
-                if (scorr) sl += -K * powf(poly6(k, d2) / wq, (float)N);
+                const real mj = s->m[j];
+                real sl = li + s->lambda[j];
+                if (scorr) sl += -K * pow(poly6(k, d2) / wq, (real)N);
                 f3 delta = smul(sl, spiky_grad(k, diff, d2));
                 if (clampv > 0) {
-                    const float len = vlen(delta);
+                    const real len = vlen(delta);
                     delta = (len < clampv) ? delta : vdiv(vmul(delta, fminf_(len, clampv)), len);
                 }
                 sum = vadd(sum, smul(mj, delta));
@@ -579,13 +610,13 @@ static void distance_constraints(or_solver *s)
 #pragma omp parallel for num_threads(g_threads)
     for (int c = 0; c < s->npairs; ++c) {
         const int id1 = s->to_new[s->pairs[2 * c]], id2 = s->to_new[s->pairs[2 * c + 1]];
-        const float d0 = s->dparams[2 * c], kst = s->dparams[2 * c + 1];
+        const real d0 = s->dparams[2 * c], kst = s->dparams[2 * c + 1];
         const f3 x12 = vsub(s->p[id1], s->p[id2]);
-        const float d12 = vlen(x12);
+        const real d12 = vlen(x12);
         if (d12 <= 1e-5f) continue;
         const f3 nn = vdiv(x12, d12);
-        const float w1 = s->w[id1], w2 = s->w[id2];
-        const float sw = w1 + w2;
+        const real w1 = s->w[id1], w2 = s->w[id2];
+        const real sw = w1 + w2;
         const f3 kk = vmul(vmul(nn, (d12 - d0) / sw), kst);
         atomic_add3(s->dX, id1, smul(-w1, kk));
         atomic_add3(s->dX, id2, smul(w2, kk));
@@ -595,7 +626,7 @@ static void distance_constraints(or_solver *s)
 /* bendingConstraints (K/bending.cuh:3-75) -> dX: the dihedral angle of the
  * triangles (1, 2, 3) and (1, 2, 4) over the hinge 1-2 pulled towards pi with
  * the gradients of Mueller et al. 2007 (appendix A), stiffness k (0.8 there). */
-static void bending_constraints(or_solver *s, float kb)
+static void bending_constraints(or_solver *s, real kb)
 {
 #pragma omp parallel for num_threads(g_threads)
     for (int c = 0; c < s->nbend; ++c) {
@@ -604,12 +635,12 @@ static void bending_constraints(or_solver *s, float kb)
         const f3 p1 = s->p[id1];
         const f3 e = vsub(s->p[id2], p1), a = vsub(s->p[id3], p1), b = vsub(s->p[id4], p1);
         const f3 ca = vcross(e, a), cb = vcross(e, b);
-        const float la = vlen(ca);
+        const real la = vlen(ca);
         if (la <= 1e-5f) continue;
-        const float lb = vlen(cb);
+        const real lb = vlen(cb);
         if (lb <= 1e-5f) continue;
         const f3 n1 = vmul(ca, 1.0f / la), n2 = vmul(cb, 1.0f / lb);
-        float d = vdot(n1, n2);
+        real d = vdot(n1, n2);
         d = fminf_(fmaxf_(d, -1.0f), 1.0f);
         const f3 en1 = vcross(e, n1), en2 = vcross(e, n2);
         const f3 an1 = vcross(a, n1), an2 = vcross(a, n2);
@@ -618,11 +649,11 @@ static void bending_constraints(or_solver *s, float kb)
         const f3 q4 = vdiv(vsub(en1, vmul(en2, d)), lb);
         const f3 q2 = vsub(vdiv(vneg(vsub(an2, vmul(an1, d))), la), vdiv(vsub(bn1, vmul(bn2, d)), lb));
         const f3 q1 = vsub(vsub(vneg(q2), q3), q4);
-        const float w1 = s->w[id1], w2 = s->w[id2], w3 = s->w[id3], w4 = s->w[id4];
-        const float den = w1 * vlen2(q1) + w2 * vlen2(q2) + w3 * vlen2(q3) + w4 * vlen2(q4);
-        const float num = sqrtf(1.0f - d * d) * (acosf(d) - 3.141592f);
+        const real w1 = s->w[id1], w2 = s->w[id2], w3 = s->w[id3], w4 = s->w[id4];
+        const real den = w1 * vlen2(q1) + w2 * vlen2(q2) + w3 * vlen2(q3) + w4 * vlen2(q4);
+        const real num = sqrt(1.0f - d * d) * (acos(d) - 3.141592f);
         if (den <= 1e-5f) continue;
-        const float sc = num / den;
+        const real sc = num / den;
         atomic_add3(s->dX, id1, vmul(vmul(smul(-w1, q1), sc), kb));
         atomic_add3(s->dX, id2, vmul(vmul(smul(-w2, q2), sc), kb));
         atomic_add3(s->dX, id3, vmul(vmul(smul(-w3, q3), sc), kb));
@@ -632,11 +663,11 @@ static void bending_constraints(or_solver *s, float kb)
 
 /* applyWindForce (K/wind.cuh:3-50) -> dX.  Reference mode uses the face's
  * mean particle velocity (Q5); textbook mode uses it relative to the wind. */
-static void wind_force(or_solver *s, float dt)
+static void wind_force(or_solver *s, real dt)
 {
     const int textbook = s->prm.mode == BP_MODE_TEXTBOOK;
-    const f3 wind = v3(s->prm.wind_velocity[0], s->prm.wind_velocity[1], s->prm.wind_velocity[2]);
-    const float cd = s->prm.wind_drag, cl = s->prm.wind_lift;
+    const f3 wind = v3(s->wind[0], s->wind[1], s->wind[2]);
+    const real cd = s->prm.wind_drag, cl = s->prm.wind_lift;
 #pragma omp parallel for num_threads(g_threads)
     for (int f = 0; f < s->nfaces; ++f) {
         const int id1 = s->to_new[s->faces[3 * f]], id2 = s->to_new[s->faces[3 * f + 1]],
@@ -645,15 +676,15 @@ static void wind_force(or_solver *s, float dt)
         const f3 a = vsub(p2, p1), b = vsub(p3, p1);
         f3 v = vdiv(vadd(vadd(s->v[id1], s->v[id2]), s->v[id3]), 3.f);
         if (textbook) v = vsub(v, wind);
-        const float lv = vlen(v);
+        const real lv = vlen(v);
         if (lv <= 1e-5f) continue;
         const f3 vh = vdiv(v, lv);
         f3 fnrm = vcross(a, b);
-        const float lf = vlen(fnrm);
+        const real lf = vlen(fnrm);
         if (lf <= 1e-5f) continue;
         fnrm = vdiv(fnrm, lf);
         fnrm = (vdot(fnrm, v) > 0) ? fnrm : vneg(fnrm);
-        const float area = 0.5f * lf;
+        const real area = 0.5f * lf;
         const f3 drag = smul(cd * (lv * lv) * area * vdot(fnrm, vh), vneg(vh));
         const f3 uh = vcross(vcross(fnrm, vh), vh);
         const f3 lift = smul(cl * (lv * lv) * area * vdot(fnrm, vh), uh);
@@ -675,22 +706,22 @@ static inline f4 qmul(f4 a, f4 b)
     r.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
     return r;
 }
-static inline f4 qaxis(f3 d, float angle)
+static inline f4 qaxis(f3 d, real angle)
 {
-    const float sh = sinf(angle * 0.5f), ch = cosf(angle * 0.5f);
+    const real sh = sin(angle * 0.5f), ch = cos(angle * 0.5f);
     f4 r = {d.x * sh, d.y * sh, d.z * sh, ch};
     return r;
 }
 static inline f4 qnormalize(f4 q)
 {
-    const float inv = 1.0f / sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+    const real inv = 1.0f / sqrt(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
     f4 r = {q.x * inv, q.y * inv, q.z * inv, q.w * inv};
     return r;
 }
 typedef struct { f3 c0, c1, c2; } m3;
 static inline m3 qmatrix(f4 q)
 {
-    const float x2 = q.x * q.x, y2 = q.y * q.y, z2 = q.z * q.z;
+    const real x2 = q.x * q.x, y2 = q.y * q.y, z2 = q.z * q.z;
     m3 m;
     m.c0 = v3(1 - 2 * y2 - 2 * z2, 2 * q.x * q.y + 2 * q.w * q.z, 2 * q.x * q.z - 2 * q.w * q.y);
     m.c1 = v3(2 * q.x * q.y - 2 * q.w * q.z, 1 - 2 * x2 - 2 * z2, 2 * q.y * q.z + 2 * q.w * q.x);
@@ -720,7 +751,7 @@ static void shape_matching(or_solver *s)
         const int np = r1 - r0;
         f3 sum = v3(0, 0, 0);
         for (int t = 0; t < np; ++t) sum = vadd(sum, s->p[s->to_new[r0 + t]]);
-        const f3 cm = vdiv(sum, (float)np);
+        const f3 cm = vdiv(sum, (real)np);
         s->cms[b] = cm;
         f3 a0 = v3(0, 0, 0), a1 = v3(0, 0, 0), a2 = v3(0, 0, 0);
         for (int t = 0; t < np; ++t) {
@@ -734,11 +765,11 @@ static void shape_matching(or_solver *s)
         for (int it = 0; it < iters; ++it) {
             const m3 R = qmatrix(q);
             const f3 num = vadd(vadd(vcross(R.c0, a0), vcross(R.c1, a1)), vcross(R.c2, a2));
-            const float den = 1.0f / fabsf(vdot(R.c0, a0) + vdot(R.c1, a1) + vdot(R.c2, a2)) + 1e-9f;
+            const real den = 1.0f / fabs(vdot(R.c0, a0) + vdot(R.c1, a1) + vdot(R.c2, a2)) + 1e-9f;
             const f3 om = vmul(num, den);
-            const float w2 = vlen2(om);
+            const real w2 = vlen2(om);
             if (w2 <= 1e-9f) break;
-            const float w = sqrtf(w2);
+            const real w = sqrt(w2);
             q = qmul(qaxis(vdiv(om, w), w), q);
             q = qnormalize(q);
         }
@@ -751,7 +782,7 @@ static void shape_matching(or_solver *s)
 /* fluidOmega (K/fluid.cuh:231-279) */
 static void fluid_omega(or_solver *s, const sph_consts *k)
 {
-    const float cell = s->prm.cell_size;
+    const real cell = s->prm.cell_size;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < s->n; ++i) {
         const int phi = s->phase[i];
@@ -762,7 +793,7 @@ static void fluid_omega(or_solver *s, const sph_consts *k)
         FOR_EACH_CANDIDATE(s, pi, j) {
             if (!(i != j && phi == s->phase[j])) continue;
             const f3 diff = vsub(pi, s->p[j]);
-            const float d2 = vlen2(diff);
+            const real d2 = vlen2(diff);
             if (d2 <= k->h2 && d2 > 0) om = vadd(om, vcross(vsub(s->v[j], vi), spiky_grad(k, diff, d2)));
         }
         s->omega[i] = om;
@@ -770,9 +801,9 @@ static void fluid_omega(or_solver *s, const sph_consts *k)
 }
 
 /* fluidVorticity (K/fluid.cuh:281-336): v updated in place (no mass division, Q9) */
-static void fluid_vorticity(or_solver *s, const sph_consts *k, float dt)
+static void fluid_vorticity(or_solver *s, const sph_consts *k, real dt)
 {
-    const float eps = s->prm.vorticity_eps, cell = s->prm.cell_size;
+    const real eps = s->prm.vorticity_eps, cell = s->prm.cell_size;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < s->n; ++i) {
         const int phi = s->phase[i];
@@ -783,7 +814,7 @@ static void fluid_vorticity(or_solver *s, const sph_consts *k, float dt)
         FOR_EACH_CANDIDATE(s, pi, j) {
             if (!(i != j && phi == s->phase[j])) continue;
             const f3 diff = vsub(pi, s->p[j]);
-            const float d2 = vlen2(diff);
+            const real d2 = vlen2(diff);
             if (d2 <= k->h2 && d2 > 0) eta = vadd(eta, smul(vlen(s->omega[j]), spiky_grad(k, diff, d2)));
         }
         if (vlen2(eta) > 1e-3f) {
@@ -797,7 +828,7 @@ static void fluid_vorticity(or_solver *s, const sph_consts *k, float dt)
  * neighbour by its volume m_j / rho_j (Macklin & Mueller 2013, eq. 17). */
 static void fluid_xsph(or_solver *s, const sph_consts *k, f3 *out)
 {
-    const float c = s->prm.xsph_c, cell = s->prm.cell_size;
+    const real c = s->prm.xsph_c, cell = s->prm.cell_size;
     const int textbook = s->prm.mode == BP_MODE_TEXTBOOK;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < s->n; ++i) {
@@ -808,9 +839,9 @@ static void fluid_xsph(or_solver *s, const sph_consts *k, f3 *out)
         const i3 c_ = grid_pos(pi, cell);
         FOR_EACH_CANDIDATE(s, pi, j) {
             if (!(i != j && phi == s->phase[j])) continue;
-            const float d2 = vlen2(vsub(pi, s->p[j]));
+            const real d2 = vlen2(vsub(pi, s->p[j]));
             if (d2 <= k->h2) {
-                float wgt = poly6(k, d2);
+                real wgt = poly6(k, d2);
                 if (textbook) wgt = wgt * (s->m[j] / s->rho[j]);
                 vn = vadd(vn, vmul(vsub(s->v[j], vi), wgt));
             }
@@ -822,7 +853,7 @@ static void fluid_xsph(or_solver *s, const sph_consts *k, f3 *out)
 /* fluidNormal (K/fluid.cuh:387-434) */
 static void fluid_normal(or_solver *s, const sph_consts *k)
 {
-    const float cell = s->prm.cell_size;
+    const real cell = s->prm.cell_size;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < s->n; ++i) {
         const int phi = s->phase[i];
@@ -833,7 +864,7 @@ static void fluid_normal(or_solver *s, const sph_consts *k)
         FOR_EACH_CANDIDATE(s, pi, j) {
             if (!(i != j && phi == s->phase[j])) continue;
             const f3 diff = vsub(pi, s->p[j]);
-            const float d2 = vlen2(diff);
+            const real d2 = vlen2(diff);
             if (d2 <= k->h2 && d2 > 0) nn = vadd(nn, smul(1.0f / s->rho[j], spiky_grad(k, diff, d2)));
         }
         s->normal[i] = smul(k->h, nn);
@@ -841,9 +872,9 @@ static void fluid_normal(or_solver *s, const sph_consts *k)
 }
 
 /* fluidAkinciTension (K/fluid.cuh:436-488) -> out (no mass division, Q7) */
-static void fluid_akinci(or_solver *s, const sph_consts *k, float dt, f3 *out)
+static void fluid_akinci(or_solver *s, const sph_consts *k, real dt, f3 *out)
 {
-    const float g = s->prm.surface_tension, rho0 = s->prm.rest_density, cell = s->prm.cell_size;
+    const real g = s->prm.surface_tension, rho0 = s->prm.rest_density, cell = s->prm.cell_size;
 #pragma omp parallel for num_threads(g_threads)
     for (int i = 0; i < s->n; ++i) {
         const int phi = s->phase[i];
@@ -855,12 +886,12 @@ static void fluid_akinci(or_solver *s, const sph_consts *k, float dt, f3 *out)
             if (!(i != j && phi == s->phase[j])) continue;
             const f3 pj = s->p[j];
             const f3 diff = vsub(pi, pj);
-            const float d2 = vlen2(diff);
+            const real d2 = vlen2(diff);
             if (d2 <= k->h2 && d2 > 0.f) {
-                const float dist = sqrtf(d2);
+                const real dist = sqrt(d2);
                 const f3 fco = vdiv(smul(-g * akinci_spline(k, dist), vsub(pi, pj)), dist);
                 const f3 fcu = smul(-g, vsub(s->normal[i], s->normal[j]));
-                const float kij = 2.0f * rho0 / (s->rho[i] + s->rho[j]);
+                const real kij = 2.0f * rho0 / (s->rho[i] + s->rho[j]);
                 ft = vadd(ft, smul(kij, vadd(fco, fcu)));
             }
         }
@@ -884,9 +915,9 @@ int or_update(or_solver *s, int nsub, float dt, int iterations, int picked, cons
     if (n <= 0) return 0;
     const bp_params *P = &s->prm;
     const int mask = P->stage_mask;
-    const float sdt = dt / (float)nsub;
+    const real sdt = dt / (real)nsub;
     const sph_consts k = make_sph(P->kernel_radius, P->mode == BP_MODE_TEXTBOOK);
-    const float r = P->particle_radius;
+    const real r = P->particle_radius;
     const f3 g = v3(P->gravity[0], P->gravity[1], P->gravity[2]);
     const f3 ppos = pp ? v3(pp[0], pp[1], pp[2]) : v3(0, 0, 0);
     const f3 pvel = pv ? v3(pv[0], pv[1], pv[2]) : v3(0, 0, 0);
@@ -904,8 +935,8 @@ int or_update(or_solver *s, int nsub, float dt, int iterations, int picked, cons
         update_grid(s);
         for (int i = 0; i < n; ++i) s->to_new[s->to_orig[i]] = i; /* inverseMapping (K/util.cuh:348-358) */
         for (int i = 0; i < n; ++i) { /* computeInvScaledMasses (PS:84-98) */
-            const float e = 2.7182818284f;
-            const float scale = powf(e, -P->mass_scaling_k * s->x[i].y);
+            const real e = 2.7182818284f;
+            const real scale = pow(e, -P->mass_scaling_k * s->x[i].y);
             s->w[i] = 1.0f / (scale * s->m[i]);
         }
         if (mask & BP_STAGE_PLANES)
@@ -930,7 +961,7 @@ int or_update(or_solver *s, int nsub, float dt, int iterations, int picked, cons
                 acc3(s->p, s->dX, n);
             }
             if (mask & BP_STAGE_FLUID) {
-                memset(s->lambda, 0, sizeof(float) * (size_t)n); /* solids: lambda 0 (Q4) */
+                memset(s->lambda, 0, sizeof(real) * (size_t)n); /* solids: lambda 0 (Q4) */
                 fluid_lambda(s, &k);
                 zero3(s->dX, n);
                 fluid_position(s, &k);
@@ -953,7 +984,7 @@ int or_update(or_solver *s, int nsub, float dt, int iterations, int picked, cons
                     s->p[id] = s->x[id];
                 }
         }
-        const float inv_dt = 1.0f / sdt;
+        const real inv_dt = 1.0f / sdt;
         for (int i = 0; i < n; ++i) { /* updateVelocity, updatePositions (PS:71-81, 121-137) */
             s->v[i] = vmul(vsub(s->p[i], s->x[i]), inv_dt);
             s->x[i] = s->p[i];
@@ -991,15 +1022,15 @@ int or_get(or_solver *s, int field, void *out)
     case 2: memcpy(out, s->v, sizeof(f3) * (size_t)n); break;
     case 3: memcpy(out, s->to_orig, sizeof(int) * (size_t)n); break;
     case 4: memcpy(out, s->to_new, sizeof(int) * (size_t)n); break;
-    case 5: memcpy(out, s->lambda, sizeof(float) * (size_t)n); break;
-    case 6: memcpy(out, s->rho, sizeof(float) * (size_t)n); break;
-    case 7: memcpy(out, s->w, sizeof(float) * (size_t)n); break;
+    case 5: memcpy(out, s->lambda, sizeof(real) * (size_t)n); break;
+    case 6: memcpy(out, s->rho, sizeof(real) * (size_t)n); break;
+    case 7: memcpy(out, s->w, sizeof(real) * (size_t)n); break;
     case 8: memcpy(out, s->sorted_cell, sizeof(int) * (size_t)n); break;
     case 9: memcpy(out, s->rot, sizeof(f4) * (size_t)s->nb); break;
     case 10: memcpy(out, s->cms, sizeof(f3) * (size_t)s->nb); break;
     case 11: memcpy(out, s->omega, sizeof(f3) * (size_t)n); break;
     case 12: memcpy(out, s->normal, sizeof(f3) * (size_t)n); break;
-    case 13: memcpy(out, s->m, sizeof(float) * (size_t)n); break;
+    case 13: memcpy(out, s->m, sizeof(real) * (size_t)n); break;
     case 14: memcpy(out, s->phase, sizeof(int) * (size_t)n); break;
     default: return 1;
     }

@@ -144,3 +144,45 @@ def test_reference_cuda_build_exports(oracle):
     for name in ("refcu_create", "refcu_destroy", "refcu_update", "refcu_time_updates", "refcu_set_state",
                  "refcu_get", "refcu_error"):
         assert hasattr(lib, name), name
+
+
+def test_fp64_oracle_tracks_fp32(bp, oracle):
+    """The FP64 host oracle is the same source in double: it builds the same
+    grid (the cell hash stays float arithmetic) and its state stays within
+    fp32 rounding of the fp32 oracle's over a few frames."""
+    scene = fluid_scene(bp, (10, 10, 10), seed=1, grid_dim=32)
+    params = oracle.reference_params(scene)
+    a = oracle.OracleSolver(scene, params)
+    b = oracle.OracleSolver(scene, params, precision=64)
+    for _ in range(3):
+        a.update(2, 1.0 / 60.0, 4)
+        b.update(2, 1.0 / 60.0, 4)
+    assert b.positions().dtype == np.float64
+    np.testing.assert_array_equal(a.get(oracle.F_TO_ORIG), b.get(oracle.F_TO_ORIG))
+    assert np.abs(a.positions() - b.positions()).max() < 1e-5
+
+
+def test_fp64_oracle_parameter_overrides(bp, oracle):
+    """Wind and stiffness set in double change the rollout as the same values
+    set through the parameters do."""
+    import copy
+
+    abi = bp.abi
+    scene = bp.scenes.flag_scene(n=8, seed=2)
+    stages = abi.BP_STAGE_PLANES | abi.BP_STAGE_WIND | abi.BP_STAGE_DISTANCE | abi.BP_STAGE_IMMOVABLE
+    params = oracle.reference_params(scene, mode=abi.BP_MODE_TEXTBOOK, stage_mask=stages,
+                                     wind_velocity=(4.0, 0.0, 0.0), wind_drag=1.0, wind_lift=0.3, mass_scaling_k=0.0)
+    p2 = copy.copy(params)
+    p2.wind_velocity[1] = 2.0
+    sc2 = copy.deepcopy(scene)
+    sc2.distance_params[:, 1] *= 0.5
+    a = oracle.OracleSolver(sc2, p2, precision=64)
+    b = oracle.OracleSolver(scene, params, precision=64)
+    b.set_wind(np.array([4.0, 2.0, 0.0]))
+    dp = scene.distance_params.astype(np.float64)
+    dp[:, 1] *= 0.5
+    b.set_distance_params(dp)
+    for s in (a, b):
+        for _ in range(3):
+            s.update(2, 1.0 / 60.0, 4)
+    np.testing.assert_array_equal(a.positions(), b.positions())
