@@ -100,13 +100,14 @@ def timed_steps(torch, stream, flush, steps, fn):
     return sum(a.elapsed_time(b) for a, b in zip(starts, ends))
 
 
-def run_adjoint(bp, torch, stream, frames=120, every=10):
+def run_adjoint(bp, torch, stream, frames=120, every=10, check_gradients=True):
     """Differentiable rollouts: a 128x128 cloth flag pinned along one edge
     under wind (4, 0, 0) m/s (loss: squared distance of the final positions to
     a seeded target) and a 64x32x32 = 65,536-particle PBF block (loss: final
     centre of mass), each for `frames` updates of 2 substeps x 4 iterations,
     checkpoints every `every` substeps.  Times one forward rollout and one
-    forward rollout recorded on a tape plus backward()."""
+    forward rollout recorded on a tape plus backward().  With check_gradients,
+    each case's gradient is compared with FP64 finite differences (fd64_check)."""
     abi = bp.abi
     out = {}
     cloth = bp.scenes.flag_scene(n=128, seed=4)
@@ -151,21 +152,234 @@ def run_adjoint(bp, torch, stream, frames=120, every=10):
         out[name] = {"particles": n, "substeps": frames * SUBSTEPS, "checkpoint_every": every,
                      "forward_ms": fwd * 1e3, "forward_adjoint_ms": both * 1e3, "ratio": both / fwd,
                      "grad_finite": bool(np.isfinite(g["velocities"]).all())}
+        if check_gradients:
+            if name.startswith("cloth"):
+                out[name]["gradient_check"] = fd64_check(bp, scene, params, g, frames, target=target)
+            else:  # the FP64 oracle's fluid rollouts take a quarter second per frame: a 10-frame horizon
+                out[name]["gradient_check"] = fd64_check(bp, scene, params, None, 10, solver_args=(stream, every))
     return out
 
 
-def run_reference_cuda(torch, scene, params, steps, warmup, flush, state=None):
+def fd64_check(bp, scene, params, grads, frames, target=None, solver_args=None, h=1e-3):
+    """Directional derivatives of the GPU adjoint against central differences
+    (step h) of the FP64 host oracle's forward, along the wind's three axes,
+    one random direction in the per-edge stiffness and one in the initial
+    velocities (cloth; loss: mean squared distance to `target`), or one
+    random initial-velocity direction (fluid; loss: sum of the centre of
+    mass's coordinates, gradients from a `frames`-update tape recorded here).
+    Each difference is taken at steps h and h/2 and Richardson-extrapolated;
+    the plain step-h difference is reported beside it."""
+    import oracle
+
+    n = scene.num_particles
+    threads = os.cpu_count() or 4
+    if grads is None:  # fluid: record a tape over `frames` updates
+        stream, every = solver_args
+        s = bp.ParticleSolver(scene, params, stream=stream.cuda_stream)
+        s.tape_begin(every)
+        for _ in range(frames):
+            s.update(SUBSTEPS, DT, ITERATIONS)
+        grads = s.backward(np.full((n, 3), 1.0 / n, np.float32))
+        s.close()
+
+    def loss(**kw):
+        o = oracle.OracleSolver(scene, params, threads=threads, precision=64)
+        if "v0" in kw:
+            o.set_state(scene.positions.astype(np.float64), kw["v0"])
+        if "wind" in kw:
+            o.set_wind(kw["wind"])
+        if "dparams" in kw:
+            o.set_distance_params(kw["dparams"])
+        for _ in range(frames):
+            o.update(SUBSTEPS, DT, ITERATIONS)
+        x = o.positions()
+        return float(np.sum((x - target) ** 2) / n) if target is not None else float(x.sum() / n)
+
+    def central(arg, base, direction):
+        dd = [(loss(**{arg: base + s * direction}) - loss(**{arg: base - s * direction})) / (2 * s)
+              for s in (h, h / 2)]
+        return dd[0], (4 * dd[1] - dd[0]) / 3
+
+    rng = np.random.default_rng(7)
+    v0 = (np.zeros((n, 3)) if scene.velocities is None else scene.velocities.astype(np.float64))
+    t0 = time.perf_counter()
+    rows = []
+    if target is not None:
+        wind = np.array(params.wind_velocity[:], np.float64)
+        for k in range(3):
+            rows.append((f"wind[{k}]", *central("wind", wind, np.eye(3)[k]), float(grads["wind_velocity"][k])))
+        dp = scene.distance_params.astype(np.float64)
+        d = rng.standard_normal(len(dp))
+        d /= np.linalg.norm(d)
+        ds = np.zeros_like(dp)
+        ds[:, 1] = d
+        rows.append(("stiffness", *central("dparams", dp, ds),
+                     float(grads["distance_stiffness"].astype(np.float64) @ d)))
+    d = rng.standard_normal((n, 3))
+    d /= np.linalg.norm(d)
+    rows.append(("velocities", *central("v0", v0, d), float(np.sum(grads["velocities"].astype(np.float64) * d))))
+    rel = {w: abs(fr - ad) / max(abs(fr), 1e-30) for w, _, fr, ad in rows}
+    rel_plain = {w: abs(fd - ad) / max(abs(fd), 1e-30) for w, fd, _, ad in rows}
+    return {"frames": frames, "fd_step": h, "max_rel_error": max(rel.values()),
+            "rel_error": {w: float(r) for w, r in rel.items()},
+            "max_rel_error_plain_step": max(rel_plain.values()),
+            "fd64": {w: fr for w, _, fr, _ in rows}, "fd64_plain_step": {w: fd for w, fd, _, _ in rows},
+            "adjoint": {w: ad for w, _, _, ad in rows},
+            "oracle": "FP64 host oracle; central differences at steps h and h/2, Richardson-extrapolated "
+                      "(the plain step-h difference beside it)", "seconds": time.perf_counter() - t0}
+
+
+# Algorithmic bytes of one PBF particle-substep: 514 + 76 I at I iterations
+# (predict + hash 56, sort 16, cell ranges 6, reorder 108, per iteration
+# lambda 24 + delta-p with planes 52, velocity + commit 64, vorticity 112,
+# Akinci 104, XSPH 48): the whole step's compulsory traffic per particle.
+STEP_BYTES_PBF = 514 + 76 * ITERATIONS
+
+
+def kernel_roofline(torch, solver, n, workload, flush, value, prof_steps=3):
+    """Per-kernel device time of `prof_steps` real updates (bp_solver_profile:
+    CUDA events after every launch on the solver's stream, L2 flushed before
+    each update) and the HBM roofline of the longest-running kernel: its
+    algorithmic bytes per launch over its average launch time, against the
+    measured copy bandwidth; beside it the step-level fraction of the PBF
+    byte model at the measured `value`.  Returns (roofline, stages, ms)."""
+    agg: dict[str, list] = {}
+    for _ in range(prof_steps):
+        flush.fill_(7)
+        torch.cuda.synchronize()
+        for name, (cnt, tot) in solver.profile(SUBSTEPS, DT, ITERATIONS).items():
+            a = agg.setdefault(name, [0, 0.0])
+            a[0] += cnt
+            a[1] += tot
+    top_name, (top_launches, top_ms) = max(agg.items(), key=lambda kv: kv[1][1])
+    avg_ms = top_ms / top_launches
+    peak, peak_kind = load_peaks()
+    bytes_per = KERNEL_BYTES.get(top_name)
+    achieved = (bytes_per * n / (avg_ms / 1e3) / 1e9) if bytes_per else None
+    step_gbs = STEP_BYTES_PBF * value / 1e9
+    roofline = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+                "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                "traffic": traffic_for(top_name, n, workload), "bytes_per_particle": bytes_per,
+                "avg_launch_ms": avg_ms, "issue": issue_for(top_name, workload),
+                "step": {"bytes_per_particle_substep": STEP_BYTES_PBF, "achieved": step_gbs,
+                         "frac": step_gbs / peak}}
+    stages = {k: round(v[1] / prof_steps, 4) for k, v in sorted(agg.items(), key=lambda kv: -kv[1][1])}
+    return roofline, stages, sum(v[1] for v in agg.values()) / prof_steps
+
+
+def run_sample(bp, torch, stream, flush, local, name, scene, params, frames, warmup, pre_frames=0,
+               reference_cuda=False):
+    """One more workload, timed like the headline one: `pre_frames` untimed
+    updates to reach the regime sampled, `warmup` more, then `frames` timed
+    updates (CUDA events on the solver's stream, L2 flushed before each),
+    clocks sampled meanwhile; the roofline of its top kernel; and, with
+    reference_cuda, the reference's CUDA step timed from the same state."""
+    n = scene.num_particles
+    solver = bp.ParticleSolver(scene, params, stream=stream.cuda_stream)
+    try:
+        with torch.cuda.stream(stream):
+            for _ in range(pre_frames):
+                solver.update(SUBSTEPS, DT, ITERATIONS)
+            state = (solver.positions(), solver.velocities()) if (reference_cuda and pre_frames) else None
+            for _ in range(warmup):
+                solver.update(SUBSTEPS, DT, ITERATIONS)
+            with ClockSampler(local) as clocks:
+                ms = timed_steps(torch, stream, flush, frames, lambda: solver.update(SUBSTEPS, DT, ITERATIONS))
+            value = n * SUBSTEPS * frames / (ms / 1e3)
+            roofline, stages, _ = kernel_roofline(torch, solver, n, name, flush, value)
+            walks = solver.walk_stats(SUBSTEPS, DT, ITERATIONS)
+            errors = solver.device_errors()
+    finally:
+        solver.close()
+    out = {"workload": name, "particles": n, "frames_before": pre_frames, "warmup": warmup, "steps": frames,
+           "value": value, "unit": "particle-substeps/s", "ms_per_step": ms / frames, "roofline": roofline,
+           "top_stages_ms_per_step": dict(list(stages.items())[:6]), "neighbor_walks": walks,
+           "device_errors": errors, "clocks": clocks.summary()}
+    if reference_cuda:
+        ref = run_reference_cuda(bp, torch, scene, params, frames, warmup, flush, state=state)
+        if ref is not None:
+            ref["ours_over_reference"] = value / ref["value"]
+            out["reference_cuda"] = ref
+    return out
+
+
+def textbook_mixed_params(bp, scene):
+    """The mixed configuration's textbook parameters: PBF with relaxation 600,
+    s_corr (n = 4 at 0.2 h; k = 0.001, the configuration's 0.1 diverges at
+    rho0 = 1000), XSPH c = 0.01, wind (3, 0, 1) m/s with lift 0.3 and drag
+    1.0, Akinci tension 0.5, 10 rotation-extraction iterations."""
+    return bp.make_params(scene, mode=bp.abi.BP_MODE_TEXTBOOK, relaxation=600.0, scorr_k=0.001, scorr_n=4,
+                          scorr_dq=0.2, xsph_c=0.01, wind_velocity=(3.0, 0.0, 1.0), wind_lift=0.3, wind_drag=1.0,
+                          surface_tension=0.5, rotation_iterations=10, mass_scaling_k=0.0)
+
+
+def run_samples(bp, torch, stream, flush, local, args):
+    """The other configurations and regimes, each a sub-object of the line:
+    the 32k dam break (its 100 frames, textbook parameters), the
+    shape-matching stress test, the 1M PBF block alone against the
+    reference's CUDA step, the mixed scene 200 frames in (late regime:
+    compressed fluid, aliased table) against the reference's CUDA step from
+    the same state, and the mixed scene with textbook parameters."""
+    sc = bp.scenes
+    out = {}
+    small = sc.dam_break_32k(seed=0)
+    out["small"] = run_sample(bp, torch, stream, flush, local, "small", small,
+                              bp.make_params(small, mode=bp.abi.BP_MODE_TEXTBOOK, relaxation=600.0, scorr_k=0.001,
+                                             scorr_n=4, scorr_dq=0.2, xsph_c=0.01), frames=100, warmup=3)
+    rigid = sc.rigid_body_pile(seed=0)
+    out["rigid"] = run_sample(bp, torch, stream, flush, local, "rigid", rigid, workload_params(bp, "rigid", rigid),
+                              frames=10, warmup=3)
+    fluid = build_scene(sc, "fluid", seed=0)
+    out["pbf_1m"] = run_sample(bp, torch, stream, flush, local, "fluid", fluid, workload_params(bp, "fluid", fluid),
+                               frames=args.steps, warmup=args.warmup, reference_cuda=not args.no_reference_cuda)
+    mixed = build_scene(sc, "mixed", seed=0)
+    out["late"] = run_sample(bp, torch, stream, flush, local, "mixed", mixed, workload_params(bp, "mixed", mixed),
+                             frames=5, warmup=0, pre_frames=200, reference_cuda=not args.no_reference_cuda)
+    out["textbook"] = run_sample(bp, torch, stream, flush, local, "mixed", mixed, textbook_mixed_params(bp, mixed),
+                                 frames=args.steps, warmup=args.warmup)
+    names = {"small": workload_name("small", small.num_particles) + ", textbook parameters, 100 frames",
+             "rigid": workload_name("rigid", rigid.num_particles),
+             "pbf_1m": workload_name("fluid", fluid.num_particles) + ", reference parameters",
+             "late": workload_name("mixed", mixed.num_particles) + ", frames 201-205 (after 200 untimed)",
+             "textbook": workload_name("mixed", mixed.num_particles) + ", textbook parameters"}
+    for k, v in out.items():
+        v["workload"] = names[k]
+    return out
+
+
+REFERENCE_MAX_BODY = 64  # NUM_MAX_PARTICLE_PER_RIGID_BODY (kernel/cubrasstower.cuh:22)
+
+
+def reference_cuda_params(bp, scene, params):
+    """The parameters the reference's CUDA step runs a workload with: its
+    shape-matching kernel handles at most 64 particles per body, and the
+    mixed scene's 512-particle cubes turn its state non-finite in the third
+    frame (their centre of mass is the sum of 64 positions over 512, so 64
+    particles per cube land inside the fluid).  A scene with larger bodies
+    leaves the stage out of the reference's run; ours keeps it."""
+    import copy
+
+    p = copy.copy(params)
+    sizes = [int(r1 - r0) for r0, r1 in scene.rigid_ranges]
+    if sizes and max(sizes) > REFERENCE_MAX_BODY:
+        p.stage_mask = int(p.stage_mask) & ~bp.abi.BP_STAGE_SHAPE_MATCHING
+    return p
+
+
+def run_reference_cuda(bp, torch, scene, params, steps, warmup, flush, state=None):
     """The reference's own step on this GPU: its kernel headers compiled by
     nvcc for sm_103a and launched by the replay driver (oracle/ref_cuda.cu) on
-    the legacy default stream, same scene, parameters, update shape, warm-up
-    and L2 flush as the GPU arm; CUDA events around each update.  `state`
-    (positions, velocities in original order) replaces the scene's initial
-    state.  None when the reference's sources were not available to build it."""
+    the legacy default stream, same scene, parameters (reference_cuda_params),
+    update shape, warm-up and L2 flush as the GPU arm; CUDA events around each
+    update.  `state` (positions, velocities in original order) replaces the
+    scene's initial state.  None when the reference's sources were not
+    available to build it."""
     import oracle
 
     if oracle.ref_cuda_lib() is None:
         return None
-    ref = oracle.RefCudaSolver(scene, params)
+    rparams = reference_cuda_params(bp, scene, params)
+    ref = oracle.RefCudaSolver(scene, rparams)
     try:
         if state is not None:
             ref.set_state(*state)
@@ -182,7 +396,7 @@ def run_reference_cuda(torch, scene, params, steps, warmup, flush, state=None):
         ref.close()
     n = scene.num_particles
     return {"value": n * SUBSTEPS * k / (ms / 1e3), "unit": "particle-substeps/s", "ms_per_step": ms / k,
-            "steps": k, "warmup": warmup, "state_finite": finite,
+            "steps": k, "warmup": warmup, "state_finite": finite, "stage_mask": int(rparams.stage_mask),
             "kind": "the reference's kernel headers (kernel/*.cuh) built unmodified for sm_103a, 128-thread "
                     "launches on the legacy default stream, toolkit CUB radix sort, stage order of "
                     "ParticleSolver::update with the constraint and wind blocks enabled"}
@@ -432,41 +646,27 @@ def run_ours(args):
         torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
     e2e_value = total_units / float(e2e_t.item())
 
-    # per-kernel device time of real updates (CUDA events on the solver's stream)
-    prof_steps = 3
-    agg: dict[str, list] = {}
-    for _ in range(prof_steps):
-        flush.fill_(7)
-        torch.cuda.synchronize()
-        for name, (cnt, tot) in solver.profile(SUBSTEPS, DT, ITERATIONS).items():
-            a = agg.setdefault(name, [0, 0.0])
-            a[0] += cnt
-            a[1] += tot
-    top = max(agg.items(), key=lambda kv: kv[1][1])
-    top_name, (top_launches, top_ms) = top
-    avg_ms = top_ms / top_launches
-    peak, peak_kind = load_peaks()
-    bytes_per = KERNEL_BYTES.get(top_name)
-    achieved = (bytes_per * n / (avg_ms / 1e3) / 1e9) if bytes_per else None
-    traffic = traffic_for(top_name, n, args.workload)
-    step_ms_total = sum(v[1] for v in agg.values()) / prof_steps
+    roofline, stages, step_ms_total = kernel_roofline(torch, solver, n, args.workload, flush, value)
     walks = solver.walk_stats(SUBSTEPS, DT, ITERATIONS)
     device_errors = solver.device_errors()  # non-finite state anywhere in the run
     solver.close()
     reference_cuda = None
     if rank == 0 and args.workload != "batch" and not args.no_reference_cuda:
         ref_scene = build_scene(bp.scenes, args.workload, seed=0)
-        reference_cuda = run_reference_cuda(torch, ref_scene, workload_params(bp, args.workload, ref_scene),
+        reference_cuda = run_reference_cuda(bp, torch, ref_scene, workload_params(bp, args.workload, ref_scene),
                                             args.steps, args.warmup, flush)
         if reference_cuda is not None:
             reference_cuda["ours_over_reference"] = value / reference_cuda["value"]
+    samples = None
+    if rank == 0 and args.workload == "mixed" and not args.no_samples:
+        samples = run_samples(bp, torch, stream, flush, local, args)
     batched = None
     if args.workload == "batch" or (args.workload == "mixed" and not args.no_batch):
-        # the ensemble against a loop of one solver per scene (bounded: 3 timed steps)
-        batched = run_batch(bp, torch, stream, flush, steps=min(args.steps, 3), warmup=3, seed=rank)
+        # the ensemble against a loop of one solver per scene, 10 timed frames each
+        batched = run_batch(bp, torch, stream, flush, steps=10, warmup=3, seed=rank)
     adjoint = None
     if args.workload == "mixed" and not args.no_adjoint:
-        adjoint = run_adjoint(bp, torch, stream)
+        adjoint = run_adjoint(bp, torch, stream, check_gradients=rank == 0 and not args.no_gradient_check)
 
     result = None
     if rank == 0:
@@ -490,13 +690,8 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "particle-substeps/s",
                     "h2d_bytes_per_step": int(2 * n * 12), "d2h_bytes_per_step": int(2 * n * 12)},
             "gpu_launches": int(launches_per_step * args.steps),
-            "roofline": {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                         "bytes_per_particle": bytes_per, "avg_launch_ms": avg_ms,
-                         "issue": issue_for(top_name, args.workload)},
-            "stages_ms_per_step": {k: round(v[1] / prof_steps, 4) for k, v in
-                                   sorted(agg.items(), key=lambda kv: -kv[1][1])},
+            "roofline": roofline,
+            "stages_ms_per_step": stages,
             "profiled_ms_per_step": step_ms_total,
             "neighbor_walks": walks,
             "device_errors": device_errors,
@@ -505,6 +700,8 @@ def run_ours(args):
         }
         if reference_cuda is not None:
             result["reference_cuda"] = reference_cuda
+        if samples is not None:
+            result["workloads"] = samples
         if batched is not None:
             result["batched"] = batched
         if adjoint is not None:
@@ -636,6 +833,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-reference-cuda", action="store_true", help="skip timing the reference's CUDA step")
+    ap.add_argument("--no-samples", action="store_true", help="skip the other configurations and regimes")
+    ap.add_argument("--no-gradient-check", action="store_true",
+                    help="skip the FP64 finite-difference check of the adjoint's gradients")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint measurement")
     ap.add_argument("--save-state", default=None, help="after the timed steps, save the state (npz) here")
     ap.add_argument("--load-state", default=None, help="start from a state saved by --save-state")

@@ -367,24 +367,33 @@ __device__ __forceinline__ float3 clamp_fwd(const SimConsts &C, float3 u)
 }
 
 // The pairs of particle k that pass test, in walk order: term(j, P[j]).
-// With C.nbr the walk only records them and the terms are summed over the
-// list (four gathers at a time); without it, or past the list's capacity,
-// the terms run inside the walk.
-template <class T, class B>
+// With C.nbr the walk records the pairs that pass `record` (a superset of
+// test's) and the terms of those that pass test are summed over the list
+// (four gathers at a time); the list's count goes to C.nbr_count[k] (-1:
+// overflow), so that a later pass over the same positions can read it.
+// Without lists, or past the list's capacity, the terms run inside the walk.
+template <class R, class T, class B>
 __device__ __forceinline__ void record_then_sum(const SimConsts &C, int k, float3 pk, const float4 *__restrict__ P,
-                                                const GridView &v, const StageShared *S, int g, T &test, B &term)
+                                                const GridView &v, const StageShared *S, int g, R &record, T &test,
+                                                B &term)
 {
     int cnt = -1;
     if (C.nbr) {
         ListWriter list(C.nbr, C.nbr_cap, C.n, k);
-        walk_neighbors<true>(k, pk, 0, P, v, C, S, g, test, [&](int j, float4) { list.push(j); });
+        walk_neighbors<true>(k, pk, 0, P, v, C, S, g, record, [&](int j, float4) { list.push(j); });
         cnt = list.finish();
-        if (cnt >= 0) for_each_in_list<false>(C.nbr, C.n, k, cnt, P, term);
+        if (C.nbr_count) C.nbr_count[k] = cnt;
+        if (cnt >= 0)
+            for_each_in_list<false>(C.nbr, C.n, k, cnt, P, [&](int j, float4 pj) {
+                if (test(j, pj)) term(j, pj);
+            });
     }
     if (cnt < 0) walk_neighbors<true>(k, pk, 0, P, v, C, S, g, test, term);
 }
 
-// Walk A: lambda-bar and the position gradient of the correction terms.
+// Walk A: lambda-bar and the position gradient of the correction terms.  It
+// records every j != k within h (the pairs of the density terms, a superset
+// of its own), so that pass B sums over the same list instead of walking.
 __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const float4 *__restrict__ P,
                                                              const float *__restrict__ mass,
                                                              const float *__restrict__ lam, const int *__restrict__ off,
@@ -436,12 +445,18 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const 
             lb += sb1 + sb2;
             pb = add3(pb, sub3(rb1, rb2));
     };
-    record_then_sum(C, k, pk, P, grid_view(C, sc, off), &S, g, test, term);
+    auto within = [&](int j, float4 pj4) {
+        const float3 r = sub3(pk, f3(pj4));
+        return j != k && dotf(r, r) <= C.h2;
+    };
+    record_then_sum(C, k, pk, P, grid_view(C, sc, off), &S, g, within, test, term);
     gLam[k] = lb;
     gPart[k] = f4(pb);
 }
 
-// Walk B: the density gradient; gP (in) = gOut + gPart + density terms.
+// Pass B: the density gradient; gP (in) = gOut + gPart + density terms.  It
+// sums over the list pass A recorded at the same positions (every j != k
+// within h, in walk order) and walks only where that list overflowed.
 __global__ void __launch_bounds__(kWalkThreads) k_adj_lambda(SimConsts C, const float4 *__restrict__ P,
                                                              const float *__restrict__ mass,
                                                              const float *__restrict__ rho, const int *__restrict__ off,
@@ -474,7 +489,9 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_lambda(SimConsts C, const 
         if (j > k) pb = add3(pb, mul3(gw, rbk * mass[j] * (phj < 0 ? 1.f : C.solid_scale)));
         else pb = add3(pb, mul3(gw, rho_bar(j, phj) * mk));
     };
-    record_then_sum(C, k, pk, P, grid_view(C, sc, off), &S, g, test, term);
+    const int cnt = (C.nbr && C.nbr_count) ? __ldg(C.nbr_count + k) : -1;
+    if (cnt >= 0) for_each_in_list(C.nbr, C.n, k, cnt, P, term);  // pass A's list: exactly test's pairs
+    else walk_neighbors<true>(k, pk, 0, P, grid_view(C, sc, off), C, &S, g, test, term);
     gIn[k] = f4(add3(add3(ld3(gOut, k), ld3(gPart, k)), pb));
 }
 
@@ -512,7 +529,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_xsph(SimConsts C, const fl
         const float3 dv = sub3(ld3(V, j), vi);
         gp = add3(gp, mul3(poly6_grad(C, r, d2), C.xsph_c * dotf(dv, sub3(go, gj))));
     };
-    record_then_sum(C, i, pi, P, grid_view(C, scene_index(C, i), off), &S, g, test, term);
+    record_then_sum(C, i, pi, P, grid_view(C, scene_index(C, i), off), &S, g, test, test, term);
     gVin[i] = f4(gv);
     gX[i] = f4(add3(ld3(gX, i), gp));
 }

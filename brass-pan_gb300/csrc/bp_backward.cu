@@ -289,7 +289,7 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
     C.cls_post = 0;
     if (!(u.prm.walk_options & BP_WALK_NO_LISTS)) {
         C.nbr = s->nbr;
-        C.nbr_count = nullptr;  // the lists live only inside one launch
+        C.nbr_count = s->nbr_count;  // the fluid adjoint's pass A leaves its lists for pass B
         C.nbr_cap = kPostListCap;
     }
     const bp_params &p = u.prm;

@@ -102,6 +102,11 @@ class ParticleSolver:
             self.handle, None if x is None else x.ctypes.data_as(C.POINTER(C.c_float)),
             None if v is None else v.ctypes.data_as(C.POINTER(C.c_float)), order))
 
+    def set_params(self, params: abi.BpParams):
+        """bp_solver_set_params: new parameters from the next update on."""
+        abi.check(self.lib, self.lib.bp_solver_set_params(self.handle, C.byref(params)))
+        self.params = params
+
     def snapshot(self) -> bytes:
         """Checkpoint: the whole state as bytes (bp_solver_snapshot_save)."""
         size = C.c_size_t()

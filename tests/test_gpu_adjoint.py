@@ -274,3 +274,136 @@ def test_backward_rejects_stages_without_adjoint(bp, gpu):
         u.backward(np.ones((cloth.num_particles, 3), np.float32))  # dihedral bending has no adjoint
     u.close()
     assert abi.BP_STAGE_VORTICITY
+
+
+# ---- against central finite differences of the FP64 host oracle -------------
+#
+# The configuration's check: gradients of the GPU adjoint (fp32 forward and
+# adjoint) against central differences with step 1e-3 of the FP64 oracle's
+# forward (the same step in double; state, wind and stiffness perturbed in
+# double), within 1e-3 relative.  A reduced differentiable-rollout
+# configuration: a 16 x 16 flag pinned along one edge under wind (4, 0, 0)
+# m/s for 20 frames of 2 substeps x 4 iterations, loss = mean squared
+# distance of the final positions to a seeded target pose, checkpoints every
+# 10 substeps; and an 8^3 PBF block (reference mode, planes, XSPH) for 5
+# frames, loss = its final centre of mass.
+#
+# The flag's loss is curved enough that the step-1e-3 central difference
+# itself is off by 2-3e-4 relative at 20-30 frames (measured against step
+# 1e-4), so the differences are Richardson-extrapolated from steps 1e-3 and
+# 5e-4 ((4 D(h/2) - D(h)) / 3, error O(h^4)).  The adjoint linearises the
+# fp32 trajectory, the differences the FP64 one; measured on the flag, the
+# initial-velocity direction agrees to 1.5e-5 at 5 frames, 3e-4 at 10-20 and
+# 1.04e-3 at 30 frames (wind and stiffness: 1e-4 to 2e-4 throughout).
+
+FD64_STEP = 1e-3
+FD64_REL = 1e-3
+
+
+def central64(L, plus, minus, h=FD64_STEP):
+    """Richardson-extrapolated central difference: plus(s) / minus(s) give
+    the perturbed arguments of L at step s."""
+    d = [(L(**plus(s)) - L(**minus(s))) / (2 * s) for s in (h, h / 2)]
+    return (4 * d[1] - d[0]) / 3
+
+
+def rollout64(oracle, scene, params, updates, x0=None, v0=None, wind=None, dparams=None, iterations=4):
+    """Final (positions, velocities) of the FP64 oracle, float64, original order."""
+    import os
+
+    o = oracle.OracleSolver(scene, params, threads=os.cpu_count() or 4, precision=64)
+    if x0 is not None or v0 is not None:  # a new solver's arrangement is the original order
+        o.set_state(x0, v0)
+    if wind is not None:
+        o.set_wind(wind)
+    if dparams is not None:
+        o.set_distance_params(dparams)
+    for _ in range(updates):
+        o.update(2, DT, iterations)
+    return o.positions(), o.velocities()
+
+
+def flag64_case(bp):
+    abi = bp.abi
+    scene = bp.scenes.flag_scene(n=16, seed=4)
+    stages = abi.BP_STAGE_PLANES | abi.BP_STAGE_WIND | abi.BP_STAGE_DISTANCE | abi.BP_STAGE_IMMOVABLE
+    params = bp.make_params(scene, mode=abi.BP_MODE_TEXTBOOK, stage_mask=stages, wind_velocity=(4.0, 0.0, 0.0),
+                            wind_drag=1.0, wind_lift=0.3, mass_scaling_k=0.0)
+    rng = np.random.default_rng(40)
+    target = scene.positions.astype(np.float64) + rng.normal(0.0, 0.05, (scene.num_particles, 3))
+    return scene, params, target
+
+
+def test_flag_gradients_match_fp64_finite_differences(bp, gpu, oracle):
+    scene, params, target = flag64_case(bp)
+    n, frames = scene.num_particles, 20
+    s = bp.ParticleSolver(scene, params)
+    s.tape_begin(10)
+    for _ in range(frames):
+        s.update(2, DT, 4)
+    x = s.positions().astype(np.float64)
+    g = s.backward(((2.0 / n) * (x - target)).astype(np.float32))
+    s.close()
+
+    def L(**kw):
+        xf, _ = rollout64(oracle, scene, params, frames, **kw)
+        return float(np.sum((xf - target) ** 2) / n)
+
+    x0 = scene.positions.astype(np.float64)
+    v0 = np.zeros((n, 3)) if scene.velocities is None else scene.velocities.astype(np.float64)
+    wind = np.array(params.wind_velocity[:], np.float64)
+    dp = scene.distance_params.astype(np.float64)
+    rng = np.random.default_rng(42)
+    pairs = []
+    for k in range(3):
+        e = np.zeros(3)
+        e[k] = 1.0
+        pairs.append((f"wind[{k}]", central64(L, lambda s: {"wind": wind + s * e}, lambda s: {"wind": wind - s * e}),
+                      float(g["wind_velocity"][k])))
+    d = rng.standard_normal(len(dp))
+    d /= np.linalg.norm(d)
+    ds = np.zeros_like(dp)
+    ds[:, 1] = d
+    pairs.append(("stiffness", central64(L, lambda s: {"dparams": dp + s * ds}, lambda s: {"dparams": dp - s * ds}),
+                  float(g["distance_stiffness"].astype(np.float64) @ d)))
+    d = rng.standard_normal((n, 3))
+    d /= np.linalg.norm(d)
+    pairs.append(("velocities", central64(L, lambda s: {"x0": x0, "v0": v0 + s * d},
+                                          lambda s: {"x0": x0, "v0": v0 - s * d}),
+                  float(np.sum(g["velocities"].astype(np.float64) * d))))
+    report = "; ".join(f"{w} fd64 {fd:.6e} adjoint {ad:.6e}" for w, fd, ad in pairs)
+    print(report)
+    floor = 1e-2 * max(abs(a) for _, _, a in pairs)
+    bad = [w for w, fd, ad in pairs if abs(fd - ad) > FD64_REL * max(abs(fd), abs(ad), floor)]
+    assert not bad, report
+
+
+def test_pbf_block_gradient_matches_fp64_finite_differences(bp, gpu, oracle):
+    abi = bp.abi
+    scene = bp.scenes.pbf_scene(8, 8, 8, spacing=0.1, seed=4, box=(1.6, 2.0, 1.6), grid_dim=16)
+    params = bp.make_params(scene, stage_mask=abi.BP_STAGE_FLUID | abi.BP_STAGE_PLANES | abi.BP_STAGE_XSPH)
+    n, frames = scene.num_particles, 5
+    s = bp.ParticleSolver(scene, params)
+    s.tape_begin(10)
+    for _ in range(frames):
+        s.update(2, DT, 4)
+    gx = np.full((n, 3), 1.0 / n, np.float32)  # loss: sum of the centre of mass's coordinates
+    g = s.backward(gx)
+    s.close()
+
+    def L(v0):
+        xf, _ = rollout64(oracle, scene, params, frames, x0=scene.positions.astype(np.float64), v0=v0)
+        return float(xf.sum() / n)
+
+    v0 = np.zeros((n, 3)) if scene.velocities is None else scene.velocities.astype(np.float64)
+    rng = np.random.default_rng(43)
+    pairs = []
+    for trial in range(2):
+        d = rng.standard_normal((n, 3))
+        d /= np.linalg.norm(d)
+        pairs.append((f"velocities#{trial}", central64(L, lambda s: {"v0": v0 + s * d}, lambda s: {"v0": v0 - s * d}),
+                      float(np.sum(g["velocities"].astype(np.float64) * d))))
+    report = "; ".join(f"{w} fd64 {fd:.6e} adjoint {ad:.6e}" for w, fd, ad in pairs)
+    print(report)
+    bad = [w for w, fd, ad in pairs if abs(fd - ad) > FD64_REL * max(abs(fd), abs(ad))]
+    assert not bad, report

@@ -1,0 +1,323 @@
+"""Parity at the benchmark configurations' own sizes and regimes.
+
+* The 32,768-particle dam break (32^3 lattice, d = 0.1, h = 2d, 64^3 table)
+  with the textbook parameters of its configuration (relaxation 600,
+  s_corr n = 4 at 0.2 h, XSPH c = 0.01), in lockstep with the fp32 oracle and
+  with the FP64 host oracle, and free-running for 100 frames with its
+  density-error statistics (mean, 99th percentile and maximum of
+  |rho/rho0 - 1| over the fluid, averaged over frames 50-99) compared with
+  the FP64 oracle's and the fp32 oracle's.
+* The 1,146,880-particle mixed scene of the benchmark, 2 substeps in lockstep
+  from its initial state, and 2 substeps from its late-frame state (200
+  frames in: compressed fluid, aliased table, alias-class walks).
+* The textbook wind (a wind vector, lift 0.3, drag 1.0) on a pinned flag,
+  the mixed configuration's textbook parameters, and granular material
+  (single-particle solids) poured onto fluid.
+
+Lockstep: the oracle adopts the GPU state (arrangement included) before
+every substep; then max |x_gpu - x_oracle| <= 1e-4 h, |v| error <= 1e-4 h/dt,
+and, against the fp32 oracle, identical sorted cell ids and sorted order.
+The FP64 oracle hashes the float-rounded position as the reference does, but
+its positions differ from the GPU's in the last bits, so a particle within
+rounding of a cell boundary may sort differently there; against it only the
+state is compared."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+from test_gpu_solver import DT, assert_parity, gpu_state
+
+pytestmark = pytest.mark.gpu
+
+THREADS = os.cpu_count() or 4
+
+
+def config0_params(bp, scene, scorr_k=0.001):
+    """The 32k dam break's textbook parameters.  s_corr k = 0.001: at the
+    configuration's k = 0.1 (with m = 1 kg, rho0 = 1000 kg/m^3) the first
+    substep from the lattice already throws particles out at up to 122 m/s
+    and the second turns the oracle's state non-finite, so k = 0.1 is checked
+    on that first substep only."""
+    return bp.make_params(scene, mode=bp.abi.BP_MODE_TEXTBOOK, relaxation=600.0, scorr_k=scorr_k, scorr_n=4,
+                          scorr_dq=0.2, xsph_c=0.01)
+
+
+def lockstep_from(bp, oracle, g, scene, params, substeps, iterations=4, precision=32, compare_grid=True):
+    """Lockstep from solver g's current state; returns per-substep errors."""
+    o = oracle.OracleSolver(scene, params, threads=THREADS, precision=precision)
+    sdt = DT / 2
+    errs = []
+    for _ in range(substeps):
+        x, v, to_orig, rot = gpu_state(bp, g)
+        o.adopt(x, v, to_orig, rot)
+        g.update(1, sdt, iterations)
+        o.update(1, sdt, iterations)
+        ex = float(np.abs(g.positions() - o.positions()).max())
+        ev = float(np.abs(g.velocities() - o.velocities()).max())
+        if compare_grid:
+            keys = np.array_equal(g.field(bp.abi.BP_FIELD_SORTED_CELL_IDS), o.get(oracle.F_SORTED_CELL))
+            order = np.array_equal(g.field(bp.abi.BP_FIELD_MAP_TO_ORIGINAL), o.get(oracle.F_TO_ORIG))
+        else:
+            keys = order = True
+        errs.append((ex, ev, keys, order))
+    return errs, scene.kernel_radius, sdt
+
+
+@pytest.mark.parametrize("mode", ["textbook", "textbook_scorr_k0.1", "reference"])
+def test_dam_break_32k_lockstep(bp, gpu, oracle, mode):
+    scene = bp.scenes.dam_break_32k(seed=0)
+    assert scene.num_particles == 32768
+    if mode == "reference":
+        params = bp.make_params(scene)
+    else:
+        params = config0_params(bp, scene, scorr_k=0.1 if mode.endswith("k0.1") else 0.001)
+    g = bp.ParticleSolver(scene, params)
+    try:
+        if mode.endswith("k0.1"):
+            # First substep from the lattice (see config0_params).  It moves
+            # particles by up to 1 m, with s_corr terms far above the lambdas,
+            # so fp32 rounding alone exceeds 1e-4 h: the GPU must then be as
+            # close to the FP64 oracle as the reference's fp32 arithmetic
+            # (the fp32 oracle) is, or within 1e-4 h.
+            x, v, to_orig, rot = gpu_state(bp, g)
+            o32 = oracle.OracleSolver(scene, params, threads=THREADS)
+            o64 = oracle.OracleSolver(scene, params, threads=THREADS, precision=64)
+            for o in (o32, o64):
+                o.adopt(x, v, to_orig, rot)
+                o.update(1, DT / 2, 4)
+            g.update(1, DT / 2, 4)
+            xg, x32, x64 = g.positions(), o32.positions(), o64.positions()
+            assert np.isfinite(xg).all()
+            assert np.array_equal(g.field(bp.abi.BP_FIELD_MAP_TO_ORIGINAL), o32.get(oracle.F_TO_ORIG))
+            e_gpu = float(np.abs(xg - x64).max())
+            e_fp32 = float(np.abs(x32 - x64).max())
+            assert e_gpu <= max(1e-4 * scene.kernel_radius, 2.0 * e_fp32), (e_gpu, e_fp32)
+        else:
+            g.update(2, DT, 4)  # leave the lattice: the fluid is moving when the lockstep starts
+            assert_parity(*lockstep_from(bp, oracle, g, scene, params, substeps=4))
+    finally:
+        g.close()
+
+
+def test_dam_break_32k_lockstep_fp64(bp, gpu, oracle):
+    """Per substep, the GPU state stays within 1e-4 h of the FP64 host
+    oracle's from the same inputs (fp32 rounding is all that separates them)."""
+    scene = bp.scenes.dam_break_32k(seed=0)
+    params = config0_params(bp, scene)
+    g = bp.ParticleSolver(scene, params)
+    try:
+        for _ in range(10):
+            g.update(2, DT, 4)
+        errs, h, sdt = lockstep_from(bp, oracle, g, scene, params, substeps=4, precision=64, compare_grid=False)
+    finally:
+        g.close()
+    assert_parity(errs, h, sdt)
+
+
+def density_error_stats(rho, rho0, phase_fluid):
+    c = np.abs(rho[phase_fluid] / rho0 - 1.0)
+    return np.array([c.mean(), np.percentile(c, 99), c.max()])
+
+
+def test_dam_break_32k_density_statistics_100_frames(bp, gpu, oracle):
+    """Free-running 100 frames (200 substeps) of the 32k dam break: the
+    density-error statistics of the GPU run agree with the FP64 oracle's and
+    the fp32 oracle's (trajectories decorrelate; the statistics must not).
+    Measured between the fp32 and FP64 oracles: 0.3 % (mean), 1.3 % (99th
+    percentile), 1e-7 (maximum: an isolated splash particle's self density)."""
+    scene = bp.scenes.dam_break_32k(seed=0)
+    params = config0_params(bp, scene)
+    rho0 = params.rest_density
+    fluid = scene.phases < 0
+    g = bp.ParticleSolver(scene, params)
+    o32 = oracle.OracleSolver(scene, params, threads=THREADS)
+    o64 = oracle.OracleSolver(scene, params, threads=THREADS, precision=64)
+    stats = {"gpu": [], "fp32": [], "fp64": []}
+    try:
+        for f in range(100):
+            g.update(2, DT, 4)
+            o32.update(2, DT, 4)
+            o64.update(2, DT, 4)
+            if f >= 50:
+                to_orig = g.field(bp.abi.BP_FIELD_MAP_TO_ORIGINAL)
+                stats["gpu"].append(density_error_stats(g.field(bp.abi.BP_FIELD_DENSITIES), rho0, fluid[to_orig]))
+                for name, o in (("fp32", o32), ("fp64", o64)):
+                    stats[name].append(density_error_stats(o.get(oracle.F_DENSITY), rho0,
+                                                           fluid[o.get(oracle.F_TO_ORIG)]))
+        assert np.isfinite(g.positions()).all() and g.device_errors() == 0
+    finally:
+        g.close()
+    mean = {k: np.mean(v, axis=0) for k, v in stats.items()}
+    print({k: [round(float(x), 5) for x in v] for k, v in mean.items()})
+    for ref in ("fp64", "fp32"):
+        rel = np.abs(mean["gpu"] - mean[ref]) / mean[ref]
+        assert rel[0] < 0.03, f"mean |C| vs {ref}: {mean['gpu'][0]:.4f} / {mean[ref][0]:.4f}"
+        assert rel[1] < 0.06, f"p99 |C| vs {ref}: {mean['gpu'][1]:.4f} / {mean[ref][1]:.4f}"
+        assert rel[2] < 0.10, f"max |C| vs {ref}: {mean['gpu'][2]:.4f} / {mean[ref][2]:.4f}"
+
+
+def mixed_params(bp, scene):
+    """The benchmark's parameters for the mixed scene: the reference's literals
+    without mass scaling."""
+    return bp.make_params(scene, mass_scaling_k=0.0)
+
+
+def lockstep_fp64_anchored(bp, oracle, g, scene, params, substeps, iterations=4):
+    """Lockstep of the GPU, the fp32 oracle and the FP64 oracle from the GPU's
+    state.  Per substep: identical sorted cell ids and order (GPU and fp32
+    oracle), and the state at least as close to the FP64 oracle as the fp32
+    oracle is (or within 1e-4 h of it).
+
+    Why the anchor: shape matching of a 512-particle cube sums 512 positions
+    of about 20 m into its centre of mass.  The fp32 oracle sums them in
+    particle order (the reference's host build does, for its 64-particle
+    bodies) and is off the FP64 sum by up to 2e-4 m; the GPU's tree
+    reduction is closer to FP64 (8e-5 m measured on the late state).  Fluid
+    touching the cubes inherits the difference through the solid density
+    and the contacts.  Returns the per-substep errors."""
+    h = scene.kernel_radius
+    sdt = DT / 2
+    o32 = oracle.OracleSolver(scene, params, threads=THREADS)
+    o64 = oracle.OracleSolver(scene, params, threads=THREADS, precision=64)
+    out = []
+    for k in range(substeps):
+        x, v, to_orig, rot = gpu_state(bp, g)
+        for o in (o32, o64):
+            o.adopt(x, v, to_orig, rot)
+            o.update(1, sdt, iterations)
+        g.update(1, sdt, iterations)
+        xg, x32, x64 = g.positions(), o32.positions(), o64.positions()
+        assert np.array_equal(g.field(bp.abi.BP_FIELD_SORTED_CELL_IDS), o32.get(oracle.F_SORTED_CELL)), k
+        assert np.array_equal(g.field(bp.abi.BP_FIELD_MAP_TO_ORIGINAL), o32.get(oracle.F_TO_ORIG)), k
+        e_gpu = float(np.abs(xg - x64).max())
+        e_fp32 = float(np.abs(x32 - x64).max())
+        assert np.isfinite(xg).all()
+        assert e_gpu <= max(1e-4 * h, e_fp32), f"substep {k}: GPU vs FP64 {e_gpu:.3e}, fp32 oracle vs FP64 {e_fp32:.3e}"
+        out.append((e_gpu, e_fp32, float(np.abs(xg - x32).max())))
+    return out
+
+
+def test_mixed_1m_lockstep_initial(bp, gpu, oracle):
+    """The benchmark's mixed scene at full size (1,146,880 particles: 1M PBF
+    fluid, a 256^2 cloth under wind, 64 rigid 8^3 cubes), 2 substeps.  The
+    fluid and the cloth (nowhere near the cubes yet) match the fp32 oracle
+    to 1e-4 h."""
+    scene = bp.scenes.mixed_phase_1m(seed=0)
+    assert scene.num_particles == 1146880
+    params = mixed_params(bp, scene)
+    g = bp.ParticleSolver(scene, params)
+    rigid = np.zeros(scene.num_particles, bool)
+    for r0, r1 in scene.rigid_ranges:
+        rigid[r0:r1] = True
+    o = oracle.OracleSolver(scene, params, threads=THREADS)
+    try:
+        x, v, to_orig, rot = gpu_state(bp, g)
+        o.adopt(x, v, to_orig, rot)
+        o.update(1, DT / 2, 4)
+        g.update(1, DT / 2, 4)
+        err = np.abs(g.positions() - o.positions()).max(axis=1)
+        assert err[~rigid].max() <= 1e-4 * scene.kernel_radius, err[~rigid].max()
+        lockstep_fp64_anchored(bp, oracle, g, scene, params, substeps=2)
+    finally:
+        g.close()
+
+
+def test_mixed_1m_lockstep_late_frames(bp, gpu, oracle):
+    """2 substeps from the mixed scene's state after 200 frames: the fluid is
+    compressed, the dam break has spread into cells the 64^3 table aliases,
+    and the walks run over alias classes and recorded lists."""
+    scene = bp.scenes.mixed_phase_1m(seed=0)
+    params = mixed_params(bp, scene)
+    g = bp.ParticleSolver(scene, params)
+    try:
+        for _ in range(200):
+            g.update(2, DT, 4)
+        walks = g.walk_stats(2, DT, 4)  # a real update: frame 201
+        assert walks["alias_classes"] > 0, walks
+        assert np.isfinite(g.positions()).all() and g.device_errors() == 0
+        lockstep_fp64_anchored(bp, oracle, g, scene, params, substeps=2)
+    finally:
+        g.close()
+
+
+def test_mixed_1m_late_fluid_lockstep(bp, gpu, oracle):
+    """The late state's fluid walks alone (planes and fluid: alias classes,
+    recorded lists, compressed cells): within 1e-4 h of the fp32 oracle, grid
+    identical.  (Contacts between solids are left to the FP64-anchored test
+    above: their friction branches make rounding differences jump.)"""
+    scene = bp.scenes.mixed_phase_1m(seed=0)
+    g = bp.ParticleSolver(scene, mixed_params(bp, scene))
+    try:
+        for _ in range(200):
+            g.update(2, DT, 4)
+        a = bp.abi
+        params = bp.make_params(scene, mass_scaling_k=0.0, stage_mask=a.BP_STAGE_PLANES | a.BP_STAGE_FLUID)
+        g.set_params(params)
+        assert_parity(*lockstep_from(bp, oracle, g, scene, params, substeps=2))
+    finally:
+        g.close()
+
+
+def test_textbook_wind_lockstep(bp, gpu, oracle):
+    """Textbook wind: drag and lift against the velocity relative to a wind
+    vector, C_L = 0.3 and C_D = 1.0 (the mixed configuration's (3, 0, 1) m/s),
+    on a flag pinned along one edge."""
+    abi = bp.abi
+    scene = bp.scenes.flag_scene(n=32, seed=3)
+    stages = abi.BP_STAGE_PLANES | abi.BP_STAGE_WIND | abi.BP_STAGE_DISTANCE | abi.BP_STAGE_IMMOVABLE
+    params = bp.make_params(scene, mode=abi.BP_MODE_TEXTBOOK, stage_mask=stages, wind_velocity=(3.0, 0.0, 1.0),
+                            wind_drag=1.0, wind_lift=0.3, mass_scaling_k=0.0)
+    g = bp.ParticleSolver(scene, params)
+    try:
+        for _ in range(5):
+            g.update(2, DT, 4)
+        assert_parity(*lockstep_from(bp, oracle, g, scene, params, substeps=4))
+    finally:
+        g.close()
+
+
+def test_textbook_mixed_lockstep(bp, gpu, oracle):
+    """The textbook parameters of the mixed configuration on the small mixed
+    scene: textbook fluid (relaxation 600, s_corr), wind (3, 0, 1) m/s with
+    lift 0.3 and drag 1.0, Akinci tension, shape matching, contacts."""
+    from conftest import small_mixed_scene
+
+    scene = small_mixed_scene(bp, seed=21)
+    params = bp.make_params(scene, mode=bp.abi.BP_MODE_TEXTBOOK, relaxation=600.0, scorr_k=0.001, scorr_dq=0.2,
+                            xsph_c=0.01, wind_velocity=(3.0, 0.0, 1.0), wind_drag=1.0, wind_lift=0.3)
+    g = bp.ParticleSolver(scene, params)
+    try:
+        assert_parity(*lockstep_from(bp, oracle, g, scene, params, substeps=6))
+    finally:
+        g.close()
+
+
+def granular_scene(bp, seed=0):
+    """Granular material (single-particle solids, each its own phase:
+    scene.cpp:130-146) poured onto a fluid pool."""
+    sc = bp.scenes
+    rng = np.random.default_rng(seed)
+    s = sc.Scene(name="granular")
+    s.particle_radius, s.kernel_radius, s.cell_size, s.grid_dim, s.rest_density = 0.05, 0.2, 0.2, 32, 1000.0
+    sc.box_planes(s, (0, 0, 0), (2.0, 4.0, 2.0))
+    s.add_fluid_block((12, 6, 12), (0.1, 0.1, 0.1), (0.1, 0.1, 0.1), 1.0, jitter=0.001, rng=rng)
+    s.add_granulars_block((6, 6, 6), (0.5, 1.0, 0.5), (0.1, 0.1, 0.1), 1.0)
+    s.velocities = rng.uniform(-0.3, 0.3, (s.num_particles, 3)).astype(np.float32)
+    return s
+
+
+def test_granular_lockstep(bp, gpu, oracle):
+    scene = granular_scene(bp, seed=4)
+    ph = scene.phases
+    assert (ph > 0).sum() == 216 and len(np.unique(ph[ph > 0])) == 216, "each grain is its own solid phase"
+    params = bp.make_params(scene)
+    g = bp.ParticleSolver(scene, params)
+    try:
+        for _ in range(10):  # the grains reach the pool
+            g.update(2, DT, 4)
+        assert_parity(*lockstep_from(bp, oracle, g, scene, params, substeps=6))
+    finally:
+        g.close()
