@@ -153,34 +153,40 @@ def run_adjoint(bp, torch, stream, frames=120, every=10, check_gradients=True):
                      "forward_ms": fwd * 1e3, "forward_adjoint_ms": both * 1e3, "ratio": both / fwd,
                      "grad_finite": bool(np.isfinite(g["velocities"]).all())}
         if check_gradients:
-            if name.startswith("cloth"):
-                out[name]["gradient_check"] = fd64_check(bp, scene, params, g, frames, target=target)
-            else:  # the FP64 oracle's fluid rollouts take a quarter second per frame: a 10-frame horizon
-                out[name]["gradient_check"] = fd64_check(bp, scene, params, None, 10, solver_args=(stream, every))
+            # horizons: a short one, where the rollout's derivative is what a
+            # finite difference measures, and the configuration's own (cloth)
+            # or as long as the FP64 fluid rollouts allow (a quarter second
+            # per frame at this size)
+            horizons = (20, frames) if name.startswith("cloth") else (2, 10)
+            out[name]["gradient_check"] = {
+                f"frames_{f}": fd64_check(bp, stream, every, scene, params, f,
+                                          target=target if name.startswith("cloth") else None)
+                for f in horizons}
     return out
 
 
-def fd64_check(bp, scene, params, grads, frames, target=None, solver_args=None, h=1e-3):
-    """Directional derivatives of the GPU adjoint against central differences
-    (step h) of the FP64 host oracle's forward, along the wind's three axes,
-    one random direction in the per-edge stiffness and one in the initial
-    velocities (cloth; loss: mean squared distance to `target`), or one
-    random initial-velocity direction (fluid; loss: sum of the centre of
-    mass's coordinates, gradients from a `frames`-update tape recorded here).
-    Each difference is taken at steps h and h/2 and Richardson-extrapolated;
-    the plain step-h difference is reported beside it."""
+def fd64_check(bp, stream, every, scene, params, frames, target=None, h=1e-3):
+    """Directional derivatives of the GPU adjoint over a `frames`-update tape
+    against central differences (step h) of the FP64 host oracle's forward,
+    along the wind's three axes, one random direction in the per-edge
+    stiffness and one in the initial velocities (cloth; loss: mean squared
+    distance to `target`), or one random initial-velocity direction (fluid;
+    loss: sum of the centre of mass's coordinates).  Each difference is taken
+    at steps h and h/2 and Richardson-extrapolated; the plain step-h
+    difference is reported beside it."""
     import oracle
 
     n = scene.num_particles
     threads = os.cpu_count() or 4
-    if grads is None:  # fluid: record a tape over `frames` updates
-        stream, every = solver_args
-        s = bp.ParticleSolver(scene, params, stream=stream.cuda_stream)
-        s.tape_begin(every)
-        for _ in range(frames):
-            s.update(SUBSTEPS, DT, ITERATIONS)
+    s = bp.ParticleSolver(scene, params, stream=stream.cuda_stream)
+    s.tape_begin(every)
+    for _ in range(frames):
+        s.update(SUBSTEPS, DT, ITERATIONS)
+    if target is not None:
+        grads = s.backward(((2.0 / n) * (s.positions().astype(np.float64) - target)).astype(np.float32))
+    else:
         grads = s.backward(np.full((n, 3), 1.0 / n, np.float32))
-        s.close()
+    s.close()
 
     def loss(**kw):
         o = oracle.OracleSolver(scene, params, threads=threads, precision=64)
