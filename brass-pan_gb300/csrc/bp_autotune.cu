@@ -3,9 +3,8 @@
 //
 // The walk variants (staging each CTA's neighbourhood in shared memory,
 // testing candidates in chunks before the pair terms, the post passes'
-// neighbour lists) give bit-identical results, and height slabs the same
-// pairs summed in another order, so the choice only affects speed (and, for
-// the slabs, fp32 rounding).  Each candidate runs one update from the same state (the first call
+// neighbour lists) give bit-identical results, so the choice only affects
+// speed.  Each candidate runs one update from the same state (the first call
 // of a configuration captures its CUDA graph; it is run once untimed), timed
 // with CUDA events on the solver's stream; the state is put back after every
 // trial and the fastest variant is kept in the solver's parameters.
@@ -43,16 +42,12 @@ extern "C" bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, floa
         cudaEventDestroy(e0);
         return fail_with(BP_ERR_CUDA, "cudaEventCreate");
     }
-    const int32_t keep =
-        s->prm.walk_options & ~(BP_WALK_NO_SPLIT | BP_WALK_NO_LISTS | BP_WALK_NO_STAGING | BP_WALK_SLABS);
+    const int32_t keep = s->prm.walk_options & ~(BP_WALK_NO_SPLIT | BP_WALK_NO_LISTS | BP_WALK_NO_STAGING);
     float best = -1.f;
     int32_t best_opt = s->prm.walk_options;
-    if (out_ms) out_ms[kNum] = 0.f;
-    // the 8 bit-identical variants, then the fastest of them with height slabs
-    const bool try_slabs = s->cls.perm && !(keep & BP_WALK_NO_ALIAS_CLASSES);
-    for (int c = 0; c < kNum + (try_slabs ? 1 : 0) && st == BP_OK; ++c) {
+    for (int c = 0; c < kNum && st == BP_OK; ++c) {
         bp_params p = s->prm;
-        p.walk_options = c < kNum ? (keep | kCandidates[c]) : (best_opt | BP_WALK_SLABS);
+        p.walk_options = keep | kCandidates[c];
         if ((st = bp_solver_set_params(s, &p)) != BP_OK) break;
         // untimed: captures this variant's graph
         if ((st = bp_solver_update(s, num_substeps, dt, iterations, -1, nullptr, nullptr)) != BP_OK) break;

@@ -133,16 +133,6 @@ struct SimConsts {
     float *cls_rho;
     float4 *cls_vel, *cls_om, *cls_nm, *cls_vb;
     int cls_post;
-    // Height slabs (BP_WALK_SLABS; cls_slab == nullptr: off).  Each (class,
-    // cell) run of the class order is ordered by the slab (quarter of the
-    // cell's height, slab_of) of each particle's hash-time z, stably.
-    // cls_slab[k * cls_T + key] packs the run's counts of particles below
-    // slab 1, 2 and 3 (10 bits each; all ones: the run is too long to
-    // count).  A walk takes, per column, only the slabs the sphere of
-    // radius h around the walker reaches once every particle may have moved
-    // *cls_delta (the largest displacement since the hash, k_class_refresh).
-    const unsigned *cls_slab;
-    const float *cls_delta;
 };
 
 // The walks use the alias classes for the rest of the substep (uniform
@@ -247,15 +237,6 @@ __device__ __forceinline__ int cell_coord(float p, float cell)
 __device__ __forceinline__ int3 cell_of(float3 p, const SimConsts &C)
 {
     return make_int3(cell_coord(p.x, C.cell), cell_coord(p.y, C.cell), cell_coord(p.z, C.cell));
-}
-// Cell coordinate u = (p + 50000) / cell before truncation (cell_coord's
-// own operations), and the slab (0..3) of a coordinate within its cell:
-// both are non-decreasing in p, so p' <= p gives (cell, slab) no greater.
-__device__ __forceinline__ float cell_u(float p, float cell) { return __fdiv_rn(__fadd_rn(p, 50000.0f), cell); }
-__device__ __forceinline__ int slab_of_u(float u)
-{
-    const int c = (int)u;
-    return min(3, (int)__fmul_rn(__fsub_rn(u, (float)c), 4.0f));
 }
 __device__ __forceinline__ int cell_addr(int x, int y, int z, int D, unsigned mask)
 {

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
                 atomicAdd(C.nl_stats + 1, 1u);
                 atomicAdd(C.nl_stats + 4, 1u);
             }
-            walk_classes<Split, true>(i, pi, cell_of(pi, C), 0, v, C, test, push);
+            walk_classes<Split, true>(i, cell_of(pi, C), 0, v, C, test, push);
         } else {
             walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, push);
         }
@@ -131,8 +131,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
                 const unsigned u = (unsigned)a & v.mask;
                 return u != 0u && u != v.mask;
             };
-            // (height slabs order each cell's particles by height instead)
-            const bool ascending = inner(c.x) && inner(c.y) && inner(c.z) && !(C.cls_slab && classes_on(C));
+            const bool ascending = inner(c.x) && inner(c.y) && inner(c.z);
             const int first = ascending ? (self & ~3) : 0;
             if (cnt >= 0 && slots) {
                 int e = first;  // entry index: ascending, the j >= i are the entries from self on
@@ -381,7 +380,7 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
             auto push = [&](int q, float4 pj4) {
                 if (q != t && phase_of(pj4) == phi) list.push(q);
             };
-            walk_classes<Split, true>(i, pi, cell_of(pi, C), 0, v, C, test, push);
+            walk_classes<Split, true>(i, cell_of(pi, C), 0, v, C, test, push);
         } else {
             walk_neighbors<Split>(i, pi, 0, P, v, C, Stage ? &S : nullptr, g, test, [&](int j, float4 pj4) {
                 if (j != i && phase_of(pj4) == phi) list.push(j);

@@ -449,10 +449,8 @@ __global__ void __launch_bounds__(256) k_class_count(int n, const int *__restric
 }
 
 // keys[q] holds the class of perm[q] on entry (the radix pass output).
-// With slabs, also the slab of each class position's hash-time height.
 __global__ void __launch_bounds__(256) k_class_keys(int n, const int *__restrict__ sorted_keys,
-                                                    const float *__restrict__ mass, ClassArrays a, Gate gate,
-                                                    float cell)
+                                                    const float *__restrict__ mass, ClassArrays a, Gate gate)
 {
     if (gate_closed(gate)) return;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -461,84 +459,24 @@ __global__ void __launch_bounds__(256) k_class_keys(int n, const int *__restrict
     a.keys[q] = a.keys[q] * a.T + __ldg(sorted_keys + j);
     a.inv[j] = q;
     a.mass[q] = __ldg(mass + j);
-    if (a.slab) a.slab[q] = slab_of_u(cell_u(__ldg(a.pos0 + j).z, cell));
 }
 
-// Height slabs: each (class, cell) run of the class order, reordered by slab
-// (stable: equal slabs keep their class order).  A particle's new place is
-// its run's start plus the number of run members before it in that order.
-__global__ void __launch_bounds__(256) k_slab_rank(int n, ClassArrays a)
-{
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    const int key = __ldg(a.keys + q);
-    const int b = __ldg(a.off + key), e = __ldg(a.off + key + 1);
-    const int sq = __ldg(a.slab + q);
-    int rank = 0;
-    for (int r = b; r < e; ++r) {
-        const int sr = __ldg(a.slab + r);
-        rank += (sr < sq || (sr == sq && r < q)) ? 1 : 0;
-    }
-    a.perm2[b + rank] = __ldg(a.perm + q);
-    a.slab2[b + rank] = sq;
-}
-
-__global__ void __launch_bounds__(256) k_slab_apply(int n, const float *__restrict__ mass, ClassArrays a)
-{
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    const int j = __ldg(a.perm2 + q);
-    a.perm[q] = j;
-    a.inv[j] = q;
-    a.mass[q] = __ldg(mass + j);
-}
-
-// Per (class, cell) key: how many of its run lie below slab 1, 2 and 3.
-__global__ void __launch_bounds__(256) k_slab_counts(int nkeys, ClassArrays a)
-{
-    const int key = blockIdx.x * blockDim.x + threadIdx.x;
-    if (key >= nkeys) return;
-    const int b = __ldg(a.off + key), e = __ldg(a.off + key + 1);
-    if (e - b > 1023) {
-        a.counts[key] = ~0u;
-        return;
-    }
-    unsigned c1 = 0, c2 = 0, c3 = 0;
-    for (int r = b; r < e; ++r) {
-        const int sr = __ldg(a.slab2 + r);
-        c1 += sr < 1;
-        c2 += sr < 2;
-        c3 += sr < 3;
-    }
-    a.counts[key] = c1 | (c2 << 10) | (c3 << 20);
-}
-
-// Without slabs the classes run only where they pay (see k_class_refresh);
-// with them they always run.
-static Gate class_gate(int n, const ClassArrays &a) { return a.slab ? Gate{} : Gate{a.mixed, (n + 31) / 32}; }
+static Gate class_gate(int n, const ClassArrays &a) { return Gate{a.mixed, (n + 31) / 32}; }
 
 void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const int *off, const float *mass,
-                        const ClassArrays &a, const SortScratch &s, LaunchLog *L, float cell)
+                        const ClassArrays &a, const SortScratch &s, LaunchLog *L)
 {
     if (n <= 0) return;
     cudaMemsetAsync(a.mixed, 0, sizeof(int), st);
     k_class_count<<<(n + 255) / 256, 256, 0, st>>>(n, sorted_keys, off, a);
     L->done("k_class_count");
+    // the rest runs only where the classes pay (see k_class_refresh)
     const Gate gate = class_gate(n, a);
     // one 9-bit digit covers the 3 class bits: a stable partition of the sorted order
     radix_sort_pairs(st, n, 8, a.cls, nullptr, a.keys, a.perm, s, false, L, gate);
-    k_class_keys<<<(n + 255) / 256, 256, 0, st>>>(n, sorted_keys, mass, a, gate, cell);
+    k_class_keys<<<(n + 255) / 256, 256, 0, st>>>(n, sorted_keys, mass, a, gate);
     L->done("k_class_keys");
     launch_cell_offsets(st, n, 8 * a.T, a.keys, a.off, L, gate);
-    if (a.slab) {
-        k_slab_rank<<<(n + 255) / 256, 256, 0, st>>>(n, a);
-        L->done("k_slab_rank");
-        k_slab_apply<<<(n + 255) / 256, 256, 0, st>>>(n, mass, a);
-        L->done("k_slab_apply");
-        const int nkeys = 8 * a.T;
-        k_slab_counts<<<(nkeys + 255) / 256, 256, 0, st>>>(nkeys, a);
-        L->done("k_slab_counts");
-    }
 }
 
 // Walks use the classes while at least 1/32 of the particles sit in a cell
@@ -552,7 +490,6 @@ __global__ void __launch_bounds__(256) k_class_refresh(int n, const float4 *__re
         return;
     }
     bool far = false;
-    float d2max = 0.f;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         const int j = __ldg(a.perm + q);
         const float4 p = P[j];
@@ -563,17 +500,9 @@ __global__ void __launch_bounds__(256) k_class_refresh(int n, const float4 *__re
         // NaN counts as moved; so do positions far enough out that the hash's
         // float rounding exceeds the reach's margin
         const bool inside = fabsf(p.x) < 4.0e4f && fabsf(p.y) < 4.0e4f && fabsf(p.z) < 4.0e4f;
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        far |= !(d2 <= a.reach2) || !inside;
-        d2max = fmaxf(d2max, d2);
+        far |= !(dx * dx + dy * dy + dz * dz <= a.reach2) || !inside;
     }
     if (far) *a.moved = 1;
-    if (a.delta) {  // the largest displacement since the hash, for the slab windows
-        for (int o = 16; o > 0; o >>= 1) d2max = fmaxf(d2max, __shfl_xor_sync(0xffffffffu, d2max, o));
-        // non-negative floats order like their bit patterns; rounded up a little
-        if ((threadIdx.x & 31) == 0 && d2max > 0.f)
-            atomicMax(reinterpret_cast<int *>(a.delta), __float_as_int(__fmul_ru(sqrtf(d2max), 1.0001f)));
-    }
 }
 
 void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L,
@@ -586,7 +515,6 @@ void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassAr
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int blocks = std::min((n + 255) / 256, std::max(sms, 1) * 8);
-    if (a.delta) cudaMemsetAsync(a.delta, 0, sizeof(float), st);
     k_class_refresh<<<blocks, 256, 0, st>>>(n, P, V, a, class_gate(n, a));
     L->done(__func__);
 }

@@ -113,19 +113,11 @@ struct ClassArrays {
     float4 *vel, *om, *nm, *vb;  // [n] each: the post passes' class-order copies (SimConsts::cls_vel ...)
     int T;           // cell keys of all scenes
     float reach2;    // squared reach (see SimConsts::cls_perm)
-    // Height slabs (SimConsts::cls_slab); slab == nullptr: off.
-    int *slab;       // [n] slab (0..3) of each class position
-    int *perm2;      // [n] scratch: the slab-ordered permutation
-    int *slab2;      // [n] scratch: slabs in slab order
-    unsigned *counts;  // [8 T] per (class, cell): particles below slab 1, 2, 3 (10 bits each)
-    float *delta;    // one word: the largest displacement since the hash (k_class_refresh)
 };
 // After k_reorder: class order (one radix pass), keys, inverse, offsets and
 // the count of particles in cells holding two classes (off: the cell offsets).
-// With a.slab, the runs are then reordered by height slab (cell: the hash's
-// cell size) and their slab counts written.
 void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const int *off, const float *mass,
-                        const ClassArrays &a, const SortScratch &s, LaunchLog *L, float cell);
+                        const ClassArrays &a, const SortScratch &s, LaunchLog *L);
 // Gathers P into class order and flags particles beyond the reach.
 // V != nullptr: also gathers V into a.vel (before the post passes).
 void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L,

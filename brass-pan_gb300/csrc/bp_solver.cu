@@ -121,13 +121,6 @@ static float class_reach(const bp_solver *s)
     return reach > 0.f ? reach : 0.f;
 }
 
-// Height slabs within the alias classes (BP_WALK_SLABS, SimConsts::cls_slab):
-// only where the classes themselves are used.
-static bool slabs_on(const bp_solver *s)
-{
-    return (s->prm.walk_options & BP_WALK_SLABS) && class_reach(s) > 0.f;
-}
-
 // Substep constants: SetKernelRadius (K/fluid.cuh:11-27) evaluated on the host.
 SimConsts bp::make_consts(const bp_solver *s, float sdt)
 {
@@ -215,10 +208,6 @@ SimConsts bp::make_consts(const bp_solver *s, float sdt)
         C.cls_om = s->cls.om;
         C.cls_nm = s->cls.nm;
         C.cls_vb = s->cls.vb;
-        if (slabs_on(s)) {
-            C.cls_slab = s->cls.counts;
-            C.cls_delta = s->cls.delta;
-        }
     }
     C.nplanes = (p.stage_mask & BP_STAGE_PLANES) ? s->nplanes : 0;
     for (int k = 0; k < s->nplanes; ++k) {
@@ -366,9 +355,7 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
             (st = s->alloc(&a.pos, N)) || (st = s->alloc(&a.mixed, 1)) || (st = s->alloc(&a.moved, 1)) ||
             (st = s->alloc(&a.mass, N)) || (st = s->alloc(&a.lam, N)) || (st = s->alloc(&a.rho, N)) ||
             (st = s->alloc(&a.vel, N)) || (st = s->alloc(&a.om, N)) || (st = s->alloc(&a.nm, N)) ||
-            (st = s->alloc(&a.vb, N)) || (st = s->alloc(&a.slab, N)) || (st = s->alloc(&a.perm2, N)) ||
-            (st = s->alloc(&a.slab2, N)) || (st = s->alloc(&a.counts, 8 * ncells)) ||
-            (st = s->alloc(&a.delta, 1)))
+            (st = s->alloc(&a.vb, N)))
             return bail(st);
         a.T = (int)ncells;
         s->cls_dmin = D;
@@ -731,16 +718,10 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         const float r = class_reach(s);
         ca.reach2 = r * r;
     }
-    if (!C.cls_slab) {  // no height slabs this update: the classes keep their gate
-        ca.slab = nullptr;
-        ca.perm2 = ca.slab2 = nullptr;
-        ca.counts = nullptr;
-        ca.delta = nullptr;
-    }
     ra.cls = classes ? ca.cls : nullptr;
     ra.pos0 = classes ? ca.pos0 : nullptr;
     launch_reorder(st, C, ra, L);
-    if (classes) launch_class_order(st, s->n, s->sorted_keys, s->off, s->mass, ca, s->sort, L, C.cell);
+    if (classes) launch_class_order(st, s->n, s->sorted_keys, s->off, s->mass, ca, s->sort, L);
     // walks read candidates in class order: gather P before each walking launch
     auto refresh = [&](const float4 *P) {
         if (classes) launch_class_refresh(st, s->n, P, ca, L);

@@ -347,19 +347,9 @@ __device__ __forceinline__ void walk_run_cls(int qb, int e, int qi, int i, int j
 // (candidates j >= lo only), a piece of i's own class starts at i's class
 // position (class order keeps sorted order); other pieces filter in the body.
 // Slots: the body gets class positions (walk_run_cls; lo must be 0).
-//
-// With height slabs (C.cls_slab), each run is narrowed to the slabs that can
-// hold a particle within h of pi: a candidate stored in a column lies, in x
-// and y, at least the walker's distance to the column's extent minus the
-// largest displacement since the hash (and 0.01 of the hash's own rounding)
-// from it, which leaves a reach w in z; its hash-time height then lies in
-// [z - w - delta, z + w + delta], whose ends map through the hash's own
-// (non-decreasing) functions to the first and last (cell, slab) taken.  A
-// column out of reach is skipped.  Slab order does not keep sorted order
-// within a cell, so lo > 0 filters in the body on every piece.
 template <bool Split, bool Slots = false, class T, class B>
-__device__ __forceinline__ void walk_classes(int i, float3 pi, int3 c, int lo, const GridView &v, const SimConsts &C,
-                                             T &test, B &body)
+__device__ __forceinline__ void walk_classes(int i, int3 c, int lo, const GridView &v, const SimConsts &C, T &test,
+                                             B &body)
 {
     const unsigned m = v.mask;
     const unsigned D = (unsigned)v.D;
@@ -372,44 +362,9 @@ __device__ __forceinline__ void walk_classes(int i, float3 pi, int3 c, int lo, c
     const int kz0 = ((c.z - 1) >> sh) & 1, kz2 = ((c.z + 1) >> sh) & 1;
     const int *__restrict__ off = C.cls_off + v.base;
     const size_t keys = (size_t)C.cls_T;
-    const bool slabs = C.cls_slab != nullptr;
-    // slab windows: the walker's offsets within its cell (m), the largest
-    // displacement plus the hash's rounding, the reach with the distance
-    // test's rounding kept clear
-    float ox = 0.f, oy = 0.f, delta = 0.f, marg = 0.f, R2 = 0.f;
-    if (slabs) {
-        ox = __fmul_rn(__fsub_rn(cell_u(pi.x, C.cell), (float)c.x), C.cell);
-        oy = __fmul_rn(__fsub_rn(cell_u(pi.y, C.cell), (float)c.y), C.cell);
-        delta = __ldg(C.cls_delta);
-        marg = delta + 0.01f;
-        const float R = C.h * 1.00001f + 1e-6f;
-        R2 = R * R;
-    }
 #pragma unroll 1
     for (int col = 0; col < 9; ++col) {
-        const int dxo = col / 3 - 1, dyo = col % 3 - 1;
-        const int xr = c.x + dxo, yr = c.y + dyo;
-        int clo = c.z - 1, chi = c.z + 1, slo = 0, shi = 3;
-        if (slabs) {
-            float dx = dxo < 0 ? ox : (dxo > 0 ? C.cell - ox : 0.f);
-            float dy = dyo < 0 ? oy : (dyo > 0 ? C.cell - oy : 0.f);
-            dx = fmaxf(dx - marg, 0.f);
-            dy = fmaxf(dy - marg, 0.f);
-            const float r2 = R2 - dx * dx - dy * dy;
-            if (r2 < 0.f) continue;  // no particle of this column can be within h
-            const float w = sqrtf(r2) + delta + 1e-5f;
-            const float ulo = cell_u(pi.z - w, C.cell), uhi = cell_u(pi.z + w, C.cell);
-            const int cl = (int)ulo, ch = (int)uhi;
-            if (cl >= clo) {
-                clo = cl;
-                slo = slab_of_u(ulo);
-            }
-            if (ch <= chi) {
-                chi = ch;
-                shi = slab_of_u(uhi);
-            }
-            if (clo > chi) continue;
-        }
+        const int xr = c.x + col / 3 - 1, yr = c.y + col % 3 - 1;
         const unsigned base = ((unsigned)xr & m) * D * D + ((unsigned)yr & m) * D;
         const int kxy = ((xr >> sh) & 1) | (((yr >> sh) & 1) << 1);
 #pragma unroll 1
@@ -418,31 +373,8 @@ __device__ __forceinline__ void walk_classes(int i, float3 pi, int3 c, int lo, c
             const unsigned zb = wrap ? (piece == 0 ? D - 1 : z2) : z2;
             const int k = kxy | ((piece == 1 ? kz2 : kz0) << 2);
             const int *o = off + (size_t)k * keys + base;
-            int b, e;
-            if (!slabs) {
-                b = __ldg(o + za);
-                e = __ldg(o + zb + 1);
-            } else {
-                // the piece's real cells: [ra, ra + (zb - za)], clipped to [clo, chi]
-                const int ra = (piece == 0) ? c.z - 1 : c.z + 1 - (int)zb;
-                const int rb = ra + (int)(zb - za);
-                const int ca = max(ra, clo), cb = min(rb, chi);
-                if (ca > cb) continue;
-                const unsigned ta = (unsigned)ca & m, tb = (unsigned)cb & m;
-                const unsigned *cnt = C.cls_slab + (size_t)k * keys + v.base + base;
-                b = __ldg(o + ta);
-                if (ca == clo && slo > 0) {
-                    const unsigned w = __ldg(cnt + ta);
-                    if (w != ~0u) b += (int)((w >> (10 * (slo - 1))) & 1023u);
-                }
-                e = __ldg(o + tb + 1);
-                if (cb == chi && shi < 3) {
-                    const unsigned w = __ldg(cnt + tb);
-                    if (w != ~0u) e = __ldg(o + tb) + (int)((w >> (10 * shi)) & 1023u);
-                }
-                if (b >= e) continue;
-            }
-            const bool own = k == ki && !slabs;
+            const int b = __ldg(o + za), e = __ldg(o + zb + 1);
+            const bool own = k == ki;
             walk_run_cls<Split, Slots>(own ? max(b, qi) : b, e, qi, i, (lo > 0 && !own) ? lo : 0, C, test, body);
         }
     }
@@ -478,7 +410,7 @@ __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const f
 
     if (C.cls_perm && !staged && __ldg(C.cls_moved) == 0) {
         if (C.nl_stats) atomicAdd(C.nl_stats + 4, 1u);
-        walk_classes<Split>(i, pi, c, lo, v, C, test, body);
+        walk_classes<Split>(i, c, lo, v, C, test, body);
         return;
     }
 

@@ -171,9 +171,9 @@ class ParticleSolver:
 
     def autotune(self, num_substeps: int, dt: float, iterations: int) -> tuple[int, list[float]]:
         """Keep the fastest walk variant for this scene; returns it and the
-        trial times (ms) of the nine candidates (bp_solver_autotune)."""
+        trial times (ms) of the eight candidates."""
         opt = C.c_int32()
-        ms = (C.c_float * 9)()
+        ms = (C.c_float * 8)()
         abi.check(self.lib, self.lib.bp_solver_autotune(self.handle, num_substeps, C.c_float(dt), iterations,
                                                         C.byref(opt), ms))
         self.params.walk_options = opt.value

@@ -91,20 +91,11 @@ typedef enum bp_mode {
  * cells wraps space, so one table cell holds every real cell D cells apart;
  * the split is kept for grids of at most 2^21 cells and used in a substep
  * while at least 1/32 of the particles share a cell with another real cell's
- * and no particle has moved (D - 2) cells - h from where it was hashed).
- * BP_WALK_SLABS (opt-in) keeps the walks on the alias classes in every
- * substep, orders the particles of each of their (class, cell) runs by the
- * quarter of the cell's height they were hashed in, and walks per column
- * only the quarters a sphere of radius h around the walker can reach (with
- * the largest displacement since the hash added): about half the
- * candidates.  The pairs found are the same; the order in which a
- * particle's pair terms are summed follows the new order, so results agree
- * with the other variants to fp32 rounding instead of bit for bit. */
+ * and no particle has moved (D - 2) cells - h from where it was hashed). */
 #define BP_WALK_NO_STAGING 0x1
 #define BP_WALK_NO_SPLIT 0x2
 #define BP_WALK_NO_LISTS 0x4
 #define BP_WALK_NO_ALIAS_CLASSES 0x8
-#define BP_WALK_SLABS 0x10
 
 /* Every literal of the reference's step as a field.  bp_params_init fills the
  * reference's values; comments give the reference location of each. */
@@ -283,17 +274,15 @@ bp_status bp_solver_profile(bp_solver *s, int32_t num_substeps, float dt, int32_
 bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
                                uint64_t out_walks[5]);
 
-/* Picks the fastest neighbour-walk variant (BP_WALK_* combinations) for this
- * solver's scene and step configuration: each candidate runs one update from
- * the current state, timed with CUDA events, and the state is put back after
- * every trial.  First the 8 combinations of the three BP_WALK_NO_* bits (all
- * give identical results), in the order 0, NO_STAGING, NO_SPLIT, NO_LISTS,
- * NO_STAGING|NO_SPLIT, NO_STAGING|NO_LISTS, NO_SPLIT|NO_LISTS, all three;
- * then the fastest of them with BP_WALK_SLABS added (results equal to fp32
- * rounding; only where the alias classes can be used).  The choice is kept
- * in the solver's parameters and written to *out_walk_options; out_ms (or
- * NULL) receives the 9 trial times in that order (the last is 0 when the
- * slab trial did not run).  No counterpart in the reference. */
+/* Picks the fastest neighbour-walk variant (BP_WALK_* combinations; all give
+ * identical results) for this solver's scene and step configuration: each
+ * candidate runs one update from the current state, timed with CUDA events,
+ * and the state is put back after every trial.  The choice is kept in the
+ * solver's parameters and written to *out_walk_options; out_ms (or NULL)
+ * receives the time of each of the 8 combinations of the three BP_WALK_NO_*
+ * bits, in the order 0, NO_STAGING, NO_SPLIT, NO_LISTS, NO_STAGING|NO_SPLIT,
+ * NO_STAGING|NO_LISTS, NO_SPLIT|NO_LISTS, all three.  No counterpart in the
+ * reference. */
 bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
                              int32_t *out_walk_options, float *out_ms);
 

@@ -28,16 +28,10 @@ def members(bp):
     return scenes
 
 
-@pytest.mark.parametrize("walk", [0, 1, 2])
+@pytest.mark.parametrize("walk", [0, 1])
 def test_batch_members_match_single_scene_solvers(bp, gpu, walk):
-    """walk 2: height slabs (BP_WALK_SLABS).  A batch's slab windows widen by
-    the largest displacement over all its scenes, but they only take or leave
-    candidates that fail the distance test, so the pairs and their order stay
-    those of the scene alone."""
     scenes = members(bp)
-    a = bp.abi
-    opts = [0, a.BP_WALK_NO_STAGING, a.BP_WALK_NO_STAGING | a.BP_WALK_SLABS][walk]
-    params = [bp.make_params(s, walk_options=opts) for s in scenes]
+    params = [bp.make_params(s, walk_options=walk * bp.abi.BP_WALK_NO_STAGING) for s in scenes]
     batch = bp.BatchSolver(scenes, params)
     singles = [bp.ParticleSolver(s, p) for s, p in zip(scenes, params)]
     for _ in range(5):

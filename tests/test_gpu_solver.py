@@ -387,8 +387,7 @@ def test_alias_classes_fall_back_past_the_reach(bp, gpu):
 
 def test_autotune_keeps_state_and_results(bp, gpu):
     """The autotuner's trial updates leave the state as it was, and the variant
-    it keeps gives the same bits as the default walk (with height slabs, the
-    same state to fp32 rounding)."""
+    it keeps gives the same bits as the default walk."""
     abi = bp.abi
     scene = small_mixed_scene(bp, seed=21)
     a = bp.ParticleSolver(scene, bp.make_params(scene))
@@ -398,17 +397,14 @@ def test_autotune_keeps_state_and_results(bp, gpu):
     x0 = a.positions()
     opt, ms = a.autotune(2, DT, 4)
     np.testing.assert_array_equal(a.positions(), x0)
-    assert 0 <= opt <= (abi.BP_WALK_NO_SPLIT | abi.BP_WALK_NO_LISTS | abi.BP_WALK_NO_STAGING | abi.BP_WALK_SLABS)
-    assert len(ms) == 9
-    assert all(t > 0 for t in ms)  # this scene's grid keeps the classes: the slab trial runs
+    assert 0 <= opt <= (abi.BP_WALK_NO_SPLIT | abi.BP_WALK_NO_LISTS | abi.BP_WALK_NO_STAGING)
+    assert len(ms) == 8
+    assert all(t > 0 for t in ms)
     for s in (a, b):
         for _ in range(3):
             s.update(2, DT, 4)
-    if opt & abi.BP_WALK_SLABS:
-        assert np.abs(a.positions() - b.positions()).max() <= 1e-4 * scene.kernel_radius
-    else:
-        np.testing.assert_array_equal(a.positions(), b.positions())
-        np.testing.assert_array_equal(a.velocities(), b.velocities())
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.velocities(), b.velocities())
     a.close()
     b.close()
 
