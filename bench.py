@@ -409,8 +409,10 @@ def run_reference_cuda(bp, torch, scene, params, steps, warmup, flush, state=Non
 
 
 def run_batch(bp, torch, stream, flush, steps, warmup, seed=0):
-    """The batched ensemble (256 scenes in one solver) against looping one
-    solver per scene over the same scenes on the same stream."""
+    """The batched ensemble (256 scenes in one solver, its walk variant
+    chosen by the autotuner after the warm-up) against looping the plain
+    single-scene solver (default parameters) over the same scenes on the same
+    stream."""
     scenes = bp.scenes.dam_break_ensemble(seed=seed)
     n = sum(s.num_particles for s in scenes)
     batch = bp.BatchSolver(scenes, stream=stream.cuda_stream)
@@ -420,6 +422,10 @@ def run_batch(bp, torch, stream, flush, steps, warmup, seed=0):
             batch.update(SUBSTEPS, DT, ITERATIONS)
             for g in singles:
                 g.update(SUBSTEPS, DT, ITERATIONS)
+        tuned, trial_ms = batch.autotune(SUBSTEPS, DT, ITERATIONS)
+        batch.update(SUBSTEPS, DT, ITERATIONS)  # the chosen variant's graph, captured outside the timing
+        for g in singles:
+            g.update(SUBSTEPS, DT, ITERATIONS)
         launches_batch = batch.last_launch_count()
         launches_loop = sum(g.last_launch_count() for g in singles)
         ms_batch = timed_steps(torch, stream, flush, steps, lambda: batch.update(SUBSTEPS, DT, ITERATIONS))
@@ -434,7 +440,8 @@ def run_batch(bp, torch, stream, flush, steps, warmup, seed=0):
             "value": units / (ms_batch / 1e3), "loop_value": units / (ms_loop / 1e3),
             "batched_vs_loop": ms_loop / ms_batch, "ms_per_step": ms_batch / steps,
             "loop_ms_per_step": ms_loop / steps, "launches_per_step": launches_batch,
-            "loop_launches_per_step": launches_loop, "device_errors": errors, "steps": steps}
+            "loop_launches_per_step": launches_loop, "device_errors": errors, "steps": steps,
+            "autotune": {"walk_options": tuned, "trial_ms": [round(t, 3) for t in trial_ms]}}
 
 
 class ClockSampler:
