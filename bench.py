@@ -1,22 +1,29 @@
 """Throughput benchmark: particle-substeps/s of the solver step on one GB300.
 
 A step is one call of update(2 substeps, dt = 1/60 s, 4 iterations) (one
-frame) on the mixed-phase scene of the benchmark configuration (1,048,576 PBF fluid
-particles, a 256x256 cloth under wind, 64 rigid 8^3 cubes; 1,146,880
-particles), reference-mode parameters.  By default the timed region is the
-configuration's 200 frames after 3 warm-up frames: throughput falls as the
-dam break spreads into cells the 64^3 table aliases and the fluid
-compresses, so short runs overstate it.  Its "e2e" object replays the
-same frames through the C ABI, each frame's state uploaded from pinned host
-memory and its positions and velocities read back.  Prints one JSON line; unless
---no-batch, its "batched" object times the batched ensemble (256 PBF dam
-breaks of 4096..262144 particles in one solver) against looping one solver
-per scene over the same scenes; unless --no-adjoint, its "adjoint" object
-times forward + backward() of differentiable rollouts against the forward
-alone (wall clock, host arrays in and out).
+frame) on the mixed-phase scene of the benchmark configuration (1,048,576 PBF
+fluid particles, a 256x256 cloth under wind, 64 rigid 8^3 cubes; 1,146,880
+particles), reference-mode parameters.  W warm-up frames, the walk autotuner,
+then K timed frames (CUDA events, L2 flushed before each).  Its "e2e" object
+replays the same frames through the C ABI, each frame's state uploaded from
+pinned host memory and its positions and velocities read back.  Prints one
+JSON line, which also carries (each can be switched off):
+  reference_cuda  the reference's own CUDA step (its kernel headers built for
+                  sm_103a, oracle/ref_cuda.cu) on the same GPU and frames;
+  workloads       the other configurations and regimes (32k dam break, the
+                  shape-matching stress test, the 1M PBF block, the mixed
+                  scene 200 frames in, the mixed scene's textbook parameters);
+  batched         256 PBF dam breaks of 4096..262144 particles in one solver
+                  against looping one solver per scene;
+  adjoint         forward + backward() of differentiable rollouts against the
+                  forward alone, with FP64 finite-difference gradient checks;
+  cpu_baseline    the reference's kernels compiled for the host, all cores.
+`--impl reference` times the reference's step on the host cores (the
+reference arm): same workload, warm-up and frames, no product code loaded.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload mixed|fluid|small|batch|rigid] [--no-batch] [--no-adjoint]
+                  [--no-reference-cuda] [--no-samples] [--no-gradient-check]
 
 Multi-GPU (torchrun, one rank per GPU): the scene does not shard, so every
 rank advances its own replica ("replicas only"); value = all ranks' particle
@@ -321,17 +328,21 @@ def textbook_mixed_params(bp, scene):
 
 def run_samples(bp, torch, stream, flush, local, args):
     """The other configurations and regimes, each a sub-object of the line:
-    the 32k dam break (its 100 frames, textbook parameters), the
-    shape-matching stress test, the 1M PBF block alone against the
-    reference's CUDA step, the mixed scene 200 frames in (late regime:
-    compressed fluid, aliased table) against the reference's CUDA step from
-    the same state, and the mixed scene with textbook parameters."""
+    the 32k dam break (its 100 frames, textbook parameters, and reference
+    parameters against the reference's CUDA step), the shape-matching stress
+    test, the 1M PBF block alone against the reference's CUDA step, the
+    mixed scene 200 frames in (late regime: compressed fluid, aliased table)
+    against the reference's CUDA step from the same state, and the mixed
+    scene with textbook parameters."""
     sc = bp.scenes
     out = {}
     small = sc.dam_break_32k(seed=0)
     out["small"] = run_sample(bp, torch, stream, flush, local, "small", small,
                               bp.make_params(small, mode=bp.abi.BP_MODE_TEXTBOOK, relaxation=600.0, scorr_k=0.001,
                                              scorr_n=4, scorr_dq=0.2, xsph_c=0.01), frames=100, warmup=3)
+    out["small_reference"] = run_sample(bp, torch, stream, flush, local, "small", small,
+                                        workload_params(bp, "small", small), frames=100, warmup=3,
+                                        reference_cuda=not args.no_reference_cuda)
     rigid = sc.rigid_body_pile(seed=0)
     out["rigid"] = run_sample(bp, torch, stream, flush, local, "rigid", rigid, workload_params(bp, "rigid", rigid),
                               frames=10, warmup=3)
@@ -344,6 +355,7 @@ def run_samples(bp, torch, stream, flush, local, args):
     out["textbook"] = run_sample(bp, torch, stream, flush, local, "mixed", mixed, textbook_mixed_params(bp, mixed),
                                  frames=args.steps, warmup=args.warmup)
     names = {"small": workload_name("small", small.num_particles) + ", textbook parameters, 100 frames",
+             "small_reference": workload_name("small", small.num_particles) + ", reference parameters, 100 frames",
              "rigid": workload_name("rigid", rigid.num_particles),
              "pbf_1m": workload_name("fluid", fluid.num_particles) + ", reference parameters",
              "late": workload_name("mixed", mixed.num_particles) + ", frames 201-205 (after 200 untimed)",
