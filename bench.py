@@ -520,11 +520,12 @@ def dist_info():
 
 
 def profile_summary(kernel: str, workload: str):
-    """The committed ncu summary of `kernel` for this workload: the late-frame
-    capture where there is one (the top kernel is profiled at the end of the
-    timed run), else the 1,048,576-particle fluid capture.  Returns (text, file)."""
+    """The committed ncu summary of `kernel` for this workload: the early-frame
+    capture where there is one (the timed frames are early ones), else the
+    late-frame capture, else the 1,048,576-particle fluid capture.  Returns
+    (text, file)."""
     name = kernel.replace("launch_", "k_")
-    for fname in (f"{name}_{workload}_late.md", f"{name}_fluid_1048576.md"):
+    for fname in (f"{name}_{workload}_early.md", f"{name}_{workload}_late.md", f"{name}_fluid_1048576.md"):
         p = REPO / "profiles" / fname
         if p.exists():
             return p.read_text(), fname
