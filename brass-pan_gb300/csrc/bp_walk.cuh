@@ -47,6 +47,37 @@ constexpr int kWalkThreads = 256;
 #define BP_CHUNK_UNROLL 4
 #endif
 constexpr int kChunkUnroll = BP_CHUNK_UNROLL;
+// Candidate tests of a chunk gathered four at a time into a nibble of
+// constant bit positions, then shifted into the chunk mask once.
+#ifndef BP_CHUNK_NIBBLES
+#define BP_CHUNK_NIBBLES 0
+#endif
+
+// The test bits of candidates [0, cnt) of a chunk read from s: bit t set when
+// test(t, s[t]) holds (t is the candidate's offset in the chunk).
+template <class F>
+__device__ __forceinline__ unsigned chunk_bits(int cnt, const float4 *s, F &&test)
+{
+    unsigned bits = 0u;
+#if BP_CHUNK_NIBBLES
+    int t = 0;
+#pragma unroll 1
+    for (; t + 4 <= cnt; t += 4) {
+        const float4 a = s[t], b = s[t + 1], c = s[t + 2], d = s[t + 3];
+        const unsigned nib = (test(t, a) ? 1u : 0u) | (test(t + 1, b) ? 2u : 0u) | (test(t + 2, c) ? 4u : 0u) |
+                             (test(t + 3, d) ? 8u : 0u);
+        bits |= nib << t;
+    }
+#pragma unroll 1
+    for (; t < cnt; ++t)
+        if (test(t, s[t])) bits |= 1u << t;
+#else
+#pragma unroll kChunkUnroll
+    for (int t = 0; t < cnt; ++t)
+        if (test(t, s[t])) bits |= 1u << t;
+#endif
+    return bits;
+}
 constexpr int kStageCap = BP_STAGE_CAP;
 constexpr int kStageSegs = 2 * 9 * 2; // groups x columns x pieces
 
@@ -215,10 +246,7 @@ __device__ __forceinline__ void walk_run(int jb, int b, int e, const float4 *src
         for (int j0 = jb; j0 < e; j0 += 32) {
             const int cnt = min(32, e - j0);
             const float4 *s = src + (j0 - b);
-            unsigned bits = 0u;
-#pragma unroll kChunkUnroll
-            for (int t = 0; t < cnt; ++t)
-                if (test(j0 + t, s[t])) bits |= 1u << t;
+            unsigned bits = chunk_bits(cnt, s, [&](int t, float4 p) { return test(j0 + t, p); });
 #pragma unroll 1
             while (bits) {
                 const int t = __ffs(bits) - 1;
@@ -321,10 +349,7 @@ __device__ __forceinline__ void walk_run_cls(int qb, int e, int qi, int i, int j
         for (int q0 = qb; q0 < e; q0 += 32) {
             const int cnt = min(32, e - q0);
             const float4 *s = src + q0;
-            unsigned bits = 0u;
-#pragma unroll kChunkUnroll
-            for (int t = 0; t < cnt; ++t)
-                if (test(q0 + t == qi ? i : -1 - (q0 + t), s[t])) bits |= 1u << t;
+            unsigned bits = chunk_bits(cnt, s, [&](int t, float4 p) { return test(q0 + t == qi ? i : -1 - (q0 + t), p); });
 #pragma unroll 1
             while (bits) {
                 const int t = __ffs(bits) - 1;
