@@ -435,6 +435,7 @@ def run_batch(bp, torch, stream, flush, steps, warmup, seed=0):
             for g in singles:
                 g.update(SUBSTEPS, DT, ITERATIONS)
         tuned, trial_ms = batch.autotune(SUBSTEPS, DT, ITERATIONS)
+        batch_shape = (batch.params.scan_block, batch.params.scan_persistent)
         batch.update(SUBSTEPS, DT, ITERATIONS)  # the chosen variant's graph, captured outside the timing
         for g in singles:
             g.update(SUBSTEPS, DT, ITERATIONS)
@@ -453,7 +454,8 @@ def run_batch(bp, torch, stream, flush, steps, warmup, seed=0):
             "batched_vs_loop": ms_loop / ms_batch, "ms_per_step": ms_batch / steps,
             "loop_ms_per_step": ms_loop / steps, "launches_per_step": launches_batch,
             "loop_launches_per_step": launches_loop, "device_errors": errors, "steps": steps,
-            "autotune": {"walk_options": tuned, "trial_ms": [round(t, 3) for t in trial_ms]}}
+            "autotune": {"walk_options": tuned, "scan_block": int(batch_shape[0]), "scan_persistent": int(batch_shape[1]),
+                         "trial_ms": [round(t, 3) for t in trial_ms]}}
 
 
 class ClockSampler:
@@ -621,7 +623,9 @@ def run_ours(args):
         if not (args.no_autotune or args.no_stage or args.no_split or args.no_lists):
             # keeps the fastest (bit-identical) walk variant
             opt, trial_ms = solver.autotune(SUBSTEPS, DT, ITERATIONS)
-            tuned_walk = {"walk_options": opt, "trial_ms": [round(t, 3) for t in trial_ms]}
+            tuned_walk = {"walk_options": opt, "scan_block": int(solver.params.scan_block),
+                          "scan_persistent": int(solver.params.scan_persistent),
+                          "trial_ms": [round(t, 3) for t in trial_ms]}
         stream.synchronize()
         launches_per_step = solver.last_launch_count()
         # the state the timed frames start from, for the end-to-end replay

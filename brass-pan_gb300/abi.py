@@ -85,7 +85,9 @@ class BpParams(C.Structure):
         ("neighbor_skin", C.c_float),
         ("walk_options", C.c_int32),
         ("bending_stiffness", C.c_float),
-        ("reserved", C.c_int32 * 5),
+        ("scan_block", C.c_int32),
+        ("scan_persistent", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -182,7 +184,8 @@ _lib = None
 
 EXPORTS = [
     "bp_params_init", "bp_solver_create", "bp_solver_destroy", "bp_solver_update", "bp_solver_step",
-    "bp_solver_set_params", "bp_solver_query_original_particle_id", "bp_solver_query_new_particle_id",
+    "bp_solver_set_params", "bp_solver_get_params", "bp_solver_query_original_particle_id",
+    "bp_solver_query_new_particle_id",
     "bp_solver_get_particle_position", "bp_solver_copy_positions", "bp_solver_copy_velocities",
     "bp_solver_set_state", "bp_solver_snapshot_size", "bp_solver_snapshot_save", "bp_solver_snapshot_load",
     "bp_solver_field", "bp_solver_copy_field", "bp_solver_pack_particle_infos",
@@ -210,6 +213,7 @@ def load(path: Path | None = None):
         "bp_solver_update": (i32, [vp, i32, f32, i32, i32, pf, pf]),
         "bp_solver_step": (i32, [vp, f32, i32, i32]),
         "bp_solver_set_params": (i32, [vp, C.POINTER(BpParams)]),
+        "bp_solver_get_params": (i32, [vp, C.POINTER(BpParams)]),
         "bp_solver_query_original_particle_id": (i32, [vp, i32, pi]),
         "bp_solver_query_new_particle_id": (i32, [vp, i32, pi]),
         "bp_solver_get_particle_position": (i32, [vp, i32, pf]),

@@ -3,8 +3,9 @@
 //
 // The walk variants (staging each CTA's neighbourhood in shared memory,
 // testing candidates in chunks before the pair terms, the post passes'
-// neighbour lists) give bit-identical results, so the choice only affects
-// speed.  Each candidate runs one update from the same state (the first call
+// neighbour lists) and the launch shapes of the unstaged scans (threads per
+// CTA, persistent CTAs) give bit-identical results, so the choice only
+// affects speed.  Each candidate runs one update from the same state (the first call
 // of a configuration captures its CUDA graph; it is run once untimed), timed
 // with CUDA events on the solver's stream; the state is put back after every
 // trial and the fastest variant is kept in the solver's parameters.
@@ -48,6 +49,8 @@ extern "C" bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, floa
     for (int c = 0; c < kNum && st == BP_OK; ++c) {
         bp_params p = s->prm;
         p.walk_options = keep | kCandidates[c];
+        p.scan_block = 0;
+        p.scan_persistent = 0;
         if ((st = bp_solver_set_params(s, &p)) != BP_OK) break;
         // untimed: captures this variant's graph
         if ((st = bp_solver_update(s, num_substeps, dt, iterations, -1, nullptr, nullptr)) != BP_OK) break;
@@ -68,11 +71,45 @@ extern "C" bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, floa
         }
         snap.restore(s);
     }
+    // then the launch shape of the unstaged scans, on the fastest walk variant:
+    // 128 and 64 threads per CTA, and persistent 256-thread CTAs
+    static const int32_t kShapes[][2] = {{128, 0}, {64, 0}, {256, 1}};
+    constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
+    int32_t best_block = s->prm.scan_block, best_persist = s->prm.scan_persistent;
+    for (int c = 0; c < kNumShapes && st == BP_OK; ++c) {
+        if (out_ms) out_ms[kNum + c] = 0.f;
+        if (!(best_opt & BP_WALK_NO_STAGING)) continue;  // staged launches keep 256-thread CTAs
+        bp_params p = s->prm;
+        p.walk_options = best_opt;
+        p.scan_block = kShapes[c][0];
+        p.scan_persistent = kShapes[c][1];
+        if ((st = bp_solver_set_params(s, &p)) != BP_OK) break;
+        if ((st = bp_solver_update(s, num_substeps, dt, iterations, -1, nullptr, nullptr)) != BP_OK) break;
+        snap.restore(s);
+        cudaEventRecord(e0, s->stream);
+        if ((st = bp_solver_update(s, num_substeps, dt, iterations, -1, nullptr, nullptr)) != BP_OK) break;
+        cudaEventRecord(e1, s->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            st = fail_with(BP_ERR_CUDA, "autotune: event");
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (out_ms) out_ms[kNum + c] = ms;
+        if (ms < best) {
+            best = ms;
+            best_block = kShapes[c][0];
+            best_persist = kShapes[c][1];
+        }
+        snap.restore(s);
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     snap.restore(s);
     bp_params p = s->prm;
     p.walk_options = best_opt;
+    p.scan_block = best_block;
+    p.scan_persistent = best_persist;
     const bp_status st2 = bp_solver_set_params(s, &p);
     cudaStreamSynchronize(s->stream);
     if (st != BP_OK) return st;

@@ -60,6 +60,8 @@ struct SimConsts {
     int nplanes;
     int stage;        // scan kernels stage their neighbourhood in shared memory
     int split;        // scan kernels test candidates in chunks before the pair terms
+    int scan_block;   // unstaged scan launches: threads per CTA (bp_params::scan_block; 256 when 0)
+    int scan_persist; // unstaged scan launches: at most one resident wave of CTAs, striding over the tiles
     float4 plane_o[kMaxPlanes];
     float4 plane_n[kMaxPlanes];
     // Verlet lists of the current substep (vl == nullptr: off).  The first

@@ -282,15 +282,22 @@ __device__ __forceinline__ void collide_one(const SimConsts &C, int i, const flo
 // solid stored in its 27 cells (solid_near, k_solid_dilate): its walk over
 // the solids would visit none.
 template <bool Split>
-__global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS)
-    k_particle_collision(SimConsts C, const float4 *__restrict__ P, const float4 *__restrict__ Xs,
-                         const float *__restrict__ w, const int *__restrict__ off, const int *__restrict__ tile_solid,
-                         const int *__restrict__ solid_prefix, const int *__restrict__ solid_list,
-                         const float4 *__restrict__ solid_pos, const unsigned long long *__restrict__ solid_near,
-                         int solids_apart, float4 *__restrict__ Pout)
+__device__ __forceinline__ void k_particle_collision_tile(
+    const SimConsts &C,
+    const float4 *__restrict__ P,
+    const float4 *__restrict__ Xs,
+    const float *__restrict__ w,
+    const int *__restrict__ off,
+    const int *__restrict__ tile_solid,
+    const int *__restrict__ solid_prefix,
+    const int *__restrict__ solid_list,
+    const float4 *__restrict__ solid_pos,
+    const unsigned long long *__restrict__ solid_near,
+    int solids_apart,
+    float4 *__restrict__ Pout,
+    int i0)
 {
     StageShared &S = stage_shared();
-    const int i0 = blockIdx.x * kWalkThreads;
     // With the solids apart, fluid threads walk the solid list, not the
     // staged runs: only the runs' solid check is needed.
     const int g = stage_block(C, P, off, i0, S, tile_solid, !solids_apart);
@@ -312,6 +319,32 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS)
         return;
     }
     collide_one<Split>(C, i, P, Xs, w, v, &S, g, solid_prefix, solid_list, solid_pos, Pout);
+}
+
+template <bool Split, bool Persist = false>
+__global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS) k_particle_collision(
+    SimConsts C,
+    const float4 *__restrict__ P,
+    const float4 *__restrict__ Xs,
+    const float *__restrict__ w,
+    const int *__restrict__ off,
+    const int *__restrict__ tile_solid,
+    const int *__restrict__ solid_prefix,
+    const int *__restrict__ solid_list,
+    const float4 *__restrict__ solid_pos,
+    const unsigned long long *__restrict__ solid_near,
+    int solids_apart,
+    float4 *__restrict__ Pout)
+{
+    // one tile of blockDim.x particles per CTA, or, persistent (an unstaged
+    // launch of at most one resident wave: SimConsts::scan_persist), every
+    // gridDim.x-th tile from blockIdx.x on
+    if constexpr (Persist) {
+        for (int i0 = blockIdx.x * blockDim.x; i0 < C.n; i0 += gridDim.x * blockDim.x)
+            k_particle_collision_tile<Split>(C, P, Xs, w, off, tile_solid, solid_prefix, solid_list, solid_pos, solid_near, solids_apart, Pout, i0);
+    } else {
+        k_particle_collision_tile<Split>(C, P, Xs, w, off, tile_solid, solid_prefix, solid_list, solid_pos, solid_near, solids_apart, Pout, blockIdx.x * blockDim.x);
+    }
 }
 
 // The positions of the compacted solids, in list order, for the fluid
@@ -354,7 +387,6 @@ void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4
                                const unsigned long long *solid_near, float4 *solid_pos, float4 *Pout, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    const int grid = (C.n + kWalkThreads - 1) / kWalkThreads;
     const int apart = (solids_apart && solid_prefix && solid_list && nsolid > 0) ? 1 : 0;
     // the cell mask describes the walks over the compacted solids only
     const unsigned long long *near = (apart && solid_prefix) ? solid_near : nullptr;
@@ -362,12 +394,15 @@ void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4
         k_gather_solids<<<(max(nsolid, 1) + 255) / 256, 256, 0, st>>>(C.n, solid_prefix, solid_list, P, solid_pos);
         L->done("k_gather_solids");
     }
-    if (C.split)
-        k_particle_collision<true><<<grid, kWalkThreads, stage_bytes(C), st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
-                                                                 solid_list, solid_pos, near, apart, Pout);
+    if (C.split && !C.stage && C.scan_persist)
+        launch_scan(k_particle_collision<true, true>, C, stage_bytes(C), st, C, P, Xs, w, off, tile_solid,
+                    solid_prefix, solid_list, solid_pos, near, apart, Pout);
+    else if (C.split)
+        launch_scan(k_particle_collision<true>, C, stage_bytes(C), st, C, P, Xs, w, off, tile_solid, solid_prefix,
+                    solid_list, solid_pos, near, apart, Pout);
     else
-        k_particle_collision<false><<<grid, kWalkThreads, stage_bytes(C), st>>>(C, P, Xs, w, off, tile_solid, solid_prefix,
-                                                                  solid_list, solid_pos, near, apart, Pout);
+        launch_scan(k_particle_collision<false>, C, stage_bytes(C), st, C, P, Xs, w, off, tile_solid, solid_prefix,
+                    solid_list, solid_pos, near, apart, Pout);
     L->done(__func__);
     if (apart) {
         const int sg = (nsolid + kWalkThreads - 1) / kWalkThreads;

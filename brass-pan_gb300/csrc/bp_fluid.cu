@@ -52,13 +52,16 @@ __device__ __forceinline__ void finish_verlet(const SimConsts &C, int i, float4 
 // gathers from fluid neighbours).  With C.vl_build it records the substep's
 // Verlet lists instead: every j within h + skin.
 template <bool Split, bool Stage>
-__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(SimConsts C, const float4 *__restrict__ P,
-                                                         const float *__restrict__ mass,
-                                                         const int *__restrict__ off, float *__restrict__ lam,
-                                                         float *__restrict__ rho)
+__device__ __forceinline__ void k_lambda_tile(
+    const SimConsts &C,
+    const float4 *__restrict__ P,
+    const float *__restrict__ mass,
+    const int *__restrict__ off,
+    float *__restrict__ lam,
+    float *__restrict__ rho,
+    int i0)
 {
     StageShared &S = stage_shared();
-    const int i0 = blockIdx.x * kScanThreads;
     const int g = Stage ? stage_block(C, P, off, i0, S) : -1;
     const int t = i0 + threadIdx.x;  // the slot of the position pass's list
     if (t >= C.n) return;
@@ -206,23 +209,46 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(Sim
     if (slots) C.cls_rho[t] = density;
 }
 
+template <bool Split, bool Stage, bool Persist = false>
+__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_lambda(
+    SimConsts C,
+    const float4 *__restrict__ P,
+    const float *__restrict__ mass,
+    const int *__restrict__ off,
+    float *__restrict__ lam,
+    float *__restrict__ rho)
+{
+    // one tile of blockDim.x particles per CTA, or, persistent (an unstaged
+    // launch of at most one resident wave: SimConsts::scan_persist), every
+    // gridDim.x-th tile from blockIdx.x on
+    if constexpr (Persist) {
+        for (int i0 = blockIdx.x * blockDim.x; i0 < C.n; i0 += gridDim.x * blockDim.x)
+            k_lambda_tile<Split, Stage>(C, P, mass, off, lam, rho, i0);
+    } else {
+        k_lambda_tile<Split, Stage>(C, P, mass, off, lam, rho, blockIdx.x * blockDim.x);
+    }
+}
+
 // Kernels with a split walk (test, then body over the hits) and a fused one.
 // Kernels instantiated for split / fused walks and staged / unstaged CTAs
 // (an unstaged instantiation carries none of the staging code or registers).
-#define BP_LAUNCH_SPLIT(kernel, grid, block, st, ...)                                                 \
+// Persistent launches (SimConsts::scan_persist) exist for the split,
+// unstaged instantiation, the one the autotuner keeps almost everywhere.
+#define BP_LAUNCH_SPLIT(kernel, st, ...)                                                              \
     do {                                                                                              \
         const size_t smem_ = stage_bytes(C);                                                          \
-        if (C.split && C.stage) kernel<true, true><<<grid, block, smem_, st>>>(__VA_ARGS__);          \
-        else if (C.split) kernel<true, false><<<grid, block, smem_, st>>>(__VA_ARGS__);               \
-        else if (C.stage) kernel<false, true><<<grid, block, smem_, st>>>(__VA_ARGS__);               \
-        else kernel<false, false><<<grid, block, smem_, st>>>(__VA_ARGS__);                           \
+        if (C.split && C.stage) launch_scan(kernel<true, true>, C, smem_, st, __VA_ARGS__);           \
+        else if (C.split && C.scan_persist) launch_scan(kernel<true, false, true>, C, smem_, st, __VA_ARGS__); \
+        else if (C.split) launch_scan(kernel<true, false>, C, smem_, st, __VA_ARGS__);                \
+        else if (C.stage) launch_scan(kernel<false, true>, C, smem_, st, __VA_ARGS__);                \
+        else launch_scan(kernel<false, false>, C, smem_, st, __VA_ARGS__);                            \
     } while (0)
 
 void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const float *mass, const int *off,
                    float *lam, float *rho, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    BP_LAUNCH_SPLIT(k_lambda, (C.n + kScanThreads - 1) / kScanThreads, kScanThreads, st, C, P, mass, off, lam, rho);
+    BP_LAUNCH_SPLIT(k_lambda, st, C, P, mass, off, lam, rho);
     L->done(__func__);
 }
 
@@ -234,10 +260,12 @@ void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // the lists k_lambda recorded at the same positions (r^2 <= h^2, walk order);
 // particles whose list overflowed walk their cells.
 template <bool Split, bool Stage>
-__global__ void __launch_bounds__(kScanThreads, BP_DELTAP_MIN_BLOCKS) k_deltap(SimConsts C, DeltaArgs a)
+__device__ __forceinline__ void k_deltap_tile(
+    const SimConsts &C,
+    DeltaArgs a,
+    int i0)
 {
     StageShared &S = stage_shared();
-    const int i0 = blockIdx.x * kScanThreads;
     const int t = i0 + threadIdx.x;  // the slot of k's list (k_lambda)
     const bool valid = t < C.n;
     const int k = (Stage || !valid) ? t : walker_index(C, t);
@@ -315,10 +343,26 @@ __global__ void __launch_bounds__(kScanThreads, BP_DELTAP_MIN_BLOCKS) k_deltap(S
     track_displacement(C, k, p, true);
 }
 
+template <bool Split, bool Stage, bool Persist = false>
+__global__ void __launch_bounds__(kScanThreads, BP_DELTAP_MIN_BLOCKS) k_deltap(
+    SimConsts C,
+    DeltaArgs a)
+{
+    // one tile of blockDim.x particles per CTA, or, persistent (an unstaged
+    // launch of at most one resident wave: SimConsts::scan_persist), every
+    // gridDim.x-th tile from blockIdx.x on
+    if constexpr (Persist) {
+        for (int i0 = blockIdx.x * blockDim.x; i0 < C.n; i0 += gridDim.x * blockDim.x)
+            k_deltap_tile<Split, Stage>(C, a, i0);
+    } else {
+        k_deltap_tile<Split, Stage>(C, a, blockIdx.x * blockDim.x);
+    }
+}
+
 void launch_deltap(cudaStream_t st, const SimConsts &C, const DeltaArgs &a, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    BP_LAUNCH_SPLIT(k_deltap, (C.n + kScanThreads - 1) / kScanThreads, kScanThreads, st, C, a);
+    BP_LAUNCH_SPLIT(k_deltap, st, C, a);
     L->done(__func__);
 }
 
@@ -334,13 +378,17 @@ __device__ __forceinline__ bool post_slots(const SimConsts &C, bool stage)
 // in one walk over same-phase neighbours with 0 < r^2 <= h^2.
 // Om[i] = (omega, |omega|); Nm[i] = (h * n, rho_i).
 template <bool Split, bool Stage>
-__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(SimConsts C, const float4 *__restrict__ P,
-                                                         const float4 *__restrict__ V,
-                                                         const float *__restrict__ rho, const int *__restrict__ off,
-                                                         float4 *__restrict__ Om, float4 *__restrict__ Nm)
+__device__ __forceinline__ void k_post_a_tile(
+    const SimConsts &C,
+    const float4 *__restrict__ P,
+    const float4 *__restrict__ V,
+    const float *__restrict__ rho,
+    const int *__restrict__ off,
+    float4 *__restrict__ Om,
+    float4 *__restrict__ Nm,
+    int i0)
 {
     StageShared &S = stage_shared();
-    const int i0 = blockIdx.x * kScanThreads;
     const int g = Stage ? stage_block(C, P, off, i0, S) : -1;
     const int t = i0 + threadIdx.x;  // the slot of the list passes B and C read
     if (t >= C.n) return;
@@ -410,6 +458,27 @@ __global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(Sim
     }
 }
 
+template <bool Split, bool Stage, bool Persist = false>
+__global__ void __launch_bounds__(kScanThreads, BP_SCAN_MIN_BLOCKS) k_post_a(
+    SimConsts C,
+    const float4 *__restrict__ P,
+    const float4 *__restrict__ V,
+    const float *__restrict__ rho,
+    const int *__restrict__ off,
+    float4 *__restrict__ Om,
+    float4 *__restrict__ Nm)
+{
+    // one tile of blockDim.x particles per CTA, or, persistent (an unstaged
+    // launch of at most one resident wave: SimConsts::scan_persist), every
+    // gridDim.x-th tile from blockIdx.x on
+    if constexpr (Persist) {
+        for (int i0 = blockIdx.x * blockDim.x; i0 < C.n; i0 += gridDim.x * blockDim.x)
+            k_post_a_tile<Split, Stage>(C, P, V, rho, off, Om, Nm, i0);
+    } else {
+        k_post_a_tile<Split, Stage>(C, P, V, rho, off, Om, Nm, blockIdx.x * blockDim.x);
+    }
+}
+
 // Passes B and C: the number of recorded neighbours of particle i (its list
 // in slot t, k_post_a), or kWalkCells when it must walk its cells (no lists,
 // or they overflowed).  Solids and indices past the end need neither (0).
@@ -427,14 +496,17 @@ __device__ __forceinline__ int post_list_count(const SimConsts &C, const float4 
 // v'' = v' + F dt, exactly the reference's sequence (in-place update followed
 // by newVelocities = velocities + F dt).  Solids pass through.
 template <bool Split, bool Stage>
-__global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_b(SimConsts C, const float4 *__restrict__ P,
-                                                         const float4 *__restrict__ V,
-                                                         const float4 *__restrict__ Om,
-                                                         const float4 *__restrict__ Nm,
-                                                         const int *__restrict__ off, float4 *__restrict__ Vout)
+__device__ __forceinline__ void k_post_b_tile(
+    const SimConsts &C,
+    const float4 *__restrict__ P,
+    const float4 *__restrict__ V,
+    const float4 *__restrict__ Om,
+    const float4 *__restrict__ Nm,
+    const int *__restrict__ off,
+    float4 *__restrict__ Vout,
+    int i0)
 {
     StageShared &S = stage_shared();
-    const int i0 = blockIdx.x * kScanThreads;
     const int t = i0 + threadIdx.x;
     const int i = (Stage || t >= C.n) ? t : walker_index(C, t);
     const int cnt = post_list_count(C, P, i, t);
@@ -495,16 +567,41 @@ __global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_b(S
     if (slots) C.cls_vb[t] = v4;  // pass C's neighbour velocities
 }
 
+template <bool Split, bool Stage, bool Persist = false>
+__global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_b(
+    SimConsts C,
+    const float4 *__restrict__ P,
+    const float4 *__restrict__ V,
+    const float4 *__restrict__ Om,
+    const float4 *__restrict__ Nm,
+    const int *__restrict__ off,
+    float4 *__restrict__ Vout)
+{
+    // one tile of blockDim.x particles per CTA, or, persistent (an unstaged
+    // launch of at most one resident wave: SimConsts::scan_persist), every
+    // gridDim.x-th tile from blockIdx.x on
+    if constexpr (Persist) {
+        for (int i0 = blockIdx.x * blockDim.x; i0 < C.n; i0 += gridDim.x * blockDim.x)
+            k_post_b_tile<Split, Stage>(C, P, V, Om, Nm, off, Vout, i0);
+    } else {
+        k_post_b_tile<Split, Stage>(C, P, V, Om, Nm, off, Vout, blockIdx.x * blockDim.x);
+    }
+}
+
 // Pass C: XSPH viscosity (fluidXSph): same phase, j != i, r^2 <= h^2 (r = 0
 // included).  Textbook mode weights each neighbour by its volume m_j / rho_j.
 template <bool Split, bool Stage>
-__global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_c(SimConsts C, const float4 *__restrict__ P,
-                                                         const float4 *__restrict__ V,
-                                                         const int *__restrict__ off, const float *__restrict__ mass,
-                                                         const float *__restrict__ rho, float4 *__restrict__ Vout)
+__device__ __forceinline__ void k_post_c_tile(
+    const SimConsts &C,
+    const float4 *__restrict__ P,
+    const float4 *__restrict__ V,
+    const int *__restrict__ off,
+    const float *__restrict__ mass,
+    const float *__restrict__ rho,
+    float4 *__restrict__ Vout,
+    int i0)
 {
     StageShared &S = stage_shared();
-    const int i0 = blockIdx.x * kScanThreads;
     const int t = i0 + threadIdx.x;
     const int i = (Stage || t >= C.n) ? t : walker_index(C, t);
     const int cnt = post_list_count(C, P, i, t);
@@ -546,25 +643,46 @@ __global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_c(S
     Vout[i] = make_float4(v.x, v.y, v.z, vi4.w);
 }
 
+template <bool Split, bool Stage, bool Persist = false>
+__global__ void __launch_bounds__(kScanThreads, BP_POSTBC_MIN_BLOCKS) k_post_c(
+    SimConsts C,
+    const float4 *__restrict__ P,
+    const float4 *__restrict__ V,
+    const int *__restrict__ off,
+    const float *__restrict__ mass,
+    const float *__restrict__ rho,
+    float4 *__restrict__ Vout)
+{
+    // one tile of blockDim.x particles per CTA, or, persistent (an unstaged
+    // launch of at most one resident wave: SimConsts::scan_persist), every
+    // gridDim.x-th tile from blockIdx.x on
+    if constexpr (Persist) {
+        for (int i0 = blockIdx.x * blockDim.x; i0 < C.n; i0 += gridDim.x * blockDim.x)
+            k_post_c_tile<Split, Stage>(C, P, V, off, mass, rho, Vout, i0);
+    } else {
+        k_post_c_tile<Split, Stage>(C, P, V, off, mass, rho, Vout, blockIdx.x * blockDim.x);
+    }
+}
+
 void launch_post_a(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float *rho,
                    const int *off, float4 *Om, float4 *Nm, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    BP_LAUNCH_SPLIT(k_post_a, (C.n + kScanThreads - 1) / kScanThreads, kScanThreads, st, C, P, V, rho, off, Om, Nm);
+    BP_LAUNCH_SPLIT(k_post_a, st, C, P, V, rho, off, Om, Nm);
     L->done(__func__);
 }
 void launch_post_b(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float4 *Om,
                    const float4 *Nm, const int *off, float4 *Vout, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    BP_LAUNCH_SPLIT(k_post_b, (C.n + kScanThreads - 1) / kScanThreads, kScanThreads, st, C, P, V, Om, Nm, off, Vout);
+    BP_LAUNCH_SPLIT(k_post_b, st, C, P, V, Om, Nm, off, Vout);
     L->done(__func__);
 }
 void launch_post_c(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
                    const float *mass, const float *rho, float4 *Vout, LaunchLog *L)
 {
     if (C.n <= 0) return;
-    BP_LAUNCH_SPLIT(k_post_c, (C.n + kScanThreads - 1) / kScanThreads, kScanThreads, st, C, P, V, off, mass, rho, Vout);
+    BP_LAUNCH_SPLIT(k_post_c, st, C, P, V, off, mass, rho, Vout);
     L->done(__func__);
 }
 

@@ -102,6 +102,10 @@ static bp_status check_params(const bp_params *p)
     if (!std::isfinite(p->bending_stiffness)) return fail(BP_ERR_INVALID_ARGUMENT, "bending_stiffness is not finite");
     if (p->scorr_n < 0 || p->scorr_n > 16) return fail(BP_ERR_INVALID_ARGUMENT, "scorr_n must be in [0, 16]");
     if (!(p->neighbor_skin >= 0.f)) return fail(BP_ERR_INVALID_ARGUMENT, "neighbor_skin < 0");
+    if (p->scan_block != 0 && p->scan_block != 64 && p->scan_block != 128 && p->scan_block != 256)
+        return fail(BP_ERR_INVALID_ARGUMENT, "scan_block must be 0, 64, 128 or 256");
+    if (p->scan_persistent != 0 && p->scan_persistent != 1)
+        return fail(BP_ERR_INVALID_ARGUMENT, "scan_persistent must be 0 or 1");
     return BP_OK;
 }
 
@@ -180,6 +184,8 @@ SimConsts bp::make_consts(const bp_solver *s, float sdt)
     C.scene_of = s->scene_of;
     C.stage = (p.walk_options & BP_WALK_NO_STAGING) ? 0 : 1;
     C.split = (p.walk_options & BP_WALK_NO_SPLIT) ? 0 : 1;
+    C.scan_block = p.scan_block > 0 ? p.scan_block : 256;
+    C.scan_persist = p.scan_persistent ? 1 : 0;
     if (p.neighbor_skin > 0.f && !s->tape && s->vl) {  // Verlet lists (enqueue_substep decides per launch)
         C.vl = s->vl;
         C.vl_count = s->vl_count;
@@ -649,6 +655,13 @@ extern "C" bp_status bp_solver_destroy(bp_solver *s)
     if (!s) return BP_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
     delete s;
+    return BP_OK;
+}
+
+extern "C" bp_status bp_solver_get_params(const bp_solver *s, bp_params *out)
+{
+    if (!s || !out) return fail(BP_ERR_INVALID_ARGUMENT, "solver or output is NULL");
+    *out = s->prm;
     return BP_OK;
 }
 

@@ -204,6 +204,27 @@ __device__ __forceinline__ int stage_block(const SimConsts &C, const float4 *__r
     return (G == 2 && t >= S.first1) ? 1 : 0;
 }
 
+// Launch of a neighbour-scan kernel over C.n particles: a staged launch takes
+// one kWalkThreads CTA per tile (its staging is sized for that); an unstaged
+// one C.scan_block threads per CTA, and with C.scan_persist no more CTAs than
+// the GPU holds at once, each striding over the tiles (the kernels loop over
+// tiles of blockDim.x particles from blockIdx.x on).
+template <class... KArgs, class... Args>
+inline void launch_scan(void (*kernel)(KArgs...), const SimConsts &C, size_t smem, cudaStream_t st, Args &&...args)
+{
+    const int block = C.stage ? kWalkThreads : C.scan_block;
+    int grid = (C.n + block - 1) / block;
+    if (!C.stage && C.scan_persist) {
+        int per = 0, dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, smem);
+        const int resident = (per > 0 ? per : 1) * (sms > 0 ? sms : 1);
+        grid = grid < resident ? grid : resident;
+    }
+    kernel<<<grid, block, smem, st>>>(static_cast<Args &&>(args)...);
+}
+
 // Shared-memory index of candidate run [b, e) of column k for group g, or -1.
 __device__ __forceinline__ int staged_index(const StageShared &S, int g, int k, int b, int e)
 {

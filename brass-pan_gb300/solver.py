@@ -170,13 +170,15 @@ class ParticleSolver:
                 "cells_displaced": int(out[3]), "alias_classes": int(out[4])}
 
     def autotune(self, num_substeps: int, dt: float, iterations: int) -> tuple[int, list[float]]:
-        """Keep the fastest walk variant for this scene; returns it and the
-        trial times (ms) of the eight candidates."""
+        """Keep the fastest walk variant and scan launch shape for this scene;
+        returns the walk options and the trial times (ms) of the eleven
+        candidates (bp_solver_autotune); the launch shape chosen is in
+        self.params (scan_block, scan_persistent)."""
         opt = C.c_int32()
-        ms = (C.c_float * 8)()
+        ms = (C.c_float * 11)()
         abi.check(self.lib, self.lib.bp_solver_autotune(self.handle, num_substeps, C.c_float(dt), iterations,
                                                         C.byref(opt), ms))
-        self.params.walk_options = opt.value
+        abi.check(self.lib, self.lib.bp_solver_get_params(self.handle, C.byref(self.params)))
         return opt.value, list(ms)
 
     # -- differentiable rollouts ------------------------------------------------------

@@ -129,7 +129,14 @@ typedef struct bp_params {
                                     (0 disables them; results are identical either way): 0 */
     int32_t walk_options;        /* BP_WALK_* tuning switches of the neighbour walks: BP_WALK_NO_STAGING */
     float bending_stiffness;     /* 0.8 (bending.cuh:71) */
-    int32_t reserved[5];
+    /* Launch shape of the neighbour-scan kernels when they do not stage
+     * (BP_WALK_NO_STAGING; results are identical under every shape):
+     * threads per CTA (0 = 256; 64, 128 or 256), and persistent launches
+     * (1: no more CTAs than fit on the GPU at once, each looping over the
+     * 256-, 128- or 64-particle tiles).  bp_solver_autotune picks them. */
+    int32_t scan_block;          /* 0 */
+    int32_t scan_persistent;     /* 0 */
+    int32_t reserved[3];
 } bp_params;
 
 /* Fills `p` with the reference's literals for a scene of the given particle
@@ -186,6 +193,11 @@ bp_status bp_solver_step(bp_solver *s, float dt, int32_t num_substeps, int32_t i
 
 /* Replaces the parameters (takes effect at the next update). */
 bp_status bp_solver_set_params(bp_solver *s, const bp_params *params);
+
+/* Copies the solver's current parameters (for instance the walk options and
+ * scan launch shape bp_solver_autotune chose).  No counterpart in the
+ * reference, whose parameters are literals. */
+bp_status bp_solver_get_params(const bp_solver *s, bp_params *out);
 
 /* queryOriginalParticleId / queryNewParticleId (particlesolver.cuh:352-366). */
 bp_status bp_solver_query_original_particle_id(bp_solver *s, int32_t sorted_index, int32_t *out);
@@ -274,14 +286,18 @@ bp_status bp_solver_profile(bp_solver *s, int32_t num_substeps, float dt, int32_
 bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
                                uint64_t out_walks[5]);
 
-/* Picks the fastest neighbour-walk variant (BP_WALK_* combinations; all give
- * identical results) for this solver's scene and step configuration: each
+/* Picks the fastest neighbour-walk variant and scan launch shape for this
+ * solver's scene and step configuration (all give identical results): each
  * candidate runs one update from the current state, timed with CUDA events,
- * and the state is put back after every trial.  The choice is kept in the
- * solver's parameters and written to *out_walk_options; out_ms (or NULL)
- * receives the time of each of the 8 combinations of the three BP_WALK_NO_*
- * bits, in the order 0, NO_STAGING, NO_SPLIT, NO_LISTS, NO_STAGING|NO_SPLIT,
- * NO_STAGING|NO_LISTS, NO_SPLIT|NO_LISTS, all three.  No counterpart in the
+ * and the state is put back after every trial.  First the 8 combinations of
+ * the three BP_WALK_NO_* bits at the default launch shape, in the order 0,
+ * NO_STAGING, NO_SPLIT, NO_LISTS, NO_STAGING|NO_SPLIT, NO_STAGING|NO_LISTS,
+ * NO_SPLIT|NO_LISTS, all three; then, when the fastest of them does not
+ * stage, its unstaged scans with 128 and with 64 threads per CTA and with
+ * persistent 256-thread CTAs (bp_params.scan_block, .scan_persistent).  The
+ * choice is kept in the solver's parameters and its walk options written to
+ * *out_walk_options; out_ms (or NULL) receives the 11 trial times in that
+ * order (0 for a launch-shape trial not run).  No counterpart in the
  * reference. */
 bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
                              int32_t *out_walk_options, float *out_ms);

@@ -386,8 +386,8 @@ def test_alias_classes_fall_back_past_the_reach(bp, gpu):
 
 
 def test_autotune_keeps_state_and_results(bp, gpu):
-    """The autotuner's trial updates leave the state as it was, and the variant
-    it keeps gives the same bits as the default walk."""
+    """The autotuner's trial updates leave the state as it was, and the walk
+    variant and launch shape it keeps give the same bits as the defaults."""
     abi = bp.abi
     scene = small_mixed_scene(bp, seed=21)
     a = bp.ParticleSolver(scene, bp.make_params(scene))
@@ -398,8 +398,10 @@ def test_autotune_keeps_state_and_results(bp, gpu):
     opt, ms = a.autotune(2, DT, 4)
     np.testing.assert_array_equal(a.positions(), x0)
     assert 0 <= opt <= (abi.BP_WALK_NO_SPLIT | abi.BP_WALK_NO_LISTS | abi.BP_WALK_NO_STAGING)
-    assert len(ms) == 8
-    assert all(t > 0 for t in ms)
+    assert len(ms) == 11
+    assert all(t > 0 for t in ms[:8])
+    assert a.params.scan_block in (0, 64, 128, 256) and a.params.scan_persistent in (0, 1)
+    assert all(t > 0 for t in ms[8:]) == bool(opt & abi.BP_WALK_NO_STAGING)
     for s in (a, b):
         for _ in range(3):
             s.update(2, DT, 4)
@@ -407,6 +409,26 @@ def test_autotune_keeps_state_and_results(bp, gpu):
     np.testing.assert_array_equal(a.velocities(), b.velocities())
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("shape", [(128, 0), (64, 0), (256, 1), (128, 1)])
+def test_scan_launch_shapes_are_bit_identical(bp, gpu, shape):
+    """Unstaged scans with other CTA sizes, or persistent CTAs striding over
+    the tiles, give the same bits as the default launch."""
+    abi = bp.abi
+    scene = small_mixed_scene(bp, seed=23)
+    base = bp.make_params(scene, walk_options=abi.BP_WALK_NO_STAGING)
+    other = bp.make_params(scene, walk_options=abi.BP_WALK_NO_STAGING, scan_block=shape[0],
+                           scan_persistent=shape[1])
+    outs = []
+    for p in (base, other):
+        g = bp.ParticleSolver(scene, p)
+        for _ in range(4):
+            g.update(2, DT, 4)
+        outs.append((g.positions(), g.velocities()))
+        g.close()
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
 def test_snapshot_resume_is_bit_identical(bp, gpu):
