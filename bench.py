@@ -283,8 +283,9 @@ def kernel_roofline(torch, solver, n, workload, flush, value, prof_steps=3):
 def run_sample(bp, torch, stream, flush, local, name, scene, params, frames, warmup, pre_frames=0,
                reference_cuda=False):
     """One more workload, timed like the headline one: `pre_frames` untimed
-    updates to reach the regime sampled, `warmup` more, then `frames` timed
-    updates (CUDA events on the solver's stream, L2 flushed before each),
+    updates to reach the regime sampled, `warmup` more, the autotuner, one
+    more untimed update, then `frames` timed updates (CUDA events on the
+    solver's stream, L2 flushed before each),
     clocks sampled meanwhile; the roofline of its top kernel; and, with
     reference_cuda, the reference's CUDA step timed from the same state."""
     n = scene.num_particles
@@ -296,6 +297,10 @@ def run_sample(bp, torch, stream, flush, local, name, scene, params, frames, war
             state = (solver.positions(), solver.velocities()) if (reference_cuda and pre_frames) else None
             for _ in range(warmup):
                 solver.update(SUBSTEPS, DT, ITERATIONS)
+            opt, _ = solver.autotune(SUBSTEPS, DT, ITERATIONS)  # as the headline workload
+            tuned = {"walk_options": opt, "scan_block": int(solver.params.scan_block),
+                     "scan_persistent": int(solver.params.scan_persistent)}
+            solver.update(SUBSTEPS, DT, ITERATIONS)  # captures the chosen variant's graph
             with ClockSampler(local) as clocks:
                 ms = timed_steps(torch, stream, flush, frames, lambda: solver.update(SUBSTEPS, DT, ITERATIONS))
             value = n * SUBSTEPS * frames / (ms / 1e3)
@@ -304,7 +309,8 @@ def run_sample(bp, torch, stream, flush, local, name, scene, params, frames, war
             errors = solver.device_errors()
     finally:
         solver.close()
-    out = {"workload": name, "particles": n, "frames_before": pre_frames, "warmup": warmup, "steps": frames,
+    out = {"workload": name, "particles": n, "frames_before": pre_frames, "warmup": warmup + 1, "steps": frames,
+           "autotune": tuned,
            "value": value, "unit": "particle-substeps/s", "ms_per_step": ms / frames, "roofline": roofline,
            "top_stages_ms_per_step": dict(list(stages.items())[:6]), "neighbor_walks": walks,
            "device_errors": errors, "clocks": clocks.summary()}
