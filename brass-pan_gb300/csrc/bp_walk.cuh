@@ -48,9 +48,12 @@ constexpr int kWalkThreads = 256;
 #endif
 constexpr int kChunkUnroll = BP_CHUNK_UNROLL;
 // Candidate tests of a chunk gathered four at a time into a nibble of
-// constant bit positions, then shifted into the chunk mask once.
+// constant bit positions, then shifted into the chunk mask once (measured on
+// the mixed scene against one variable shift per candidate: lambda 5.73 ->
+// 5.60 ms per frame early, 6.96 -> 6.73 late; the step 222.0 -> 225.2 M and
+// 133.5 -> 137.3 M particle-substeps/s).  0 keeps the per-candidate form.
 #ifndef BP_CHUNK_NIBBLES
-#define BP_CHUNK_NIBBLES 0
+#define BP_CHUNK_NIBBLES 1
 #endif
 
 // The test bits of candidates [0, cnt) of a chunk read from s: bit t set when
