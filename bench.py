@@ -460,8 +460,8 @@ def run_batch(bp, torch, stream, flush, steps, warmup, seed=0):
             "batched_vs_loop": ms_loop / ms_batch, "ms_per_step": ms_batch / steps,
             "loop_ms_per_step": ms_loop / steps, "launches_per_step": launches_batch,
             "loop_launches_per_step": launches_loop, "device_errors": errors, "steps": steps,
-            "autotune": {"walk_options": tuned, "scan_block": int(batch_shape[0]), "scan_persistent": int(batch_shape[1]),
-                         "trial_ms": [round(t, 3) for t in trial_ms]}}
+            "autotune": {"walk_options": tuned, "scan_block": int(batch_shape[0]),
+                         "scan_persistent": int(batch_shape[1]), "trial_ms": [round(t, 3) for t in trial_ms]}}
 
 
 class ClockSampler:

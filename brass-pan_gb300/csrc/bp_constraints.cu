@@ -341,9 +341,11 @@ __global__ void __launch_bounds__(kWalkThreads, BP_SCAN_MIN_BLOCKS) k_particle_c
     // gridDim.x-th tile from blockIdx.x on
     if constexpr (Persist) {
         for (int i0 = blockIdx.x * blockDim.x; i0 < C.n; i0 += gridDim.x * blockDim.x)
-            k_particle_collision_tile<Split>(C, P, Xs, w, off, tile_solid, solid_prefix, solid_list, solid_pos, solid_near, solids_apart, Pout, i0);
+            k_particle_collision_tile<Split>(C, P, Xs, w, off, tile_solid, solid_prefix, solid_list, solid_pos,
+                                             solid_near, solids_apart, Pout, i0);
     } else {
-        k_particle_collision_tile<Split>(C, P, Xs, w, off, tile_solid, solid_prefix, solid_list, solid_pos, solid_near, solids_apart, Pout, blockIdx.x * blockDim.x);
+        k_particle_collision_tile<Split>(C, P, Xs, w, off, tile_solid, solid_prefix, solid_list, solid_pos,
+                                         solid_near, solids_apart, Pout, blockIdx.x * blockDim.x);
     }
 }
 
@@ -404,14 +406,15 @@ void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4
         launch_scan(k_particle_collision<false>, C, stage_bytes(C), st, C, P, Xs, w, off, tile_solid, solid_prefix,
                     solid_list, solid_pos, near, apart, Pout);
     L->done(__func__);
-    if (apart) {
-        const int sg = (nsolid + kWalkThreads - 1) / kWalkThreads;
+    if (apart) {  // the unstaged scans' CTA size (SimConsts::scan_block) here too
+        const int sb = C.scan_block > 0 ? C.scan_block : kWalkThreads;
+        const int sg = (nsolid + sb - 1) / sb;
         if (C.split)
-            k_particle_collision_solids<true><<<sg, kWalkThreads, 0, st>>>(C, nsolid, P, Xs, w, off, solid_prefix,
-                                                                          solid_list, Pout);
+            k_particle_collision_solids<true><<<sg, sb, 0, st>>>(C, nsolid, P, Xs, w, off, solid_prefix, solid_list,
+                                                                Pout);
         else
-            k_particle_collision_solids<false><<<sg, kWalkThreads, 0, st>>>(C, nsolid, P, Xs, w, off, solid_prefix,
-                                                                           solid_list, Pout);
+            k_particle_collision_solids<false><<<sg, sb, 0, st>>>(C, nsolid, P, Xs, w, off, solid_prefix, solid_list,
+                                                                 Pout);
         L->done("launch_particle_collision_solids");
     }
 }

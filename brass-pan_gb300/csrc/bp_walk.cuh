@@ -373,7 +373,8 @@ __device__ __forceinline__ void walk_run_cls(int qb, int e, int qi, int i, int j
         for (int q0 = qb; q0 < e; q0 += 32) {
             const int cnt = min(32, e - q0);
             const float4 *s = src + q0;
-            unsigned bits = chunk_bits(cnt, s, [&](int t, float4 p) { return test(q0 + t == qi ? i : -1 - (q0 + t), p); });
+            unsigned bits =
+                chunk_bits(cnt, s, [&](int t, float4 p) { return test(q0 + t == qi ? i : -1 - (q0 + t), p); });
 #pragma unroll 1
             while (bits) {
                 const int t = __ffs(bits) - 1;
