@@ -9,10 +9,11 @@
 // the same positions).
 //
 // Supported stages: prediction and reorder, planes (stabilisation and
-// collision), wind, reference-mode fluid density / lambda / position
-// correction (with s_corr and the per-pair clamp), distance constraints,
-// shape matching (rotation differentiated at its fixed point), immovables,
-// the velocity update and reference-mode XSPH.
+// collision), wind, particle-particle contacts with friction, reference-mode
+// fluid density / lambda / position correction (with s_corr and the per-pair
+// clamp), distance constraints, dihedral bending, shape matching (rotation
+// differentiated at its fixed point), immovables, the velocity update,
+// vorticity confinement, Akinci tension and reference-mode XSPH.
 #include "bp_dual.cuh"
 #include "bp_internal.h"
 #include "bp_walk.cuh"
@@ -462,7 +463,8 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_lambda(SimConsts C, const 
                                                              const float *__restrict__ rho, const int *__restrict__ off,
                                                              const float *__restrict__ gLam,
                                                              const float4 *__restrict__ gPart,
-                                                             const float4 *__restrict__ gOut, float4 *__restrict__ gIn)
+                                                             const float4 *__restrict__ gOut,
+                                                             const float *__restrict__ gRho, float4 *__restrict__ gIn)
 {
     StageShared &S = stage_shared();
     const int g = stage_block(C, P, off, blockIdx.x * kWalkThreads, S);
@@ -475,8 +477,9 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_lambda(SimConsts C, const 
     const float rho0 = rest_density(C, sc);
     auto rho_bar = [&](int j, int phj) {
         if (phj > 0) return 0.f;  // solids: lambda is 0 whatever the density
-        if (C.clamp_c && !(rho[j] / rho0 - 1.0f > 0.f)) return 0.f;
-        return -gLam[j] / (C.lambda_den * rho0);
+        const float ext = gRho ? gRho[j] : 0.f;  // the density's gradient through the post passes
+        if (C.clamp_c && !(rho[j] / rho0 - 1.0f > 0.f)) return ext;
+        return ext - gLam[j] / (C.lambda_den * rho0);
     };
     const float rbk = rho_bar(k, phk);
     const float mk = mass[k] * (phk < 0 ? 1.f : C.solid_scale);
@@ -678,6 +681,413 @@ __global__ void __launch_bounds__(kAdjSmThreads) k_adj_shape_matching(RigidArgs 
     }
 }
 
+// ---- particle-particle contacts (collide_one, bp_constraints.cu) ----
+// Only the mover i changes: p_i' = p_i + sum_j dx_ij + (1 / c_i) sum_{j counted}
+// f_ij, where dx_ij is the mass-weighted projection of the pair, f_ij its
+// friction move (from the substep-start positions Xs) and c_i the number of
+// counted pairs of i (piecewise constant: no derivative).  Inputs of a pair:
+// both predicted positions, both start positions, both inverse scaled masses.
+
+// The pair filter of collide_one: different phases, one of them solid, closer
+// than two radii and not coincident.
+__device__ __forceinline__ bool contact_pair(const SimConsts &C, float3 pi, int phi, float4 pj4)
+{
+    const int phj = phase_of(pj4);
+    const float d2 = len2(pi - f3(pj4));
+    const float r = C.radius;
+    return phi != phj && (phi > 0 || phj > 0) && d2 < r * r * 4.0f && d2 > 1e-5f;
+}
+
+// Does the pair count for friction (collide_one's test, in its float operations)?
+__device__ __forceinline__ bool contact_counted(const SimConsts &C, float3 pi, float wi, float3 pj, float wj)
+{
+    const float r = C.radius;
+    const float3 diff = pi - pj;
+    const float dist = __fsqrt_rn(len2(diff));
+    const float w1 = __fdiv_rn(wi, __fadd_rn(wi, wj));
+    const float3 dxi = w1 * (diff * __fsub_rn(__fdiv_rn(2.0f * r, dist), 1.0f));
+    return len2(dxi) > r * r * 0.001f * 0.001f;
+}
+
+// The move of mover i from partner j, on dual numbers; count: c_i.
+template <int N>
+__device__ __forceinline__ V3<Dual<N>> dcontact(const SimConsts &C, const V3<Dual<N>> &pi, const V3<Dual<N>> &xi,
+                                const Dual<N> &wi, const V3<Dual<N>> &pj, const V3<Dual<N>> &xj,
+                                const Dual<N> &wj, bool counted, int count)
+{
+    const float r = C.radius;
+    const V3<Dual<N>> diff = pi - pj;
+    const Dual<N> dist = dsqrt(dot(diff, diff));
+    const Dual<N> sw = wi + wj;
+    const Dual<N> w1 = wi / sw, w2 = wj / sw;
+    const V3<Dual<N>> proj = scale(diff, dconst<N>(2.0f * r) / dist + (-1.0f));
+    const V3<Dual<N>> dxi = scale(proj, w1);
+    if (!counted || count <= 0) return dxi;
+    const Dual<N> dxi2 = dot(dxi, dxi);
+    const V3<Dual<N>> t1 = (dxi + pi - xi) - (scale(proj, -w2) + pj - xj);
+    const V3<Dual<N>> nn = scale(diff, dconst<N>(1.0f) / dist);
+    const V3<Dual<N>> tdx = t1 - scale(nn, dot(t1, nn));
+    const Dual<N> tl2 = dot(tdx, tdx);
+    V3<Dual<N>> f = scale(tdx, -w1);
+    if (!(tl2.v <= C.fs * C.fs * dxi2.v)) f = scale(f, dmin(C.fd * dsqrt(dxi2 / tl2), 1.0f));
+    return dxi + scale(f, 1.0f / (float)count);
+}
+
+// Pass A: c_k, from the same pairs and float operations as the forward.
+__global__ void __launch_bounds__(kWalkThreads) k_adj_contact_count(SimConsts C, const float4 *__restrict__ P,
+                                                                    const float *__restrict__ w,
+                                                                    const int *__restrict__ off, int *__restrict__ count)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= C.n) return;
+    const float4 pk4 = P[k];
+    const float3 pk = f3(pk4);
+    const int phk = phase_of(pk4);
+    const float wk = w[k];
+    int c = 0;
+    auto test = [&](int j, float4 pj4) { return j != k && contact_pair(C, pk, phk, pj4); };
+    auto body = [&](int j, float4 pj4) { c += contact_counted(C, pk, wk, f3(pj4), w[j]) ? 1 : 0; };
+    walk_neighbors<true>(k, pk, 0, P, grid_view(C, scene_index(C, k), off), C, nullptr, -1, test, body);
+    count[k] = c;
+}
+
+// Pass B: gIn = gOut + the pairs' Jacobians: those of k's own moves (its
+// inputs as mover) and those of its neighbours' moves (its inputs as partner),
+// gathered over the same pairs (the filter is symmetric).  Start-position and
+// mass gradients add to gXs and gW.
+__global__ void __launch_bounds__(kWalkThreads) k_adj_contact(SimConsts C, const float4 *__restrict__ P,
+                                                              const float4 *__restrict__ Xs,
+                                                              const float *__restrict__ w, const int *__restrict__ off,
+                                                              const int *__restrict__ count,
+                                                              const float4 *__restrict__ gOut,
+                                                              float4 *__restrict__ gIn, float4 *__restrict__ gXs,
+                                                              float *__restrict__ gW)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= C.n) return;
+    const float4 pk4 = P[k];
+    const float3 pk = f3(pk4), xk = ld3(Xs, k), gk = ld3(gOut, k);
+    const int phk = phase_of(pk4);
+    const float wk = w[k];
+    const int ck = count[k];
+    float acc[7] = {gk.x, gk.y, gk.z, 0.f, 0.f, 0.f, 0.f};  // p_k, X_k, w_k
+    auto test = [&](int j, float4 pj4) { return j != k && contact_pair(C, pk, phk, pj4); };
+    auto body = [&](int j, float4 pj4) {
+        const float3 pj = f3(pj4), xj = ld3(Xs, j);
+        const float wj = w[j];
+        {  // k moves
+            const V3<Dual<7>> out =
+                dcontact<7>(C, dv3var<7>(pk, 0), dv3var<7>(xk, 3), dvar<7>(wk, 6), dv3<7>(pj), dv3<7>(xj),
+                            dconst<7>(wj), contact_counted(C, pk, wk, pj, wj), ck);
+#pragma unroll
+            for (int q = 0; q < 7; ++q) acc[q] += vjp(out, gk, q);
+        }
+        {  // j moves, k is its partner
+            const V3<Dual<7>> out =
+                dcontact<7>(C, dv3<7>(pj), dv3<7>(xj), dconst<7>(wj), dv3var<7>(pk, 0), dv3var<7>(xk, 3),
+                            dvar<7>(wk, 6), contact_counted(C, pj, wj, pk, wk), __ldg(count + j));
+            const float3 gj = ld3(gOut, j);
+#pragma unroll
+            for (int q = 0; q < 7; ++q) acc[q] += vjp(out, gj, q);
+        }
+    };
+    walk_neighbors<true>(k, pk, 0, P, grid_view(C, scene_index(C, k), off), C, nullptr, -1, test, body);
+    gIn[k] = make_float4(acc[0], acc[1], acc[2], 0.f);
+    gXs[k] = f4(add3(ld3(gXs, k), make_float3(acc[3], acc[4], acc[5])));
+    gW[k] += acc[6];
+}
+
+// ---- dihedral bending (k_bending_terms, bp_constraints.cu) ----
+// The four corrections of a quad as functions of its corners' positions and
+// inverse scaled masses, on dual numbers (the same formulas as the forward).
+template <int N>
+__device__ __forceinline__ void dbending(const V3<Dual<N>> (&p)[4], const Dual<N> (&w)[4], float kb,
+                                         V3<Dual<N>> (&out)[4])
+{
+#pragma unroll
+    for (int c = 0; c < 4; ++c) out[c] = dv3<N>(make_float3(0.f, 0.f, 0.f));
+    const V3<Dual<N>> e = p[1] - p[0], a = p[2] - p[0], b = p[3] - p[0];
+    const V3<Dual<N>> ca = cross(e, a), cb = cross(e, b);
+    const Dual<N> la = dsqrt(dot(ca, ca)), lb = dsqrt(dot(cb, cb));
+    if (la.v <= 1e-5f || lb.v <= 1e-5f) return;
+    const Dual<N> ila = dconst<N>(1.0f) / la, ilb = dconst<N>(1.0f) / lb;
+    const V3<Dual<N>> n1 = scale(ca, ila), n2 = scale(cb, ilb);
+    const Dual<N> d = dclamp(dot(n1, n2), -1.0f, 1.0f);
+    const V3<Dual<N>> en1 = cross(e, n1), en2 = cross(e, n2);
+    const V3<Dual<N>> an1 = cross(a, n1), an2 = cross(a, n2);
+    const V3<Dual<N>> bn1 = cross(b, n1), bn2 = cross(b, n2);
+    V3<Dual<N>> q[4];
+    q[2] = scale(en2 - scale(en1, d), ila);
+    q[3] = scale(en1 - scale(en2, d), ilb);
+    q[1] = -scale(an2 - scale(an1, d), ila) - scale(bn1 - scale(bn2, d), ilb);
+    q[0] = (-q[1] - q[2]) - q[3];
+    Dual<N> den = w[0] * dot(q[0], q[0]);
+#pragma unroll
+    for (int c = 1; c < 4; ++c) den = den + w[c] * dot(q[c], q[c]);
+    if (den.v <= 1e-5f) return;
+    const Dual<N> num = dsqrt(dconst<N>(1.0f) - d * d) * (dacos(d) + (-3.141592f));
+    const Dual<N> s = num / den;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) out[c] = scale(q[c], (-w[c] * s) * kb);
+}
+
+// Per quad and corner c: the gradient of the loss through the quad's four
+// corrections with respect to corner c's position (xyz) and inverse scaled
+// mass (w), one dual evaluation per corner; laid out as the forward's terms.
+__global__ void k_adj_bending_terms(int nq, const int4 *__restrict__ quads, const float4 *__restrict__ Pin,
+                                    const float *__restrict__ w, const int *__restrict__ to_new, float kb,
+                                    const float4 *__restrict__ gOut, float4 *__restrict__ terms)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const int4 ids = quads[q];
+    const int id[4] = {to_new[ids.x], to_new[ids.y], to_new[ids.z], to_new[ids.w]};
+    float3 p[4], g[4];
+    float wv[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        p[c] = ld3(Pin, id[c]);
+        g[c] = ld3(gOut, id[c]);
+        wv[c] = w[id[c]];
+    }
+#pragma unroll 1
+    for (int ci = 0; ci < 4; ++ci) {
+        V3<Dual<4>> P[4], D[4];
+        Dual<4> W[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            P[c] = c == ci ? dv3var<4>(p[c], 0) : dv3<4>(p[c]);
+            W[c] = c == ci ? dvar<4>(wv[c], 3) : dconst<4>(wv[c]);
+        }
+        dbending<4>(P, W, kb, D);
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[k] += vjp(D[c], g[c], k);
+        terms[4 * (size_t)q + ci] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    }
+}
+
+// gP += the terms of each particle's quads (CSR order), gW += their w parts.
+__global__ void k_adj_bending_apply(int nn_, const int *__restrict__ node_ids, const int *__restrict__ ptr,
+                                    const int *__restrict__ inc, const float4 *__restrict__ terms,
+                                    const int *__restrict__ to_new, float4 *__restrict__ gP, float *__restrict__ gW)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nn_) return;
+    const int i = to_new[node_ids[t]];
+    float3 g = ld3(gP, i);
+    float gw = gW[i];
+    for (int q = ptr[t]; q < ptr[t + 1]; ++q) {
+        const float4 c = terms[inc[q]];
+        g = add3(g, f3(c));
+        gw += c.w;
+    }
+    gP[i] = f4(g);
+    gW[i] = gw;
+}
+
+// ---- vorticity confinement and Akinci tension (k_post_a / k_post_b, bp_fluid.cu) ----
+// Over the fluid neighbours j of the same phase within h (r_ij = p_i - p_j != 0),
+// with G(r) the spiky gradient and H(r) its (even, symmetric) Jacobian:
+//   pass A: w_i = sum_j (v_j - v_i) x G(r_ij);  n_i = h sum_j G(r_ij) / rho_j
+//   pass B: eta_i = sum_j |w_j| G(r_ij);
+//           v_i' = v_i + dt eps (eta_i / |eta_i|) x w_i   (where |eta_i|^2 > 1e-3)
+//                + dt sum_j k_ij (F(|r_ij|) r_ij - gamma (n_i - n_j)),
+//           k_ij = 2 rho0 / (rho_i + rho_j), F(r) = -gamma A(r) / r (A: Akinci's spline).
+// Three gathers: eta-bar per particle; then pass B's adjoint (w-bar, n-bar,
+// rho-bar, positions); then pass A's (velocities, positions, rho-bar).  Each
+// sums a particle's terms as the mover and, through the symmetric pair set,
+// its terms as the neighbour of its neighbours' sums.
+
+// F(r) r and the product of its Jacobian F I + F' r r^T / |r| with u.
+struct AkinciD {
+    float F, Fp;
+};
+__device__ __forceinline__ AkinciD akinci_d(const SimConsts &C, float rl)
+{
+    const float t = (C.h - rl) * rl;
+    const float two = rl >= C.half_h ? 1.0f : 2.0f;
+    const float A = rl >= C.half_h ? C.c_akinci * t * t * t : 2.0f * C.c_akinci * t * t * t - C.c_akinci_off;
+    const float Ap = two * C.c_akinci * 3.0f * t * t * (C.h - 2.0f * rl);
+    AkinciD a;
+    a.F = -C.tension * A / rl;
+    a.Fp = -C.tension * (Ap / rl - A / (rl * rl));
+    return a;
+}
+__device__ __forceinline__ float3 akinci_jac_mul(const AkinciD &a, float3 r, float rl, float3 u)
+{
+    return add3(mul3(u, a.F), mul3(r, a.Fp * dotf(r, u) / rl));
+}
+__device__ __forceinline__ float3 cross_f(float3 a, float3 b)
+{
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+// The pass-A neighbours of fluid particle k: body(j, p_j, r = p_k - p_j, |r|).
+template <class B>
+__device__ __forceinline__ void post_pairs(const SimConsts &C, int k, float3 pk, int phk, const float4 *__restrict__ P,
+                                           const int *__restrict__ off, B &&body)
+{
+    auto test = [&](int j, float4 pj4) {
+        const float3 r = sub3(pk, f3(pj4));
+        const float d2 = dotf(r, r);
+        return j != k && phase_of(pj4) == phk && d2 <= C.h2 && d2 > 0.f;
+    };
+    auto term = [&](int j, float4 pj4) {
+        const float3 r = sub3(pk, f3(pj4));
+        body(j, r, sqrtf(dotf(r, r)));
+    };
+    walk_neighbors<true>(k, pk, 0, P, grid_view(C, scene_index(C, k), off), C, nullptr, -1, test, term);
+}
+
+// eta-bar_i and the w-bar of i's own confinement term (zero where it is off).
+__global__ void __launch_bounds__(kWalkThreads) k_adj_post_eta(SimConsts C, const float4 *__restrict__ P,
+                                                               const int *__restrict__ off,
+                                                               const float4 *__restrict__ Om,
+                                                               const float4 *__restrict__ gVb,
+                                                               float4 *__restrict__ etab, float4 *__restrict__ omb)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= C.n) return;
+    const float4 pk4 = P[k];
+    const int phk = phase_of(pk4);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (phk >= 0 || !C.use_vort) {
+        etab[k] = zero;
+        omb[k] = zero;
+        return;
+    }
+    float3 eta = make_float3(0.f, 0.f, 0.f);
+    post_pairs(C, k, f3(pk4), phk, P, off, [&](int j, float3 r, float rl) {
+        eta = add3(eta, mul3(spiky_d(C, r, rl).g, Om[j].w));
+    });
+    const float e2 = dotf(eta, eta);
+    if (!(e2 > 1e-3f)) {
+        etab[k] = zero;
+        omb[k] = zero;
+        return;
+    }
+    const float el = sqrtf(e2);
+    const float3 eh = mul3(eta, 1.0f / el), g = ld3(gVb, k), om = ld3(Om, k);
+    const float a = C.dt * C.vort_eps;
+    const float3 ehb = mul3(cross_f(om, g), a);  // (eta-hat x w) . g
+    etab[k] = f4(mul3(sub3(ehb, mul3(eh, dotf(eh, ehb))), 1.0f / el));
+    omb[k] = f4(mul3(cross_f(g, eh), a));
+}
+
+// Pass B's adjoint: w-bar (omb in, the full w-bar out in ombo), n-bar, rho-bar
+// and the position gradient (added to gX).
+__global__ void __launch_bounds__(kWalkThreads) k_adj_post_b(SimConsts C, const float4 *__restrict__ P,
+                                                             const int *__restrict__ off,
+                                                             const float4 *__restrict__ Om,
+                                                             const float4 *__restrict__ Nm,
+                                                             const float4 *__restrict__ gVb,
+                                                             const float4 *__restrict__ etab,
+                                                             const float4 *__restrict__ omb,
+                                                             float4 *__restrict__ ombo, float4 *__restrict__ nmb,
+                                                             float *__restrict__ gRho, float4 *__restrict__ gX)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= C.n) return;
+    const float4 pk4 = P[k];
+    const int phk = phase_of(pk4);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (phk >= 0) {
+        ombo[k] = zero;
+        nmb[k] = zero;
+        gRho[k] = 0.f;
+        return;
+    }
+    const float rho0 = rest_density(C, scene_index(C, k));
+    const float4 om4 = Om[k], nm4 = Nm[k];
+    const float3 gk = ld3(gVb, k), ek = ld3(etab, k), nk = f3(nm4);
+    const float rk = nm4.w, dt = C.dt, gam = C.tension;
+    float abs_omb = 0.f, rb = 0.f;
+    float3 pb = make_float3(0.f, 0.f, 0.f), nb = make_float3(0.f, 0.f, 0.f);
+    post_pairs(C, k, f3(pk4), phk, P, off, [&](int j, float3 r, float rl) {
+        const SpikyD sp = spiky_d(C, r, rl);
+        const float4 omj = Om[j], nmj = Nm[j];
+        if (C.use_vort) {
+            const float3 ej = ld3(etab, j);
+            pb = add3(pb, mul3(spiky_hess_mul(sp, r, rl, ek), omj.w));  // k's eta through r
+            pb = sub3(pb, mul3(spiky_hess_mul(sp, r, rl, ej), om4.w));  // j's eta through r_jk = -r
+            abs_omb -= dotf(ej, sp.g);                                   // j's eta: |w_k| G(-r)
+        }
+        if (C.use_akinci) {
+            const AkinciD ak = akinci_d(C, rl);
+            const float3 fco = mul3(r, ak.F);
+            const float3 gj = ld3(gVb, j), nj = f3(nmj);
+            const float sr = rk + nmj.w;
+            const float kk = 2.0f * rho0 / sr, kd = -2.0f * rho0 / (sr * sr);
+            // k moves: k_kj (fco(r) - gamma (n_k - n_j))
+            nb = sub3(nb, mul3(gk, gam * dt * kk));
+            rb += dt * kd * dotf(gk, sub3(fco, mul3(sub3(nk, nj), gam)));
+            pb = add3(pb, mul3(akinci_jac_mul(ak, r, rl, gk), dt * kk));
+            // j moves: k_jk (fco(-r) - gamma (n_j - n_k))
+            nb = add3(nb, mul3(gj, gam * dt * kk));
+            rb += dt * kd * dotf(gj, sub3(mul3(fco, -1.f), mul3(sub3(nj, nk), gam)));
+            pb = sub3(pb, mul3(akinci_jac_mul(ak, r, rl, gj), dt * kk));
+        }
+    });
+    float3 wb = ld3(omb, k);
+    if (om4.w > 0.f) wb = add3(wb, mul3(f3(om4), abs_omb / om4.w));
+    ombo[k] = f4(wb);
+    nmb[k] = f4(nb);
+    gRho[k] = rb;
+    gX[k] = f4(add3(ld3(gX, k), pb));
+}
+
+// Pass A's adjoint: gV = gVb + the velocity terms of w; positions to gX,
+// density to gRho.
+__global__ void __launch_bounds__(kWalkThreads) k_adj_post_a(SimConsts C, const float4 *__restrict__ P,
+                                                             const float4 *__restrict__ V, const int *__restrict__ off,
+                                                             const float *__restrict__ rho,
+                                                             const float4 *__restrict__ gVb,
+                                                             const float4 *__restrict__ ombo,
+                                                             const float4 *__restrict__ nmb,
+                                                             float4 *__restrict__ gV, float *__restrict__ gRho,
+                                                             float4 *__restrict__ gX)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= C.n) return;
+    const float4 pk4 = P[k];
+    const int phk = phase_of(pk4);
+    float3 gv = ld3(gVb, k);
+    if (phk >= 0) {
+        gV[k] = f4(gv);
+        return;
+    }
+    const float3 vk = ld3(V, k), wk = ld3(ombo, k), nk = ld3(nmb, k);
+    const float rk = rho[k], h = C.h;
+    float3 pb = make_float3(0.f, 0.f, 0.f);
+    float rb = 0.f;
+    post_pairs(C, k, f3(pk4), phk, P, off, [&](int j, float3 r, float rl) {
+        const SpikyD sp = spiky_d(C, r, rl);
+        const float3 vj = ld3(V, j);
+        if (C.use_vort) {
+            const float3 wj = ld3(ombo, j);
+            // k's w: (v_j - v_k) x G(r)
+            gv = sub3(gv, cross_f(sp.g, wk));
+            pb = add3(pb, spiky_hess_mul(sp, r, rl, cross_f(wk, sub3(vj, vk))));
+            // j's w: (v_k - v_j) x G(-r)
+            gv = sub3(gv, cross_f(sp.g, wj));
+            pb = sub3(pb, spiky_hess_mul(sp, r, rl, cross_f(wj, sub3(vk, vj))));
+        }
+        if (C.use_akinci) {
+            const float3 nj = ld3(nmb, j);
+            const float rj = rho[j];
+            pb = add3(pb, mul3(spiky_hess_mul(sp, r, rl, nk), h / rj));  // k's n: G(r) / rho_j
+            pb = sub3(pb, mul3(spiky_hess_mul(sp, r, rl, nj), h / rk));  // j's n: G(-r) / rho_k
+            rb += h / (rk * rk) * dotf(nj, sp.g);
+        }
+    });
+    gV[k] = f4(gv);
+    gRho[k] += rb;
+    gX[k] = f4(add3(ld3(gX, k), pb));
+}
+
 // ---- launchers ----
 
 static int blocks(int n, int t = 256) { return (n + t - 1) / t; }
@@ -727,11 +1137,13 @@ void adj_wind(cudaStream_t st, const SimConsts &C, const WindArgs &a, const floa
     k_adj_sum4<<<1, 1024, 0, st>>>(a.num_faces, FW, g_wind);
 }
 void adj_fluid(cudaStream_t st, const SimConsts &C, const float4 *Pin, const float *mass, const float *lam,
-               const float *rho, const int *off, const float4 *gOut, float *gLam, float4 *gPart, float4 *gIn)
+               const float *rho, const int *off, const float4 *gOut, const float *gRho, float *gLam, float4 *gPart,
+               float4 *gIn)
 {
     if (C.n <= 0) return;
-    k_adj_deltap<<<blocks(C.n, kWalkThreads), kWalkThreads, stage_bytes(C), st>>>(C, Pin, mass, lam, off, gOut, gLam, gPart);
-    k_adj_lambda<<<blocks(C.n, kWalkThreads), kWalkThreads, stage_bytes(C), st>>>(C, Pin, mass, rho, off, gLam, gPart, gOut, gIn);
+    const int b = blocks(C.n, kWalkThreads);
+    k_adj_deltap<<<b, kWalkThreads, stage_bytes(C), st>>>(C, Pin, mass, lam, off, gOut, gLam, gPart);
+    k_adj_lambda<<<b, kWalkThreads, stage_bytes(C), st>>>(C, Pin, mass, rho, off, gLam, gPart, gOut, gRho, gIn);
 }
 void adj_shape_matching(cudaStream_t st, const RigidArgs &a, const float4 *rot, const float4 *Pin, const int *to_new,
                         float4 *gP)
@@ -744,6 +1156,34 @@ void adj_xsph(cudaStream_t st, const SimConsts &C, const float4 *P, const float4
 {
     if (C.n <= 0) return;
     k_adj_xsph<<<blocks(C.n, kWalkThreads), kWalkThreads, stage_bytes(C), st>>>(C, P, V, off, gVout, gVin, gX);
+}
+
+void adj_contacts(cudaStream_t st, const SimConsts &C, const float4 *Pin, const float4 *Xs, const float *w,
+                  const int *off, int *count, const float4 *gOut, float4 *gIn, float4 *gXs, float *gW)
+{
+    if (C.n <= 0) return;
+    k_adj_contact_count<<<blocks(C.n, kWalkThreads), kWalkThreads, 0, st>>>(C, Pin, w, off, count);
+    k_adj_contact<<<blocks(C.n, kWalkThreads), kWalkThreads, 0, st>>>(C, Pin, Xs, w, off, count, gOut, gIn, gXs, gW);
+}
+
+void adj_bending(cudaStream_t st, const BendingArgs &a, float kb, const float4 *Pin, const float *w, const int *to_new,
+                 float4 *gP, float *gW)
+{
+    if (a.num_quads <= 0) return;
+    k_adj_bending_terms<<<blocks(a.num_quads), 256, 0, st>>>(a.num_quads, a.quads, Pin, w, to_new, kb, gP, a.terms);
+    k_adj_bending_apply<<<blocks(a.num_nodes), 256, 0, st>>>(a.num_nodes, a.node_ids, a.node_ptr, a.node_inc, a.terms,
+                                                             to_new, gP, gW);
+}
+
+void adj_post(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float4 *Om,
+              const float4 *Nm, const float *rho, const int *off, const float4 *gVb, float4 *gV, float4 *gX,
+              float *gRho, float4 *etab, float4 *omb, float4 *ombo, float4 *nmb)
+{
+    if (C.n <= 0) return;
+    const int b = blocks(C.n, kWalkThreads);
+    k_adj_post_eta<<<b, kWalkThreads, 0, st>>>(C, P, off, Om, gVb, etab, omb);
+    k_adj_post_b<<<b, kWalkThreads, 0, st>>>(C, P, off, Om, Nm, gVb, etab, omb, ombo, nmb, gRho, gX);
+    k_adj_post_a<<<b, kWalkThreads, 0, st>>>(C, P, V, off, rho, gVb, ombo, nmb, gV, gRho, gX);
 }
 
 }  // namespace bp

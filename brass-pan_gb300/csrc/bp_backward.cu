@@ -35,11 +35,19 @@ void adj_wind(cudaStream_t st, const SimConsts &C, const WindArgs &a, const floa
               const float *mass, const int *to_new, float4 *gP, float4 *gVs, float4 *FG, float4 *FV, float4 *FW,
               float4 *g_wind);
 void adj_fluid(cudaStream_t st, const SimConsts &C, const float4 *Pin, const float *mass, const float *lam,
-               const float *rho, const int *off, const float4 *gOut, float *gLam, float4 *gPart, float4 *gIn);
+               const float *rho, const int *off, const float4 *gOut, const float *gRho, float *gLam, float4 *gPart,
+               float4 *gIn);
 void adj_xsph(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
               const float4 *gVout, float4 *gVin, float4 *gX);
 void adj_shape_matching(cudaStream_t st, const RigidArgs &a, const float4 *rot, const float4 *Pin, const int *to_new,
                         float4 *gP);
+void adj_contacts(cudaStream_t st, const SimConsts &C, const float4 *Pin, const float4 *Xs, const float *w,
+                  const int *off, int *count, const float4 *gOut, float4 *gIn, float4 *gXs, float *gW);
+void adj_bending(cudaStream_t st, const BendingArgs &a, float kb, const float4 *Pin, const float *w, const int *to_new,
+                 float4 *gP, float *gW);
+void adj_post(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float4 *Om,
+              const float4 *Nm, const float *rho, const int *off, const float4 *gVb, float4 *gV, float4 *gX,
+              float *gRho, float4 *etab, float4 *omb, float4 *ombo, float4 *nmb);
 
 namespace {
 
@@ -104,6 +112,11 @@ struct Tape {
     float *gW = nullptr, *gLam = nullptr;
     float4 *G1 = nullptr, *G2 = nullptr, *FG = nullptr, *FV = nullptr, *FW = nullptr, *g_wind = nullptr;
     float *g_stiff = nullptr, *g_rest = nullptr;
+    int *contacts = nullptr;  // per particle: its friction contacts (the collision adjoint's pass A)
+    // the post passes' adjoint: density gradient (read by the last fluid stage's adjoint), eta-bar,
+    // omega-bar of the confinement term, full omega-bar, normal-bar
+    float *gRho = nullptr;
+    float4 *etab = nullptr, *omb = nullptr, *ombo = nullptr, *nmb = nullptr;
 };
 
 void destroy_tape(Tape *t)
@@ -227,15 +240,11 @@ bp_status check_supported(const bp_solver *s, const Tape &t)
     if (t.picked) return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: picking was used while recording");
     for (const Tape::Sub &u : t.subs) {
         const bp_params &p = u.prm;
-        if (stage_on(p, BP_STAGE_PARTICLE_COLLISION) && s->has_solid)
-            return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: particle collisions have no adjoint");
-        if (stage_on(p, BP_STAGE_VORTICITY) || stage_on(p, BP_STAGE_AKINCI))
-            return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: vorticity and Akinci tension have no adjoint");
-        if (stage_on(p, BP_STAGE_BENDING) && s->bend.num_quads > 0)
-            return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: dihedral bending has no adjoint");
-        if (p.mode == BP_MODE_TEXTBOOK && (stage_on(p, BP_STAGE_FLUID) || stage_on(p, BP_STAGE_XSPH)))
+        if (p.mode == BP_MODE_TEXTBOOK && (stage_on(p, BP_STAGE_FLUID) || stage_on(p, BP_STAGE_XSPH) ||
+                                           stage_on(p, BP_STAGE_VORTICITY) || stage_on(p, BP_STAGE_AKINCI)))
             return fail_with(BP_ERR_INVALID_ARGUMENT,
-                             "backward: the fluid and XSPH adjoints are for reference-mode parameters");
+                             "backward: the fluid, XSPH, vorticity and Akinci adjoints are for reference-mode "
+                             "parameters");
     }
     return BP_OK;
 }
@@ -264,8 +273,15 @@ bp_status ensure_grads(Tape &t, const bp_solver *s)
     t.g_wind = t.pool.get<float4>(1);
     t.g_stiff = t.pool.get<float>(m);
     t.g_rest = t.pool.get<float>(m);
+    t.contacts = t.pool.get<int>(n);
+    t.gRho = t.pool.get<float>(n);
+    t.etab = t.pool.get<float4>(n);
+    t.omb = t.pool.get<float4>(n);
+    t.ombo = t.pool.get<float4>(n);
+    t.nmb = t.pool.get<float4>(n);
     if (!(t.gX && t.gV && t.gXn && t.gVn && t.gP && t.gP2 && t.gXs && t.gVs && t.gPart && t.gW && t.gLam && t.G1 &&
-          t.G2 && t.FG && t.FV && t.FW && t.g_wind && t.g_stiff && t.g_rest))
+          t.G2 && t.FG && t.FV && t.FW && t.g_wind && t.g_stiff && t.g_rest && t.contacts && t.gRho && t.etab &&
+          t.omb && t.ombo && t.nmb))
         return fail_with(BP_ERR_OUT_OF_MEMORY, "backward: gradient buffers");
     t.grads_ready = true;
     return BP_OK;
@@ -296,9 +312,29 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
     const bool planes = stage_on(p, BP_STAGE_PLANES) && s->nplanes > 0;
     const bool distance = stage_on(p, BP_STAGE_DISTANCE) && s->dist.num_edges > 0;
     const bool pcoll = stage_on(p, BP_STAGE_PARTICLE_COLLISION) && s->has_solid;
+    const bool bending = stage_on(p, BP_STAGE_BENDING) && s->bend.num_quads > 0;
+    bool rho_pending = false;  // the post passes' density gradient awaits the last fluid stage
     for (int r = (int)T.recs.size() - 1; r >= 0; --r) {
         const TapeRec &rec = T.recs[r];
         switch (rec.stage) {
+        case TS_POST_AB: {  // positions: the commit's input; velocities before pass A in the slot
+            int c = r - 1;
+            while (c >= 0 && T.recs[c].stage != TS_COMMIT) --c;
+            const float4 *Pc = T.pool4[T.recs[c].slot];
+            const size_t bytes = (size_t)s->n * sizeof(float4);
+            if (C.use_xsph) {  // pass C first: gV -> the gradient of pass B's velocities
+                adj_xsph(st, C, Pc, T.pool4[rec.aux + 2], s->off, t.gV, t.gVn, t.gX);
+                cudaMemcpyAsync(t.gV, t.gVn, bytes, cudaMemcpyDeviceToDevice, st);
+            }
+            adj_post(st, C, Pc, T.pool4[rec.slot], T.pool4[rec.aux], T.pool4[rec.aux + 1], T.pool1[rec.aux1], s->off,
+                     t.gV, t.gVn, t.gX, t.gRho, t.etab, t.omb, t.ombo, t.nmb);
+            cudaMemcpyAsync(t.gV, t.gVn, bytes, cudaMemcpyDeviceToDevice, st);
+            rho_pending = true;
+            break;
+        }
+        case TS_BENDING:
+            adj_bending(st, s->bend, p.bending_stiffness, T.pool4[rec.slot], s->w, s->to_new, t.gP, t.gW);
+            break;
         case TS_XSPH: {  // velocities before XSPH in the slot; positions: the commit's input
             int c = r - 1;
             while (c >= 0 && T.recs[c].stage != TS_COMMIT) --c;
@@ -318,11 +354,16 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
             break;
         case TS_FLUID:
             adj_fluid(st, C, T.pool4[rec.slot], s->mass, T.pool1[rec.aux], T.pool1[rec.aux + 1], s->off, t.gP,
-                      t.gLam, t.gPart, t.gP2);
+                      rho_pending ? t.gRho : nullptr, t.gLam, t.gPart, t.gP2);
+            rho_pending = false;
             cudaMemcpyAsync(t.gP, t.gP2, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
             break;
         case TS_PLANES:
             adj_planes(st, C, s->Xs, T.pool4[rec.slot], t.gP, t.gXs);
+            break;
+        case TS_PCOLL:
+            adj_contacts(st, C, T.pool4[rec.slot], s->Xs, s->w, s->off, t.contacts, t.gP, t.gP2, t.gXs, t.gW);
+            cudaMemcpyAsync(t.gP, t.gP2, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
             break;
         case TS_SHAPE:
             adj_shape_matching(st, s->rigid, T.pool4[rec.aux], T.pool4[rec.slot], s->to_new, t.gP);
@@ -335,8 +376,9 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
             break;
         }
     }
-    adj_reorder(st, C, s->order, start.X, start.V, planes ? 1 : 0, (distance || pcoll) ? 1 : 0, t.gP, t.gXs,
-                t.gVs, t.gW, t.gXn, t.gVn);
+    const int inv_scaled = (distance || bending || pcoll) ? 1 : 0;  // the stages that read w
+    adj_reorder(st, C, s->order, start.X, start.V, planes ? 1 : 0, inv_scaled, t.gP, t.gXs, t.gVs, t.gW, t.gXn,
+                t.gVn);
     cudaMemcpyAsync(t.gX, t.gXn, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(t.gV, t.gVn, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
 }

@@ -103,6 +103,26 @@ __device__ __forceinline__ Dual<N> dmin(const Dual<N> &a, float s)
 {
     return (a.v < s) ? a : dconst<N>(s);
 }
+// min(max(a, lo), hi) as fminf(fmaxf(a, lo), hi) picks it
+template <int N>
+__device__ __forceinline__ Dual<N> dclamp(const Dual<N> &a, float lo, float hi)
+{
+    if (!(a.v > lo)) return dconst<N>(lo);
+    if (!(a.v < hi)) return dconst<N>(hi);
+    return a;
+}
+// arccos; d/da = -1 / sqrt(1 - a^2), taken as 0 where |a| = 1
+template <int N>
+__device__ __forceinline__ Dual<N> dacos(const Dual<N> &a)
+{
+    Dual<N> r;
+    r.v = acosf(a.v);
+    const float s = 1.0f - a.v * a.v;
+    const float g = s > 0.f ? -1.0f / sqrtf(s) : 0.f;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = a.d[k] * g;
+    return r;
+}
 template <int N>
 __device__ __forceinline__ Dual<N> dexp(const Dual<N> &a)
 {

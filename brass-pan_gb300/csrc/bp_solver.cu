@@ -841,7 +841,8 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             if (tape) tape->push(TS_DISTANCE, cur);
             launch_distance(st, Cpost, s->dist, cur, s->w, s->to_new, s->err, L);
         }
-        if (bending) {  // PS:956-969 (no adjoint)
+        if (bending) {  // PS:956-969
+            if (tape) tape->push(TS_BENDING, cur);
             BendingArgs ba = s->bend;
             ba.stiffness = s->prm.bending_stiffness;
             launch_bending(st, Cpost, ba, cur, s->w, s->to_new, L);
@@ -882,6 +883,13 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         Cl.cls_post = post_slots ? 1 : 0;
         launch_post_a(st, Cl, cur, s->Vc, s->rho, s->off, s->Om, s->Nm, L);
         launch_post_b(st, Cl, cur, s->Vc, s->Om, s->Nm, s->off, C.use_xsph ? s->Vs : s->Vc, L);
+        if (tape) {  // what the passes' adjoint reads: omega, normals, pass B's velocities, density
+            TapeRec &r = tape->recs.back();
+            r.aux = tape->snap4(s->Om);
+            tape->snap4(s->Nm);
+            if (C.use_xsph) tape->snap4(s->Vs);
+            r.aux1 = tape->snap1(s->rho);
+        }
         if (C.use_xsph) launch_post_c(st, Cl, cur, s->Vs, s->off, s->mass, s->rho, s->Vc, L);
     } else if (C.use_xsph) {
         SimConsts Cx = Cpost;  // records its own pairs, then sums over them

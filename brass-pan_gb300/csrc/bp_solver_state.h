@@ -44,12 +44,17 @@ enum TapeStage : int {
     TS_IMMOVABLE,
     TS_COMMIT,
     TS_XSPH,
-    TS_POST_AB
+    TS_POST_AB,
+    TS_BENDING
 };
 struct TapeRec {
     int stage;
-    int slot;  // snapshot of the stage's input: positions, or velocities for TS_XSPH
-    int aux;   // TS_FLUID: snapshot of lambda (aux) and density (aux + 1); TS_SHAPE: the rotations after it
+    int slot;  // snapshot of the stage's input: positions, or velocities for TS_XSPH and TS_POST_AB
+    // TS_FLUID: snapshots of lambda (aux) and density (aux + 1) in pool1; TS_SHAPE: the rotations after
+    // it; TS_POST_AB: omega (aux) and normals (aux + 1) after pass A, and with XSPH the velocities
+    // after pass B (aux + 2)
+    int aux;
+    int aux1 = -1;  // TS_POST_AB: the density the passes read (pool1)
 };
 
 // The intermediates of one substep re-run for its adjoint: each stage's
@@ -70,7 +75,7 @@ struct SubstepTape {
     }
     int snap4(const float4 *src, size_t count = 0);  // count 0: one per particle (count <= particles)
     int snap1(const float *src);
-    void push(int stage, const float4 *src, int aux = -1) { recs.push_back(TapeRec{stage, snap4(src), aux}); }
+    void push(int stage, const float4 *src, int aux = -1) { recs.push_back(TapeRec{stage, snap4(src), aux, -1}); }
 };
 }  // namespace bp
 

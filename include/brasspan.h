@@ -314,12 +314,13 @@ bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, float dt, int32
  * of the re-run forward pass) and restores the solver's state afterwards, so
  * stepping may continue; the tape stays open until bp_solver_tape_end.
  *
- * Stages with an adjoint: planes, wind, distance constraints, shape matching
- * (the extracted rotation differentiated at its fixed point), immovables,
- * the velocity update, and in reference mode the fluid density / lambda /
- * position correction and XSPH.  Recordings that used particle collisions
- * between solids, vorticity or Akinci tension, or textbook fluid passes
- * return BP_ERR_INVALID_ARGUMENT from bp_solver_backward. */
+ * Stages with an adjoint: planes, wind, particle-particle contacts with
+ * friction, distance constraints, dihedral bending, shape matching (the
+ * extracted rotation differentiated at its fixed point), immovables, the
+ * velocity update, and in reference mode the fluid density / lambda /
+ * position correction, vorticity confinement, Akinci tension and XSPH.
+ * Recordings that used picking or textbook-mode fluid passes return
+ * BP_ERR_INVALID_ARGUMENT from bp_solver_backward. */
 typedef struct bp_gradients {
     float *positions;            /* [N][3] dL/dx at tape begin, original order, or NULL */
     float *velocities;           /* [N][3] dL/dv at tape begin, or NULL */

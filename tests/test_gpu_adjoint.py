@@ -250,30 +250,25 @@ def test_backward_restores_the_state(bp, gpu):
     b.close()
 
 
-def test_backward_rejects_stages_without_adjoint(bp, gpu):
+def test_backward_rejects_what_has_no_adjoint(bp, gpu):
     abi = bp.abi
     scene, _ = fluid_case(bp, n=4)
-    s = bp.ParticleSolver(scene, bp.make_params(scene))  # vorticity and Akinci on
+    s = bp.ParticleSolver(scene, bp.make_params(scene, mode=abi.BP_MODE_TEXTBOOK))
     s.tape_begin(1)
     s.update(1, DT, 2)
     with pytest.raises(bp.BrassPanError):
-        s.backward(np.ones((scene.num_particles, 3), np.float32))
+        s.backward(np.ones((scene.num_particles, 3), np.float32))  # textbook-mode fluid
     s.close()
     t = bp.ParticleSolver(scene, bp.make_params(scene))
     with pytest.raises(bp.BrassPanError):
         t.backward(np.ones((scene.num_particles, 3), np.float32))  # nothing recorded
     t.close()
-    from conftest import cloth_bending_scene
-
-    cloth = cloth_bending_scene(bp, seed=1, n=6)
-    stages = abi.BP_STAGE_PLANES | abi.BP_STAGE_DISTANCE | abi.BP_STAGE_BENDING | abi.BP_STAGE_IMMOVABLE
-    u = bp.ParticleSolver(cloth, bp.make_params(cloth, stage_mask=stages))
+    u = bp.ParticleSolver(scene, bp.make_params(scene))
     u.tape_begin(1)
-    u.update(1, DT, 2)
+    u.update(1, DT, 2, picked_original_id=3, picked_position=(0.3, 0.5, 0.3))
     with pytest.raises(bp.BrassPanError):
-        u.backward(np.ones((cloth.num_particles, 3), np.float32))  # dihedral bending has no adjoint
+        u.backward(np.ones((scene.num_particles, 3), np.float32))  # picking
     u.close()
-    assert abi.BP_STAGE_VORTICITY
 
 
 # ---- against central finite differences of the FP64 host oracle -------------
@@ -407,3 +402,135 @@ def test_pbf_block_gradient_matches_fp64_finite_differences(bp, gpu, oracle):
     print(report)
     bad = [w for w, fd, ad in pairs if abs(fd - ad) > FD64_REL * max(abs(fd), abs(ad))]
     assert not bad, report
+
+
+# ---- the remaining stages against FP64 finite differences ---------------------
+#
+# Particle contacts with friction, vorticity confinement with Akinci tension
+# (reference mode, through the density of the last lambda pass), and dihedral
+# bending: each on a small scene over a few substeps, loss = random weights on
+# the final positions and velocities, directional derivatives along random
+# unit directions of the initial velocities (step 1e-3) and positions.
+#
+# The step map is only piecewise smooth in the positions: reference-mode
+# density sums over sorted j >= i, so it jumps where a particle crosses a cell
+# boundary, vorticity confinement switches on where |eta|^2 passes 1e-3, and
+# contact friction switches between its static and kinetic forms.  Along a
+# position direction, steps of 1e-3 to 1e-5 straddle such jumps in these
+# scenes (measured: the quotient changes sign between them), so positions are
+# differenced at step 1e-6 (the same quotient as at 1e-7 to 7 digits; the
+# FP64 forward resolves it to about 1e-9); the scenes start away from cell
+# boundaries.
+
+
+def fd64_state_pairs(oracle, scene, params, frames, wx, wv, g, seed, x_step=1e-6):
+    def L(x0, v0):
+        xf, vf = rollout64(oracle, scene, params, frames, x0=x0, v0=v0)
+        return float(np.sum(xf * wx) + np.sum(vf * wv))
+
+    n = scene.num_particles
+    x0 = scene.positions.astype(np.float64)
+    v0 = np.zeros((n, 3)) if scene.velocities is None else scene.velocities.astype(np.float64)
+    rng = np.random.default_rng(seed)
+    pairs = []
+    for key in ("velocities", "positions"):
+        d = rng.standard_normal((n, 3))
+        d /= np.linalg.norm(d)
+        if key == "velocities":
+            fd = central64(lambda **kw: L(**kw), lambda s: {"x0": x0, "v0": v0 + s * d},
+                           lambda s: {"x0": x0, "v0": v0 - s * d})
+        else:
+            fd = central64(lambda **kw: L(**kw), lambda s: {"x0": x0 + s * d, "v0": v0},
+                           lambda s: {"x0": x0 - s * d, "v0": v0}, h=x_step)
+        pairs.append((key, fd, float(np.sum(g[key].astype(np.float64) * d))))
+    return pairs
+
+
+def assert_fd64(pairs):
+    report = "; ".join(f"{w} fd64 {fd:.6e} adjoint {ad:.6e}" for w, fd, ad in pairs)
+    print(report)
+    floor = 1e-2 * max(abs(a) for _, _, a in pairs)
+    bad = [w for w, fd, ad in pairs if abs(fd - ad) > FD64_REL * max(abs(fd), abs(ad), floor)]
+    assert not bad, report
+
+
+def gpu_gradients(bp, scene, params, frames, wx, wv, every=2):
+    s = bp.ParticleSolver(scene, params)
+    s.tape_begin(every)
+    for _ in range(frames):
+        s.update(2, DT, 4)
+    g = s.backward(wx.astype(np.float32), wv.astype(np.float32))
+    s.close()
+    return g
+
+
+def grains_case(bp, fluid=False):
+    """A block of grains (single-particle solids) packed closer than two radii,
+    so that every grain starts in contact; optionally over a small fluid pool."""
+    abi = bp.abi
+    sc = bp.scenes
+    rng = np.random.default_rng(9)
+    s = sc.Scene(name="grains")
+    s.particle_radius, s.kernel_radius, s.cell_size, s.grid_dim, s.rest_density = 0.05, 0.2, 0.2, 16, 1000.0
+    sc.box_planes(s, (0, 0, 0), (1.6, 3.0, 1.6))
+    stages = abi.BP_STAGE_PLANES | abi.BP_STAGE_PARTICLE_COLLISION
+    if fluid:
+        s.add_fluid_block((8, 3, 8), (0.35, 0.05, 0.35), (0.1, 0.1, 0.1), 1.0, jitter=0.001, rng=rng)
+        stages |= abi.BP_STAGE_FLUID
+    s.add_granulars_block((4, 4, 4), (0.65, 0.45 if fluid else 0.35, 0.65), (0.09, 0.09, 0.09), 1.0)
+    s.velocities = rng.uniform(-0.3, 0.3, (s.num_particles, 3)).astype(np.float32)
+    return s, bp.make_params(s, stage_mask=stages)
+
+
+@pytest.mark.parametrize("fluid", [False, True], ids=["grains", "grains_on_fluid"])
+def test_contact_gradients_match_fp64_finite_differences(bp, gpu, oracle, fluid):
+    scene, params = grains_case(bp, fluid)
+    frames = 2
+    wx, wv = loss_weights(scene.num_particles, seed=21)
+    g = gpu_gradients(bp, scene, params, frames, wx, wv)
+    assert_fd64(fd64_state_pairs(oracle, scene, params, frames, wx, wv, g, seed=22))
+
+
+def test_vorticity_and_akinci_gradients_match_fp64_finite_differences(bp, gpu, oracle):
+    abi = bp.abi
+    scene = bp.scenes.pbf_scene(6, 6, 6, spacing=0.1, seed=7, box=(1.2, 2.0, 1.2), grid_dim=16)
+    scene.positions = (scene.positions + np.float32(0.05)).astype(np.float32)  # off the cell boundaries
+    rng = np.random.default_rng(8)
+    scene.velocities = rng.uniform(-0.5, 0.5, (scene.num_particles, 3)).astype(np.float32)
+    stages = (abi.BP_STAGE_FLUID | abi.BP_STAGE_PLANES | abi.BP_STAGE_VORTICITY | abi.BP_STAGE_AKINCI |
+              abi.BP_STAGE_XSPH)
+    params = bp.make_params(scene, stage_mask=stages)
+    frames = 2
+    wx, wv = loss_weights(scene.num_particles, seed=23)
+    g = gpu_gradients(bp, scene, params, frames, wx, wv)
+    assert_fd64(fd64_state_pairs(oracle, scene, params, frames, wx, wv, g, seed=24))
+
+
+def twisted_cloth(bp):
+    """The pinned cloth of the bending tests, twisted (height 0.8 (x - cx)(z - cz)),
+    so that every hinge starts about 0.1 rad from flat and stays above 0.03
+    rad over the rollout.  Near flat the reference's bending term cannot be
+    differentiated in fp32: its dihedral cosine d rounds to -1 within 3.5e-4
+    rad of flat, where sqrt(1 - d^2) is then a few rounding steps of 1 + d,
+    so the fp32 forward's slope there is rounding noise (measured on the
+    initially flat cloth: 2-100 % from the FP64 differences, while without
+    bending the same rollout agrees to 4e-5)."""
+    from conftest import cloth_bending_scene
+
+    scene = cloth_bending_scene(bp, seed=3, n=8)
+    x = scene.positions.astype(np.float64)
+    c = x[:, [0, 2]].mean(axis=0)
+    x[:, 1] += 0.8 * (x[:, 0] - c[0]) * (x[:, 2] - c[1])
+    scene.positions = x.astype(np.float32)
+    return scene
+
+
+def test_bending_gradients_match_fp64_finite_differences(bp, gpu, oracle):
+    abi = bp.abi
+    scene = twisted_cloth(bp)
+    stages = abi.BP_STAGE_PLANES | abi.BP_STAGE_DISTANCE | abi.BP_STAGE_BENDING | abi.BP_STAGE_IMMOVABLE
+    params = bp.make_params(scene, stage_mask=stages, bending_stiffness=0.2)
+    frames = 2
+    wx, wv = loss_weights(scene.num_particles, seed=25)
+    g = gpu_gradients(bp, scene, params, frames, wx, wv)
+    assert_fd64(fd64_state_pairs(oracle, scene, params, frames, wx, wv, g, seed=26, x_step=FD64_STEP))  # smooth
