@@ -9,11 +9,11 @@
 // the same positions).
 //
 // Supported stages: prediction and reorder, planes (stabilisation and
-// collision), wind, particle-particle contacts with friction, reference-mode
-// fluid density / lambda / position correction (with s_corr and the per-pair
+// collision), wind, particle-particle contacts with friction, fluid density /
+// lambda / position correction in both modes (with s_corr and the per-pair
 // clamp), distance constraints, dihedral bending, shape matching (rotation
 // differentiated at its fixed point), immovables, the velocity update,
-// vorticity confinement, Akinci tension and reference-mode XSPH.
+// vorticity confinement, Akinci tension and XSPH.
 #include "bp_dual.cuh"
 #include "bp_internal.h"
 #include "bp_walk.cuh"
@@ -414,16 +414,21 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const 
     const float3 gk = ld3(gOut, k);
     float lb = 0.f;
     float3 pb = make_float3(0.f, 0.f, 0.f);
+    // reference mode: the pair counts for both ends when its lower index is
+    // fluid; textbook mode: every fluid particle gathers over all neighbours
     auto test = [&](int j, float4 pj4) {
         const float3 r = sub3(pk, f3(pj4));
         const float d2 = dotf(r, r);
-        const bool inc = (j > k) ? (phk < 0) : (phase_of(pj4) < 0);
+        const bool fj = phase_of(pj4) < 0;
+        const bool inc = C.textbook ? (phk < 0 || fj) : ((j > k) ? (phk < 0) : fj);
         return j != k && d2 <= C.h2 && d2 > 0.f && inc;
     };
     auto term = [&](int j, float4 pj4) {
             const float3 r = sub3(pk, f3(pj4));
             const float d2 = dotf(r, r);
             const float rl = sqrtf(d2);
+            const bool own = !C.textbook || phk < 0;               // dp_k has the pair
+            const bool other = !C.textbook || phase_of(pj4) < 0;  // dp_j has the pair
             const SpikyD sp = spiky_d(C, r, rl);
             float s = lk + lam[j];
             float3 dsc = make_float3(0.f, 0.f, 0.f);  // d scorr / d r
@@ -434,12 +439,14 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const 
                     dsc = mul3(poly6_grad(C, r, d2), C.scorr_k * C.scorr_ni * ipowf(x, C.scorr_ni - 1) * C.scorr_inv_wq);
             }
             // term of dp_k: (m_j / rho0) clamp(s gradW(r))
-            const float3 u1b = mul3(clamp_vjp(C, mul3(sp.g, s), gk), mass[j] * inv_rho0);
+            const float3 u1b = own ? mul3(clamp_vjp(C, mul3(sp.g, s), gk), mass[j] * inv_rho0)
+                                   : make_float3(0.f, 0.f, 0.f);
             const float sb1 = dotf(u1b, sp.g);
             const float3 rb1 = sub3(mul3(spiky_hess_mul(sp, r, rl, u1b), s), mul3(dsc, sb1));
             // term of dp_j: (m_k / rho0) clamp(s gradW(-r))
             const float3 g_neg = mul3(sp.g, -1.f);
-            const float3 u2b = mul3(clamp_vjp(C, mul3(g_neg, s), ld3(gOut, j)), mk * inv_rho0);
+            const float3 u2b = other ? mul3(clamp_vjp(C, mul3(g_neg, s), ld3(gOut, j)), mk * inv_rho0)
+                                     : make_float3(0.f, 0.f, 0.f);
             const float sb2 = dotf(u2b, g_neg);
             // gradient w.r.t. r_jk = -r: H(-r) = H(r), dscorr(-r) = -dscorr(r)
             const float3 rb2 = add3(mul3(spiky_hess_mul(sp, r, rl, u2b), s), mul3(dsc, sb2));
@@ -498,13 +505,116 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_lambda(SimConsts C, const 
     gIn[k] = f4(add3(add3(ld3(gOut, k), ld3(gPart, k)), pb));
 }
 
-// ---- XSPH, reference mode: v'_i = v_i + c sum_j W6(r_ij) (v_j - v_i) ----
-// Positions are the committed ones; gX receives their gradient.
+// ---- fluid, textbook mode ----
+// rho_i = sum_j m_j s_j W6(r_ij) (all j, the particle itself included),
+// G_i = sum_{j != i} a_j gradW(r_ij), a_j = m_j / rho0,
+// D_i = sum_{j != i} a_j^2 |gradW(r_ij)|^2 + |G_i|^2 + eps, lambda_i = -C_i / D_i;
+// dp_k as in reference mode for every fluid k over all its neighbours.
+// Pass T2 turns lambda-bar into rho-bar and D-bar per fluid particle; pass T3
+// gathers their position terms: as particle i of its own sums and as
+// neighbour j of its neighbours' sums.
+
+__global__ void __launch_bounds__(kWalkThreads) k_adj_lambda_tb_prep(SimConsts C, const float4 *__restrict__ P,
+                                                                     const float *__restrict__ mass,
+                                                                     const int *__restrict__ off,
+                                                                     const float *__restrict__ gLam,
+                                                                     const float *__restrict__ gRho,
+                                                                     float4 *__restrict__ GD, float *__restrict__ rhob)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= C.n) return;
+    const float4 pk4 = P[k];
+    if (phase_of(pk4) > 0) {  // solids: lambda 0 whatever their neighbours
+        GD[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        rhob[k] = 0.f;
+        return;
+    }
+    const float3 pk = f3(pk4);
+    const int sc = scene_index(C, k);
+    const float rho0 = rest_density(C, sc), inv_rho0 = 1.0f / rho0;
+    float rho = 0.f, g2 = 0.f;
+    float3 G = make_float3(0.f, 0.f, 0.f);
+    auto test = [&](int, float4 pj4) { return dotf(sub3(pk, f3(pj4)), sub3(pk, f3(pj4))) <= C.h2; };
+    auto term = [&](int j, float4 pj4) {
+        const float3 r = sub3(pk, f3(pj4));
+        const float d2 = dotf(r, r);
+        const float ld = mass[j] * poly6(C, d2);
+        rho += phase_of(pj4) < 0 ? ld : C.solid_scale * ld;
+        if (d2 > 0.f) {
+            const float3 g = mul3(spiky_d(C, r, sqrtf(d2)).g, mass[j] * inv_rho0);
+            g2 += dotf(g, g);
+            G = add3(G, g);
+        }
+    };
+    walk_neighbors<true>(k, pk, 0, P, grid_view(C, sc, off), C, nullptr, -1, test, term);
+    const float D = g2 + dotf(G, G) + C.relaxation;
+    float c = rho / rho0 - 1.0f;
+    const bool clamped = C.clamp_c && !(c > 0.f);
+    if (clamped) c = 0.f;
+    const float lb = gLam[k];
+    const float cb = clamped ? 0.f : -lb / D;
+    GD[k] = f4(G, lb * c / (D * D));
+    rhob[k] = cb / rho0 + (gRho ? gRho[k] : 0.f);
+}
+
+__global__ void __launch_bounds__(kWalkThreads) k_adj_lambda_tb(SimConsts C, const float4 *__restrict__ P,
+                                                                const float *__restrict__ mass,
+                                                                const int *__restrict__ off,
+                                                                const float4 *__restrict__ GD,
+                                                                const float *__restrict__ rhob,
+                                                                const float4 *__restrict__ gPart,
+                                                                const float4 *__restrict__ gOut,
+                                                                float4 *__restrict__ gIn)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= C.n) return;
+    const float4 pk4 = P[k];
+    const int phk = phase_of(pk4);
+    const float3 pk = f3(pk4);
+    const int sc = scene_index(C, k);
+    const float inv_rho0 = inv_rest_density(C, sc);
+    const float4 gdk = GD[k];
+    const float3 Gk = f3(gdk);
+    const float Dbk = gdk.w, rbk = rhob[k];
+    const float mk = mass[k], ak = mk * inv_rho0, sk = phk < 0 ? 1.f : C.solid_scale;
+    float3 pb = make_float3(0.f, 0.f, 0.f);
+    auto test = [&](int j, float4 pj4) {
+        const float3 r = sub3(pk, f3(pj4));
+        const float d2 = dotf(r, r);
+        return j != k && d2 <= C.h2 && d2 > 0.f;
+    };
+    auto term = [&](int j, float4 pj4) {
+        const float3 r = sub3(pk, f3(pj4));
+        const float d2 = dotf(r, r), rl = sqrtf(d2);
+        const SpikyD sp = spiky_d(C, r, rl);
+        const float3 w6 = poly6_grad(C, r, d2);
+        const int phj = phase_of(pj4);
+        const float mj = mass[j], aj = mj * inv_rho0;
+        if (phk < 0) {  // k's own density and denominator
+            const float3 u = mul3(add3(mul3(sp.g, 2.f * aj * aj), mul3(Gk, 2.f * aj)), Dbk);
+            pb = add3(add3(pb, spiky_hess_mul(sp, r, rl, u)), mul3(w6, rbk * mj * (phj < 0 ? 1.f : C.solid_scale)));
+        }
+        if (phj < 0) {  // j's, through r_jk = -r
+            const float4 gdj = GD[j];
+            const float3 u = mul3(sub3(mul3(sp.g, 2.f * ak * ak), mul3(f3(gdj), 2.f * ak)), gdj.w);
+            pb = add3(add3(pb, spiky_hess_mul(sp, r, rl, u)), mul3(w6, rhob[j] * mk * sk));
+        }
+    };
+    walk_neighbors<true>(k, pk, 0, P, grid_view(C, sc, off), C, nullptr, -1, test, term);
+    gIn[k] = f4(add3(add3(ld3(gOut, k), ld3(gPart, k)), pb));
+}
+
+// ---- XSPH: v'_i = v_i + c sum_j W6(r_ij) b_j (v_j - v_i) ----
+// b_j = 1 in reference mode, m_j / rho_j in textbook mode (whose density
+// gradient is added to gRho).  Positions are the committed ones; gX receives
+// their gradient.
 
 __global__ void __launch_bounds__(kWalkThreads) k_adj_xsph(SimConsts C, const float4 *__restrict__ P,
                                                            const float4 *__restrict__ V, const int *__restrict__ off,
+                                                           const float *__restrict__ mass,
+                                                           const float *__restrict__ rho,
                                                            const float4 *__restrict__ gVout, float4 *__restrict__ gVin,
-                                                           float4 *__restrict__ gX)
+                                                           float4 *__restrict__ gX, float *__restrict__ gRho)
 {
     StageShared &S = stage_shared();
     const int g = stage_block(C, P, off, blockIdx.x * kWalkThreads, S);
@@ -518,7 +628,9 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_xsph(SimConsts C, const fl
         return;
     }
     const float3 pi = f3(pi4), vi = ld3(V, i);
+    const float bi = C.textbook ? mass[i] / rho[i] : 1.f;
     float3 gv = go, gp = make_float3(0.f, 0.f, 0.f);
+    float rb = 0.f;
     auto test = [&](int j, float4 pj4) {
         const float3 r = sub3(pi, f3(pj4));
         return j != i && phase_of(pj4) == phi && dotf(r, r) <= C.h2;
@@ -527,14 +639,17 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_xsph(SimConsts C, const fl
         const float3 r = sub3(pi, f3(pj4));
         const float d2 = dotf(r, r);
         const float w = poly6(C, d2);
+        const float bj = C.textbook ? mass[j] / rho[j] : 1.f;
         const float3 gj = ld3(gVout, j);
-        gv = add3(gv, mul3(sub3(gj, go), C.xsph_c * w));
+        gv = add3(gv, mul3(sub3(mul3(gj, bi), mul3(go, bj)), C.xsph_c * w));
         const float3 dv = sub3(ld3(V, j), vi);
-        gp = add3(gp, mul3(poly6_grad(C, r, d2), C.xsph_c * dotf(dv, sub3(go, gj))));
+        gp = add3(gp, mul3(poly6_grad(C, r, d2), C.xsph_c * (bj * dotf(dv, go) - bi * dotf(dv, gj))));
+        if (C.textbook) rb -= C.xsph_c * w * dotf(dv, gj);  // j's sum: c W b_i (v_i - v_j) . g_j
     };
     record_then_sum(C, i, pi, P, grid_view(C, scene_index(C, i), off), &S, g, test, test, term);
     gVin[i] = f4(gv);
     gX[i] = f4(add3(ld3(gX, i), gp));
+    if (C.textbook) gRho[i] -= rb * bi / rho[i];  // d b_i / d rho_i = -b_i / rho_i
 }
 
 // ---- shape matching (alpha = 1): g_i = R q_i + cm ----
@@ -977,8 +1092,8 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_post_eta(SimConsts C, cons
     omb[k] = f4(mul3(cross_f(g, eh), a));
 }
 
-// Pass B's adjoint: w-bar (omb in, the full w-bar out in ombo), n-bar, rho-bar
-// and the position gradient (added to gX).
+// Pass B's adjoint: w-bar (omb in, the full w-bar out in ombo), n-bar, and
+// the density and position gradients (added to gRho and gX).
 __global__ void __launch_bounds__(kWalkThreads) k_adj_post_b(SimConsts C, const float4 *__restrict__ P,
                                                              const int *__restrict__ off,
                                                              const float4 *__restrict__ Om,
@@ -997,7 +1112,6 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_post_b(SimConsts C, const 
     if (phk >= 0) {
         ombo[k] = zero;
         nmb[k] = zero;
-        gRho[k] = 0.f;
         return;
     }
     const float rho0 = rest_density(C, scene_index(C, k));
@@ -1035,7 +1149,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_post_b(SimConsts C, const 
     if (om4.w > 0.f) wb = add3(wb, mul3(f3(om4), abs_omb / om4.w));
     ombo[k] = f4(wb);
     nmb[k] = f4(nb);
-    gRho[k] = rb;
+    gRho[k] += rb;
     gX[k] = f4(add3(ld3(gX, k), pb));
 }
 
@@ -1138,12 +1252,17 @@ void adj_wind(cudaStream_t st, const SimConsts &C, const WindArgs &a, const floa
 }
 void adj_fluid(cudaStream_t st, const SimConsts &C, const float4 *Pin, const float *mass, const float *lam,
                const float *rho, const int *off, const float4 *gOut, const float *gRho, float *gLam, float4 *gPart,
-               float4 *gIn)
+               float4 *GD, float *rhob, float4 *gIn)
 {
     if (C.n <= 0) return;
     const int b = blocks(C.n, kWalkThreads);
     k_adj_deltap<<<b, kWalkThreads, stage_bytes(C), st>>>(C, Pin, mass, lam, off, gOut, gLam, gPart);
-    k_adj_lambda<<<b, kWalkThreads, stage_bytes(C), st>>>(C, Pin, mass, rho, off, gLam, gPart, gOut, gRho, gIn);
+    if (C.textbook) {
+        k_adj_lambda_tb_prep<<<b, kWalkThreads, 0, st>>>(C, Pin, mass, off, gLam, gRho, GD, rhob);
+        k_adj_lambda_tb<<<b, kWalkThreads, 0, st>>>(C, Pin, mass, off, GD, rhob, gPart, gOut, gIn);
+    } else {
+        k_adj_lambda<<<b, kWalkThreads, stage_bytes(C), st>>>(C, Pin, mass, rho, off, gLam, gPart, gOut, gRho, gIn);
+    }
 }
 void adj_shape_matching(cudaStream_t st, const RigidArgs &a, const float4 *rot, const float4 *Pin, const int *to_new,
                         float4 *gP)
@@ -1152,10 +1271,11 @@ void adj_shape_matching(cudaStream_t st, const RigidArgs &a, const float4 *rot, 
     k_adj_shape_matching<<<a.num_bodies, kAdjSmThreads, 0, st>>>(a, rot, Pin, to_new, gP);
 }
 void adj_xsph(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
-              const float4 *gVout, float4 *gVin, float4 *gX)
+              const float *mass, const float *rho, const float4 *gVout, float4 *gVin, float4 *gX, float *gRho)
 {
     if (C.n <= 0) return;
-    k_adj_xsph<<<blocks(C.n, kWalkThreads), kWalkThreads, stage_bytes(C), st>>>(C, P, V, off, gVout, gVin, gX);
+    k_adj_xsph<<<blocks(C.n, kWalkThreads), kWalkThreads, stage_bytes(C), st>>>(C, P, V, off, mass, rho, gVout,
+                                                                               gVin, gX, gRho);
 }
 
 void adj_contacts(cudaStream_t st, const SimConsts &C, const float4 *Pin, const float4 *Xs, const float *w,

@@ -36,9 +36,9 @@ void adj_wind(cudaStream_t st, const SimConsts &C, const WindArgs &a, const floa
               float4 *g_wind);
 void adj_fluid(cudaStream_t st, const SimConsts &C, const float4 *Pin, const float *mass, const float *lam,
                const float *rho, const int *off, const float4 *gOut, const float *gRho, float *gLam, float4 *gPart,
-               float4 *gIn);
+               float4 *GD, float *rhob, float4 *gIn);
 void adj_xsph(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const int *off,
-              const float4 *gVout, float4 *gVin, float4 *gX);
+              const float *mass, const float *rho, const float4 *gVout, float4 *gVin, float4 *gX, float *gRho);
 void adj_shape_matching(cudaStream_t st, const RigidArgs &a, const float4 *rot, const float4 *Pin, const int *to_new,
                         float4 *gP);
 void adj_contacts(cudaStream_t st, const SimConsts &C, const float4 *Pin, const float4 *Xs, const float *w,
@@ -117,6 +117,9 @@ struct Tape {
     // omega-bar of the confinement term, full omega-bar, normal-bar
     float *gRho = nullptr;
     float4 *etab = nullptr, *omb = nullptr, *ombo = nullptr, *nmb = nullptr;
+    // the textbook fluid adjoint: (G, D-bar) and rho-bar per particle
+    float4 *GD = nullptr;
+    float *rhob = nullptr;
 };
 
 void destroy_tape(Tape *t)
@@ -234,18 +237,11 @@ void copy_ctx(bp_solver *s, const SubCtx &c, bool save)
 
 bool stage_on(const bp_params &p, int bit) { return (p.stage_mask & bit) != 0; }
 
-// Which recorded configurations have an adjoint.
-bp_status check_supported(const bp_solver *s, const Tape &t)
+// Which recorded configurations have an adjoint: every stage, but not picking
+// (its target is an input without a gradient).
+bp_status check_supported(const Tape &t)
 {
     if (t.picked) return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: picking was used while recording");
-    for (const Tape::Sub &u : t.subs) {
-        const bp_params &p = u.prm;
-        if (p.mode == BP_MODE_TEXTBOOK && (stage_on(p, BP_STAGE_FLUID) || stage_on(p, BP_STAGE_XSPH) ||
-                                           stage_on(p, BP_STAGE_VORTICITY) || stage_on(p, BP_STAGE_AKINCI)))
-            return fail_with(BP_ERR_INVALID_ARGUMENT,
-                             "backward: the fluid, XSPH, vorticity and Akinci adjoints are for reference-mode "
-                             "parameters");
-    }
     return BP_OK;
 }
 
@@ -279,9 +275,11 @@ bp_status ensure_grads(Tape &t, const bp_solver *s)
     t.omb = t.pool.get<float4>(n);
     t.ombo = t.pool.get<float4>(n);
     t.nmb = t.pool.get<float4>(n);
+    t.GD = t.pool.get<float4>(n);
+    t.rhob = t.pool.get<float>(n);
     if (!(t.gX && t.gV && t.gXn && t.gVn && t.gP && t.gP2 && t.gXs && t.gVs && t.gPart && t.gW && t.gLam && t.G1 &&
           t.G2 && t.FG && t.FV && t.FW && t.g_wind && t.g_stiff && t.g_rest && t.contacts && t.gRho && t.etab &&
-          t.omb && t.ombo && t.nmb))
+          t.omb && t.ombo && t.nmb && t.GD && t.rhob))
         return fail_with(BP_ERR_OUT_OF_MEMORY, "backward: gradient buffers");
     t.grads_ready = true;
     return BP_OK;
@@ -313,7 +311,9 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
     const bool distance = stage_on(p, BP_STAGE_DISTANCE) && s->dist.num_edges > 0;
     const bool pcoll = stage_on(p, BP_STAGE_PARTICLE_COLLISION) && s->has_solid;
     const bool bending = stage_on(p, BP_STAGE_BENDING) && s->bend.num_quads > 0;
-    bool rho_pending = false;  // the post passes' density gradient awaits the last fluid stage
+    // the post passes' and XSPH's density gradient, for the last fluid stage (the density they read)
+    cudaMemsetAsync(t.gRho, 0, (size_t)s->n * sizeof(float), st);
+    bool last_fluid = true;
     for (int r = (int)T.recs.size() - 1; r >= 0; --r) {
         const TapeRec &rec = T.recs[r];
         switch (rec.stage) {
@@ -322,14 +322,14 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
             while (c >= 0 && T.recs[c].stage != TS_COMMIT) --c;
             const float4 *Pc = T.pool4[T.recs[c].slot];
             const size_t bytes = (size_t)s->n * sizeof(float4);
+            const float *rho = T.pool1[rec.aux1];
             if (C.use_xsph) {  // pass C first: gV -> the gradient of pass B's velocities
-                adj_xsph(st, C, Pc, T.pool4[rec.aux + 2], s->off, t.gV, t.gVn, t.gX);
+                adj_xsph(st, C, Pc, T.pool4[rec.aux + 2], s->off, s->mass, rho, t.gV, t.gVn, t.gX, t.gRho);
                 cudaMemcpyAsync(t.gV, t.gVn, bytes, cudaMemcpyDeviceToDevice, st);
             }
-            adj_post(st, C, Pc, T.pool4[rec.slot], T.pool4[rec.aux], T.pool4[rec.aux + 1], T.pool1[rec.aux1], s->off,
-                     t.gV, t.gVn, t.gX, t.gRho, t.etab, t.omb, t.ombo, t.nmb);
+            adj_post(st, C, Pc, T.pool4[rec.slot], T.pool4[rec.aux], T.pool4[rec.aux + 1], rho, s->off, t.gV, t.gVn,
+                     t.gX, t.gRho, t.etab, t.omb, t.ombo, t.nmb);
             cudaMemcpyAsync(t.gV, t.gVn, bytes, cudaMemcpyDeviceToDevice, st);
-            rho_pending = true;
             break;
         }
         case TS_BENDING:
@@ -338,7 +338,8 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
         case TS_XSPH: {  // velocities before XSPH in the slot; positions: the commit's input
             int c = r - 1;
             while (c >= 0 && T.recs[c].stage != TS_COMMIT) --c;
-            adj_xsph(st, C, T.pool4[T.recs[c].slot], T.pool4[rec.slot], s->off, t.gV, t.gVn, t.gX);
+            adj_xsph(st, C, T.pool4[T.recs[c].slot], T.pool4[rec.slot], s->off, s->mass, T.pool1[rec.aux1], t.gV,
+                     t.gVn, t.gX, t.gRho);
             cudaMemcpyAsync(t.gV, t.gVn, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
             break;
         }
@@ -354,8 +355,8 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
             break;
         case TS_FLUID:
             adj_fluid(st, C, T.pool4[rec.slot], s->mass, T.pool1[rec.aux], T.pool1[rec.aux + 1], s->off, t.gP,
-                      rho_pending ? t.gRho : nullptr, t.gLam, t.gPart, t.gP2);
-            rho_pending = false;
+                      last_fluid ? t.gRho : nullptr, t.gLam, t.gPart, t.GD, t.rhob, t.gP2);
+            last_fluid = false;
             cudaMemcpyAsync(t.gP, t.gP2, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
             break;
         case TS_PLANES:
@@ -470,7 +471,7 @@ extern "C" bp_status bp_solver_backward(bp_solver *s, const float *grad_position
     if (!s->tape || s->tape->subs.empty()) return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: nothing recorded");
     Tape &t = *s->tape;
     bp_status stt;
-    if ((stt = check_supported(s, t)) != BP_OK) return stt;
+    if ((stt = check_supported(t)) != BP_OK) return stt;
     if ((stt = ensure_grads(t, s)) != BP_OK) return stt;
     const cudaStream_t st = s->stream;
     const int n = s->n;

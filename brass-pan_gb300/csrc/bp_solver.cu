@@ -865,7 +865,10 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
 
     const bool post_ab = C.use_vort || C.use_akinci;
     if (tape && post_ab) tape->push(TS_POST_AB, s->Vc);
-    if (tape && !post_ab && C.use_xsph) tape->push(TS_XSPH, s->Vc);
+    if (tape && !post_ab && C.use_xsph) {
+        tape->push(TS_XSPH, s->Vc);
+        tape->recs.back().aux1 = tape->snap1(s->rho);  // the density textbook XSPH weighs with
+    }
     // The post passes keep class positions in their lists where lambda left
     // its densities in class order (SimConsts::cls_post); the velocities are
     // gathered into class order with the positions.

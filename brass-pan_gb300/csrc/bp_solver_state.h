@@ -54,7 +54,7 @@ struct TapeRec {
     // it; TS_POST_AB: omega (aux) and normals (aux + 1) after pass A, and with XSPH the velocities
     // after pass B (aux + 2)
     int aux;
-    int aux1 = -1;  // TS_POST_AB: the density the passes read (pool1)
+    int aux1 = -1;  // TS_POST_AB, TS_XSPH: the density the passes read (pool1)
 };
 
 // The intermediates of one substep re-run for its adjoint: each stage's

@@ -317,10 +317,9 @@ bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, float dt, int32
  * Stages with an adjoint: planes, wind, particle-particle contacts with
  * friction, distance constraints, dihedral bending, shape matching (the
  * extracted rotation differentiated at its fixed point), immovables, the
- * velocity update, and in reference mode the fluid density / lambda /
- * position correction, vorticity confinement, Akinci tension and XSPH.
- * Recordings that used picking or textbook-mode fluid passes return
- * BP_ERR_INVALID_ARGUMENT from bp_solver_backward. */
+ * velocity update, the fluid density / lambda / position correction (both
+ * modes), vorticity confinement, Akinci tension and XSPH.  Recordings that
+ * used picking return BP_ERR_INVALID_ARGUMENT from bp_solver_backward. */
 typedef struct bp_gradients {
     float *positions;            /* [N][3] dL/dx at tape begin, original order, or NULL */
     float *velocities;           /* [N][3] dL/dv at tape begin, or NULL */

@@ -251,14 +251,7 @@ def test_backward_restores_the_state(bp, gpu):
 
 
 def test_backward_rejects_what_has_no_adjoint(bp, gpu):
-    abi = bp.abi
     scene, _ = fluid_case(bp, n=4)
-    s = bp.ParticleSolver(scene, bp.make_params(scene, mode=abi.BP_MODE_TEXTBOOK))
-    s.tape_begin(1)
-    s.update(1, DT, 2)
-    with pytest.raises(bp.BrassPanError):
-        s.backward(np.ones((scene.num_particles, 3), np.float32))  # textbook-mode fluid
-    s.close()
     t = bp.ParticleSolver(scene, bp.make_params(scene))
     with pytest.raises(bp.BrassPanError):
         t.backward(np.ones((scene.num_particles, 3), np.float32))  # nothing recorded
@@ -534,3 +527,22 @@ def test_bending_gradients_match_fp64_finite_differences(bp, gpu, oracle):
     wx, wv = loss_weights(scene.num_particles, seed=25)
     g = gpu_gradients(bp, scene, params, frames, wx, wv)
     assert_fd64(fd64_state_pairs(oracle, scene, params, frames, wx, wv, g, seed=26, x_step=FD64_STEP))  # smooth
+
+
+def test_textbook_fluid_gradients_match_fp64_finite_differences(bp, gpu, oracle):
+    """Textbook mode: density over all neighbours, the exact lambda denominator
+    (its gradient norms differentiated through the spiky Hessian), s_corr, and
+    XSPH weighted by m_j / rho_j, whose density gradient joins the last lambda
+    pass's; with vorticity and Akinci tension."""
+    abi = bp.abi
+    scene = bp.scenes.pbf_scene(6, 6, 6, spacing=0.1, seed=11, box=(1.2, 2.0, 1.2), grid_dim=16)
+    scene.positions = (scene.positions + np.float32(0.05)).astype(np.float32)  # off the cell boundaries
+    rng = np.random.default_rng(12)
+    scene.velocities = rng.uniform(-0.5, 0.5, (scene.num_particles, 3)).astype(np.float32)
+    stages = (abi.BP_STAGE_FLUID | abi.BP_STAGE_PLANES | abi.BP_STAGE_VORTICITY | abi.BP_STAGE_AKINCI |
+              abi.BP_STAGE_XSPH)
+    params = bp.make_params(scene, mode=abi.BP_MODE_TEXTBOOK, stage_mask=stages)
+    frames = 2
+    wx, wv = loss_weights(scene.num_particles, seed=27)
+    g = gpu_gradients(bp, scene, params, frames, wx, wv)
+    assert_fd64(fd64_state_pairs(oracle, scene, params, frames, wx, wv, g, seed=28))
