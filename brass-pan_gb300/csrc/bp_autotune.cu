@@ -3,9 +3,10 @@
 //
 // The walk variants (staging each CTA's neighbourhood in shared memory,
 // testing candidates in chunks before the pair terms, the post passes'
-// neighbour lists) and the launch shapes of the unstaged scans (threads per
-// CTA, persistent CTAs) give bit-identical results, so the choice only
-// affects speed.  Each candidate runs one update from the same state (the first call
+// neighbour lists), the launch shapes of the unstaged scans (threads per
+// CTA, persistent CTAs) and iteration fusion (plane collision and commit in
+// the reorder's and the position pass's epilogues) give bit-identical
+// results, so the choice only affects speed.  Each candidate runs one update from the same state (the first call
 // of a configuration captures its CUDA graph; it is run once untimed), timed
 // with CUDA events on the solver's stream; the state is put back after every
 // trial and the fastest variant is kept in the solver's parameters.
@@ -43,7 +44,8 @@ extern "C" bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, floa
         cudaEventDestroy(e0);
         return fail_with(BP_ERR_CUDA, "cudaEventCreate");
     }
-    const int32_t keep = s->prm.walk_options & ~(BP_WALK_NO_SPLIT | BP_WALK_NO_LISTS | BP_WALK_NO_STAGING);
+    const int32_t keep =
+        s->prm.walk_options & ~(BP_WALK_NO_SPLIT | BP_WALK_NO_LISTS | BP_WALK_NO_STAGING | BP_WALK_NO_FUSION);
     float best = -1.f;
     int32_t best_opt = s->prm.walk_options;
     for (int c = 0; c < kNum && st == BP_OK; ++c) {
@@ -100,6 +102,35 @@ extern "C" bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, floa
             best = ms;
             best_block = kShapes[c][0];
             best_persist = kShapes[c][1];
+        }
+        snap.restore(s);
+    }
+    // last, iteration fusion: the fastest so far with its fused launches split,
+    // kept only if it is more than 1 % faster (it launches more kernels for the
+    // same work, so a smaller lead is timing noise)
+    if (st == BP_OK) {
+        bp_params p = s->prm;
+        p.walk_options = best_opt | BP_WALK_NO_FUSION;
+        p.scan_block = best_block;
+        p.scan_persistent = best_persist;
+        if ((st = bp_solver_set_params(s, &p)) == BP_OK &&
+            (st = bp_solver_update(s, num_substeps, dt, iterations, -1, nullptr, nullptr)) == BP_OK) {
+            snap.restore(s);
+            cudaEventRecord(e0, s->stream);
+            if ((st = bp_solver_update(s, num_substeps, dt, iterations, -1, nullptr, nullptr)) == BP_OK) {
+                cudaEventRecord(e1, s->stream);
+                if (cudaEventSynchronize(e1) != cudaSuccess) {
+                    st = fail_with(BP_ERR_CUDA, "autotune: event");
+                } else {
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (out_ms) out_ms[kNum + kNumShapes] = ms;
+                    if (ms < 0.99f * best) {
+                        best = ms;
+                        best_opt = p.walk_options;
+                    }
+                }
+            }
         }
         snap.restore(s);
     }

@@ -708,7 +708,11 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     radix_sort_pairs(st, s->n, s->sort_dim, s->keys, nullptr, s->sorted_keys, s->order, s->sort, true, L);
     launch_cell_offsets(st, s->n, (int)s->ncells, s->sorted_keys, s->off, L);
 
-    const bool fuse_first_planes = planes && !wind && !picking && iterations > 0 && !tape;
+    // iteration fusion: the reorder takes iteration 0's plane collision, and the
+    // position pass the next iteration's or the final commit (BP_WALK_NO_FUSION:
+    // launches of their own; bit-identical either way)
+    const bool fuse = !tape && !(s->prm.walk_options & BP_WALK_NO_FUSION);
+    const bool fuse_first_planes = planes && !wind && !picking && iterations > 0 && fuse;
     ReorderArgs ra;
     ra.order = s->order;
     ra.Xc = s->Xc;
@@ -825,7 +829,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             da.Vs = s->Vs;
             da.orig_s = s->orig_s;
             da.orig_c = s->orig_c;
-            if (!tail && !tape) {
+            if (!tail && fuse) {
                 if (it == iterations - 1) {
                     da.epilogue = 2;
                     committed = true;

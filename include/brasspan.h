@@ -91,11 +91,16 @@ typedef enum bp_mode {
  * cells wraps space, so one table cell holds every real cell D cells apart;
  * the split is kept for grids of at most 2^21 cells and used in a substep
  * while at least 1/32 of the particles share a cell with another real cell's
- * and no particle has moved (D - 2) cells - h from where it was hashed). */
+ * and no particle has moved (D - 2) cells - h from where it was hashed);
+ * BP_WALK_NO_FUSION runs each iteration's plane collision and the final
+ * velocity update and commit as launches of their own, instead of fused into
+ * the reorder (iteration 0's planes) and the position pass's epilogue (the
+ * next iteration's planes, or the commit after the last iteration). */
 #define BP_WALK_NO_STAGING 0x1
 #define BP_WALK_NO_SPLIT 0x2
 #define BP_WALK_NO_LISTS 0x4
 #define BP_WALK_NO_ALIAS_CLASSES 0x8
+#define BP_WALK_NO_FUSION 0x10
 
 /* Every literal of the reference's step as a field.  bp_params_init fills the
  * reference's values; comments give the reference location of each. */
@@ -294,9 +299,11 @@ bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int
  * NO_STAGING, NO_SPLIT, NO_LISTS, NO_STAGING|NO_SPLIT, NO_STAGING|NO_LISTS,
  * NO_SPLIT|NO_LISTS, all three; then, when the fastest of them does not
  * stage, its unstaged scans with 128 and with 64 threads per CTA and with
- * persistent 256-thread CTAs (bp_params.scan_block, .scan_persistent).  The
+ * persistent 256-thread CTAs (bp_params.scan_block, .scan_persistent); last,
+ * the fastest so far without iteration fusion (BP_WALK_NO_FUSION), kept only
+ * when more than 1 % faster.  The
  * choice is kept in the solver's parameters and its walk options written to
- * *out_walk_options; out_ms (or NULL) receives the 11 trial times in that
+ * *out_walk_options; out_ms (or NULL) receives the 12 trial times in that
  * order (0 for a launch-shape trial not run).  No counterpart in the
  * reference. */
 bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,

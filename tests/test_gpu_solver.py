@@ -397,11 +397,12 @@ def test_autotune_keeps_state_and_results(bp, gpu):
     x0 = a.positions()
     opt, ms = a.autotune(2, DT, 4)
     np.testing.assert_array_equal(a.positions(), x0)
-    assert 0 <= opt <= (abi.BP_WALK_NO_SPLIT | abi.BP_WALK_NO_LISTS | abi.BP_WALK_NO_STAGING)
-    assert len(ms) == 11
-    assert all(t > 0 for t in ms[:8])
+    assert 0 <= opt <= (abi.BP_WALK_NO_SPLIT | abi.BP_WALK_NO_LISTS | abi.BP_WALK_NO_STAGING |
+                        abi.BP_WALK_NO_FUSION) and not opt & abi.BP_WALK_NO_ALIAS_CLASSES
+    assert len(ms) == 12
+    assert all(t > 0 for t in ms[:8]) and ms[11] > 0
     assert a.params.scan_block in (0, 64, 128, 256) and a.params.scan_persistent in (0, 1)
-    assert all(t > 0 for t in ms[8:]) == bool(opt & abi.BP_WALK_NO_STAGING)
+    assert all(t > 0 for t in ms[8:11]) == bool(opt & abi.BP_WALK_NO_STAGING)
     for s in (a, b):
         for _ in range(3):
             s.update(2, DT, 4)
@@ -429,6 +430,24 @@ def test_scan_launch_shapes_are_bit_identical(bp, gpu, shape):
         g.close()
     np.testing.assert_array_equal(outs[0][0], outs[1][0])
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
+def test_iteration_fusion_is_bit_identical(bp, gpu):
+    """Plane collision and the final commit fused into the reorder and the
+    position pass's epilogue (the default) or run as launches of their own
+    (BP_WALK_NO_FUSION): the same bits, on a fluid scene with planes and on
+    the mixed scene (whose constraint stages leave only the first fusion)."""
+    abi = bp.abi
+    for scene in (fluid_scene(bp, seed=24), small_mixed_scene(bp, seed=24)):
+        outs = []
+        for opt in (0, abi.BP_WALK_NO_FUSION):
+            g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=opt))
+            for _ in range(4):
+                g.update(2, DT, 4)
+            outs.append((g.positions(), g.velocities()))
+            g.close()
+        np.testing.assert_array_equal(outs[0][0], outs[1][0])
+        np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
 def test_snapshot_resume_is_bit_identical(bp, gpu):
