@@ -345,10 +345,10 @@ def run_samples(bp, torch, stream, flush, local, args):
     """The other configurations and regimes, each a sub-object of the line:
     the 32k dam break (its 100 frames, textbook parameters, and reference
     parameters against the reference's CUDA step), the shape-matching stress
-    test, the 1M PBF block alone against the reference's CUDA step, the
-    mixed scene 200 frames in (late regime: compressed fluid, aliased table)
-    against the reference's CUDA step from the same state, and the mixed
-    scene with textbook parameters."""
+    test, the 1M PBF block alone and a 16.8M block 16 times wider (both
+    against the reference's CUDA step), the mixed scene 200 frames in (late
+    regime: compressed fluid, aliased table) against the reference's CUDA
+    step from the same state, and the mixed scene with textbook parameters."""
     sc = bp.scenes
     out = {}
     small = sc.dam_break_32k(seed=0)
@@ -364,6 +364,10 @@ def run_samples(bp, torch, stream, flush, local, args):
     fluid = build_scene(sc, "fluid", seed=0)
     out["pbf_1m"] = run_sample(bp, torch, stream, flush, local, "fluid", fluid, workload_params(bp, "fluid", fluid),
                                frames=args.steps, warmup=args.warmup, reference_cuda=not args.no_reference_cuda)
+    big = sc.pbf_scene(512, 64, 512, spacing=0.1, seed=0, box=(51.4, 16.0, 51.4), grid_dim=256)
+    out["pbf_16m"] = run_sample(bp, torch, stream, flush, local, "fluid", big, workload_params(bp, "fluid", big),
+                                frames=min(args.steps, 10), warmup=3, reference_cuda=not args.no_reference_cuda)
+    del big
     mixed = build_scene(sc, "mixed", seed=0)
     out["late"] = run_sample(bp, torch, stream, flush, local, "mixed", mixed, workload_params(bp, "mixed", mixed),
                              frames=5, warmup=0, pre_frames=200, reference_cuda=not args.no_reference_cuda)
@@ -373,6 +377,8 @@ def run_samples(bp, torch, stream, flush, local, args):
              "small_reference": workload_name("small", small.num_particles) + ", reference parameters, 100 frames",
              "rigid": workload_name("rigid", rigid.num_particles),
              "pbf_1m": workload_name("fluid", fluid.num_particles) + ", reference parameters",
+             "pbf_16m": f"PBF dam break 512x64x512 (the 1M block 16 times wider), 2^24-cell table, "
+                        f"N={512 * 64 * 512}, reference parameters, {min(args.steps, 10)} frames after 4 untimed",
              "late": workload_name("mixed", mixed.num_particles) + ", frames 201-205 (after 200 untimed)",
              "textbook": workload_name("mixed", mixed.num_particles) + ", textbook parameters"}
     for k, v in out.items():
