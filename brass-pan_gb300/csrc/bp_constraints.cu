@@ -13,6 +13,8 @@
 // Scatter-with-atomics constraints become two deterministic passes: one
 // thread per constraint computes its correction once, then one thread per
 // affected particle sums its incident corrections in a fixed (CSR) order.
+#include <algorithm>
+
 #include "bp_internal.h"
 #include "bp_walk.cuh"
 
@@ -161,8 +163,70 @@ __global__ void __launch_bounds__(256) k_solid_dilate(int D, int nwords, const u
     near[k] = acc;
 }
 
+// The half of its cell p lies in on each axis (bit 0: x, 1: y, 2: z; set: the
+// upper half, whose contact walks reach the next cell rather than the one
+// before).
+__device__ __forceinline__ int octant_of(float3 p, float cell)
+{
+    const float hc = 0.5f * cell;
+    const int ox = cell_coord(__fsub_rn(p.x, hc), cell) == cell_coord(p.x, cell) ? 1 : 0;
+    const int oy = cell_coord(__fsub_rn(p.y, hc), cell) == cell_coord(p.y, cell) ? 2 : 0;
+    const int oz = cell_coord(__fsub_rn(p.z, hc), cell) == cell_coord(p.z, cell) ? 4 : 0;
+    return ox | oy | oz;
+}
+
+// oct[0..7] += the listed solids of each octant (oct zeroed before).
+__global__ void __launch_bounds__(256) k_solid_octant_count(int n, const int *__restrict__ prefix,
+                                                            const int *__restrict__ list, const float4 *__restrict__ P,
+                                                            float cell, int *__restrict__ oct)
+{
+    __shared__ int h[8];
+    if (threadIdx.x < 8) h[threadIdx.x] = 0;
+    __syncthreads();
+    const int total = __ldg(prefix + n);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
+        atomicAdd(&h[octant_of(f3(P[__ldg(list + t)]), cell)], 1);
+    __syncthreads();
+    if (threadIdx.x < 8 && h[threadIdx.x]) atomicAdd(oct + threadIdx.x, h[threadIdx.x]);
+}
+
+// walk = the listed solids grouped by octant (octant o from the sum of the
+// counts before it on; oct[8 + o]: the cursor of octant o, zeroed before).
+// The order within an octant is any: every solid's result is its own.
+__global__ void __launch_bounds__(256) k_solid_octant_scatter(int n, const int *__restrict__ prefix,
+                                                              const int *__restrict__ list,
+                                                              const float4 *__restrict__ P, float cell,
+                                                              int *__restrict__ oct, int *__restrict__ walk)
+{
+    __shared__ int first[8], h[8], base[8];
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int o = 0; o < 8; ++o) {
+            first[o] = run;
+            run += oct[o];
+        }
+    }
+    const int total = __ldg(prefix + n);
+    for (int t0 = blockIdx.x * blockDim.x; t0 < total; t0 += gridDim.x * blockDim.x) {  // uniform per CTA
+        if (threadIdx.x < 8) h[threadIdx.x] = 0;
+        __syncthreads();
+        const int t = t0 + threadIdx.x;
+        int o = -1, i = 0, rank = 0;
+        if (t < total) {
+            i = __ldg(list + t);
+            o = octant_of(f3(P[i]), cell);
+            rank = atomicAdd(&h[o], 1);
+        }
+        __syncthreads();
+        if (threadIdx.x < 8) base[threadIdx.x] = h[threadIdx.x] ? atomicAdd(oct + 8 + threadIdx.x, h[threadIdx.x]) : 0;
+        __syncthreads();
+        if (o >= 0) walk[first[o] + base[o] + rank] = i;
+        __syncthreads();
+    }
+}
+
 void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int *prefix, int *list,
-                       const SolidCells &sc, LaunchLog *L)
+                       const SolidCells &sc, LaunchLog *L, int nsolid, float cell, int *walk, int *oct)
 {
     if (n <= 0) return;
     const int nb = (n + kScanBlock - 1) / kScanBlock;
@@ -178,23 +242,101 @@ void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int
         k_solid_dilate<<<(nwords + 255) / 256, 256, 0, st>>>(sc.D, nwords, sc.cells, sc.near);
         L->done("k_solid_dilate");
     }
+    if (walk && oct && nsolid > 0) {  // launches sized by the count at creation, loops to the device total
+        const int blocks = (nsolid + 255) / 256;
+        cudaMemsetAsync(oct, 0, 16 * sizeof(int), st);
+        k_solid_octant_count<<<blocks, 256, 0, st>>>(n, prefix, list, P, cell, oct);
+        L->done("k_solid_octant_count");
+        k_solid_octant_scatter<<<blocks, 256, 0, st>>>(n, prefix, list, P, cell, oct, walk);
+        L->done("k_solid_octant_scatter");
+    }
 }
 
-// The solids among the candidates of particle i's 27 cells, in walk order:
-// body(j, P[j]) for every solid j with test(-1, P[j]) (a fluid walker: no
-// candidate is itself).  spos[k] = P[list[k]] (k_gather_solids).
+// ---- contact walks over the cells a partner can be stored in ----
+// A contact partner j of walker i lies within 2r of p_i on every axis, and
+// j's cell was hashed from a position at most d (C.contact_reach) from p_j
+// on every axis, so it is the cell of a point within 2r + d of p_i.  The cell
+// function (float add and divide, truncation) is monotone, so on each axis
+// that cell lies between the cells of p_i -+ (2r + d + margin); the margin
+// covers the rounding of p_i -+ (...).  The range is clipped to the walker's
+// 27 cells, which the full walk visits: both walks meet the same pairs in
+// the same order.  A particle stored outside the range has no pair with i.
+
+__device__ __forceinline__ bool contact_axis(float p, int c, float R, float cell, int &lo, int &hi)
+{
+    const float w = R + (1e-4f + fabsf(p) * 2.4e-7f);
+    if (!(w < cell)) return false;  // also a NaN or infinite bound: the whole walk
+    lo = max(cell_coord(__fsub_rn(p, w), cell) - c, -1);
+    hi = min(cell_coord(__fadd_rn(p, w), cell) - c, 1);
+    return true;
+}
+
+// The range of walker i at p (its cell c); the whole 27 cells without a bound.
+__device__ __forceinline__ CellRange contact_range(const SimConsts &C, float3 p)
+{
+    CellRange rg;
+    if (!C.contact_reach) return rg;
+    const float R = __fadd_rn(2.0f * C.radius, __uint_as_float(__ldg(C.contact_reach)));
+    const int3 c = cell_of(p, C);
+    CellRange r;
+    if (contact_axis(p.x, c.x, R, C.cell, r.lox, r.hix) && contact_axis(p.y, c.y, R, C.cell, r.loy, r.hiy) &&
+        contact_axis(p.z, c.z, R, C.cell, r.loz, r.hiz))
+        rg = r;
+    return rg;
+}
+
+// The bound: per axis, the largest |p - p_hash| over all particles (positions
+// P against the positions their cells were hashed from), as float bits (the
+// maximum of non-negative floats is the maximum of their bits; a NaN's bits
+// exceed every finite value's).  *reach must be 0 before the launch.
+__global__ void __launch_bounds__(256) k_contact_reach(int n, const float4 *__restrict__ P,
+                                                       const float4 *__restrict__ hashed, unsigned *__restrict__ reach)
+{
+    unsigned best = 0u;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = P[i], q = __ldg(hashed + i);
+        const float d = fmaxf(fmaxf(fabsf(__fsub_rn(p.x, q.x)), fabsf(__fsub_rn(p.y, q.y))),
+                              fabsf(__fsub_rn(p.z, q.z)));
+        const bool finite = d <= 3.0e38f;
+        best = max(best, finite ? __float_as_uint(d) : 0x7f800000u);
+    }
+    best = __reduce_max_sync(0xffffffffu, best);
+    if ((threadIdx.x & 31) == 0 && best) atomicMax(reach, best);
+}
+
+void launch_contact_reach(cudaStream_t st, int n, const float4 *P, const float4 *hashed, unsigned *reach,
+                          LaunchLog *L)
+{
+    cudaMemsetAsync(reach, 0, sizeof(unsigned), st);
+    if (n <= 0) return;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = std::min((n + 255) / 256, std::max(sms, 1) * 8);
+    k_contact_reach<<<blocks, 256, 0, st>>>(n, P, hashed, reach);
+    L->done("k_contact_reach");
+}
+
+// The solids among the candidates of particle i's 27 cells (or of the cells
+// of rg), in walk order: body(j, P[j]) for every solid j with test(-1, P[j])
+// (a fluid walker: no candidate is itself).  spos[k] = P[list[k]]
+// (k_gather_solids).
 template <class T, class B>
 __device__ __forceinline__ void walk_solids(float3 pi, const float4 *__restrict__ spos, const GridView &v,
                                             const SimConsts &C, const int *__restrict__ prefix,
-                                            const int *__restrict__ list, T &&test, B &&body)
+                                            const int *__restrict__ list, T &&test, B &&body,
+                                            CellRange rg = CellRange{})
 {
     const int3 c = cell_of(pi, C);
     const unsigned m = v.mask, D = (unsigned)v.D;
-    const unsigned z0 = (unsigned)(c.z - 1) & m, z2 = (unsigned)(c.z + 1) & m;
-    const bool wrap = !(z0 < z2);
+    const unsigned z0 = (unsigned)(c.z + rg.loz) & m, z2 = (unsigned)(c.z + rg.hiz) & m;
+    // a range of 3 cells never starts and ends on one table cell (D >= 4)
+    const bool wrap = (rg.hiz - rg.loz == 2) ? !(z0 < z2) : z0 > z2;
 #pragma unroll 1
     for (int col = 0; col < 9; ++col) {
-        const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
+        const int dx = col / 3 - 1, dy = col % 3 - 1;
+        if (dx < rg.lox || dx > rg.hix || dy < rg.loy || dy > rg.hiy) continue;
+        const unsigned x = (unsigned)(c.x + dx) & m, y = (unsigned)(c.y + dy) & m;
         const unsigned base = x * D * D + y * D;
 #pragma unroll 1
         for (int piece = 0; piece < (wrap ? 2 : 1); ++piece) {
@@ -267,8 +409,9 @@ __device__ __forceinline__ void collide_one(const SimConsts &C, int i, const flo
                     sf -= (w1 * tdx) * fminf(__fmul_rn(C.fd, __fsqrt_rn(__fdiv_rn(dxi2, tl2))), 1.0f);
             }
     };
-    if (phi < 0 && solid_prefix) walk_solids(xip, solid_pos, v, C, solid_prefix, solid_list, test, body);
-    else walk_neighbors<Split>(i, xip, 0, P, v, C, S, g, test, body);
+    const CellRange rg = contact_range(C, xip);
+    if (phi < 0 && solid_prefix) walk_solids(xip, solid_pos, v, C, solid_prefix, solid_list, test, body, rg);
+    else walk_neighbors<Split, true>(i, xip, 0, P, v, C, S, g, test, body, rg);
     const float3 d = (count == 0) ? sd : sd + sf / (float)count;
     const float3 p = xip + d;
     Pout[i] = make_float4(p.x, p.y, p.z, pi4.w);
@@ -364,8 +507,10 @@ __global__ void __launch_bounds__(256) k_gather_solids(int n, const int *__restr
         spos[k] = P[__ldg(list + k)];
 }
 
-// The solid particles, one thread each through the compacted list, so the
-// long walks of solids scattered through fluid run in full warps.
+// The solid particles, one thread each through the compacted list (in
+// walk order: grouped by octant, so that a warp's contact walks take the same
+// cells), so the long walks of solids scattered through fluid run in full
+// warps.
 template <bool Split>
 __global__ void __launch_bounds__(kWalkThreads)
     k_particle_collision_solids(SimConsts C, int nsolid, const float4 *__restrict__ P,
@@ -385,7 +530,7 @@ __global__ void __launch_bounds__(kWalkThreads)
 
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
                                const float *w, const int *off, const int *tile_solid, const int *solid_prefix,
-                               const int *solid_list, int nsolid, bool solids_apart,
+                               const int *solid_list, const int *solid_walk, int nsolid, bool solids_apart,
                                const unsigned long long *solid_near, float4 *solid_pos, float4 *Pout, LaunchLog *L)
 {
     if (C.n <= 0) return;
@@ -409,12 +554,11 @@ void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4
     if (apart) {  // the unstaged scans' CTA size (SimConsts::scan_block) here too
         const int sb = C.scan_block > 0 ? C.scan_block : kWalkThreads;
         const int sg = (nsolid + sb - 1) / sb;
+        const int *order = solid_walk ? solid_walk : solid_list;
         if (C.split)
-            k_particle_collision_solids<true><<<sg, sb, 0, st>>>(C, nsolid, P, Xs, w, off, solid_prefix, solid_list,
-                                                                Pout);
+            k_particle_collision_solids<true><<<sg, sb, 0, st>>>(C, nsolid, P, Xs, w, off, solid_prefix, order, Pout);
         else
-            k_particle_collision_solids<false><<<sg, sb, 0, st>>>(C, nsolid, P, Xs, w, off, solid_prefix, solid_list,
-                                                                 Pout);
+            k_particle_collision_solids<false><<<sg, sb, 0, st>>>(C, nsolid, P, Xs, w, off, solid_prefix, order, Pout);
         L->done("launch_particle_collision_solids");
     }
 }

@@ -405,6 +405,7 @@ __global__ void __launch_bounds__(256) k_reorder(SimConsts C, ReorderArgs a)
         a.cls[i] = alias_class(c.x, c.y, c.z, s < 0 ? C.D : C.scn[s].D);
         a.pos0[i] = make_float4(p.x, p.y, p.z, 0.f);
     }
+    if (a.hash_pos) a.hash_pos[i] = make_float4(p.x, p.y, p.z, 0.f);  // the position its cell was hashed from
     if (a.inv_scaled) {
         const float scale = powf(2.7182818284f, -C.mass_k * x.y);
         a.inv_scaled[i] = 1.0f / (scale * X.w);

@@ -93,6 +93,7 @@ struct ReorderArgs {
     int *tile_solid;       // nullptr, or flags set for 256-particle tiles holding a solid (cleared before)
     int *cls;              // nullptr, or the alias class of each sorted particle at hash time
     float4 *pos0;          // with cls: the hash-time (predicted) position of each sorted particle
+    float4 *hash_pos;      // nullptr, or the same for the contact walks' reach (k_contact_reach)
 };
 void launch_reorder(cudaStream_t st, const SimConsts &C, const ReorderArgs &a, LaunchLog *L);
 
@@ -159,10 +160,17 @@ void launch_commit(cudaStream_t st, const SimConsts &C, const float4 *P, const f
 // solid_pos: C.n + 1 float4 of scratch (the listed solids' positions, gathered
 // first); the kernels take the solid count from solid_prefix[C.n] (this
 // substep's compaction), nsolid (the count at creation) only sizes launches.
+// solid_walk: nullptr, or the listed solids in the order their launch takes
+// them (launch_solid_list).  With C.contact_reach the contact walks visit only
+// the cells a partner can be stored in (launch_contact_reach, just before).
 void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *Xs,
                                const float *w, const int *off, const int *tile_solid, const int *solid_prefix,
-                               const int *solid_list, int nsolid, bool solids_apart,
+                               const int *solid_list, const int *solid_walk, int nsolid, bool solids_apart,
                                const unsigned long long *solid_near, float4 *solid_pos, float4 *Pout, LaunchLog *L);
+// *reach = the bits of the largest per-axis |P - hashed| over the n particles
+// (NaN or infinite: +inf).
+void launch_contact_reach(cudaStream_t st, int n, const float4 *P, const float4 *hashed, unsigned *reach,
+                          LaunchLog *L);
 // Bit masks over the D^3 table cells of one scene (cells == nullptr: not built):
 // cells marks the stored cells (keys) of the solids, near the cells whose 27
 // cells hold one.
@@ -173,8 +181,12 @@ struct SolidCells {
 };
 // solid_prefix[i] (i <= n): solids among sorted [0, i); solid_list: their sorted indices in order.
 // totals: (n + 1023) / 1024 ints of scratch.
+// With walk (and oct, 16 ints of scratch): the listed solids again, grouped
+// by the half of its cell each one's position lies in on every axis, for the
+// solids' contact launch (the warps of a group walk the same cells).
 void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int *solid_prefix, int *solid_list,
-                       const SolidCells &sc, LaunchLog *L);
+                       const SolidCells &sc, LaunchLog *L, int nsolid = 0, float cell = 0.f, int *walk = nullptr,
+                       int *oct = nullptr);
 struct DistanceArgs {
     int num_edges;
     const int2 *pairs;       // original ids

@@ -83,8 +83,9 @@ extern "C" void bp_params_init(bp_params *p, float r)
     p->rotation_iterations = 20;
     p->neighbor_skin = 0.0f;  // Verlet lists measured slower than the lambda-recorded lists (opt-in)
     // staging each CTA's neighbourhood in shared memory measured slower than
-    // reading it through a full-size L1 (opt-in; bp_solver_autotune times both)
-    p->walk_options = BP_WALK_NO_STAGING;
+    // reading it through a full-size L1, and the contact walks' cell culling
+    // pays only where solids dominate (both opt-in; bp_solver_autotune times them)
+    p->walk_options = BP_WALK_NO_STAGING | BP_WALK_NO_CONTACT_CULLING;
     p->bending_stiffness = 0.8f;                   // bending.cuh:71
 }
 
@@ -394,6 +395,10 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         (st = s->alloc(&s->solid_list, N)) || (st = s->alloc(&s->solid_totals, (N + 1023) / 1024)) ||
         (st = s->alloc(&s->nbr, N * kPostListCap)) ||
         (st = s->alloc(&s->nbr_count, N)))
+        return bail(st);
+    // contact walks restricted to the cells a partner can be stored in
+    if (has_solid && ((st = s->alloc(&s->hash_pos, N)) || (st = s->alloc(&s->contact_reach, 1)) ||
+                      (st = s->alloc(&s->solid_walk, N)) || (st = s->alloc(&s->solid_oct, 16))))
         return bail(st);
     // fluid next to solids: the cell masks that let fluid far from every
     // solid skip its walk over the solids (one scene's table)
@@ -737,6 +742,9 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     }
     ra.cls = classes ? ca.cls : nullptr;
     ra.pos0 = classes ? ca.pos0 : nullptr;
+    // the contact walks' reach (BP_WALK_NO_CONTACT_CULLING: the 27 cells)
+    const bool culling = pcoll && s->hash_pos && !(s->prm.walk_options & BP_WALK_NO_CONTACT_CULLING);
+    ra.hash_pos = culling ? s->hash_pos : nullptr;
     launch_reorder(st, C, ra, L);
     if (classes) launch_class_order(st, s->n, s->sorted_keys, s->off, s->mass, ca, s->sort, L);
     // walks read candidates in class order: gather P before each walking launch
@@ -779,7 +787,8 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             sc.cells = s->solid_cells;
             sc.near = s->solid_near;
         }
-        launch_solid_list(st, s->n, cur, s->solid_totals, s->solid_prefix, s->solid_list, sc, L);
+        launch_solid_list(st, s->n, cur, s->solid_totals, s->solid_prefix, s->solid_list, sc, L, s->num_solids,
+                          C.cell, culling ? s->solid_walk : nullptr, s->solid_oct);
     }
     if (wind) {
         if (tape) tape->push(TS_WIND, cur);
@@ -802,8 +811,14 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             // faster than walking them in the staged CTAs, whether solids are
             // scattered through fluid or the whole scene)
             refresh(cur);
-            launch_particle_collision(st, Cit, cur, s->Xs, s->w, s->off, s->tile_solid, s->solid_prefix,
-                                      s->solid_list, s->num_solids, true, s->solid_near, s->solid_pos, other, L);
+            SimConsts Cc = Cit;
+            if (culling) {
+                launch_contact_reach(st, s->n, cur, s->hash_pos, s->contact_reach, L);
+                Cc.contact_reach = s->contact_reach;
+            }
+            launch_particle_collision(st, Cc, cur, s->Xs, s->w, s->off, s->tile_solid, s->solid_prefix,
+                                      s->solid_list, culling ? s->solid_walk : nullptr, s->num_solids, true,
+                                      s->solid_near, s->solid_pos, other, L);
             std::swap(cur, other);
         }
         if (fluid) {

@@ -228,6 +228,14 @@ inline void launch_scan(void (*kernel)(KArgs...), const SimConsts &C, size_t sme
     kernel<<<grid, block, smem, st>>>(static_cast<Args &&>(args)...);
 }
 
+// The cells a ranged walk visits: offsets from the walker's cell, each axis
+// a sub-range of -1..1 (the whole 27 cells: CellRange{}).  The cells are
+// visited in the order of the full walk, so a walk over a sub-range meets its
+// candidates in the same order as the full walk does.
+struct CellRange {
+    int lox = -1, hix = 1, loy = -1, hiy = 1, loz = -1, hiz = 1;
+};
+
 // Shared-memory index of candidate run [b, e) of column k for group g, or -1.
 __device__ __forceinline__ int staged_index(const StageShared &S, int g, int k, int b, int e)
 {
@@ -397,23 +405,30 @@ __device__ __forceinline__ void walk_run_cls(int qb, int e, int qi, int i, int j
 // (candidates j >= lo only), a piece of i's own class starts at i's class
 // position (class order keeps sorted order); other pieces filter in the body.
 // Slots: the body gets class positions (walk_run_cls; lo must be 0).
-template <bool Split, bool Slots = false, class T, class B>
+// Ranged: only the cells of rg (the columns and z cells outside it skipped).
+template <bool Split, bool Slots = false, bool Ranged = false, class T, class B>
 __device__ __forceinline__ void walk_classes(int i, int3 c, int lo, const GridView &v, const SimConsts &C, T &test,
-                                             B &body)
+                                             B &body, CellRange rg = CellRange{})
 {
     const unsigned m = v.mask;
     const unsigned D = (unsigned)v.D;
     const int sh = __ffs(v.D) - 1;
     const int qi = __ldg(C.cls_inv + i);
     const int ki = lo > 0 ? __ldg(C.cls_of + i) : -1;
-    const unsigned z0 = (unsigned)(c.z - 1) & m;
-    const unsigned z2 = (unsigned)(c.z + 1) & m;
-    const bool wrap = !(z0 < z2);
-    const int kz0 = ((c.z - 1) >> sh) & 1, kz2 = ((c.z + 1) >> sh) & 1;
+    const int zl = Ranged ? c.z + rg.loz : c.z - 1, zh = Ranged ? c.z + rg.hiz : c.z + 1;
+    const unsigned z0 = (unsigned)zl & m;
+    const unsigned z2 = (unsigned)zh & m;
+    // a range of 3 cells never starts and ends on one table cell (D >= 4)
+    const bool wrap = (Ranged && zh - zl != 2) ? z0 > z2 : !(z0 < z2);
+    const int kz0 = (zl >> sh) & 1, kz2 = (zh >> sh) & 1;
     const int *__restrict__ off = C.cls_off + v.base;
     const size_t keys = (size_t)C.cls_T;
 #pragma unroll 1
     for (int col = 0; col < 9; ++col) {
+        if constexpr (Ranged) {
+            const int dx = col / 3 - 1, dy = col % 3 - 1;
+            if (dx < rg.lox || dx > rg.hix || dy < rg.loy || dy > rg.hiy) continue;
+        }
         const int xr = c.x + col / 3 - 1, yr = c.y + col % 3 - 1;
         const unsigned base = ((unsigned)xr & m) * D * D + ((unsigned)yr & m) * D;
         const int kxy = ((xr >> sh) & 1) | (((yr >> sh) & 1) << 1);
@@ -437,10 +452,12 @@ __device__ __forceinline__ void walk_classes(int i, int3 c, int lo, const GridVi
 // list's entries instead, in their recorded (walk) order.  The pair arithmetic of the
 // callers uses explicitly rounded operations, so every inlined copy of the
 // pair functions produces the same bits.
-template <bool Split, class T, class B>
+// Ranged: only the cells of rg (the walk over its sub-range, or the Verlet
+// list, whose entries are the full walk's).
+template <bool Split, bool Ranged = false, class T, class B>
 __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const float4 *__restrict__ P,
                                                const GridView &v, const SimConsts &C, const StageShared *S, int g,
-                                               T &&test, B &&body)
+                                               T &&test, B &&body, CellRange rg = CellRange{})
 {
     const int3 c = cell_of(pi, C);
     const unsigned m = v.mask;
@@ -455,19 +472,23 @@ __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const f
         });
         return;
     }
-    const unsigned z0 = (unsigned)(c.z - 1) & m;
-    const unsigned z2 = (unsigned)(c.z + 1) & m;
+    const unsigned z0 = (unsigned)(c.z + (Ranged ? rg.loz : -1)) & m;
+    const unsigned z2 = (unsigned)(c.z + (Ranged ? rg.hiz : 1)) & m;
 
     if (C.cls_perm && !staged && __ldg(C.cls_moved) == 0) {
         if (C.nl_stats) atomicAdd(C.nl_stats + 4, 1u);
-        walk_classes<Split>(i, c, lo, v, C, test, body);
+        walk_classes<Split, false, Ranged>(i, c, lo, v, C, test, body, rg);
         return;
     }
 
     // 27-cell walk: 9 column runs, split where z wraps around the table
-    const bool wrap = !(z0 < z2);
+    const bool wrap = (Ranged && rg.hiz - rg.loz != 2) ? z0 > z2 : !(z0 < z2);
 #pragma unroll 1
     for (int col = 0; col < 9; ++col) {
+        if constexpr (Ranged) {
+            const int dx = col / 3 - 1, dy = col % 3 - 1;
+            if (dx < rg.lox || dx > rg.hix || dy < rg.loy || dy > rg.hiy) continue;
+        }
         const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
         const unsigned base = x * D * D + y * D;
 #pragma unroll 1

@@ -171,11 +171,11 @@ class ParticleSolver:
 
     def autotune(self, num_substeps: int, dt: float, iterations: int) -> tuple[int, list[float]]:
         """Keep the fastest walk variant and scan launch shape for this scene;
-        returns the walk options and the trial times (ms) of the twelve
+        returns the walk options and the trial times (ms) of the thirteen
         candidates (bp_solver_autotune); the launch shape chosen is in
         self.params (scan_block, scan_persistent)."""
         opt = C.c_int32()
-        ms = (C.c_float * 12)()
+        ms = (C.c_float * 13)()
         abi.check(self.lib, self.lib.bp_solver_autotune(self.handle, num_substeps, C.c_float(dt), iterations,
                                                         C.byref(opt), ms))
         abi.check(self.lib, self.lib.bp_solver_get_params(self.handle, C.byref(self.params)))

@@ -95,12 +95,16 @@ typedef enum bp_mode {
  * BP_WALK_NO_FUSION runs each iteration's plane collision and the final
  * velocity update and commit as launches of their own, instead of fused into
  * the reorder (iteration 0's planes) and the position pass's epilogue (the
- * next iteration's planes, or the commit after the last iteration). */
+ * next iteration's planes, or the commit after the last iteration);
+ * BP_WALK_NO_CONTACT_CULLING makes the particle-contact walks visit all 27
+ * cells instead of only the cells a contact partner can be stored in (from
+ * a bound on every particle's displacement since its cell was hashed). */
 #define BP_WALK_NO_STAGING 0x1
 #define BP_WALK_NO_SPLIT 0x2
 #define BP_WALK_NO_LISTS 0x4
 #define BP_WALK_NO_ALIAS_CLASSES 0x8
 #define BP_WALK_NO_FUSION 0x10
+#define BP_WALK_NO_CONTACT_CULLING 0x20
 
 /* Every literal of the reference's step as a field.  bp_params_init fills the
  * reference's values; comments give the reference location of each. */
@@ -132,7 +136,8 @@ typedef struct bp_params {
     int32_t rotation_iterations; /* 20 (shapematching.cuh:72) */
     float neighbor_skin;         /* skin of the per-substep Verlet lists, as a fraction of h
                                     (0 disables them; results are identical either way): 0 */
-    int32_t walk_options;        /* BP_WALK_* tuning switches of the neighbour walks: BP_WALK_NO_STAGING */
+    int32_t walk_options;        /* BP_WALK_* tuning switches of the neighbour walks:
+                                    BP_WALK_NO_STAGING | BP_WALK_NO_CONTACT_CULLING */
     float bending_stiffness;     /* 0.8 (bending.cuh:71) */
     /* Launch shape of the neighbour-scan kernels when they do not stage
      * (BP_WALK_NO_STAGING; results are identical under every shape):
@@ -299,13 +304,13 @@ bp_status bp_solver_walk_stats(bp_solver *s, int32_t num_substeps, float dt, int
  * NO_STAGING, NO_SPLIT, NO_LISTS, NO_STAGING|NO_SPLIT, NO_STAGING|NO_LISTS,
  * NO_SPLIT|NO_LISTS, all three; then, when the fastest of them does not
  * stage, its unstaged scans with 128 and with 64 threads per CTA and with
- * persistent 256-thread CTAs (bp_params.scan_block, .scan_persistent); last,
- * the fastest so far without iteration fusion (BP_WALK_NO_FUSION), kept only
- * when more than 1 % faster.  The
+ * persistent 256-thread CTAs (bp_params.scan_block, .scan_persistent); then
+ * the fastest so far without iteration fusion (BP_WALK_NO_FUSION), and, in a
+ * scene with particle contacts, with the contact walks' cell culling (without
+ * BP_WALK_NO_CONTACT_CULLING), each kept only when more than 1 % faster.  The
  * choice is kept in the solver's parameters and its walk options written to
- * *out_walk_options; out_ms (or NULL) receives the 12 trial times in that
- * order (0 for a launch-shape trial not run).  No counterpart in the
- * reference. */
+ * *out_walk_options; out_ms (or NULL) receives the 13 trial times in that
+ * order (0 for a trial not run).  No counterpart in the reference. */
 bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, float dt, int32_t iterations,
                              int32_t *out_walk_options, float *out_ms);
 

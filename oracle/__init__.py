@@ -117,7 +117,7 @@ REFERENCE_LITERALS = dict(
     mode=0, stage_mask=0x7FF, solid_density_scale=2.0, lambda_denominator=15000.0, relaxation=300.0,
     scorr_k=0.0001, scorr_n=4, scorr_dq=0.03, delta_clamp=5.0, vorticity_eps=0.001, surface_tension=0.5,
     xsph_c=0.0002, friction_static=0.5, friction_dynamic=0.0, mass_scaling_k=2.0, wind_drag=10.0,
-    wind_lift=100.0, rotation_iterations=20, neighbor_skin=0.0, walk_options=1, bending_stiffness=0.8)
+    wind_lift=100.0, rotation_iterations=20, neighbor_skin=0.0, walk_options=0x21, bending_stiffness=0.8)
 
 
 def reference_params(scene, **overrides):

@@ -398,9 +398,10 @@ def test_autotune_keeps_state_and_results(bp, gpu):
     opt, ms = a.autotune(2, DT, 4)
     np.testing.assert_array_equal(a.positions(), x0)
     assert 0 <= opt <= (abi.BP_WALK_NO_SPLIT | abi.BP_WALK_NO_LISTS | abi.BP_WALK_NO_STAGING |
-                        abi.BP_WALK_NO_FUSION) and not opt & abi.BP_WALK_NO_ALIAS_CLASSES
-    assert len(ms) == 12
-    assert all(t > 0 for t in ms[:8]) and ms[11] > 0
+                        abi.BP_WALK_NO_FUSION | abi.BP_WALK_NO_CONTACT_CULLING)
+    assert not opt & abi.BP_WALK_NO_ALIAS_CLASSES
+    assert len(ms) == 13
+    assert all(t > 0 for t in ms[:8]) and ms[11] > 0 and ms[12] > 0  # the scene has contacts
     assert a.params.scan_block in (0, 64, 128, 256) and a.params.scan_persistent in (0, 1)
     assert all(t > 0 for t in ms[8:11]) == bool(opt & abi.BP_WALK_NO_STAGING)
     for s in (a, b):
@@ -443,6 +444,47 @@ def test_iteration_fusion_is_bit_identical(bp, gpu):
         for opt in (0, abi.BP_WALK_NO_FUSION):
             g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=opt))
             for _ in range(4):
+                g.update(2, DT, 4)
+            outs.append((g.positions(), g.velocities()))
+            g.close()
+        np.testing.assert_array_equal(outs[0][0], outs[1][0])
+        np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
+def contact_scene(bp, seed=0):
+    """Grains, two rigid boxes and a rope over a fluid pool, with random
+    velocities: contacts between every pair of phases."""
+    sc = bp.scenes
+    rng = np.random.default_rng(seed)
+    s = sc.Scene(name="contacts")
+    s.particle_radius, s.kernel_radius, s.cell_size, s.grid_dim, s.rest_density = 0.05, 0.2, 0.2, 16, 1000.0
+    sc.box_planes(s, (0, 0, 0), (1.6, 3.0, 1.6))
+    s.add_fluid_block((12, 4, 12), (0.1, 0.05, 0.1), (0.1, 0.1, 0.1), 1.0, jitter=0.002, rng=rng)
+    s.add_granulars_block((5, 5, 5), (0.4, 0.5, 0.4), (0.095, 0.095, 0.095), 1.0)
+    s.add_rigid_box((3, 3, 3), (0.9, 0.7, 0.9), (0.1, 0.1, 0.1), 1.0)
+    s.add_rigid_box((4, 2, 3), (0.2, 1.1, 0.9), (0.1, 0.1, 0.1), 1.0)
+    s.add_rope((0.1, 1.4, 0.2), (1.4, 1.4, 1.3), 16, 0.5)
+    s.velocities = rng.uniform(-0.5, 0.5, (s.num_particles, 3)).astype(np.float32)
+    return s
+
+
+@pytest.mark.parametrize("walk", [0, "NO_STAGING", "NO_SPLIT"])
+def test_contact_culling_is_bit_identical(bp, gpu, walk):
+    """Contact walks over only the cells a partner can be stored in (the
+    default) against the full 27-cell walks (BP_WALK_NO_CONTACT_CULLING): the
+    same bits, on a scene with contacts between every pair of phases, the
+    mixed scene and grains alone."""
+    abi = bp.abi
+    wo = 0 if walk == 0 else getattr(abi, "BP_WALK_" + walk)
+    grains = bp.scenes.Scene(name="grains")
+    grains.particle_radius, grains.kernel_radius, grains.cell_size, grains.grid_dim = 0.05, 0.2, 0.2, 16
+    bp.scenes.box_planes(grains, (0, 0, 0), (1.6, 3.0, 1.6))
+    grains.add_granulars_block((6, 6, 6), (0.3, 0.2, 0.3), (0.09, 0.09, 0.09), 1.0)
+    for scene in (contact_scene(bp, seed=5), small_mixed_scene(bp, seed=25), grains):
+        outs = []
+        for opt in (wo, wo | abi.BP_WALK_NO_CONTACT_CULLING):
+            g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=opt))
+            for _ in range(6):
                 g.update(2, DT, 4)
             outs.append((g.positions(), g.velocities()))
             g.close()
