@@ -335,27 +335,61 @@ __global__ void k_reset_start_end(int n, const int *__restrict__ sorted, int *__
 }
 
 // Dense prefix: off[c] = number of particles whose key is below c, for
-// c in [0, ncells].  Each thread takes `per` consecutive cells: one binary
-// search for the first, then a forward scan over the keys of its cells.
-// Tables with many more cells than particles (mostly empty cells) take 8
-// cells per thread, so they cost one search per 8 cells; dense tables take
-// one, so no thread walks a long run of keys.
-__global__ void k_cell_offsets(int n, int ncells, int per, const int *__restrict__ sorted, int *__restrict__ off,
-                               Gate gate)
+// c in [0, ncells].  Dense tables (per == 1): one cell per thread, found by
+// a binary search over all keys.  Tables with many more cells than
+// particles (mostly empty cells) give each warp 32 * per consecutive cells:
+// lanes 0 and 31 search the keys at the ends of that range, the warp copies
+// the keys between them into shared memory, and lane l takes cells l,
+// l + 32, l + 64, ... of the range (so that every store of the warp writes
+// 32 consecutive entries), counting the copied keys below each cell from
+// where its previous cell's count stopped.  A range holding more keys than
+// the copy takes searches among them instead.
+constexpr int kOffsetKeysPerWarp = 512;
+
+__device__ __forceinline__ int lower_bound_key(const int *__restrict__ sorted, int lo, int hi, long long c)
 {
-    if (gate_closed(gate)) return;
-    const long long c0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * per;
-    if (c0 > ncells) return;
-    int lo = 0, hi = n;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (__ldg(sorted + mid) < c0) lo = mid + 1;
+        if (__ldg(sorted + mid) < c) lo = mid + 1;
         else hi = mid;
     }
-    const long long c1 = min(c0 + per, (long long)ncells + 1);
-    for (long long c = c0; c < c1; ++c) {
-        while (lo < n && __ldg(sorted + lo) < c) ++lo;
-        off[c] = lo;
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) k_cell_offsets(int n, int ncells, int per, const int *__restrict__ sorted,
+                                                      int *__restrict__ off, Gate gate)
+{
+    __shared__ int keys[256 / 32][kOffsetKeysPerWarp];
+    if (gate_closed(gate)) return;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (per == 1) {
+        if (t <= ncells) off[t] = lower_bound_key(sorted, 0, n, t);
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    int *wk = keys[threadIdx.x >> 5];
+    const long long w0 = (t - lane) * per, w1 = w0 + 32LL * per;  // the warp's cells [w0, w1)
+    int a = 0, b = n;
+    if (lane == 0) a = lower_bound_key(sorted, 0, n, w0);
+    if (lane == 31) b = lower_bound_key(sorted, 0, n, w1);
+    a = __shfl_sync(0xffffffffu, a, 0);
+    b = __shfl_sync(0xffffffffu, b, 31);
+    // every key before a is below w0, the key at b (if any) is at least w1
+    const int cnt = b - a;
+    if (cnt <= kOffsetKeysPerWarp) {
+        for (int q = lane; q < cnt; q += 32) wk[q] = __ldg(sorted + a + q);
+        __syncwarp();
+        int lo = 0;
+        for (long long c = w0 + lane; c < w1 && c <= ncells; c += 32) {
+            while (lo < cnt && wk[lo] < c) ++lo;
+            off[c] = a + lo;
+        }
+    } else {
+        int lo = a;
+        for (long long c = w0 + lane; c < w1 && c <= ncells; c += 32) {
+            lo = lower_bound_key(sorted, lo, b, c);
+            off[c] = lo;
+        }
     }
 }
 
@@ -375,7 +409,7 @@ void launch_reset_start_end(cudaStream_t st, int n, const int *sorted, int *star
 
 void launch_cell_offsets(cudaStream_t st, int n, int ncells, const int *sorted, int *off, LaunchLog *L, Gate gate)
 {
-    const int per = ncells > 4LL * n ? 8 : 1;
+    const int per = ncells > 4LL * n ? 32 : 1;
     const long long threads = ((long long)ncells + 1 + per - 1) / per;
     k_cell_offsets<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(n, ncells, per, sorted, off, gate);
     L->done(__func__);
