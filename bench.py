@@ -620,6 +620,8 @@ def run_ours(args):
             p.walk_options |= bp.abi.BP_WALK_NO_SPLIT
         if args.no_lists:
             p.walk_options |= bp.abi.BP_WALK_NO_LISTS
+        if args.contact_culling:
+            p.walk_options &= ~bp.abi.BP_WALK_NO_CONTACT_CULLING
         return p
 
     if args.workload == "batch":
@@ -895,6 +897,8 @@ def main():
     ap.add_argument("--no-split", action="store_true", help="evaluate pair terms as candidates are tested")
     ap.add_argument("--no-lists", action="store_true", help="post passes B and C walk their cells")
     ap.add_argument("--no-autotune", action="store_true", help="keep the walk options given instead of timing them")
+    ap.add_argument("--contact-culling", action="store_true",
+                    help="contact walks over only the cells a partner can be stored in (with --no-autotune)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
