@@ -13,7 +13,9 @@
 // lambda / position correction in both modes (with s_corr and the per-pair
 // clamp), distance constraints, dihedral bending, shape matching (rotation
 // differentiated at its fixed point), immovables, the velocity update,
-// vorticity confinement, Akinci tension and XSPH.
+// vorticity confinement, Akinci tension, XSPH and picking.
+#include <algorithm>
+
 #include "bp_dual.cuh"
 #include "bp_internal.h"
 #include "bp_walk.cuh"
@@ -1304,6 +1306,37 @@ void adj_post(cudaStream_t st, const SimConsts &C, const float4 *P, const float4
     k_adj_post_eta<<<b, kWalkThreads, 0, st>>>(C, P, off, Om, gVb, etab, omb);
     k_adj_post_b<<<b, kWalkThreads, 0, st>>>(C, P, off, Om, Nm, gVb, etab, omb, ombo, nmb, gRho, gX);
     k_adj_post_a<<<b, kWalkThreads, 0, st>>>(C, P, V, off, rho, gVb, ombo, nmb, gV, gRho, gX);
+}
+
+// ---- picking: the picked particle's position (and velocity) is overwritten
+// with the target, so nothing before it reaches the loss through them ----
+
+__global__ void k_adj_unpick(int id, const int *__restrict__ to_new, float4 *__restrict__ g1, float4 *__restrict__ g2)
+{
+    const int i = to_new[id];
+    g1[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (g2) g2[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void k_adj_unpick_orig(int n, int id, const int *__restrict__ orig, float4 *__restrict__ g1,
+                                  float4 *__restrict__ g2)
+{
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < n; o += gridDim.x * blockDim.x)
+        if (orig[o] == id) {
+            g1[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+            g2[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+}
+
+void adj_unpick(cudaStream_t st, int id, const int *to_new, float4 *g1, float4 *g2)
+{
+    k_adj_unpick<<<1, 1, 0, st>>>(id, to_new, g1, g2);
+}
+
+void adj_unpick_orig(cudaStream_t st, int n, int id, const int *orig, float4 *g1, float4 *g2)
+{
+    if (n <= 0) return;
+    k_adj_unpick_orig<<<std::min(blocks(n), 1024), 256, 0, st>>>(n, id, orig, g1, g2);
 }
 
 }  // namespace bp

@@ -43,6 +43,8 @@ void adj_shape_matching(cudaStream_t st, const RigidArgs &a, const float4 *rot, 
                         float4 *gP);
 void adj_contacts(cudaStream_t st, const SimConsts &C, const float4 *Pin, const float4 *Xs, const float *w,
                   const int *off, int *count, const float4 *gOut, float4 *gIn, float4 *gXs, float *gW);
+void adj_unpick(cudaStream_t st, int id, const int *to_new, float4 *g1, float4 *g2);
+void adj_unpick_orig(cudaStream_t st, int n, int id, const int *orig, float4 *g1, float4 *g2);
 void adj_bending(cudaStream_t st, const BendingArgs &a, float kb, const float4 *Pin, const float *w, const int *to_new,
                  float4 *gP, float *gW);
 void adj_post(cudaStream_t st, const SimConsts &C, const float4 *P, const float4 *V, const float4 *Om,
@@ -72,6 +74,7 @@ struct DevPool {
 struct StateBuf {
     float4 *X = nullptr, *V = nullptr, *rot = nullptr, *cm = nullptr;
     int *orig = nullptr;
+    int *to_new = nullptr;  // the inverse of orig (picking finds the picked particle through it)
 };
 
 // What a substep leaves in the solver's buffers that its adjoint reads: the
@@ -91,11 +94,15 @@ struct Tape {
         bp_params prm;
         int iterations;
         int ckpt;  // checkpoint taken at the start of this substep, or -1
+        // picking (original id, or -1): the target position, and after the
+        // last substep of its update (last) the velocity the particle gets
+        int picked;
+        float3 ppos, pvel;
+        bool last;
     };
     std::vector<Sub> subs;
     std::vector<StateBuf> ckpts;
     int since = 0;
-    bool picked = false;
     DevPool pool;
     // per position in a segment: the substep's start state, its stage records,
     // the grid and order it ran with, and the CUDA graphs of its recording
@@ -174,9 +181,10 @@ bool alloc_state(Tape &t, const bp_solver *s, StateBuf &b)
     b.X = t.pool.get<float4>(s->n);
     b.V = t.pool.get<float4>(s->n);
     b.orig = t.pool.get<int>(s->n);
+    b.to_new = t.pool.get<int>(s->n);
     b.rot = t.pool.get<float4>(nb);
     b.cm = t.pool.get<float4>(nb);
-    return b.X && b.V && b.orig && b.rot && b.cm;
+    return b.X && b.V && b.orig && b.to_new && b.rot && b.cm;
 }
 
 void save_state(const bp_solver *s, const StateBuf &b)
@@ -185,6 +193,7 @@ void save_state(const bp_solver *s, const StateBuf &b)
     cudaMemcpyAsync(b.X, s->Xc, n * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream);
     cudaMemcpyAsync(b.V, s->Vc, n * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream);
     cudaMemcpyAsync(b.orig, s->orig_c, n * sizeof(int), cudaMemcpyDeviceToDevice, s->stream);
+    cudaMemcpyAsync(b.to_new, s->to_new, n * sizeof(int), cudaMemcpyDeviceToDevice, s->stream);
     if (s->rigid.num_bodies > 0) {
         const size_t nb = (size_t)s->rigid.num_bodies;
         cudaMemcpyAsync(b.rot, s->rigid.rot, nb * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream);
@@ -198,6 +207,7 @@ void load_state(bp_solver *s, const StateBuf &b)
     cudaMemcpyAsync(s->Xc, b.X, n * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream);
     cudaMemcpyAsync(s->Vc, b.V, n * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream);
     cudaMemcpyAsync(s->orig_c, b.orig, n * sizeof(int), cudaMemcpyDeviceToDevice, s->stream);
+    cudaMemcpyAsync(s->to_new, b.to_new, n * sizeof(int), cudaMemcpyDeviceToDevice, s->stream);
     if (s->rigid.num_bodies > 0) {
         const size_t nb = (size_t)s->rigid.num_bodies;
         cudaMemcpyAsync(s->rigid.rot, b.rot, nb * sizeof(float4), cudaMemcpyDeviceToDevice, s->stream);
@@ -236,14 +246,6 @@ void copy_ctx(bp_solver *s, const SubCtx &c, bool save)
 }
 
 bool stage_on(const bp_params &p, int bit) { return (p.stage_mask & bit) != 0; }
-
-// Which recorded configurations have an adjoint: every stage, but not picking
-// (its target is an input without a gradient).
-bp_status check_supported(const Tape &t)
-{
-    if (t.picked) return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: picking was used while recording");
-    return BP_OK;
-}
 
 bp_status ensure_grads(Tape &t, const bp_solver *s)
 {
@@ -314,6 +316,8 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
     // the post passes' and XSPH's density gradient, for the last fluid stage (the density they read)
     cudaMemsetAsync(t.gRho, 0, (size_t)s->n * sizeof(float), st);
     bool last_fluid = true;
+    // the velocity the update gave the picked particle after its last substep
+    if (u.last && u.picked >= 0) adj_unpick(st, u.picked, s->to_new, t.gV, nullptr);
     for (int r = (int)T.recs.size() - 1; r >= 0; --r) {
         const TapeRec &rec = T.recs[r];
         switch (rec.stage) {
@@ -332,6 +336,9 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
             cudaMemcpyAsync(t.gV, t.gVn, bytes, cudaMemcpyDeviceToDevice, st);
             break;
         }
+        case TS_PICK:  // the iteration's target position
+            adj_unpick(st, u.picked, s->to_new, t.gP, nullptr);
+            break;
         case TS_BENDING:
             adj_bending(st, s->bend, p.bending_stiffness, T.pool4[rec.slot], s->w, s->to_new, t.gP, t.gW);
             break;
@@ -382,16 +389,22 @@ void adjoint_substep(bp_solver *s, Tape &t, const Tape::Sub &u, const StateBuf &
                 t.gVn);
     cudaMemcpyAsync(t.gX, t.gXn, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(t.gV, t.gVn, (size_t)s->n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+    // the substep began by setting the picked particle's position and velocity
+    if (u.picked >= 0) adj_unpick_orig(st, s->n, u.picked, start.orig, t.gX, t.gV);
 }
 
 // The bytes a captured substep depends on: its constants, iteration count and
 // parameters (buffer pointers inside them are the solver's own, fixed).
 std::vector<char> sub_key(const Tape::Sub &u)
 {
-    std::vector<char> k(sizeof(SimConsts) + sizeof(int) + sizeof(bp_params));
-    memcpy(k.data(), &u.C, sizeof(SimConsts));
-    memcpy(k.data() + sizeof(SimConsts), &u.iterations, sizeof(int));
-    memcpy(k.data() + sizeof(SimConsts) + sizeof(int), &u.prm, sizeof(bp_params));
+    const float pick[8] = {(float)u.picked, u.ppos.x, u.ppos.y, u.ppos.z, u.pvel.x, u.pvel.y, u.pvel.z,
+                           u.last ? 1.f : 0.f};
+    std::vector<char> k(sizeof(SimConsts) + sizeof(int) + sizeof(bp_params) + sizeof(pick));
+    char *p = k.data();
+    memcpy(p, &u.C, sizeof(SimConsts));
+    memcpy(p += sizeof(SimConsts), &u.iterations, sizeof(int));
+    memcpy(p += sizeof(int), &u.prm, sizeof(bp_params));
+    memcpy(p += sizeof(bp_params), pick, sizeof(pick));
     return k;
 }
 
@@ -419,10 +432,9 @@ bp_status replay(bp_solver *s, cudaGraphExec_t &exec, std::vector<char> &key, co
 }  // namespace
 
 // Called by bp_solver_update before it enqueues an update while a tape is open.
-bp_status tape_record_update(bp_solver *s, int nsub, float dt, int iterations, bool picked)
+bp_status tape_record_update(bp_solver *s, int nsub, float dt, int iterations, int picked, float3 ppos, float3 pvel)
 {
     Tape &t = *s->tape;
-    if (picked) t.picked = true;
     int ck = -1;
     if (t.subs.empty() || t.since >= t.every) {
         StateBuf b;
@@ -433,7 +445,8 @@ bp_status tape_record_update(bp_solver *s, int nsub, float dt, int iterations, b
         t.since = 0;
     }
     const SimConsts C = make_consts(s, dt / (float)nsub);
-    for (int k = 0; k < nsub; ++k) t.subs.push_back(Tape::Sub{C, s->prm, iterations, k == 0 ? ck : -1});
+    for (int k = 0; k < nsub; ++k)
+        t.subs.push_back(Tape::Sub{C, s->prm, iterations, k == 0 ? ck : -1, picked, ppos, pvel, k == nsub - 1});
     t.since += nsub;
     return BP_OK;
 }
@@ -471,7 +484,6 @@ extern "C" bp_status bp_solver_backward(bp_solver *s, const float *grad_position
     if (!s->tape || s->tape->subs.empty()) return fail_with(BP_ERR_INVALID_ARGUMENT, "backward: nothing recorded");
     Tape &t = *s->tape;
     bp_status stt;
-    if ((stt = check_supported(t)) != BP_OK) return stt;
     if ((stt = ensure_grads(t, s)) != BP_OK) return stt;
     const cudaStream_t st = s->stream;
     const int n = s->n;
@@ -536,7 +548,9 @@ extern "C" bp_status bp_solver_backward(bp_solver *s, const float *grad_position
             auto body = [&] {
                 save_state(s, t.seg[q]);
                 t.tapes[q]->reset();
-                enqueue_substep(s, u.C, u.iterations, -1, make_float3(0.f, 0.f, 0.f), &L, t.tapes[q]);
+                enqueue_substep(s, u.C, u.iterations, u.picked, u.ppos, &L, t.tapes[q]);
+                if (u.last && u.picked >= 0)  // the end of its update: the picked particle's velocity
+                    launch_pick(s->stream, u.picked, s->to_new, s->Xc, u.ppos, 0, s->Vc, u.pvel, &L);
                 copy_ctx(s, t.ctxs[q], true);
             };
             if (sub_key(u) != t.key_warm[q]) {  // a new configuration runs once directly, growing

@@ -799,7 +799,10 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     bool committed = false;
     for (int it = 0; it < iterations; ++it) {
         const SimConsts &Cit = it == 0 ? Cpre : Cpost;  // stages before lambda
-        if (picking) launch_pick(st, picked, s->to_new, cur, ppos, 1, nullptr, make_float3(0.f, 0.f, 0.f), L);
+        if (picking) {
+            if (tape) tape->mark(TS_PICK);
+            launch_pick(st, picked, s->to_new, cur, ppos, 1, nullptr, make_float3(0.f, 0.f, 0.f), L);
+        }
         if (planes && !planes_done) {
             if (tape) tape->push(TS_PLANES, cur);
             launch_planes(st, Cit, s->Xs, cur, L);
@@ -953,7 +956,7 @@ extern "C" bp_status bp_solver_update(bp_solver *s, int32_t nsub, float dt, int3
     const float3 pp = ppos ? make_float3(ppos[0], ppos[1], ppos[2]) : make_float3(0.f, 0.f, 0.f);
     const float3 pv = pvel ? make_float3(pvel[0], pvel[1], pvel[2]) : make_float3(0.f, 0.f, 0.f);
     if (s->tape) {
-        const bp_status st = tape_record_update(s, nsub, dt, iterations, picked >= 0);
+        const bp_status st = tape_record_update(s, nsub, dt, iterations, picked, pp, pv);
         if (st != BP_OK) return st;
     }
     LaunchLog L;

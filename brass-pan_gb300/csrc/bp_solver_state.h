@@ -45,7 +45,8 @@ enum TapeStage : int {
     TS_COMMIT,
     TS_XSPH,
     TS_POST_AB,
-    TS_BENDING
+    TS_BENDING,
+    TS_PICK  // the picked particle set to the target (no snapshot)
 };
 struct TapeRec {
     int stage;
@@ -76,6 +77,7 @@ struct SubstepTape {
     int snap4(const float4 *src, size_t count = 0);  // count 0: one per particle (count <= particles)
     int snap1(const float *src);
     void push(int stage, const float4 *src, int aux = -1) { recs.push_back(TapeRec{stage, snap4(src), aux, -1}); }
+    void mark(int stage) { recs.push_back(TapeRec{stage, -1, -1, -1}); }
 };
 }  // namespace bp
 
@@ -201,7 +203,7 @@ namespace bp {
 // Substep constants of solver s for substep length sdt.
 SimConsts make_consts(const bp_solver *s, float sdt);
 // Records an update about to be enqueued while s->tape is open.
-bp_status tape_record_update(bp_solver *s, int nsub, float dt, int iterations, bool picked);
+bp_status tape_record_update(bp_solver *s, int nsub, float dt, int iterations, int picked, float3 ppos, float3 pvel);
 // Enqueues one substep on s->stream.  With a tape, the fused epilogues are
 // replaced by their separate kernels and every stage's input is recorded.
 void enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int picked, float3 ppos, LaunchLog *L,

@@ -330,8 +330,8 @@ bp_status bp_solver_autotune(bp_solver *s, int32_t num_substeps, float dt, int32
  * friction, distance constraints, dihedral bending, shape matching (the
  * extracted rotation differentiated at its fixed point), immovables, the
  * velocity update, the fluid density / lambda / position correction (both
- * modes), vorticity confinement, Akinci tension and XSPH.  Recordings that
- * used picking return BP_ERR_INVALID_ARGUMENT from bp_solver_backward. */
+ * modes), vorticity confinement, Akinci tension, XSPH and picking (the
+ * picked particle's gradient is 0 before each point where it is set). */
 typedef struct bp_gradients {
     float *positions;            /* [N][3] dL/dx at tape begin, original order, or NULL */
     float *velocities;           /* [N][3] dL/dv at tape begin, or NULL */

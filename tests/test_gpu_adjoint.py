@@ -250,18 +250,12 @@ def test_backward_restores_the_state(bp, gpu):
     b.close()
 
 
-def test_backward_rejects_what_has_no_adjoint(bp, gpu):
+def test_backward_without_a_recording_is_refused(bp, gpu):
     scene, _ = fluid_case(bp, n=4)
     t = bp.ParticleSolver(scene, bp.make_params(scene))
     with pytest.raises(bp.BrassPanError):
         t.backward(np.ones((scene.num_particles, 3), np.float32))  # nothing recorded
     t.close()
-    u = bp.ParticleSolver(scene, bp.make_params(scene))
-    u.tape_begin(1)
-    u.update(1, DT, 2, picked_original_id=3, picked_position=(0.3, 0.5, 0.3))
-    with pytest.raises(bp.BrassPanError):
-        u.backward(np.ones((scene.num_particles, 3), np.float32))  # picking
-    u.close()
 
 
 # ---- against central finite differences of the FP64 host oracle -------------
@@ -546,3 +540,47 @@ def test_textbook_fluid_gradients_match_fp64_finite_differences(bp, gpu, oracle)
     wx, wv = loss_weights(scene.num_particles, seed=27)
     g = gpu_gradients(bp, scene, params, frames, wx, wv)
     assert_fd64(fd64_state_pairs(oracle, scene, params, frames, wx, wv, g, seed=28))
+
+
+def test_picking_gradients_match_fp64_finite_differences(bp, gpu, oracle):
+    """Picking: the picked particle is set to its target at the start of every
+    substep and of every iteration, and given the picked velocity after the
+    update, so nothing before those reaches the loss through it; the other
+    particles' gradients flow through its constraints."""
+    import os
+
+    scene, params = cloth_case(bp)
+    n, frames, pick = scene.num_particles, 3, 44
+    target = (scene.positions[pick] + np.array([0.05, 0.1, -0.03])).astype(np.float32)
+    pvel = np.array([0.5, 0.0, 0.2], np.float32)
+    wx, wv = loss_weights(n, seed=29)
+    s = bp.ParticleSolver(scene, params)
+    s.tape_begin(2)
+    for _ in range(frames):
+        s.update(2, DT, 4, picked_original_id=pick, picked_position=target, picked_velocity=pvel)
+    g = s.backward(wx, wv)
+    s.close()
+    assert np.all(g["positions"][pick] == 0) and np.all(g["velocities"][pick] == 0)
+
+    def L(x0, v0):
+        o = oracle.OracleSolver(scene, params, threads=os.cpu_count() or 4, precision=64)
+        o.set_state(x0, v0)
+        for _ in range(frames):
+            o.update(2, DT, 4, picked=pick, picked_position=target, picked_velocity=pvel)
+        return float(np.sum(o.positions() * wx) + np.sum(o.velocities() * wv))
+
+    x0 = scene.positions.astype(np.float64)
+    v0 = np.zeros((n, 3)) if scene.velocities is None else scene.velocities.astype(np.float64)
+    rng = np.random.default_rng(30)
+    pairs = []
+    for key in ("velocities", "positions"):
+        d = rng.standard_normal((n, 3))
+        d /= np.linalg.norm(d)
+        if key == "velocities":
+            fd = central64(lambda **kw: L(**kw), lambda h: {"x0": x0, "v0": v0 + h * d},
+                           lambda h: {"x0": x0, "v0": v0 - h * d})
+        else:
+            fd = central64(lambda **kw: L(**kw), lambda h: {"x0": x0 + h * d, "v0": v0},
+                           lambda h: {"x0": x0 - h * d, "v0": v0})
+        pairs.append((key, fd, float(np.sum(g[key].astype(np.float64) * d))))
+    assert_fd64(pairs)
