@@ -62,10 +62,11 @@ struct SimConsts {
     int split;        // scan kernels test candidates in chunks before the pair terms
     int scan_block;   // unstaged scan launches: threads per CTA (bp_params::scan_block; 256 when 0)
     int scan_persist; // unstaged scan launches: at most one resident wave of CTAs, striding over the tiles
-    // Contact walks (nullptr: the 27 cells): the bits of a float bounding, per
-    // axis, every particle's displacement since its cell was hashed, written
-    // by k_contact_reach before the collision pass; the walks then visit only
-    // the cells a contact partner can be stored in.
+    // Contact walks (nullptr: the 27 cells): the bits of floats bounding, per
+    // axis, every particle's ([0]) and every solid's ([1]) displacement since
+    // its cell was hashed, written by k_contact_reach before the collision
+    // pass; the walks then visit only the cells a contact partner can be
+    // stored in.
     const unsigned *contact_reach;
     float4 plane_o[kMaxPlanes];
     float4 plane_n[kMaxPlanes];

@@ -254,8 +254,10 @@ void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int
 
 // ---- contact walks over the cells a partner can be stored in ----
 // A contact partner j of walker i lies within 2r of p_i on every axis, and
-// j's cell was hashed from a position at most d (C.contact_reach) from p_j
-// on every axis, so it is the cell of a point within 2r + d of p_i.  The cell
+// j's cell was hashed from a position at most d from p_j on every axis (d:
+// C.contact_reach[0] over all particles, or [1] over the solids, the only
+// partners of a fluid walker), so it is the cell of a point within 2r + d of
+// p_i.  The cell
 // function (float add and divide, truncation) is monotone, so on each axis
 // that cell lies between the cells of p_i -+ (2r + d + margin); the margin
 // covers the rounding of p_i -+ (...).  The range is clipped to the walker's
@@ -271,12 +273,13 @@ __device__ __forceinline__ bool contact_axis(float p, int c, float R, float cell
     return true;
 }
 
-// The range of walker i at p (its cell c); the whole 27 cells without a bound.
-__device__ __forceinline__ CellRange contact_range(const SimConsts &C, float3 p)
+// The range of walker i at p (its cell c; fluid: it meets solids only); the
+// whole 27 cells without a bound.
+__device__ __forceinline__ CellRange contact_range(const SimConsts &C, float3 p, bool fluid)
 {
     CellRange rg;
     if (!C.contact_reach) return rg;
-    const float R = __fadd_rn(2.0f * C.radius, __uint_as_float(__ldg(C.contact_reach)));
+    const float R = __fadd_rn(2.0f * C.radius, __uint_as_float(__ldg(C.contact_reach + (fluid ? 1 : 0))));
     const int3 c = cell_of(p, C);
     CellRange r;
     if (contact_axis(p.x, c.x, R, C.cell, r.lox, r.hix) && contact_axis(p.y, c.y, R, C.cell, r.loy, r.hiy) &&
@@ -285,33 +288,66 @@ __device__ __forceinline__ CellRange contact_range(const SimConsts &C, float3 p)
     return rg;
 }
 
-// The bound: per axis, the largest |p - p_hash| over all particles (positions
-// P against the positions their cells were hashed from), as float bits (the
-// maximum of non-negative floats is the maximum of their bits; a NaN's bits
-// exceed every finite value's).  *reach must be 0 before the launch.
+// The bounds: per axis, the largest |p - p_hash| over all particles (reach[0])
+// and over the solids (reach[1]), positions P against the positions their
+// cells were hashed from, as float bits (the maximum of non-negative floats is
+// the maximum of their bits; a NaN's bits exceed every finite value's).
+// reach[0..1] must be 0 before the launch.
 __global__ void __launch_bounds__(256) k_contact_reach(int n, const float4 *__restrict__ P,
                                                        const float4 *__restrict__ hashed, unsigned *__restrict__ reach)
 {
-    unsigned best = 0u;
+    unsigned best = 0u, best_solid = 0u;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 p = P[i], q = __ldg(hashed + i);
         const float d = fmaxf(fmaxf(fabsf(__fsub_rn(p.x, q.x)), fabsf(__fsub_rn(p.y, q.y))),
                               fabsf(__fsub_rn(p.z, q.z)));
         const bool finite = d <= 3.0e38f;
-        best = max(best, finite ? __float_as_uint(d) : 0x7f800000u);
+        const unsigned b = finite ? __float_as_uint(d) : 0x7f800000u;
+        best = max(best, b);
+        if (phase_of(p) > 0) best_solid = max(best_solid, b);
     }
     best = __reduce_max_sync(0xffffffffu, best);
+    best_solid = __reduce_max_sync(0xffffffffu, best_solid);
     if ((threadIdx.x & 31) == 0 && best) atomicMax(reach, best);
+    if ((threadIdx.x & 31) == 0 && best_solid) atomicMax(reach + 1, best_solid);
+}
+
+// The solids' bound only (reach[1]), over the compacted list; reach[0] = +inf
+// (the solid walkers take all 27 cells).  reach[1] must be 0 before the launch.
+__global__ void __launch_bounds__(256) k_contact_reach_solids(int n, const int *__restrict__ prefix,
+                                                              const int *__restrict__ list,
+                                                              const float4 *__restrict__ P,
+                                                              const float4 *__restrict__ hashed,
+                                                              unsigned *__restrict__ reach)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) reach[0] = 0x7f800000u;
+    const int total = __ldg(prefix + n);
+    unsigned best = 0u;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const int i = __ldg(list + t);
+        const float4 p = P[i], q = __ldg(hashed + i);
+        const float d = fmaxf(fmaxf(fabsf(__fsub_rn(p.x, q.x)), fabsf(__fsub_rn(p.y, q.y))),
+                              fabsf(__fsub_rn(p.z, q.z)));
+        best = max(best, d <= 3.0e38f ? __float_as_uint(d) : 0x7f800000u);
+    }
+    best = __reduce_max_sync(0xffffffffu, best);
+    if ((threadIdx.x & 31) == 0 && best) atomicMax(reach + 1, best);
 }
 
 void launch_contact_reach(cudaStream_t st, int n, const float4 *P, const float4 *hashed, unsigned *reach,
-                          LaunchLog *L)
+                          LaunchLog *L, int nsolid, const int *solid_prefix, const int *solid_list)
 {
-    cudaMemsetAsync(reach, 0, sizeof(unsigned), st);
+    cudaMemsetAsync(reach, 0, 2 * sizeof(unsigned), st);
     if (n <= 0) return;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (solid_list && 2LL * nsolid < n) {  // mostly fluid: bound the solids only
+        const int blocks = std::min((std::max(nsolid, 1) + 255) / 256, std::max(sms, 1) * 8);
+        k_contact_reach_solids<<<blocks, 256, 0, st>>>(n, solid_prefix, solid_list, P, hashed, reach);
+        L->done("k_contact_reach_solids");
+        return;
+    }
     const int blocks = std::min((n + 255) / 256, std::max(sms, 1) * 8);
     k_contact_reach<<<blocks, 256, 0, st>>>(n, P, hashed, reach);
     L->done("k_contact_reach");
@@ -409,7 +445,7 @@ __device__ __forceinline__ void collide_one(const SimConsts &C, int i, const flo
                     sf -= (w1 * tdx) * fminf(__fmul_rn(C.fd, __fsqrt_rn(__fdiv_rn(dxi2, tl2))), 1.0f);
             }
     };
-    const CellRange rg = contact_range(C, xip);
+    const CellRange rg = contact_range(C, xip, phi < 0 && solid_prefix);
     if (phi < 0 && solid_prefix) walk_solids(xip, solid_pos, v, C, solid_prefix, solid_list, test, body, rg);
     else walk_neighbors<Split, true>(i, xip, 0, P, v, C, S, g, test, body, rg);
     const float3 d = (count == 0) ? sd : sd + sf / (float)count;

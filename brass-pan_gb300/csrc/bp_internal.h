@@ -167,10 +167,14 @@ void launch_particle_collision(cudaStream_t st, const SimConsts &C, const float4
                                const float *w, const int *off, const int *tile_solid, const int *solid_prefix,
                                const int *solid_list, const int *solid_walk, int nsolid, bool solids_apart,
                                const unsigned long long *solid_near, float4 *solid_pos, float4 *Pout, LaunchLog *L);
-// *reach = the bits of the largest per-axis |P - hashed| over the n particles
-// (NaN or infinite: +inf).
+// reach[0] = the bits of the largest per-axis |P - hashed| over the n
+// particles, reach[1] over the solids (NaN or infinite: +inf).  With a solid
+// list and fewer than n / 2 solids (nsolid: the count at creation) only the
+// solids are bounded, over the list, and reach[0] = +inf: the solid walkers
+// then take all 27 cells.
 void launch_contact_reach(cudaStream_t st, int n, const float4 *P, const float4 *hashed, unsigned *reach,
-                          LaunchLog *L);
+                          LaunchLog *L, int nsolid = 0, const int *solid_prefix = nullptr,
+                          const int *solid_list = nullptr);
 // Bit masks over the D^3 table cells of one scene (cells == nullptr: not built):
 // cells marks the stored cells (keys) of the solids, near the cells whose 27
 // cells hold one.

@@ -397,7 +397,7 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         (st = s->alloc(&s->nbr_count, N)))
         return bail(st);
     // contact walks restricted to the cells a partner can be stored in
-    if (has_solid && ((st = s->alloc(&s->hash_pos, N)) || (st = s->alloc(&s->contact_reach, 1)) ||
+    if (has_solid && ((st = s->alloc(&s->hash_pos, N)) || (st = s->alloc(&s->contact_reach, 2)) ||
                       (st = s->alloc(&s->solid_walk, N)) || (st = s->alloc(&s->solid_oct, 16))))
         return bail(st);
     // fluid next to solids: the cell masks that let fluid far from every
@@ -744,6 +744,9 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     ra.pos0 = classes ? ca.pos0 : nullptr;
     // the contact walks' reach (BP_WALK_NO_CONTACT_CULLING: the 27 cells)
     const bool culling = pcoll && s->hash_pos && !(s->prm.walk_options & BP_WALK_NO_CONTACT_CULLING);
+    // the solids' own walks are culled (and their walkers grouped by octant)
+    // only where solids are at least half the particles (launch_contact_reach)
+    const bool solid_culling = culling && 2LL * s->num_solids >= s->n;
     ra.hash_pos = culling ? s->hash_pos : nullptr;
     launch_reorder(st, C, ra, L);
     if (classes) launch_class_order(st, s->n, s->sorted_keys, s->off, s->mass, ca, s->sort, L);
@@ -788,7 +791,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             sc.near = s->solid_near;
         }
         launch_solid_list(st, s->n, cur, s->solid_totals, s->solid_prefix, s->solid_list, sc, L, s->num_solids,
-                          C.cell, culling ? s->solid_walk : nullptr, s->solid_oct);
+                          C.cell, solid_culling ? s->solid_walk : nullptr, s->solid_oct);
     }
     if (wind) {
         if (tape) tape->push(TS_WIND, cur);
@@ -816,11 +819,12 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             refresh(cur);
             SimConsts Cc = Cit;
             if (culling) {
-                launch_contact_reach(st, s->n, cur, s->hash_pos, s->contact_reach, L);
+                launch_contact_reach(st, s->n, cur, s->hash_pos, s->contact_reach, L, s->num_solids,
+                                     s->solid_prefix, s->solid_list);
                 Cc.contact_reach = s->contact_reach;
             }
             launch_particle_collision(st, Cc, cur, s->Xs, s->w, s->off, s->tile_solid, s->solid_prefix,
-                                      s->solid_list, culling ? s->solid_walk : nullptr, s->num_solids, true,
+                                      s->solid_list, solid_culling ? s->solid_walk : nullptr, s->num_solids, true,
                                       s->solid_near, s->solid_pos, other, L);
             std::swap(cur, other);
         }
