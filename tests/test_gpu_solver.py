@@ -468,14 +468,17 @@ def contact_scene(bp, seed=0):
     return s
 
 
-@pytest.mark.parametrize("walk", [0, "NO_STAGING", "NO_SPLIT"])
+@pytest.mark.parametrize("walk", [0, "NO_STAGING", "NO_SPLIT", "VERLET"])
 def test_contact_culling_is_bit_identical(bp, gpu, walk):
-    """Contact walks over only the cells a partner can be stored in (the
-    default) against the full 27-cell walks (BP_WALK_NO_CONTACT_CULLING): the
-    same bits, on a scene with contacts between every pair of phases, the
-    mixed scene and grains alone."""
+    """Contact walks over only the cells a partner can be stored in against
+    the full 27-cell walks (BP_WALK_NO_CONTACT_CULLING): the same bits, on a
+    scene with contacts between every pair of phases (mostly fluid: only the
+    fluid walkers cull), the mixed scene and grains alone (all solids: the
+    solids cull too), also with Verlet lists (whose entries a culled walk may
+    test instead of its cells)."""
     abi = bp.abi
-    wo = 0 if walk == 0 else getattr(abi, "BP_WALK_" + walk)
+    skin = 0.3 if walk == "VERLET" else 0.0
+    wo = 0 if walk in (0, "VERLET") else getattr(abi, "BP_WALK_" + walk)
     grains = bp.scenes.Scene(name="grains")
     grains.particle_radius, grains.kernel_radius, grains.cell_size, grains.grid_dim = 0.05, 0.2, 0.2, 16
     bp.scenes.box_planes(grains, (0, 0, 0), (1.6, 3.0, 1.6))
@@ -483,7 +486,7 @@ def test_contact_culling_is_bit_identical(bp, gpu, walk):
     for scene in (contact_scene(bp, seed=5), small_mixed_scene(bp, seed=25), grains):
         outs = []
         for opt in (wo, wo | abi.BP_WALK_NO_CONTACT_CULLING):
-            g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=opt))
+            g = bp.ParticleSolver(scene, bp.make_params(scene, walk_options=opt, neighbor_skin=skin))
             for _ in range(6):
                 g.update(2, DT, 4)
             outs.append((g.positions(), g.velocities()))
