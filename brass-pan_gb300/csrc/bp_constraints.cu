@@ -77,7 +77,8 @@ __global__ void __launch_bounds__(kScanBlock) k_solid_count(int n, const float4 
 }
 
 // Exclusive scan of the block totals in one CTA (fixed order: deterministic).
-__global__ void __launch_bounds__(kScanBlock) k_solid_scan_totals(int nb, int *__restrict__ totals, int *__restrict__ prefix, int n)
+__global__ void __launch_bounds__(kScanBlock) k_solid_scan_totals(int nb, int *__restrict__ totals,
+                                                                   int *__restrict__ prefix, int n)
 {
     __shared__ int part[kScanBlock];
     const int per = (nb + kScanBlock - 1) / kScanBlock;

@@ -234,8 +234,8 @@ struct RigidArgs {
 };
 void launch_shape_matching(cudaStream_t st, const SimConsts &C, const RigidArgs &a, float4 *P,
                            const int *to_new, LaunchLog *L);
-void launch_immovable(cudaStream_t st, const SimConsts &C, int k, const int *ids, const int *to_new, const float4 *Xs, float4 *P,
-                      LaunchLog *L);
+void launch_immovable(cudaStream_t st, const SimConsts &C, int k, const int *ids, const int *to_new, const float4 *Xs,
+                      float4 *P, LaunchLog *L);
 void launch_pick(cudaStream_t st, int id_orig, const int *to_new, float4 *pos, float3 p, int set_pos, float4 *vel,
                  float3 v, LaunchLog *L);
 void launch_pack_infos(cudaStream_t st, int n, const float4 *X, const float4 *V, void *out);

@@ -347,7 +347,8 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         (st = s->alloc(&s->off, ncells + 1)) || (st = s->alloc(&s->mass, N)) || (st = s->alloc(&s->lam, N)) ||
         (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)) ||
         (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->vl, NM * kVerletCap)) ||
-        (st = s->alloc(&s->nl_cell, NM)) || (st = s->alloc(&s->nl_pos, NM)) || (st = s->alloc(&s->nl_outlier, (size_t)D * D * ((D + 63) / 64))) ||
+        (st = s->alloc(&s->nl_cell, NM)) || (st = s->alloc(&s->nl_pos, NM)) ||
+        (st = s->alloc(&s->nl_outlier, (size_t)D * D * ((D + 63) / 64))) ||
         (st = s->alloc(&s->vl_count, NM)) || (st = s->alloc(&s->nl_stats, 5)))
         return bail(st);
     {
