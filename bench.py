@@ -542,6 +542,18 @@ def dist_info():
     return rank, world, local
 
 
+def replica_throughput(torch, local_time, units_per_rank, world, device="cuda"):
+    """Whole-job throughput of `world` replicas (each rank advances its own
+    scene; no collective on the data path): every rank's units over the
+    slowest rank's time (the maximum over ranks).  Returns (value, max time);
+    times in seconds or milliseconds, value per the same unit."""
+    t = torch.tensor([float(local_time)], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    t_max = float(t.item())
+    return float(units_per_rank) * world / t_max, t_max
+
+
 def profile_summary(kernel: str, workload: str):
     """The committed ncu summary of `kernel` for this workload: the early-frame
     capture where there is one (the timed frames are early ones), else the
@@ -671,12 +683,9 @@ def run_ours(args):
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     if args.save_state and rank == 0:
         np.savez(args.save_state, x=solver.positions(), v=solver.velocities())
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    total_units = float(n) * SUBSTEPS * args.steps * world
-    value = total_units / (ms_max / 1e3)
+    units = float(n) * SUBSTEPS * args.steps  # per rank
+    value, ms_max = replica_throughput(torch, ms / 1e3, units, world)
+    ms_max *= 1e3
 
     # end to end through the C ABI with host buffers: the same frames again,
     # each one's state uploaded from pinned host memory and its result
@@ -694,10 +703,7 @@ def run_ours(args):
         bp.abi.check(lib, lib.bp_solver_copy_positions(solver.handle, xs, bp.abi.BP_ORDER_ORIGINAL))
         bp.abi.check(lib, lib.bp_solver_copy_velocities(solver.handle, vs, bp.abi.BP_ORDER_ORIGINAL))
     e2e_s = time.perf_counter() - t0
-    e2e_t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(e2e_t, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = total_units / float(e2e_t.item())
+    e2e_value, _ = replica_throughput(torch, e2e_s, units, world)
 
     roofline, stages, step_ms_total = kernel_roofline(torch, solver, n, args.workload, flush, value)
     walks = solver.walk_stats(SUBSTEPS, DT, ITERATIONS)
