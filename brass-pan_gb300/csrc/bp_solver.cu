@@ -118,6 +118,27 @@ static bp_status check_params(const bp_params *p)
 // boundary by less than 0.01 for |p| < 4e4 (checked by k_class_refresh), and
 // 1e-3 h keeps the distance test's own rounding clear.  Taped updates walk
 // whole cells (the adjoint re-runs do not record the classes).
+// Whether the scene's planes hold it inside one period of the table on every
+// axis: an axis-aligned box at most D - 2 cells wide, so that no 27-cell walk
+// of a particle inside it meets two real cells in one table cell.  Such a
+// scene gets no alias classes (their walks would skip nothing; a particle
+// that leaves the box is still walked exactly, through whole table cells).
+static bool planes_confine(const bp_solver *s, int D, float cell)
+{
+    for (int a = 0; a < 3; ++a) {
+        float lo = -INFINITY, hi = INFINITY;
+        for (int k = 0; k < s->nplanes; ++k) {
+            const float *pl = s->planes[k];  // origin xyz, normal xyz
+            const float n = pl[3 + a];
+            if (!(fabsf(n) == 1.f && pl[3 + (a + 1) % 3] == 0.f && pl[3 + (a + 2) % 3] == 0.f)) continue;
+            if (n > 0.f) lo = fmaxf(lo, pl[a]);
+            else hi = fminf(hi, pl[a]);
+        }
+        if (!(hi - lo <= (float)(D - 2) * cell)) return false;
+    }
+    return true;
+}
+
 static float class_reach(const bp_solver *s)
 {
     const bp_params &p = s->prm;
@@ -356,7 +377,7 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         if ((st = s->alloc(&scratch, sort_scratch_bytes((int)N, s->sort_dim)))) return bail(st);
         sort_scratch_carve(scratch, (int)N, s->sort_dim, &s->sort);
     }
-    if (ncells <= kClassMaxCells) {
+    if (ncells <= kClassMaxCells && (batch || !planes_confine(s, D, prm->cell_size))) {
         ClassArrays &a = s->cls;
         if ((st = s->alloc(&a.cls, N)) || (st = s->alloc(&a.pos0, N)) || (st = s->alloc(&a.keys, N)) ||
             (st = s->alloc(&a.perm, N)) || (st = s->alloc(&a.inv, N)) || (st = s->alloc(&a.off, 8 * ncells + 1)) ||
