@@ -176,37 +176,16 @@ __device__ __forceinline__ int octant_of(float3 p, float cell)
     return ox | oy | oz;
 }
 
-// oct[0..7] += the listed solids of each octant (oct zeroed before).
-__global__ void __launch_bounds__(256) k_solid_octant_count(int n, const int *__restrict__ prefix,
-                                                            const int *__restrict__ list, const float4 *__restrict__ P,
-                                                            float cell, int *__restrict__ oct)
+// walk = the listed solids, each tile of 256 consecutive entries (cells in
+// sorted order) regrouped by octant: the warps of a group take the same cells
+// in their contact walks, and a tile's walks stay within its neighbourhood.
+// The order within a group is any: every solid's result is its own.
+__global__ void __launch_bounds__(256) k_solid_octant_tiles(int n, const int *__restrict__ prefix,
+                                                            const int *__restrict__ list,
+                                                            const float4 *__restrict__ P, float cell,
+                                                            int *__restrict__ walk)
 {
-    __shared__ int h[8];
-    if (threadIdx.x < 8) h[threadIdx.x] = 0;
-    __syncthreads();
-    const int total = __ldg(prefix + n);
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
-        atomicAdd(&h[octant_of(f3(P[__ldg(list + t)]), cell)], 1);
-    __syncthreads();
-    if (threadIdx.x < 8 && h[threadIdx.x]) atomicAdd(oct + threadIdx.x, h[threadIdx.x]);
-}
-
-// walk = the listed solids grouped by octant (octant o from the sum of the
-// counts before it on; oct[8 + o]: the cursor of octant o, zeroed before).
-// The order within an octant is any: every solid's result is its own.
-__global__ void __launch_bounds__(256) k_solid_octant_scatter(int n, const int *__restrict__ prefix,
-                                                              const int *__restrict__ list,
-                                                              const float4 *__restrict__ P, float cell,
-                                                              int *__restrict__ oct, int *__restrict__ walk)
-{
-    __shared__ int first[8], h[8], base[8];
-    if (threadIdx.x == 0) {
-        int run = 0;
-        for (int o = 0; o < 8; ++o) {
-            first[o] = run;
-            run += oct[o];
-        }
-    }
+    __shared__ int h[8], base[8];
     const int total = __ldg(prefix + n);
     for (int t0 = blockIdx.x * blockDim.x; t0 < total; t0 += gridDim.x * blockDim.x) {  // uniform per CTA
         if (threadIdx.x < 8) h[threadIdx.x] = 0;
@@ -219,15 +198,21 @@ __global__ void __launch_bounds__(256) k_solid_octant_scatter(int n, const int *
             rank = atomicAdd(&h[o], 1);
         }
         __syncthreads();
-        if (threadIdx.x < 8) base[threadIdx.x] = h[threadIdx.x] ? atomicAdd(oct + 8 + threadIdx.x, h[threadIdx.x]) : 0;
+        if (threadIdx.x == 0) {
+            int run = 0;
+            for (int q = 0; q < 8; ++q) {
+                base[q] = run;
+                run += h[q];
+            }
+        }
         __syncthreads();
-        if (o >= 0) walk[first[o] + base[o] + rank] = i;
+        if (o >= 0) walk[t0 + base[o] + rank] = i;
         __syncthreads();
     }
 }
 
 void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int *prefix, int *list,
-                       const SolidCells &sc, LaunchLog *L, int nsolid, float cell, int *walk, int *oct)
+                       const SolidCells &sc, LaunchLog *L, int nsolid, float cell, int *walk)
 {
     if (n <= 0) return;
     const int nb = (n + kScanBlock - 1) / kScanBlock;
@@ -243,13 +228,9 @@ void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int
         k_solid_dilate<<<(nwords + 255) / 256, 256, 0, st>>>(sc.D, nwords, sc.cells, sc.near);
         L->done("k_solid_dilate");
     }
-    if (walk && oct && nsolid > 0) {  // launches sized by the count at creation, loops to the device total
-        const int blocks = (nsolid + 255) / 256;
-        cudaMemsetAsync(oct, 0, 16 * sizeof(int), st);
-        k_solid_octant_count<<<blocks, 256, 0, st>>>(n, prefix, list, P, cell, oct);
-        L->done("k_solid_octant_count");
-        k_solid_octant_scatter<<<blocks, 256, 0, st>>>(n, prefix, list, P, cell, oct, walk);
-        L->done("k_solid_octant_scatter");
+    if (walk && nsolid > 0) {  // sized by the count at creation, loops to the device total
+        k_solid_octant_tiles<<<(nsolid + 255) / 256, 256, 0, st>>>(n, prefix, list, P, cell, walk);
+        L->done("k_solid_octant_tiles");
     }
 }
 

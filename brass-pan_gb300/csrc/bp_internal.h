@@ -185,12 +185,11 @@ struct SolidCells {
 };
 // solid_prefix[i] (i <= n): solids among sorted [0, i); solid_list: their sorted indices in order.
 // totals: (n + 1023) / 1024 ints of scratch.
-// With walk (and oct, 16 ints of scratch): the listed solids again, grouped
-// by the half of its cell each one's position lies in on every axis, for the
-// solids' contact launch (the warps of a group walk the same cells).
+// With walk: the listed solids again, each tile of 256 entries grouped by the
+// half of its cell each one's position lies in on every axis, for the solids'
+// contact launch (the warps of a group walk the same cells).
 void launch_solid_list(cudaStream_t st, int n, const float4 *P, int *totals, int *solid_prefix, int *solid_list,
-                       const SolidCells &sc, LaunchLog *L, int nsolid = 0, float cell = 0.f, int *walk = nullptr,
-                       int *oct = nullptr);
+                       const SolidCells &sc, LaunchLog *L, int nsolid = 0, float cell = 0.f, int *walk = nullptr);
 struct DistanceArgs {
     int num_edges;
     const int2 *pairs;       // original ids

@@ -420,7 +420,7 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         return bail(st);
     // contact walks restricted to the cells a partner can be stored in
     if (has_solid && ((st = s->alloc(&s->hash_pos, N)) || (st = s->alloc(&s->contact_reach, 2)) ||
-                      (st = s->alloc(&s->solid_walk, N)) || (st = s->alloc(&s->solid_oct, 16))))
+                      (st = s->alloc(&s->solid_walk, N))))
         return bail(st);
     // fluid next to solids: the cell masks that let fluid far from every
     // solid skip its walk over the solids (one scene's table)
@@ -813,7 +813,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             sc.near = s->solid_near;
         }
         launch_solid_list(st, s->n, cur, s->solid_totals, s->solid_prefix, s->solid_list, sc, L, s->num_solids,
-                          C.cell, solid_culling ? s->solid_walk : nullptr, s->solid_oct);
+                          C.cell, solid_culling ? s->solid_walk : nullptr);
     }
     if (wind) {
         if (tape) tape->push(TS_WIND, cur);

@@ -128,11 +128,11 @@ struct bp_solver {
     int *solid_prefix = nullptr, *solid_list = nullptr, *solid_totals = nullptr;  // compacted solids
     unsigned long long *solid_cells = nullptr, *solid_near = nullptr;  // SolidCells masks (one scene with fluid)
     float4 *solid_pos = nullptr;  // positions of the compacted solids (launch_particle_collision)
-    // contact walks: hash-time positions, the reach bound, the solids' walk
-    // order and its octant counts (allocated with solids at creation)
+    // contact walks: hash-time positions, the reach bounds and the solids'
+    // walk order (allocated with solids at creation)
     float4 *hash_pos = nullptr;
     unsigned *contact_reach = nullptr;
-    int *solid_walk = nullptr, *solid_oct = nullptr;
+    int *solid_walk = nullptr;
     int *nbr = nullptr, *nbr_count = nullptr;  // post-pass neighbour lists [kPostListCap][N], counts
     SortScratch sort{};
     // alias classes (SimConsts::cls_perm); cls.perm == nullptr: not allocated
