@@ -634,6 +634,8 @@ def run_ours(args):
             p.walk_options |= bp.abi.BP_WALK_NO_LISTS
         if args.contact_culling:
             p.walk_options &= ~bp.abi.BP_WALK_NO_CONTACT_CULLING
+        if args.no_planes:
+            p.walk_options |= bp.abi.BP_WALK_NO_PLANES
         return p
 
     if args.workload == "batch":
@@ -902,6 +904,8 @@ def main():
     ap.add_argument("--no-stage", action="store_true", help="read neighbours from global memory only")
     ap.add_argument("--no-split", action="store_true", help="evaluate pair terms as candidates are tested")
     ap.add_argument("--no-lists", action="store_true", help="post passes B and C walk their cells")
+    ap.add_argument("--no-planes", action="store_true",
+                    help="recording walks read the position records instead of the walk planes")
     ap.add_argument("--no-autotune", action="store_true", help="keep the walk options given instead of timing them")
     ap.add_argument("--contact-culling", action="store_true",
                     help="contact walks over only the cells a partner can be stored in (with --no-autotune)")

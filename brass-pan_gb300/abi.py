@@ -50,6 +50,7 @@ BP_WALK_NO_LISTS = 0x4
 BP_WALK_NO_ALIAS_CLASSES = 0x8
 BP_WALK_NO_FUSION = 0x10
 BP_WALK_NO_CONTACT_CULLING = 0x20
+BP_WALK_NO_PLANES = 0x40
 
 (BP_FIELD_POSITIONS, BP_FIELD_NEW_POSITIONS, BP_FIELD_VELOCITIES, BP_FIELD_MAP_TO_ORIGINAL,
  BP_FIELD_MAP_TO_NEW, BP_FIELD_LAMBDAS, BP_FIELD_DENSITIES, BP_FIELD_SORTED_CELL_IDS,

@@ -141,13 +141,47 @@ struct SimConsts {
     float *cls_rho;
     float4 *cls_vel, *cls_om, *cls_nm, *cls_vb;
     int cls_post;
+    // Walk planes (nullptr: off): x, y, z and the phase bits of every
+    // particle in four planes of walk_stride floats (a multiple of 4, at
+    // least n + kPlanePad), written just before the lambda pass and post
+    // pass A, whose recording walks test four candidates per three 16-byte
+    // loads with paired fp32 arithmetic and append each chunk's hits to the
+    // list a record at a time.  They hold class order while the classes are
+    // on and sorted order where the classes are closed or absent (see
+    // walk_planes_order).
+    const float *walk_xyz;
+    int walk_stride;
 };
 
 // The walks use the alias classes for the rest of the substep (uniform
 // over a launch: the flag is written by k_class_refresh before it).
+// *cls_moved: 0 classes on, 1 gate closed, 2 a particle left the reach.
 __device__ __forceinline__ bool classes_on(const SimConsts &C)
 {
     return C.cls_perm && __ldg(C.cls_moved) == 0;
+}
+
+// Quads of candidates a recording walk over the walk planes tests per loop
+// trip (loads in flight: three per quad).
+#ifndef BP_PLANE_QUADS
+#define BP_PLANE_QUADS 1
+#endif
+constexpr int kPlaneQuads = BP_PLANE_QUADS;
+// Floats past n a walk-plane read may reach: the last trip of a chunk reads
+// up to kPlaneQuads quads from an aligned start below the run's end.
+constexpr int kPlanePad = 4 * kPlaneQuads + 4;
+
+// Order of the walk planes: 2 class order (the classes are on), 1 sorted
+// order (no classes, or their gate is closed: k_class_refresh then writes
+// the planes in sorted order), 0 none usable (no planes, or the classes
+// closed because a particle left the reach after the planes were written in
+// class order).
+__device__ __forceinline__ int walk_planes_order(const SimConsts &C)
+{
+    if (!C.walk_xyz) return 0;
+    if (!C.cls_perm) return 1;
+    const int m = __ldg(C.cls_moved);
+    return m == 0 ? 2 : (m == 1 ? 1 : 0);
 }
 
 // Class (0..7) of real cell c on a table of D cells per axis (D a power of two).

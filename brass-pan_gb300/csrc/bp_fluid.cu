@@ -26,6 +26,12 @@ constexpr int kScanThreads = kWalkThreads;  // scan kernels stage their neighbou
 #ifndef BP_DELTAP_MIN_BLOCKS
 #define BP_DELTAP_MIN_BLOCKS 5
 #endif
+// The lambda pass's recording walk over the walk planes appends each chunk's
+// hits with ListWriter::push_bits (whole records of four at a time); 0: one
+// push per hit.
+#ifndef BP_PLANE_PUSH_BITS
+#define BP_PLANE_PUSH_BITS 1
+#endif
 #ifndef BP_POSTBC_MIN_BLOCKS
 #define BP_POSTBC_MIN_BLOCKS BP_SCAN_MIN_BLOCKS
 #endif
@@ -101,7 +107,26 @@ __device__ __forceinline__ void k_lambda_tile(
             list.push(j);
         };
         auto test = [&](int, float4 pj) { return len2(pi - f3(pj)) <= r2; };
-        if (slots) {  // the class walk walk_neighbors would take (no staging, no Verlet list), counted alike
+        // the walk planes hold the order this walk reads (class positions with
+        // slots, sorted indices otherwise): the same hits in the same order
+        const int planes = (Split && !Stage && !C.vl) ? walk_planes_order(C) : 0;
+        if (planes == (slots ? 2 : 1)) {
+            const int me = slots ? t : i;  // the particle's own entry
+            record_walk_planes(planes, pi, r2, v, C, [&](int c0, unsigned bits) {
+#if BP_PLANE_PUSH_BITS
+                const unsigned d = (unsigned)(me - c0);
+                if (d < 32u && ((bits >> d) & 1u)) self = list.cnt + __popc(bits & ((1u << d) - 1u));
+                list.push_bits(c0, bits);
+#else
+                while (bits) {
+                    const int q = c0 + __ffs(bits) - 1;
+                    bits &= bits - 1u;
+                    if (q == me) self = list.cnt;
+                    list.push(q);
+                }
+#endif
+            });
+        } else if (slots) {  // the class walk walk_neighbors would take (no staging, no Verlet list), counted alike
             if (C.nl_stats) {
                 atomicAdd(C.nl_stats + 1, 1u);
                 atomicAdd(C.nl_stats + 4, 1u);
@@ -420,7 +445,28 @@ __device__ __forceinline__ void k_post_a_tile(
     int cnt = -1;
     if (C.nbr) {
         ListWriter list(C.nbr, C.nbr_cap, C.n, t);
-        if (slots) {  // the class walk walk_neighbors would take, recording class positions
+        // the walk planes hold the order this walk reads (class positions with
+        // slots, sorted indices otherwise): the same hits in the same order,
+        // each chunk's kept where the phase plane matches and not the own entry
+        const int planes = (Split && !Stage && !C.vl) ? walk_planes_order(C) : 0;
+        if (planes == (slots ? 2 : 1)) {
+            const int *__restrict__ W = reinterpret_cast<const int *>(C.walk_xyz) + 3 * (size_t)C.walk_stride;
+            const int me = slots ? t : i;
+            record_walk_planes(planes, pi, C.h2, v, C, [&](int c0, unsigned bits) {
+                const unsigned d = (unsigned)(me - c0);
+                if (d < 32u) bits &= ~(1u << d);
+                unsigned same = 0u;
+                for (unsigned quads = bits; quads;) {  // the phases of the quads holding hits
+                    const int q4 = (__ffs(quads) - 1) & ~3;
+                    const int4 w = __ldg(reinterpret_cast<const int4 *>(W + c0 + q4));
+                    same |= ((w.x == phi ? 1u : 0u) | (w.y == phi ? 2u : 0u) | (w.z == phi ? 4u : 0u) |
+                             (w.w == phi ? 8u : 0u))
+                            << q4;
+                    quads &= ~(0xfu << q4);
+                }
+                list.push_bits(c0, bits & same);
+            });
+        } else if (slots) {  // the class walk walk_neighbors would take, recording class positions
             if (C.nl_stats) {
                 atomicAdd(C.nl_stats + 1, 1u);
                 atomicAdd(C.nl_stats + 4, 1u);

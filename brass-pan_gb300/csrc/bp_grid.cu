@@ -517,14 +517,31 @@ void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const in
     launch_cell_offsets(st, n, 8 * a.T, a.keys, a.off, L, gate);
 }
 
+// Writes particle p's x, y, z and phase bits to slot q of the walk planes
+// (SimConsts::walk_xyz).
+__device__ __forceinline__ void put_planes(float *planes, int stride, int q, float4 p)
+{
+    planes[q] = p.x;
+    planes[stride + q] = p.y;
+    planes[2 * stride + q] = p.z;
+    planes[3 * stride + q] = p.w;
+}
+
 // Walks use the classes while at least 1/32 of the particles sit in a cell
 // holding another class (below that the extra indirection costs more than
 // the skipped candidates save) and no particle has left the reach.
+// *moved: 1 where the gate is closed, 2 where a particle left the reach.
+// planes != nullptr: also writes the walk planes, in sorted order where the
+// gate is closed and in class order where it is open.
 __global__ void __launch_bounds__(256) k_class_refresh(int n, const float4 *__restrict__ P,
-                                                       const float4 *__restrict__ V, ClassArrays a, Gate gate)
+                                                       const float4 *__restrict__ V, ClassArrays a, Gate gate,
+                                                       float *__restrict__ planes, int stride)
 {
     if (gate_closed(gate)) {  // uniform: written by an earlier kernel
         if (blockIdx.x == 0 && threadIdx.x == 0) *a.moved = 1;
+        if (planes)
+            for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+                put_planes(planes, stride, i, P[i]);
         return;
     }
     bool far = false;
@@ -532,6 +549,7 @@ __global__ void __launch_bounds__(256) k_class_refresh(int n, const float4 *__re
         const int j = __ldg(a.perm + q);
         const float4 p = P[j];
         a.pos[q] = p;
+        if (planes) put_planes(planes, stride, q, p);
         if (V) a.vel[q] = V[j];
         const float4 p0 = __ldg(a.pos0 + j);
         const float dx = p.x - p0.x, dy = p.y - p0.y, dz = p.z - p0.z;
@@ -540,20 +558,42 @@ __global__ void __launch_bounds__(256) k_class_refresh(int n, const float4 *__re
         const bool inside = fabsf(p.x) < 4.0e4f && fabsf(p.y) < 4.0e4f && fabsf(p.z) < 4.0e4f;
         far |= !(dx * dx + dy * dy + dz * dz <= a.reach2) || !inside;
     }
-    if (far) *a.moved = 1;
+    if (far) *a.moved = 2;
 }
 
-void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L,
-                          const float4 *V)
+// A grid-stride loop over one resident wave (8 CTAs of 256 per SM).
+static int wave_blocks(int n)
 {
-    if (n <= 0) return;
-    // a grid-stride loop over one resident wave (8 CTAs of 256 per SM): the
-    // common case is the gate's early exit
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int blocks = std::min((n + 255) / 256, std::max(sms, 1) * 8);
-    k_class_refresh<<<blocks, 256, 0, st>>>(n, P, V, a, class_gate(n, a));
+    return std::min((n + 255) / 256, std::max(sms, 1) * 8);
+}
+
+void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L,
+                          const float4 *V, float *planes, int stride)
+{
+    if (n <= 0) return;
+    // the common case without planes is the gate's early exit (one wave);
+    // with planes, a thread per particle (measured: a wave striding over the
+    // particles took 25 us per launch on 1.1M particles)
+    const int blocks = planes ? (n + 255) / 256 : wave_blocks(n);
+    k_class_refresh<<<blocks, 256, 0, st>>>(n, P, V, a, class_gate(n, a), planes, stride);
+    L->done(__func__);
+}
+
+// The walk planes in sorted order (scenes without alias classes).
+__global__ void __launch_bounds__(256) k_walk_planes(int n, const float4 *__restrict__ P, float *__restrict__ planes,
+                                                     int stride)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        put_planes(planes, stride, i, P[i]);
+}
+
+void launch_walk_planes(cudaStream_t st, int n, const float4 *P, float *planes, int stride, LaunchLog *L)
+{
+    if (n <= 0) return;
+    k_walk_planes<<<(n + 255) / 256, 256, 0, st>>>(n, P, planes, stride);
     L->done(__func__);
 }
 

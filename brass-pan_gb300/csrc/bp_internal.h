@@ -121,8 +121,12 @@ void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const in
                         const ClassArrays &a, const SortScratch &s, LaunchLog *L);
 // Gathers P into class order and flags particles beyond the reach.
 // V != nullptr: also gathers V into a.vel (before the post passes).
+// planes != nullptr: also writes the walk planes (SimConsts::walk_xyz), in
+// class order where the classes are open and in sorted order where not.
 void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassArrays &a, LaunchLog *L,
-                          const float4 *V = nullptr);
+                          const float4 *V = nullptr, float *planes = nullptr, int stride = 0);
+// The walk planes in sorted order (scenes without alias classes).
+void launch_walk_planes(cudaStream_t st, int n, const float4 *P, float *planes, int stride, LaunchLog *L);
 
 // ---- fluid kernels ----
 void launch_lambda(cudaStream_t st, const SimConsts &C, const float4 *P, const float *mass, const int *off,

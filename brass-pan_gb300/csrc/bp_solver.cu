@@ -416,8 +416,11 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         (st = s->alloc(&s->solid_pos, N + 1)) ||  // phases may change after creation: room for every particle
         (st = s->alloc(&s->solid_list, N)) || (st = s->alloc(&s->solid_totals, (N + 1023) / 1024)) ||
         (st = s->alloc(&s->nbr, N * kPostListCap)) ||
+        (st = s->alloc(&s->walk_xyz, 4 * (((N + 3) & ~(size_t)3) + kPlanePad))) ||
         (st = s->alloc(&s->nbr_count, N)))
         return bail(st);
+    s->walk_stride = (int)(((N + 3) & ~(size_t)3) + kPlanePad);
+    BP_CUDA_BAIL(cudaMemset(s->walk_xyz, 0, 4 * (size_t)s->walk_stride * sizeof(float)));
     // contact walks restricted to the cells a partner can be stored in
     if (has_solid && ((st = s->alloc(&s->hash_pos, N)) || (st = s->alloc(&s->contact_reach, 2)) ||
                       (st = s->alloc(&s->solid_walk, N))))
@@ -794,11 +797,24 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     // With Verlet lists the later lambda passes read them and record the exact
     // lists as well; the pass that builds them does not, so the position pass
     // right after it reads the Verlet lists instead.
+    // The recording walks of the lambda pass and post pass A read their
+    // candidates from the walk planes, written just before them
+    // (BP_WALK_NO_PLANES: from the position records).
+    const bool walk_planes = lists && !verlet && s->walk_xyz && C.split && !C.stage &&
+                        !(s->prm.walk_options & BP_WALK_NO_PLANES);
+    auto refresh_planes = [&](const float4 *P) {
+        if (classes) launch_class_refresh(st, s->n, P, ca, L, nullptr, s->walk_xyz, s->walk_stride);
+        else launch_walk_planes(st, s->n, P, s->walk_xyz, s->walk_stride, L);
+    };
     SimConsts Cf = Cpost;
     if (lists) {
         Cf.nbr = s->nbr;
         Cf.nbr_count = s->nbr_count;
         Cf.nbr_cap = kPostListCap;
+    }
+    if (walk_planes) {
+        Cf.walk_xyz = s->walk_xyz;
+        Cf.walk_stride = s->walk_stride;
     }
     SimConsts Cbuild = verlet ? Cpost : Cf;
     Cbuild.vl_build = verlet ? 1 : 0;
@@ -851,7 +867,9 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             std::swap(cur, other);
         }
         if (fluid) {
-            refresh(cur);  // lambda and delta-p read the same positions
+            // lambda and delta-p read the same positions
+            if (walk_planes) refresh_planes(cur);
+            else refresh(cur);
             if (verlet && it == 0)
                 cudaMemsetAsync(s->nl_outlier, 0, (size_t)C.D * C.D * C.nl_zwords * sizeof(unsigned long long), st);
             launch_lambda(st, it == 0 ? Cbuild : Cf, cur, s->mass, s->off, s->lam, s->rho, L);
@@ -921,8 +939,12 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
     // its densities in class order (SimConsts::cls_post); the velocities are
     // gathered into class order with the positions.
     const bool post_slots = classes && lists && post_ab && fluid && iterations > 0 && !verlet;
+    const bool post_planes = walk_planes && post_ab;
     if ((post_ab || C.use_xsph) && classes)  // the post passes read the same positions
-        launch_class_refresh(st, s->n, cur, ca, L, post_slots ? s->Vc : nullptr);
+        launch_class_refresh(st, s->n, cur, ca, L, post_slots ? s->Vc : nullptr, post_planes ? s->walk_xyz : nullptr,
+                             s->walk_stride);
+    else if (post_planes)
+        launch_walk_planes(st, s->n, cur, s->walk_xyz, s->walk_stride, L);
     if (post_ab) {
         // pass A records each fluid particle's neighbours for passes B and C
         SimConsts Cl = Cpost;
@@ -930,6 +952,10 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
             Cl.nbr = s->nbr;
             Cl.nbr_count = s->nbr_count;
             Cl.nbr_cap = kPostListCap;
+        }
+        if (post_planes) {
+            Cl.walk_xyz = s->walk_xyz;
+            Cl.walk_stride = s->walk_stride;
         }
         Cl.cls_post = post_slots ? 1 : 0;
         launch_post_a(st, Cl, cur, s->Vc, s->rho, s->off, s->Om, s->Nm, L);

@@ -134,6 +134,8 @@ struct bp_solver {
     unsigned *contact_reach = nullptr;
     int *solid_walk = nullptr;
     int *nbr = nullptr, *nbr_count = nullptr;  // post-pass neighbour lists [kPostListCap][N], counts
+    float *walk_xyz = nullptr;  // walk planes (SimConsts::walk_xyz): 4 planes of walk_stride floats
+    int walk_stride = 0;
     SortScratch sort{};
     // alias classes (SimConsts::cls_perm); cls.perm == nullptr: not allocated
     // (key spaces above kClassMaxCells cells)

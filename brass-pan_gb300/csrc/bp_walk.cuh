@@ -311,6 +311,36 @@ struct ListWriter {
         if (q == 3 && cnt < cap) rec[(size_t)(cnt >> 2) * stride] = buf;
         ++cnt;
     }
+    // Appends c0 + t for every set bit t of bits, in ascending t: singly up
+    // to a record boundary, then whole records of four (no per-entry select),
+    // then the rest singly.  The entries are those push() gives.
+    __device__ __forceinline__ void push_bits(int c0, unsigned bits)
+    {
+#pragma unroll 1
+        while (bits && (cnt & 3)) {
+            push(c0 + __ffs(bits) - 1);
+            bits &= bits - 1u;
+        }
+#pragma unroll 1
+        while (__popc(bits) >= 4) {
+            int4 r;
+            r.x = c0 + __ffs(bits) - 1;
+            bits &= bits - 1u;
+            r.y = c0 + __ffs(bits) - 1;
+            bits &= bits - 1u;
+            r.z = c0 + __ffs(bits) - 1;
+            bits &= bits - 1u;
+            r.w = c0 + __ffs(bits) - 1;
+            bits &= bits - 1u;
+            if (cnt < cap) rec[(size_t)(cnt >> 2) * stride] = r;
+            cnt += 4;
+        }
+#pragma unroll 1
+        while (bits) {
+            push(c0 + __ffs(bits) - 1);
+            bits &= bits - 1u;
+        }
+    }
     // Writes the last partial record; returns the count to store (-1: overflow).
     __device__ __forceinline__ int finish()
     {
@@ -499,6 +529,119 @@ __device__ __forceinline__ void walk_neighbors(int i, float3 pi, int lo, const f
             const int sidx = staged ? staged_index(*S, g, col, b, e) : -1;
             const float4 *src = sidx >= 0 ? S->pos + sidx : P + b;
             walk_run<Split>(max(b, lo), b, e, src, test, body);
+        }
+    }
+}
+
+// ---- recording walks over the walk planes (SimConsts::walk_xyz) ----
+
+// Candidates [b, e) of one run, indices into the planes X, Y, Z: the q with
+// |pi - p_q|^2 <= r2, in ascending q, as chunk(c0, bits) calls (q = c0 + t
+// for each set bit t, chunks in ascending c0).  The run is read in quads
+// aligned to 16 bytes, 32 candidates to a chunk mask (the candidates of a
+// quad outside [b, e) are tested and dropped; the planes are padded by
+// kPlanePad floats), and each paired fp32 operation serves two candidates.
+// The squared distance has the bits len2(pi - pj) gives: pj + (-pi) is
+// exactly -(pi - pj), its square the same, and each lane of a paired
+// operation rounds as the scalar operation does.
+template <class H>
+__device__ __forceinline__ void record_run_planes(int b, int e, const float *__restrict__ X,
+                                                  const float *__restrict__ Y, const float *__restrict__ Z,
+                                                  float2 nx, float2 ny, float2 nz, float r2, H &chunk)
+{
+    if (b >= e) return;
+#pragma unroll 1
+    for (int c0 = b & ~3; c0 < e; c0 += 32) {
+        const int cnt = min(32, e - c0);
+        unsigned bits = 0u;
+#pragma unroll 1
+        for (int t = 0; t < cnt; t += 4 * kPlaneQuads) {
+            float4 x[kPlaneQuads], y[kPlaneQuads], z[kPlaneQuads];
+#pragma unroll
+            for (int u = 0; u < kPlaneQuads; ++u) {
+                x[u] = __ldg(reinterpret_cast<const float4 *>(X + c0 + t + 4 * u));
+                y[u] = __ldg(reinterpret_cast<const float4 *>(Y + c0 + t + 4 * u));
+                z[u] = __ldg(reinterpret_cast<const float4 *>(Z + c0 + t + 4 * u));
+            }
+            unsigned nib = 0u;
+#pragma unroll
+            for (int u = 0; u < kPlaneQuads; ++u) {
+                const float2 xa = __fadd2_rn(make_float2(x[u].x, x[u].y), nx);
+                const float2 xb = __fadd2_rn(make_float2(x[u].z, x[u].w), nx);
+                const float2 ya = __fadd2_rn(make_float2(y[u].x, y[u].y), ny);
+                const float2 yb = __fadd2_rn(make_float2(y[u].z, y[u].w), ny);
+                const float2 za = __fadd2_rn(make_float2(z[u].x, z[u].y), nz);
+                const float2 zb = __fadd2_rn(make_float2(z[u].z, z[u].w), nz);
+                const float2 da = __ffma2_rn(za, za, __ffma2_rn(ya, ya, __fmul2_rn(xa, xa)));
+                const float2 db = __ffma2_rn(zb, zb, __ffma2_rn(yb, yb, __fmul2_rn(xb, xb)));
+                nib |= ((da.x <= r2 ? 1u : 0u) | (da.y <= r2 ? 2u : 0u) | (db.x <= r2 ? 4u : 0u) |
+                        (db.y <= r2 ? 8u : 0u))
+                       << (4 * u);
+            }
+            bits |= nib << t;
+        }
+        bits &= ~0u << max(b - c0, 0);        // below the run (first chunk only)
+        if (cnt < 32) bits &= (1u << cnt) - 1u;  // past its end
+        if (bits) chunk(c0, bits);
+    }
+}
+
+// The recording walk of a particle at pi over the walk planes, unstaged and
+// without Verlet lists, for the test |pi - pj|^2 <= r2: the hits in walk
+// order, as chunk(c0, bits) calls (record_run_planes).
+// order 2 (classes on): the pieces of walk_classes, q a class position;
+// order 1: the table walk of walk_neighbors, q a sorted index.  Counted in
+// C.nl_stats as those walks count.
+template <class H>
+__device__ __forceinline__ void record_walk_planes(int order, float3 pi, float r2, const GridView &v,
+                                                   const SimConsts &C, H &&chunk)
+{
+    const size_t st = (size_t)C.walk_stride;
+    const float *__restrict__ X = C.walk_xyz;
+    const float *__restrict__ Y = X + st;
+    const float *__restrict__ Z = Y + st;
+    const float2 nx = make_float2(-pi.x, -pi.x), ny = make_float2(-pi.y, -pi.y), nz = make_float2(-pi.z, -pi.z);
+    if (C.nl_stats) {
+        atomicAdd(C.nl_stats + 1, 1u);
+        if (order == 2) atomicAdd(C.nl_stats + 4, 1u);
+    }
+    const int3 c = cell_of(pi, C);
+    const unsigned m = v.mask;
+    const unsigned D = (unsigned)v.D;
+    const unsigned z0 = (unsigned)(c.z - 1) & m;
+    const unsigned z2 = (unsigned)(c.z + 1) & m;
+    const bool wrap = !(z0 < z2);
+    if (order == 2) {
+        const int sh = __ffs(v.D) - 1;
+        const int kz0 = ((c.z - 1) >> sh) & 1, kz2 = ((c.z + 1) >> sh) & 1;
+        const int *__restrict__ off = C.cls_off + v.base;
+        const size_t keys = (size_t)C.cls_T;
+#pragma unroll 1
+        for (int col = 0; col < 9; ++col) {
+            const int xr = c.x + col / 3 - 1, yr = c.y + col % 3 - 1;
+            const unsigned base = ((unsigned)xr & m) * D * D + ((unsigned)yr & m) * D;
+            const int kxy = ((xr >> sh) & 1) | (((yr >> sh) & 1) << 1);
+#pragma unroll 1
+            for (int piece = 0; piece < (wrap ? 2 : 1); ++piece) {
+                const unsigned za = (wrap && piece == 1) ? 0u : z0;
+                const unsigned zb = wrap ? (piece == 0 ? D - 1 : z2) : z2;
+                const int k = kxy | ((piece == 1 ? kz2 : kz0) << 2);
+                const int *o = off + (size_t)k * keys + base;
+                record_run_planes(__ldg(o + za), __ldg(o + zb + 1), X, Y, Z, nx, ny, nz, r2, chunk);
+            }
+        }
+    } else {
+        const int *__restrict__ off = v.off;
+#pragma unroll 1
+        for (int col = 0; col < 9; ++col) {
+            const unsigned x = (unsigned)(c.x + col / 3 - 1) & m, y = (unsigned)(c.y + col % 3 - 1) & m;
+            const unsigned base = x * D * D + y * D;
+#pragma unroll 1
+            for (int piece = 0; piece < (wrap ? 2 : 1); ++piece) {
+                const unsigned za = (wrap && piece == 1) ? 0u : z0;
+                const unsigned zb = wrap ? (piece == 0 ? D - 1 : z2) : z2;
+                record_run_planes(__ldg(off + base + za), __ldg(off + base + zb + 1), X, Y, Z, nx, ny, nz, r2, chunk);
+            }
         }
     }
 }

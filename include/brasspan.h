@@ -98,13 +98,20 @@ typedef enum bp_mode {
  * next iteration's planes, or the commit after the last iteration);
  * BP_WALK_NO_CONTACT_CULLING makes the particle-contact walks visit all 27
  * cells instead of only the cells a contact partner can be stored in (from
- * a bound on every particle's displacement since its cell was hashed). */
+ * a bound on every particle's displacement since its cell was hashed);
+ * BP_WALK_NO_PLANES makes the recording walks of the lambda pass and the
+ * first post pass (unstaged, split) read each candidate's position record
+ * instead of the walk planes, copies of x, y, z and the phase in separate
+ * arrays written just before those passes, from which four candidates are
+ * tested per three vector loads with paired fp32 arithmetic and each chunk
+ * of 32 candidates' hits is appended to the list a record at a time. */
 #define BP_WALK_NO_STAGING 0x1
 #define BP_WALK_NO_SPLIT 0x2
 #define BP_WALK_NO_LISTS 0x4
 #define BP_WALK_NO_ALIAS_CLASSES 0x8
 #define BP_WALK_NO_FUSION 0x10
 #define BP_WALK_NO_CONTACT_CULLING 0x20
+#define BP_WALK_NO_PLANES 0x40
 
 /* Every literal of the reference's step as a field.  bp_params_init fills the
  * reference's values; comments give the reference location of each. */

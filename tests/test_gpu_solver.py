@@ -350,6 +350,37 @@ def test_split_walks_match_one_thread_walks_on_aliased_grid(bp, gpu):
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
 
 
+@pytest.mark.parametrize("case", ["sorted", "classes", "no_classes", "textbook"])
+def test_walk_planes_are_bit_identical(bp, gpu, case):
+    """The walks that record the lambda pass's and post pass A's lists read
+    their candidates from the walk planes (x, y, z and phase in arrays of
+    their own, four candidates per three loads, paired fp32 arithmetic) and
+    append each chunk's hits a record at a time: the same lists and bits as
+    walks over the position records, with the planes in sorted order
+    (classes gated off, or none), in class order (8^3 table) and in textbook
+    mode."""
+    abi = bp.abi
+    base = abi.BP_WALK_NO_STAGING | (abi.BP_WALK_NO_ALIAS_CLASSES if case == "no_classes" else 0)
+    mode = abi.BP_MODE_TEXTBOOK if case == "textbook" else abi.BP_MODE_REFERENCE
+    aliased = case in ("classes", "textbook")
+    scene = small_mixed_scene(bp, seed=19, fluid=(20, 8, 20) if aliased else (10, 10, 10),
+                              grid_dim=8 if aliased else 32)
+    outs = []
+    for w in (base, base | abi.BP_WALK_NO_PLANES):
+        g = bp.ParticleSolver(scene, bp.make_params(scene, mode=mode, walk_options=w))
+        walks = g.walk_stats(2, DT, 4)  # a real update
+        if aliased:
+            assert walks["alias_classes"] > walks["cells_no_list"] // 2, walks
+        else:
+            assert walks["alias_classes"] == 0, walks
+        for _ in range(5):
+            g.update(2, DT, 4)
+        outs.append((g.positions(), g.velocities()))
+        g.close()
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
 def test_alias_classes_parity_on_aliased_grid(bp, gpu, oracle):
     scene = small_mixed_scene(bp, seed=16, fluid=(20, 8, 20), grid_dim=8)
     assert_parity(*lockstep(bp, oracle, scene, bp.make_params(scene), substeps=4))
