@@ -105,6 +105,9 @@ struct SimConsts {
     int *nbr;
     int *nbr_count;
     int nbr_cap;
+    // With the position pass's lists: (lambda, mass) of every sorted particle,
+    // written by k_lambda beside lam where its lists hold sorted indices.
+    float2 *lm;
     // Batched ensembles (nullptr: one scene, described by the fields above).
     // scene_of[i] is the scene of particle i; it holds for sorted and
     // original indices alike, because every scene keeps its segment.
@@ -131,9 +134,10 @@ struct SimConsts {
     const int *cls_moved;
     int cls_T;              // cell keys of all scenes
     // Class-order copies for the position pass's slot lists (k_lambda):
-    // masses (k_class_keys) and the lambdas k_lambda writes beside lam.
+    // masses (k_class_keys) and (lambda, mass) pairs k_lambda writes beside
+    // lam, which the position pass gathers in one 8-byte load per neighbour.
     const float *cls_mass;
-    float *cls_lam;
+    float2 *cls_lm;
     // And for the post passes' slot lists (k_post_a), used where cls_post is
     // set (a lambda pass of the substep wrote cls_rho): densities, committed
     // velocities (gathered with the positions before pass A), pass A's

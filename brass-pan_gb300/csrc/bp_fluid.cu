@@ -20,11 +20,13 @@ namespace bp {
 
 constexpr int kScanThreads = kWalkThreads;  // scan kernels stage their neighbourhood (bp_walk.cuh)
 
-// CTAs per SM the list-reading passes are compiled for: they mostly wait on
-// the lists' gathers, so they gain from more resident warps (position pass,
-// 4 -> 5: 3.4 -> 3.1 ms per frame late, 48 registers with a few bytes spilled).
+// CTAs per SM the list-reading passes are compiled for.  The position pass
+// loads each record's four positions and (lambda, mass) pairs before its four
+// pair terms; at 4 CTAs (64 registers) that measured faster than at 5 (48
+// registers, spilling), and than 5 CTAs with the pairs loaded per term
+// (mixed scene 9.86 -> 9.68 ms per frame early, 15.40 -> 15.17 late).
 #ifndef BP_DELTAP_MIN_BLOCKS
-#define BP_DELTAP_MIN_BLOCKS 5
+#define BP_DELTAP_MIN_BLOCKS 4
 #endif
 // The lambda pass's recording walk over the walk planes appends each chunk's
 // hits with ListWriter::push_bits (whole records of four at a time); 0: one
@@ -32,8 +34,13 @@ constexpr int kScanThreads = kWalkThreads;  // scan kernels stage their neighbou
 #ifndef BP_PLANE_PUSH_BITS
 #define BP_PLANE_PUSH_BITS 1
 #endif
+// Passes B and C load each record's neighbour data (|omega| and normal, or
+// velocity) with the positions before the four pair terms; at 3 CTAs (80
+// registers) that measured faster than at 4 (64, spilling) and than 4 CTAs
+// with the data loaded per term (mixed scene 9.75 -> 9.62 ms per frame early,
+// 15.24 -> 15.09 late).
 #ifndef BP_POSTBC_MIN_BLOCKS
-#define BP_POSTBC_MIN_BLOCKS BP_SCAN_MIN_BLOCKS
+#define BP_POSTBC_MIN_BLOCKS 3
 #endif
 
 // Ends the Verlet list build of particle i (SimConsts::vl): its count, and
@@ -80,9 +87,15 @@ __device__ __forceinline__ void k_lambda_tile(
     // pass gathers positions, masses and lambdas from the class-order copies.
     const bool slots = !Stage && C.nbr && !build && !C.vl && classes_on(C);
     const bool solid = phase_of(pi4) > 0;
+    // (lambda, mass) for the position pass's gathers: by slot with slot
+    // lists, by sorted index with lists of sorted indices
+    auto put_lm = [&](float l) {
+        if (slots) C.cls_lm[t] = make_float2(l, __ldg(mass + i));
+        else if (C.lm && !build) C.lm[i] = make_float2(l, __ldg(mass + i));
+    };
     if (solid) {  // solids carry lambda 0 (read by the position pass)
         lam[i] = 0.f;
-        if (slots) C.cls_lam[t] = 0.f;
+        put_lm(0.f);
     }
     if (solid && (C.textbook || !rec)) {
         if (build) C.nl_cell[i] = -1;
@@ -188,7 +201,7 @@ __device__ __forceinline__ void k_lambda_tile(
         float c = density / rho0 - 1.0f;
         if (C.clamp_c) c = fmaxf(c, 0.0f);
         lam[i] = -c / C.lambda_den;
-        if (slots) C.cls_lam[t] = lam[i];
+        put_lm(lam[i]);
     } else {
         const float inv_rho0 = inv_rest_density(C, sc);
         float sum_g2 = 0.f;
@@ -228,7 +241,7 @@ __device__ __forceinline__ void k_lambda_tile(
         if (C.clamp_c) c = fmaxf(c, 0.0f);
         sum_g2 += dot3(gi, gi);
         lam[i] = -c / (sum_g2 + C.relaxation);
-        if (slots) C.cls_lam[t] = lam[i];
+        put_lm(lam[i]);
     }
     rho[i] = density;
     if (slots) C.cls_rho[t] = density;
@@ -327,8 +340,11 @@ __device__ __forceinline__ void k_deltap_tile(
         // from the class-order copies, the sorted index only where one of the
         // two is a solid (the fluid-fluid pairs pass the rule either way)
         const bool slots = !Stage && C.nbr && !C.vl && classes_on(C);
+        // each entry's (lambda, mass) loads with its position, before the
+        // four pair terms of a record
         if (!walk && slots) {
-            for_each_in_list(C.nbr, C.n, t, listed, C.cls_pos, [&](int q, float4 pj4) {
+            auto fetch = [&](int q) { return __ldg(C.cls_lm + q); };
+            for_each_in_list_with(C.nbr, C.n, t, listed, C.cls_pos, fetch, [&](int q, float4 pj4, float2 lm) {
                 if (!(len2(pk - f3(pj4)) > 0.f)) return;  // r = 0 excludes k itself
                 if (!C.textbook) {
                     const bool fj = phase_of(pj4) < 0;
@@ -337,7 +353,14 @@ __device__ __forceinline__ void k_deltap_tile(
                         if (!((j > k) ? (phk < 0) : fj)) return;
                     }
                 }
-                pair(pj4, __ldg(C.cls_lam + q), __ldg(C.cls_mass + q));
+                pair(pj4, lm.x, lm.y);
+            });
+        } else if (!walk && C.lm) {
+            auto fetch = [&](int j) { return __ldg(C.lm + j); };
+            for_each_in_list_with(C.nbr, C.n, t, listed, a.P, fetch, [&](int j, float4 pj4, float2 lm) {
+                if (!(len2(pk - f3(pj4)) > 0.f)) return;  // r = 0 excludes k itself
+                if (!C.textbook && !((j > k) ? (phk < 0) : (phase_of(pj4) < 0))) return;
+                pair(pj4, lm.x, lm.y);
             });
         } else if (!walk) {
             auto listed_body = [&](int j, float4 pj4) {  // r = 0 excludes k itself
@@ -574,14 +597,25 @@ __device__ __forceinline__ void k_post_b_tile(
     float3 eta = make_float3(0.f, 0.f, 0.f), ft = make_float3(0.f, 0.f, 0.f);
     const bool want_v = C.use_vort, want_t = C.use_akinci;
     const bool slots = post_slots(C, Stage);
-    auto body_at = [&](const float4 *__restrict__ Omp, const float4 *__restrict__ Nmp, int j, float4 pj4) {
+    // a neighbour's |omega| and (h n, rho), as the pair terms read them
+    struct Nb {
+        float om;
+        float4 nm;
+    };
+    auto fetch_at = [&](const float4 *__restrict__ Omp, const float4 *__restrict__ Nmp, int j) {
+        Nb r;
+        r.om = want_v ? Omp[j].w : 0.f;
+        r.nm = want_t ? Nmp[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        return r;
+    };
+    auto pair_terms = [&](float4 pj4, const Nb &nb) {
         const float3 diff = pi - f3(pj4);
         const float d2 = len2(diff);
         if (!(d2 > 0.f)) return;
         const float inv_r = rsqrtf(d2);
-        if (want_v) eta = fma3(Omp[j].w, spiky_grad_r(C, diff, d2, inv_r), eta);
+        if (want_v) eta = fma3(nb.om, spiky_grad_r(C, diff, d2, inv_r), eta);
         if (want_t) {
-            const float4 nj4 = Nmp[j];
+            const float4 nj4 = nb.nm;
             const float dist = __fmul_rn(d2, inv_r);
             const float3 fco = __fmul_rn(__fmul_rn(-C.tension, akinci_spline(C, dist)), inv_r) * diff;
             const float3 fcu = (-C.tension) * (ni - f3(nj4));
@@ -589,12 +623,15 @@ __device__ __forceinline__ void k_post_b_tile(
             ft = fma3(kij, fco + fcu, ft);
         }
     };
-    auto body = [&](int j, float4 pj4) { body_at(Om, Nm, j, pj4); };
+    auto body = [&](int j, float4 pj4) { pair_terms(pj4, fetch_at(Om, Nm, j)); };
+    // each entry's omega and normal load with its position, before the four
+    // pair terms of a record
+    auto listed = [&](int, float4 pj4, const Nb &nb) { pair_terms(pj4, nb); };
     if (cnt != kWalkCells && slots) {
-        for_each_in_list(C.nbr, C.n, t, cnt, C.cls_pos,
-                         [&](int q, float4 pj4) { body_at(C.cls_om, C.cls_nm, q, pj4); });
+        for_each_in_list_with(C.nbr, C.n, t, cnt, C.cls_pos,
+                              [&](int q) { return fetch_at(C.cls_om, C.cls_nm, q); }, listed);
     } else if (cnt != kWalkCells) {
-        for_each_in_list(C.nbr, C.n, t, cnt, P, body);
+        for_each_in_list_with(C.nbr, C.n, t, cnt, P, [&](int j) { return fetch_at(Om, Nm, j); }, listed);
     } else {
         walk_neighbors<Split>(
             i, pi, 0, P, grid_view(C, sc, off), C, Stage ? &S : nullptr, g,
@@ -672,7 +709,14 @@ __device__ __forceinline__ void k_post_c_tile(
     auto test = [&](int j, float4 pj4) { return j != i && phase_of(pj4) == phi && len2(pi - f3(pj4)) <= C.h2; };
     const GridView gv = grid_view(C, scene_index(C, i), off);
     int own = -1;
-    if (cnt != kWalkCells && post_slots(C, Stage)) {  // V is pass B's output, kept in class order beside it
+    // reference mode: each entry's velocity loads with its position, before
+    // the four pair terms of a record
+    auto listed = [&](int, float4 pj4, float4 vj4) { vn = fma3(poly6(C, len2(pi - f3(pj4))), f3(vj4) - vi, vn); };
+    if (cnt != kWalkCells && post_slots(C, Stage) && !C.textbook) {  // V: pass B's output, in class order
+        for_each_in_list_with(C.nbr, C.n, t, cnt, C.cls_pos, [&](int q) { return C.cls_vb[q]; }, listed);
+    } else if (cnt != kWalkCells && !C.textbook) {
+        for_each_in_list_with(C.nbr, C.n, t, cnt, P, [&](int j) { return V[j]; }, listed);
+    } else if (cnt != kWalkCells && post_slots(C, Stage)) {
         for_each_in_list(C.nbr, C.n, t, cnt, C.cls_pos,
                          [&](int q, float4 pj4) { body_at(C.cls_vb, C.cls_mass, C.cls_rho, q, pj4); });
     } else if (cnt != kWalkCells) {

@@ -109,7 +109,7 @@ struct ClassArrays {
     int *mixed;      // one word: particles whose class differs from their cell's first particle's
     int *moved;      // one word
     float *mass;     // [n] masses in class order (k_class_keys)
-    float *lam;      // [n] lambdas in class order (k_lambda, slot lists)
+    float2 *lm;      // [n] (lambda, mass) in class order (k_lambda, slot lists)
     float *rho;      // [n] densities in class order (k_lambda, slot lists)
     float4 *vel, *om, *nm, *vb;  // [n] each: the post passes' class-order copies (SimConsts::cls_vel ...)
     int T;           // cell keys of all scenes

@@ -230,7 +230,7 @@ SimConsts bp::make_consts(const bp_solver *s, float sdt)
         C.cls_moved = s->cls.moved;
         C.cls_T = s->cls.T;
         C.cls_mass = s->cls.mass;
-        C.cls_lam = s->cls.lam;
+        C.cls_lm = s->cls.lm;
         C.cls_rho = s->cls.rho;
         C.cls_vel = s->cls.vel;
         C.cls_om = s->cls.om;
@@ -365,7 +365,7 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         (st = s->alloc(&s->Om, N)) || (st = s->alloc(&s->Nm, N)) || (st = s->alloc(&s->orig_c, N)) ||
         (st = s->alloc(&s->orig_s, N)) || (st = s->alloc(&s->to_new, N)) || (st = s->alloc(&s->group, N)) ||
         (st = s->alloc(&s->keys, N)) || (st = s->alloc(&s->sorted_keys, N)) || (st = s->alloc(&s->order, N)) ||
-        (st = s->alloc(&s->off, ncells + 1)) || (st = s->alloc(&s->mass, N)) || (st = s->alloc(&s->lam, N)) ||
+        (st = s->alloc(&s->off, ncells + 1)) || (st = s->alloc(&s->mass, N)) || (st = s->alloc(&s->lam, N)) || (st = s->alloc(&s->lm, N)) ||
         (st = s->alloc(&s->rho, N)) || (st = s->alloc(&s->w, N)) || (st = s->alloc(&s->err, 1)) ||
         (st = s->alloc(&s->staging, 6 * N)) || (st = s->alloc(&s->vl, NM * kVerletCap)) ||
         (st = s->alloc(&s->nl_cell, NM)) || (st = s->alloc(&s->nl_pos, NM)) ||
@@ -382,7 +382,7 @@ static bp_status create_solver(const bp_scene_desc *sc, const bp_params *prm, vo
         if ((st = s->alloc(&a.cls, N)) || (st = s->alloc(&a.pos0, N)) || (st = s->alloc(&a.keys, N)) ||
             (st = s->alloc(&a.perm, N)) || (st = s->alloc(&a.inv, N)) || (st = s->alloc(&a.off, 8 * ncells + 1)) ||
             (st = s->alloc(&a.pos, N)) || (st = s->alloc(&a.mixed, 1)) || (st = s->alloc(&a.moved, 1)) ||
-            (st = s->alloc(&a.mass, N)) || (st = s->alloc(&a.lam, N)) || (st = s->alloc(&a.rho, N)) ||
+            (st = s->alloc(&a.mass, N)) || (st = s->alloc(&a.lm, N)) || (st = s->alloc(&a.rho, N)) ||
             (st = s->alloc(&a.vel, N)) || (st = s->alloc(&a.om, N)) || (st = s->alloc(&a.nm, N)) ||
             (st = s->alloc(&a.vb, N)))
             return bail(st);
@@ -811,6 +811,7 @@ void bp::enqueue_substep(bp_solver *s, const SimConsts &C, int iterations, int p
         Cf.nbr = s->nbr;
         Cf.nbr_count = s->nbr_count;
         Cf.nbr_cap = kPostListCap;
+        Cf.lm = s->lm;
     }
     if (walk_planes) {
         Cf.walk_xyz = s->walk_xyz;

@@ -134,6 +134,7 @@ struct bp_solver {
     unsigned *contact_reach = nullptr;
     int *solid_walk = nullptr;
     int *nbr = nullptr, *nbr_count = nullptr;  // post-pass neighbour lists [kPostListCap][N], counts
+    float2 *lm = nullptr;  // (lambda, mass) per sorted particle (SimConsts::lm)
     float *walk_xyz = nullptr;  // walk planes (SimConsts::walk_xyz): 4 planes of walk_stride floats
     int walk_stride = 0;
     SortScratch sort{};

@@ -382,6 +382,40 @@ __device__ __forceinline__ void for_each_in_list(const int *base, int n, int i, 
     }
 }
 
+// As for_each_in_list, with each entry's own data, fetch(j), loaded beside
+// its position before the four calls: f(j, P[j], fetch(j)).
+template <bool ReadOnly = true, class G, class F>
+__device__ __forceinline__ void for_each_in_list_with(const int *base, int n, int i, int cnt,
+                                                      const float4 *__restrict__ P, G &&fetch, F &&f, int first = 0)
+{
+    using T = decltype(fetch(0));
+    const int4 *rec = reinterpret_cast<const int4 *>(base) + i;
+    const size_t stride = (size_t)n;
+    auto load = [&](int k) {
+        const int4 *rp = rec + (size_t)(k >> 2) * stride;
+        return ReadOnly ? __ldg(rp) : *rp;
+    };
+    int4 next = first < cnt ? load(first) : make_int4(0, 0, 0, 0);
+#pragma unroll 1
+    for (int k = first; k < cnt; k += 4) {
+        const int4 r = next;
+        if (k + 4 < cnt) next = load(k + 4);
+        const int m = min(4, cnt - k);
+        const int j[4] = {r.x, r.y, r.z, r.w};
+        float4 pj[4];
+        T xj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (q < m) {
+                pj[q] = P[j[q]];
+                xj[q] = fetch(j[q]);
+            }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (q < m) f(j[q], pj[q], xj[q]);
+    }
+}
+
 // Candidates [qb, e) of one (class, cell) run in class order, read from
 // C.cls_pos.  test() sees a stand-in index that equals i only for particle i
 // itself (tests compare it with i and nothing else); the body gets the sorted
