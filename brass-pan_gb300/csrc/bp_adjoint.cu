@@ -369,16 +369,17 @@ __device__ __forceinline__ float3 clamp_fwd(const SimConsts &C, float3 u)
     return mul3(u, C.delta_clamp / sqrtf(l2));
 }
 
-// The pairs of particle k that pass test, in walk order: term(j, P[j]).
-// With C.nbr the walk records the pairs that pass `record` (a superset of
-// test's) and the terms of those that pass test are summed over the list
-// (four gathers at a time); the list's count goes to C.nbr_count[k] (-1:
-// overflow), so that a later pass over the same positions can read it.
-// Without lists, or past the list's capacity, the terms run inside the walk.
-template <class R, class T, class B>
+// The pairs of particle k that pass test, in walk order: term(j, P[j],
+// fetch(j)).  With C.nbr the walk records the pairs that pass `record` (a
+// superset of test's) and the terms of those that pass test are summed over
+// the list, each record's four positions and fetch() data loaded before its
+// four terms; the list's count goes to C.nbr_count[k] (-1: overflow), so that
+// a later pass over the same positions can read it.  Without lists, or past
+// the list's capacity, the terms run inside the walk.
+template <class R, class T, class G, class B>
 __device__ __forceinline__ void record_then_sum(const SimConsts &C, int k, float3 pk, const float4 *__restrict__ P,
                                                 const GridView &v, const StageShared *S, int g, R &record, T &test,
-                                                B &term)
+                                                G &fetch, B &term)
 {
     int cnt = -1;
     if (C.nbr) {
@@ -387,11 +388,21 @@ __device__ __forceinline__ void record_then_sum(const SimConsts &C, int k, float
         cnt = list.finish();
         if (C.nbr_count) C.nbr_count[k] = cnt;
         if (cnt >= 0)
-            for_each_in_list<false>(C.nbr, C.n, k, cnt, P, [&](int j, float4 pj) {
-                if (test(j, pj)) term(j, pj);
+            for_each_in_list_with<false>(C.nbr, C.n, k, cnt, P, fetch, [&](int j, float4 pj, const auto &nb) {
+                if (test(j, pj)) term(j, pj, nb);
             });
     }
-    if (cnt < 0) walk_neighbors<true>(k, pk, 0, P, v, C, S, g, test, term);
+    if (cnt < 0) walk_neighbors<true>(k, pk, 0, P, v, C, S, g, test, [&](int j, float4 pj) { term(j, pj, fetch(j)); });
+}
+// The same with no per-neighbour data: term(j, P[j]).
+template <class R, class T, class B>
+__device__ __forceinline__ void record_then_sum(const SimConsts &C, int k, float3 pk, const float4 *__restrict__ P,
+                                                const GridView &v, const StageShared *S, int g, R &record, T &test,
+                                                B &term)
+{
+    auto none = [](int) { return 0; };
+    auto term3 = [&](int j, float4 pj, int) { term(j, pj); };
+    record_then_sum(C, k, pk, P, v, S, g, record, test, none, term3);
 }
 
 // Walk A: lambda-bar and the position gradient of the correction terms.  It
@@ -425,14 +436,20 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const 
         const bool inc = C.textbook ? (phk < 0 || fj) : ((j > k) ? (phk < 0) : fj);
         return j != k && d2 <= C.h2 && d2 > 0.f && inc;
     };
-    auto term = [&](int j, float4 pj4) {
+    // a neighbour's lambda, mass and incoming gradient
+    struct Nb {
+        float lam, mass;
+        float4 g;
+    };
+    auto fetch = [&](int j) { return Nb{__ldg(lam + j), __ldg(mass + j), gOut[j]}; };
+    auto term = [&](int j, float4 pj4, const Nb &nb) {
             const float3 r = sub3(pk, f3(pj4));
             const float d2 = dotf(r, r);
             const float rl = sqrtf(d2);
             const bool own = !C.textbook || phk < 0;               // dp_k has the pair
             const bool other = !C.textbook || phase_of(pj4) < 0;  // dp_j has the pair
             const SpikyD sp = spiky_d(C, r, rl);
-            float s = lk + lam[j];
+            float s = lk + nb.lam;
             float3 dsc = make_float3(0.f, 0.f, 0.f);  // d scorr / d r
             if (C.scorr_on) {
                 const float x = poly6(C, d2) * C.scorr_inv_wq;
@@ -441,13 +458,13 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const 
                     dsc = mul3(poly6_grad(C, r, d2), C.scorr_k * C.scorr_ni * ipowf(x, C.scorr_ni - 1) * C.scorr_inv_wq);
             }
             // term of dp_k: (m_j / rho0) clamp(s gradW(r))
-            const float3 u1b = own ? mul3(clamp_vjp(C, mul3(sp.g, s), gk), mass[j] * inv_rho0)
+            const float3 u1b = own ? mul3(clamp_vjp(C, mul3(sp.g, s), gk), nb.mass * inv_rho0)
                                    : make_float3(0.f, 0.f, 0.f);
             const float sb1 = dotf(u1b, sp.g);
             const float3 rb1 = sub3(mul3(spiky_hess_mul(sp, r, rl, u1b), s), mul3(dsc, sb1));
             // term of dp_j: (m_k / rho0) clamp(s gradW(-r))
             const float3 g_neg = mul3(sp.g, -1.f);
-            const float3 u2b = other ? mul3(clamp_vjp(C, mul3(g_neg, s), ld3(gOut, j)), mk * inv_rho0)
+            const float3 u2b = other ? mul3(clamp_vjp(C, mul3(g_neg, s), f3(nb.g)), mk * inv_rho0)
                                      : make_float3(0.f, 0.f, 0.f);
             const float sb2 = dotf(u2b, g_neg);
             // gradient w.r.t. r_jk = -r: H(-r) = H(r), dscorr(-r) = -dscorr(r)
@@ -459,7 +476,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const 
         const float3 r = sub3(pk, f3(pj4));
         return j != k && dotf(r, r) <= C.h2;
     };
-    record_then_sum(C, k, pk, P, grid_view(C, sc, off), &S, g, within, test, term);
+    record_then_sum(C, k, pk, P, grid_view(C, sc, off), &S, g, within, test, fetch, term);
     gLam[k] = lb;
     gPart[k] = f4(pb);
 }
@@ -467,7 +484,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_deltap(SimConsts C, const 
 // Pass B: the density gradient; gP (in) = gOut + gPart + density terms.  It
 // sums over the list pass A recorded at the same positions (every j != k
 // within h, in walk order) and walks only where that list overflowed.
-__global__ void __launch_bounds__(kWalkThreads) k_adj_lambda(SimConsts C, const float4 *__restrict__ P,
+__global__ void __launch_bounds__(kWalkThreads, 3) k_adj_lambda(SimConsts C, const float4 *__restrict__ P,
                                                              const float *__restrict__ mass,
                                                              const float *__restrict__ rho, const int *__restrict__ off,
                                                              const float *__restrict__ gLam,
@@ -494,16 +511,30 @@ __global__ void __launch_bounds__(kWalkThreads) k_adj_lambda(SimConsts C, const 
     const float mk = mass[k] * (phk < 0 ? 1.f : C.solid_scale);
     float3 pb = make_float3(0.f, 0.f, 0.f);
     auto test = [&](int j, float4 pj4) { return j != k && dotf(sub3(pk, f3(pj4)), sub3(pk, f3(pj4))) <= C.h2; };
-    auto term = [&](int j, float4 pj4) {
+    // what rho_bar and the term read of a neighbour, loaded with its position
+    struct Nb {
+        float gl, gr, rh, m;
+    };
+    auto fetch = [&](int j) { return Nb{gLam[j], gRho ? gRho[j] : 0.f, rho[j], mass[j]}; };
+    auto term = [&](int j, float4 pj4, const Nb &nb) {
         const int phj = phase_of(pj4);
         const float3 r = sub3(pk, f3(pj4));
         const float3 gw = poly6_grad(C, r, dotf(r, r));
-        if (j > k) pb = add3(pb, mul3(gw, rbk * mass[j] * (phj < 0 ? 1.f : C.solid_scale)));
-        else pb = add3(pb, mul3(gw, rho_bar(j, phj) * mk));
+        if (j > k) {
+            pb = add3(pb, mul3(gw, rbk * nb.m * (phj < 0 ? 1.f : C.solid_scale)));
+        } else {
+            // rho_bar(j, phj) from the loaded values
+            float rb = 0.f;
+            if (phj <= 0) rb = (C.clamp_c && !(nb.rh / rho0 - 1.0f > 0.f)) ? nb.gr : nb.gr - nb.gl / (C.lambda_den * rho0);
+            pb = add3(pb, mul3(gw, rb * mk));
+        }
     };
     const int cnt = (C.nbr && C.nbr_count) ? __ldg(C.nbr_count + k) : -1;
-    if (cnt >= 0) for_each_in_list(C.nbr, C.n, k, cnt, P, term);  // pass A's list: exactly test's pairs
-    else walk_neighbors<true>(k, pk, 0, P, grid_view(C, sc, off), C, &S, g, test, term);
+    if (cnt >= 0)  // pass A's list: exactly test's pairs
+        for_each_in_list_with(C.nbr, C.n, k, cnt, P, fetch, term);
+    else
+        walk_neighbors<true>(k, pk, 0, P, grid_view(C, sc, off), C, &S, g, test,
+                             [&](int j, float4 pj4) { term(j, pj4, fetch(j)); });
     gIn[k] = f4(add3(add3(ld3(gOut, k), ld3(gPart, k)), pb));
 }
 
