@@ -521,10 +521,11 @@ void launch_class_order(cudaStream_t st, int n, const int *sorted_keys, const in
 // (SimConsts::walk_xyz).
 __device__ __forceinline__ void put_planes(float *planes, int stride, int q, float4 p)
 {
+    const size_t st = (size_t)stride;
     planes[q] = p.x;
-    planes[stride + q] = p.y;
-    planes[2 * stride + q] = p.z;
-    planes[3 * stride + q] = p.w;
+    planes[st + q] = p.y;
+    planes[2 * st + q] = p.z;
+    planes[3 * st + q] = p.w;
 }
 
 // Walks use the classes while at least 1/32 of the particles sit in a cell
@@ -561,7 +562,7 @@ __global__ void __launch_bounds__(256) k_class_refresh(int n, const float4 *__re
     if (far) *a.moved = 2;
 }
 
-// A grid-stride loop over one resident wave (8 CTAs of 256 per SM).
+// Blocks of a grid-stride loop over one resident wave (8 CTAs of 256 per SM).
 static int wave_blocks(int n)
 {
     int dev = 0, sms = 0;
@@ -575,8 +576,7 @@ void launch_class_refresh(cudaStream_t st, int n, const float4 *P, const ClassAr
 {
     if (n <= 0) return;
     // the common case without planes is the gate's early exit (one wave);
-    // with planes, a thread per particle (measured: a wave striding over the
-    // particles took 25 us per launch on 1.1M particles)
+    // with planes, a thread per particle
     const int blocks = planes ? (n + 255) / 256 : wave_blocks(n);
     k_class_refresh<<<blocks, 256, 0, st>>>(n, P, V, a, class_gate(n, a), planes, stride);
     L->done(__func__);
