@@ -28,12 +28,6 @@ constexpr int kScanThreads = kWalkThreads;  // scan kernels stage their neighbou
 #ifndef BP_DELTAP_MIN_BLOCKS
 #define BP_DELTAP_MIN_BLOCKS 4
 #endif
-// The lambda pass's recording walk over the walk planes appends each chunk's
-// hits with ListWriter::push_bits (whole records of four at a time); 0: one
-// push per hit.
-#ifndef BP_PLANE_PUSH_BITS
-#define BP_PLANE_PUSH_BITS 1
-#endif
 // Passes B and C load each record's neighbour data (|omega| and normal, or
 // velocity) with the positions before the four pair terms; at 3 CTAs (80
 // registers) that measured faster than at 4 (64, spilling) and than 4 CTAs
@@ -126,18 +120,9 @@ __device__ __forceinline__ void k_lambda_tile(
         if (planes == (slots ? 2 : 1)) {
             const int me = slots ? t : i;  // the particle's own entry
             record_walk_planes(planes, pi, r2, v, C, [&](int c0, unsigned bits) {
-#if BP_PLANE_PUSH_BITS
                 const unsigned d = (unsigned)(me - c0);
                 if (d < 32u && ((bits >> d) & 1u)) self = list.cnt + __popc(bits & ((1u << d) - 1u));
                 list.push_bits(c0, bits);
-#else
-                while (bits) {
-                    const int q = c0 + __ffs(bits) - 1;
-                    bits &= bits - 1u;
-                    if (q == me) self = list.cnt;
-                    list.push(q);
-                }
-#endif
             });
         } else if (slots) {  // the class walk walk_neighbors would take (no staging, no Verlet list), counted alike
             if (C.nl_stats) {
