@@ -56,6 +56,7 @@ BP_WALK_NO_PLANES = 0x40
  BP_FIELD_MAP_TO_NEW, BP_FIELD_LAMBDAS, BP_FIELD_DENSITIES, BP_FIELD_SORTED_CELL_IDS,
  BP_FIELD_CELL_OFFSETS, BP_FIELD_RIGID_ROTATIONS, BP_FIELD_RIGID_CMS,
  BP_FIELD_INV_SCALED_MASSES) = range(12)
+BP_FIELD_COUNT = 12
 
 
 class BpParams(C.Structure):

@@ -40,6 +40,32 @@ def test_library_exports_every_declared_symbol(bp):
     assert lib.bp_abi_version() == 1
 
 
+def header_constants():
+    """Every integer `#define BP_...` and enumerator `BP_... = value` of the
+    headers."""
+    out = {}
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for name, val in re.findall(r"#define\s+(BP_[A-Z0-9_]+)\s+(0x[0-9a-fA-F]+|[0-9]+)u?\b", text):
+            out[name] = int(val, 0)
+        for name, val in re.findall(r"\b(BP_[A-Z0-9_]+)\s*=\s*(0x[0-9a-fA-F]+|[0-9]+)\b", text):
+            out[name] = int(val, 0)
+    return out
+
+
+def test_python_constants_match_header(bp):
+    """The ctypes mirror's constants carry the header's values, and the
+    header's walk and stage bits are all mirrored."""
+    consts = header_constants()
+    assert consts["BP_WALK_NO_PLANES"] == 0x40 and consts["BP_STAGE_ALL"] == 0x7FF
+    mirrored = {k: getattr(bp.abi, k) for k in consts if hasattr(bp.abi, k)}
+    wrong = {k: (v, consts[k]) for k, v in mirrored.items() if int(v) != consts[k]}
+    assert not wrong, f"python value != header value: {wrong}"
+    needed = [k for k in consts if k.startswith(("BP_WALK_", "BP_STAGE_", "BP_MODE_", "BP_FIELD_"))]
+    missing = [k for k in needed if k not in mirrored]
+    assert not missing, f"not mirrored in abi.py: {missing}"
+
+
 def test_struct_layout_matches_header(bp, tmp_path):
     abi = bp.abi
     fields = {"bp_params": abi.BpParams, "bp_scene_desc": abi.BpSceneDesc, "bp_gradients": abi.BpGradients}
